@@ -1,0 +1,147 @@
+/*
+ * lmtg.h -- C ABI of the GB300 finite-element hot path (element matrices -> assembly -> solve).
+ *
+ * This is the drop-in boundary for LMT++'s formulation/assemble/solve API.  Each entry point
+ * names the reference interface it replaces (paths inside the LMTpp project):
+ *
+ *   FormulationAncestor<T>            include/formulation/formulation_ancestor.h:18-262
+ *   Formulation<...>::allocate_matrices include/formulation/formulation.h:338-412
+ *   Formulation<...>::assemble        include/formulation/formulation.h:1112-1125
+ *   Formulation<...>::solve_system    include/formulation/formulation.h:1494-1504
+ *   Formulation<...>::solve           include/formulation/formulation.h:1517-1568
+ *   add_constraint / assemble_constraints include/formulation/formulation.h:1028-1091
+ *   get_mat / get_sollicitation / get_result  formulation_ancestor.h:88-120
+ *
+ * Conventions: every function returns an int status (LMTG_OK == 0).  No C++ exception crosses
+ * the ABI.  Host buffers are caller-owned and only read or written during the call; device
+ * buffers are owned by the context.  A context is bound to one CUDA device and must not be
+ * used from two host threads at once.  lmtg_last_error() gives a message for the last failure.
+ */
+#ifndef LMTG_H
+#define LMTG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define LMTG_OK 0
+#define LMTG_ERR_ARG 1           /* bad argument or size */
+#define LMTG_ERR_CUDA 2          /* CUDA runtime error */
+#define LMTG_ERR_STATE 3         /* call out of order (e.g. solve before assemble) */
+#define LMTG_ERR_NOT_CONVERGED 4 /* iteration cap reached (reference: SolveException) */
+#define LMTG_ERR_TIMEOUT 5       /* host wall-clock watchdog expired */
+#define LMTG_ERR_NAN 6           /* NaN / Inf in a PCG scalar */
+#define LMTG_ERR_NOMEM 7         /* device allocation failed */
+#define LMTG_ERR_UNSUPPORTED 8   /* element type / size not supported */
+
+/* ---- element types (nodes per element) ---- */
+#define LMTG_ELEM_HEXA8 8
+
+/* ---- lmtg_assemble flags ---- */
+#define LMTG_ASM_MAT64 1        /* FP64 element matrices -> FP64 K */
+#define LMTG_ASM_MAT32 2        /* FP32 copy of K rounded from the FP64 assembly (inner operator) */
+#define LMTG_ASM_VEC 4          /* sollicitation vector (loads + constraint right-hand sides) */
+#define LMTG_ASM_MAT32_NATIVE 8 /* FP32 element kernel -> FP32 K (no FP64 pass) */
+
+/* ---- solve modes ---- */
+#define LMTG_SOLVE_PCG_F64 0  /* plain FP64 block-Jacobi PCG */
+#define LMTG_SOLVE_MIXED_IR 1 /* FP32 inner PCG wrapped in FP64 iterative refinement */
+
+/* ---- stopping criteria ---- */
+#define LMTG_CRIT_REL_RESIDUAL 0   /* |b - K u|_2 <= tol |b|_2 */
+#define LMTG_CRIT_NORM_INF_DELTA 1 /* |alpha d|_inf <= tol (ConvergenceCriteriumNormInfDelta,
+                                      include/containers/conjugate_gradient.h:100-111) */
+#define LMTG_CRIT_NORM2_DELTA 2    /* |alpha d|_2 < tol (ConvergenceCriteriumNorm2, :113-123) */
+#define LMTG_CRIT_ABS_RESIDUAL_INF 3 /* |r|_inf <= tol (solve_using_incomplete_chol_factorize,
+                                        include/containers/matinvsparse.h:453-491) */
+
+typedef struct lmtg_ctx lmtg_ctx;
+
+typedef struct lmtg_solve_stats {
+    int iterations;       /* total PCG iterations (inner iterations for the mixed mode) */
+    int outer_iterations; /* FP64 refinement steps (mixed mode), 0 for plain PCG */
+    int status;           /* same as the return value */
+    int reserved;
+    double rel_residual;  /* final |b - K u|_2 / |b|_2, recomputed in FP64 */
+    double device_ms;     /* device time of the solve (CUDA events) */
+} lmtg_solve_stats;
+
+/* Context.  Replaces the construction of Problem/Formulation objects. */
+int lmtg_create(int device, lmtg_ctx **ctx);
+int lmtg_destroy(lmtg_ctx *ctx);
+const char *lmtg_last_error(const lmtg_ctx *ctx);
+const char *lmtg_status_string(int status);
+
+/* Structured unit-box Hexa mesh on the host, identical node order and coordinates to
+ * make_rect(m, Hexa(), X0, X1, nb_points) (include/mesh/make_rect.h:653-679).
+ * pos: nn*3 doubles, conn: ne*8 (nn = prod nb_points, ne = prod (nb_points-1)). */
+int lmtg_make_rect_hexa(const double X0[3], const double X1[3], const uint32_t nb_points[3],
+                        double *pos, uint32_t *conn);
+
+/* Mesh (the TM object a Formulation points to, formulation.h:2740-2745): node positions
+ * (nn*3), element connectivity (ne*nodes_per_element), DOF numbering node*3 as the reference's
+ * default indice_noda (formulation.h:283-325, no AMD/RCM renumbering). */
+int lmtg_mesh_set(lmtg_ctx *ctx, int elem_type, uint64_t nn, const double *pos, uint64_t ne,
+                  const uint32_t *conn);
+
+/* Material: elastic_modulus (one value, or one per element) and poisson_ratio
+ * (formulations/formulation_elasticity_iso.py:5-6). */
+int lmtg_material_set(lmtg_ctx *ctx, const double *E, uint64_t nE, double nu);
+
+/* allocate_matrices (formulation.h:338-412): builds the node-block sparsity pattern, the
+ * element-to-block gather lists and all device buffers.  *nnz_lower (optional) receives the
+ * number of stored scalar entries of the lower triangle (the SparseLine nb_nz()). */
+int lmtg_allocate_matrices(lmtg_ctx *ctx, uint64_t *nnz_lower);
+
+/* Nodal loads f_nodal (n = 3*nn doubles), replacing the current nodal load vector. */
+int lmtg_set_nodal_loads(lmtg_ctx *ctx, const double *F);
+/* Uniform traction f_surf on Quad4 skin faces (nfaces*4 node ids), accumulated into the load
+ * vector as consistent nodal loads (the add_skin_elem_matrix terms, formulation.h:584-594). */
+int lmtg_add_skin_traction(lmtg_ctx *ctx, uint64_t nfaces, const uint32_t *faces,
+                           const double traction[3]);
+
+/* Penalty constraints: add_constraint("coef*node[i].dep[d] - res", penalty) for linear
+ * single-unknown constraints; assembled as in assemble_constraints (formulation.h:1028-1071):
+ * K(j,j) += coef^2 * max|diag K| * penalty, F(j) += coef * max|diag K| * penalty * res. */
+int lmtg_set_constraints(lmtg_ctx *ctx, uint64_t nc, const uint32_t *dof, const double *coef,
+                         const double *res, double penalty);
+
+/* assemble(assemble_mat, assemble_vec) (formulation.h:1112-1125), flags LMTG_ASM_*. */
+int lmtg_assemble(lmtg_ctx *ctx, int flags);
+
+/* get_mat: the assembled FP64 matrix as the reference's Sym SparseLine lower CSR (row i holds
+ * columns j <= i ascending, diagonal last).  rowptr: n+1, col/val: nnz_lower. */
+int lmtg_get_matrix_lower(lmtg_ctx *ctx, uint64_t *rowptr, uint32_t *col, double *val);
+/* get_sollicitation: the assembled right-hand side (n doubles). */
+int lmtg_get_sollicitation(lmtg_ctx *ctx, double *F);
+/* Element matrices of elements [e0, e0+count) as dense row-major 24x24 (test/inspection). */
+int lmtg_get_element_matrices(lmtg_ctx *ctx, int precision, uint64_t e0, uint64_t count,
+                              double *Ke);
+
+/* solve_system(iterative_criterium) (formulation.h:1494-1504) on the assembled system.
+ * The initial guess is the current result vector (zero after allocate_matrices).  maxit caps
+ * the PCG iterations; timeout_s > 0 bounds the host wall clock. */
+int lmtg_solve_system(lmtg_ctx *ctx, int mode, int crit_kind, double tol, int maxit,
+                      double timeout_s, lmtg_solve_stats *stats);
+/* solve(): assemble(mat and vec) followed by solve_system (formulation.h:1517-1568). */
+int lmtg_solve(lmtg_ctx *ctx, int mode, int crit_kind, double tol, int maxit, double timeout_s,
+               lmtg_solve_stats *stats);
+
+/* get_result(0): the solution vector (n doubles); set_result: the initial guess. */
+int lmtg_get_result(lmtg_ctx *ctx, double *u);
+int lmtg_set_result(lmtg_ctx *ctx, const double *u);
+
+/* y = K x with the assembled matrix in FP64 (precision 0) or FP32 (precision 1). */
+int lmtg_spmv(lmtg_ctx *ctx, int precision, const double *x, double *y);
+
+/* Sizes of the current problem. */
+int lmtg_get_sizes(lmtg_ctx *ctx, uint64_t *nn, uint64_t *ne, uint64_t *ndof, uint64_t *nnz_blocks);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LMTG_H */

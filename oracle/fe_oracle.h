@@ -1,0 +1,107 @@
+/*
+ * fe_oracle.h -- CPU restatement of LMT++'s finite-element hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker for the GPU path:
+ * only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may
+ * load it.  The product (liblmtg.so) never links or calls it.
+ *
+ * Every function restates one piece of the reference, cited file:line
+ * (paths inside the LMTpp project):
+ *   mesh           include/mesh/make_rect.h:653-679, include/util/rectilinear_iterator.h:20-45
+ *   Gauss tables   include/mesh/element_Hexa.h:5-20, include/mesh/element_Quad.h:5-12
+ *   element K_e    formulations/formulation_elasticity_iso.py:45-60,
+ *                  formal_lf/material_help.py:116-134,175-183,
+ *                  include/codegen/__init__.py:23-42,82-87,
+ *                  include/formulation/formulation.h:2918-2932 (Gauss-point loop)
+ *   pattern        include/formulation/formulation.h:200-241 (ResizeMat)
+ *   scatter        formal_lf/calculate_matrix.py:64-98, include/containers/matsparse.h:757-770
+ *   penalty        include/formulation/formulation.h:1028-1071
+ *   IC(0)          include/containers/matinvsparse.h:201-261,397-423,453-491
+ *   generic CG     include/containers/conjugate_gradient.h:27-68,100-123
+ *   SpMV (Sym)     include/containers/matsparse.h:5368-5408
+ *
+ * Matrices are the reference's Mat<T,Sym<>,SparseLine<>> restated as a lower
+ * CSR: row i holds the columns j <= i in ascending order, so the diagonal is
+ * the last entry of each row.
+ */
+#ifndef FE_ORACLE_H
+#define FE_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------- mesh ---------------- */
+/* Structured Hexa mesh, nb_points[d] nodes along axis d; node creation order is x-fastest,
+ * coordinates accumulated as the reference iterator does (pos += inc).
+ * pos: nn*3, conn: ne*8.  Returns 0 on success. */
+int orc_make_rect_hexa(const double X0[3], const double X1[3], const uint32_t nb_points[3],
+                       double *pos, uint32_t *conn);
+
+/* ---------------- Gauss tables (reference C++ tables, 12-digit constants) ---------------- */
+/* Returns number of points; w[np], xi[np*dim]. */
+int orc_gauss_hexa_order2(double *w, double *xi);
+int orc_gauss_quad_order2(double *w, double *xi);
+
+/* ---------------- element matrices ---------------- */
+/* Hexa8 isotropic elasticity, one Gauss point: Ke(24x24, row-major) += w*detJ*B^T (W H) B.
+ * Returns detJ. */
+double orc_hexa8_elast_gp(const double *xyz, double E, double nu, double w, const double *xi,
+                          double *Ke);
+/* Whole element (order-2 rule, 8 points). */
+void orc_hexa8_elast_ke(const double *xyz, double E, double nu, double *Ke);
+
+/* ---------------- pattern / assembly ---------------- */
+/* Structural lower pattern (node-pair product x nnu^2, j<=i).  rowptr has n+1 entries.
+ * Phase 1: col==NULL returns nnz in *nnz (rowptr filled).  Phase 2 fills col. */
+int orc_pattern_lower(uint64_t nn, int nnu, uint64_t ne, int npe, const uint32_t *conn,
+                      uint64_t *rowptr, uint32_t *col, uint64_t *nnz);
+
+/* Assemble elasticity K (lower CSR, pattern from orc_pattern_lower) for an element type
+ * (8 = Hexa8).  E has ne entries (E_per_elem=1) or 1 entry. */
+int orc_assemble_elast(int npe, uint64_t nn, uint64_t ne, const double *pos, const uint32_t *conn,
+                       const double *E, int E_per_elem, double nu,
+                       const uint64_t *rowptr, const uint32_t *col, double *val);
+
+/* Consistent nodal loads of a uniform traction on Quad4 faces (4 node ids per face,
+ * order-2 quad rule).  F has nn*3 entries and is accumulated. */
+int orc_quad4_traction(uint64_t nfaces, const uint32_t *faces, const double *pos,
+                       const double traction[3], double *F);
+
+/* Penalty constraints (include/formulation/formulation.h:1028-1071): one coefficient per
+ * constraint.  max|diag| is taken over the current K.  Returns max|diag|. */
+double orc_penalty(uint64_t n, const uint64_t *rowptr, const uint32_t *col, double *val, double *F,
+                   uint64_t nc, const uint32_t *dof, const double *coef, const double *res,
+                   double penalty);
+
+/* y = K x for the lower-stored symmetric matrix (reference partial_mul, one thread). */
+void orc_spmv_sym_lower(uint64_t n, const uint64_t *rowptr, const uint32_t *col, const double *val,
+                        const double *x, double *y);
+
+/* ---------------- solvers ---------------- */
+/* Dense-envelope (skyline) Cholesky solve of the lower-stored SPD matrix.  x = K^-1 b. */
+int orc_skyline_solve(uint64_t n, const uint64_t *rowptr, const uint32_t *col, const double *val,
+                      const double *b, double *x);
+
+/* IC(0) factorization in place on a copy of the lower CSR (simplified variant: diagonal
+ * stores 1/sqrt(d)), reference matinvsparse.h:201-261. */
+void orc_ic0_factorize(uint64_t n, const uint64_t *rowptr, const uint32_t *col, double *val);
+/* Forward/backward solve with the factor, reference matinvsparse.h:397-423. */
+void orc_ic0_apply(uint64_t n, const uint64_t *rowptr, const uint32_t *col, const double *fac,
+                   const double *r, double *z);
+/* IC-PCG with true residual each iteration and |r|_inf <= crit (matinvsparse.h:453-491).
+ * Returns iterations or -1 when maxit is hit. */
+int orc_ic_pcg(uint64_t n, const uint64_t *rowptr, const uint32_t *col, const double *val,
+               const double *fac, const double *b, double *x, double crit, int maxit);
+/* Generic preconditioned CG (conjugate_gradient.h:27-68) with IC(0) preconditioner.
+ * crit_kind 0: NormInfDelta on alpha*d; 1: Norm2 on alpha*d; 2: relative residual
+ * |r|_2 <= crit |b|_2 (the GPU solver's criterion).  precond 0: IC(0) (fac), 1: Jacobi. */
+int orc_cg(uint64_t n, const uint64_t *rowptr, const uint32_t *col, const double *val,
+           const double *fac, int precond, const double *b, double *x, int crit_kind,
+           double crit, int maxit);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,201 @@
+"""ctypes front-end of the C oracle (TEST INFRASTRUCTURE ONLY).
+
+The oracle is the CPU restatement of LMT++'s finite-element hot path (fe_oracle.c).  Only the
+tests, the smoke check and the CPU-baseline leg of bench.py use it, always as the checker or
+the timed CPU baseline, never as part of the GPU product path.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "liboracle.so")
+
+_u64p = ctypes.POINTER(ctypes.c_uint64)
+_u32p = ctypes.POINTER(ctypes.c_uint32)
+_f64p = ctypes.POINTER(ctypes.c_double)
+
+
+def build(force=False):
+    """Compile fe_oracle.c into oracle/_build/liboracle.so (plain gcc, portable flags)."""
+    src = os.path.join(HERE, "fe_oracle.c")
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(
+            os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "fe_oracle.h"))):
+        return LIB
+    os.makedirs(BUILD, exist_ok=True)
+    tmp = LIB + ".%d.tmp" % os.getpid()
+    subprocess.check_call(["gcc", "-O2", "-std=c99", "-fPIC", "-shared", src, "-o", tmp, "-lm"])
+    os.replace(tmp, LIB)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = ctypes.CDLL(LIB)
+    return _lib
+
+
+def _p(a, t):
+    return a.ctypes.data_as(t) if a is not None else None
+
+
+def make_rect_hexa(nb_points, X0=(0.0, 0.0, 0.0), X1=(1.0, 1.0, 1.0)):
+    nbp = np.asarray(nb_points if np.ndim(nb_points) else [nb_points] * 3, dtype=np.uint32)
+    nn = int(np.prod(nbp.astype(np.int64)))
+    ne = int(np.prod(nbp.astype(np.int64) - 1))
+    pos = np.zeros((nn, 3))
+    conn = np.zeros((ne, 8), dtype=np.uint32)
+    x0 = np.asarray(X0, dtype=np.float64)
+    x1 = np.asarray(X1, dtype=np.float64)
+    rc = lib().orc_make_rect_hexa(_p(x0, _f64p), _p(x1, _f64p), _p(nbp, _u32p), _p(pos, _f64p),
+                                  _p(conn, _u32p))
+    if rc:
+        raise RuntimeError("orc_make_rect_hexa failed")
+    return pos, conn
+
+
+def hexa8_ke(xyz, E, nu):
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    Ke = np.zeros((24, 24))
+    lib().orc_hexa8_elast_ke(_p(xyz, _f64p), ctypes.c_double(E), ctypes.c_double(nu), _p(Ke, _f64p))
+    return Ke
+
+
+def pattern_lower(nn, nnu, conn):
+    conn = np.ascontiguousarray(conn, dtype=np.uint32)
+    ne, npe = conn.shape
+    n = nn * nnu
+    rowptr = np.zeros(n + 1, dtype=np.uint64)
+    nnz = ctypes.c_uint64(0)
+    L = lib()
+    L.orc_pattern_lower(ctypes.c_uint64(nn), ctypes.c_int(nnu), ctypes.c_uint64(ne), ctypes.c_int(npe),
+                        _p(conn, _u32p), _p(rowptr, _u64p), None, ctypes.byref(nnz))
+    col = np.zeros(nnz.value, dtype=np.uint32)
+    L.orc_pattern_lower(ctypes.c_uint64(nn), ctypes.c_int(nnu), ctypes.c_uint64(ne), ctypes.c_int(npe),
+                        _p(conn, _u32p), _p(rowptr, _u64p), _p(col, _u32p), ctypes.byref(nnz))
+    return rowptr, col
+
+
+def assemble_elast(pos, conn, E, nu, rowptr, col):
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    conn = np.ascontiguousarray(conn, dtype=np.uint32)
+    E = np.ascontiguousarray(np.atleast_1d(E), dtype=np.float64)
+    val = np.zeros(col.shape[0])
+    rc = lib().orc_assemble_elast(ctypes.c_int(conn.shape[1]), ctypes.c_uint64(pos.shape[0]),
+                                  ctypes.c_uint64(conn.shape[0]), _p(pos, _f64p), _p(conn, _u32p),
+                                  _p(E, _f64p), ctypes.c_int(1 if E.shape[0] > 1 else 0),
+                                  ctypes.c_double(nu), _p(rowptr, _u64p), _p(col, _u32p),
+                                  _p(val, _f64p))
+    if rc:
+        raise RuntimeError("orc_assemble_elast failed: %d" % rc)
+    return val
+
+
+def quad4_traction(faces, pos, t, F):
+    faces = np.ascontiguousarray(faces, dtype=np.uint32)
+    t = np.asarray(t, dtype=np.float64)
+    lib().orc_quad4_traction(ctypes.c_uint64(faces.shape[0]), _p(faces, _u32p), _p(pos, _f64p),
+                             _p(t, _f64p), _p(F, _f64p))
+    return F
+
+
+def penalty(rowptr, col, val, F, dofs, coef, res, pen):
+    dofs = np.ascontiguousarray(dofs, dtype=np.uint32)
+    coef = np.ascontiguousarray(coef, dtype=np.float64)
+    res = np.ascontiguousarray(res, dtype=np.float64)
+    f = lib().orc_penalty
+    f.restype = ctypes.c_double
+    return f(ctypes.c_uint64(rowptr.shape[0] - 1), _p(rowptr, _u64p), _p(col, _u32p), _p(val, _f64p),
+             _p(F, _f64p), ctypes.c_uint64(dofs.shape[0]), _p(dofs, _u32p), _p(coef, _f64p),
+             _p(res, _f64p), ctypes.c_double(pen))
+
+
+def spmv(rowptr, col, val, x):
+    y = np.zeros(rowptr.shape[0] - 1)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    lib().orc_spmv_sym_lower(ctypes.c_uint64(y.shape[0]), _p(rowptr, _u64p), _p(col, _u32p),
+                             _p(val, _f64p), _p(x, _f64p), _p(y, _f64p))
+    return y
+
+
+def skyline_solve(rowptr, col, val, b):
+    x = np.zeros(rowptr.shape[0] - 1)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    rc = lib().orc_skyline_solve(ctypes.c_uint64(x.shape[0]), _p(rowptr, _u64p), _p(col, _u32p),
+                                 _p(val, _f64p), _p(b, _f64p), _p(x, _f64p))
+    if rc:
+        raise RuntimeError("skyline solve failed: %d" % rc)
+    return x
+
+
+def ic0(rowptr, col, val):
+    fac = np.array(val, dtype=np.float64, copy=True)
+    lib().orc_ic0_factorize(ctypes.c_uint64(rowptr.shape[0] - 1), _p(rowptr, _u64p), _p(col, _u32p),
+                            _p(fac, _f64p))
+    return fac
+
+
+def ic_pcg(rowptr, col, val, fac, b, crit, maxit=100000, x0=None):
+    n = rowptr.shape[0] - 1
+    x = np.zeros(n) if x0 is None else np.array(x0, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    it = lib().orc_ic_pcg(ctypes.c_uint64(n), _p(rowptr, _u64p), _p(col, _u32p), _p(val, _f64p),
+                          _p(fac, _f64p), _p(b, _f64p), _p(x, _f64p), ctypes.c_double(crit),
+                          ctypes.c_int(maxit))
+    return x, it
+
+
+def cg(rowptr, col, val, b, crit, crit_kind=2, precond=0, fac=None, maxit=100000, x0=None):
+    n = rowptr.shape[0] - 1
+    x = np.zeros(n) if x0 is None else np.array(x0, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    it = lib().orc_cg(ctypes.c_uint64(n), _p(rowptr, _u64p), _p(col, _u32p), _p(val, _f64p),
+                      _p(fac, _f64p), ctypes.c_int(precond), _p(b, _f64p), _p(x, _f64p),
+                      ctypes.c_int(crit_kind), ctypes.c_double(crit), ctypes.c_int(maxit))
+    return x, it
+
+
+def dense_to_lower_csr(A):
+    """Lower-CSR (SparseLine Sym) of a dense symmetric matrix, dropping exact zeros."""
+    n = A.shape[0]
+    rowptr = np.zeros(n + 1, dtype=np.uint64)
+    cols, vals = [], []
+    for i in range(n):
+        for j in range(i + 1):
+            if A[i, j] != 0.0:
+                cols.append(j)
+                vals.append(A[i, j])
+        rowptr[i + 1] = len(cols)
+    return rowptr, np.array(cols, dtype=np.uint32), np.array(vals, dtype=np.float64)
+
+
+def x1_faces_hexa(pos, conn, x1=1.0, eps=1e-6):
+    """Quad4 skin faces [1,2,6,5] of Hexa elements lying on the plane x = x1."""
+    q = conn[:, [1, 2, 6, 5]]
+    on = np.all(pos[q, 0] > x1 - eps, axis=1)
+    return np.ascontiguousarray(q[on], dtype=np.uint32)
+
+
+def elasticity_problem(nb_points, E=210000.0, nu=0.3, pen=1e5, traction=(1.0, 0.0, 0.0)):
+    """The elasticity workload of the reference's example: unit cube of Hexa8, penalty clamp of
+    every node on x = 0, uniform traction on x = 1.  Returns a dict of oracle arrays."""
+    pos, conn = make_rect_hexa(nb_points)
+    nn = pos.shape[0]
+    rowptr, col = pattern_lower(nn, 3, conn)
+    val = assemble_elast(pos, conn, E, nu, rowptr, col)
+    F = np.zeros(3 * nn)
+    faces = x1_faces_hexa(pos, conn)
+    quad4_traction(faces, pos, traction, F)
+    clamped = np.nonzero(pos[:, 0] < 1e-6)[0]
+    dofs = (3 * clamped[:, None] + np.arange(3)[None, :]).ravel()
+    md = penalty(rowptr, col, val, F, dofs, np.ones(dofs.shape[0]), np.zeros(dofs.shape[0]), pen)
+    return dict(pos=pos, conn=conn, rowptr=rowptr, col=col, val=val, F=F, faces=faces, dofs=dofs,
+                max_diag=md, E=E, nu=nu, penalty=pen)

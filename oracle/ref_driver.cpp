@@ -1,0 +1,162 @@
+/*
+ * ref_driver.cpp -- runs LMT++'s own runtime on the elasticity hot path (TEST INFRASTRUCTURE).
+ *
+ * Compiled against the reference's headers and its vendored LDL/AMD sources by
+ * oracle/build_ref.sh into oracle/_ref/ (never into the product).  What comes from the
+ * reference here:
+ *   - the mesh:        make_rect(m, Hexa(), X0, X1, nb_points)   include/mesh/make_rect.h:653-679
+ *   - the storage:     Mat<double,Sym<>,SparseLine<> > with its insert-on-nonzero /
+ *                      erase-on-exact-zero semantics              include/containers/vecsparse.h:9-47
+ *   - max|diag| penalty constraints                               include/formulation/formulation.h:1028-1071
+ *   - the direct solve: LDL_solver (AMD + LDL)                     include/util/solveLDL.cpp:10-125,560
+ *   - IC(0) + IC-PCG                                              include/containers/matinvsparse.h:201-261,453-491
+ * The per-Gauss-point element integrand is the oracle's restatement (orc_hexa8_elast_gp),
+ * because the reference's element routines are produced by a Python 2 code generator that
+ * cannot run here; it is scattered exactly as the generated code does it
+ * (formal_lf/calculate_matrix.py:86-98): for each Gauss point, matrix(i,j) += tmp for j >= i.
+ *
+ * Usage: ref_driver hexa <nb_points> <E> <nu> <penalty> <outdir>
+ * Writes little-endian raw arrays: pos.f64 conn.u32 rowptr.u64 col.u32 val.f64 F.f64
+ * u_ldl.f64 u_icpcg.f64 and info.txt.
+ */
+#include "mesh/meshcaracstd.h"
+#include "mesh/make_rect.h"
+#include "containers/matinvsparse.h"
+#include "util/solveLDL.h"
+#include <cstdio>
+#include <cstdlib>
+#include <string>
+#include <vector>
+#include "fe_oracle.h"
+
+using namespace LMT;
+
+template <class T>
+static void dump(const std::string &path, const std::vector<T> &v) {
+    FILE *f = fopen(path.c_str(), "wb");
+    if (!f) { fprintf(stderr, "cannot write %s\n", path.c_str()); exit(2); }
+    if (v.size()) fwrite(&v[0], sizeof(T), v.size(), f);
+    fclose(f);
+}
+
+int main(int argc, char **argv) {
+    if (argc != 7 || std::string(argv[1]) != "hexa") {
+        fprintf(stderr, "usage: ref_driver hexa <nb_points> <E> <nu> <penalty> <outdir>\n");
+        return 1;
+    }
+    unsigned nbp = atoi(argv[2]);
+    double E = atof(argv[3]), nu = atof(argv[4]), penalty = atof(argv[5]);
+    std::string out = argv[6];
+
+    typedef Mesh<MeshCaracStd<3, 3, 1, double, 1> > TM; /* nb=1, degree 1 -> Hexa */
+    TM m;
+    make_rect(m, Hexa(), TM::Pvec(0, 0, 0), TM::Pvec(1, 1, 1), TM::Pvec(nbp, nbp, nbp));
+    unsigned nn = m.node_list.size(), ne = m.elem_list.size(), n = 3 * nn;
+
+    std::vector<double> pos(3 * nn);
+    for (unsigned i = 0; i < nn; ++i)
+        for (int d = 0; d < 3; ++d) pos[3 * i + d] = m.node_list[i].pos[d];
+    std::vector<unsigned> conn(8 * ne);
+    for (unsigned e = 0; e < ne; ++e)
+        for (int a = 0; a < 8; ++a) conn[8 * e + a] = m.node_list.number(*m.elem_list[e]->node_virtual(a));
+
+    /* assembly into an empty SparseLine matrix (the preallocated pattern is cleared before
+       every assembly, formulation.h:931-950) */
+    Mat<double, Sym<>, SparseLine<> > K(n, n);
+    double w[8], xi[24];
+    orc_gauss_hexa_order2(w, xi);
+    for (unsigned e = 0; e < ne; ++e) {
+        double xyz[24];
+        unsigned in[8];
+        for (int a = 0; a < 8; ++a) {
+            in[a] = 3 * conn[8 * e + a]; /* indice_noda = node * nnu */
+            for (int d = 0; d < 3; ++d) xyz[3 * a + d] = pos[3 * conn[8 * e + a] + d];
+        }
+        for (int g = 0; g < 8; ++g) {
+            double Ke[576] = {0};
+            orc_hexa8_elast_gp(xyz, E, nu, w[g], xi + 3 * g, Ke);
+            for (int i = 0; i < 24; ++i)
+                for (int j = i; j < 24; ++j)
+                    K(in[i / 3] + i % 3, in[j / 3] + j % 3) += Ke[24 * i + j];
+        }
+    }
+
+    /* sollicitation: uniform traction (1,0,0) on the Quad4 skin faces at x = 1 */
+    std::vector<double> F(n, 0.0);
+    std::vector<unsigned> faces;
+    for (unsigned e = 0; e < ne; ++e) {
+        const unsigned *c = &conn[8 * e];
+        /* Hexa child face 5 is nodes [1,2,6,5] (formulations/element_Hexa.py:22-29) */
+        unsigned q[4] = {c[1], c[2], c[6], c[5]};
+        bool on = true;
+        for (int a = 0; a < 4; ++a) on = on && pos[3 * q[a]] > 1 - 1e-6;
+        if (on) faces.insert(faces.end(), q, q + 4);
+    }
+    double t[3] = {1, 0, 0};
+    orc_quad4_traction(faces.size() / 4, faces.empty() ? 0 : &faces[0], &pos[0], t, &F[0]);
+
+    /* penalty constraints: node[i].dep[d] = 0 for every node on x = 0 */
+    double max_diag = max(abs(K.diag()));
+    unsigned ncons = 0;
+    for (unsigned i = 0; i < nn; ++i)
+        if (pos[3 * i] < 1e-6)
+            for (int d = 0; d < 3; ++d) {
+                double C = 1.0 * max_diag * penalty;
+                F[3 * i + d] += C * 0.0;
+                K(3 * i + d, 3 * i + d) += C * 1.0;
+                ++ncons;
+            }
+
+    /* export the lower CSR */
+    std::vector<unsigned long long> rowptr(n + 1, 0);
+    std::vector<unsigned> col;
+    std::vector<double> val;
+    for (unsigned i = 0; i < n; ++i) {
+        for (unsigned k = 0; k < K.data[i].indices.size(); ++k) {
+            col.push_back(K.data[i].indices[k]);
+            val.push_back(K.data[i].data[k]);
+        }
+        rowptr[i + 1] = col.size();
+    }
+
+    /* direct solve through the reference's LDL */
+    Mat<double, Sym<>, SparseLine<> > Kc = K;
+    LDL_solver ldl;
+    ldl.get_factorization(Kc, false);
+    Vec<double> sol;
+    sol.resize(n);
+    for (unsigned i = 0; i < n; ++i) sol[i] = F[i];
+    ldl.solve(sol);
+    std::vector<double> u_ldl(n);
+    for (unsigned i = 0; i < n; ++i) u_ldl[i] = sol[i];
+
+    /* IC(0)-PCG of the reference with |r|_inf <= 1e-10 * max|F| */
+    Mat<double, Sym<>, SparseLine<> > P = K;
+    incomplete_chol_factorize(P);
+    Vec<double> b;
+    b.resize(n);
+    double fmax = 0;
+    for (unsigned i = 0; i < n; ++i) {
+        b[i] = F[i];
+        fmax = std::max(fmax, std::abs(F[i]));
+    }
+    Vec<double> x;
+    x.resize(n, 0.0);
+    int it = solve_using_incomplete_chol_factorize(P, K, b, x, 1e-10 * fmax, false);
+    std::vector<double> u_ic(n);
+    for (unsigned i = 0; i < n; ++i) u_ic[i] = x[i];
+
+    dump(out + "/pos.f64", pos);
+    dump(out + "/conn.u32", conn);
+    dump(out + "/rowptr.u64", rowptr);
+    dump(out + "/col.u32", col);
+    dump(out + "/val.f64", val);
+    dump(out + "/F.f64", F);
+    dump(out + "/u_ldl.f64", u_ldl);
+    dump(out + "/u_icpcg.f64", u_ic);
+    FILE *f = fopen((out + "/info.txt").c_str(), "w");
+    fprintf(f, "nn %u\nne %u\nn %u\nnnz %zu\nmax_diag %.17g\nncons %u\nnfaces %zu\nicpcg_iter %d\n",
+            nn, ne, n, col.size(), max_diag, ncons, faces.size() / 4, it);
+    fclose(f);
+    return 0;
+}
