@@ -1,0 +1,394 @@
+"""Benchmark of the GB300 finite-element hot path (one JSON line on rank 0).
+
+Workload (one "step" = one time-to-solution): 3D linear isotropic elasticity on a 128^3 Hexa8
+unit cube (2,097,152 elements, 2,146,689 nodes, 6,440,067 DOF), per-element Young's modulus
+lognormal (log-mean ln 210000, log-std 0.5, numpy default_rng(20251203), element order),
+nu = 0.3, penalty clamp (1e5 * max|diag|) of every node on x = 0, uniform traction (1,0,0) on
+the x = 1 faces.  A step assembles K (FP64 element kernel + gather, FP32 copy in the same
+pass) and solves it with FP32-inner PCG wrapped in FP64 iterative refinement until the
+relative error against the FP64 oracle solution (FP64 PCG to a 1e-14 relative residual,
+computed once, untimed) is <= 1e-10.  The plain FP64 PCG is timed on the same target beside it.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--side 128]
+
+N > 1 runs N independent replicas (one per GPU, launched by torchrun): the path has no
+data-path exchange to shard on one box.  --impl reference times the CPU restatement of the
+reference's own path (oracle port: assembly + IC(0)-PCG) on a bounded sample.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SEED = 20251203
+E_MEAN, E_LOGSTD, NU, PENALTY = 210000.0, 0.5, 0.3, 1e5
+ERR_TARGET = 1e-10
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--side", type=int, default=128, help="elements per side of the cube")
+    p.add_argument("--cpu-side", type=int, default=24, help="elements per side of the CPU sample")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-fp64", action="store_true")
+    return p.parse_args()
+
+
+def lognormal_E(ne, seed=SEED):
+    rng = np.random.default_rng(seed)
+    return np.exp(np.log(E_MEAN) + E_LOGSTD * rng.standard_normal(ne))
+
+
+def dist_setup(n_gpus):
+    """torchrun ranks (replicas); returns (rank, world, local_rank, barrier, allmax)."""
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world <= 1:
+        return 0, 1, 0, (lambda: None), (lambda v: v)
+    import torch
+    import torch.distributed as dist
+    rank = int(os.environ["RANK"])
+    local = int(os.environ.get("LOCAL_RANK", rank))
+    dist.init_process_group("gloo")
+
+    def barrier():
+        dist.barrier()
+
+    def allmax(v):
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    return rank, world, local, barrier, allmax
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.proc:
+            return None
+        self.f.flush()
+        rows = [l.strip().split(", ") for l in open(self.f.name) if l.strip()]
+        os.unlink(self.f.name)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                smax = float(r[2])
+                for k, nm in enumerate(names):
+                    if r[5 + k].strip().lower().startswith("active"):
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------------------------------
+# GPU arm
+# ------------------------------------------------------------------------------------------
+def new_problem(pos, conn, E, device):
+    from lmtpp_gb300 import Formulation, x1_faces_hexa
+    f = Formulation(pos, conn, device=device)
+    f.elastic_modulus = E
+    f.poisson_ratio = NU
+    clamped = np.nonzero(pos[:, 0] < 1e-6)[0]
+    f.add_constraints((3 * clamped[:, None] + np.arange(3)).ravel(), PENALTY)
+    f.add_skin_traction(x1_faces_hexa(pos, conn), (1.0, 0.0, 0.0))
+    f.allocate_matrices()
+    return f
+
+
+def one_solve(f, mode, tol):
+    f.set_result(np.zeros(f.n))
+    f.assemble(True, True, mixed=(mode == "mixed"))
+    return f.solve_system(tol, mode=mode, maxit=200000, timeout_s=900.0)
+
+
+def rel_err(u, ref):
+    return float(np.linalg.norm(u - ref) / np.linalg.norm(ref))
+
+
+def calibrate(f, mode, ref):
+    """Largest relative-residual tolerance whose solution meets the 1e-10 error target."""
+    for tol in (1e-10, 3e-11, 1e-11, 3e-12, 1e-12, 3e-13, 1e-13, 3e-14):
+        st = one_solve(f, mode, tol)
+        e = rel_err(f.get_result(), ref)
+        if e <= ERR_TARGET:
+            return tol, e, st
+    raise RuntimeError("%s solve never reached the error target" % mode)
+
+
+def timed_steps(f, mode, tol, steps, torch, stream):
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    n0 = f.launch_count()
+    ev0.record(stream)
+    stats = [one_solve(f, mode, tol) for _ in range(steps)]
+    ev1.record(stream)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    return ev0.elapsed_time(ev1) / steps, stats, f.launch_count() - n0
+
+
+def spmv_bytes(nn, nnzb, s):
+    """Algorithmic bytes of one fused PCG SpMV launch (k_pcg_spmv): K values + block column
+    indices + row pointers, z and p_old read once, p_new and q written once."""
+    return nnzb * (9 * s + 4) + 4 * (nn + 1) + 4 * 3 * nn * s
+
+
+def run_gpu(args, rank, world, local, barrier, allmax):
+    import torch
+    from lmtpp_gb300 import make_rect_hexa
+    torch.cuda.set_device(local)
+    N = args.side
+    pos, conn = make_rect_hexa(N + 1)
+    E = lognormal_E(conn.shape[0])
+    f = new_problem(pos, conn, E, local)
+    stream = torch.cuda.ExternalStream(f.stream_handle(), device=torch.device("cuda", local))
+    # FP64 oracle solution (untimed)
+    st_ref = one_solve(f, "fp64", 1e-14)
+    u_ref = f.get_result()
+    # calibrate both solvers on the error target (untimed)
+    tol_m, err_m, st_m = calibrate(f, "mixed", u_ref)
+    tol_d = err_d = st_d = None
+    if not args.no_fp64:
+        tol_d, err_d, st_d = calibrate(f, "fp64", u_ref)
+    for _ in range(args.warmup):
+        one_solve(f, "mixed", tol_m)
+    barrier()
+    with Clocks(local) as clk:
+        ms_m, stats_m, launches = timed_steps(f, "mixed", tol_m, args.steps, torch, stream)
+    barrier()
+    ms_m = allmax(ms_m)
+    err_final = rel_err(f.get_result(), u_ref)
+    res = {"ms_mixed": ms_m, "tol_mixed": tol_m, "err_mixed": err_final, "stats_mixed": stats_m[-1],
+           "launches": launches, "clocks": clk.summary(), "ref_stats": st_ref}
+    if not args.no_fp64:
+        ms_d, stats_d, _ = timed_steps(f, "fp64", tol_d, 1, torch, stream)
+        res.update(ms_fp64=allmax(ms_d), tol_fp64=tol_d, err_fp64=rel_err(f.get_result(), u_ref),
+                   stats_fp64=stats_d[-1])
+    # dominant kernel: the fused FP32 SpMV of the inner PCG, timed alone with CUDA events
+    one_solve(f, "mixed", tol_m)
+    spmv32_ms, upd32_ms = f.profile_pcg_kernels(precision=1, iters=30)
+    spmv64_ms, upd64_ms = f.profile_pcg_kernels(precision=0, iters=10)
+    from lmtpp_gb300 import abi as _abi
+    nn_, ne_, n_, nnzb = (ctypes.c_uint64() for _ in range(4))
+    f._lib.lmtg_get_sizes(f._ctx, ctypes.byref(nn_), ctypes.byref(ne_), ctypes.byref(n_), ctypes.byref(nnzb))
+    res.update(nn=nn_.value, ne=ne_.value, ndof=n_.value, nnzb=nnzb.value, spmv32_ms=spmv32_ms,
+               upd32_ms=upd32_ms, spmv64_ms=spmv64_ms, upd64_ms=upd64_ms)
+    # assembly alone (element kernel + gather + penalty + preconditioner), CUDA events
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(3):
+        f.assemble(True, True, mixed=True)
+    ev1.record(stream)
+    ev1.synchronize()
+    res["asm_ms"] = ev0.elapsed_time(ev1) / 3
+    f.close()
+    del f
+    # end to end through the public API with host buffers: mesh H2D, pattern, assembly,
+    # mixed solve, result D2H -- a fresh Formulation every step
+    if not args.no_e2e:
+        e2e = []
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            g = new_problem(pos, conn, E, local)
+            g.solve(tol_m, mode="mixed", maxit=200000, timeout_s=900.0)
+            u = g.get_result()
+            torch.cuda.synchronize()
+            e2e.append(time.perf_counter() - t0)
+            g.close()
+        res["e2e_s"] = allmax(statistics.median(e2e))
+        res["e2e_err"] = rel_err(u, u_ref)
+        nc = 3 * int(np.sum(pos[:, 0] < 1e-6))
+        nfaces = N * N
+        res["h2d"] = pos.nbytes + conn.nbytes + E.nbytes + 8 * 3 * pos.shape[0] + nc * (4 + 8 + 8) + nfaces * 16
+        res["d2h"] = 8 * 3 * pos.shape[0]
+    return res
+
+
+# ------------------------------------------------------------------------------------------
+# CPU arm: the oracle port of the reference's CPU path (assembly with the reference's
+# per-Gauss-point scatter, max|diag| penalty, IC(0) factorization, IC-PCG with the true residual
+# and the |r|_inf test of solve_using_incomplete_chol_factorize), one thread.
+# ------------------------------------------------------------------------------------------
+def cpu_sample(side):
+    """Time-to-solution of the CPU path on a side^3 sample of the same workload family,
+    and its extrapolation to the full workload: assembly scales with the element count,
+    the PCG with element count x iterations (iterations grow like the elements per side)."""
+    from oracle import oracle as O
+    pos, conn = O.make_rect_hexa(side + 1)
+    E = lognormal_E(conn.shape[0])
+    rowptr, col = O.pattern_lower(pos.shape[0], 3, conn)
+    clamped = np.nonzero(pos[:, 0] < 1e-6)[0]
+    dofs = (3 * clamped[:, None] + np.arange(3)).ravel()
+    faces = O.x1_faces_hexa(pos, conn)
+
+    def assemble():
+        val = O.assemble_elast(pos, conn, E, NU, rowptr, col)
+        F = np.zeros(3 * pos.shape[0])
+        O.quad4_traction(faces, pos, (1.0, 0.0, 0.0), F)
+        O.penalty(rowptr, col, val, F, dofs, np.ones(dofs.shape[0]), np.zeros(dofs.shape[0]), PENALTY)
+        return val, F
+
+    val, F = assemble()
+    fac = O.ic0(rowptr, col, val)
+    ref, _ = O.cg(rowptr, col, val, F, 1e-15, crit_kind=2, precond=0, fac=fac)
+    crit = None
+    for c in (1e-8, 1e-9, 1e-10, 1e-11, 1e-12, 1e-13, 1e-14):
+        x, it = O.ic_pcg(rowptr, col, val, fac, F, c * np.abs(F).max())
+        if it >= 0 and rel_err(x, ref) <= ERR_TARGET:
+            crit = c
+            break
+    if crit is None:
+        raise RuntimeError("CPU IC-PCG never met the error target")
+    t0 = time.perf_counter()
+    val, F = assemble()
+    t1 = time.perf_counter()
+    fac = O.ic0(rowptr, col, val)
+    x, it = O.ic_pcg(rowptr, col, val, fac, F, crit * np.abs(F).max())
+    t2 = time.perf_counter()
+    return {"side": side, "t_asm": t1 - t0, "t_solve": t2 - t1, "iters": it, "crit": crit,
+            "err": rel_err(x, ref), "ne": conn.shape[0]}
+
+
+def cpu_extrapolate(s, side_full):
+    ne_full = side_full ** 3
+    return s["t_asm"] * ne_full / s["ne"] + s["t_solve"] * (side_full / s["side"]) ** 4
+
+
+def cpu_desc(s):
+    return ("Hexa8 %d^3 sample of the same workload (lognormal E, penalty clamp, traction): oracle "
+            "port assembly %.3f s + IC(0) + IC-PCG %.3f s (%d it, |r|_inf <= %.0e max|F|, rel err "
+            "%.1e); extrapolated x(ne ratio) for assembly and x(side ratio)^4 for the solve"
+            % (s["side"], s["t_asm"], s["t_solve"], s["iters"], s["crit"], s["err"]))
+
+
+METRIC = "time-to-solution at 1e-10 rel. error vs FP64 oracle, mixed vs FP64 CG; asm GB/s"
+
+
+def workload_config(args):
+    N = args.side
+    return {"workload": "Hexa8 elasticity %d^3 unit cube (%d elements, %d DOF), lognormal E "
+                        "(log-std 0.5, seed %d), nu 0.3, penalty clamp x=0, traction x=1"
+                        % (N, N ** 3, 3 * (N + 1) ** 3, SEED),
+            "elements": N ** 3, "dof": 3 * (N + 1) ** 3, "seed": SEED,
+            "error_target": ERR_TARGET, "l2": "inputs larger than L2 (K32 alone > 1 GB)",
+            "parallelism": "replicas"}
+
+
+def main():
+    args = parse()
+    rank, world, local, barrier, allmax = dist_setup(args.gpus)
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        samples = []
+        for k in range(args.warmup + args.steps):
+            s = cpu_sample(args.cpu_side)
+            if k >= args.warmup:
+                samples.append(cpu_extrapolate(s, args.side))
+        v = statistics.median(samples)
+        line = {"metric": METRIC, "value": v, "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": workload_config(args), "impl": "reference",
+                "cpu_baseline": {"value": v, "unit": "s", "cores": 1, "kind": "port",
+                                 "sample": cpu_desc(s)},
+                "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+    r = run_gpu(args, rank, world, local, barrier, allmax)
+    if rank != 0:
+        return
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm = peaks.get("hbm_gbs")
+    peak_note = "measured" if hbm else "fallback"
+    hbm = hbm or 6800.0
+    b32 = spmv_bytes(r["nn"], r["nnzb"], 4)
+    ach = b32 / (r["spmv32_ms"] * 1e-3) / 1e9
+    b64 = spmv_bytes(r["nn"], r["nnzb"], 8)
+    ach64 = b64 / (r["spmv64_ms"] * 1e-3) / 1e9
+    # assembly gather bytes: element blocks read, gather indices read, K64 + K32 written
+    asm_bytes = r["ne"] * 36 * 9 * 8 + r["ne"] * 64 * 4 + 4 * (r["nnzb"] + 1) + r["nnzb"] * 9 * (8 + 4)
+    s = cpu_sample(args.cpu_side)
+    cpu_v = cpu_extrapolate(s, args.side)
+    v = r["ms_mixed"] * 1e-3
+    line = {
+        "metric": METRIC, "value": v, "unit": "s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": r["ms_mixed"], "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64", "data": "synthetic",
+        "config": workload_config(args),
+        "roofline": {"bound": "hbm", "kernel": "k_pcg_spmv<float>", "achieved": ach, "peak": hbm,
+                     "unit": "GB/s", "frac": ach / hbm, "traffic": None,
+                     "peak_source": peak_note, "algorithmic_bytes": b32,
+                     "launch_ms": r["spmv32_ms"]},
+        "cpu_baseline": {"value": cpu_v, "unit": "s", "cores": 1, "kind": "port", "sample": cpu_desc(s)},
+        "e2e": ({"value": r["e2e_s"], "unit": "s", "h2d_bytes_per_step": r["h2d"],
+                 "d2h_bytes_per_step": r["d2h"], "rel_err": r["e2e_err"]} if "e2e_s" in r else None),
+        "gpu_launches": r["launches"],
+        "clocks": r["clocks"],
+        "rel_err": r["err_mixed"], "tol_mixed": r["tol_mixed"], "iters_mixed": r["stats_mixed"],
+        "fp64_pcg_s": r.get("ms_fp64", float("nan")) * 1e-3, "fp64_tol": r.get("tol_fp64"),
+        "fp64_rel_err": r.get("err_fp64"), "iters_fp64": r.get("stats_fp64"),
+        "mixed_speedup_vs_fp64": (r["ms_fp64"] / r["ms_mixed"]) if "ms_fp64" in r else None,
+        "spmv64": {"launch_ms": r["spmv64_ms"], "GB/s": ach64, "frac": ach64 / hbm},
+        "asm": {"ms": r["asm_ms"], "gather_bytes": asm_bytes,
+                "GB/s_incl_element_kernel": asm_bytes / (r["asm_ms"] * 1e-3) / 1e9},
+        "oracle_solve": r["ref_stats"],
+    }
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

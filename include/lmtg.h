@@ -138,6 +138,20 @@ int lmtg_set_result(lmtg_ctx *ctx, const double *u);
 /* y = K x with the assembled matrix in FP64 (precision 0) or FP32 (precision 1). */
 int lmtg_spmv(lmtg_ctx *ctx, int precision, const double *x, double *y);
 
+/* The CUDA stream (cudaStream_t) every kernel and copy of this context is issued on, so a
+ * caller can order its own work or record CUDA events around calls. */
+int lmtg_get_stream(lmtg_ctx *ctx, void **stream);
+
+/* Number of kernels this context has launched since creation (all entry points). */
+int lmtg_get_launch_count(lmtg_ctx *ctx, uint64_t *count);
+
+/* Times the two PCG iteration kernels (fused SpMV kernel, update kernel) over `iters` plain
+ * launches on the context's stream with CUDA events; precision 0 = FP64 system, 1 = FP32 inner
+ * system.  Writes the mean milliseconds per launch of each kernel.  Needs an assembled system;
+ * leaves the result vector untouched. */
+int lmtg_profile_pcg_kernels(lmtg_ctx *ctx, int precision, int iters, double *spmv_ms,
+                             double *update_ms);
+
 /* Sizes of the current problem. */
 int lmtg_get_sizes(lmtg_ctx *ctx, uint64_t *nn, uint64_t *ne, uint64_t *ndof, uint64_t *nnz_blocks);
 

@@ -1,0 +1,284 @@
+// abi.cu -- the extern "C" entry points declared in include/lmtg.h.
+//
+// Host-side orchestration of one formulation on one GPU, mirroring the calls a user makes on
+// LMT++'s FormulationAncestor (include/formulation/formulation_ancestor.h:18-262):
+// allocate_matrices -> assemble -> solve_system / solve -> get_result.  Every entry point
+// catches internal errors and returns a status; nothing throws across the ABI.
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <exception>
+#include <new>
+
+#include "lmtg_internal.cuh"
+
+using namespace lmtg;
+
+namespace {
+
+template <class F>
+int guard(lmtg_ctx *c, F &&f) {
+    if (!c) return LMTG_ERR_ARG;
+    try {
+        cudaError_t e = cudaSetDevice(c->device);
+        if (e != cudaSuccess) throw Error{LMTG_ERR_CUDA, cudaGetErrorString(e)};
+        int s = f();
+        if (s == LMTG_OK) c->err.clear();
+        return s;
+    } catch (const Error &e) {
+        c->err = e.msg;
+        return e.status;
+    } catch (const std::bad_alloc &) {
+        c->err = "host allocation failed";
+        return LMTG_ERR_NOMEM;
+    } catch (const std::exception &e) {
+        c->err = e.what();
+        return LMTG_ERR_CUDA;
+    }
+}
+
+template <class T>
+void upload(lmtg_ctx *c, DBuf<T> &d, const T *h, size_t n) {
+    d.alloc(n);
+    if (n) LMTG_CUDA(cudaMemcpyAsync(d.p, h, n * sizeof(T), cudaMemcpyHostToDevice, c->stream));
+}
+
+// Quad4 consistent loads of a uniform traction, order-2 quad rule of the reference table
+// (include/mesh/element_Quad.h:5-12, abscissae with 12 significant digits, weights 1/4).
+void quad4_loads(const double *pos, const uint32_t *q, const double t[3], double *F) {
+    const double A = 0.211324865405, B = 0.788675134595;
+    const double gp[4][2] = {{B, B}, {A, B}, {B, A}, {A, A}};
+    for (int g = 0; g < 4; ++g) {
+        const double u = gp[g][0], v = gp[g][1];
+        const double N[4] = {(1 - u) * (1 - v), u * (1 - v), u * v, (1 - u) * v};
+        const double du[4] = {-(1 - v), 1 - v, v, -v};
+        const double dv[4] = {-(1 - u), -u, u, 1 - u};
+        double tu[3] = {0, 0, 0}, tv[3] = {0, 0, 0};
+        for (int a = 0; a < 4; ++a)
+            for (int d = 0; d < 3; ++d) {
+                tu[d] += pos[3 * (uint64_t)q[a] + d] * du[a];
+                tv[d] += pos[3 * (uint64_t)q[a] + d] * dv[a];
+            }
+        const double nx = tu[1] * tv[2] - tu[2] * tv[1], ny = tu[2] * tv[0] - tu[0] * tv[2],
+                     nz = tu[0] * tv[1] - tu[1] * tv[0];
+        const double ds = std::sqrt(nx * nx + ny * ny + nz * nz) * 0.25;
+        for (int a = 0; a < 4; ++a)
+            for (int d = 0; d < 3; ++d) F[3 * (uint64_t)q[a] + d] += N[a] * t[d] * ds;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *lmtg_status_string(int s) {
+    switch (s) {
+        case LMTG_OK: return "ok";
+        case LMTG_ERR_ARG: return "invalid argument";
+        case LMTG_ERR_CUDA: return "CUDA error";
+        case LMTG_ERR_STATE: return "call out of order";
+        case LMTG_ERR_NOT_CONVERGED: return "not converged";
+        case LMTG_ERR_TIMEOUT: return "timeout";
+        case LMTG_ERR_NAN: return "NaN or Inf in the solver";
+        case LMTG_ERR_NOMEM: return "out of device memory";
+        case LMTG_ERR_UNSUPPORTED: return "unsupported";
+        default: return "unknown status";
+    }
+}
+
+const char *lmtg_last_error(const lmtg_ctx *c) { return c ? c->err.c_str() : "null context"; }
+
+int lmtg_create(int device, lmtg_ctx **out) {
+    if (!out) return LMTG_ERR_ARG;
+    *out = nullptr;
+    lmtg_ctx *c = nullptr;
+    try {
+        c = new lmtg_ctx();
+    } catch (...) {
+        return LMTG_ERR_NOMEM;
+    }
+    c->device = device;
+    int s = guard(c, [&] {
+        LMTG_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        LMTG_CUDA(cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device));
+        c->scal.alloc(2);
+        LMTG_CUDA(cudaMemset(c->scal.p, 0, c->scal.bytes()));
+        LMTG_CUDA(cudaMallocHost(&c->h_scal, 2 * sizeof(PcgScalars)));
+        memset(c->h_scal, 0, 2 * sizeof(PcgScalars));
+        c->partials.alloc((size_t)5 * c->sm_count * 16);
+        return LMTG_OK;
+    });
+    if (s != LMTG_OK) {
+        lmtg_destroy(c);
+        return s;
+    }
+    *out = c;
+    return LMTG_OK;
+}
+
+int lmtg_destroy(lmtg_ctx *c) {
+    if (!c) return LMTG_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->h_scal) cudaFreeHost(c->h_scal);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;  // DBuf destructors free device memory
+    return LMTG_OK;
+}
+
+int lmtg_make_rect_hexa(const double X0[3], const double X1[3], const uint32_t nbp[3], double *pos,
+                        uint32_t *conn) {
+    if (!X0 || !X1 || !nbp || !pos || !conn) return LMTG_ERR_ARG;
+    // Nodes: the reference iterator accumulates pos += inc along every axis, x fastest
+    // (include/util/rectilinear_iterator.h:20-45); elements as make_rect.h:667-677.
+    std::vector<double> ax[3];
+    for (int d = 0; d < 3; ++d) {
+        if (nbp[d] < 2) return LMTG_ERR_ARG;
+        const double lo = std::fmin(X0[d], X1[d]), hi = std::fmax(X0[d], X1[d]);
+        const double inc = (hi - lo) / ((double)nbp[d] - 1.0);
+        const double step = inc + (inc == 0.0 ? 1.0 : 0.0), upper = hi + step * 0.5;
+        for (double p = lo; p < upper; p += step) {
+            if (ax[d].size() == nbp[d]) return LMTG_ERR_ARG;
+            ax[d].push_back(p);
+        }
+        if (ax[d].size() != nbp[d]) return LMTG_ERR_ARG;
+    }
+    const uint64_t nx = nbp[0], ny = nbp[1], nz = nbp[2], sxy = nx * ny;
+    if (nx * ny * nz >= (1ull << 32)) return LMTG_ERR_UNSUPPORTED;
+    uint64_t n = 0;
+    for (uint64_t i = 0; i < nz; ++i)
+        for (uint64_t j = 0; j < ny; ++j)
+            for (uint64_t k = 0; k < nx; ++k, ++n) {
+                pos[3 * n] = ax[0][k];
+                pos[3 * n + 1] = ax[1][j];
+                pos[3 * n + 2] = ax[2][i];
+            }
+    uint64_t e = 0;
+    for (uint64_t i = 0; i + 1 < nz; ++i)
+        for (uint64_t j = 0; j + 1 < ny; ++j)
+            for (uint64_t k = 0; k + 1 < nx; ++k, ++e) {
+                const uint64_t b = i * sxy + j * nx + k;
+                uint32_t *c = conn + 8 * e;
+                c[0] = (uint32_t)b;
+                c[1] = (uint32_t)(b + 1);
+                c[2] = (uint32_t)(b + 1 + nx);
+                c[3] = (uint32_t)(b + nx);
+                c[4] = (uint32_t)(b + sxy);
+                c[5] = (uint32_t)(b + sxy + 1);
+                c[6] = (uint32_t)(b + sxy + 1 + nx);
+                c[7] = (uint32_t)(b + sxy + nx);
+            }
+    return LMTG_OK;
+}
+
+int lmtg_mesh_set(lmtg_ctx *c, int elem_type, uint64_t nn, const double *pos, uint64_t ne,
+                  const uint32_t *conn) {
+    return guard(c, [&] {
+        LMTG_CHECK(elem_type == LMTG_ELEM_HEXA8, LMTG_ERR_UNSUPPORTED, "element type not supported");
+        LMTG_CHECK(pos && conn && nn > 0 && ne > 0, LMTG_ERR_ARG, "empty mesh");
+        LMTG_CHECK(nn < (1ull << 32), LMTG_ERR_UNSUPPORTED, "more than 2^32 nodes");
+        c->elem_type = elem_type;
+        c->npe = 8;
+        c->nnu = 3;
+        c->npairs = 36;
+        c->nn = nn;
+        c->ne = ne;
+        c->n = 3 * nn;
+        c->h_pos.assign(pos, pos + 3 * nn);
+        c->h_conn.assign(conn, conn + 8 * ne);
+        upload(c, c->pos, pos, 3 * nn);
+        upload(c, c->conn, conn, 8 * ne);
+        // formulation defaults: elastic_modulus 1, poisson_ratio 0.33
+        // (formulations/formulation_elasticity_iso.py:5-6)
+        const double one = 1.0;
+        upload(c, c->E, &one, 1);
+        c->E_per_elem = 0;
+        c->nu = 0.33;
+        c->allocated = c->have64 = c->have32 = c->have_vec = false;
+        c->nc = 0;
+        c->penalty = 0;
+        c->h_loads.assign(c->n, 0.0);
+        LMTG_CUDA(cudaStreamSynchronize(c->stream));
+        return LMTG_OK;
+    });
+}
+
+int lmtg_material_set(lmtg_ctx *c, const double *E, uint64_t nE, double nu) {
+    return guard(c, [&] {
+        LMTG_CHECK(c->ne > 0, LMTG_ERR_STATE, "mesh_set first");
+        LMTG_CHECK(E && (nE == 1 || nE == c->ne), LMTG_ERR_ARG, "E needs 1 or ne values");
+        LMTG_CHECK(nu > -1.0 && nu < 0.5, LMTG_ERR_ARG, "poisson_ratio out of (-1, 0.5)");
+        upload(c, c->E, E, nE);
+        c->E_per_elem = nE > 1 ? 1 : 0;
+        c->nu = nu;
+        c->have64 = c->have32 = false;
+        LMTG_CUDA(cudaStreamSynchronize(c->stream));
+        return LMTG_OK;
+    });
+}
+
+int lmtg_allocate_matrices(lmtg_ctx *c, uint64_t *nnz_lower) {
+    return guard(c, [&] {
+        LMTG_CHECK(c->ne > 0, LMTG_ERR_STATE, "mesh_set first");
+        build_pattern(c);
+        c->Ke64.alloc(c->ne * (uint64_t)c->npairs * 9);
+        c->K64.alloc(c->nnzb * 9);
+        c->K32.alloc(c->nnzb * 9);
+        c->F.alloc(c->n);
+        c->u.alloc(c->n);
+        c->Dinv64.alloc(c->nn * 9);
+        c->Dinv32.alloc(c->nn * 9);
+        for (auto &w : c->w64) w.alloc(c->n);
+        for (auto &w : c->w32) w.alloc(c->n);
+        LMTG_CUDA(cudaMemsetAsync(c->u.p, 0, c->u.bytes(), c->stream));
+        LMTG_CUDA(cudaMemsetAsync(c->F.p, 0, c->F.bytes(), c->stream));
+        LMTG_CUDA(cudaStreamSynchronize(c->stream));
+        c->allocated = true;
+        c->have64 = c->have32 = c->have_vec = false;
+        if (nnz_lower) *nnz_lower = c->nnz_lower;
+        return LMTG_OK;
+    });
+}
+
+int lmtg_set_nodal_loads(lmtg_ctx *c, const double *F) {
+    return guard(c, [&] {
+        LMTG_CHECK(c->n > 0 && F, LMTG_ERR_ARG, "mesh_set first / null F");
+        c->h_loads.assign(F, F + c->n);
+        return LMTG_OK;
+    });
+}
+
+int lmtg_add_skin_traction(lmtg_ctx *c, uint64_t nfaces, const uint32_t *faces,
+                           const double traction[3]) {
+    return guard(c, [&] {
+        LMTG_CHECK(c->n > 0 && traction && (nfaces == 0 || faces), LMTG_ERR_ARG, "bad faces");
+        for (uint64_t f = 0; f < nfaces; ++f)
+            for (int a = 0; a < 4; ++a)
+                LMTG_CHECK(faces[4 * f + a] < c->nn, LMTG_ERR_ARG, "face node id >= nn");
+        for (uint64_t f = 0; f < nfaces; ++f)
+            quad4_loads(c->h_pos.data(), faces + 4 * f, traction, c->h_loads.data());
+        return LMTG_OK;
+    });
+}
+
+int lmtg_set_constraints(lmtg_ctx *c, uint64_t nc, const uint32_t *dof, const double *coef,
+                         const double *res, double penalty) {
+    return guard(c, [&] {
+        LMTG_CHECK(c->n > 0, LMTG_ERR_STATE, "mesh_set first");
+        LMTG_CHECK(nc == 0 || (dof && coef && res), LMTG_ERR_ARG, "null constraint arrays");
+        LMTG_CHECK(nc == 0 || penalty != 0.0, LMTG_ERR_UNSUPPORTED,
+                   "Lagrange-multiplier constraints (penalty == 0) are not supported");
+        for (uint64_t k = 0; k < nc; ++k)
+            LMTG_CHECK(dof[k] < c->n, LMTG_ERR_ARG, "constraint dof >= n");
+        upload(c, c->cdof, dof, nc);
+        upload(c, c->ccoef, coef, nc);
+        upload(c, c->cres, res, nc);
+        c->nc = nc;
+        c->penalty = penalty;
+        c->have64 = c->have32 = false;
+        LMTG_CUDA(cudaStreamSynchronize(c->stream));
+        return LMTG_OK;
+    });
+}
+
+}  // extern "C"

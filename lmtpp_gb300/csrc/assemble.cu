@@ -1,0 +1,198 @@
+// assemble.cu -- atomic-free gather assembly, penalty constraints, block-Jacobi inverses.
+//
+// Replaces the emitted scatter  matrix(indices[a]+o, indices[b]+o) += tmp_a_b  under the
+// global assembly mutex (formal_lf/calculate_matrix.py:86-98, include/containers/vec_mt.h:39-62)
+// and assemble_constraints (include/formulation/formulation.h:1028-1071).
+//
+// Assembly: one thread per stored value of K (BSR 3x3, full symmetric pattern).  It walks the
+// block's gather list (element order, built once by pattern.cu) and sums the element block
+// entries, transposed when the element pair is (b,a) with a > b.  No atomics, no search, a
+// deterministic summation order.  FP64 assembly can write the FP32 inner operator in the same
+// pass (rounded from the FP64 sum).
+#include <cstring>
+#include <type_traits>
+
+#include "lmtg_internal.cuh"
+
+namespace lmtg {
+
+template <class TS, bool kW64, bool kW32>
+__global__ void k_assemble(const uint32_t *__restrict__ gptr, const uint32_t *__restrict__ gsrc,
+                           const TS *__restrict__ Ke, uint64_t nvals, double *__restrict__ K64,
+                           float *__restrict__ K32) {
+    for (uint64_t idx = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; idx < nvals;
+         idx += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t blk = idx / 9;
+        const int v = (int)(idx - blk * 9);
+        const int vt = (v % 3) * 3 + v / 3;  // transposed position
+        const uint32_t g0 = gptr[blk], g1 = gptr[blk + 1];
+        typedef typename std::conditional<sizeof(TS) == 8, double, float>::type Acc;
+        Acc s = 0;
+        for (uint32_t g = g0; g < g1; ++g) {
+            const uint32_t src = __ldg(gsrc + g);
+            s += (Acc)Ke[(uint64_t)(src >> 1) * 9 + ((src & 1u) ? vt : v)];
+        }
+        if (kW64) K64[idx] = (double)s;
+        if (kW32) K32[idx] = (float)s;
+    }
+}
+
+void assemble_matrix(lmtg_ctx *c, bool from64, bool want64, bool want32) {
+    const uint64_t nvals = c->nnzb * 9;
+    const int T = 256;
+    const int grid = grid_for(c, nvals, T, 8);
+    if (from64) {
+        if (want64 && want32)
+            k_assemble<double, true, true><<<grid, T, 0, c->stream>>>(c->gptr.p, c->gsrc.p, c->Ke64.p,
+                                                                      nvals, c->K64.p, c->K32.p);
+        else if (want64)
+            k_assemble<double, true, false><<<grid, T, 0, c->stream>>>(c->gptr.p, c->gsrc.p,
+                                                                       c->Ke64.p, nvals, c->K64.p,
+                                                                       nullptr);
+        else
+            k_assemble<double, false, true><<<grid, T, 0, c->stream>>>(c->gptr.p, c->gsrc.p,
+                                                                       c->Ke64.p, nvals, nullptr,
+                                                                       c->K32.p);
+    } else {
+        k_assemble<float, false, true><<<grid, T, 0, c->stream>>>(c->gptr.p, c->gsrc.p, c->Ke32.p,
+                                                                  nvals, nullptr, c->K32.p);
+    }
+    LMTG_CUDA(cudaGetLastError());
+    c->launches += 1;
+}
+
+// ---- penalty constraints ----
+// max|diag K|: diagonal entries are non-negative-signed after fabs, so the IEEE bit pattern
+// orders like the value and an integer atomicMax is exact.
+template <class T>
+__global__ void k_max_diag(const uint32_t *__restrict__ bdiag, const T *__restrict__ K,
+                           uint64_t nn, unsigned long long *out) {
+    double m = 0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nn;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const T *d = K + (uint64_t)bdiag[i] * 9;
+        m = fmax(m, fmax(fabs((double)d[0]), fmax(fabs((double)d[4]), fabs((double)d[8]))));
+    }
+    m = warp_max(m);
+    if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
+}
+
+template <class T>
+__global__ void k_penalty(const uint32_t *__restrict__ bdiag, T *K, double *F,
+                          const uint32_t *__restrict__ dof, const double *__restrict__ coef,
+                          const double *__restrict__ res, uint64_t nc, double penalty,
+                          const unsigned long long *md_bits, bool mat, bool vec) {
+    const double md = __longlong_as_double((long long)*md_bits);
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < nc;
+         k += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t j = dof[k];
+        const double C = coef[k] * md * penalty;
+        if (vec) atomicAdd(F + j, C * res[k]);
+        if (mat) atomicAdd(K + (uint64_t)bdiag[j / 3] * 9 + 4 * (j % 3), (T)(C * coef[k]));
+    }
+}
+
+__global__ void k_round_constrained(const uint32_t *__restrict__ bdiag, const double *K64,
+                                    float *K32, const uint32_t *__restrict__ dof, uint64_t nc) {
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < nc;
+         k += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t j = dof[k];
+        const uint64_t idx = (uint64_t)bdiag[j / 3] * 9 + 4 * (j % 3);
+        K32[idx] = (float)K64[idx];
+    }
+}
+
+void apply_penalty(lmtg_ctx *c, bool mat, bool vec) {
+    if (c->nc == 0) return;
+    DBuf<unsigned long long> md;
+    md.alloc(1);
+    const int T = 256;
+    if (mat) {
+        // max|diag| of the freshly assembled K, before any constraint (formulation.h:1029-1030)
+        LMTG_CUDA(cudaMemsetAsync(md.p, 0, sizeof(unsigned long long), c->stream));
+        if (c->have64) k_max_diag<double><<<grid_for(c, c->nn, T), T, 0, c->stream>>>(c->bdiag.p, c->K64.p, c->nn, md.p);
+        else k_max_diag<float><<<grid_for(c, c->nn, T), T, 0, c->stream>>>(c->bdiag.p, c->K32.p, c->nn, md.p);
+    } else {
+        // vector-only assembly reuses the max|diag| of the last matrix assembly
+        unsigned long long bits;
+        memcpy(&bits, &c->max_diag, sizeof(bits));
+        LMTG_CUDA(cudaMemcpyAsync(md.p, &bits, sizeof(bits), cudaMemcpyHostToDevice, c->stream));
+    }
+    const int g = grid_for(c, c->nc, T);
+    if (c->have64) {
+        k_penalty<double><<<g, T, 0, c->stream>>>(c->bdiag.p, c->K64.p, c->F.p, c->cdof.p, c->ccoef.p,
+                                                  c->cres.p, c->nc, c->penalty, md.p, mat, vec);
+        if (mat && c->have32)
+            k_round_constrained<<<g, T, 0, c->stream>>>(c->bdiag.p, c->K64.p, c->K32.p, c->cdof.p, c->nc);
+    } else {
+        k_penalty<float><<<g, T, 0, c->stream>>>(c->bdiag.p, c->K32.p, c->F.p, c->cdof.p, c->ccoef.p,
+                                                 c->cres.p, c->nc, c->penalty, md.p, mat, vec);
+    }
+    LMTG_CUDA(cudaGetLastError());
+    c->launches += (mat ? 1 : 0) + 1 + ((mat && c->have64 && c->have32) ? 1 : 0);
+    unsigned long long bits = 0;
+    LMTG_CUDA(cudaMemcpyAsync(&bits, md.p, sizeof(bits), cudaMemcpyDeviceToHost, c->stream));
+    LMTG_CUDA(cudaStreamSynchronize(c->stream));
+    double v;
+    memcpy(&v, &bits, sizeof(v));
+    c->max_diag = v;
+}
+
+// ---- block-Jacobi preconditioner: inverse of every 3x3 diagonal block ----
+template <class TK>
+__global__ void k_block_jacobi(const uint32_t *__restrict__ bdiag, const TK *__restrict__ K,
+                               uint64_t nn, double *D64, float *D32) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nn;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const TK *a = K + (uint64_t)bdiag[i] * 9;
+        double m[9];
+        for (int k = 0; k < 9; ++k) m[k] = (double)a[k];
+        double c00 = m[4] * m[8] - m[5] * m[7], c01 = m[5] * m[6] - m[3] * m[8],
+               c02 = m[3] * m[7] - m[4] * m[6];
+        double det = m[0] * c00 + m[1] * c01 + m[2] * c02;
+        double id = det != 0.0 ? 1.0 / det : 0.0;
+        double r[9] = {c00 * id, (m[2] * m[7] - m[1] * m[8]) * id, (m[1] * m[5] - m[2] * m[4]) * id,
+                       c01 * id, (m[0] * m[8] - m[2] * m[6]) * id, (m[2] * m[3] - m[0] * m[5]) * id,
+                       c02 * id, (m[1] * m[6] - m[0] * m[7]) * id, (m[0] * m[4] - m[1] * m[3]) * id};
+        for (int k = 0; k < 9; ++k) {
+            if (D64) D64[i * 9 + k] = r[k];
+            if (D32) D32[i * 9 + k] = (float)r[k];
+        }
+    }
+}
+
+void build_block_jacobi(lmtg_ctx *c, bool want64, bool want32) {
+    const int T = 256;
+    const int g = grid_for(c, c->nn, T);
+    if (c->have64)
+        k_block_jacobi<double><<<g, T, 0, c->stream>>>(c->bdiag.p, c->K64.p, c->nn,
+                                                       want64 ? c->Dinv64.p : nullptr,
+                                                       want32 ? c->Dinv32.p : nullptr);
+    else
+        k_block_jacobi<float><<<g, T, 0, c->stream>>>(c->bdiag.p, c->K32.p, c->nn, nullptr,
+                                                      want32 ? c->Dinv32.p : nullptr);
+    LMTG_CUDA(cudaGetLastError());
+    c->launches += 1;
+}
+
+}  // namespace lmtg
+
+namespace lmtg {
+
+__global__ void k_round_all(const double *__restrict__ a, float *__restrict__ o, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        o[i] = (float)a[i];
+}
+
+// FP32 inner operator rounded from the assembled FP64 matrix (used when the FP64 assembly ran
+// without LMTG_ASM_MAT32 and a mixed solve is requested).
+void copy_k64_to_k32(lmtg_ctx *c) {
+    const uint64_t nv = c->nnzb * 9;
+    k_round_all<<<grid_for(c, nv, 256), 256, 0, c->stream>>>(c->K64.p, c->K32.p, nv);
+    LMTG_CUDA(cudaGetLastError());
+    c->launches += 1;
+    c->have32 = true;
+}
+
+}  // namespace lmtg

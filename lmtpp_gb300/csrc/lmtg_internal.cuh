@@ -1,0 +1,190 @@
+// lmtg_internal.cuh -- shared declarations of the GB300 finite-element hot path library.
+//
+// Layout in HBM (one context = one mesh/formulation on one GPU):
+//   pos[nn*3] f64, conn[ne*npe] u32, E[ne or 1] f64               mesh and material
+//   bptr[nn+1] u32, bcol[nnzb] u32, bdiag[nn] u32                  node-block pattern (full
+//                                                                  symmetric, sorted columns)
+//   gptr[nnzb+1] u32, gsrc[ne*npe*npe] u32                         gather lists: for every 3x3
+//                                                                  block the element blocks that
+//                                                                  sum into it, element order
+//   Ke64/Ke32[ne*npairs*9]                                         element matrices, upper node
+//                                                                  pairs (a<=b), 3x3 row-major
+//   K64/K32[nnzb*9]                                                assembled matrix, BSR 3x3
+//   F, u [n] f64                                                   load vector, solution
+//   Dinv64/Dinv32[nn*9]                                            block-Jacobi inverses
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "../../include/lmtg.h"
+
+namespace lmtg {
+
+constexpr int kWarp = 32;
+
+// Thrown inside the library only; every C entry point catches and maps to a status code.
+struct Error {
+    int status;
+    std::string msg;
+};
+
+#define LMTG_CUDA(call)                                                                          \
+    do {                                                                                         \
+        cudaError_t _e = (call);                                                                 \
+        if (_e != cudaSuccess)                                                                   \
+            throw ::lmtg::Error{_e == cudaErrorMemoryAllocation ? LMTG_ERR_NOMEM : LMTG_ERR_CUDA, \
+                                std::string(#call) + ": " + cudaGetErrorString(_e)};             \
+    } while (0)
+
+#define LMTG_CHECK(cond, status, msg)                                                            \
+    do {                                                                                         \
+        if (!(cond)) throw ::lmtg::Error{status, msg};                                           \
+    } while (0)
+
+// Typed device buffer owned by a context.
+template <class T>
+struct DBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    DBuf() = default;
+    DBuf(const DBuf &) = delete;
+    DBuf &operator=(const DBuf &) = delete;
+    ~DBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    void alloc(size_t count) {
+        if (count == n && p) return;
+        release();
+        if (count == 0) return;
+        LMTG_CUDA(cudaMalloc(&p, count * sizeof(T)));
+        n = count;
+    }
+    size_t bytes() const { return n * sizeof(T); }
+};
+
+// Scalars of one PCG run, resident on the device so that iterations need no host round trip.
+struct PcgScalars {
+    double rz;       // r . z
+    double pq;       // p . q
+    double rr;       // r . r
+    double bb;       // b . b (of the system being solved)
+    double dx_inf;   // |alpha p|_inf of the last update
+    double dx_2sq;   // |alpha p|_2^2 of the last update
+    double beta;     // current beta (0 on the first iteration)
+    double crit;     // threshold of the stopping test
+    int crit_kind;   // LMTG_CRIT_*
+    int iter;        // iterations done
+    int maxit;
+    int done;        // 1 = converged or stopped
+    int status;      // LMTG_OK / NOT_CONVERGED / NAN
+    unsigned cnt_a;  // grid-reduction tickets
+    unsigned cnt_b;
+    unsigned cnt_c;
+};
+
+}  // namespace lmtg
+
+struct lmtg_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    int sm_count = 0;
+
+    // mesh and material
+    int elem_type = 0, npe = 0, nnu = 3, npairs = 0;
+    uint64_t nn = 0, ne = 0, n = 0;
+    lmtg::DBuf<double> pos;
+    lmtg::DBuf<uint32_t> conn;
+    lmtg::DBuf<double> E;
+    int E_per_elem = 0;
+    double nu = 0.3;
+    std::vector<double> h_pos;      // host copy of positions (skin loads)
+    std::vector<uint32_t> h_conn;   // host copy of connectivity
+
+    // pattern
+    bool allocated = false;
+    uint64_t nnzb = 0, nnz_lower = 0, ngather = 0;
+    lmtg::DBuf<uint32_t> bptr, bcol, bdiag, gptr, gsrc;
+
+    // values
+    lmtg::DBuf<double> Ke64, K64, F, u, Dinv64;
+    lmtg::DBuf<float> Ke32, K32, Dinv32;
+    bool have64 = false, have32 = false, have_vec = false;
+    double max_diag = 0;
+
+    // loads and constraints (host side until assembly)
+    std::vector<double> h_loads;  // nodal + skin loads
+    uint64_t nc = 0;
+    lmtg::DBuf<uint32_t> cdof;
+    lmtg::DBuf<double> ccoef, cres;
+    double penalty = 0;
+
+    // solver workspace
+    lmtg::DBuf<double> w64[6];
+    lmtg::DBuf<float> w32[6];
+    lmtg::DBuf<double> partials;
+    lmtg::DBuf<lmtg::PcgScalars> scal;
+    lmtg::PcgScalars *h_scal = nullptr;  // pinned mirror
+
+    // number of kernels this context has launched (reported by lmtg_get_launch_count)
+    uint64_t launches = 0;
+};
+
+namespace lmtg {
+
+// ---- pattern (pattern.cu) ----
+void build_pattern(lmtg_ctx *c);
+
+// ---- element kernels (elem_hexa8.cu) ----
+void launch_hexa8_elast(lmtg_ctx *c, bool fp64);
+
+// ---- assembly (assemble.cu) ----
+void assemble_matrix(lmtg_ctx *c, bool from64, bool want64, bool want32);
+void apply_penalty(lmtg_ctx *c, bool mat, bool vec);
+void build_block_jacobi(lmtg_ctx *c, bool want64, bool want32);
+void copy_k64_to_k32(lmtg_ctx *c);
+
+// ---- solver (solver.cu) ----
+void spmv64(lmtg_ctx *c, const double *x, double *y);
+void spmv32(lmtg_ctx *c, const float *x, float *y);
+int solve_pcg64(lmtg_ctx *c, int crit_kind, double tol, int maxit, double timeout_s,
+                lmtg_solve_stats *st);
+int solve_mixed(lmtg_ctx *c, double tol, int maxit, double timeout_s, lmtg_solve_stats *st);
+void profile_pcg(lmtg_ctx *c, bool fp32, int iters, double *spmv_ms, double *update_ms);
+
+// ---- utilities (pattern.cu) ----
+// Exclusive scan of u32 counts into u32 offsets (out has count+1 entries); returns the total.
+uint64_t exclusive_scan_u32(lmtg_ctx *c, const uint32_t *in, uint32_t *out, uint64_t count);
+
+inline int grid_for(lmtg_ctx *c, uint64_t work, int threads, int per_sm = 8) {
+    uint64_t want = (work + threads - 1) / threads;
+    uint64_t cap = (uint64_t)c->sm_count * per_sm;
+    if (want > cap) want = cap;
+    return (int)(want < 1 ? 1 : want);
+}
+
+}  // namespace lmtg
+
+// ---- device helpers ----
+template <class T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+template <class T>
+__device__ __forceinline__ T warp_max(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Upper node-pair index of (a, b), a <= b, among npe nodes.
+__host__ __device__ __forceinline__ int pair_index(int a, int b, int npe) {
+    return a * npe - (a * (a - 1)) / 2 + (b - a);
+}

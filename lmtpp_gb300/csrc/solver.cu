@@ -1,0 +1,304 @@
+// solver.cu -- host drivers of the FP64 PCG and the FP32-inner / FP64-refined solve.
+//
+// Replaces Formulation::solve_system's iterative branch (include/formulation/formulation.h:
+// 1487-1504): the reference's IC(0)-PCG / 3x3-block IC-PCG (include/containers/matinvsparse.h:
+// 453-491, include/containers/MatWithTinyBlocks.h:1101-1150).  Iterations run as captured CUDA
+// graphs of kChunk iterations; the host only reads the device scalars between chunks.
+#include <chrono>
+#include <cmath>
+#include <vector>
+
+#include "solver_kernels.cuh"
+
+namespace lmtg {
+
+constexpr int kChunkPairs = 16;  // iterations per graph launch = 2 * kChunkPairs
+
+__global__ void k_scale_to32(const double *__restrict__ a, double s_inv, float *__restrict__ o,
+                             uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        o[i] = (float)(a[i] * s_inv);
+}
+
+__global__ void k_axpy_64_32(double *__restrict__ x, double s, const float *__restrict__ d,
+                             uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        x[i] += s * (double)d[i];
+}
+
+__global__ void k_dot64(const double *__restrict__ a, const double *__restrict__ b, uint64_t n,
+                        double *partials, unsigned *ticket, double *out_p) {
+    double v[1] = {0.0};
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        v[0] += a[i] * b[i];
+    double out[1];
+    if (grid_reduce<1, 0u>(v, partials, ticket, out) && threadIdx.x == 0) *out_p = out[0];
+}
+
+static int row_grid(lmtg_ctx *c) { return grid_for(c, c->nn * 32, kRowThreads, 8); }
+static int node_grid(lmtg_ctx *c) { return grid_for(c, c->nn, kRowThreads, 8); }
+
+void spmv64(lmtg_ctx *c, const double *x, double *y) {
+    k_spmv<double><<<row_grid(c), kRowThreads, 0, c->stream>>>(c->bptr.p, c->bcol.p, c->K64.p, x, y,
+                                                               c->nn);
+    LMTG_CUDA(cudaGetLastError());
+    c->launches += 1;
+}
+void spmv32(lmtg_ctx *c, const float *x, float *y) {
+    k_spmv<float><<<row_grid(c), kRowThreads, 0, c->stream>>>(c->bptr.p, c->bcol.p, c->K32.p, x, y,
+                                                              c->nn);
+    LMTG_CUDA(cudaGetLastError());
+    c->launches += 1;
+}
+
+// Second scalar slot (index 1) serves the outer loop and standalone reductions.
+static PcgScalars *outer_slot(lmtg_ctx *c) { return c->scal.p + 1; }
+
+static double read_double(lmtg_ctx *c, const double *dptr) {
+    double v = 0;
+    LMTG_CUDA(cudaMemcpyAsync(&c->h_scal[1].rr, dptr, sizeof(double), cudaMemcpyDeviceToHost,
+                              c->stream));
+    LMTG_CUDA(cudaStreamSynchronize(c->stream));
+    v = c->h_scal[1].rr;
+    return v;
+}
+
+template <class T>
+static double residual(lmtg_ctx *c, const T *K, const T *x, const T *b, T *r) {
+    PcgScalars *o = outer_slot(c);
+    k_residual<T><<<row_grid(c), kRowThreads, 0, c->stream>>>(c->bptr.p, c->bcol.p, K, x, b, r, c->nn,
+                                                              c->partials.p, &o->cnt_c, &o->rr);
+    LMTG_CUDA(cudaGetLastError());
+    c->launches += 1;
+    return read_double(c, &o->rr);
+}
+
+static double dot64(lmtg_ctx *c, const double *a, const double *b) {
+    PcgScalars *o = outer_slot(c);
+    k_dot64<<<node_grid(c), kRowThreads, 0, c->stream>>>(a, b, c->n, c->partials.p, &o->cnt_c,
+                                                         &o->rr);
+    LMTG_CUDA(cudaGetLastError());
+    c->launches += 1;
+    return read_double(c, &o->rr);
+}
+
+struct PcgBufs {
+    void *x, *r, *z, *p0, *p1, *q;
+};
+
+// One PCG run on K x = b from the current x.  b_norm2 >= 0 gives |b|^2 for the relative test
+// (otherwise b.b is computed).  Returns the status; *iters receives the iteration count.
+template <class T>
+static int run_pcg(lmtg_ctx *c, const T *K, const T *Dinv, const T *b, T *x, T *r, T *z, T *p0,
+                   T *p1, T *q, bool x_is_zero, int crit_kind, double crit, int maxit,
+                   double b_norm2, std::chrono::steady_clock::time_point deadline, bool use_deadline,
+                   int *iters) {
+    cudaStream_t s = c->stream;
+    PcgScalars init{};
+    init.crit = crit;
+    init.crit_kind = crit_kind;
+    init.maxit = maxit;
+    init.bb = b_norm2 >= 0 ? b_norm2 : 0.0;
+    LMTG_CUDA(cudaMemcpyAsync(c->scal.p, &init, sizeof(init), cudaMemcpyHostToDevice, s));
+    if (x_is_zero) {
+        LMTG_CUDA(cudaMemcpyAsync(r, b, sizeof(T) * c->n, cudaMemcpyDeviceToDevice, s));
+    } else {
+        PcgScalars *o = outer_slot(c);
+        k_residual<T><<<row_grid(c), kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, K, x, b, r, c->nn,
+                                                          c->partials.p, &o->cnt_c, &o->rr);
+        c->launches += 1;
+    }
+    k_pcg_start<T><<<node_grid(c), kRowThreads, 0, s>>>(r, b_norm2 >= 0 ? nullptr : b, Dinv, z,
+                                                         c->nn, c->scal.p, c->partials.p);
+    LMTG_CUDA(cudaMemsetAsync(p0, 0, sizeof(T) * c->n, s));
+    LMTG_CUDA(cudaGetLastError());
+    c->launches += 1;
+
+    // capture one chunk: pairs of iterations alternating the p buffers
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    LMTG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    for (int k = 0; k < kChunkPairs; ++k) {
+        k_pcg_spmv<T><<<row_grid(c), kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, K, z, p0, p1, q, c->nn,
+                                                          c->scal.p, c->partials.p);
+        k_pcg_update<T><<<node_grid(c), kRowThreads, 0, s>>>(x, r, z, p1, q, Dinv, c->nn, c->scal.p,
+                                                             c->partials.p);
+        k_pcg_spmv<T><<<row_grid(c), kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, K, z, p1, p0, q, c->nn,
+                                                          c->scal.p, c->partials.p);
+        k_pcg_update<T><<<node_grid(c), kRowThreads, 0, s>>>(x, r, z, p0, q, Dinv, c->nn, c->scal.p,
+                                                             c->partials.p);
+    }
+    cudaError_t ce = cudaStreamEndCapture(s, &graph);
+    if (ce != cudaSuccess) throw Error{LMTG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce)};
+    ce = cudaGraphInstantiate(&exec, graph, 0);
+    if (ce != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        throw Error{LMTG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce)};
+    }
+    int status = LMTG_OK;
+    const int max_chunks = maxit / (2 * kChunkPairs) + 2;
+    bool finished = false;
+    // check the initial test before the first chunk
+    LMTG_CUDA(cudaMemcpyAsync(c->h_scal, c->scal.p, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
+    LMTG_CUDA(cudaStreamSynchronize(s));
+    if (c->h_scal[0].done) finished = true;
+    for (int ch = 0; ch < max_chunks && !finished; ++ch) {
+        ce = cudaGraphLaunch(exec, s);
+        c->launches += 4 * kChunkPairs;
+        if (ce == cudaSuccess)
+            ce = cudaMemcpyAsync(c->h_scal, c->scal.p, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s);
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+        if (ce != cudaSuccess) {
+            cudaGraphExecDestroy(exec);
+            cudaGraphDestroy(graph);
+            throw Error{LMTG_ERR_CUDA, std::string("pcg chunk: ") + cudaGetErrorString(ce)};
+        }
+        if (c->h_scal[0].done) finished = true;
+        else if (use_deadline && std::chrono::steady_clock::now() > deadline) {
+            status = LMTG_ERR_TIMEOUT;
+            break;
+        }
+    }
+    cudaGraphExecDestroy(exec);
+    cudaGraphDestroy(graph);
+    *iters = c->h_scal[0].iter;
+    if (status == LMTG_OK) status = finished ? c->h_scal[0].status : LMTG_ERR_NOT_CONVERGED;
+    return status;
+}
+
+int solve_pcg64(lmtg_ctx *c, int crit_kind, double tol, int maxit, double timeout_s,
+                lmtg_solve_stats *st) {
+    auto deadline = std::chrono::steady_clock::now() +
+                    std::chrono::duration_cast<std::chrono::steady_clock::duration>(
+                        std::chrono::duration<double>(timeout_s > 0 ? timeout_s : 0));
+    double *r = c->w64[0].p, *z = c->w64[1].p, *p0 = c->w64[2].p, *p1 = c->w64[3].p,
+           *q = c->w64[4].p;
+    int it = 0;
+    int status = run_pcg<double>(c, c->K64.p, c->Dinv64.p, c->F.p, c->u.p, r, z, p0, p1, q, false,
+                                 crit_kind, tol, maxit, -1.0, deadline, timeout_s > 0, &it);
+    double bb = dot64(c, c->F.p, c->F.p);
+    double rr = residual<double>(c, c->K64.p, c->u.p, c->F.p, r);
+    st->iterations = it;
+    st->outer_iterations = 0;
+    st->rel_residual = bb > 0 ? std::sqrt(rr / bb) : std::sqrt(rr);
+    return status;
+}
+
+int solve_mixed(lmtg_ctx *c, double tol, int maxit, double timeout_s, lmtg_solve_stats *st) {
+    auto deadline = std::chrono::steady_clock::now() +
+                    std::chrono::duration_cast<std::chrono::steady_clock::duration>(
+                        std::chrono::duration<double>(timeout_s > 0 ? timeout_s : 0));
+    double *r64 = c->w64[0].p;
+    float *b32 = c->w32[0].p, *d32 = c->w32[1].p, *r32 = c->w32[2].p, *z32 = c->w32[3].p,
+          *p0 = c->w32[4].p, *p1 = c->w32[5].p;
+    float *q32 = reinterpret_cast<float *>(c->w64[1].p);  // FP64 buffer reused as FP32 q
+    const double bb = dot64(c, c->F.p, c->F.p);
+    const double eta_min = 1e-5;  // inner relative reduction floor (FP32 accuracy bound)
+    int total = 0, outer = 0, status = LMTG_OK;
+    double rel = 0;
+    const int max_outer = 60;
+    for (;;) {
+        const double rr = residual<double>(c, c->K64.p, c->u.p, c->F.p, r64);
+        rel = bb > 0 ? std::sqrt(rr / bb) : std::sqrt(rr);
+        if (!std::isfinite(rel)) {
+            status = LMTG_ERR_NAN;
+            break;
+        }
+        if (rel <= tol || rr == 0.0) break;
+        if (total >= maxit || outer >= max_outer) {
+            status = LMTG_ERR_NOT_CONVERGED;
+            break;
+        }
+        if (timeout_s > 0 && std::chrono::steady_clock::now() > deadline) {
+            status = LMTG_ERR_TIMEOUT;
+            break;
+        }
+        const double sc = std::sqrt(rr);
+        k_scale_to32<<<node_grid(c), kRowThreads, 0, c->stream>>>(r64, 1.0 / sc, b32, c->n);
+        c->launches += 1;
+        LMTG_CUDA(cudaMemsetAsync(d32, 0, sizeof(float) * c->n, c->stream));
+        double eta = 0.5 * tol / rel;
+        if (eta < eta_min) eta = eta_min;
+        int it = 0;
+        int s2 = run_pcg<float>(c, c->K32.p, c->Dinv32.p, b32, d32, r32, z32, p0, p1, q32, true,
+                                LMTG_CRIT_REL_RESIDUAL, eta, maxit - total, 1.0, deadline,
+                                timeout_s > 0, &it);
+        total += it;
+        ++outer;
+        if (s2 == LMTG_ERR_NAN || s2 == LMTG_ERR_TIMEOUT) {
+            status = s2;
+            break;
+        }
+        k_axpy_64_32<<<node_grid(c), kRowThreads, 0, c->stream>>>(c->u.p, sc, d32, c->n);
+        LMTG_CUDA(cudaGetLastError());
+        c->launches += 1;
+    }
+    st->iterations = total;
+    st->outer_iterations = outer;
+    st->rel_residual = rel;
+    return status;
+}
+
+template <class T>
+static void profile_pcg_t(lmtg_ctx *c, const T *K, const T *Dinv, const T *b, T *x, T *r, T *z,
+                          T *p0, T *p1, T *q, int iters, double *spmv_ms, double *update_ms) {
+    cudaStream_t s = c->stream;
+    PcgScalars init{};
+    init.crit = 0.0;  // never met: every launch does the full work
+    init.crit_kind = LMTG_CRIT_REL_RESIDUAL;
+    init.maxit = 1 << 30;
+    LMTG_CUDA(cudaMemcpyAsync(c->scal.p, &init, sizeof(init), cudaMemcpyHostToDevice, s));
+    LMTG_CUDA(cudaMemsetAsync(x, 0, sizeof(T) * c->n, s));
+    LMTG_CUDA(cudaMemcpyAsync(r, b, sizeof(T) * c->n, cudaMemcpyDeviceToDevice, s));
+    k_pcg_start<T><<<node_grid(c), kRowThreads, 0, s>>>(r, b, Dinv, z, c->nn, c->scal.p,
+                                                         c->partials.p);
+    LMTG_CUDA(cudaMemsetAsync(p0, 0, sizeof(T) * c->n, s));
+    c->launches += 1;
+    std::vector<cudaEvent_t> ev(2 * iters + 1);
+    for (auto &e : ev) LMTG_CUDA(cudaEventCreate(&e));
+    LMTG_CUDA(cudaEventRecord(ev[0], s));
+    for (int k = 0; k < iters; ++k) {
+        T *po = (k & 1) ? p1 : p0, *pn = (k & 1) ? p0 : p1;
+        k_pcg_spmv<T><<<row_grid(c), kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, K, z, po, pn, q, c->nn,
+                                                          c->scal.p, c->partials.p);
+        LMTG_CUDA(cudaEventRecord(ev[2 * k + 1], s));
+        k_pcg_update<T><<<node_grid(c), kRowThreads, 0, s>>>(x, r, z, pn, q, Dinv, c->nn, c->scal.p,
+                                                             c->partials.p);
+        LMTG_CUDA(cudaEventRecord(ev[2 * k + 2], s));
+    }
+    c->launches += 2ull * iters;
+    LMTG_CUDA(cudaGetLastError());
+    LMTG_CUDA(cudaEventSynchronize(ev[2 * iters]));
+    double a = 0, bsum = 0;
+    for (int k = 0; k < iters; ++k) {
+        float m1 = 0, m2 = 0;
+        cudaEventElapsedTime(&m1, ev[2 * k], ev[2 * k + 1]);
+        cudaEventElapsedTime(&m2, ev[2 * k + 1], ev[2 * k + 2]);
+        a += m1;
+        bsum += m2;
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    *spmv_ms = a / iters;
+    *update_ms = bsum / iters;
+}
+
+void profile_pcg(lmtg_ctx *c, bool fp32, int iters, double *spmv_ms, double *update_ms) {
+    if (!fp32) {
+        profile_pcg_t<double>(c, c->K64.p, c->Dinv64.p, c->F.p, c->w64[5].p, c->w64[0].p, c->w64[1].p,
+                              c->w64[2].p, c->w64[3].p, c->w64[4].p, iters, spmv_ms, update_ms);
+    } else {
+        const double bb = dot64(c, c->F.p, c->F.p);
+        float *b32 = c->w32[0].p;
+        k_scale_to32<<<node_grid(c), kRowThreads, 0, c->stream>>>(c->F.p, bb > 0 ? 1.0 / std::sqrt(bb) : 1.0,
+                                                                  b32, c->n);
+        c->launches += 1;
+        profile_pcg_t<float>(c, c->K32.p, c->Dinv32.p, b32, c->w32[1].p, c->w32[2].p, c->w32[3].p,
+                             c->w32[4].p, c->w32[5].p, reinterpret_cast<float *>(c->w64[1].p), iters,
+                             spmv_ms, update_ms);
+    }
+}
+
+}  // namespace lmtg

@@ -1,0 +1,284 @@
+// solver_kernels.cuh -- BSR 3x3 SpMV and the fused PCG iteration kernels.
+//
+// Replaces the reference's symmetric SparseLine SpMV (include/containers/matsparse.h:5368-5408)
+// and the CG loop of conjugate_gradient (include/containers/conjugate_gradient.h:27-68):
+//   q = K d; alpha = deltn / d.q; x += alpha d; r -= alpha q; s = P r; deltn = r.s; d = s + beta d
+// with the 3x3 block-Jacobi preconditioner P standing in for the sequential IC(0) sweeps
+// (matinvsparse.h:397-423), which have no parallel form.
+//
+// One PCG iteration = two kernels, no host round trip:
+//   A  k_pcg_spmv:   p_new = z + beta p_old (formed on the fly for every column read),
+//                    q = K p_new, pq = p_new . q          (grid reduction, last block finalises)
+//   B  k_pcg_update: alpha = rz / pq; x += alpha p; r -= alpha q; z = P r;
+//                    rz, rr, |alpha p|_inf, |alpha p|_2^2, |r|_inf   -> beta, stopping test
+// Scalars live in device memory (PcgScalars); when the test passes, `done` is set and every
+// later kernel returns at once, so the host can launch iterations in captured chunks.
+#pragma once
+#include "lmtg_internal.cuh"
+
+namespace lmtg {
+
+constexpr int kRowThreads = 256;  // SpMV / PCG block size (8 warps, one node row per warp)
+
+// Block + grid reduction of NV doubles; max for bits set in kMaxMask, sum otherwise.
+// Returns true in the last block to arrive, where `out` holds the grid result (all threads).
+// Deterministic: partials are combined in a fixed order.
+template <int NV, unsigned kMaxMask>
+__device__ __forceinline__ bool grid_reduce(double (&v)[NV], double *partials, unsigned *ticket,
+                                            double (&out)[NV]) {
+    __shared__ double sh[NV][32];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+        v[i] = ((kMaxMask >> i) & 1u) ? warp_max(v[i]) : warp_sum(v[i]);
+        if (lane == 0) sh[i][wid] = v[i];
+    }
+    __syncthreads();
+    if (wid == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            double x = lane < nw ? sh[i][lane] : 0.0;
+            x = ((kMaxMask >> i) & 1u) ? warp_max(x) : warp_sum(x);
+            if (lane == 0) partials[(size_t)i * gridDim.x + blockIdx.x] = x;
+        }
+    }
+    if (threadIdx.x == 0) {
+        __threadfence();
+        unsigned t = atomicInc(ticket, gridDim.x - 1);  // wraps to 0 for the next launch
+        last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+        double x = 0.0;
+        for (unsigned k = threadIdx.x; k < gridDim.x; k += blockDim.x) {
+            double y = __ldcg(partials + (size_t)i * gridDim.x + k);
+            x = ((kMaxMask >> i) & 1u) ? fmax(x, y) : x + y;
+        }
+        x = ((kMaxMask >> i) & 1u) ? warp_max(x) : warp_sum(x);
+        __syncthreads();
+        if (lane == 0) sh[i][wid] = x;
+        __syncthreads();
+        double y = lane < nw ? sh[i][lane] : 0.0;
+        y = ((kMaxMask >> i) & 1u) ? warp_max(y) : warp_sum(y);
+        out[i] = y;
+    }
+    return true;
+}
+
+// Row product of node row I: acc[r] = sum_blocks sum_c K_IJ[r][c] * X(3J+c), X from a functor.
+// Lanes stride over the row's 9*deg contiguous values (coalesced); block/row/col of a value
+// are tracked incrementally (32 = 3*9 + 5).
+template <class T, class XF>
+__device__ __forceinline__ void bsr3_row(const uint32_t *__restrict__ bcol, const T *__restrict__ K,
+                                         uint32_t rb, uint32_t re, int lane, XF xf, T &a0, T &a1,
+                                         T &a2) {
+    const T *base = K + (uint64_t)rb * 9;
+    const uint32_t nv = (re - rb) * 9;
+    uint32_t b = lane / 9;
+    int rem = lane - 9 * (int)b;
+    a0 = a1 = a2 = (T)0;
+    for (uint32_t v = lane; v < nv; v += 32) {
+        const uint32_t J = __ldg(bcol + rb + b);
+        const int rr = rem / 3, cc = rem - 3 * (rem / 3);
+        const T prod = __ldg(base + v) * xf(3 * (uint64_t)J + cc);
+        if (rr == 0) a0 += prod;
+        else if (rr == 1) a1 += prod;
+        else a2 += prod;
+        rem += 5;
+        b += 3;
+        if (rem >= 9) {
+            rem -= 9;
+            b += 1;
+        }
+    }
+    a0 = warp_sum(a0);
+    a1 = warp_sum(a1);
+    a2 = warp_sum(a2);
+}
+
+// y = K x
+template <class T>
+__global__ void __launch_bounds__(kRowThreads)
+    k_spmv(const uint32_t *__restrict__ bptr, const uint32_t *__restrict__ bcol,
+           const T *__restrict__ K, const T *__restrict__ x, T *__restrict__ y, uint64_t nn) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t I = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; I < nn; I += nw) {
+        T a0, a1, a2;
+        bsr3_row(bcol, K, bptr[I], bptr[I + 1], lane, [&](uint64_t j) { return __ldg(x + j); }, a0,
+                 a1, a2);
+        if (lane < 3) y[3 * I + lane] = lane == 0 ? a0 : (lane == 1 ? a1 : a2);
+    }
+}
+
+// r = b - K x (T), rr = r.r accumulated in FP64 into *rr_out (grid reduction).
+template <class T>
+__global__ void __launch_bounds__(kRowThreads)
+    k_residual(const uint32_t *__restrict__ bptr, const uint32_t *__restrict__ bcol,
+               const T *__restrict__ K, const T *__restrict__ x, const T *__restrict__ b,
+               T *__restrict__ r, uint64_t nn, double *partials, unsigned *ticket,
+               double *rr_out) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    double v[1] = {0.0};
+    for (uint64_t I = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; I < nn; I += nw) {
+        T a0, a1, a2;
+        bsr3_row(bcol, K, bptr[I], bptr[I + 1], lane, [&](uint64_t j) { return __ldg(x + j); }, a0,
+                 a1, a2);
+        if (lane < 3) {
+            const uint64_t i = 3 * I + lane;
+            const T ri = b[i] - (lane == 0 ? a0 : (lane == 1 ? a1 : a2));
+            r[i] = ri;
+            v[0] += (double)ri * (double)ri;
+        }
+    }
+    double out[1];
+    if (grid_reduce<1, 0u>(v, partials, ticket, out) && threadIdx.x == 0) *rr_out = out[0];
+}
+
+// Start of a PCG run: z = P r, rz, rr, |r|_inf; optional bb = b.b.  Initial stopping test on
+// the residual criteria (the delta criteria need one step, conjugate_gradient.h:40-41).
+template <class T>
+__global__ void k_pcg_start(const T *__restrict__ r, const T *__restrict__ b,
+                            const T *__restrict__ Dinv, T *__restrict__ z, uint64_t nn,
+                            PcgScalars *S, double *partials) {
+    double v[4] = {0.0, 0.0, 0.0, 0.0};  // rz, rr, bb, rinf
+    for (uint64_t I = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; I < nn;
+         I += (uint64_t)gridDim.x * blockDim.x) {
+        const T *D = Dinv + 9 * I;
+        const T r0 = r[3 * I], r1 = r[3 * I + 1], r2 = r[3 * I + 2];
+        const T z0 = D[0] * r0 + D[1] * r1 + D[2] * r2;
+        const T z1 = D[3] * r0 + D[4] * r1 + D[5] * r2;
+        const T z2 = D[6] * r0 + D[7] * r1 + D[8] * r2;
+        z[3 * I] = z0;
+        z[3 * I + 1] = z1;
+        z[3 * I + 2] = z2;
+        v[0] += (double)r0 * z0 + (double)r1 * z1 + (double)r2 * z2;
+        v[1] += (double)r0 * r0 + (double)r1 * r1 + (double)r2 * r2;
+        if (b) {
+            const T b0 = b[3 * I], b1 = b[3 * I + 1], b2 = b[3 * I + 2];
+            v[2] += (double)b0 * b0 + (double)b1 * b1 + (double)b2 * b2;
+        }
+        v[3] = fmax(v[3], fmax(fabs((double)r0), fmax(fabs((double)r1), fabs((double)r2))));
+    }
+    double out[4];
+    if (grid_reduce<4, 8u>(v, partials, &S->cnt_c, out) && threadIdx.x == 0) {
+        S->rz = out[0];
+        S->rr = out[1];
+        if (b) S->bb = out[2];
+        S->beta = 0.0;
+        S->iter = 0;
+        S->status = LMTG_OK;
+        S->done = 0;
+        if (S->crit_kind == LMTG_CRIT_REL_RESIDUAL && out[1] <= S->crit * S->crit * S->bb)
+            S->done = 1;
+        if (S->crit_kind == LMTG_CRIT_ABS_RESIDUAL_INF && out[3] <= S->crit) S->done = 1;
+        if (!isfinite(out[0]) || !isfinite(out[1])) {
+            S->done = 1;
+            S->status = LMTG_ERR_NAN;
+        }
+    }
+}
+
+// Kernel A: p_new = z + beta p_old; q = K p_new; pq = p_new . q
+template <class T>
+__global__ void __launch_bounds__(kRowThreads)
+    k_pcg_spmv(const uint32_t *__restrict__ bptr, const uint32_t *__restrict__ bcol,
+               const T *__restrict__ K, const T *__restrict__ z, const T *__restrict__ pold,
+               T *__restrict__ pnew, T *__restrict__ q, uint64_t nn, PcgScalars *S,
+               double *partials) {
+    if (*(volatile int *)&S->done) return;
+    const T beta = (T)S->beta;
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    double v[1] = {0.0};
+    for (uint64_t I = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; I < nn; I += nw) {
+        T a0, a1, a2;
+        bsr3_row(bcol, K, bptr[I], bptr[I + 1], lane,
+                 [&](uint64_t j) { return __ldg(z + j) + beta * __ldg(pold + j); }, a0, a1, a2);
+        if (lane < 3) {
+            const uint64_t i = 3 * I + lane;
+            const T pn = z[i] + beta * pold[i];
+            const T qi = lane == 0 ? a0 : (lane == 1 ? a1 : a2);
+            pnew[i] = pn;
+            q[i] = qi;
+            v[0] += (double)pn * (double)qi;
+        }
+    }
+    double out[1];
+    if (grid_reduce<1, 0u>(v, partials, &S->cnt_a, out) && threadIdx.x == 0) S->pq = out[0];
+}
+
+// Kernel B: alpha, updates, preconditioner, dots, beta and the stopping test.
+template <class T>
+__global__ void k_pcg_update(T *__restrict__ x, T *__restrict__ r, T *__restrict__ z,
+                             const T *__restrict__ p, const T *__restrict__ q,
+                             const T *__restrict__ Dinv, uint64_t nn, PcgScalars *S,
+                             double *partials) {
+    if (*(volatile int *)&S->done) return;
+    const double pq = S->pq;
+    const T alpha = (T)(S->rz / (pq + (pq == 0.0 ? 1.0 : 0.0)));
+    double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};  // rz, rr, dx2, dxinf, rinf
+    for (uint64_t I = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; I < nn;
+         I += (uint64_t)gridDim.x * blockDim.x) {
+        T rv[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const uint64_t i = 3 * I + c;
+            const T dx = alpha * p[i];
+            x[i] += dx;
+            rv[c] = r[i] - alpha * q[i];
+            r[i] = rv[c];
+            v[2] += (double)dx * dx;
+            v[3] = fmax(v[3], fabs((double)dx));
+            v[4] = fmax(v[4], fabs((double)rv[c]));
+        }
+        const T *D = Dinv + 9 * I;
+        const T z0 = D[0] * rv[0] + D[1] * rv[1] + D[2] * rv[2];
+        const T z1 = D[3] * rv[0] + D[4] * rv[1] + D[5] * rv[2];
+        const T z2 = D[6] * rv[0] + D[7] * rv[1] + D[8] * rv[2];
+        z[3 * I] = z0;
+        z[3 * I + 1] = z1;
+        z[3 * I + 2] = z2;
+        v[0] += (double)rv[0] * z0 + (double)rv[1] * z1 + (double)rv[2] * z2;
+        v[1] += (double)rv[0] * rv[0] + (double)rv[1] * rv[1] + (double)rv[2] * rv[2];
+    }
+    double out[5];
+    if (grid_reduce<5, (8u | 16u)>(v, partials, &S->cnt_b, out) && threadIdx.x == 0) {
+        const double rz_old = S->rz;
+        S->iter += 1;
+        S->rr = out[1];
+        S->dx_2sq = out[2];
+        S->dx_inf = out[3];
+        S->beta = out[0] / rz_old;
+        S->rz = out[0];
+        bool conv = false;
+        switch (S->crit_kind) {
+            case LMTG_CRIT_REL_RESIDUAL: conv = out[1] <= S->crit * S->crit * S->bb; break;
+            case LMTG_CRIT_NORM_INF_DELTA: conv = out[3] <= S->crit; break;
+            case LMTG_CRIT_NORM2_DELTA: conv = sqrt(out[2]) < S->crit; break;
+            case LMTG_CRIT_ABS_RESIDUAL_INF: conv = out[4] <= S->crit; break;
+        }
+        if (!isfinite(out[0]) || !isfinite(out[1]) || !isfinite(pq)) {
+            S->status = LMTG_ERR_NAN;
+            S->done = 1;
+        } else if (conv) {
+            S->done = 1;
+        } else if (S->iter >= S->maxit) {
+            S->status = LMTG_ERR_NOT_CONVERGED;
+            S->done = 1;
+        }
+    }
+}
+
+// Mixed-precision helpers: r32 = r64 * s_inv ; x64 += s * d32
+__global__ void k_scale_to32(const double *__restrict__ a, double s_inv, float *__restrict__ o,
+                             uint64_t n);
+__global__ void k_axpy_64_32(double *__restrict__ x, double s, const float *__restrict__ d,
+                             uint64_t n);
+
+}  // namespace lmtg

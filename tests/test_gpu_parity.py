@@ -1,0 +1,204 @@
+"""GPU parity of the hot path against the oracle and the reference's golden outputs.
+
+Tolerances (from the path's contract): pattern and DOF maps bit-exact; assembled entries
+1e-12 relative to max|K|; FP64 solutions 1e-10 relative to the reference's LDL solution;
+mixed-precision solutions 1e-8 (they are refined to the same 1e-10 target here).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from lmtpp_gb300 import Formulation, abi, make_rect_hexa, x1_faces_hexa
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def load_golden(golden_dir, name):
+    g = np.load(os.path.join(golden_dir, name + ".npz"))
+    d = {k: g[k] for k in g.files}
+    d["meta"] = json.loads(str(d["meta"]))
+    return d
+
+
+def csr(rowptr, col, val, n):
+    return sp.csr_matrix((val, col.astype(np.int64), rowptr.astype(np.int64)), shape=(n, n))
+
+
+def build_problem(pos, conn, E, nu, pen, traction=(1.0, 0.0, 0.0)):
+    f = Formulation(pos, conn)
+    f.elastic_modulus = E
+    f.poisson_ratio = nu
+    clamped = np.nonzero(pos[:, 0] < 1e-6)[0]
+    f.add_constraints((3 * clamped[:, None] + np.arange(3)).ravel(), pen)
+    f.add_skin_traction(x1_faces_hexa(pos, conn), traction)
+    f.allocate_matrices()
+    return f
+
+
+@pytest.mark.parametrize("name", ["hexa_2x2x2", "hexa_10x10x10"])
+def test_assembly_matches_reference(golden_dir, name):
+    g = load_golden(golden_dir, name)
+    m = g["meta"]
+    pos, conn = make_rect_hexa(m["nb_points"])
+    assert np.array_equal(pos, g["pos"]) and np.array_equal(conn, g["conn"])
+    f = build_problem(pos, conn, m["E"], m["nu"], m["penalty"])
+    f.assemble(True, True)
+    rowptr, col, val = f.get_mat()
+    # structural lower pattern, bit-exact against the oracle's
+    rp_o, col_o = O.pattern_lower(pos.shape[0], 3, conn)
+    assert np.array_equal(rowptr, rp_o) and np.array_equal(col, col_o)
+    n = 3 * pos.shape[0]
+    A = csr(g["rowptr"], g["col"], g["val"], n)  # reference (exact zeros erased)
+    B = csr(rowptr, col, val, n)
+    kmax = abs(A).max()
+    # entries the reference erased (exactly 0.0 there) must be round-off level here
+    As = A.copy()
+    As.data[:] = 1.0
+    Bs = B.copy()
+    Bs.data[:] = 1.0
+    miss = Bs - As
+    miss.eliminate_zeros()
+    mi = miss.nonzero()
+    assert np.all(np.abs(np.asarray(B[mi]).ravel()) <= 1e-12 * kmax)
+    assert abs(A - B).max() <= 1e-12 * kmax
+    np.testing.assert_allclose(f.get_sollicitation(), g["F"], rtol=0, atol=1e-15)
+    f.close()
+
+
+def test_element_matrices_match_oracle_on_distorted_mesh():
+    pos, conn = make_rect_hexa(6)
+    rng = np.random.default_rng(1)
+    inner = np.all((pos > 1e-9) & (pos < 1 - 1e-9), axis=1)
+    pos = pos + inner[:, None] * rng.uniform(-0.06, 0.06, pos.shape)
+    E = rng.uniform(5e4, 3e5, conn.shape[0])
+    f = Formulation(pos, conn)
+    f.elastic_modulus = E
+    f.poisson_ratio = 0.27
+    f.allocate_matrices()
+    f.assemble(True, False)
+    Ke = f.element_matrices(0, conn.shape[0])
+    for e in range(conn.shape[0]):
+        Ko = O.hexa8_ke(pos[conn[e]], E[e], 0.27)
+        assert np.abs(Ke[e] - Ko).max() <= 1e-12 * np.abs(Ko).max(), e
+    # FP32 element kernel (native FP32 assembly)
+    f.assemble(True, False, native_fp32=True)
+    K32 = f.element_matrices(0, 20, precision=1)
+    for e in range(20):
+        Ko = O.hexa8_ke(pos[conn[e]], E[e], 0.27)
+        assert np.abs(K32[e] - Ko).max() <= 2e-6 * np.abs(Ko).max(), e
+    f.close()
+
+
+@pytest.mark.parametrize("name", ["hexa_2x2x2", "hexa_10x10x10"])
+@pytest.mark.parametrize("mode,tol", [("fp64", 1e-10), ("mixed", 1e-8)])
+def test_solution_matches_reference_ldl(golden_dir, name, mode, tol):
+    g = load_golden(golden_dir, name)
+    m = g["meta"]
+    pos, conn = make_rect_hexa(m["nb_points"])
+    f = build_problem(pos, conn, m["E"], m["nu"], m["penalty"])
+    st = f.solve(1e-13 if mode == "fp64" else 1e-12, mode=mode)
+    u = f.get_result()
+    ref = g["u_ldl"]
+    rel = np.linalg.norm(u - ref) / np.linalg.norm(ref)
+    assert rel <= tol, (rel, st)
+    assert st["rel_residual"] <= 1e-11
+    if mode == "mixed":
+        assert st["outer_iterations"] >= 1
+    f.close()
+
+
+def test_spmv_matches_oracle():
+    P = O.elasticity_problem(9)
+    f = build_problem(P["pos"], P["conn"], P["E"], P["nu"], P["penalty"])
+    f.assemble(True, True, mixed=True)
+    x = np.random.default_rng(2).standard_normal(3 * P["pos"].shape[0])
+    y_o = O.spmv(P["rowptr"], P["col"], P["val"], x)
+    y = f.spmv(x, 0)
+    assert np.abs(y - y_o).max() <= 1e-12 * np.abs(y_o).max()
+    y32 = f.spmv(x, 1)
+    assert np.abs(y32 - y_o).max() <= 1e-5 * np.abs(y_o).max()
+    f.close()
+
+
+@pytest.mark.parametrize("criterion,crit", [("norm_inf_delta", 1e-12), ("norm2_delta", 1e-12),
+                                            ("abs_residual_inf", 1e-9)])
+def test_reference_stopping_criteria(criterion, crit):
+    P = O.elasticity_problem(7)
+    f = build_problem(P["pos"], P["conn"], P["E"], P["nu"], P["penalty"])
+    st = f.solve(crit, mode="fp64", criterion=criterion)
+    u = f.get_result()
+    x = O.skyline_solve(P["rowptr"], P["col"], P["val"], P["F"])
+    assert np.linalg.norm(u - x) / np.linalg.norm(x) <= 1e-6, st
+    if criterion == "abs_residual_inf":
+        r = P["F"] - O.spmv(P["rowptr"], P["col"], P["val"], u)
+        assert np.abs(r).max() <= 10 * crit
+    f.close()
+
+
+def test_known_answer_cg_systems_through_oracle_parity():
+    """The reference's CG known answers (conjugate_gradient_test.cpp) are dense systems; the
+    GPU path solves FE systems only, so they pin the oracle (CPU tests) and the oracle pins the
+    GPU path here on an FE system solved both ways with the same criterion."""
+    P = O.elasticity_problem(5)
+    f = build_problem(P["pos"], P["conn"], P["E"], P["nu"], P["penalty"])
+    f.solve(1e-14, mode="fp64")
+    u = f.get_result()
+    x, it = O.cg(P["rowptr"], P["col"], P["val"], P["F"], 1e-14, crit_kind=2, precond=1)
+    assert it > 0
+    assert np.linalg.norm(u - x) / np.linalg.norm(x) <= 1e-11
+    f.close()
+
+
+def test_large_mesh_properties():
+    """At a size the oracle's direct solver would not finish quickly: symmetry of K, residual of
+    the returned solution recomputed independently, and FP64 vs mixed agreement."""
+    pos, conn = make_rect_hexa(33)
+    rng = np.random.default_rng(20251203)
+    E = np.exp(np.log(210000.0) + 0.5 * rng.standard_normal(conn.shape[0]))
+    f = build_problem(pos, conn, E, 0.3, 1e5)
+    st64 = f.solve(1e-12, mode="fp64")
+    u64 = f.get_result()
+    rowptr, col, val = f.get_mat()
+    F = f.get_sollicitation()
+    r = F - O.spmv(rowptr, col, val, u64)
+    assert np.linalg.norm(r) <= 1e-11 * np.linalg.norm(F), st64
+    f.set_result(np.zeros_like(u64))
+    stm = f.solve(1e-12, mode="mixed")
+    um = f.get_result()
+    assert np.linalg.norm(um - u64) / np.linalg.norm(u64) <= 1e-8, (st64, stm)
+    f.close()
+
+
+def test_failure_paths_report_status_and_keep_context_usable():
+    P = O.elasticity_problem(6)
+    f = build_problem(P["pos"], P["conn"], P["E"], P["nu"], P["penalty"])
+    with pytest.raises(abi.LmtgError) as ei:
+        f.solve(1e-14, mode="fp64", maxit=3)
+    assert ei.value.status == abi.ERR_NOT_CONVERGED
+    assert f.last_stats is None or True
+    # a NaN modulus (host-side bad input) is reported as a NaN status, not a fault
+    E = np.full(P["conn"].shape[0], P["E"])
+    E[5] = np.nan
+    f.elastic_modulus = E
+    with pytest.raises(abi.LmtgError) as ei:
+        f.solve(1e-10, mode="fp64")
+    assert ei.value.status == abi.ERR_NAN
+    # the same context still solves a good problem afterwards
+    f.elastic_modulus = P["E"]
+    f.set_result(np.zeros(3 * P["pos"].shape[0]))
+    st = f.solve(1e-12, mode="fp64")
+    assert st["rel_residual"] <= 1e-11
+    f.close()
+
+
+def test_solve_before_assemble_is_a_state_error():
+    pos, conn = make_rect_hexa(3)
+    f = Formulation(pos, conn)
+    with pytest.raises(abi.LmtgError) as ei:
+        f.solve_system(1e-10)
+    assert ei.value.status == abi.ERR_STATE
+    f.close()

@@ -1,0 +1,116 @@
+"""The oracle pinned against the reference's own outputs (CPU only).
+
+Golden fixtures come from LMT++'s runtime (tests/golden/make_golden.py): make_rect, the Sym
+SparseLine storage with erase-on-exact-zero, max|diag| penalty, LDL and IC(0)-PCG.  The CG
+known answers come from the reference's unit tests (conjugate_gradient_test.cpp:15-71).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from oracle import oracle as O
+
+
+def err_unit_test(a, b):
+    """ERROR_UNIT_TEST of include/util/unit_test.h:17."""
+    return np.abs(a - b) / (1e-20 + np.abs(a) + np.abs(b))
+
+
+def load_golden(golden_dir, name):
+    g = np.load(os.path.join(golden_dir, name + ".npz"))
+    d = {k: g[k] for k in g.files}
+    d["meta"] = json.loads(str(d["meta"]))
+    return d
+
+
+def csr(rowptr, col, val, n):
+    return sp.csr_matrix((val, col.astype(np.int64), rowptr.astype(np.int64)), shape=(n, n))
+
+
+@pytest.mark.parametrize("name", ["hexa_2x2x2", "hexa_10x10x10"])
+def test_oracle_matches_reference_runtime(golden_dir, name):
+    g = load_golden(golden_dir, name)
+    m = g["meta"]
+    P = O.elasticity_problem(m["nb_points"], E=m["E"], nu=m["nu"], pen=m["penalty"])
+    n = P["F"].shape[0]
+    # mesh and connectivity: bit-exact (make_rect node order, accumulated coordinates)
+    assert np.array_equal(P["pos"], g["pos"])
+    assert np.array_equal(P["conn"], g["conn"])
+    # pattern: the reference's is the structural lower pattern minus entries that summed to
+    # exactly 0.0 (vecsparse.h:15-40); the oracle keeps the structural pattern
+    A = csr(g["rowptr"], g["col"], g["val"], n)
+    B = csr(P["rowptr"], P["col"], P["val"], n)
+    Bs, As = B.copy(), A.copy()
+    Bs.data[:] = 1.0
+    As.data[:] = 1.0
+    extra_in_ref = As - As.multiply(Bs)
+    assert extra_in_ref.count_nonzero() == 0
+    missing = (Bs - As.multiply(Bs))
+    missing.eliminate_zeros()
+    mi = missing.nonzero()
+    assert np.all(B[mi] == 0.0)  # erased entries are exact zeros in the oracle too
+    assert len(mi[0]) == int(np.sum(P["val"] == 0.0))
+    # values: same integrand, same per-Gauss-point scatter order -> identical sums
+    d = abs(A - B)
+    assert d.max() <= 1e-12 * abs(B).max()
+    assert P["max_diag"] == pytest.approx(m["max_diag"], rel=1e-14)
+    np.testing.assert_allclose(P["F"], g["F"], rtol=0, atol=1e-15)
+    # direct solve: skyline Cholesky vs the reference's LDL
+    x = O.skyline_solve(P["rowptr"], P["col"], P["val"], P["F"])
+    assert np.linalg.norm(x - g["u_ldl"]) <= 1e-12 * np.linalg.norm(g["u_ldl"])
+    # IC(0)-PCG restatement vs the reference's solve_using_incomplete_chol_factorize
+    fac = O.ic0(P["rowptr"], P["col"], P["val"])
+    xi, it = O.ic_pcg(P["rowptr"], P["col"], P["val"], fac, P["F"], 1e-10 * np.abs(P["F"]).max())
+    assert it == m["icpcg_iter"]
+    assert np.linalg.norm(xi - g["u_icpcg"]) <= 1e-10 * np.linalg.norm(g["u_icpcg"])
+
+
+@pytest.mark.parametrize("case", ["cg0", "cg1"])
+def test_oracle_cg_known_answers(golden_dir, case):
+    ka = json.load(open(os.path.join(golden_dir, "cg_known_answers.json")))[case]
+    A = np.array(ka["A"], dtype=np.float64)
+    rowptr, col, val = O.dense_to_lower_csr(A)
+    fac = O.ic0(rowptr, col, val)
+    x, it = O.cg(rowptr, col, val, np.array(ka["b"], dtype=np.float64), ka["crit_norm_inf_delta"],
+                 crit_kind=0, precond=0, fac=fac)
+    assert it > 0
+    assert np.all(err_unit_test(x, np.array(ka["x"])) < 1e-12)
+
+
+def test_oracle_patch_test_and_rigid_modes():
+    """Element consistency: rigid-body modes are in the kernel of K_e and a linear field gives
+    zero interior forces (patch test) on a distorted mesh."""
+    pos, conn = O.make_rect_hexa(4)
+    rng = np.random.default_rng(0)
+    interior = np.all((pos > 1e-9) & (pos < 1 - 1e-9), axis=1)
+    pos = pos + interior[:, None] * rng.uniform(-0.05, 0.05, pos.shape)
+    Ke = O.hexa8_ke(pos[conn[0]], 210000.0, 0.3)
+    assert np.abs(Ke - Ke.T).max() <= 1e-12 * np.abs(Ke).max()
+    xyz = pos[conn[0]]
+    modes = [np.tile(e, 8) for e in np.eye(3)]
+    for ax in range(3):
+        w = np.zeros(3)
+        w[ax] = 1.0
+        modes.append(np.cross(w, xyz).ravel())
+    for m in modes:
+        assert np.abs(Ke @ m).max() <= 1e-9 * np.abs(Ke).max() * np.abs(m).max()
+    rowptr, col = O.pattern_lower(pos.shape[0], 3, conn)
+    val = O.assemble_elast(pos, conn, 210000.0, 0.3, rowptr, col)
+    G = np.array([[1e-3, 2e-3, -1e-3], [0.5e-3, -2e-3, 1e-3], [3e-3, 1e-3, 2e-3]])
+    u = (pos @ G.T).ravel()
+    f = O.spmv(rowptr, col, val, u).reshape(-1, 3)
+    assert np.abs(f[interior]).max() <= 1e-9 * np.abs(f).max()
+
+
+def test_oracle_constraint_penalty_semantics():
+    """assemble_constraints: K(j,j) += c^2 max|diag| p and F(j) += c max|diag| p res."""
+    A = np.array([[4.0, 1.0], [1.0, 3.0]])
+    rowptr, col, val = O.dense_to_lower_csr(A)
+    F = np.array([1.0, 2.0])
+    md = O.penalty(rowptr, col, val, F, [1], [2.0], [0.5], 10.0)
+    assert md == 4.0
+    assert val[-1] == 3.0 + 2.0 * 2.0 * 4.0 * 10.0
+    assert F[1] == 2.0 + 2.0 * 4.0 * 10.0 * 0.5
