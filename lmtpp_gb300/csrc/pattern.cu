@@ -225,6 +225,8 @@ __global__ void k_gather(const uint32_t *conn, int npe, int npairs, const uint32
             for (int b = 0; b < npe; ++b) {
                 uint32_t j = conn[e * npe + b];
                 int slot = find_in_row(bcol, rb, re, j);
+                if (slot >= deg || bcol[rb + slot] != j) continue;  // cannot happen for a
+                                                                     // consistent pattern
                 if (kFill) {
                     int lo = a < b ? a : b, hi = a < b ? b : a;
                     gsrc[cur[slot]++] =
