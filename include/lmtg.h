@@ -152,6 +152,20 @@ int lmtg_get_launch_count(lmtg_ctx *ctx, uint64_t *count);
 int lmtg_profile_pcg_kernels(lmtg_ctx *ctx, int precision, int iters, double *spmv_ms,
                              double *update_ms);
 
+/* Allocation-free residual: r = b - K x and *rr_host = |r|_2^2 (FP64) for a 3x3-block
+ * matrix the caller already holds on the device (bptr[nn+1], bcol[nnz_blocks] as u32,
+ * K[9*nnz_blocks] row-major blocks, full symmetric pattern; x, b, r of 3*nn doubles), issued
+ * on `stream` (NULL = default stream).  It has no counterpart in the reference: it is for
+ * callers that cannot call cudaMalloc (device memory owned by their own arena, no allocation
+ * allowed between steps).  It allocates nothing: its reduction scratch is a fixed 512 KiB
+ * device array, so nn is limited to 524,288 node rows (LMTG_ERR_ARG beyond).  The first call
+ * on each device looks up that array's address (make it before any stream capture).  All
+ * calls share the array: calls that overlap on the GPU race.  rr_host may be NULL (then the
+ * call does not synchronize the stream). */
+int lmtg_residual_norm_noalloc(void *stream, uint64_t nn, const uint32_t *bptr,
+                               const uint32_t *bcol, const double *K, const double *x,
+                               const double *b, double *r, double *rr_host);
+
 /* Sizes of the current problem. */
 int lmtg_get_sizes(lmtg_ctx *ctx, uint64_t *nn, uint64_t *ne, uint64_t *ndof, uint64_t *nnz_blocks);
 

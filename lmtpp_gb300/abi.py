@@ -58,6 +58,7 @@ _SIGS = {
     "lmtg_get_sizes": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "lmtg_get_launch_count": (_i, [_vp, ctypes.POINTER(_u64)]),
     "lmtg_get_stream": (_i, [_vp, ctypes.POINTER(_vp)]),
+    "lmtg_residual_norm_noalloc": (_i, [_vp, _u64, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.POINTER(_d)]),
     "lmtg_profile_pcg_kernels": (_i, [_vp, _i, _i, ctypes.POINTER(_d), ctypes.POINTER(_d)]),
 }
 
