@@ -45,6 +45,10 @@ def parse():
     p.add_argument("--cpu-side", type=int, default=24, help="elements per side of the CPU sample")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
+    p.add_argument("--mode", default="bench", choices=["bench", "profile", "solve"],
+                   help="profile: time the PCG kernels once on --side (small ncu case); "
+                        "solve: one assemble + mixed solve at --tol (launch-list case)")
+    p.add_argument("--tol", type=float, default=1e-10)
     return p.parse_args()
 
 
@@ -323,8 +327,27 @@ def workload_config(args):
             "parallelism": "replicas"}
 
 
+def run_small(args):
+    """Single-purpose runs with few launches, for ncu captures."""
+    from lmtpp_gb300 import make_rect_hexa
+    pos, conn = make_rect_hexa(args.side + 1)
+    f = new_problem(pos, conn, lognormal_E(conn.shape[0]), 0)
+    out = {"mode": args.mode, "side": args.side}
+    if args.mode == "profile":
+        f.assemble(True, True, mixed=True)
+        out["spmv32_ms"], out["upd32_ms"] = f.profile_pcg_kernels(precision=1, iters=5)
+        out["spmv64_ms"], out["upd64_ms"] = f.profile_pcg_kernels(precision=0, iters=3)
+    else:
+        out["stats"] = one_solve(f, "mixed", args.tol)
+    out["launches"] = f.launch_count()
+    f.close()
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
+    if args.mode != "bench":
+        return run_small(args)
     rank, world, local, barrier, allmax = dist_setup(args.gpus)
     if args.impl == "reference":
         if rank != 0:

@@ -100,18 +100,74 @@ __device__ __forceinline__ void bsr3_row(const uint32_t *__restrict__ bcol, cons
     a2 = warp_sum(a2);
 }
 
+// Row product of node row I, one 3x3 block per lane.  The warp first loads up to 32 blocks of
+// the row (9 values each) with coalesced loads into a per-warp shared buffer while every lane
+// fetches its block's column index and the 3 x values it needs -- all loads independent, so a
+// warp keeps ~12 requests in flight.  Lane b then multiplies block b (stride-9 shared reads are
+// bank-conflict free) and the three row sums are combined with a reduce-scatter (6 shuffles
+// instead of 3 x 5).  Returns in every lane the total of output component (lane >> 3) & 3
+// (lanes 0, 8, 16 hold rows 3I, 3I+1, 3I+2).
+template <class T, class XF>
+__device__ __forceinline__ T bsr3_row_lanes(const uint32_t *__restrict__ bcol,
+                                            const T *__restrict__ K, uint32_t rb, uint32_t re,
+                                            int lane, T *buf, XF xf) {
+    T a0 = (T)0, a1 = (T)0, a2 = (T)0;
+    for (uint32_t cb = rb; cb < re; cb += 32) {
+        const uint32_t nb = min(32u, re - cb);
+        const uint32_t nv = nb * 9;
+        const T *src = K + (uint64_t)cb * 9;
+        T v[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            const uint32_t i = lane + 32 * k;
+            v[k] = i < nv ? __ldg(src + i) : (T)0;
+        }
+        T x0 = (T)0, x1 = (T)0, x2 = (T)0;
+        if ((uint32_t)lane < nb) {
+            const uint64_t j = 3 * (uint64_t)__ldg(bcol + cb + lane);
+            x0 = xf(j);
+            x1 = xf(j + 1);
+            x2 = xf(j + 2);
+        }
+        __syncwarp();
+#pragma unroll
+        for (int k = 0; k < 9; ++k) buf[lane + 32 * k] = v[k];
+        __syncwarp();
+        if ((uint32_t)lane < nb) {
+            const T *m = buf + 9 * lane;
+            a0 = fma(m[0], x0, a0); a0 = fma(m[1], x1, a0); a0 = fma(m[2], x2, a0);
+            a1 = fma(m[3], x0, a1); a1 = fma(m[4], x1, a1); a1 = fma(m[5], x2, a1);
+            a2 = fma(m[6], x0, a2); a2 = fma(m[7], x1, a2); a2 = fma(m[8], x2, a2);
+        }
+    }
+    // reduce-scatter of (a0, a1, a2, 0) over the warp
+    const bool hi16 = (lane & 16) != 0, hi8 = (lane & 8) != 0;
+    const T s0 = hi16 ? a0 : a2, s1 = hi16 ? a1 : (T)0;
+    const T k0 = hi16 ? a2 : a0, k1 = hi16 ? (T)0 : a1;
+    const T b0 = k0 + __shfl_xor_sync(0xffffffffu, s0, 16);
+    const T b1 = k1 + __shfl_xor_sync(0xffffffffu, s1, 16);
+    T c = (hi8 ? b1 : b0) + __shfl_xor_sync(0xffffffffu, hi8 ? b0 : b1, 8);
+    c += __shfl_xor_sync(0xffffffffu, c, 4);
+    c += __shfl_xor_sync(0xffffffffu, c, 2);
+    c += __shfl_xor_sync(0xffffffffu, c, 1);
+    return c;
+}
+
+constexpr int kRowBuf = 288;  // per-warp shared buffer: 32 blocks x 9 values
+
 // y = K x
 template <class T>
 __global__ void __launch_bounds__(kRowThreads)
     k_spmv(const uint32_t *__restrict__ bptr, const uint32_t *__restrict__ bcol,
            const T *__restrict__ K, const T *__restrict__ x, T *__restrict__ y, uint64_t nn) {
+    __shared__ T sbuf[kRowThreads / 32][kRowBuf];
     const int lane = threadIdx.x & 31;
+    T *buf = sbuf[threadIdx.x >> 5];
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     for (uint64_t I = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; I < nn; I += nw) {
-        T a0, a1, a2;
-        bsr3_row(bcol, K, bptr[I], bptr[I + 1], lane, [&](uint64_t j) { return __ldg(x + j); }, a0,
-                 a1, a2);
-        if (lane < 3) y[3 * I + lane] = lane == 0 ? a0 : (lane == 1 ? a1 : a2);
+        const T v = bsr3_row_lanes(bcol, K, bptr[I], bptr[I + 1], lane, buf,
+                                   [&](uint64_t j) { return __ldg(x + j); });
+        if ((lane & 7) == 0 && lane < 24) y[3 * I + (lane >> 3)] = v;
     }
 }
 
@@ -122,16 +178,17 @@ __global__ void __launch_bounds__(kRowThreads)
                const T *__restrict__ K, const T *__restrict__ x, const T *__restrict__ b,
                T *__restrict__ r, uint64_t nn, double *partials, unsigned *ticket,
                double *rr_out) {
+    __shared__ T sbuf[kRowThreads / 32][kRowBuf];
     const int lane = threadIdx.x & 31;
+    T *buf = sbuf[threadIdx.x >> 5];
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     double v[1] = {0.0};
     for (uint64_t I = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; I < nn; I += nw) {
-        T a0, a1, a2;
-        bsr3_row(bcol, K, bptr[I], bptr[I + 1], lane, [&](uint64_t j) { return __ldg(x + j); }, a0,
-                 a1, a2);
-        if (lane < 3) {
-            const uint64_t i = 3 * I + lane;
-            const T ri = b[i] - (lane == 0 ? a0 : (lane == 1 ? a1 : a2));
+        const T a = bsr3_row_lanes(bcol, K, bptr[I], bptr[I + 1], lane, buf,
+                                   [&](uint64_t j) { return __ldg(x + j); });
+        if ((lane & 7) == 0 && lane < 24) {
+            const uint64_t i = 3 * I + (lane >> 3);
+            const T ri = b[i] - a;
             r[i] = ri;
             v[0] += (double)ri * (double)ri;
         }
@@ -192,18 +249,18 @@ __global__ void __launch_bounds__(kRowThreads)
                T *__restrict__ pnew, T *__restrict__ q, uint64_t nn, PcgScalars *S,
                double *partials) {
     if (*(volatile int *)&S->done) return;
+    __shared__ T sbuf[kRowThreads / 32][kRowBuf];
     const T beta = (T)S->beta;
     const int lane = threadIdx.x & 31;
+    T *buf = sbuf[threadIdx.x >> 5];
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     double v[1] = {0.0};
     for (uint64_t I = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; I < nn; I += nw) {
-        T a0, a1, a2;
-        bsr3_row(bcol, K, bptr[I], bptr[I + 1], lane,
-                 [&](uint64_t j) { return __ldg(z + j) + beta * __ldg(pold + j); }, a0, a1, a2);
-        if (lane < 3) {
-            const uint64_t i = 3 * I + lane;
-            const T pn = z[i] + beta * pold[i];
-            const T qi = lane == 0 ? a0 : (lane == 1 ? a1 : a2);
+        const T qi = bsr3_row_lanes(bcol, K, bptr[I], bptr[I + 1], lane, buf,
+                                    [&](uint64_t j) { return fma(beta, __ldg(pold + j), __ldg(z + j)); });
+        if ((lane & 7) == 0 && lane < 24) {
+            const uint64_t i = 3 * I + (lane >> 3);
+            const T pn = fma(beta, pold[i], z[i]);
             pnew[i] = pn;
             q[i] = qi;
             v[0] += (double)pn * (double)qi;
