@@ -229,7 +229,7 @@ int lmtg_allocate_matrices(lmtg_ctx *c, uint64_t *nnz_lower) {
         c->Dinv64.alloc(c->nn * 9);
         c->Dinv32.alloc(c->nn * 9);
         for (auto &w : c->w64) w.alloc(c->n);
-        for (auto &w : c->w32) w.alloc(c->n);
+        for (auto &w : c->w32) w.alloc(4 * c->nn);  // room for 16-byte padded node vectors
         LMTG_CUDA(cudaMemsetAsync(c->u.p, 0, c->u.bytes(), c->stream));
         LMTG_CUDA(cudaMemsetAsync(c->F.p, 0, c->F.bytes(), c->stream));
         LMTG_CUDA(cudaStreamSynchronize(c->stream));

@@ -14,6 +14,10 @@ namespace lmtg {
 
 constexpr int kChunkPairs = 16;  // iterations per graph launch = 2 * kChunkPairs
 
+// node stride of the gathered PCG vectors: padded 16-byte nodes in FP32, packed in FP64
+template <class T> struct GatherStride { static constexpr int value = 3; };
+template <> struct GatherStride<float> { static constexpr int value = 4; };
+
 __global__ void k_scale_to32(const double *__restrict__ a, double s_inv, float *__restrict__ o,
                              uint64_t n) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
@@ -111,9 +115,11 @@ static int run_pcg(lmtg_ctx *c, const T *K, const T *Dinv, const T *b, T *x, T *
                                                           c->partials.p, &o->cnt_c, &o->rr);
         c->launches += 1;
     }
-    k_pcg_start<T><<<node_grid(c), kRowThreads, 0, s>>>(r, b_norm2 >= 0 ? nullptr : b, Dinv, z,
-                                                         c->nn, c->scal.p, c->partials.p);
-    LMTG_CUDA(cudaMemsetAsync(p0, 0, sizeof(T) * c->n, s));
+    constexpr int VS = GatherStride<T>::value;
+    k_pcg_start<T, VS><<<node_grid(c), kRowThreads, 0, s>>>(r, b_norm2 >= 0 ? nullptr : b, Dinv, z,
+                                                             c->nn, c->scal.p, c->partials.p);
+    LMTG_CUDA(cudaMemsetAsync(p0, 0, sizeof(T) * VS * c->nn, s));
+    LMTG_CUDA(cudaMemsetAsync(p1, 0, sizeof(T) * VS * c->nn, s));
     LMTG_CUDA(cudaGetLastError());
     c->launches += 1;
 
@@ -122,14 +128,14 @@ static int run_pcg(lmtg_ctx *c, const T *K, const T *Dinv, const T *b, T *x, T *
     cudaGraphExec_t exec = nullptr;
     LMTG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < kChunkPairs; ++k) {
-        k_pcg_spmv<T><<<row_grid(c), kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, K, z, p0, p1, q, c->nn,
-                                                          c->scal.p, c->partials.p);
-        k_pcg_update<T><<<node_grid(c), kRowThreads, 0, s>>>(x, r, z, p1, q, Dinv, c->nn, c->scal.p,
-                                                             c->partials.p);
-        k_pcg_spmv<T><<<row_grid(c), kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, K, z, p1, p0, q, c->nn,
-                                                          c->scal.p, c->partials.p);
-        k_pcg_update<T><<<node_grid(c), kRowThreads, 0, s>>>(x, r, z, p0, q, Dinv, c->nn, c->scal.p,
-                                                             c->partials.p);
+        k_pcg_spmv<T, VS><<<row_grid(c), kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, K, z, p0, p1, q,
+                                                              c->nn, c->scal.p, c->partials.p);
+        k_pcg_update<T, VS><<<node_grid(c), kRowThreads, 0, s>>>(x, r, z, p1, q, Dinv, c->nn,
+                                                                 c->scal.p, c->partials.p);
+        k_pcg_spmv<T, VS><<<row_grid(c), kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, K, z, p1, p0, q,
+                                                              c->nn, c->scal.p, c->partials.p);
+        k_pcg_update<T, VS><<<node_grid(c), kRowThreads, 0, s>>>(x, r, z, p0, q, Dinv, c->nn,
+                                                                 c->scal.p, c->partials.p);
     }
     cudaError_t ce = cudaStreamEndCapture(s, &graph);
     if (ce != cudaSuccess) throw Error{LMTG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce)};
@@ -253,19 +259,21 @@ static void profile_pcg_t(lmtg_ctx *c, const T *K, const T *Dinv, const T *b, T 
     LMTG_CUDA(cudaMemcpyAsync(c->scal.p, &init, sizeof(init), cudaMemcpyHostToDevice, s));
     LMTG_CUDA(cudaMemsetAsync(x, 0, sizeof(T) * c->n, s));
     LMTG_CUDA(cudaMemcpyAsync(r, b, sizeof(T) * c->n, cudaMemcpyDeviceToDevice, s));
-    k_pcg_start<T><<<node_grid(c), kRowThreads, 0, s>>>(r, b, Dinv, z, c->nn, c->scal.p,
-                                                         c->partials.p);
-    LMTG_CUDA(cudaMemsetAsync(p0, 0, sizeof(T) * c->n, s));
+    constexpr int VS = GatherStride<T>::value;
+    k_pcg_start<T, VS><<<node_grid(c), kRowThreads, 0, s>>>(r, b, Dinv, z, c->nn, c->scal.p,
+                                                             c->partials.p);
+    LMTG_CUDA(cudaMemsetAsync(p0, 0, sizeof(T) * VS * c->nn, s));
+    LMTG_CUDA(cudaMemsetAsync(p1, 0, sizeof(T) * VS * c->nn, s));
     c->launches += 1;
     std::vector<cudaEvent_t> ev(2 * iters + 1);
     for (auto &e : ev) LMTG_CUDA(cudaEventCreate(&e));
     LMTG_CUDA(cudaEventRecord(ev[0], s));
     for (int k = 0; k < iters; ++k) {
         T *po = (k & 1) ? p1 : p0, *pn = (k & 1) ? p0 : p1;
-        k_pcg_spmv<T><<<row_grid(c), kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, K, z, po, pn, q, c->nn,
-                                                          c->scal.p, c->partials.p);
+        k_pcg_spmv<T, VS><<<row_grid(c), kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, K, z, po, pn, q,
+                                                              c->nn, c->scal.p, c->partials.p);
         LMTG_CUDA(cudaEventRecord(ev[2 * k + 1], s));
-        k_pcg_update<T><<<node_grid(c), kRowThreads, 0, s>>>(x, r, z, pn, q, Dinv, c->nn, c->scal.p,
+        k_pcg_update<T, VS><<<node_grid(c), kRowThreads, 0, s>>>(x, r, z, pn, q, Dinv, c->nn, c->scal.p,
                                                              c->partials.p);
         LMTG_CUDA(cudaEventRecord(ev[2 * k + 2], s));
     }

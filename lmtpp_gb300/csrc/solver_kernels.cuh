@@ -155,6 +155,75 @@ __device__ __forceinline__ T bsr3_row_lanes(const uint32_t *__restrict__ bcol,
 
 constexpr int kRowBuf = 288;  // per-warp shared buffer: 32 blocks x 9 values
 
+// Node vectors gathered by the SpMV (z, p) are stored with a stride VS per node: 3 (packed) or
+// 4 (FP32, padded so that a node's three components are one aligned 16-byte load).
+template <class T, int VS>
+struct NodeVec {
+    static __device__ __forceinline__ void load(const T *__restrict__ v, uint64_t J, T &a, T &b, T &c) {
+        a = __ldg(v + VS * J);
+        b = __ldg(v + VS * J + 1);
+        c = __ldg(v + VS * J + 2);
+    }
+};
+template <>
+struct NodeVec<float, 4> {
+    static __device__ __forceinline__ void load(const float *__restrict__ v, uint64_t J, float &a,
+                                                float &b, float &c) {
+        const float4 q = __ldg(reinterpret_cast<const float4 *>(v) + J);
+        a = q.x;
+        b = q.y;
+        c = q.z;
+    }
+};
+
+// Pieces of bsr3_row_lanes for rows of at most 32 blocks, so that a warp can issue the loads of
+// two rows before it consumes either (twice the requests in flight).
+template <class T, class XF>
+__device__ __forceinline__ void bsr3_load32(const uint32_t *__restrict__ bcol,
+                                            const T *__restrict__ K, uint32_t rb, uint32_t nb,
+                                            int lane, XF xf, T (&v)[9], T &x0, T &x1, T &x2) {
+    const uint32_t nv = nb * 9;
+    const T *src = K + (uint64_t)rb * 9;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        const uint32_t i = lane + 32 * k;
+        v[k] = i < nv ? __ldg(src + i) : (T)0;
+    }
+    x0 = x1 = x2 = (T)0;
+    if ((uint32_t)lane < nb) {
+        const uint64_t j = 3 * (uint64_t)__ldg(bcol + rb + lane);
+        x0 = xf(j);
+        x1 = xf(j + 1);
+        x2 = xf(j + 2);
+    }
+}
+
+template <class T>
+__device__ __forceinline__ T bsr3_mul32(T *buf, const T (&v)[9], T x0, T x1, T x2, uint32_t nb,
+                                        int lane) {
+    T a0 = (T)0, a1 = (T)0, a2 = (T)0;
+    __syncwarp();
+#pragma unroll
+    for (int k = 0; k < 9; ++k) buf[lane + 32 * k] = v[k];
+    __syncwarp();
+    if ((uint32_t)lane < nb) {
+        const T *m = buf + 9 * lane;
+        a0 = fma(m[0], x0, a0); a0 = fma(m[1], x1, a0); a0 = fma(m[2], x2, a0);
+        a1 = fma(m[3], x0, a1); a1 = fma(m[4], x1, a1); a1 = fma(m[5], x2, a1);
+        a2 = fma(m[6], x0, a2); a2 = fma(m[7], x1, a2); a2 = fma(m[8], x2, a2);
+    }
+    const bool hi16 = (lane & 16) != 0, hi8 = (lane & 8) != 0;
+    const T s0 = hi16 ? a0 : a2, s1 = hi16 ? a1 : (T)0;
+    const T k0 = hi16 ? a2 : a0, k1 = hi16 ? (T)0 : a1;
+    const T b0 = k0 + __shfl_xor_sync(0xffffffffu, s0, 16);
+    const T b1 = k1 + __shfl_xor_sync(0xffffffffu, s1, 16);
+    T c = (hi8 ? b1 : b0) + __shfl_xor_sync(0xffffffffu, hi8 ? b0 : b1, 8);
+    c += __shfl_xor_sync(0xffffffffu, c, 4);
+    c += __shfl_xor_sync(0xffffffffu, c, 2);
+    c += __shfl_xor_sync(0xffffffffu, c, 1);
+    return c;
+}
+
 // y = K x
 template <class T>
 __global__ void __launch_bounds__(kRowThreads)
@@ -199,11 +268,11 @@ __global__ void __launch_bounds__(kRowThreads)
 
 // Start of a PCG run: z = P r, rz, rr, |r|_inf; optional bb = b.b.  Initial stopping test on
 // the residual criteria (the delta criteria need one step, conjugate_gradient.h:40-41).
-template <class T>
+template <class T, int VS>
 __global__ void k_pcg_start(const T *__restrict__ r, const T *__restrict__ b,
                             const T *__restrict__ Dinv, T *__restrict__ z, uint64_t nn,
                             PcgScalars *S, double *partials) {
-    double v[4] = {0.0, 0.0, 0.0, 0.0};  // rz, rr, bb, rinf
+    T t[4] = {(T)0, (T)0, (T)0, (T)0};  // rz, rr, bb, rinf per thread (T); grid sum in FP64
     for (uint64_t I = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; I < nn;
          I += (uint64_t)gridDim.x * blockDim.x) {
         const T *D = Dinv + 9 * I;
@@ -211,17 +280,18 @@ __global__ void k_pcg_start(const T *__restrict__ r, const T *__restrict__ b,
         const T z0 = D[0] * r0 + D[1] * r1 + D[2] * r2;
         const T z1 = D[3] * r0 + D[4] * r1 + D[5] * r2;
         const T z2 = D[6] * r0 + D[7] * r1 + D[8] * r2;
-        z[3 * I] = z0;
-        z[3 * I + 1] = z1;
-        z[3 * I + 2] = z2;
-        v[0] += (double)r0 * z0 + (double)r1 * z1 + (double)r2 * z2;
-        v[1] += (double)r0 * r0 + (double)r1 * r1 + (double)r2 * r2;
+        z[VS * I] = z0;
+        z[VS * I + 1] = z1;
+        z[VS * I + 2] = z2;
+        t[0] += r0 * z0 + r1 * z1 + r2 * z2;
+        t[1] += r0 * r0 + r1 * r1 + r2 * r2;
         if (b) {
             const T b0 = b[3 * I], b1 = b[3 * I + 1], b2 = b[3 * I + 2];
-            v[2] += (double)b0 * b0 + (double)b1 * b1 + (double)b2 * b2;
+            t[2] += b0 * b0 + b1 * b1 + b2 * b2;
         }
-        v[3] = fmax(v[3], fmax(fabs((double)r0), fmax(fabs((double)r1), fabs((double)r2))));
+        t[3] = fmax(t[3], fmax(fabs(r0), fmax(fabs(r1), fabs(r2))));
     }
+    double v[4] = {(double)t[0], (double)t[1], (double)t[2], (double)t[3]};
     double out[4];
     if (grid_reduce<4, 8u>(v, partials, &S->cnt_c, out) && threadIdx.x == 0) {
         S->rz = out[0];
@@ -241,8 +311,8 @@ __global__ void k_pcg_start(const T *__restrict__ r, const T *__restrict__ b,
     }
 }
 
-// Kernel A: p_new = z + beta p_old; q = K p_new; pq = p_new . q
-template <class T>
+// Kernel A: p_new = z + beta p_old; q = K p_new; pq = p_new . q  (z, p with node stride VS)
+template <class T, int VS>
 __global__ void __launch_bounds__(kRowThreads)
     k_pcg_spmv(const uint32_t *__restrict__ bptr, const uint32_t *__restrict__ bcol,
                const T *__restrict__ K, const T *__restrict__ z, const T *__restrict__ pold,
@@ -254,24 +324,73 @@ __global__ void __launch_bounds__(kRowThreads)
     const int lane = threadIdx.x & 31;
     T *buf = sbuf[threadIdx.x >> 5];
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    double v[1] = {0.0};
-    for (uint64_t I = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; I < nn; I += nw) {
-        const T qi = bsr3_row_lanes(bcol, K, bptr[I], bptr[I + 1], lane, buf,
-                                    [&](uint64_t j) { return fma(beta, __ldg(pold + j), __ldg(z + j)); });
+    // x value of column DOF j = 3J + c (generic path) and of a whole node J (fast path)
+    auto xf = [&](uint64_t j) {
+        const uint64_t J = j / 3, cc = j - 3 * J;
+        return fma(beta, __ldg(pold + VS * J + cc), __ldg(z + VS * J + cc));
+    };
+    auto xnode = [&](uint64_t J, T &a, T &b, T &c) {
+        T za, zb, zc, pa, pb, pc;
+        NodeVec<T, VS>::load(z, J, za, zb, zc);
+        NodeVec<T, VS>::load(pold, J, pa, pb, pc);
+        a = fma(beta, pa, za);
+        b = fma(beta, pb, zb);
+        c = fma(beta, pc, zc);
+    };
+    T acc = (T)0;  // per-thread partial of p.q in T; the grid reduction is FP64
+    auto finish = [&](uint64_t I, T qi) {
         if ((lane & 7) == 0 && lane < 24) {
-            const uint64_t i = 3 * I + (lane >> 3);
-            const T pn = fma(beta, pold[i], z[i]);
-            pnew[i] = pn;
-            q[i] = qi;
-            v[0] += (double)pn * (double)qi;
+            const uint64_t iv = VS * I + (lane >> 3);
+            const T pn = fma(beta, pold[iv], z[iv]);
+            pnew[iv] = pn;
+            q[3 * I + (lane >> 3)] = qi;
+            acc = fma(pn, qi, acc);
+        }
+    };
+    // Each block owns a contiguous range of rows (neighbouring rows gather mostly the same
+    // x entries, so the range's gathers hit L1); each warp takes two adjacent rows per step.
+    (void)nw;
+    const uint64_t per_block = (nn + gridDim.x - 1) / gridDim.x;
+    const uint64_t row0 = blockIdx.x * per_block;
+    const uint64_t row_end = min(nn, row0 + per_block);
+    const uint64_t wid = threadIdx.x >> 5, nwb = blockDim.x >> 5;
+    for (uint64_t I = row0 + 2 * wid; I < row_end; I += 2 * nwb) {
+        const uint64_t I1 = I + 1;
+        const uint32_t rb0 = bptr[I], re0 = bptr[I + 1];
+        const uint32_t rb1 = I1 < row_end ? bptr[I1] : 0u, re1 = I1 < row_end ? bptr[I1 + 1] : 0u;
+        if (re0 - rb0 <= 32 && re1 - rb1 <= 32) {
+            // issue order: both rows' matrix values and column indices first (independent),
+            // then the dependent x gathers, then the products
+            const uint32_t nb0 = re0 - rb0, nb1 = re1 - rb1;
+            T v0[9], v1[9];
+            const T *s0 = K + (uint64_t)rb0 * 9, *s1 = K + (uint64_t)rb1 * 9;
+#pragma unroll
+            for (int k = 0; k < 9; ++k) {
+                const uint32_t i = lane + 32 * k;
+                v0[k] = i < nb0 * 9 ? __ldg(s0 + i) : (T)0;
+                v1[k] = i < nb1 * 9 ? __ldg(s1 + i) : (T)0;
+            }
+            const uint32_t j0 = (uint32_t)lane < nb0 ? __ldg(bcol + rb0 + lane) : 0u;
+            const uint32_t j1 = (uint32_t)lane < nb1 ? __ldg(bcol + rb1 + lane) : 0u;
+            T x00 = 0, x01 = 0, x02 = 0, x10 = 0, x11 = 0, x12 = 0;
+            if ((uint32_t)lane < nb0) xnode(j0, x00, x01, x02);
+            if ((uint32_t)lane < nb1) xnode(j1, x10, x11, x12);
+            const T q0 = bsr3_mul32(buf, v0, x00, x01, x02, re0 - rb0, lane);
+            const T q1 = bsr3_mul32(buf, v1, x10, x11, x12, re1 - rb1, lane);
+            finish(I, q0);
+            if (I1 < row_end) finish(I1, q1);
+        } else {
+            finish(I, bsr3_row_lanes(bcol, K, rb0, re0, lane, buf, xf));
+            if (I1 < row_end) finish(I1, bsr3_row_lanes(bcol, K, rb1, re1, lane, buf, xf));
         }
     }
+    double v[1] = {(double)acc};
     double out[1];
     if (grid_reduce<1, 0u>(v, partials, &S->cnt_a, out) && threadIdx.x == 0) S->pq = out[0];
 }
 
 // Kernel B: alpha, updates, preconditioner, dots, beta and the stopping test.
-template <class T>
+template <class T, int VS>
 __global__ void k_pcg_update(T *__restrict__ x, T *__restrict__ r, T *__restrict__ z,
                              const T *__restrict__ p, const T *__restrict__ q,
                              const T *__restrict__ Dinv, uint64_t nn, PcgScalars *S,
@@ -279,31 +398,32 @@ __global__ void k_pcg_update(T *__restrict__ x, T *__restrict__ r, T *__restrict
     if (*(volatile int *)&S->done) return;
     const double pq = S->pq;
     const T alpha = (T)(S->rz / (pq + (pq == 0.0 ? 1.0 : 0.0)));
-    double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};  // rz, rr, dx2, dxinf, rinf
+    T t[5] = {(T)0, (T)0, (T)0, (T)0, (T)0};  // rz, rr, dx2, dxinf, rinf per thread (T)
     for (uint64_t I = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; I < nn;
          I += (uint64_t)gridDim.x * blockDim.x) {
         T rv[3];
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             const uint64_t i = 3 * I + c;
-            const T dx = alpha * p[i];
+            const T dx = alpha * p[VS * I + c];
             x[i] += dx;
-            rv[c] = r[i] - alpha * q[i];
+            rv[c] = fma(-alpha, q[i], r[i]);
             r[i] = rv[c];
-            v[2] += (double)dx * dx;
-            v[3] = fmax(v[3], fabs((double)dx));
-            v[4] = fmax(v[4], fabs((double)rv[c]));
+            t[2] = fma(dx, dx, t[2]);
+            t[3] = fmax(t[3], fabs(dx));
+            t[4] = fmax(t[4], fabs(rv[c]));
         }
         const T *D = Dinv + 9 * I;
         const T z0 = D[0] * rv[0] + D[1] * rv[1] + D[2] * rv[2];
         const T z1 = D[3] * rv[0] + D[4] * rv[1] + D[5] * rv[2];
         const T z2 = D[6] * rv[0] + D[7] * rv[1] + D[8] * rv[2];
-        z[3 * I] = z0;
-        z[3 * I + 1] = z1;
-        z[3 * I + 2] = z2;
-        v[0] += (double)rv[0] * z0 + (double)rv[1] * z1 + (double)rv[2] * z2;
-        v[1] += (double)rv[0] * rv[0] + (double)rv[1] * rv[1] + (double)rv[2] * rv[2];
+        z[VS * I] = z0;
+        z[VS * I + 1] = z1;
+        z[VS * I + 2] = z2;
+        t[0] += rv[0] * z0 + rv[1] * z1 + rv[2] * z2;
+        t[1] += rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
     }
+    double v[5] = {(double)t[0], (double)t[1], (double)t[2], (double)t[3], (double)t[4]};
     double out[5];
     if (grid_reduce<5, (8u | 16u)>(v, partials, &S->cnt_b, out) && threadIdx.x == 0) {
         const double rz_old = S->rz;
