@@ -95,11 +95,13 @@ struct PcgBufs {
 
 // One PCG run on K x = b from the current x.  b_norm2 >= 0 gives |b|^2 for the relative test
 // (otherwise b.b is computed).  Returns the status; *iters receives the iteration count.
+// beta_den > 0 continues from the search direction held in p0 (reliable update); otherwise the
+// run starts fresh (p = z).
 template <class T>
 static int run_pcg(lmtg_ctx *c, const T *K, const T *Dinv, const T *b, T *x, T *r, T *z, T *p0,
                    T *p1, T *q, bool x_is_zero, int crit_kind, double crit, int maxit,
                    double b_norm2, std::chrono::steady_clock::time_point deadline, bool use_deadline,
-                   int *iters) {
+                   int *iters, double beta_den = 0.0) {
     cudaStream_t s = c->stream;
     PcgScalars init{};
     init.crit = crit;
@@ -117,9 +119,12 @@ static int run_pcg(lmtg_ctx *c, const T *K, const T *Dinv, const T *b, T *x, T *
     }
     constexpr int VS = GatherStride<T>::value;
     k_pcg_start<T, VS><<<node_grid(c), kRowThreads, 0, s>>>(r, b_norm2 >= 0 ? nullptr : b, Dinv, z,
-                                                             c->nn, c->scal.p, c->partials.p);
-    LMTG_CUDA(cudaMemsetAsync(p0, 0, sizeof(T) * VS * c->nn, s));
-    LMTG_CUDA(cudaMemsetAsync(p1, 0, sizeof(T) * VS * c->nn, s));
+                                                             c->nn, c->scal.p, c->partials.p,
+                                                             beta_den);
+    if (beta_den <= 0.0) {
+        LMTG_CUDA(cudaMemsetAsync(p0, 0, sizeof(T) * VS * c->nn, s));
+        LMTG_CUDA(cudaMemsetAsync(p1, 0, sizeof(T) * VS * c->nn, s));
+    }
     LMTG_CUDA(cudaGetLastError());
     c->launches += 1;
 
@@ -193,19 +198,27 @@ int solve_pcg64(lmtg_ctx *c, int crit_kind, double tol, int maxit, double timeou
     return status;
 }
 
+// FP32-inner / FP64-refined solve with reliable updates (residual replacement).
+// The FP32 PCG runs in segments on the scaled system K32 d = r / s.  A segment ends when its
+// recursive residual has dropped by kDelta; then u += s d in FP64, the true residual
+// r = F - K64 u is recomputed in FP64 and becomes the new FP32 residual (rescaled), and the
+// search direction is kept (beta folded with the rescaling), so the Krylov recurrence is not
+// restarted.  A segment that fails to reduce the true residual restarts from p = z (a classic
+// iterative-refinement step).  Convergence is judged on the FP64 true residual only.
 int solve_mixed(lmtg_ctx *c, double tol, int maxit, double timeout_s, lmtg_solve_stats *st) {
     auto deadline = std::chrono::steady_clock::now() +
                     std::chrono::duration_cast<std::chrono::steady_clock::duration>(
                         std::chrono::duration<double>(timeout_s > 0 ? timeout_s : 0));
     double *r64 = c->w64[0].p;
     float *b32 = c->w32[0].p, *d32 = c->w32[1].p, *r32 = c->w32[2].p, *z32 = c->w32[3].p,
-          *p0 = c->w32[4].p, *p1 = c->w32[5].p;
+          *pa = c->w32[4].p, *pb = c->w32[5].p;
     float *q32 = reinterpret_cast<float *>(c->w64[1].p);  // FP64 buffer reused as FP32 q
     const double bb = dot64(c, c->F.p, c->F.p);
-    const double eta_min = 1e-5;  // inner relative reduction floor (FP32 accuracy bound)
+    constexpr double kDelta = 0.1;  // recursive-residual reduction per segment
     int total = 0, outer = 0, status = LMTG_OK;
-    double rel = 0;
-    const int max_outer = 60;
+    double rel = 0, s_prev = 0, rz_prev = 0, rel_prev = 0;
+    bool have_dir = false;
+    const int max_outer = 400;
     for (;;) {
         const double rr = residual<double>(c, c->K64.p, c->u.p, c->F.p, r64);
         rel = bb > 0 ? std::sqrt(rr / bb) : std::sqrt(rr);
@@ -222,22 +235,35 @@ int solve_mixed(lmtg_ctx *c, double tol, int maxit, double timeout_s, lmtg_solve
             status = LMTG_ERR_TIMEOUT;
             break;
         }
+        // a segment that did not reduce the true residual by 2x restarts the direction
+        if (have_dir && rel > 0.5 * rel_prev) have_dir = false;
         const double sc = std::sqrt(rr);
         k_scale_to32<<<node_grid(c), kRowThreads, 0, c->stream>>>(r64, 1.0 / sc, b32, c->n);
         c->launches += 1;
         LMTG_CUDA(cudaMemsetAsync(d32, 0, sizeof(float) * c->n, c->stream));
+        const double f = have_dir ? s_prev / sc : 0.0;
+        const double beta_den = have_dir ? rz_prev * f : 0.0;
+        // stop the segment after a kDelta reduction, or at the final target if closer
         double eta = 0.5 * tol / rel;
-        if (eta < eta_min) eta = eta_min;
+        if (eta < kDelta) eta = kDelta;
         int it = 0;
-        int s2 = run_pcg<float>(c, c->K32.p, c->Dinv32.p, b32, d32, r32, z32, p0, p1, q32, true,
+        int s2 = run_pcg<float>(c, c->K32.p, c->Dinv32.p, b32, d32, r32, z32, pa, pb, q32, true,
                                 LMTG_CRIT_REL_RESIDUAL, eta, maxit - total, 1.0, deadline,
-                                timeout_s > 0, &it);
+                                timeout_s > 0, &it, beta_den);
         total += it;
         ++outer;
         if (s2 == LMTG_ERR_NAN || s2 == LMTG_ERR_TIMEOUT) {
             status = s2;
             break;
         }
+        // latest direction: iteration k writes p[(k+1) % 2]; keep it in pa for the next segment
+        if (it & 1) std::swap(pa, pb);
+        // the continued recurrence needs r.z from before the segment's last update:
+        // beta_k = rz_{k+1} / rz_k, so rz_k = rz / beta of the final scalars
+        rz_prev = c->h_scal[0].beta != 0.0 ? c->h_scal[0].rz / c->h_scal[0].beta : 0.0;
+        s_prev = sc;
+        rel_prev = rel;
+        have_dir = it > 0 && rz_prev > 0.0;
         k_axpy_64_32<<<node_grid(c), kRowThreads, 0, c->stream>>>(c->u.p, sc, d32, c->n);
         LMTG_CUDA(cudaGetLastError());
         c->launches += 1;
@@ -261,7 +287,7 @@ static void profile_pcg_t(lmtg_ctx *c, const T *K, const T *Dinv, const T *b, T 
     LMTG_CUDA(cudaMemcpyAsync(r, b, sizeof(T) * c->n, cudaMemcpyDeviceToDevice, s));
     constexpr int VS = GatherStride<T>::value;
     k_pcg_start<T, VS><<<node_grid(c), kRowThreads, 0, s>>>(r, b, Dinv, z, c->nn, c->scal.p,
-                                                             c->partials.p);
+                                                             c->partials.p, 0.0);
     LMTG_CUDA(cudaMemsetAsync(p0, 0, sizeof(T) * VS * c->nn, s));
     LMTG_CUDA(cudaMemsetAsync(p1, 0, sizeof(T) * VS * c->nn, s));
     c->launches += 1;

@@ -271,7 +271,7 @@ __global__ void __launch_bounds__(kRowThreads)
 template <class T, int VS>
 __global__ void k_pcg_start(const T *__restrict__ r, const T *__restrict__ b,
                             const T *__restrict__ Dinv, T *__restrict__ z, uint64_t nn,
-                            PcgScalars *S, double *partials) {
+                            PcgScalars *S, double *partials, double beta_den) {
     T t[4] = {(T)0, (T)0, (T)0, (T)0};  // rz, rr, bb, rinf per thread (T); grid sum in FP64
     for (uint64_t I = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; I < nn;
          I += (uint64_t)gridDim.x * blockDim.x) {
@@ -297,7 +297,9 @@ __global__ void k_pcg_start(const T *__restrict__ r, const T *__restrict__ b,
         S->rz = out[0];
         S->rr = out[1];
         if (b) S->bb = out[2];
-        S->beta = 0.0;
+        // beta_den > 0 continues a previous run after a residual replacement: the search
+        // direction is kept and beta = rz_new / beta_den (the caller folds in the rescaling)
+        S->beta = beta_den > 0.0 ? out[0] / beta_den : 0.0;
         S->iter = 0;
         S->status = LMTG_OK;
         S->done = 0;
