@@ -314,6 +314,10 @@ def cpu_desc(s):
             % (s["side"], s["t_asm"], s["t_solve"], s["iters"], s["crit"], s["err"]))
 
 
+# dram__bytes_read.sum + dram__bytes_write.sum / algorithmic bytes of one k_pcg_spmv<float>
+# launch, ncu capture of the Hexa8 64^3 case (301.4 MB + 8.4 MB over 301.4 MB)
+SPMV32_TRAFFIC_RATIO = (301.365 + 8.372) / 301.365
+
 METRIC = "time-to-solution at 1e-10 rel. error vs FP64 oracle, mixed vs FP64 CG; asm GB/s"
 
 
@@ -393,7 +397,10 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64", "data": "synthetic",
         "config": workload_config(args),
         "roofline": {"bound": "hbm", "kernel": "k_pcg_spmv<float>", "achieved": ach, "peak": hbm,
-                     "unit": "GB/s", "frac": ach / hbm, "traffic": None,
+                     "unit": "GB/s", "frac": ach / hbm,
+                     "traffic": b32 * SPMV32_TRAFFIC_RATIO, "traffic_source": "ncu dram bytes of a "
+                     "64^3 capture scaled by the block count (traffic/algorithmic = %.3f)"
+                     % SPMV32_TRAFFIC_RATIO,
                      "peak_source": peak_note, "algorithmic_bytes": b32,
                      "launch_ms": r["spmv32_ms"]},
         "cpu_baseline": {"value": cpu_v, "unit": "s", "cores": 1, "kind": "port", "sample": cpu_desc(s)},

@@ -23,7 +23,7 @@ constexpr int kRowThreads = 256;  // SpMV / PCG block size (8 warps, one node ro
 // Block + grid reduction of NV doubles; max for bits set in kMaxMask, sum otherwise.
 // Returns true in the last block to arrive, where `out` holds the grid result (all threads).
 // Deterministic: partials are combined in a fixed order.
-template <int NV, unsigned kMaxMask>
+template <int NV, unsigned kMaxMask, bool kWarpDone = false>
 __device__ __forceinline__ bool grid_reduce(double (&v)[NV], double *partials, unsigned *ticket,
                                             double (&out)[NV]) {
     __shared__ double sh[NV][32];
@@ -31,7 +31,7 @@ __device__ __forceinline__ bool grid_reduce(double (&v)[NV], double *partials, u
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
     for (int i = 0; i < NV; ++i) {
-        v[i] = ((kMaxMask >> i) & 1u) ? warp_max(v[i]) : warp_sum(v[i]);
+        if (!kWarpDone) v[i] = ((kMaxMask >> i) & 1u) ? warp_max(v[i]) : warp_sum(v[i]);
         if (lane == 0) sh[i][wid] = v[i];
     }
     __syncthreads();
@@ -67,6 +67,21 @@ __device__ __forceinline__ bool grid_reduce(double (&v)[NV], double *partials, u
         out[i] = y;
     }
     return true;
+}
+
+// Grid reduction of per-thread partials held in T: the warp level runs in T (FP32 shuffles
+// and adds for the FP32 solver -- GB300's FP64 pipe is ~60x narrower), block and grid levels
+// in FP64.
+template <int NV, unsigned kMaxMask, class T>
+__device__ __forceinline__ bool grid_reduce_t(const T (&t)[NV], double *partials, unsigned *ticket,
+                                              double (&out)[NV]) {
+    double v[NV];
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+        const T w = ((kMaxMask >> i) & 1u) ? warp_max(t[i]) : warp_sum(t[i]);
+        v[i] = (double)w;
+    }
+    return grid_reduce<NV, kMaxMask, true>(v, partials, ticket, out);
 }
 
 // Row product of node row I: acc[r] = sum_blocks sum_c K_IJ[r][c] * X(3J+c), X from a functor.
@@ -291,9 +306,8 @@ __global__ void k_pcg_start(const T *__restrict__ r, const T *__restrict__ b,
         }
         t[3] = fmax(t[3], fmax(fabs(r0), fmax(fabs(r1), fabs(r2))));
     }
-    double v[4] = {(double)t[0], (double)t[1], (double)t[2], (double)t[3]};
     double out[4];
-    if (grid_reduce<4, 8u>(v, partials, &S->cnt_c, out) && threadIdx.x == 0) {
+    if (grid_reduce_t<4, 8u>(t, partials, &S->cnt_c, out) && threadIdx.x == 0) {
         S->rz = out[0];
         S->rr = out[1];
         if (b) S->bb = out[2];
@@ -386,9 +400,9 @@ __global__ void __launch_bounds__(kRowThreads)
             if (I1 < row_end) finish(I1, bsr3_row_lanes(bcol, K, rb1, re1, lane, buf, xf));
         }
     }
-    double v[1] = {(double)acc};
+    const T tacc[1] = {acc};
     double out[1];
-    if (grid_reduce<1, 0u>(v, partials, &S->cnt_a, out) && threadIdx.x == 0) S->pq = out[0];
+    if (grid_reduce_t<1, 0u>(tacc, partials, &S->cnt_a, out) && threadIdx.x == 0) S->pq = out[0];
 }
 
 // Kernel B: alpha, updates, preconditioner, dots, beta and the stopping test.
@@ -425,9 +439,8 @@ __global__ void k_pcg_update(T *__restrict__ x, T *__restrict__ r, T *__restrict
         t[0] += rv[0] * z0 + rv[1] * z1 + rv[2] * z2;
         t[1] += rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
     }
-    double v[5] = {(double)t[0], (double)t[1], (double)t[2], (double)t[3], (double)t[4]};
     double out[5];
-    if (grid_reduce<5, (8u | 16u)>(v, partials, &S->cnt_b, out) && threadIdx.x == 0) {
+    if (grid_reduce_t<5, (8u | 16u)>(t, partials, &S->cnt_b, out) && threadIdx.x == 0) {
         const double rz_old = S->rz;
         S->iter += 1;
         S->rr = out[1];
