@@ -45,7 +45,8 @@ def parse():
     p.add_argument("--cpu-side", type=int, default=24, help="elements per side of the CPU sample")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
-    p.add_argument("--mode", default="bench", choices=["bench", "profile", "solve"],
+    p.add_argument("--fd", type=int, default=32, help="elements checked by central differences (adjoint mode)")
+    p.add_argument("--mode", default="bench", choices=["bench", "profile", "solve", "adjoint"],
                    help="profile: time the PCG kernels once on --side (small ncu case); "
                         "solve: one assemble + mixed solve at --tol (launch-list case)")
     p.add_argument("--tol", type=float, default=1e-10)
@@ -348,8 +349,76 @@ def run_small(args):
     print(json.dumps(out), flush=True)
 
 
+def run_adjoint(args):
+    """Forward time-to-solution vs adjoint gradient cost (compliance and displacement misfit)
+    on the bench workload, and a central-difference check on --fd random elements
+    (default_rng(seed + 1)), h = 1e-6 E_e.  J(E +- h) is evaluated through the exact difference
+    u+- = u + delta+-, K(E +- h) delta+- = F - K(E +- h) u, solved with the mixed solver."""
+    import torch
+    from lmtpp_gb300 import make_rect_hexa
+    N = args.side
+    pos, conn = make_rect_hexa(N + 1)
+    E = lognormal_E(conn.shape[0])
+    f = new_problem(pos, conn, E, 0)
+    stream = torch.cuda.ExternalStream(f.stream_handle(), device=torch.device("cuda", 0))
+    one_solve(f, "mixed", 1e-12)
+    f.set_penalty_scale(f.get_penalty_scale())  # gradients hold the penalty scale fixed
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
+    torch.cuda.synchronize()
+    ev[0].record(stream)
+    st_fwd = one_solve(f, "mixed", args.tol)
+    ev[1].record(stream)
+    Jc, gc, _ = f.adjoint_grad("compliance")
+    ev[2].record(stream)
+    rng = np.random.default_rng(SEED + 1)
+    u = f.get_result()
+    t = u * (1.0 + 0.1 * rng.standard_normal(u.shape[0]))
+    ev[3].record(stream)
+    Jm, gm, st_adj = f.adjoint_grad("misfit", target=t, mode="mixed", tol=args.tol)
+    ev[4].record(stream)
+    ev[4].synchronize()
+    fwd_ms = ev[0].elapsed_time(ev[1])
+    comp_ms = ev[1].elapsed_time(ev[2])
+    mis_ms = ev[3].elapsed_time(ev[4])
+    # central differences
+    F = f.get_sollicitation()
+    r = u - t
+    picks = rng.choice(conn.shape[0], args.fd, replace=False)
+    errs_c, errs_m = [], []
+    for e in picks:
+        h = 1e-6 * E[e]
+        d = {}
+        for sgn in (1, -1):
+            Ep = E.copy()
+            Ep[e] += sgn * h
+            f.elastic_modulus = Ep
+            f.assemble(True, False, mixed=True)
+            f.set_nodal_loads(F - f.spmv(u, 0))
+            f.assemble(False, True)
+            f.set_result(np.zeros_like(u))
+            f.solve_system(1e-12, mode="mixed", maxit=200000, timeout_s=900.0)
+            d[sgn] = f.get_result()
+        fd_c = (F @ d[1] - F @ d[-1]) / (2 * h)
+        fd_m = ((r @ d[1] + 0.5 * d[1] @ d[1]) - (r @ d[-1] + 0.5 * d[-1] @ d[-1])) / (2 * h)
+        errs_c.append(abs(fd_c - gc[e]) / abs(gc[e]))
+        errs_m.append(abs(fd_m - gm[e]) / max(abs(gm[e]), 1e-300))
+    f.close()
+    out = {"mode": "adjoint", "workload": workload_config(args)["workload"],
+           "forward_ms": fwd_ms, "forward_iters": st_fwd["iterations"],
+           "compliance_grad_ms": comp_ms, "compliance_ratio_vs_forward": comp_ms / fwd_ms,
+           "misfit_grad_ms": mis_ms, "misfit_ratio_vs_forward": mis_ms / fwd_ms,
+           "misfit_adjoint_iters": st_adj["iterations"],
+           "fd_elements": int(args.fd), "fd_h_rel": 1e-6,
+           "fd_max_rel_err_compliance": max(errs_c), "fd_max_rel_err_misfit": max(errs_m),
+           "fd_median_rel_err_compliance": float(np.median(errs_c)),
+           "fd_median_rel_err_misfit": float(np.median(errs_m))}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
+    if args.mode == "adjoint":
+        return run_adjoint(args)
     if args.mode != "bench":
         return run_small(args)
     rank, world, local, barrier, allmax = dist_setup(args.gpus)

@@ -59,6 +59,10 @@ extern "C" {
 #define LMTG_CRIT_ABS_RESIDUAL_INF 3 /* |r|_inf <= tol (solve_using_incomplete_chol_factorize,
                                         include/containers/matinvsparse.h:453-491) */
 
+/* ---- adjoint objectives ---- */
+#define LMTG_OBJ_COMPLIANCE 0 /* J = F . u */
+#define LMTG_OBJ_MISFIT 1     /* J = 1/2 sum_i w_i (u_i - t_i)^2 */
+
 typedef struct lmtg_ctx lmtg_ctx;
 
 typedef struct lmtg_solve_stats {
@@ -134,6 +138,24 @@ int lmtg_solve(lmtg_ctx *ctx, int mode, int crit_kind, double tol, int maxit, do
 /* get_result(0): the solution vector (n doubles); set_result: the initial guess. */
 int lmtg_get_result(lmtg_ctx *ctx, double *u);
 int lmtg_set_result(lmtg_ctx *ctx, const double *u);
+
+/* Penalty scale: 0 (default) recomputes max|diag K| at every matrix assembly as the reference
+ * does (formulation.h:1029-1030); a positive value is used instead, which holds the penalty fixed
+ * while the material changes (the gradients below treat it as constant).
+ * lmtg_get_penalty_scale returns the value used by the last assembly. */
+int lmtg_set_penalty_scale(lmtg_ctx *ctx, double max_diag);
+int lmtg_get_penalty_scale(lmtg_ctx *ctx, double *max_diag);
+
+/* Adjoint gradient of an objective of the current solution u w.r.t. every element's Young's
+ * modulus (ne doubles into dJdE) and the objective value J.  No counterpart in the reference,
+ * which offers forward sensitivities only (solve_and_get_derivatives, formulation.h:1588-1652:
+ * one solve per parameter).  Compliance needs no extra solve (the adjoint is u); the misfit
+ * (target t and weights w of n doubles, NULL = 0 and 1) solves K lambda = w (u - t) with `mode`
+ * (LMTG_SOLVE_*) to the relative residual `tol`.  dJ/dE_e = -lambda_e^T (K_e / E_e) u_e with the
+ * element matrix recomputed, not stored; the penalty scale is held constant. */
+int lmtg_adjoint_grad(lmtg_ctx *ctx, int objective, const double *target, const double *weights,
+                      int mode, double tol, int maxit, double timeout_s, double *J, double *dJdE,
+                      lmtg_solve_stats *stats);
 
 /* y = K x with the assembled matrix in FP64 (precision 0) or FP32 (precision 1). */
 int lmtg_spmv(lmtg_ctx *ctx, int precision, const double *x, double *y);

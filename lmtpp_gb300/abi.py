@@ -16,6 +16,7 @@ ELEM_HEXA8 = 8
 ASM_MAT64, ASM_MAT32, ASM_VEC, ASM_MAT32_NATIVE = 1, 2, 4, 8
 SOLVE_PCG_F64, SOLVE_MIXED_IR = 0, 1
 CRIT_REL_RESIDUAL, CRIT_NORM_INF_DELTA, CRIT_NORM2_DELTA, CRIT_ABS_RESIDUAL_INF = 0, 1, 2, 3
+OBJ_COMPLIANCE, OBJ_MISFIT = 0, 1
 
 _vp = ctypes.c_void_p
 _u64 = ctypes.c_uint64
@@ -57,6 +58,10 @@ _SIGS = {
     "lmtg_spmv": (_i, [_vp, _i, _vp, _vp]),
     "lmtg_get_sizes": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "lmtg_get_launch_count": (_i, [_vp, ctypes.POINTER(_u64)]),
+    "lmtg_set_penalty_scale": (_i, [_vp, _d]),
+    "lmtg_get_penalty_scale": (_i, [_vp, ctypes.POINTER(_d)]),
+    "lmtg_adjoint_grad": (_i, [_vp, _i, _vp, _vp, _i, _d, _i, _d, ctypes.POINTER(_d), _vp,
+                               ctypes.POINTER(SolveStats)]),
     "lmtg_get_stream": (_i, [_vp, ctypes.POINTER(_vp)]),
     "lmtg_residual_norm_noalloc": (_i, [_vp, _u64, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.POINTER(_d)]),
     "lmtg_profile_pcg_kernels": (_i, [_vp, _i, _i, ctypes.POINTER(_d), ctypes.POINTER(_d)]),

@@ -107,7 +107,12 @@ void apply_penalty(lmtg_ctx *c, bool mat, bool vec) {
     DBuf<unsigned long long> md;
     md.alloc(1);
     const int T = 256;
-    if (mat) {
+    if (mat && c->penalty_scale > 0.0) {
+        // caller-fixed scale (held constant for sensitivities w.r.t. the material)
+        unsigned long long bits;
+        memcpy(&bits, &c->penalty_scale, sizeof(bits));
+        LMTG_CUDA(cudaMemcpyAsync(md.p, &bits, sizeof(bits), cudaMemcpyHostToDevice, c->stream));
+    } else if (mat) {
         // max|diag| of the freshly assembled K, before any constraint (formulation.h:1029-1030)
         LMTG_CUDA(cudaMemsetAsync(md.p, 0, sizeof(unsigned long long), c->stream));
         if (c->have64) k_max_diag<double><<<grid_for(c, c->nn, T), T, 0, c->stream>>>(c->bdiag.p, c->K64.p, c->nn, md.p);
@@ -129,7 +134,7 @@ void apply_penalty(lmtg_ctx *c, bool mat, bool vec) {
                                                  c->cres.p, c->nc, c->penalty, md.p, mat, vec);
     }
     LMTG_CUDA(cudaGetLastError());
-    c->launches += (mat ? 1 : 0) + 1 + ((mat && c->have64 && c->have32) ? 1 : 0);
+    c->launches += ((mat && c->penalty_scale <= 0.0) ? 1 : 0) + 1 + ((mat && c->have64 && c->have32) ? 1 : 0);
     unsigned long long bits = 0;
     LMTG_CUDA(cudaMemcpyAsync(&bits, md.p, sizeof(bits), cudaMemcpyDeviceToHost, c->stream));
     LMTG_CUDA(cudaStreamSynchronize(c->stream));

@@ -113,6 +113,7 @@ struct lmtg_ctx {
 
     // values
     lmtg::DBuf<double> Ke64, K64, F, u, Dinv64;
+    lmtg::DBuf<double> adj_rhs, adj_lam, grad;  // adjoint workspace
     lmtg::DBuf<float> Ke32, K32, Dinv32;
     bool have64 = false, have32 = false, have_vec = false;
     double max_diag = 0;
@@ -123,6 +124,7 @@ struct lmtg_ctx {
     lmtg::DBuf<uint32_t> cdof;
     lmtg::DBuf<double> ccoef, cres;
     double penalty = 0;
+    double penalty_scale = 0;  // > 0: fixed max|diag| used by the penalty instead of recomputing it
 
     // solver workspace
     lmtg::DBuf<double> w64[6];
@@ -149,12 +151,17 @@ void apply_penalty(lmtg_ctx *c, bool mat, bool vec);
 void build_block_jacobi(lmtg_ctx *c, bool want64, bool want32);
 void copy_k64_to_k32(lmtg_ctx *c);
 
+// ---- adjoint (adjoint.cu) ----
+void launch_hexa8_grad_E(lmtg_ctx *c, const double *a, const double *b, double *g);
+
 // ---- solver (solver.cu) ----
 void spmv64(lmtg_ctx *c, const double *x, double *y);
 void spmv32(lmtg_ctx *c, const float *x, float *y);
+// Solves K x = b (defaults: b = F, x = u) from the current x.
 int solve_pcg64(lmtg_ctx *c, int crit_kind, double tol, int maxit, double timeout_s,
-                lmtg_solve_stats *st);
-int solve_mixed(lmtg_ctx *c, double tol, int maxit, double timeout_s, lmtg_solve_stats *st);
+                lmtg_solve_stats *st, const double *b = nullptr, double *x = nullptr);
+int solve_mixed(lmtg_ctx *c, double tol, int maxit, double timeout_s, lmtg_solve_stats *st,
+                const double *b = nullptr, double *x = nullptr);
 void profile_pcg(lmtg_ctx *c, bool fp32, int iters, double *spmv_ms, double *update_ms);
 
 // ---- utilities (pattern.cu) ----

@@ -181,17 +181,19 @@ static int run_pcg(lmtg_ctx *c, const T *K, const T *Dinv, const T *b, T *x, T *
 }
 
 int solve_pcg64(lmtg_ctx *c, int crit_kind, double tol, int maxit, double timeout_s,
-                lmtg_solve_stats *st) {
+                lmtg_solve_stats *st, const double *bvec, double *xvec) {
+    const double *Fb = bvec ? bvec : c->F.p;
+    double *ux = xvec ? xvec : c->u.p;
     auto deadline = std::chrono::steady_clock::now() +
                     std::chrono::duration_cast<std::chrono::steady_clock::duration>(
                         std::chrono::duration<double>(timeout_s > 0 ? timeout_s : 0));
     double *r = c->w64[0].p, *z = c->w64[1].p, *p0 = c->w64[2].p, *p1 = c->w64[3].p,
            *q = c->w64[4].p;
     int it = 0;
-    int status = run_pcg<double>(c, c->K64.p, c->Dinv64.p, c->F.p, c->u.p, r, z, p0, p1, q, false,
+    int status = run_pcg<double>(c, c->K64.p, c->Dinv64.p, Fb, ux, r, z, p0, p1, q, false,
                                  crit_kind, tol, maxit, -1.0, deadline, timeout_s > 0, &it);
-    double bb = dot64(c, c->F.p, c->F.p);
-    double rr = residual<double>(c, c->K64.p, c->u.p, c->F.p, r);
+    double bb = dot64(c, Fb, Fb);
+    double rr = residual<double>(c, c->K64.p, ux, Fb, r);
     st->iterations = it;
     st->outer_iterations = 0;
     st->rel_residual = bb > 0 ? std::sqrt(rr / bb) : std::sqrt(rr);
@@ -205,7 +207,10 @@ int solve_pcg64(lmtg_ctx *c, int crit_kind, double tol, int maxit, double timeou
 // search direction is kept (beta folded with the rescaling), so the Krylov recurrence is not
 // restarted.  A segment that fails to reduce the true residual restarts from p = z (a classic
 // iterative-refinement step).  Convergence is judged on the FP64 true residual only.
-int solve_mixed(lmtg_ctx *c, double tol, int maxit, double timeout_s, lmtg_solve_stats *st) {
+int solve_mixed(lmtg_ctx *c, double tol, int maxit, double timeout_s, lmtg_solve_stats *st,
+                const double *bvec, double *xvec) {
+    const double *Fb = bvec ? bvec : c->F.p;
+    double *ux = xvec ? xvec : c->u.p;
     auto deadline = std::chrono::steady_clock::now() +
                     std::chrono::duration_cast<std::chrono::steady_clock::duration>(
                         std::chrono::duration<double>(timeout_s > 0 ? timeout_s : 0));
@@ -213,14 +218,14 @@ int solve_mixed(lmtg_ctx *c, double tol, int maxit, double timeout_s, lmtg_solve
     float *b32 = c->w32[0].p, *d32 = c->w32[1].p, *r32 = c->w32[2].p, *z32 = c->w32[3].p,
           *pa = c->w32[4].p, *pb = c->w32[5].p;
     float *q32 = reinterpret_cast<float *>(c->w64[1].p);  // FP64 buffer reused as FP32 q
-    const double bb = dot64(c, c->F.p, c->F.p);
+    const double bb = dot64(c, Fb, Fb);
     constexpr double kDelta = 0.1;  // recursive-residual reduction per segment
     int total = 0, outer = 0, status = LMTG_OK;
     double rel = 0, s_prev = 0, rz_prev = 0, rel_prev = 0;
     bool have_dir = false;
     const int max_outer = 400;
     for (;;) {
-        const double rr = residual<double>(c, c->K64.p, c->u.p, c->F.p, r64);
+        const double rr = residual<double>(c, c->K64.p, ux, Fb, r64);
         rel = bb > 0 ? std::sqrt(rr / bb) : std::sqrt(rr);
         if (!std::isfinite(rel)) {
             status = LMTG_ERR_NAN;
@@ -264,7 +269,7 @@ int solve_mixed(lmtg_ctx *c, double tol, int maxit, double timeout_s, lmtg_solve
         s_prev = sc;
         rel_prev = rel;
         have_dir = it > 0 && rz_prev > 0.0;
-        k_axpy_64_32<<<node_grid(c), kRowThreads, 0, c->stream>>>(c->u.p, sc, d32, c->n);
+        k_axpy_64_32<<<node_grid(c), kRowThreads, 0, c->stream>>>(ux, sc, d32, c->n);
         LMTG_CUDA(cudaGetLastError());
         c->launches += 1;
     }

@@ -239,6 +239,32 @@ class Formulation:
         abi.check(self._lib.lmtg_spmv(self._ctx, precision, abi.ptr(x), abi.ptr(y)), self._ctx, "spmv")
         return y
 
+    # -- sensitivities -------------------------------------------------------------------------
+    def set_penalty_scale(self, max_diag):
+        """Hold the penalty scale at max_diag (0 = recompute max|diag K| at each assembly)."""
+        abi.check(self._lib.lmtg_set_penalty_scale(self._ctx, float(max_diag)), self._ctx, "penalty scale")
+
+    def get_penalty_scale(self):
+        v = ctypes.c_double()
+        abi.check(self._lib.lmtg_get_penalty_scale(self._ctx, ctypes.byref(v)), self._ctx, "penalty scale")
+        return v.value
+
+    def adjoint_grad(self, objective="compliance", target=None, weights=None, mode="mixed",
+                     tol=1e-10, maxit=100000, timeout_s=600.0):
+        """Adjoint gradient dJ/dE (one value per element) of the compliance F.u or of the misfit
+        1/2 sum w (u - t)^2 at the current solution; returns (J, dJdE, adjoint solve stats)."""
+        obj = {"compliance": abi.OBJ_COMPLIANCE, "misfit": abi.OBJ_MISFIT}[objective]
+        t = None if target is None else np.ascontiguousarray(target, dtype=np.float64)
+        w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64)
+        g = np.zeros(self.ne)
+        J = ctypes.c_double()
+        st = abi.SolveStats()
+        m = {"fp64": abi.SOLVE_PCG_F64, "mixed": abi.SOLVE_MIXED_IR}[mode]
+        abi.check(self._lib.lmtg_adjoint_grad(self._ctx, obj, abi.ptr(t), abi.ptr(w), m, float(tol),
+                                              int(maxit), float(timeout_s), ctypes.byref(J), abi.ptr(g),
+                                              ctypes.byref(st)), self._ctx, "adjoint_grad")
+        return J.value, g, st.as_dict()
+
     def stream_handle(self):
         """cudaStream_t of this formulation (every kernel and copy is issued on it)."""
         s = ctypes.c_void_p()

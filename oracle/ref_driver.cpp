@@ -17,7 +17,7 @@
  *
  * Usage: ref_driver hexa <nb_points> <E> <nu> <penalty> <outdir>
  * Writes little-endian raw arrays: pos.f64 conn.u32 rowptr.u64 col.u32 val.f64 F.f64
- * u_ldl.f64 u_icpcg.f64 and info.txt.
+ * u_ldl.f64 u_icpcg.f64 lam_ldl.f64 (LDL solution of K lambda = u_ldl) and info.txt.
  */
 #include "mesh/meshcaracstd.h"
 #include "mesh/make_rect.h"
@@ -129,6 +129,13 @@ int main(int argc, char **argv) {
     ldl.solve(sol);
     std::vector<double> u_ldl(n);
     for (unsigned i = 0; i < n; ++i) u_ldl[i] = sol[i];
+    /* adjoint of the misfit 1/2 |u|^2 (target 0, unit weights): K lambda = u, same factorization */
+    Vec<double> sol2;
+    sol2.resize(n);
+    for (unsigned i = 0; i < n; ++i) sol2[i] = u_ldl[i];
+    ldl.solve(sol2);
+    std::vector<double> lam_ldl(n);
+    for (unsigned i = 0; i < n; ++i) lam_ldl[i] = sol2[i];
 
     /* IC(0)-PCG of the reference with |r|_inf <= 1e-10 * max|F| */
     Mat<double, Sym<>, SparseLine<> > P = K;
@@ -154,6 +161,7 @@ int main(int argc, char **argv) {
     dump(out + "/F.f64", F);
     dump(out + "/u_ldl.f64", u_ldl);
     dump(out + "/u_icpcg.f64", u_ic);
+    dump(out + "/lam_ldl.f64", lam_ldl);
     FILE *f = fopen((out + "/info.txt").c_str(), "w");
     fprintf(f, "nn %u\nne %u\nn %u\nnnz %zu\nmax_diag %.17g\nncons %u\nnfaces %zu\nicpcg_iter %d\n",
             nn, ne, n, col.size(), max_diag, ncons, faces.size() / 4, it);

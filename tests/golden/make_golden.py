@@ -2,7 +2,8 @@
 
 Runs oracle/_ref/ref_driver (LMT++'s make_rect, Sym SparseLine assembly semantics, max|diag|
 penalty constraints, LDL and IC(0)-PCG, built by oracle/build_ref.sh from the LMTpp sources)
-on the elasticity workload of the reference's example -- unit cube of Hexa8, penalty clamp of
+(and the LDL solution of K lambda = u, the adjoint of the misfit 1/2 |u|^2) on the elasticity
+workload of the reference's example -- unit cube of Hexa8, penalty clamp of
 x = 0, uniform traction (1,0,0) on x = 1 -- and stores its outputs as compressed npz.
 
 Also records the known-answer vectors of the reference's solver unit tests
@@ -39,7 +40,7 @@ def run_case(name, nbp, E, nu, pen):
             pos=r("pos.f64", np.float64).reshape(-1, 3), conn=r("conn.u32", np.uint32).reshape(-1, 8),
             rowptr=r("rowptr.u64", np.uint64), col=r("col.u32", np.uint32), val=r("val.f64", np.float64),
             F=r("F.f64", np.float64), u_ldl=r("u_ldl.f64", np.float64),
-            u_icpcg=r("u_icpcg.f64", np.float64),
+            u_icpcg=r("u_icpcg.f64", np.float64), lam_ldl=r("lam_ldl.f64", np.float64),
             meta=np.array(json.dumps(dict(nb_points=nbp, E=E, nu=nu, penalty=pen,
                                           max_diag=float(info["max_diag"]),
                                           icpcg_iter=int(info["icpcg_iter"]),

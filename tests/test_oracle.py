@@ -114,3 +114,12 @@ def test_oracle_constraint_penalty_semantics():
     assert md == 4.0
     assert val[-1] == 3.0 + 2.0 * 2.0 * 4.0 * 10.0
     assert F[1] == 2.0 + 2.0 * 4.0 * 10.0 * 0.5
+
+
+def test_oracle_adjoint_solve_matches_reference_ldl(golden_dir):
+    """K lambda = u (the misfit adjoint) with the oracle's direct solver vs the reference's LDL."""
+    g = load_golden(golden_dir, "hexa_10x10x10")
+    m = g["meta"]
+    P = O.elasticity_problem(m["nb_points"], E=m["E"], nu=m["nu"], pen=m["penalty"])
+    lam = O.skyline_solve(P["rowptr"], P["col"], P["val"], g["u_ldl"])
+    assert np.linalg.norm(lam - g["lam_ldl"]) <= 1e-12 * np.linalg.norm(g["lam_ldl"])
