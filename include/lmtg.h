@@ -62,6 +62,7 @@ extern "C" {
 /* ---- adjoint objectives ---- */
 #define LMTG_OBJ_COMPLIANCE 0 /* J = F . u */
 #define LMTG_OBJ_MISFIT 1     /* J = 1/2 sum_i w_i (u_i - t_i)^2 */
+#define LMTG_OBJ_LINEAR 2     /* J = c . u, c passed as `target` (adjoint of any upstream gradient) */
 
 typedef struct lmtg_ctx lmtg_ctx;
 
@@ -150,7 +151,8 @@ int lmtg_get_penalty_scale(lmtg_ctx *ctx, double *max_diag);
  * modulus (ne doubles into dJdE) and the objective value J.  No counterpart in the reference,
  * which offers forward sensitivities only (solve_and_get_derivatives, formulation.h:1588-1652:
  * one solve per parameter).  Compliance needs no extra solve (the adjoint is u); the misfit
- * (target t and weights w of n doubles, NULL = 0 and 1) solves K lambda = w (u - t) with `mode`
+ * (target t and weights w of n doubles, NULL = 0 and 1) solves K lambda = w (u - t), the linear
+ * objective (c in `target`) solves K lambda = c, with `mode`
  * (LMTG_SOLVE_*) to the relative residual `tol`.  dJ/dE_e = -lambda_e^T (K_e / E_e) u_e with the
  * element matrix recomputed, not stored; the penalty scale is held constant. */
 int lmtg_adjoint_grad(lmtg_ctx *ctx, int objective, const double *target, const double *weights,

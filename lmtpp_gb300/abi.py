@@ -16,7 +16,7 @@ ELEM_HEXA8 = 8
 ASM_MAT64, ASM_MAT32, ASM_VEC, ASM_MAT32_NATIVE = 1, 2, 4, 8
 SOLVE_PCG_F64, SOLVE_MIXED_IR = 0, 1
 CRIT_REL_RESIDUAL, CRIT_NORM_INF_DELTA, CRIT_NORM2_DELTA, CRIT_ABS_RESIDUAL_INF = 0, 1, 2, 3
-OBJ_COMPLIANCE, OBJ_MISFIT = 0, 1
+OBJ_COMPLIANCE, OBJ_MISFIT, OBJ_LINEAR = 0, 1, 2
 
 _vp = ctypes.c_void_p
 _u64 = ctypes.c_uint64

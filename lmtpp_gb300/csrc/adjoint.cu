@@ -6,6 +6,7 @@
 // (+ penalty terms, held at a fixed max|diag| scale), K u = F and an objective J(u):
 //   compliance  J = F.u                      adjoint lambda = u (no extra solve)
 //   misfit      J = 1/2 sum_i w_i (u_i - t_i)^2   K lambda = w (u - t)   (one PCG solve)
+//   linear      J = c.u                      K lambda = c           (one PCG solve)
 //   dJ/dE_e = -lambda_e^T Khat_e u_e.
 // The element matrix is not stored: k_hexa8_grad_E recomputes the geometry per Gauss point
 // and evaluates the bilinear form directly,
@@ -186,8 +187,10 @@ int lmtg_adjoint_grad(lmtg_ctx *c, int objective, const double *target, const do
     return guard3(c, [&] {
         LMTG_CHECK(c->have64 && c->have_vec, LMTG_ERR_STATE, "assemble (FP64) and solve first");
         LMTG_CHECK(dJdE && J, LMTG_ERR_ARG, "null output");
-        LMTG_CHECK(objective == LMTG_OBJ_COMPLIANCE || objective == LMTG_OBJ_MISFIT, LMTG_ERR_ARG,
-                   "unknown objective");
+        LMTG_CHECK(objective == LMTG_OBJ_COMPLIANCE || objective == LMTG_OBJ_MISFIT ||
+                       objective == LMTG_OBJ_LINEAR,
+                   LMTG_ERR_ARG, "unknown objective");
+        LMTG_CHECK(objective != LMTG_OBJ_LINEAR || target, LMTG_ERR_ARG, "linear objective needs c");
         c->grad.alloc(c->ne);
         PcgScalars *o = c->scal.p + 1;
         const int T = 256;
@@ -209,8 +212,15 @@ int lmtg_adjoint_grad(lmtg_ctx *c, int objective, const double *target, const do
             }
             c->adj_rhs.alloc(c->n);
             c->adj_lam.alloc(c->n);
-            k_misfit<<<grid, T, 0, c->stream>>>(c->u.p, dt.p, dw.p, c->n, c->adj_rhs.p, c->partials.p,
-                                                &o->cnt_c, &o->rr);
+            if (objective == LMTG_OBJ_MISFIT) {
+                k_misfit<<<grid, T, 0, c->stream>>>(c->u.p, dt.p, dw.p, c->n, c->adj_rhs.p,
+                                                    c->partials.p, &o->cnt_c, &o->rr);
+            } else {  // linear: rhs = c, J = c . u
+                LMTG_CUDA(cudaMemcpyAsync(c->adj_rhs.p, dt.p, c->n * 8, cudaMemcpyDeviceToDevice,
+                                          c->stream));
+                k_dot_small<<<grid, T, 0, c->stream>>>(dt.p, c->u.p, c->n, c->partials.p, &o->cnt_c,
+                                                       &o->rr);
+            }
             c->launches += 1;
             double jv = 0;
             LMTG_CUDA(cudaMemcpyAsync(&jv, &o->rr, 8, cudaMemcpyDeviceToHost, c->stream));

@@ -251,9 +251,11 @@ class Formulation:
 
     def adjoint_grad(self, objective="compliance", target=None, weights=None, mode="mixed",
                      tol=1e-10, maxit=100000, timeout_s=600.0):
-        """Adjoint gradient dJ/dE (one value per element) of the compliance F.u or of the misfit
-        1/2 sum w (u - t)^2 at the current solution; returns (J, dJdE, adjoint solve stats)."""
-        obj = {"compliance": abi.OBJ_COMPLIANCE, "misfit": abi.OBJ_MISFIT}[objective]
+        """Adjoint gradient dJ/dE (one value per element) of the compliance F.u, of the misfit
+        1/2 sum w (u - t)^2, or of the linear objective c.u (c passed as target) at the current
+        solution; returns (J, dJdE, adjoint solve stats)."""
+        obj = {"compliance": abi.OBJ_COMPLIANCE, "misfit": abi.OBJ_MISFIT,
+               "linear": abi.OBJ_LINEAR}[objective]
         t = None if target is None else np.ascontiguousarray(target, dtype=np.float64)
         w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64)
         g = np.zeros(self.ne)

@@ -95,3 +95,21 @@ def test_adjoint_gradients_match_central_differences():
         assert fd_c == pytest.approx(gc[e], rel=1e-5), (e, fd_c, gc[e])
         assert fd_m == pytest.approx(gm[e], rel=1e-5), (e, fd_m, gm[e])
     f.close()
+
+
+def test_autograd_wrapper_matches_adjoint_misfit():
+    torch = pytest.importorskip("torch")
+    from lmtpp_gb300.autograd import elastic_displacement
+    pos, conn = make_rect_hexa(9)
+    rng = np.random.default_rng(3)
+    E0 = np.exp(np.log(210000.0) + 0.3 * rng.standard_normal(conn.shape[0]))
+    f = build(pos, conn, E0, 0.3, 1e5)
+    E = torch.tensor(E0, dtype=torch.float64, requires_grad=True)
+    u = elastic_displacement(E, f, "fp64", 1e-13)
+    t = torch.from_numpy(rng.standard_normal(u.shape[0]) * 1e-6)
+    loss = 0.5 * ((u - t) ** 2).sum()
+    loss.backward()
+    Jm, gm, _ = f.adjoint_grad("misfit", target=t.numpy(), mode="fp64", tol=1e-13)
+    assert float(loss.detach()) == pytest.approx(Jm, rel=1e-12)
+    assert np.linalg.norm(E.grad.numpy() - gm) <= 1e-9 * np.linalg.norm(gm)
+    f.close()
