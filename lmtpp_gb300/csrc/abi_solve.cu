@@ -89,13 +89,14 @@ int lmtg_get_matrix_lower(lmtg_ctx *c, uint64_t *rowptr, uint32_t *col, double *
         rowptr[0] = 0;
         for (uint64_t i = 0; i < c->nn; ++i)
             for (int r = 0; r < 3; ++r) {
-                for (uint32_t k = bptr[i]; k < bptr[i + 1]; ++k) {
+                const uint32_t rb = bptr[i], deg = bptr[i + 1] - rb;
+                for (uint32_t k = rb; k < rb + deg; ++k) {
                     const uint32_t J = bcol[k];
                     if (J > i) break;
                     const int dmax = (J == i) ? r : 2;
                     for (int d = 0; d <= dmax; ++d) {
                         col[w] = 3 * J + d;
-                        val[w] = K[(uint64_t)k * 9 + 3 * r + d];
+                        val[w] = K[kidx(rb, deg, k - rb, 3 * r + d)];
                         ++w;
                     }
                 }

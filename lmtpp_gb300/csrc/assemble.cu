@@ -17,13 +17,24 @@
 namespace lmtg {
 
 template <class TS, bool kW64, bool kW32>
-__global__ void k_assemble(const uint32_t *__restrict__ gptr, const uint32_t *__restrict__ gsrc,
+__global__ void k_assemble(const uint32_t *__restrict__ bptr, uint64_t nn,
+                           const uint32_t *__restrict__ gptr, const uint32_t *__restrict__ gsrc,
                            const TS *__restrict__ Ke, uint64_t nvals, double *__restrict__ K64,
                            float *__restrict__ K32) {
     for (uint64_t idx = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; idx < nvals;
          idx += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t blk = idx / 9;
-        const int v = (int)(idx - blk * 9);
+        // output position -> (row, component, block) of the planar row layout
+        const uint64_t bi = idx / 9;  // some block of the row that contains idx
+        uint64_t lo = 0, hi = nn;     // row I with bptr[I] <= bi < bptr[I+1]
+        while (hi - lo > 1) {
+            const uint64_t mid = (lo + hi) >> 1;
+            if (__ldg(bptr + mid) <= bi) lo = mid;
+            else hi = mid;
+        }
+        const uint32_t rb = __ldg(bptr + lo), deg = __ldg(bptr + lo + 1) - rb;
+        const uint64_t off = idx - 9ull * rb;
+        const int v = (int)(off / deg);
+        const uint64_t blk = rb + (off - (uint64_t)v * deg);
         const int vt = (v % 3) * 3 + v / 3;  // transposed position
         const uint32_t g0 = gptr[blk], g1 = gptr[blk + 1];
         typedef typename std::conditional<sizeof(TS) == 8, double, float>::type Acc;
@@ -43,18 +54,22 @@ void assemble_matrix(lmtg_ctx *c, bool from64, bool want64, bool want32) {
     const int grid = grid_for(c, nvals, T, 8);
     if (from64) {
         if (want64 && want32)
-            k_assemble<double, true, true><<<grid, T, 0, c->stream>>>(c->gptr.p, c->gsrc.p, c->Ke64.p,
-                                                                      nvals, c->K64.p, c->K32.p);
+            k_assemble<double, true, true><<<grid, T, 0, c->stream>>>(c->bptr.p, c->nn, c->gptr.p,
+                                                                      c->gsrc.p, c->Ke64.p, nvals,
+                                                                      c->K64.p, c->K32.p);
         else if (want64)
-            k_assemble<double, true, false><<<grid, T, 0, c->stream>>>(c->gptr.p, c->gsrc.p,
+            k_assemble<double, true, false><<<grid, T, 0, c->stream>>>(c->bptr.p, c->nn, c->gptr.p,
+                                                                       c->gsrc.p,
                                                                        c->Ke64.p, nvals, c->K64.p,
                                                                        nullptr);
         else
-            k_assemble<double, false, true><<<grid, T, 0, c->stream>>>(c->gptr.p, c->gsrc.p,
+            k_assemble<double, false, true><<<grid, T, 0, c->stream>>>(c->bptr.p, c->nn, c->gptr.p,
+                                                                       c->gsrc.p,
                                                                        c->Ke64.p, nvals, nullptr,
                                                                        c->K32.p);
     } else {
-        k_assemble<float, false, true><<<grid, T, 0, c->stream>>>(c->gptr.p, c->gsrc.p, c->Ke32.p,
+        k_assemble<float, false, true><<<grid, T, 0, c->stream>>>(c->bptr.p, c->nn, c->gptr.p,
+                                                                  c->gsrc.p, c->Ke32.p,
                                                                   nvals, nullptr, c->K32.p);
     }
     LMTG_CUDA(cudaGetLastError());
@@ -65,20 +80,21 @@ void assemble_matrix(lmtg_ctx *c, bool from64, bool want64, bool want32) {
 // max|diag K|: diagonal entries are non-negative-signed after fabs, so the IEEE bit pattern
 // orders like the value and an integer atomicMax is exact.
 template <class T>
-__global__ void k_max_diag(const uint32_t *__restrict__ bdiag, const T *__restrict__ K,
-                           uint64_t nn, unsigned long long *out) {
+__global__ void k_max_diag(const uint32_t *__restrict__ bptr, const uint32_t *__restrict__ bdiag,
+                           const T *__restrict__ K, uint64_t nn, unsigned long long *out) {
     double m = 0;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nn;
          i += (uint64_t)gridDim.x * blockDim.x) {
-        const T *d = K + (uint64_t)bdiag[i] * 9;
-        m = fmax(m, fmax(fabs((double)d[0]), fmax(fabs((double)d[4]), fabs((double)d[8]))));
+        const uint32_t rb = bptr[i], deg = bptr[i + 1] - rb, d = bdiag[i] - rb;
+        m = fmax(m, fmax(fabs((double)K[kidx(rb, deg, d, 0)]),
+                         fmax(fabs((double)K[kidx(rb, deg, d, 4)]), fabs((double)K[kidx(rb, deg, d, 8)]))));
     }
     m = warp_max(m);
     if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
 }
 
 template <class T>
-__global__ void k_penalty(const uint32_t *__restrict__ bdiag, T *K, double *F,
+__global__ void k_penalty(const uint32_t *__restrict__ bptr, const uint32_t *__restrict__ bdiag, T *K, double *F,
                           const uint32_t *__restrict__ dof, const double *__restrict__ coef,
                           const double *__restrict__ res, uint64_t nc, double penalty,
                           const unsigned long long *md_bits, bool mat, bool vec) {
@@ -88,16 +104,20 @@ __global__ void k_penalty(const uint32_t *__restrict__ bdiag, T *K, double *F,
         const uint32_t j = dof[k];
         const double C = coef[k] * md * penalty;
         if (vec) atomicAdd(F + j, C * res[k]);
-        if (mat) atomicAdd(K + (uint64_t)bdiag[j / 3] * 9 + 4 * (j % 3), (T)(C * coef[k]));
+        if (mat) {
+            const uint32_t I = j / 3, rb = bptr[I];
+            atomicAdd(K + kidx(rb, bptr[I + 1] - rb, bdiag[I] - rb, 4 * (j % 3)), (T)(C * coef[k]));
+        }
     }
 }
 
-__global__ void k_round_constrained(const uint32_t *__restrict__ bdiag, const double *K64,
+__global__ void k_round_constrained(const uint32_t *__restrict__ bptr,
+                                    const uint32_t *__restrict__ bdiag, const double *K64,
                                     float *K32, const uint32_t *__restrict__ dof, uint64_t nc) {
     for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < nc;
          k += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t j = dof[k];
-        const uint64_t idx = (uint64_t)bdiag[j / 3] * 9 + 4 * (j % 3);
+        const uint32_t j = dof[k], I = j / 3, rb = bptr[I];
+        const uint64_t idx = kidx(rb, bptr[I + 1] - rb, bdiag[I] - rb, 4 * (j % 3));
         K32[idx] = (float)K64[idx];
     }
 }
@@ -115,8 +135,8 @@ void apply_penalty(lmtg_ctx *c, bool mat, bool vec) {
     } else if (mat) {
         // max|diag| of the freshly assembled K, before any constraint (formulation.h:1029-1030)
         LMTG_CUDA(cudaMemsetAsync(md.p, 0, sizeof(unsigned long long), c->stream));
-        if (c->have64) k_max_diag<double><<<grid_for(c, c->nn, T), T, 0, c->stream>>>(c->bdiag.p, c->K64.p, c->nn, md.p);
-        else k_max_diag<float><<<grid_for(c, c->nn, T), T, 0, c->stream>>>(c->bdiag.p, c->K32.p, c->nn, md.p);
+        if (c->have64) k_max_diag<double><<<grid_for(c, c->nn, T), T, 0, c->stream>>>(c->bptr.p, c->bdiag.p, c->K64.p, c->nn, md.p);
+        else k_max_diag<float><<<grid_for(c, c->nn, T), T, 0, c->stream>>>(c->bptr.p, c->bdiag.p, c->K32.p, c->nn, md.p);
     } else {
         // vector-only assembly reuses the max|diag| of the last matrix assembly
         unsigned long long bits;
@@ -125,12 +145,12 @@ void apply_penalty(lmtg_ctx *c, bool mat, bool vec) {
     }
     const int g = grid_for(c, c->nc, T);
     if (c->have64) {
-        k_penalty<double><<<g, T, 0, c->stream>>>(c->bdiag.p, c->K64.p, c->F.p, c->cdof.p, c->ccoef.p,
+        k_penalty<double><<<g, T, 0, c->stream>>>(c->bptr.p, c->bdiag.p, c->K64.p, c->F.p, c->cdof.p, c->ccoef.p,
                                                   c->cres.p, c->nc, c->penalty, md.p, mat, vec);
         if (mat && c->have32)
-            k_round_constrained<<<g, T, 0, c->stream>>>(c->bdiag.p, c->K64.p, c->K32.p, c->cdof.p, c->nc);
+            k_round_constrained<<<g, T, 0, c->stream>>>(c->bptr.p, c->bdiag.p, c->K64.p, c->K32.p, c->cdof.p, c->nc);
     } else {
-        k_penalty<float><<<g, T, 0, c->stream>>>(c->bdiag.p, c->K32.p, c->F.p, c->cdof.p, c->ccoef.p,
+        k_penalty<float><<<g, T, 0, c->stream>>>(c->bptr.p, c->bdiag.p, c->K32.p, c->F.p, c->cdof.p, c->ccoef.p,
                                                  c->cres.p, c->nc, c->penalty, md.p, mat, vec);
     }
     LMTG_CUDA(cudaGetLastError());
@@ -145,13 +165,13 @@ void apply_penalty(lmtg_ctx *c, bool mat, bool vec) {
 
 // ---- block-Jacobi preconditioner: inverse of every 3x3 diagonal block ----
 template <class TK>
-__global__ void k_block_jacobi(const uint32_t *__restrict__ bdiag, const TK *__restrict__ K,
-                               uint64_t nn, double *D64, float *D32) {
+__global__ void k_block_jacobi(const uint32_t *__restrict__ bptr, const uint32_t *__restrict__ bdiag,
+                               const TK *__restrict__ K, uint64_t nn, double *D64, float *D32) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nn;
          i += (uint64_t)gridDim.x * blockDim.x) {
-        const TK *a = K + (uint64_t)bdiag[i] * 9;
+        const uint32_t rb = bptr[i], deg = bptr[i + 1] - rb, d = bdiag[i] - rb;
         double m[9];
-        for (int k = 0; k < 9; ++k) m[k] = (double)a[k];
+        for (int k = 0; k < 9; ++k) m[k] = (double)K[kidx(rb, deg, d, k)];
         double c00 = m[4] * m[8] - m[5] * m[7], c01 = m[5] * m[6] - m[3] * m[8],
                c02 = m[3] * m[7] - m[4] * m[6];
         double det = m[0] * c00 + m[1] * c01 + m[2] * c02;
@@ -170,11 +190,11 @@ void build_block_jacobi(lmtg_ctx *c, bool want64, bool want32) {
     const int T = 256;
     const int g = grid_for(c, c->nn, T);
     if (c->have64)
-        k_block_jacobi<double><<<g, T, 0, c->stream>>>(c->bdiag.p, c->K64.p, c->nn,
+        k_block_jacobi<double><<<g, T, 0, c->stream>>>(c->bptr.p, c->bdiag.p, c->K64.p, c->nn,
                                                        want64 ? c->Dinv64.p : nullptr,
                                                        want32 ? c->Dinv32.p : nullptr);
     else
-        k_block_jacobi<float><<<g, T, 0, c->stream>>>(c->bdiag.p, c->K32.p, c->nn, nullptr,
+        k_block_jacobi<float><<<g, T, 0, c->stream>>>(c->bptr.p, c->bdiag.p, c->K32.p, c->nn, nullptr,
                                                       want32 ? c->Dinv32.p : nullptr);
     LMTG_CUDA(cudaGetLastError());
     c->launches += 1;

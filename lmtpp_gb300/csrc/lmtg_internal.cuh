@@ -9,7 +9,8 @@
 //                                                                  sum into it, element order
 //   Ke64/Ke32[ne*npairs*9]                                         element matrices, upper node
 //                                                                  pairs (a<=b), 3x3 row-major
-//   K64/K32[nnzb*9]                                                assembled matrix, BSR 3x3
+//   K64/K32[nnzb*9]                                                assembled matrix, 3x3 node
+//                                                                  blocks, planar per row (kidx)
 //   F, u [n] f64                                                   load vector, solution
 //   Dinv64/Dinv32[nn*9]                                            block-Jacobi inverses
 #pragma once
@@ -189,6 +190,13 @@ __device__ __forceinline__ T warp_max(T v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
     return v;
+}
+
+// Position of component v (0..8, row-major 3x3) of local block b of a node row that starts at
+// block rb and has deg blocks.  Rows are stored planar: the deg values of each component are
+// contiguous, so lane b of a warp reads component v of its block with one coalesced load.
+__host__ __device__ __forceinline__ uint64_t kidx(uint32_t rb, uint32_t deg, uint32_t b, int v) {
+    return 9ull * rb + (uint64_t)v * deg + b;
 }
 
 // Upper node-pair index of (a, b), a <= b, among npe nodes.

@@ -115,47 +115,10 @@ __device__ __forceinline__ void bsr3_row(const uint32_t *__restrict__ bcol, cons
     a2 = warp_sum(a2);
 }
 
-// Row product of node row I, one 3x3 block per lane.  The warp first loads up to 32 blocks of
-// the row (9 values each) with coalesced loads into a per-warp shared buffer while every lane
-// fetches its block's column index and the 3 x values it needs -- all loads independent, so a
-// warp keeps ~12 requests in flight.  Lane b then multiplies block b (stride-9 shared reads are
-// bank-conflict free) and the three row sums are combined with a reduce-scatter (6 shuffles
-// instead of 3 x 5).  Returns in every lane the total of output component (lane >> 3) & 3
-// (lanes 0, 8, 16 hold rows 3I, 3I+1, 3I+2).
-template <class T, class XF>
-__device__ __forceinline__ T bsr3_row_lanes(const uint32_t *__restrict__ bcol,
-                                            const T *__restrict__ K, uint32_t rb, uint32_t re,
-                                            int lane, T *buf, XF xf) {
-    T a0 = (T)0, a1 = (T)0, a2 = (T)0;
-    for (uint32_t cb = rb; cb < re; cb += 32) {
-        const uint32_t nb = min(32u, re - cb);
-        const uint32_t nv = nb * 9;
-        const T *src = K + (uint64_t)cb * 9;
-        T v[9];
-#pragma unroll
-        for (int k = 0; k < 9; ++k) {
-            const uint32_t i = lane + 32 * k;
-            v[k] = i < nv ? __ldg(src + i) : (T)0;
-        }
-        T x0 = (T)0, x1 = (T)0, x2 = (T)0;
-        if ((uint32_t)lane < nb) {
-            const uint64_t j = 3 * (uint64_t)__ldg(bcol + cb + lane);
-            x0 = xf(j);
-            x1 = xf(j + 1);
-            x2 = xf(j + 2);
-        }
-        __syncwarp();
-#pragma unroll
-        for (int k = 0; k < 9; ++k) buf[lane + 32 * k] = v[k];
-        __syncwarp();
-        if ((uint32_t)lane < nb) {
-            const T *m = buf + 9 * lane;
-            a0 = fma(m[0], x0, a0); a0 = fma(m[1], x1, a0); a0 = fma(m[2], x2, a0);
-            a1 = fma(m[3], x0, a1); a1 = fma(m[4], x1, a1); a1 = fma(m[5], x2, a1);
-            a2 = fma(m[6], x0, a2); a2 = fma(m[7], x1, a2); a2 = fma(m[8], x2, a2);
-        }
-    }
-    // reduce-scatter of (a0, a1, a2, 0) over the warp
+// Reduce-scatter of (a0, a1, a2, 0) over the warp: returns in every lane the total of
+// component (lane >> 3) & 3 (lanes 0, 8, 16 hold rows 3I, 3I+1, 3I+2); 6 shuffles instead of 15.
+template <class T>
+__device__ __forceinline__ T reduce_scatter3(T a0, T a1, T a2, int lane) {
     const bool hi16 = (lane & 16) != 0, hi8 = (lane & 8) != 0;
     const T s0 = hi16 ? a0 : a2, s1 = hi16 ? a1 : (T)0;
     const T k0 = hi16 ? a2 : a0, k1 = hi16 ? (T)0 : a1;
@@ -168,7 +131,37 @@ __device__ __forceinline__ T bsr3_row_lanes(const uint32_t *__restrict__ bcol,
     return c;
 }
 
-constexpr int kRowBuf = 288;  // per-warp shared buffer: 32 blocks x 9 values
+// 3x3 block times a node vector, accumulated into (a0, a1, a2).
+template <class T>
+__device__ __forceinline__ void block_fma(const T (&m)[9], T x0, T x1, T x2, T &a0, T &a1, T &a2) {
+    a0 = fma(m[0], x0, a0); a0 = fma(m[1], x1, a0); a0 = fma(m[2], x2, a0);
+    a1 = fma(m[3], x0, a1); a1 = fma(m[4], x1, a1); a1 = fma(m[5], x2, a1);
+    a2 = fma(m[6], x0, a2); a2 = fma(m[7], x1, a2); a2 = fma(m[8], x2, a2);
+}
+
+// Row product of node row I (any number of blocks), one 3x3 block per lane.  Rows are stored
+// planar (kidx): lane b reads component k of its block at 9 rb + k deg + b, so each of the 9
+// loads is one coalesced warp access straight into registers.  xnode(J, x0, x1, x2) fetches
+// the three x values of node J.  Returns the reduce_scatter3 layout.
+template <class T, class XN>
+__device__ __forceinline__ T bsr3_row_lanes(const uint32_t *__restrict__ bcol,
+                                            const T *__restrict__ K, uint32_t rb, uint32_t re,
+                                            int lane, XN xnode) {
+    const uint32_t deg = re - rb;
+    T a0 = (T)0, a1 = (T)0, a2 = (T)0;
+    for (uint32_t b0 = 0; b0 < deg; b0 += 32) {
+        const uint32_t bl = b0 + lane;
+        if (bl < deg) {
+            T m[9];
+#pragma unroll
+            for (int k = 0; k < 9; ++k) m[k] = __ldg(K + kidx(rb, deg, bl, k));
+            T x0, x1, x2;
+            xnode(__ldg(bcol + rb + bl), x0, x1, x2);
+            block_fma(m, x0, x1, x2, a0, a1, a2);
+        }
+    }
+    return reduce_scatter3(a0, a1, a2, lane);
+}
 
 // Node vectors gathered by the SpMV (z, p) are stored with a stride VS per node: 3 (packed) or
 // 4 (FP32, padded so that a node's three components are one aligned 16-byte load).
@@ -191,66 +184,16 @@ struct NodeVec<float, 4> {
     }
 };
 
-// Pieces of bsr3_row_lanes for rows of at most 32 blocks, so that a warp can issue the loads of
-// two rows before it consumes either (twice the requests in flight).
-template <class T, class XF>
-__device__ __forceinline__ void bsr3_load32(const uint32_t *__restrict__ bcol,
-                                            const T *__restrict__ K, uint32_t rb, uint32_t nb,
-                                            int lane, XF xf, T (&v)[9], T &x0, T &x1, T &x2) {
-    const uint32_t nv = nb * 9;
-    const T *src = K + (uint64_t)rb * 9;
-#pragma unroll
-    for (int k = 0; k < 9; ++k) {
-        const uint32_t i = lane + 32 * k;
-        v[k] = i < nv ? __ldg(src + i) : (T)0;
-    }
-    x0 = x1 = x2 = (T)0;
-    if ((uint32_t)lane < nb) {
-        const uint64_t j = 3 * (uint64_t)__ldg(bcol + rb + lane);
-        x0 = xf(j);
-        x1 = xf(j + 1);
-        x2 = xf(j + 2);
-    }
-}
-
-template <class T>
-__device__ __forceinline__ T bsr3_mul32(T *buf, const T (&v)[9], T x0, T x1, T x2, uint32_t nb,
-                                        int lane) {
-    T a0 = (T)0, a1 = (T)0, a2 = (T)0;
-    __syncwarp();
-#pragma unroll
-    for (int k = 0; k < 9; ++k) buf[lane + 32 * k] = v[k];
-    __syncwarp();
-    if ((uint32_t)lane < nb) {
-        const T *m = buf + 9 * lane;
-        a0 = fma(m[0], x0, a0); a0 = fma(m[1], x1, a0); a0 = fma(m[2], x2, a0);
-        a1 = fma(m[3], x0, a1); a1 = fma(m[4], x1, a1); a1 = fma(m[5], x2, a1);
-        a2 = fma(m[6], x0, a2); a2 = fma(m[7], x1, a2); a2 = fma(m[8], x2, a2);
-    }
-    const bool hi16 = (lane & 16) != 0, hi8 = (lane & 8) != 0;
-    const T s0 = hi16 ? a0 : a2, s1 = hi16 ? a1 : (T)0;
-    const T k0 = hi16 ? a2 : a0, k1 = hi16 ? (T)0 : a1;
-    const T b0 = k0 + __shfl_xor_sync(0xffffffffu, s0, 16);
-    const T b1 = k1 + __shfl_xor_sync(0xffffffffu, s1, 16);
-    T c = (hi8 ? b1 : b0) + __shfl_xor_sync(0xffffffffu, hi8 ? b0 : b1, 8);
-    c += __shfl_xor_sync(0xffffffffu, c, 4);
-    c += __shfl_xor_sync(0xffffffffu, c, 2);
-    c += __shfl_xor_sync(0xffffffffu, c, 1);
-    return c;
-}
-
 // y = K x
 template <class T>
 __global__ void __launch_bounds__(kRowThreads)
     k_spmv(const uint32_t *__restrict__ bptr, const uint32_t *__restrict__ bcol,
            const T *__restrict__ K, const T *__restrict__ x, T *__restrict__ y, uint64_t nn) {
-    __shared__ T sbuf[kRowThreads / 32][kRowBuf];
     const int lane = threadIdx.x & 31;
-    T *buf = sbuf[threadIdx.x >> 5];
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     for (uint64_t I = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; I < nn; I += nw) {
-        const T v = bsr3_row_lanes(bcol, K, bptr[I], bptr[I + 1], lane, buf,
-                                   [&](uint64_t j) { return __ldg(x + j); });
+        const T v = bsr3_row_lanes(bcol, K, bptr[I], bptr[I + 1], lane,
+                                   [&](uint64_t J, T &a, T &b, T &c) { NodeVec<T, 3>::load(x, J, a, b, c); });
         if ((lane & 7) == 0 && lane < 24) y[3 * I + (lane >> 3)] = v;
     }
 }
@@ -262,14 +205,12 @@ __global__ void __launch_bounds__(kRowThreads)
                const T *__restrict__ K, const T *__restrict__ x, const T *__restrict__ b,
                T *__restrict__ r, uint64_t nn, double *partials, unsigned *ticket,
                double *rr_out) {
-    __shared__ T sbuf[kRowThreads / 32][kRowBuf];
     const int lane = threadIdx.x & 31;
-    T *buf = sbuf[threadIdx.x >> 5];
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     double v[1] = {0.0};
     for (uint64_t I = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; I < nn; I += nw) {
-        const T a = bsr3_row_lanes(bcol, K, bptr[I], bptr[I + 1], lane, buf,
-                                   [&](uint64_t j) { return __ldg(x + j); });
+        const T a = bsr3_row_lanes(bcol, K, bptr[I], bptr[I + 1], lane,
+                                   [&](uint64_t J, T &p, T &q, T &w) { NodeVec<T, 3>::load(x, J, p, q, w); });
         if ((lane & 7) == 0 && lane < 24) {
             const uint64_t i = 3 * I + (lane >> 3);
             const T ri = b[i] - a;
@@ -335,16 +276,8 @@ __global__ void __launch_bounds__(kRowThreads)
                T *__restrict__ pnew, T *__restrict__ q, uint64_t nn, PcgScalars *S,
                double *partials) {
     if (*(volatile int *)&S->done) return;
-    __shared__ T sbuf[kRowThreads / 32][kRowBuf];
     const T beta = (T)S->beta;
     const int lane = threadIdx.x & 31;
-    T *buf = sbuf[threadIdx.x >> 5];
-    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    // x value of column DOF j = 3J + c (generic path) and of a whole node J (fast path)
-    auto xf = [&](uint64_t j) {
-        const uint64_t J = j / 3, cc = j - 3 * J;
-        return fma(beta, __ldg(pold + VS * J + cc), __ldg(z + VS * J + cc));
-    };
     auto xnode = [&](uint64_t J, T &a, T &b, T &c) {
         T za, zb, zc, pa, pb, pc;
         NodeVec<T, VS>::load(z, J, za, zb, zc);
@@ -364,8 +297,8 @@ __global__ void __launch_bounds__(kRowThreads)
         }
     };
     // Each block owns a contiguous range of rows (neighbouring rows gather mostly the same
-    // x entries, so the range's gathers hit L1); each warp takes two adjacent rows per step.
-    (void)nw;
+    // x entries, so the range's gathers hit L1); each warp takes two adjacent rows per step and
+    // issues both rows' matrix loads and column indices before the dependent x gathers.
     const uint64_t per_block = (nn + gridDim.x - 1) / gridDim.x;
     const uint64_t row0 = blockIdx.x * per_block;
     const uint64_t row_end = min(nn, row0 + per_block);
@@ -374,30 +307,30 @@ __global__ void __launch_bounds__(kRowThreads)
         const uint64_t I1 = I + 1;
         const uint32_t rb0 = bptr[I], re0 = bptr[I + 1];
         const uint32_t rb1 = I1 < row_end ? bptr[I1] : 0u, re1 = I1 < row_end ? bptr[I1 + 1] : 0u;
-        if (re0 - rb0 <= 32 && re1 - rb1 <= 32) {
-            // issue order: both rows' matrix values and column indices first (independent),
-            // then the dependent x gathers, then the products
-            const uint32_t nb0 = re0 - rb0, nb1 = re1 - rb1;
-            T v0[9], v1[9];
-            const T *s0 = K + (uint64_t)rb0 * 9, *s1 = K + (uint64_t)rb1 * 9;
+        const uint32_t d0 = re0 - rb0, d1 = re1 - rb1;
+        if (d0 <= 32 && d1 <= 32) {
+            T m0[9], m1[9];
+            const bool on0 = (uint32_t)lane < d0, on1 = (uint32_t)lane < d1;
 #pragma unroll
             for (int k = 0; k < 9; ++k) {
-                const uint32_t i = lane + 32 * k;
-                v0[k] = i < nb0 * 9 ? __ldg(s0 + i) : (T)0;
-                v1[k] = i < nb1 * 9 ? __ldg(s1 + i) : (T)0;
+                m0[k] = on0 ? __ldg(K + kidx(rb0, d0, lane, k)) : (T)0;
+                m1[k] = on1 ? __ldg(K + kidx(rb1, d1, lane, k)) : (T)0;
             }
-            const uint32_t j0 = (uint32_t)lane < nb0 ? __ldg(bcol + rb0 + lane) : 0u;
-            const uint32_t j1 = (uint32_t)lane < nb1 ? __ldg(bcol + rb1 + lane) : 0u;
+            const uint32_t j0 = on0 ? __ldg(bcol + rb0 + lane) : 0u;
+            const uint32_t j1 = on1 ? __ldg(bcol + rb1 + lane) : 0u;
             T x00 = 0, x01 = 0, x02 = 0, x10 = 0, x11 = 0, x12 = 0;
-            if ((uint32_t)lane < nb0) xnode(j0, x00, x01, x02);
-            if ((uint32_t)lane < nb1) xnode(j1, x10, x11, x12);
-            const T q0 = bsr3_mul32(buf, v0, x00, x01, x02, re0 - rb0, lane);
-            const T q1 = bsr3_mul32(buf, v1, x10, x11, x12, re1 - rb1, lane);
+            if (on0) xnode(j0, x00, x01, x02);
+            if (on1) xnode(j1, x10, x11, x12);
+            T a00 = 0, a01 = 0, a02 = 0, a10 = 0, a11 = 0, a12 = 0;
+            block_fma(m0, x00, x01, x02, a00, a01, a02);
+            block_fma(m1, x10, x11, x12, a10, a11, a12);
+            const T q0 = reduce_scatter3(a00, a01, a02, lane);
+            const T q1 = reduce_scatter3(a10, a11, a12, lane);
             finish(I, q0);
             if (I1 < row_end) finish(I1, q1);
         } else {
-            finish(I, bsr3_row_lanes(bcol, K, rb0, re0, lane, buf, xf));
-            if (I1 < row_end) finish(I1, bsr3_row_lanes(bcol, K, rb1, re1, lane, buf, xf));
+            finish(I, bsr3_row_lanes(bcol, K, rb0, re0, lane, xnode));
+            if (I1 < row_end) finish(I1, bsr3_row_lanes(bcol, K, rb1, re1, lane, xnode));
         }
     }
     const T tacc[1] = {acc};
