@@ -39,7 +39,8 @@ extern "C" {
 #define LMTG_ERR_UNSUPPORTED 8   /* element type / size not supported */
 
 /* ---- element types (nodes per element) ---- */
-#define LMTG_ELEM_HEXA8 8
+#define LMTG_ELEM_HEXA8 8    /* faces: Quad4 (4 node ids) */
+#define LMTG_ELEM_TETRA10 10 /* faces: Triangle_6 (6 node ids: vertices, then mid-edges 01 12 20) */
 
 /* ---- lmtg_assemble flags ---- */
 #define LMTG_ASM_MAT64 1        /* FP64 element matrices -> FP64 K */
@@ -87,6 +88,15 @@ const char *lmtg_status_string(int status);
 int lmtg_make_rect_hexa(const double X0[3], const double X1[3], const uint32_t nb_points[3],
                         double *pos, uint32_t *conn);
 
+/* Structured unit-box Tetra_10 mesh on the host, identical to
+ * make_rect(m, Tetra_10(), X0, X1, nb_points) (include/mesh/make_rect.h:443-545): 6 tetrahedra
+ * per cube, nodes in first-creation order (the reference's distance search replaced by exact
+ * half-grid coordinates: same order, same stored positions), negative-Jacobian tetrahedra
+ * renumbered as permutation_if_jac_neg (include/mesh/element_Tetra_10.h:122-130).
+ * Two-phase: with pos or conn NULL only *nn and *ne are written. */
+int lmtg_make_rect_tetra10(const double X0[3], const double X1[3], const uint32_t nb_points[3],
+                           uint64_t *nn, uint64_t *ne, double *pos, uint32_t *conn);
+
 /* Mesh (the TM object a Formulation points to, formulation.h:2740-2745): node positions
  * (nn*3), element connectivity (ne*nodes_per_element), DOF numbering node*3 as the reference's
  * default indice_noda (formulation.h:283-325, no AMD/RCM renumbering). */
@@ -104,8 +114,10 @@ int lmtg_allocate_matrices(lmtg_ctx *ctx, uint64_t *nnz_lower);
 
 /* Nodal loads f_nodal (n = 3*nn doubles), replacing the current nodal load vector. */
 int lmtg_set_nodal_loads(lmtg_ctx *ctx, const double *F);
-/* Uniform traction f_surf on Quad4 skin faces (nfaces*4 node ids), accumulated into the load
- * vector as consistent nodal loads (the add_skin_elem_matrix terms, formulation.h:584-594). */
+/* Uniform traction f_surf on skin faces (Quad4 for Hexa8 meshes: nfaces*4 node ids; Triangle_6
+ * for Tetra10 meshes: nfaces*6), accumulated into the load vector as consistent nodal loads (the
+ * add_skin_elem_matrix terms, formulation.h:584-594; order-2 rules of element_Quad.h /
+ * element_Triangle_6.h). */
 int lmtg_add_skin_traction(lmtg_ctx *ctx, uint64_t nfaces, const uint32_t *faces,
                            const double traction[3]);
 
@@ -123,7 +135,8 @@ int lmtg_assemble(lmtg_ctx *ctx, int flags);
 int lmtg_get_matrix_lower(lmtg_ctx *ctx, uint64_t *rowptr, uint32_t *col, double *val);
 /* get_sollicitation: the assembled right-hand side (n doubles). */
 int lmtg_get_sollicitation(lmtg_ctx *ctx, double *F);
-/* Element matrices of elements [e0, e0+count) as dense row-major 24x24 (test/inspection). */
+/* Element matrices of elements [e0, e0+count) as dense row-major (3 npe) x (3 npe) blocks
+ * (24x24 Hexa8, 30x30 Tetra10), for tests and inspection. */
 int lmtg_get_element_matrices(lmtg_ctx *ctx, int precision, uint64_t e0, uint64_t count,
                               double *Ke);
 

@@ -5,6 +5,8 @@ this package holds its in-tree build, the ctypes binding and the Python mirror o
 Formulation API.
 """
 from . import abi
-from .formulation import Formulation, make_rect_hexa, x1_faces_hexa
+from .formulation import (Formulation, make_rect_hexa, make_rect_tetra10, x1_faces, x1_faces_hexa,
+                          x1_faces_tetra10)
 
-__all__ = ["abi", "Formulation", "make_rect_hexa", "x1_faces_hexa"]
+__all__ = ["abi", "Formulation", "make_rect_hexa", "make_rect_tetra10", "x1_faces", "x1_faces_hexa",
+           "x1_faces_tetra10"]

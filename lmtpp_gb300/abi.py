@@ -12,7 +12,7 @@ HEADER = os.path.join(os.path.dirname(HERE), "include", "lmtg.h")
 
 OK = 0
 ERR_ARG, ERR_CUDA, ERR_STATE, ERR_NOT_CONVERGED, ERR_TIMEOUT, ERR_NAN, ERR_NOMEM, ERR_UNSUPPORTED = range(1, 9)
-ELEM_HEXA8 = 8
+ELEM_HEXA8, ELEM_TETRA10 = 8, 10
 ASM_MAT64, ASM_MAT32, ASM_VEC, ASM_MAT32_NATIVE = 1, 2, 4, 8
 SOLVE_PCG_F64, SOLVE_MIXED_IR = 0, 1
 CRIT_REL_RESIDUAL, CRIT_NORM_INF_DELTA, CRIT_NORM2_DELTA, CRIT_ABS_RESIDUAL_INF = 0, 1, 2, 3
@@ -41,6 +41,7 @@ _SIGS = {
     "lmtg_last_error": (_cp, [_vp]),
     "lmtg_status_string": (_cp, [_i]),
     "lmtg_make_rect_hexa": (_i, [_vp, _vp, _vp, _vp, _vp]),
+    "lmtg_make_rect_tetra10": (_i, [_vp, _vp, _vp, ctypes.POINTER(_u64), ctypes.POINTER(_u64), _vp, _vp]),
     "lmtg_mesh_set": (_i, [_vp, _i, _u64, _vp, _u64, _vp]),
     "lmtg_material_set": (_i, [_vp, _vp, _u64, _d]),
     "lmtg_allocate_matrices": (_i, [_vp, ctypes.POINTER(_u64)]),

@@ -67,6 +67,30 @@ void quad4_loads(const double *pos, const uint32_t *q, const double t[3], double
     }
 }
 
+// Triangle_6 consistent loads of a uniform traction, order-2 rule of the reference table
+// (include/mesh/element_Triangle_6.h:5-15: 3 edge-midpoint points, weights 1/6).
+void tri6_loads(const double *pos, const uint32_t *q, const double t[3], double *F) {
+    const double gp[3][2] = {{0.5, 0.0}, {0.5, 0.5}, {0.0, 0.5}};
+    for (int g = 0; g < 3; ++g) {
+        const double u = gp[g][0], v = gp[g][1], X0 = 1 - u - v;
+        const double N[6] = {X0 * (2 * X0 - 1), u * (2 * u - 1), v * (2 * v - 1),
+                             4 * X0 * u,        4 * u * v,       4 * v * X0};
+        const double du[6] = {-(4 * X0 - 1), 4 * u - 1, 0, 4 * (X0 - u), 4 * v, -4 * v};
+        const double dv[6] = {-(4 * X0 - 1), 0, 4 * v - 1, -4 * u, 4 * u, 4 * (X0 - v)};
+        double tu[3] = {0, 0, 0}, tv[3] = {0, 0, 0};
+        for (int a = 0; a < 6; ++a)
+            for (int d = 0; d < 3; ++d) {
+                tu[d] += pos[3 * (uint64_t)q[a] + d] * du[a];
+                tv[d] += pos[3 * (uint64_t)q[a] + d] * dv[a];
+            }
+        const double nx = tu[1] * tv[2] - tu[2] * tv[1], ny = tu[2] * tv[0] - tu[0] * tv[2],
+                     nz = tu[0] * tv[1] - tu[1] * tv[0];
+        const double ds = std::sqrt(nx * nx + ny * ny + nz * nz) * 0.16666666666666666667;
+        for (int a = 0; a < 6; ++a)
+            for (int d = 0; d < 3; ++d) F[3 * (uint64_t)q[a] + d] += N[a] * t[d] * ds;
+    }
+}
+
 }  // namespace
 
 extern "C" {
@@ -171,23 +195,100 @@ int lmtg_make_rect_hexa(const double X0[3], const double X1[3], const uint32_t n
     return LMTG_OK;
 }
 
+int lmtg_make_rect_tetra10(const double X0_[3], const double X1_[3], const uint32_t nbp[3],
+                           uint64_t *nn_out, uint64_t *ne_out, double *pos, uint32_t *conn) {
+    if (!X0_ || !X1_ || !nbp || !nn_out || !ne_out) return LMTG_ERR_ARG;
+    // vertex positions of the reference element and the 6 tetrahedra of a cube: translation (in
+    // units of incr) and basis columns, as make_rect.h:466-543
+    static const double rela[10][3] = {{0, 0, 0},     {1, 0, 0},     {0, 1, 0},   {0, 0, 1},
+                                       {0.5, 0, 0},   {0.5, 0.5, 0}, {0, 0.5, 0}, {0, 0, 0.5},
+                                       {0.5, 0, 0.5}, {0, 0.5, 0.5}};
+    static const int trs[6][3] = {{0, 0, 0}, {1, 1, 0}, {1, 0, 0}, {1, 0, 1}, {1, 1, 0}, {1, 1, 1}};
+    static const int bas[6][3][3] = {{{1, 0, 0}, {0, 1, 0}, {0, 0, 1}},
+                                     {{-1, 0, 0}, {0, -1, 0}, {0, -1, 1}},
+                                     {{-1, 0, 1}, {-1, 1, 0}, {0, 0, 1}},
+                                     {{-1, 0, 0}, {-1, 1, 0}, {-1, 1, -1}},
+                                     {{-1, 0, 0}, {-1, 0, 1}, {0, -1, 1}},
+                                     {{-1, 0, 0}, {0, -1, 0}, {0, 0, -1}}};
+    static const int perm[10] = {0, 1, 3, 2, 4, 8, 7, 6, 5, 9};
+    uint64_t ne3[3];
+    double X0[3], incr[3];
+    for (int d = 0; d < 3; ++d) {
+        if (nbp[d] < 2) return LMTG_ERR_ARG;
+        X0[d] = std::fmin(X0_[d], X1_[d]);
+        const double x1 = std::fmax(X0_[d], X1_[d]);
+        ne3[d] = nbp[d] - 1;
+        incr[d] = (x1 - X0[d]) / (double)ne3[d];
+    }
+    const uint64_t gx = 2 * ne3[0] + 1, gy = 2 * ne3[1] + 1, gz = 2 * ne3[2] + 1;
+    const uint64_t nn = gx * gy * gz, ne = 6 * ne3[0] * ne3[1] * ne3[2];
+    if (nn >= (1ull << 32)) return LMTG_ERR_UNSUPPORTED;
+    *nn_out = nn;
+    *ne_out = ne;
+    if (!pos || !conn) return LMTG_OK;
+    std::vector<uint32_t> id(nn, 0xffffffffu);
+    uint32_t next = 0;
+    uint64_t e = 0;
+    for (uint64_t i = 0; i < ne3[2]; ++i)
+        for (uint64_t j = 0; j < ne3[1]; ++j)
+            for (uint64_t k = 0; k < ne3[0]; ++k) {
+                const double O[3] = {X0[0] + k * incr[0], X0[1] + j * incr[1], X0[2] + i * incr[2]};
+                const uint64_t kk[3] = {k, j, i};
+                for (int s = 0; s < 6; ++s) {
+                    uint32_t vn[10];
+                    for (int t = 0; t < 10; ++t) {
+                        double p[3];
+                        int64_t g[3];
+                        for (int r = 0; r < 3; ++r) {
+                            const double w = bas[s][0][r] * rela[t][0] + bas[s][1][r] * rela[t][1] +
+                                             bas[s][2][r] * rela[t][2];
+                            const double base = s == 0 ? O[r] : O[r] + trs[s][r] * incr[r];
+                            p[r] = base + incr[r] * w;
+                            g[r] = 2 * (int64_t)kk[r] + 2 * trs[s][r] + (int64_t)std::llround(2 * w);
+                        }
+                        const uint64_t key = ((uint64_t)g[2] * gy + (uint64_t)g[1]) * gx + (uint64_t)g[0];
+                        if (id[key] == 0xffffffffu) {
+                            id[key] = next;
+                            for (int r = 0; r < 3; ++r) pos[3ull * next + r] = p[r];
+                            ++next;
+                        }
+                        vn[t] = id[key];
+                    }
+                    double a[3], b[3], cc[3];
+                    for (int r = 0; r < 3; ++r) {
+                        a[r] = pos[3ull * vn[1] + r] - pos[3ull * vn[0] + r];
+                        b[r] = pos[3ull * vn[2] + r] - pos[3ull * vn[0] + r];
+                        cc[r] = pos[3ull * vn[3] + r] - pos[3ull * vn[0] + r];
+                    }
+                    const double det = a[0] * (b[1] * cc[2] - b[2] * cc[1]) -
+                                       a[1] * (b[0] * cc[2] - b[2] * cc[0]) +
+                                       a[2] * (b[0] * cc[1] - b[1] * cc[0]);
+                    for (int t = 0; t < 10; ++t) conn[10 * e + t] = det < 0 ? vn[perm[t]] : vn[t];
+                    ++e;
+                }
+            }
+    return next == nn ? LMTG_OK : LMTG_ERR_ARG;
+}
+
 int lmtg_mesh_set(lmtg_ctx *c, int elem_type, uint64_t nn, const double *pos, uint64_t ne,
                   const uint32_t *conn) {
     return guard(c, [&] {
-        LMTG_CHECK(elem_type == LMTG_ELEM_HEXA8, LMTG_ERR_UNSUPPORTED, "element type not supported");
+        LMTG_CHECK(elem_type == LMTG_ELEM_HEXA8 || elem_type == LMTG_ELEM_TETRA10,
+                   LMTG_ERR_UNSUPPORTED, "element type not supported");
         LMTG_CHECK(pos && conn && nn > 0 && ne > 0, LMTG_ERR_ARG, "empty mesh");
         LMTG_CHECK(nn < (1ull << 32), LMTG_ERR_UNSUPPORTED, "more than 2^32 nodes");
+        const int npe = elem_type;
         c->elem_type = elem_type;
-        c->npe = 8;
+        c->npe = npe;
         c->nnu = 3;
-        c->npairs = 36;
+        c->npairs = npe * (npe + 1) / 2;
         c->nn = nn;
         c->ne = ne;
         c->n = 3 * nn;
         c->h_pos.assign(pos, pos + 3 * nn);
-        c->h_conn.assign(conn, conn + 8 * ne);
+        c->h_conn.assign(conn, conn + (uint64_t)npe * ne);
         upload(c, c->pos, pos, 3 * nn);
-        upload(c, c->conn, conn, 8 * ne);
+        upload(c, c->conn, conn, (uint64_t)npe * ne);
         // formulation defaults: elastic_modulus 1, poisson_ratio 0.33
         // (formulations/formulation_elasticity_iso.py:5-6)
         const double one = 1.0;
@@ -252,11 +353,14 @@ int lmtg_add_skin_traction(lmtg_ctx *c, uint64_t nfaces, const uint32_t *faces,
                            const double traction[3]) {
     return guard(c, [&] {
         LMTG_CHECK(c->n > 0 && traction && (nfaces == 0 || faces), LMTG_ERR_ARG, "bad faces");
+        const int fn = c->elem_type == LMTG_ELEM_HEXA8 ? 4 : 6;
         for (uint64_t f = 0; f < nfaces; ++f)
-            for (int a = 0; a < 4; ++a)
-                LMTG_CHECK(faces[4 * f + a] < c->nn, LMTG_ERR_ARG, "face node id >= nn");
-        for (uint64_t f = 0; f < nfaces; ++f)
-            quad4_loads(c->h_pos.data(), faces + 4 * f, traction, c->h_loads.data());
+            for (int a = 0; a < fn; ++a)
+                LMTG_CHECK(faces[fn * f + a] < c->nn, LMTG_ERR_ARG, "face node id >= nn");
+        for (uint64_t f = 0; f < nfaces; ++f) {
+            if (fn == 4) quad4_loads(c->h_pos.data(), faces + 4 * f, traction, c->h_loads.data());
+            else tri6_loads(c->h_pos.data(), faces + 6 * f, traction, c->h_loads.data());
+        }
         return LMTG_OK;
     });
 }

@@ -38,13 +38,13 @@ void do_assemble(lmtg_ctx *c, int flags) {
     if (flags & (LMTG_ASM_MAT64 | LMTG_ASM_MAT32)) {
         const bool want32 = (flags & LMTG_ASM_MAT32) != 0;
         const bool want64 = (flags & LMTG_ASM_MAT64) != 0 || true;  // the FP64 sum is kept
-        launch_hexa8_elast(c, true);
+        launch_elem_elast(c, true);
         assemble_matrix(c, true, want64, want32);
         c->have64 = true;
         c->have32 = want32;
     } else if (flags & LMTG_ASM_MAT32_NATIVE) {
         c->Ke32.alloc(c->ne * (uint64_t)c->npairs * 9);
-        launch_hexa8_elast(c, false);
+        launch_elem_elast(c, false);
         assemble_matrix(c, false, false, true);
         c->have64 = false;
         c->have32 = true;

@@ -8,51 +8,47 @@
 //   misfit      J = 1/2 sum_i w_i (u_i - t_i)^2   K lambda = w (u - t)   (one PCG solve)
 //   linear      J = c.u                      K lambda = c           (one PCG solve)
 //   dJ/dE_e = -lambda_e^T Khat_e u_e.
-// The element matrix is not stored: k_hexa8_grad_E recomputes the geometry per Gauss point
+// The element matrix is not stored: k_grad_E recomputes the geometry per Gauss point
 // and evaluates the bilinear form directly,
 //   a^T Khat_e b = sum_gp w detJ [lhat tr(A) tr(B) + mhat (A:B + tr(A B))],  A = grad a, B = grad b,
 // with lhat = nu / ((1+nu)(1-2nu)) and mhat = 1 / (2(1+nu)) (unit modulus), the same weak form
-// and Gauss rule as the element kernel (formulations/formulation_elasticity_iso.py:45-60,
-// include/mesh/element_Hexa.h:5-20).
+// and Gauss rules as the element kernel (formulations/formulation_elasticity_iso.py:45-60,
+// elem_traits.cuh).
 #include <cmath>
 #include <cstring>
 #include <exception>
 #include <new>
 
+#include "elem_traits.cuh"
 #include "solver_kernels.cuh"
 
 namespace lmtg {
 
+template <class EL>
 __global__ void __launch_bounds__(128)
-    k_hexa8_grad_E(const double *__restrict__ pos, const uint32_t *__restrict__ conn, double nu,
-                   uint64_t ne, const double *__restrict__ a, const double *__restrict__ b,
-                   double *__restrict__ g) {
-    const double ga = 0.211324865405, gb = 0.788675134595;  // reference Gauss table, order 2
+    k_grad_E(const double *__restrict__ pos, const uint32_t *__restrict__ conn, double nu,
+             uint64_t ne, const double *__restrict__ a, const double *__restrict__ b,
+             double *__restrict__ g) {
+    constexpr int NPE = EL::npe;
     const double lh = nu / ((1.0 + nu) * (1.0 - 2.0 * nu)), mh = 1.0 / (2.0 * (1.0 + nu));
     for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < ne;
          e += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t nd[8];
-        double xyz[8][3];
+        uint32_t nd[NPE];
+        double xyz[NPE][3];
 #pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            nd[k] = conn[8 * e + k];
+        for (int k = 0; k < NPE; ++k) {
+            nd[k] = conn[NPE * e + k];
 #pragma unroll
             for (int d = 0; d < 3; ++d) xyz[k][d] = pos[3ull * nd[k] + d];
         }
         double acc = 0.0;
 #pragma unroll 1
-        for (int gp = 0; gp < 8; ++gp) {
-            const double x = (gp == 1 || gp == 2 || gp == 5 || gp == 6) ? gb : ga;
-            const double y = (gp == 2 || gp == 3 || gp == 6 || gp == 7) ? gb : ga;
-            const double z = (gp >= 4) ? gb : ga;
-            const double mx = 1 - x, my = 1 - y, mz = 1 - z;
-            const double dN[8][3] = {{-my * mz, -mx * mz, -mx * my}, {my * mz, -x * mz, -x * my},
-                                     {y * mz, x * mz, -x * y},      {-y * mz, mx * mz, -mx * y},
-                                     {-my * z, -mx * z, mx * my},   {my * z, -x * z, x * my},
-                                     {y * z, x * z, x * y},         {-y * z, mx * z, mx * y}};
+        for (int gp = 0; gp < EL::ngp; ++gp) {
+            double dN[NPE][3];
+            EL::dN(gp, dN);
             double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
 #pragma unroll
-            for (int k = 0; k < 8; ++k)
+            for (int k = 0; k < NPE; ++k)
 #pragma unroll
                 for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -71,7 +67,7 @@ __global__ void __launch_bounds__(128)
                  (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id}};
             double A[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, B[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
 #pragma unroll
-            for (int k = 0; k < 8; ++k) {
+            for (int k = 0; k < NPE; ++k) {
                 double gr[3];
 #pragma unroll
                 for (int j = 0; j < 3; ++j)
@@ -93,16 +89,19 @@ __global__ void __launch_bounds__(128)
             for (int i = 0; i < 3; ++i)
 #pragma unroll
                 for (int j = 0; j < 3; ++j) ddot += A[i][j] * (B[i][j] + B[j][i]);
-            acc += 0.125 * det * (lh * trA * trB + mh * ddot);
+            acc += EL::template weight<double>(gp) * det * (lh * trA * trB + mh * ddot);
         }
         g[e] = -acc;
     }
 }
 
-void launch_hexa8_grad_E(lmtg_ctx *c, const double *a, const double *b, double *g) {
+void launch_grad_E(lmtg_ctx *c, const double *a, const double *b, double *g) {
     const int T = 128;
-    k_hexa8_grad_E<<<grid_for(c, c->ne, T, 16), T, 0, c->stream>>>(c->pos.p, c->conn.p, c->nu, c->ne,
-                                                                    a, b, g);
+    const int grid = grid_for(c, c->ne, T, 16);
+    if (c->elem_type == LMTG_ELEM_HEXA8)
+        k_grad_E<Hexa8><<<grid, T, 0, c->stream>>>(c->pos.p, c->conn.p, c->nu, c->ne, a, b, g);
+    else
+        k_grad_E<Tetra10><<<grid, T, 0, c->stream>>>(c->pos.p, c->conn.p, c->nu, c->ne, a, b, g);
     LMTG_CUDA(cudaGetLastError());
     c->launches += 1;
 }
@@ -245,7 +244,7 @@ int lmtg_adjoint_grad(lmtg_ctx *c, int objective, const double *target, const do
             }
             lam = c->adj_lam.p;
         }
-        launch_hexa8_grad_E(c, lam, c->u.p, c->grad.p);
+        launch_grad_E(c, lam, c->u.p, c->grad.p);
         if (objective == LMTG_OBJ_COMPLIANCE) {
             double jv = 0;
             LMTG_CUDA(cudaMemcpyAsync(&jv, &o->rr, 8, cudaMemcpyDeviceToHost, c->stream));

@@ -143,8 +143,8 @@ namespace lmtg {
 // ---- pattern (pattern.cu) ----
 void build_pattern(lmtg_ctx *c);
 
-// ---- element kernels (elem_hexa8.cu) ----
-void launch_hexa8_elast(lmtg_ctx *c, bool fp64);
+// ---- element kernels (elem_elast.cu) ----
+void launch_elem_elast(lmtg_ctx *c, bool fp64);
 
 // ---- assembly (assemble.cu) ----
 void assemble_matrix(lmtg_ctx *c, bool from64, bool want64, bool want32);
@@ -153,7 +153,7 @@ void build_block_jacobi(lmtg_ctx *c, bool want64, bool want32);
 void copy_k64_to_k32(lmtg_ctx *c);
 
 // ---- adjoint (adjoint.cu) ----
-void launch_hexa8_grad_E(lmtg_ctx *c, const double *a, const double *b, double *g);
+void launch_grad_E(lmtg_ctx *c, const double *a, const double *b, double *g);
 
 // ---- solver (solver.cu) ----
 void spmv64(lmtg_ctx *c, const double *x, double *y);

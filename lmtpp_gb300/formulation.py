@@ -53,6 +53,41 @@ def make_rect_hexa(nb_points, X0=(0.0, 0.0, 0.0), X1=(1.0, 1.0, 1.0)):
     return pos, conn
 
 
+def make_rect_tetra10(nb_points, X0=(0.0, 0.0, 0.0), X1=(1.0, 1.0, 1.0)):
+    """make_rect(m, Tetra_10(), X0, X1, nb_points) (include/mesh/make_rect.h:443-545) -> pos, conn."""
+    nbp = np.asarray(nb_points if np.ndim(nb_points) else [nb_points] * 3, dtype=np.uint32)
+    x0 = np.ascontiguousarray(X0, dtype=np.float64)
+    x1 = np.ascontiguousarray(X1, dtype=np.float64)
+    lib = abi.load()
+    nn, ne = ctypes.c_uint64(), ctypes.c_uint64()
+    abi.check(lib.lmtg_make_rect_tetra10(abi.ptr(x0), abi.ptr(x1), abi.ptr(nbp), ctypes.byref(nn),
+                                         ctypes.byref(ne), None, None), None, "make_rect_tetra10")
+    pos = np.zeros((nn.value, 3))
+    conn = np.zeros((ne.value, 10), dtype=np.uint32)
+    abi.check(lib.lmtg_make_rect_tetra10(abi.ptr(x0), abi.ptr(x1), abi.ptr(nbp), ctypes.byref(nn),
+                                         ctypes.byref(ne), abi.ptr(pos), abi.ptr(conn)), None,
+              "make_rect_tetra10")
+    return pos, conn
+
+
+# Tetra_10 children faces as Triangle_6 (formulations/element_Tetra_10.py:16-21)
+TETRA10_FACES = np.array([[0, 2, 1, 6, 5, 4], [0, 1, 3, 4, 8, 7], [0, 3, 2, 7, 9, 6],
+                          [1, 2, 3, 5, 9, 8]])
+
+
+def x1_faces_tetra10(pos, conn, x1=1.0, eps=1e-6):
+    """Triangle_6 skin faces of Tetra10 elements lying on the plane x = x1 (element order, then
+    child order)."""
+    q = conn[:, TETRA10_FACES]  # ne x 4 x 6
+    on = np.all(pos[q, 0] > x1 - eps, axis=2)
+    return np.ascontiguousarray(q[on], dtype=np.uint32)
+
+
+def x1_faces(pos, conn, x1=1.0, eps=1e-6):
+    """Skin faces on x = x1 for a Hexa8 (Quad4 faces) or Tetra10 (Triangle_6 faces) mesh."""
+    return x1_faces_hexa(pos, conn, x1, eps) if conn.shape[1] == 8 else x1_faces_tetra10(pos, conn, x1, eps)
+
+
 def x1_faces_hexa(pos, conn, x1=1.0, eps=1e-6):
     """Quad4 skin faces (Hexa child [1,2,6,5], formulations/element_Hexa.py:22-29) on x = x1."""
     q = conn[:, [1, 2, 6, 5]]
@@ -61,11 +96,15 @@ def x1_faces_hexa(pos, conn, x1=1.0, eps=1e-6):
 
 
 class Formulation:
-    """One elasticity_iso formulation on a Hexa8 mesh, resident on one GPU."""
+    """One elasticity_iso formulation on a Hexa8 or Tetra10 mesh (the element type follows from
+    the connectivity width), resident on one GPU."""
 
-    def __init__(self, pos, conn, device=0, elem="Hexa"):
-        if elem != "Hexa":
-            raise abi.LmtgError(abi.ERR_UNSUPPORTED, "element %s not supported" % elem)
+    def __init__(self, pos, conn, device=0):
+        conn = np.asarray(conn)
+        elem = {8: abi.ELEM_HEXA8, 10: abi.ELEM_TETRA10}.get(conn.shape[1])
+        if elem is None:
+            raise abi.LmtgError(abi.ERR_UNSUPPORTED, "elements with %d nodes are not supported" % conn.shape[1])
+        self.npe = conn.shape[1]
         self._lib = abi.load()
         self._ctx = ctypes.c_void_p()
         abi.check(self._lib.lmtg_create(device, ctypes.byref(self._ctx)), None, "lmtg_create")
@@ -73,7 +112,7 @@ class Formulation:
         self.conn = np.ascontiguousarray(conn, dtype=np.uint32)
         self.nn, self.ne = self.pos.shape[0], self.conn.shape[0]
         self.n = 3 * self.nn
-        abi.check(self._lib.lmtg_mesh_set(self._ctx, abi.ELEM_HEXA8, self.nn, abi.ptr(self.pos),
+        abi.check(self._lib.lmtg_mesh_set(self._ctx, elem, self.nn, abi.ptr(self.pos),
                                           self.ne, abi.ptr(self.conn)), self._ctx, "mesh_set")
         # formulation defaults (formulations/formulation_elasticity_iso.py:5-6)
         self._E = np.array([1.0])
@@ -228,7 +267,8 @@ class Formulation:
         return rowptr, col, val
 
     def element_matrices(self, e0=0, count=1, precision=0):
-        Ke = np.zeros((count, 24, 24))
+        nd = 3 * self.npe
+        Ke = np.zeros((count, nd, nd))
         abi.check(self._lib.lmtg_get_element_matrices(self._ctx, precision, e0, count, abi.ptr(Ke)),
                   self._ctx, "element matrices")
         return Ke

@@ -99,6 +99,30 @@ int orc_gauss_quad_order2(double *w, double *xi) {
     return 4;
 }
 
+/* Tetra_10 order 2: 4 points, weights 1/24 (include/mesh/element_Tetra_10.h:5-16; 16-digit
+ * abscissae), on the unit reference tetrahedron. */
+#define TA 0.1381966011250105
+#define TB 0.5854101966249685
+int orc_gauss_tetra_order2(double *w, double *xi) {
+    static const double t[4][3] = {{TA, TA, TA}, {TB, TA, TA}, {TA, TB, TA}, {TA, TA, TB}};
+    for (int g = 0; g < 4; ++g) {
+        w[g] = 0.041666666666666666667;
+        for (int d = 0; d < 3; ++d) xi[3 * g + d] = t[g][d];
+    }
+    return 4;
+}
+
+/* Triangle_6 order 2: 3 edge-midpoint points, weights 1/6 (include/mesh/element_Triangle_6.h:5-15). */
+int orc_gauss_triangle_order2(double *w, double *xi) {
+    static const double t[3][2] = {{0.5, 0.0}, {0.5, 0.5}, {0.0, 0.5}};
+    for (int g = 0; g < 3; ++g) {
+        w[g] = 0.16666666666666666667;
+        xi[2 * g] = t[g][0];
+        xi[2 * g + 1] = t[g][1];
+    }
+    return 3;
+}
+
 /* ------------------------------------------------------------------------------------------
  * Hooke law: compliance (s1, s2, s3) inverted (formal_lf/material_help.py:116-134), energy
  * trace_sym_col with the factor 2 on the shear terms (include/codegen/__init__.py:82-87),
@@ -144,24 +168,42 @@ static void hexa8_dN(const double *xi, double dN[8][3]) {
     memcpy(dN, v, sizeof(v));
 }
 
-double orc_hexa8_elast_gp(const double *xyz, double E, double nu, double w, const double *xi,
-                          double *Ke) {
-    double dN[8][3], J[3][3] = {{0}}, Ji[3][3], det, D[6][6], g[8][3];
-    hexa8_dN(xi, dN);
-    for (int a = 0; a < 8; ++a)
+/* Quadratic tetrahedron shape-function derivatives (formulations/element_Tetra_10.py:27-41):
+ * X0 = 1 - x - y - z, X1 = x, X2 = y, X3 = z; vertices Xi (2 Xi - 1), edges 4 Xa Xb in the
+ * node order 4:(0,1) 5:(1,2) 6:(0,2) 7:(0,3) 8:(1,3) 9:(2,3). */
+static void tetra10_dN(const double *xi, double dN[10][3]) {
+    const double X[4] = {1 - xi[0] - xi[1] - xi[2], xi[0], xi[1], xi[2]};
+    const double dX[4][3] = {{-1, -1, -1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    for (int i = 0; i < 4; ++i)
+        for (int d = 0; d < 3; ++d) dN[i][d] = (4 * X[i] - 1) * dX[i][d];
+    static const int ed[6][2] = {{0, 1}, {1, 2}, {0, 2}, {0, 3}, {1, 3}, {2, 3}};
+    for (int k = 0; k < 6; ++k) {
+        const int a = ed[k][0], b = ed[k][1];
+        for (int d = 0; d < 3; ++d) dN[4 + k][d] = 4 * (X[b] * dX[a][d] + X[a] * dX[b][d]);
+    }
+}
+
+/* One Gauss point of the isotropic-elasticity weak form for an element of npe nodes with
+ * reference-cell shape-function derivatives dN[npe][3]: Ke (3npe x 3npe, row-major) +=
+ * w * detJ * B^T (W Kglo) B.  Returns detJ. */
+static double elast_gp(int npe, const double *xyz, const double (*dN)[3], double E, double nu,
+                       double w, double *Ke) {
+    const int nd = 3 * npe;
+    double J[3][3] = {{0}}, Ji[3][3], det, D[6][6], g[10][3];
+    for (int a = 0; a < npe; ++a)
         for (int i = 0; i < 3; ++i)
             for (int j = 0; j < 3; ++j) J[i][j] += xyz[3 * a + i] * dN[a][j];
     inv3(J, Ji, &det);
-    for (int a = 0; a < 8; ++a)
+    for (int a = 0; a < npe; ++a)
         for (int i = 0; i < 3; ++i) {
             double s = 0;
             for (int j = 0; j < 3; ++j) s += Ji[j][i] * dN[a][j];
             g[a][i] = s;
         }
     hooke_energy_matrix(E, nu, D);
-    double B[6][24];
+    double B[6][30], DB[6][30];
     memset(B, 0, sizeof(B));
-    for (int a = 0; a < 8; ++a) {
+    for (int a = 0; a < npe; ++a) {
         double gx = g[a][0], gy = g[a][1], gz = g[a][2];
         B[0][3 * a + 0] = gx;
         B[1][3 * a + 1] = gy;
@@ -173,21 +215,41 @@ double orc_hexa8_elast_gp(const double *xyz, double E, double nu, double w, cons
         B[5][3 * a + 1] = 0.5 * gz;
         B[5][3 * a + 2] = 0.5 * gy;
     }
-    double DB[6][24];
     for (int k = 0; k < 6; ++k)
-        for (int c = 0; c < 24; ++c) {
+        for (int c = 0; c < nd; ++c) {
             double s = 0;
             for (int l = 0; l < 6; ++l) s += D[k][l] * B[l][c];
             DB[k][c] = s;
         }
     double f = w * det;
-    for (int r = 0; r < 24; ++r)
-        for (int c = 0; c < 24; ++c) {
+    for (int r = 0; r < nd; ++r)
+        for (int c = 0; c < nd; ++c) {
             double s = 0;
             for (int k = 0; k < 6; ++k) s += B[k][r] * DB[k][c];
-            Ke[24 * r + c] += f * s;
+            Ke[nd * r + c] += f * s;
         }
     return det;
+}
+
+double orc_hexa8_elast_gp(const double *xyz, double E, double nu, double w, const double *xi,
+                          double *Ke) {
+    double dN[8][3];
+    hexa8_dN(xi, dN);
+    return elast_gp(8, xyz, (const double(*)[3])dN, E, nu, w, Ke);
+}
+
+double orc_tetra10_elast_gp(const double *xyz, double E, double nu, double w, const double *xi,
+                            double *Ke) {
+    double dN[10][3];
+    tetra10_dN(xi, dN);
+    return elast_gp(10, xyz, (const double(*)[3])dN, E, nu, w, Ke);
+}
+
+void orc_tetra10_elast_ke(const double *xyz, double E, double nu, double *Ke) {
+    double w[4], xi[12];
+    memset(Ke, 0, sizeof(double) * 900);
+    orc_gauss_tetra_order2(w, xi);
+    for (int g = 0; g < 4; ++g) orc_tetra10_elast_gp(xyz, E, nu, w[g], xi + 3 * g, Ke);
 }
 
 void orc_hexa8_elast_ke(const double *xyz, double E, double nu, double *Ke) {
@@ -289,20 +351,21 @@ int orc_assemble_elast(int npe, uint64_t nn, uint64_t ne, const double *pos, con
                        const double *E, int E_per_elem, double nu,
                        const uint64_t *rowptr, const uint32_t *col, double *val) {
     (void)nn;
-    if (npe != 8) return -1;
-    const int nd = 24;
+    if (npe != 8 && npe != 10) return -1;
+    const int nd = 3 * npe;
     double w[8], xi[24];
-    orc_gauss_hexa_order2(w, xi);
+    const int ngp = npe == 8 ? orc_gauss_hexa_order2(w, xi) : orc_gauss_tetra_order2(w, xi);
     memset(val, 0, sizeof(double) * rowptr[nn * 3]);
-    double xyz[24], Ke[576];
+    double xyz[30], Ke[900];
     for (uint64_t e = 0; e < ne; ++e) {
         const uint32_t *c = conn + (uint64_t)npe * e;
         for (int a = 0; a < npe; ++a)
             for (int d = 0; d < 3; ++d) xyz[3 * a + d] = pos[3 * (uint64_t)c[a] + d];
         double Ee = E[E_per_elem ? e : 0];
-        for (int g = 0; g < 8; ++g) {
+        for (int g = 0; g < ngp; ++g) {
             memset(Ke, 0, sizeof(Ke));
-            orc_hexa8_elast_gp(xyz, Ee, nu, w[g], xi + 3 * g, Ke);
+            if (npe == 8) orc_hexa8_elast_gp(xyz, Ee, nu, w[g], xi + 3 * g, Ke);
+            else orc_tetra10_elast_gp(xyz, Ee, nu, w[g], xi + 3 * g, Ke);
             for (int r = 0; r < nd; ++r)
                 for (int s = r; s < nd; ++s) {
                     uint64_t gi = (uint64_t)c[r / 3] * 3 + r % 3, gj = (uint64_t)c[s / 3] * 3 + s % 3;
@@ -381,6 +444,124 @@ void orc_spmv_sym_lower(uint64_t n, const uint64_t *rowptr, const uint32_t *col,
         r += val[j] * x[col[j]];
         y[i] += r;
     }
+}
+
+/* ------------------------------------------------------------------------------------------
+ * make_rect(m, Tetra_10(), X0, X1, nb_points) -- include/mesh/make_rect.h:443-545.  Each cube
+ * (i,j,k) of the grid (x fastest) is split into 6 tetrahedra; node t of tetrahedron s sits at
+ * O + tr_s + incr * (chgt_s * rela_t), O = X0 + (k incr0, j incr1, i incr2), and nodes are
+ * de-duplicated in first-creation order (BestialNodeAdder, make_rect.h:26-39; here the point's
+ * exact half-grid coordinates replace the O(N^2) distance search -- same order, same first
+ * stored position).  A tetrahedron with a negative Jacobian is renumbered
+ * [0,1,3,2,4,8,7,6,5,9] (permutation_if_jac_neg, include/mesh/element_Tetra_10.h:122-130).
+ * ------------------------------------------------------------------------------------------ */
+int orc_make_rect_tetra10(const double X0_[3], const double X1_[3], const uint32_t nbp[3],
+                          uint64_t *nn_out, uint64_t *ne_out, double *pos, uint32_t *conn) {
+    static const double rela[10][3] = {{0, 0, 0},     {1, 0, 0},     {0, 1, 0},   {0, 0, 1},
+                                       {0.5, 0, 0},   {0.5, 0.5, 0}, {0, 0.5, 0}, {0, 0, 0.5},
+                                       {0.5, 0, 0.5}, {0, 0.5, 0.5}};
+    /* translation (in units of incr) and basis columns of the 6 tetrahedra */
+    static const int trs[6][3] = {{0, 0, 0}, {1, 1, 0}, {1, 0, 0}, {1, 0, 1}, {1, 1, 0}, {1, 1, 1}};
+    static const int bas[6][3][3] = {{{1, 0, 0}, {0, 1, 0}, {0, 0, 1}},
+                                     {{-1, 0, 0}, {0, -1, 0}, {0, -1, 1}},
+                                     {{-1, 0, 1}, {-1, 1, 0}, {0, 0, 1}},
+                                     {{-1, 0, 0}, {-1, 1, 0}, {-1, 1, -1}},
+                                     {{-1, 0, 0}, {-1, 0, 1}, {0, -1, 1}},
+                                     {{-1, 0, 0}, {0, -1, 0}, {0, 0, -1}}};
+    uint32_t ne3[3];
+    double X0[3], X1[3], incr[3];
+    for (int d = 0; d < 3; ++d) {
+        if (nbp[d] < 2) return -1;
+        X0[d] = X0_[d] < X1_[d] ? X0_[d] : X1_[d];
+        X1[d] = X0_[d] < X1_[d] ? X1_[d] : X0_[d];
+        ne3[d] = nbp[d] - 1;
+        incr[d] = (X1[d] - X0[d]) / ne3[d];
+    }
+    const uint64_t gx = 2ull * ne3[0] + 1, gy = 2ull * ne3[1] + 1, gz = 2ull * ne3[2] + 1;
+    const uint64_t nn = gx * gy * gz, ne = 6ull * ne3[0] * ne3[1] * ne3[2];
+    *nn_out = nn;
+    *ne_out = ne;
+    if (!pos || !conn) return 0;
+    uint32_t *id = (uint32_t *)malloc(sizeof(uint32_t) * nn);
+    for (uint64_t q = 0; q < nn; ++q) id[q] = 0xffffffffu;
+    uint32_t next = 0;
+    uint64_t e = 0;
+    for (uint32_t i = 0; i < ne3[2]; ++i)
+        for (uint32_t j = 0; j < ne3[1]; ++j)
+            for (uint32_t k = 0; k < ne3[0]; ++k) {
+                const double O[3] = {X0[0] + k * incr[0], X0[1] + j * incr[1], X0[2] + i * incr[2]};
+                for (int s = 0; s < 6; ++s) {
+                    uint32_t vn[10];
+                    double vp[10][3];
+                    for (int t = 0; t < 10; ++t) {
+                        double wv[3];
+                        for (int r = 0; r < 3; ++r)
+                            wv[r] = bas[s][0][r] * rela[t][0] + bas[s][1][r] * rela[t][1] +
+                                    bas[s][2][r] * rela[t][2];
+                        double p[3];
+                        int64_t g[3];
+                        const uint32_t kk[3] = {k, j, i};
+                        for (int r = 0; r < 3; ++r) {
+                            const double base = s == 0 ? O[r] : O[r] + trs[s][r] * incr[r];
+                            p[r] = base + incr[r] * wv[r];
+                            g[r] = 2 * (int64_t)kk[r] + 2 * trs[s][r] + (int64_t)llround(2 * wv[r]);
+                        }
+                        const uint64_t key = ((uint64_t)g[2] * gy + (uint64_t)g[1]) * gx + (uint64_t)g[0];
+                        if (id[key] == 0xffffffffu) {
+                            id[key] = next;
+                            for (int r = 0; r < 3; ++r) pos[3ull * next + r] = p[r];
+                            ++next;
+                        }
+                        vn[t] = id[key];
+                        for (int r = 0; r < 3; ++r) vp[t][r] = pos[3ull * vn[t] + r];
+                    }
+                    /* sign of the Jacobian from the vertex positions */
+                    double a[3], b[3], c[3];
+                    for (int r = 0; r < 3; ++r) {
+                        a[r] = vp[1][r] - vp[0][r];
+                        b[r] = vp[2][r] - vp[0][r];
+                        c[r] = vp[3][r] - vp[0][r];
+                    }
+                    const double det = a[0] * (b[1] * c[2] - b[2] * c[1]) -
+                                       a[1] * (b[0] * c[2] - b[2] * c[0]) +
+                                       a[2] * (b[0] * c[1] - b[1] * c[0]);
+                    static const int perm[10] = {0, 1, 3, 2, 4, 8, 7, 6, 5, 9};
+                    for (int t = 0; t < 10; ++t) conn[10 * e + t] = det < 0 ? vn[perm[t]] : vn[t];
+                    ++e;
+                }
+            }
+    free(id);
+    return next == nn ? 0 : -2;
+}
+
+/* Consistent loads of a uniform traction on Triangle_6 faces (6 node ids per face: vertices
+ * then mid-edges (01),(12),(20)), order-2 rule of the Triangle_6 table. */
+int orc_tri6_traction(uint64_t nfaces, const uint32_t *faces, const double *pos, const double t[3],
+                      double *F) {
+    double w[3], xi[6];
+    orc_gauss_triangle_order2(w, xi);
+    for (uint64_t f = 0; f < nfaces; ++f) {
+        const uint32_t *q = faces + 6 * f;
+        for (int g = 0; g < 3; ++g) {
+            const double u = xi[2 * g], v = xi[2 * g + 1], X0 = 1 - u - v;
+            const double N[6] = {X0 * (2 * X0 - 1), u * (2 * u - 1), v * (2 * v - 1),
+                                 4 * X0 * u,        4 * u * v,       4 * v * X0};
+            const double dNu[6] = {-(4 * X0 - 1), 4 * u - 1, 0, 4 * (X0 - u), 4 * v, -4 * v};
+            const double dNv[6] = {-(4 * X0 - 1), 0, 4 * v - 1, -4 * u, 4 * u, 4 * (X0 - v)};
+            double tu[3] = {0, 0, 0}, tv[3] = {0, 0, 0};
+            for (int a = 0; a < 6; ++a)
+                for (int d = 0; d < 3; ++d) {
+                    tu[d] += pos[3 * (uint64_t)q[a] + d] * dNu[a];
+                    tv[d] += pos[3 * (uint64_t)q[a] + d] * dNv[a];
+                }
+            const double nx = tu[1] * tv[2] - tu[2] * tv[1], ny = tu[2] * tv[0] - tu[0] * tv[2],
+                         nz = tu[0] * tv[1] - tu[1] * tv[0];
+            const double ds = sqrt(nx * nx + ny * ny + nz * nz) * w[g];
+            for (int a = 0; a < 6; ++a)
+                for (int d = 0; d < 3; ++d) F[3 * (uint64_t)q[a] + d] += N[a] * t[d] * ds;
+        }
+    }
+    return 0;
 }
 
 /* ------------------------------------------------------------------------------------------

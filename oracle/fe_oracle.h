@@ -7,8 +7,10 @@
  *
  * Every function restates one piece of the reference, cited file:line
  * (paths inside the LMTpp project):
- *   mesh           include/mesh/make_rect.h:653-679, include/util/rectilinear_iterator.h:20-45
- *   Gauss tables   include/mesh/element_Hexa.h:5-20, include/mesh/element_Quad.h:5-12
+ *   mesh           include/mesh/make_rect.h:653-679 (Hexa), 443-545 (Tetra_10),
+ *                  include/util/rectilinear_iterator.h:20-45
+ *   Gauss tables   include/mesh/element_Hexa.h:5-20, include/mesh/element_Quad.h:5-12,
+ *                  include/mesh/element_Tetra_10.h:5-16, include/mesh/element_Triangle_6.h:5-15
  *   element K_e    formulations/formulation_elasticity_iso.py:45-60,
  *                  formal_lf/material_help.py:116-134,175-183,
  *                  include/codegen/__init__.py:23-42,82-87,
@@ -39,10 +41,17 @@ extern "C" {
 int orc_make_rect_hexa(const double X0[3], const double X1[3], const uint32_t nb_points[3],
                        double *pos, uint32_t *conn);
 
+/* Structured Tetra_10 mesh (6 tets per cube), first-creation node order of the reference.
+ * Two-phase: pos == NULL or conn == NULL only returns nn and ne. */
+int orc_make_rect_tetra10(const double X0[3], const double X1[3], const uint32_t nb_points[3],
+                          uint64_t *nn, uint64_t *ne, double *pos, uint32_t *conn);
+
 /* ---------------- Gauss tables (reference C++ tables, 12-digit constants) ---------------- */
 /* Returns number of points; w[np], xi[np*dim]. */
 int orc_gauss_hexa_order2(double *w, double *xi);
 int orc_gauss_quad_order2(double *w, double *xi);
+int orc_gauss_tetra_order2(double *w, double *xi);
+int orc_gauss_triangle_order2(double *w, double *xi);
 
 /* ---------------- element matrices ---------------- */
 /* Hexa8 isotropic elasticity, one Gauss point: Ke(24x24, row-major) += w*detJ*B^T (W H) B.
@@ -51,6 +60,10 @@ double orc_hexa8_elast_gp(const double *xyz, double E, double nu, double w, cons
                           double *Ke);
 /* Whole element (order-2 rule, 8 points). */
 void orc_hexa8_elast_ke(const double *xyz, double E, double nu, double *Ke);
+/* Tetra10 isotropic elasticity: one Gauss point / whole element (order 2, 4 points), Ke 30x30. */
+double orc_tetra10_elast_gp(const double *xyz, double E, double nu, double w, const double *xi,
+                            double *Ke);
+void orc_tetra10_elast_ke(const double *xyz, double E, double nu, double *Ke);
 
 /* ---------------- pattern / assembly ---------------- */
 /* Structural lower pattern (node-pair product x nnu^2, j<=i).  rowptr has n+1 entries.
@@ -59,7 +72,7 @@ int orc_pattern_lower(uint64_t nn, int nnu, uint64_t ne, int npe, const uint32_t
                       uint64_t *rowptr, uint32_t *col, uint64_t *nnz);
 
 /* Assemble elasticity K (lower CSR, pattern from orc_pattern_lower) for an element type
- * (8 = Hexa8).  E has ne entries (E_per_elem=1) or 1 entry. */
+ * (8 = Hexa8, 10 = Tetra10).  E has ne entries (E_per_elem=1) or 1 entry. */
 int orc_assemble_elast(int npe, uint64_t nn, uint64_t ne, const double *pos, const uint32_t *conn,
                        const double *E, int E_per_elem, double nu,
                        const uint64_t *rowptr, const uint32_t *col, double *val);
@@ -68,6 +81,10 @@ int orc_assemble_elast(int npe, uint64_t nn, uint64_t ne, const double *pos, con
  * order-2 quad rule).  F has nn*3 entries and is accumulated. */
 int orc_quad4_traction(uint64_t nfaces, const uint32_t *faces, const double *pos,
                        const double traction[3], double *F);
+
+/* Same for Triangle_6 faces (6 node ids per face), order-2 triangle rule. */
+int orc_tri6_traction(uint64_t nfaces, const uint32_t *faces, const double *pos,
+                      const double traction[3], double *F);
 
 /* Penalty constraints (include/formulation/formulation.h:1028-1071): one coefficient per
  * constraint.  max|diag| is taken over the current K.  Returns max|diag|. */

@@ -62,6 +62,53 @@ def make_rect_hexa(nb_points, X0=(0.0, 0.0, 0.0), X1=(1.0, 1.0, 1.0)):
     return pos, conn
 
 
+def make_rect_tetra10(nb_points, X0=(0.0, 0.0, 0.0), X1=(1.0, 1.0, 1.0)):
+    nbp = np.asarray(nb_points if np.ndim(nb_points) else [nb_points] * 3, dtype=np.uint32)
+    x0 = np.asarray(X0, dtype=np.float64)
+    x1 = np.asarray(X1, dtype=np.float64)
+    nn, ne = ctypes.c_uint64(), ctypes.c_uint64()
+    L = lib()
+    L.orc_make_rect_tetra10(_p(x0, _f64p), _p(x1, _f64p), _p(nbp, _u32p), ctypes.byref(nn),
+                            ctypes.byref(ne), None, None)
+    pos = np.zeros((nn.value, 3))
+    conn = np.zeros((ne.value, 10), dtype=np.uint32)
+    rc = L.orc_make_rect_tetra10(_p(x0, _f64p), _p(x1, _f64p), _p(nbp, _u32p), ctypes.byref(nn),
+                                 ctypes.byref(ne), _p(pos, _f64p), _p(conn, _u32p))
+    if rc:
+        raise RuntimeError("orc_make_rect_tetra10 failed: %d" % rc)
+    return pos, conn
+
+
+def tetra10_ke(xyz, E, nu):
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    Ke = np.zeros((30, 30))
+    lib().orc_tetra10_elast_ke(_p(xyz, _f64p), ctypes.c_double(E), ctypes.c_double(nu), _p(Ke, _f64p))
+    return Ke
+
+
+def tri6_traction(faces, pos, t, F):
+    faces = np.ascontiguousarray(faces, dtype=np.uint32)
+    t = np.asarray(t, dtype=np.float64)
+    lib().orc_tri6_traction(ctypes.c_uint64(faces.shape[0]), _p(faces, _u32p), _p(pos, _f64p),
+                            _p(t, _f64p), _p(F, _f64p))
+    return F
+
+
+TETRA10_CHILDREN = [[0, 2, 1, 6, 5, 4], [0, 1, 3, 4, 8, 7], [0, 3, 2, 7, 9, 6], [1, 2, 3, 5, 9, 8]]
+
+
+def x1_faces_tetra10(pos, conn, x1=1.0, eps=1e-6):
+    """Triangle_6 skin faces (Tetra_10 children, formulations/element_Tetra_10.py:16-21) on x = x1,
+    in element order then child order."""
+    out = []
+    for e in range(conn.shape[0]):
+        for ch in TETRA10_CHILDREN:
+            q = conn[e, ch]
+            if np.all(pos[q, 0] > x1 - eps):
+                out.append(q)
+    return np.ascontiguousarray(np.array(out, dtype=np.uint32).reshape(-1, 6))
+
+
 def hexa8_ke(xyz, E, nu):
     xyz = np.ascontiguousarray(xyz, dtype=np.float64)
     Ke = np.zeros((24, 24))
@@ -184,16 +231,23 @@ def x1_faces_hexa(pos, conn, x1=1.0, eps=1e-6):
     return np.ascontiguousarray(q[on], dtype=np.uint32)
 
 
-def elasticity_problem(nb_points, E=210000.0, nu=0.3, pen=1e5, traction=(1.0, 0.0, 0.0)):
-    """The elasticity workload of the reference's example: unit cube of Hexa8, penalty clamp of
-    every node on x = 0, uniform traction on x = 1.  Returns a dict of oracle arrays."""
-    pos, conn = make_rect_hexa(nb_points)
+def elasticity_problem(nb_points, E=210000.0, nu=0.3, pen=1e5, traction=(1.0, 0.0, 0.0), elem="hexa"):
+    """The elasticity workload of the reference's example: unit cube of Hexa8 (or Tetra10),
+    penalty clamp of every node on x = 0, uniform traction on x = 1.  Returns oracle arrays."""
+    if elem == "hexa":
+        pos, conn = make_rect_hexa(nb_points)
+    else:
+        pos, conn = make_rect_tetra10(nb_points)
     nn = pos.shape[0]
     rowptr, col = pattern_lower(nn, 3, conn)
     val = assemble_elast(pos, conn, E, nu, rowptr, col)
     F = np.zeros(3 * nn)
-    faces = x1_faces_hexa(pos, conn)
-    quad4_traction(faces, pos, traction, F)
+    if elem == "hexa":
+        faces = x1_faces_hexa(pos, conn)
+        quad4_traction(faces, pos, traction, F)
+    else:
+        faces = x1_faces_tetra10(pos, conn)
+        tri6_traction(faces, pos, traction, F)
     clamped = np.nonzero(pos[:, 0] < 1e-6)[0]
     dofs = (3 * clamped[:, None] + np.arange(3)[None, :]).ravel()
     md = penalty(rowptr, col, val, F, dofs, np.ones(dofs.shape[0]), np.zeros(dofs.shape[0]), pen)

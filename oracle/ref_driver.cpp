@@ -4,7 +4,8 @@
  * Compiled against the reference's headers and its vendored LDL/AMD sources by
  * oracle/build_ref.sh into oracle/_ref/ (never into the product).  What comes from the
  * reference here:
- *   - the mesh:        make_rect(m, Hexa(), X0, X1, nb_points)   include/mesh/make_rect.h:653-679
+ *   - the mesh:        make_rect(m, Hexa() | Tetra_10(), X0, X1, nb_points)
+ *                      include/mesh/make_rect.h:653-679, 443-545
  *   - the storage:     Mat<double,Sym<>,SparseLine<> > with its insert-on-nonzero /
  *                      erase-on-exact-zero semantics              include/containers/vecsparse.h:9-47
  *   - max|diag| penalty constraints                               include/formulation/formulation.h:1028-1071
@@ -15,7 +16,7 @@
  * cannot run here; it is scattered exactly as the generated code does it
  * (formal_lf/calculate_matrix.py:86-98): for each Gauss point, matrix(i,j) += tmp for j >= i.
  *
- * Usage: ref_driver hexa <nb_points> <E> <nu> <penalty> <outdir>
+ * Usage: ref_driver hexa|tetra10 <nb_points> <E> <nu> <penalty> <outdir>
  * Writes little-endian raw arrays: pos.f64 conn.u32 rowptr.u64 col.u32 val.f64 F.f64
  * u_ldl.f64 u_icpcg.f64 lam_ldl.f64 (LDL solution of K lambda = u_ldl) and info.txt.
  */
@@ -39,61 +40,96 @@ static void dump(const std::string &path, const std::vector<T> &v) {
     fclose(f);
 }
 
+template <class TM>
+static void read_mesh(TM &m, int npe, std::vector<double> &pos, std::vector<unsigned> &conn) {
+    unsigned nn = m.node_list.size(), ne = m.elem_list.size();
+    pos.resize(3 * nn);
+    for (unsigned i = 0; i < nn; ++i)
+        for (int d = 0; d < 3; ++d) pos[3 * i + d] = m.node_list[i].pos[d];
+    conn.resize(npe * ne);
+    for (unsigned e = 0; e < ne; ++e)
+        for (int a = 0; a < npe; ++a)
+            conn[npe * e + a] = m.node_list.number(*m.elem_list[e]->node_virtual(a));
+}
+
 int main(int argc, char **argv) {
-    if (argc != 7 || std::string(argv[1]) != "hexa") {
-        fprintf(stderr, "usage: ref_driver hexa <nb_points> <E> <nu> <penalty> <outdir>\n");
+    if (argc != 7 || (std::string(argv[1]) != "hexa" && std::string(argv[1]) != "tetra10")) {
+        fprintf(stderr, "usage: ref_driver hexa|tetra10 <nb_points> <E> <nu> <penalty> <outdir>\n");
         return 1;
     }
+    const bool tet = std::string(argv[1]) == "tetra10";
+    const int npe = tet ? 10 : 8, nd = 3 * npe;
     unsigned nbp = atoi(argv[2]);
     double E = atof(argv[3]), nu = atof(argv[4]), penalty = atof(argv[5]);
     std::string out = argv[6];
 
-    typedef Mesh<MeshCaracStd<3, 3, 1, double, 1> > TM; /* nb=1, degree 1 -> Hexa */
-    TM m;
-    make_rect(m, Hexa(), TM::Pvec(0, 0, 0), TM::Pvec(1, 1, 1), TM::Pvec(nbp, nbp, nbp));
-    unsigned nn = m.node_list.size(), ne = m.elem_list.size(), n = 3 * nn;
-
-    std::vector<double> pos(3 * nn);
-    for (unsigned i = 0; i < nn; ++i)
-        for (int d = 0; d < 3; ++d) pos[3 * i + d] = m.node_list[i].pos[d];
-    std::vector<unsigned> conn(8 * ne);
-    for (unsigned e = 0; e < ne; ++e)
-        for (int a = 0; a < 8; ++a) conn[8 * e + a] = m.node_list.number(*m.elem_list[e]->node_virtual(a));
+    std::vector<double> pos;
+    std::vector<unsigned> conn;
+    if (tet) {
+        typedef Mesh<MeshCaracStd<3, 3, 0, double, 2> > TM; /* nb=0, degree 2 -> Tetra_10 */
+        TM m;
+        make_rect(m, Tetra_10(), TM::Pvec(0, 0, 0), TM::Pvec(1, 1, 1), TM::Pvec(nbp, nbp, nbp));
+        read_mesh(m, npe, pos, conn);
+    } else {
+        typedef Mesh<MeshCaracStd<3, 3, 1, double, 1> > TM; /* nb=1, degree 1 -> Hexa */
+        TM m;
+        make_rect(m, Hexa(), TM::Pvec(0, 0, 0), TM::Pvec(1, 1, 1), TM::Pvec(nbp, nbp, nbp));
+        read_mesh(m, npe, pos, conn);
+    }
+    unsigned nn = pos.size() / 3, ne = conn.size() / npe, n = 3 * nn;
 
     /* assembly into an empty SparseLine matrix (the preallocated pattern is cleared before
        every assembly, formulation.h:931-950) */
     Mat<double, Sym<>, SparseLine<> > K(n, n);
     double w[8], xi[24];
-    orc_gauss_hexa_order2(w, xi);
+    const int ngp = tet ? orc_gauss_tetra_order2(w, xi) : orc_gauss_hexa_order2(w, xi);
     for (unsigned e = 0; e < ne; ++e) {
-        double xyz[24];
-        unsigned in[8];
-        for (int a = 0; a < 8; ++a) {
-            in[a] = 3 * conn[8 * e + a]; /* indice_noda = node * nnu */
-            for (int d = 0; d < 3; ++d) xyz[3 * a + d] = pos[3 * conn[8 * e + a] + d];
+        double xyz[30];
+        unsigned in[10];
+        for (int a = 0; a < npe; ++a) {
+            in[a] = 3 * conn[npe * e + a]; /* indice_noda = node * nnu */
+            for (int d = 0; d < 3; ++d) xyz[3 * a + d] = pos[3 * conn[npe * e + a] + d];
         }
-        for (int g = 0; g < 8; ++g) {
-            double Ke[576] = {0};
-            orc_hexa8_elast_gp(xyz, E, nu, w[g], xi + 3 * g, Ke);
-            for (int i = 0; i < 24; ++i)
-                for (int j = i; j < 24; ++j)
-                    K(in[i / 3] + i % 3, in[j / 3] + j % 3) += Ke[24 * i + j];
+        for (int g = 0; g < ngp; ++g) {
+            double Ke[900] = {0};
+            if (tet) orc_tetra10_elast_gp(xyz, E, nu, w[g], xi + 3 * g, Ke);
+            else orc_hexa8_elast_gp(xyz, E, nu, w[g], xi + 3 * g, Ke);
+            for (int i = 0; i < nd; ++i)
+                for (int j = i; j < nd; ++j)
+                    K(in[i / 3] + i % 3, in[j / 3] + j % 3) += Ke[nd * i + j];
         }
     }
 
     /* sollicitation: uniform traction (1,0,0) on the Quad4 skin faces at x = 1 */
     std::vector<double> F(n, 0.0);
     std::vector<unsigned> faces;
-    for (unsigned e = 0; e < ne; ++e) {
-        const unsigned *c = &conn[8 * e];
-        /* Hexa child face 5 is nodes [1,2,6,5] (formulations/element_Hexa.py:22-29) */
-        unsigned q[4] = {c[1], c[2], c[6], c[5]};
-        bool on = true;
-        for (int a = 0; a < 4; ++a) on = on && pos[3 * q[a]] > 1 - 1e-6;
-        if (on) faces.insert(faces.end(), q, q + 4);
-    }
     double t[3] = {1, 0, 0};
-    orc_quad4_traction(faces.size() / 4, faces.empty() ? 0 : &faces[0], &pos[0], t, &F[0]);
+    if (!tet) {
+        for (unsigned e = 0; e < ne; ++e) {
+            const unsigned *c = &conn[8 * e];
+            /* Hexa child face 5 is nodes [1,2,6,5] (formulations/element_Hexa.py:22-29) */
+            unsigned q[4] = {c[1], c[2], c[6], c[5]};
+            bool on = true;
+            for (int a = 0; a < 4; ++a) on = on && pos[3 * q[a]] > 1 - 1e-6;
+            if (on) faces.insert(faces.end(), q, q + 4);
+        }
+        orc_quad4_traction(faces.size() / 4, faces.empty() ? 0 : &faces[0], &pos[0], t, &F[0]);
+    } else {
+        /* Tetra_10 children (formulations/element_Tetra_10.py:16-21) */
+        static const int ch[4][6] = {{0, 2, 1, 6, 5, 4}, {0, 1, 3, 4, 8, 7}, {0, 3, 2, 7, 9, 6},
+                                     {1, 2, 3, 5, 9, 8}};
+        for (unsigned e = 0; e < ne; ++e)
+            for (int f = 0; f < 4; ++f) {
+                unsigned q[6];
+                bool on = true;
+                for (int a = 0; a < 6; ++a) {
+                    q[a] = conn[10 * e + ch[f][a]];
+                    on = on && pos[3 * q[a]] > 1 - 1e-6;
+                }
+                if (on) faces.insert(faces.end(), q, q + 6);
+            }
+        orc_tri6_traction(faces.size() / 6, faces.empty() ? 0 : &faces[0], &pos[0], t, &F[0]);
+    }
 
     /* penalty constraints: node[i].dep[d] = 0 for every node on x = 0 */
     double max_diag = max(abs(K.diag()));
@@ -164,7 +200,7 @@ int main(int argc, char **argv) {
     dump(out + "/lam_ldl.f64", lam_ldl);
     FILE *f = fopen((out + "/info.txt").c_str(), "w");
     fprintf(f, "nn %u\nne %u\nn %u\nnnz %zu\nmax_diag %.17g\nncons %u\nnfaces %zu\nicpcg_iter %d\n",
-            nn, ne, n, col.size(), max_diag, ncons, faces.size() / 4, it);
+            nn, ne, n, col.size(), max_diag, ncons, faces.size() / (tet ? 6 : 4), it);
     fclose(f);
     return 0;
 }

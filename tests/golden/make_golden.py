@@ -3,8 +3,8 @@
 Runs oracle/_ref/ref_driver (LMT++'s make_rect, Sym SparseLine assembly semantics, max|diag|
 penalty constraints, LDL and IC(0)-PCG, built by oracle/build_ref.sh from the LMTpp sources)
 (and the LDL solution of K lambda = u, the adjoint of the misfit 1/2 |u|^2) on the elasticity
-workload of the reference's example -- unit cube of Hexa8, penalty clamp of
-x = 0, uniform traction (1,0,0) on x = 1 -- and stores its outputs as compressed npz.
+workload of the reference's example -- unit cube of Hexa8 or Tetra_10, penalty clamp
+of x = 0, uniform traction (1,0,0) on x = 1 -- and stores its outputs as compressed npz.
 
 Also records the known-answer vectors of the reference's solver unit tests
 (tests/include/containers/conjugate_gradient_test.cpp:15-71) as JSON.
@@ -23,25 +23,27 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 
-CASES = [  # name, nb_points, E, nu, penalty
-    ("hexa_2x2x2", 3, 210000.0, 0.3, 1e5),
-    ("hexa_10x10x10", 11, 210000.0, 0.3, 1e5),
+CASES = [  # name, element, nb_points, E, nu, penalty
+    ("hexa_2x2x2", "hexa", 3, 210000.0, 0.3, 1e5),
+    ("hexa_10x10x10", "hexa", 11, 210000.0, 0.3, 1e5),
+    ("tetra10_3x3x3", "tetra10", 4, 210000.0, 0.3, 1e5),
 ]
 
 
-def run_case(name, nbp, E, nu, pen):
+def run_case(name, elem, nbp, E, nu, pen):
     drv = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
+    npe = 8 if elem == "hexa" else 10
     with tempfile.TemporaryDirectory() as d:
-        subprocess.check_call([drv, "hexa", str(nbp), repr(E), repr(nu), repr(pen), d])
+        subprocess.check_call([drv, elem, str(nbp), repr(E), repr(nu), repr(pen), d])
         r = lambda f, t: np.fromfile(os.path.join(d, f), dtype=t)
         info = dict(l.split() for l in open(os.path.join(d, "info.txt")))
         np.savez_compressed(
             os.path.join(HERE, name + ".npz"),
-            pos=r("pos.f64", np.float64).reshape(-1, 3), conn=r("conn.u32", np.uint32).reshape(-1, 8),
+            pos=r("pos.f64", np.float64).reshape(-1, 3), conn=r("conn.u32", np.uint32).reshape(-1, npe),
             rowptr=r("rowptr.u64", np.uint64), col=r("col.u32", np.uint32), val=r("val.f64", np.float64),
             F=r("F.f64", np.float64), u_ldl=r("u_ldl.f64", np.float64),
             u_icpcg=r("u_icpcg.f64", np.float64), lam_ldl=r("lam_ldl.f64", np.float64),
-            meta=np.array(json.dumps(dict(nb_points=nbp, E=E, nu=nu, penalty=pen,
+            meta=np.array(json.dumps(dict(elem=elem, nb_points=nbp, E=E, nu=nu, penalty=pen,
                                           max_diag=float(info["max_diag"]),
                                           icpcg_iter=int(info["icpcg_iter"]),
                                           nnz=int(info["nnz"])))))

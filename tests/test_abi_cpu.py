@@ -75,3 +75,12 @@ def test_constraint_parser(txt, expect):
 def test_constraint_parser_rejects_nonlinear():
     with pytest.raises(abi.LmtgError):
         parse_constraint("sin(node[0].dep[0]) - 0.1")
+
+
+@pytest.mark.parametrize("nbp", [(2, 2, 2), (4, 4, 4), (3, 5, 4)])
+def test_make_rect_tetra10_matches_oracle(nbp):
+    from lmtpp_gb300 import make_rect_tetra10
+    pos, conn = make_rect_tetra10(nbp)
+    pos_o, conn_o = O.make_rect_tetra10(nbp)
+    assert np.array_equal(pos, pos_o)
+    assert np.array_equal(conn, conn_o)

@@ -59,6 +59,29 @@ def test_adjoint_gradients_match_reference_ldl(golden_dir, mode):
     f.close()
 
 
+def test_tetra10_adjoint_matches_oracle_gradient():
+    from lmtpp_gb300 import make_rect_tetra10, x1_faces
+    pos, conn = make_rect_tetra10(4)
+    rng = np.random.default_rng(11)
+    E = rng.uniform(1e5, 3e5, conn.shape[0])
+    f = Formulation(pos, conn)
+    f.elastic_modulus = E
+    f.poisson_ratio = 0.3
+    clamped = np.nonzero(pos[:, 0] < 1e-6)[0]
+    f.add_constraints((3 * clamped[:, None] + np.arange(3)).ravel(), 1e5)
+    f.add_skin_traction(x1_faces(pos, conn), (1.0, 0.0, 0.0))
+    f.solve(1e-13, mode="fp64")
+    u = f.get_result()
+    _, g, _ = f.adjoint_grad("compliance")
+    g_ref = np.zeros(conn.shape[0])
+    for e in range(conn.shape[0]):
+        Kh = O.tetra10_ke(pos[conn[e]], 1.0, 0.3)
+        dofs = (3 * conn[e][:, None].astype(np.int64) + np.arange(3)).ravel()
+        g_ref[e] = -u[dofs] @ Kh @ u[dofs]
+    assert np.linalg.norm(g - g_ref) <= 1e-10 * np.linalg.norm(g_ref)
+    f.close()
+
+
 def test_adjoint_gradients_match_central_differences():
     """Central differences with h = 1e-6 E_e on random elements of a lognormal-E mesh.  J(E +- h)
     is evaluated through u+- = u + delta+-, K(E +- h) delta+- = F - K(E +- h) u, which is exact

@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 import scipy.sparse as sp
 
-from lmtpp_gb300 import Formulation, abi, make_rect_hexa, x1_faces_hexa
+from lmtpp_gb300 import Formulation, abi, make_rect_hexa, make_rect_tetra10, x1_faces
 from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
@@ -34,16 +34,20 @@ def build_problem(pos, conn, E, nu, pen, traction=(1.0, 0.0, 0.0)):
     f.poisson_ratio = nu
     clamped = np.nonzero(pos[:, 0] < 1e-6)[0]
     f.add_constraints((3 * clamped[:, None] + np.arange(3)).ravel(), pen)
-    f.add_skin_traction(x1_faces_hexa(pos, conn), traction)
+    f.add_skin_traction(x1_faces(pos, conn), traction)
     f.allocate_matrices()
     return f
 
 
-@pytest.mark.parametrize("name", ["hexa_2x2x2", "hexa_10x10x10"])
+def mesh_of(m):
+    return (make_rect_hexa if m["elem"] == "hexa" else make_rect_tetra10)(m["nb_points"])
+
+
+@pytest.mark.parametrize("name", ["hexa_2x2x2", "hexa_10x10x10", "tetra10_3x3x3"])
 def test_assembly_matches_reference(golden_dir, name):
     g = load_golden(golden_dir, name)
     m = g["meta"]
-    pos, conn = make_rect_hexa(m["nb_points"])
+    pos, conn = mesh_of(m)
     assert np.array_equal(pos, g["pos"]) and np.array_equal(conn, g["conn"])
     f = build_problem(pos, conn, m["E"], m["nu"], m["penalty"])
     f.assemble(True, True)
@@ -93,12 +97,12 @@ def test_element_matrices_match_oracle_on_distorted_mesh():
     f.close()
 
 
-@pytest.mark.parametrize("name", ["hexa_2x2x2", "hexa_10x10x10"])
+@pytest.mark.parametrize("name", ["hexa_2x2x2", "hexa_10x10x10", "tetra10_3x3x3"])
 @pytest.mark.parametrize("mode,tol", [("fp64", 1e-10), ("mixed", 1e-8)])
 def test_solution_matches_reference_ldl(golden_dir, name, mode, tol):
     g = load_golden(golden_dir, name)
     m = g["meta"]
-    pos, conn = make_rect_hexa(m["nb_points"])
+    pos, conn = mesh_of(m)
     f = build_problem(pos, conn, m["E"], m["nu"], m["penalty"])
     st = f.solve(1e-13 if mode == "fp64" else 1e-12, mode=mode)
     u = f.get_result()
@@ -108,6 +112,45 @@ def test_solution_matches_reference_ldl(golden_dir, name, mode, tol):
     assert st["rel_residual"] <= 1e-11
     if mode == "mixed":
         assert st["outer_iterations"] >= 1
+    f.close()
+
+
+def test_tetra10_element_matrices_match_oracle_on_distorted_mesh():
+    pos, conn = make_rect_tetra10(4)
+    rng = np.random.default_rng(5)
+    inner = np.all((pos > 1e-9) & (pos < 1 - 1e-9), axis=1)
+    pos = pos + inner[:, None] * rng.uniform(-0.03, 0.03, pos.shape)
+    E = rng.uniform(5e4, 3e5, conn.shape[0])
+    f = Formulation(pos, conn)
+    f.elastic_modulus = E
+    f.poisson_ratio = 0.31
+    f.allocate_matrices()
+    f.assemble(True, False)
+    Ke = f.element_matrices(0, conn.shape[0])
+    for e in range(conn.shape[0]):
+        Ko = O.tetra10_ke(pos[conn[e]], E[e], 0.31)
+        assert np.abs(Ke[e] - Ko).max() <= 1e-12 * np.abs(Ko).max(), e
+    f.assemble(True, False, native_fp32=True)
+    K32 = f.element_matrices(0, 10, precision=1)
+    for e in range(10):
+        Ko = O.tetra10_ke(pos[conn[e]], E[e], 0.31)
+        assert np.abs(K32[e] - Ko).max() <= 2e-6 * np.abs(Ko).max(), e
+    f.close()
+
+
+def test_tetra10_medium_mesh_fp64_vs_mixed():
+    """A 12^3 x 6 Tetra10 mesh: rows with more than 32 blocks take the chunked SpMV path."""
+    pos, conn = make_rect_tetra10(13)
+    f = build_problem(pos, conn, 210000.0, 0.3, 1e5)
+    st = f.solve(1e-12, mode="fp64")
+    u = f.get_result()
+    rowptr, col, val = f.get_mat()
+    F = f.get_sollicitation()
+    r = F - O.spmv(rowptr, col, val, u)
+    assert np.linalg.norm(r) <= 1e-11 * np.linalg.norm(F), st
+    f.set_result(np.zeros_like(u))
+    f.solve(1e-12, mode="mixed")
+    assert np.linalg.norm(f.get_result() - u) <= 1e-8 * np.linalg.norm(u)
     f.close()
 
 

@@ -30,11 +30,11 @@ def csr(rowptr, col, val, n):
     return sp.csr_matrix((val, col.astype(np.int64), rowptr.astype(np.int64)), shape=(n, n))
 
 
-@pytest.mark.parametrize("name", ["hexa_2x2x2", "hexa_10x10x10"])
+@pytest.mark.parametrize("name", ["hexa_2x2x2", "hexa_10x10x10", "tetra10_3x3x3"])
 def test_oracle_matches_reference_runtime(golden_dir, name):
     g = load_golden(golden_dir, name)
     m = g["meta"]
-    P = O.elasticity_problem(m["nb_points"], E=m["E"], nu=m["nu"], pen=m["penalty"])
+    P = O.elasticity_problem(m["nb_points"], E=m["E"], nu=m["nu"], pen=m["penalty"], elem=m["elem"])
     n = P["F"].shape[0]
     # mesh and connectivity: bit-exact (make_rect node order, accumulated coordinates)
     assert np.array_equal(P["pos"], g["pos"])
