@@ -41,8 +41,11 @@ def parse():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--side", type=int, default=128, help="elements per side of the cube")
-    p.add_argument("--cpu-side", type=int, default=24, help="elements per side of the CPU sample")
+    p.add_argument("--side", type=int, default=128, help="elements (cubes) per side of the unit cube")
+    p.add_argument("--elem", default="hexa8", choices=["hexa8", "tetra10"],
+                   help="hexa8: N^3 Hexa8 (default N=128); tetra10: N^3 cubes x 6 Tetra10 (N=40)")
+    p.add_argument("--cpu-side", type=int, default=0,
+                   help="cubes per side of the CPU sample (default 24 Hexa8 / 8 Tetra10)")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--fd", type=int, default=32, help="elements checked by central differences (adjoint mode)")
@@ -135,14 +138,19 @@ class Clocks:
 # ------------------------------------------------------------------------------------------
 # GPU arm
 # ------------------------------------------------------------------------------------------
+def make_mesh(args):
+    from lmtpp_gb300 import make_rect_hexa, make_rect_tetra10
+    return (make_rect_hexa if args.elem == "hexa8" else make_rect_tetra10)(args.side + 1)
+
+
 def new_problem(pos, conn, E, device):
-    from lmtpp_gb300 import Formulation, x1_faces_hexa
+    from lmtpp_gb300 import Formulation, x1_faces
     f = Formulation(pos, conn, device=device)
     f.elastic_modulus = E
     f.poisson_ratio = NU
     clamped = np.nonzero(pos[:, 0] < 1e-6)[0]
     f.add_constraints((3 * clamped[:, None] + np.arange(3)).ravel(), PENALTY)
-    f.add_skin_traction(x1_faces_hexa(pos, conn), (1.0, 0.0, 0.0))
+    f.add_skin_traction(x1_faces(pos, conn), (1.0, 0.0, 0.0))
     f.allocate_matrices()
     return f
 
@@ -188,10 +196,9 @@ def spmv_bytes(nn, nnzb, s):
 
 def run_gpu(args, rank, world, local, barrier, allmax):
     import torch
-    from lmtpp_gb300 import make_rect_hexa
     torch.cuda.set_device(local)
     N = args.side
-    pos, conn = make_rect_hexa(N + 1)
+    pos, conn = make_mesh(args)
     E = lognormal_E(conn.shape[0])
     f = new_problem(pos, conn, E, local)
     stream = torch.cuda.ExternalStream(f.stream_handle(), device=torch.device("cuda", local))
@@ -252,8 +259,9 @@ def run_gpu(args, rank, world, local, barrier, allmax):
         res["e2e_s"] = allmax(statistics.median(e2e))
         res["e2e_err"] = rel_err(u, u_ref)
         nc = 3 * int(np.sum(pos[:, 0] < 1e-6))
-        nfaces = N * N
-        res["h2d"] = pos.nbytes + conn.nbytes + E.nbytes + 8 * 3 * pos.shape[0] + nc * (4 + 8 + 8) + nfaces * 16
+        from lmtpp_gb300 import x1_faces
+        res["h2d"] = (pos.nbytes + conn.nbytes + E.nbytes + 8 * 3 * pos.shape[0] + nc * (4 + 8 + 8)
+                      + x1_faces(pos, conn).nbytes)
         res["d2h"] = 8 * 3 * pos.shape[0]
     return res
 
@@ -263,22 +271,23 @@ def run_gpu(args, rank, world, local, barrier, allmax):
 # per-Gauss-point scatter, max|diag| penalty, IC(0) factorization, IC-PCG with the true residual
 # and the |r|_inf test of solve_using_incomplete_chol_factorize), one thread.
 # ------------------------------------------------------------------------------------------
-def cpu_sample(side):
+def cpu_sample(side, elem="hexa8"):
     """Time-to-solution of the CPU path on a side^3 sample of the same workload family,
     and its extrapolation to the full workload: assembly scales with the element count,
     the PCG with element count x iterations (iterations grow like the elements per side)."""
     from oracle import oracle as O
-    pos, conn = O.make_rect_hexa(side + 1)
+    hexa = elem == "hexa8"
+    pos, conn = (O.make_rect_hexa if hexa else O.make_rect_tetra10)(side + 1)
     E = lognormal_E(conn.shape[0])
     rowptr, col = O.pattern_lower(pos.shape[0], 3, conn)
     clamped = np.nonzero(pos[:, 0] < 1e-6)[0]
     dofs = (3 * clamped[:, None] + np.arange(3)).ravel()
-    faces = O.x1_faces_hexa(pos, conn)
+    faces = O.x1_faces_hexa(pos, conn) if hexa else O.x1_faces_tetra10(pos, conn)
 
     def assemble():
         val = O.assemble_elast(pos, conn, E, NU, rowptr, col)
         F = np.zeros(3 * pos.shape[0])
-        O.quad4_traction(faces, pos, (1.0, 0.0, 0.0), F)
+        (O.quad4_traction if hexa else O.tri6_traction)(faces, pos, (1.0, 0.0, 0.0), F)
         O.penalty(rowptr, col, val, F, dofs, np.ones(dofs.shape[0]), np.zeros(dofs.shape[0]), PENALTY)
         return val, F
 
@@ -300,19 +309,20 @@ def cpu_sample(side):
     x, it = O.ic_pcg(rowptr, col, val, fac, F, crit * np.abs(F).max())
     t2 = time.perf_counter()
     return {"side": side, "t_asm": t1 - t0, "t_solve": t2 - t1, "iters": it, "crit": crit,
-            "err": rel_err(x, ref), "ne": conn.shape[0]}
+            "err": rel_err(x, ref), "ne": conn.shape[0], "elem": elem}
 
 
 def cpu_extrapolate(s, side_full):
-    ne_full = side_full ** 3
+    ne_full = side_full ** 3 * (1 if s["elem"] == "hexa8" else 6)
     return s["t_asm"] * ne_full / s["ne"] + s["t_solve"] * (side_full / s["side"]) ** 4
 
 
 def cpu_desc(s):
-    return ("Hexa8 %d^3 sample of the same workload (lognormal E, penalty clamp, traction): oracle "
+    return ("%s %d^3 sample of the same workload (lognormal E, penalty clamp, traction): oracle "
             "port assembly %.3f s + IC(0) + IC-PCG %.3f s (%d it, |r|_inf <= %.0e max|F|, rel err "
             "%.1e); extrapolated x(ne ratio) for assembly and x(side ratio)^4 for the solve"
-            % (s["side"], s["t_asm"], s["t_solve"], s["iters"], s["crit"], s["err"]))
+            % ("Hexa8" if s["elem"] == "hexa8" else "Tetra10 (6 per cube)", s["side"], s["t_asm"],
+               s["t_solve"], s["iters"], s["crit"], s["err"]))
 
 
 # dram__bytes_read.sum + dram__bytes_write.sum / algorithmic bytes of one k_pcg_spmv<float>
@@ -324,20 +334,22 @@ METRIC = "time-to-solution at 1e-10 rel. error vs FP64 oracle, mixed vs FP64 CG;
 
 def workload_config(args):
     N = args.side
-    return {"workload": "Hexa8 elasticity %d^3 unit cube (%d elements, %d DOF), lognormal E "
-                        "(log-std 0.5, seed %d), nu 0.3, penalty clamp x=0, traction x=1"
-                        % (N, N ** 3, 3 * (N + 1) ** 3, SEED),
-            "elements": N ** 3, "dof": 3 * (N + 1) ** 3, "seed": SEED,
+    if args.elem == "hexa8":
+        ne, ndof, name = N ** 3, 3 * (N + 1) ** 3, "Hexa8 elasticity %d^3 unit cube" % N
+    else:
+        ne, ndof, name = 6 * N ** 3, 3 * (2 * N + 1) ** 3, "Tetra10 elasticity %d^3 cubes x 6" % N
+    return {"workload": "%s (%d elements, %d DOF), lognormal E (log-std 0.5, seed %d), nu 0.3, "
+                        "penalty clamp x=0, traction x=1" % (name, ne, ndof, SEED),
+            "elements": ne, "dof": ndof, "seed": SEED,
             "error_target": ERR_TARGET, "l2": "inputs larger than L2 (K32 alone > 1 GB)",
             "parallelism": "replicas"}
 
 
 def run_small(args):
     """Single-purpose runs with few launches, for ncu captures."""
-    from lmtpp_gb300 import make_rect_hexa
-    pos, conn = make_rect_hexa(args.side + 1)
+    pos, conn = make_mesh(args)
     f = new_problem(pos, conn, lognormal_E(conn.shape[0]), 0)
-    out = {"mode": args.mode, "side": args.side}
+    out = {"mode": args.mode, "side": args.side, "elem": args.elem}
     if args.mode == "profile":
         f.assemble(True, True, mixed=True)
         out["spmv32_ms"], out["upd32_ms"] = f.profile_pcg_kernels(precision=1, iters=5)
@@ -355,9 +367,8 @@ def run_adjoint(args):
     (default_rng(seed + 1)), h = 1e-6 E_e.  J(E +- h) is evaluated through the exact difference
     u+- = u + delta+-, K(E +- h) delta+- = F - K(E +- h) u, solved with the mixed solver."""
     import torch
-    from lmtpp_gb300 import make_rect_hexa
     N = args.side
-    pos, conn = make_rect_hexa(N + 1)
+    pos, conn = make_mesh(args)
     E = lognormal_E(conn.shape[0])
     f = new_problem(pos, conn, E, 0)
     stream = torch.cuda.ExternalStream(f.stream_handle(), device=torch.device("cuda", 0))
@@ -417,6 +428,8 @@ def run_adjoint(args):
 
 def main():
     args = parse()
+    if args.cpu_side == 0:
+        args.cpu_side = 24 if args.elem == "hexa8" else 8
     if args.mode == "adjoint":
         return run_adjoint(args)
     if args.mode != "bench":
@@ -427,7 +440,7 @@ def main():
             return
         samples = []
         for k in range(args.warmup + args.steps):
-            s = cpu_sample(args.cpu_side)
+            s = cpu_sample(args.cpu_side, args.elem)
             if k >= args.warmup:
                 samples.append(cpu_extrapolate(s, args.side))
         v = statistics.median(samples)
@@ -457,7 +470,7 @@ def main():
     ach64 = b64 / (r["spmv64_ms"] * 1e-3) / 1e9
     # assembly gather bytes: element blocks read, gather indices read, K64 + K32 written
     asm_bytes = r["ne"] * 36 * 9 * 8 + r["ne"] * 64 * 4 + 4 * (r["nnzb"] + 1) + r["nnzb"] * 9 * (8 + 4)
-    s = cpu_sample(args.cpu_side)
+    s = cpu_sample(args.cpu_side, args.elem)
     cpu_v = cpu_extrapolate(s, args.side)
     v = r["ms_mixed"] * 1e-3
     line = {
