@@ -41,6 +41,7 @@ extern "C" {
 /* ---- element types (nodes per element) ---- */
 #define LMTG_ELEM_HEXA8 8    /* faces: Quad4 (4 node ids) */
 #define LMTG_ELEM_TETRA10 10 /* faces: Triangle_6 (6 node ids: vertices, then mid-edges 01 12 20) */
+#define LMTG_ELEM_TRIANGLE6 6 /* 2D heat diffusion (lmtg_diff_*), one unknown per node */
 
 /* ---- lmtg_assemble flags ---- */
 #define LMTG_ASM_MAT64 1        /* FP64 element matrices -> FP64 K */
@@ -202,6 +203,40 @@ int lmtg_profile_pcg_kernels(lmtg_ctx *ctx, int precision, int iters, double *sp
 int lmtg_residual_norm_noalloc(void *stream, uint64_t nn, const uint32_t *bptr,
                                const uint32_t *bcol, const double *K, const double *x,
                                const double *b, double *r, double *rr_host);
+
+/* ---- transient heat diffusion (formulation difftherm on Triangle_6) ----
+ * formulations/formulation_difftherm.py:24-30; theta scheme A T_{n+1} = B T_n with
+ * A = M/dt + theta K, B = M/dt - (1 - theta) K, K = int a grad N . grad N, a = conductivity /
+ * rho_c.  theta = 1/2 reproduces the reference's time integration (the residual at the interval
+ * midpoint, formal_lf/formulation.py:506-509); theta = 1 is implicit Euler. */
+
+/* Structured Triangle_6 mesh of make_rect(m, Triangle_6(), X0, X1, nb_points)
+ * (include/mesh/make_rect.h:141-170): pos nn*2, conn ne*6.  Two-phase like Tetra_10. */
+int lmtg_make_rect_triangle6(const double X0[2], const double X1[2], const uint32_t nb_points[2],
+                             uint64_t *nn, uint64_t *ne, double *pos, uint32_t *conn);
+/* 2D mesh of a diffusion context (created with lmtg_create). */
+int lmtg_diff_mesh_set(lmtg_ctx *ctx, uint64_t nn, const double *pos, uint64_t ne,
+                       const uint32_t *conn);
+/* Conductivity (1 or ne values), rho_c, time step, theta, and T = 0 on the given nodes by the
+ * reference's penalty (scale max|diag A| * penalty, or the fixed lmtg_set_penalty_scale value).
+ * Builds the pattern (first call), the element matrices and A, B. */
+int lmtg_diff_setup(lmtg_ctx *ctx, const double *k, uint64_t nk, double rho_c, double dt,
+                    double theta, uint64_t nbnd, const uint32_t *bnd_nodes, double penalty);
+/* Temperature state (nn doubles). */
+int lmtg_diff_set_state(lmtg_ctx *ctx, const double *T);
+int lmtg_diff_get_state(lmtg_ctx *ctx, double *T);
+/* nsteps time steps from the current state, each solved by FP64 Jacobi-PCG to the relative
+ * residual tol (warm start from the previous state). */
+int lmtg_diff_run(lmtg_ctx *ctx, int nsteps, double tol, int maxit, lmtg_solve_stats *stats);
+/* Final-time misfit J = 1/2 |T_N - target|^2 of nsteps steps from the current state and its
+ * adjoint gradient w.r.t. every element's conductivity (ne doubles into dJdk), with forward
+ * states checkpointed every `checkpoint_every` steps and recomputed per segment in the backward
+ * sweep (no reference counterpart).  The penalty scale is held constant.  Leaves T_N as state. */
+int lmtg_diff_adjoint_misfit(lmtg_ctx *ctx, int nsteps, int checkpoint_every, const double *target,
+                             double tol, int maxit, double *J, double *dJdk,
+                             lmtg_solve_stats *stats);
+/* A and B as lower CSR (rowptr nn+1, col/A/B nnz_lower = (blocks - nn)/2 + nn entries). */
+int lmtg_diff_get_matrices(lmtg_ctx *ctx, uint64_t *rowptr, uint32_t *col, double *A, double *B);
 
 /* Sizes of the current problem. */
 int lmtg_get_sizes(lmtg_ctx *ctx, uint64_t *nn, uint64_t *ne, uint64_t *ndof, uint64_t *nnz_blocks);

@@ -12,7 +12,7 @@ HEADER = os.path.join(os.path.dirname(HERE), "include", "lmtg.h")
 
 OK = 0
 ERR_ARG, ERR_CUDA, ERR_STATE, ERR_NOT_CONVERGED, ERR_TIMEOUT, ERR_NAN, ERR_NOMEM, ERR_UNSUPPORTED = range(1, 9)
-ELEM_HEXA8, ELEM_TETRA10 = 8, 10
+ELEM_HEXA8, ELEM_TETRA10, ELEM_TRIANGLE6 = 8, 10, 6
 ASM_MAT64, ASM_MAT32, ASM_VEC, ASM_MAT32_NATIVE = 1, 2, 4, 8
 SOLVE_PCG_F64, SOLVE_MIXED_IR = 0, 1
 CRIT_REL_RESIDUAL, CRIT_NORM_INF_DELTA, CRIT_NORM2_DELTA, CRIT_ABS_RESIDUAL_INF = 0, 1, 2, 3
@@ -59,6 +59,15 @@ _SIGS = {
     "lmtg_spmv": (_i, [_vp, _i, _vp, _vp]),
     "lmtg_get_sizes": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "lmtg_get_launch_count": (_i, [_vp, ctypes.POINTER(_u64)]),
+    "lmtg_make_rect_triangle6": (_i, [_vp, _vp, _vp, ctypes.POINTER(_u64), ctypes.POINTER(_u64), _vp, _vp]),
+    "lmtg_diff_mesh_set": (_i, [_vp, _u64, _vp, _u64, _vp]),
+    "lmtg_diff_setup": (_i, [_vp, _vp, _u64, _d, _d, _d, _u64, _vp, _d]),
+    "lmtg_diff_set_state": (_i, [_vp, _vp]),
+    "lmtg_diff_get_state": (_i, [_vp, _vp]),
+    "lmtg_diff_run": (_i, [_vp, _i, _d, _i, ctypes.POINTER(SolveStats)]),
+    "lmtg_diff_adjoint_misfit": (_i, [_vp, _i, _i, _vp, _d, _i, ctypes.POINTER(_d), _vp,
+                                      ctypes.POINTER(SolveStats)]),
+    "lmtg_diff_get_matrices": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "lmtg_set_penalty_scale": (_i, [_vp, _d]),
     "lmtg_get_penalty_scale": (_i, [_vp, ctypes.POINTER(_d)]),
     "lmtg_adjoint_grad": (_i, [_vp, _i, _vp, _vp, _i, _d, _i, _d, ctypes.POINTER(_d), _vp,

@@ -321,6 +321,7 @@ int lmtg_material_set(lmtg_ctx *c, const double *E, uint64_t nE, double nu) {
 int lmtg_allocate_matrices(lmtg_ctx *c, uint64_t *nnz_lower) {
     return guard(c, [&] {
         LMTG_CHECK(c->ne > 0, LMTG_ERR_STATE, "mesh_set first");
+        LMTG_CHECK(c->nnu == 3, LMTG_ERR_STATE, "elasticity call on a diffusion context");
         build_pattern(c);
         c->Ke64.alloc(c->ne * (uint64_t)c->npairs * 9);
         c->K64.alloc(c->nnzb * 9);

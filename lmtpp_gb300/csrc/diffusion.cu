@@ -1,0 +1,807 @@
+// diffusion.cu -- transient heat diffusion on Triangle_6 (formulation difftherm): element matrices,
+// theta-scheme assembly, scalar CSR PCG, time stepping and the misfit adjoint with checkpoints.
+//
+// Reference: formulations/formulation_difftherm.py:24-30 (a grad T . grad v + T' v, a =
+// conductivity / (density * heat capacity)); time integration: the residual evaluated at the
+// midpoint of [t_n, t_n+1] with T interpolated linearly (formal_lf/formulation.py:506-509,
+// formal_lf/extrapolation.py:21-40, formal_lf/gauss_integration.py:52-63), i.e. the theta
+// scheme with theta = 1/2:
+//     A T_{n+1} = B T_n,   A = M/dt + theta K,   B = M/dt - (1 - theta) K,
+// theta = 1 gives implicit Euler.  Element rule: the 6-point triangle rule of the closed-form
+// element integration (formulations/element_Triangle_6.py:92-99).  Dirichlet T = 0 uses the
+// reference's penalty (formulation.h:1028-1071) on A.
+//
+// One unknown per node: the node-block pattern of pattern.cu is the scalar CSR pattern; a row
+// holds ~9-19 entries, so the SpMV uses 8 lanes per row (4 rows per warp).
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <exception>
+#include <new>
+#include <vector>
+
+#include "solver_kernels.cuh"
+
+namespace lmtg {
+
+constexpr int kTriPairs = 21;
+
+__device__ __forceinline__ void tri6_point(int g, double &w, double &u, double &v) {
+    const double a = 0.445948490915965, b = 0.091576213509771;
+    const double wa = 0.111690794839005, wb = 0.054975871827661;
+    const int k = g % 3;
+    const double p = g < 3 ? a : b;
+    w = g < 3 ? wa : wb;
+    u = k == 1 ? 1.0 - 2.0 * p : p;
+    v = k == 2 ? 1.0 - 2.0 * p : p;
+}
+
+__device__ __forceinline__ void tri6_shape(double u, double v, double (&N)[6], double (&dN)[6][2]) {
+    const double X0 = 1 - u - v;
+    N[0] = X0 * (2 * X0 - 1); N[1] = u * (2 * u - 1); N[2] = v * (2 * v - 1);
+    N[3] = 4 * X0 * u;        N[4] = 4 * u * v;       N[5] = 4 * v * X0;
+    dN[0][0] = -(4 * X0 - 1); dN[0][1] = -(4 * X0 - 1);
+    dN[1][0] = 4 * u - 1;     dN[1][1] = 0;
+    dN[2][0] = 0;             dN[2][1] = 4 * v - 1;
+    dN[3][0] = 4 * (X0 - u);  dN[3][1] = -4 * u;
+    dN[4][0] = 4 * v;         dN[4][1] = 4 * u;
+    dN[5][0] = -4 * v;        dN[5][1] = 4 * (X0 - v);
+}
+
+// gradients of the 6 shape functions and w*detJ at Gauss point g
+__device__ __forceinline__ double tri6_geom(const double (&xy)[6][2], int g, double (&N)[6],
+                                            double (&gx)[6][2]) {
+    double w, u, v, dN[6][2];
+    tri6_point(g, w, u, v);
+    tri6_shape(u, v, N, dN);
+    double J[2][2] = {{0, 0}, {0, 0}};
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+#pragma unroll
+        for (int i = 0; i < 2; ++i)
+#pragma unroll
+            for (int j = 0; j < 2; ++j) J[i][j] = fma(xy[k][i], dN[k][j], J[i][j]);
+    const double det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+    const double id = 1.0 / det;
+    const double Ji[2][2] = {{J[1][1] * id, -J[0][1] * id}, {-J[1][0] * id, J[0][0] * id}};
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+#pragma unroll
+        for (int i = 0; i < 2; ++i) gx[k][i] = Ji[0][i] * dN[k][0] + Ji[1][i] * dN[k][1];
+    return w * det;
+}
+
+// element blocks of A = M/dt + theta K and B = M/dt - (1-theta) K (upper pairs, 21 each)
+__global__ void k_tri6_diff(const double *__restrict__ pos, const uint32_t *__restrict__ conn,
+                            const double *__restrict__ a, int a_per_elem, double inv_rho_c,
+                            double dt, double theta, uint64_t ne, double *__restrict__ KA,
+                            double *__restrict__ KB) {
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < ne;
+         e += (uint64_t)gridDim.x * blockDim.x) {
+        double xy[6][2];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            const uint64_t n = conn[6 * e + k];
+            xy[k][0] = pos[2 * n];
+            xy[k][1] = pos[2 * n + 1];
+        }
+        const double ae = a[a_per_elem ? e : 0] * inv_rho_c;
+        double K[kTriPairs], M[kTriPairs];
+#pragma unroll
+        for (int p = 0; p < kTriPairs; ++p) K[p] = M[p] = 0.0;
+#pragma unroll 1
+        for (int g = 0; g < 6; ++g) {
+            double N[6], gx[6][2];
+            const double wd = tri6_geom(xy, g, N, gx);
+            int p = 0;
+#pragma unroll
+            for (int i = 0; i < 6; ++i)
+#pragma unroll
+                for (int j = i; j < 6; ++j, ++p) {
+                    K[p] = fma(wd, gx[i][0] * gx[j][0] + gx[i][1] * gx[j][1], K[p]);
+                    M[p] = fma(wd, N[i] * N[j], M[p]);
+                }
+        }
+        const double idt = 1.0 / dt;
+#pragma unroll
+        for (int p = 0; p < kTriPairs; ++p) {
+            KA[e * kTriPairs + p] = M[p] * idt + theta * ae * K[p];
+            KB[e * kTriPairs + p] = M[p] * idt - (1.0 - theta) * ae * K[p];
+        }
+    }
+}
+
+// gather assembly of the scalar matrices (one value per pattern entry); A also rounded to FP32
+__global__ void k_assemble_s(const uint32_t *__restrict__ gptr, const uint32_t *__restrict__ gsrc,
+                             const double *__restrict__ KA, const double *__restrict__ KB,
+                             uint64_t nnz, double *__restrict__ A, double *__restrict__ B,
+                             float *__restrict__ A32) {
+    for (uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; q < nnz;
+         q += (uint64_t)gridDim.x * blockDim.x) {
+        double sa = 0.0, sb = 0.0;
+        for (uint32_t g = gptr[q]; g < gptr[q + 1]; ++g) {
+            const uint32_t src = __ldg(gsrc + g) >> 1;  // 1x1 blocks: no transpose
+            sa += KA[src];
+            sb += KB[src];
+        }
+        A[q] = sa;
+        B[q] = sb;
+        A32[q] = (float)sa;
+    }
+}
+
+__global__ void k_max_diag_s(const uint32_t *__restrict__ bdiag, const double *__restrict__ A,
+                             uint64_t nn, unsigned long long *out) {
+    double m = 0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nn;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        m = fmax(m, fabs(A[bdiag[i]]));
+    m = warp_max(m);
+    if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
+}
+
+__global__ void k_penalty_s(const uint32_t *__restrict__ bdiag, double *A, float *A32,
+                            const uint32_t *__restrict__ nodes, uint64_t nc, double penalty,
+                            const unsigned long long *md_bits) {
+    const double md = __longlong_as_double((long long)*md_bits);
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < nc;
+         k += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t d = bdiag[nodes[k]];
+        atomicAdd(A + d, md * penalty);
+    }
+}
+
+template <class T>
+__global__ void k_jacobi_s(const uint32_t *__restrict__ bdiag, const double *__restrict__ A,
+                           uint64_t nn, T *Dinv, float *A32) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nn;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const double d = A[bdiag[i]];
+        Dinv[i] = (T)(d != 0.0 ? 1.0 / d : 0.0);
+        if (A32) A32[bdiag[i]] = (float)d;  // constrained diagonals after the penalty
+    }
+}
+
+// ---- scalar CSR kernels: 8 lanes per row, 4 rows per warp --------------------------------
+template <class T, class XF>
+__device__ __forceinline__ T csr_row8(const uint32_t *__restrict__ col, const T *__restrict__ K,
+                                      uint32_t rb, uint32_t re, int sub, XF xf) {
+    T acc = (T)0;
+    for (uint32_t q = rb + sub; q < re; q += 8) acc = fma(__ldg(K + q), xf(__ldg(col + q)), acc);
+    acc += __shfl_xor_sync(0xffffffffu, acc, 4);
+    acc += __shfl_xor_sync(0xffffffffu, acc, 2);
+    acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+    return acc;
+}
+
+template <class T>
+__global__ void __launch_bounds__(kRowThreads)
+    k_spmv_s(const uint32_t *__restrict__ rp, const uint32_t *__restrict__ col,
+             const T *__restrict__ K, const T *__restrict__ x, T *__restrict__ y, uint64_t n) {
+    const int lane = threadIdx.x & 31, sub = lane & 7;
+    const uint64_t nq = ((uint64_t)gridDim.x * blockDim.x) >> 3;
+    for (uint64_t base = ((blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5) * 4;
+         base < n; base += nq) {
+        const uint64_t I = base + (lane >> 3);
+        const bool on = I < n;
+        const T v = csr_row8(col, K, on ? rp[I] : 0u, on ? rp[I + 1] : 0u, sub,
+                             [&](uint32_t j) { return __ldg(x + j); });
+        if (on && sub == 0) y[I] = v;
+    }
+}
+
+template <class T>
+__global__ void __launch_bounds__(kRowThreads)
+    k_residual_s(const uint32_t *__restrict__ rp, const uint32_t *__restrict__ col,
+                 const T *__restrict__ K, const T *__restrict__ x, const T *__restrict__ b,
+                 T *__restrict__ r, uint64_t n, double *partials, unsigned *ticket, double *rr_out) {
+    const int lane = threadIdx.x & 31, sub = lane & 7;
+    const uint64_t nq = ((uint64_t)gridDim.x * blockDim.x) >> 3;
+    T acc = (T)0;
+    for (uint64_t base = ((blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5) * 4;
+         base < n; base += nq) {
+        const uint64_t I = base + (lane >> 3);
+        const bool on = I < n;
+        const T v = csr_row8(col, K, on ? rp[I] : 0u, on ? rp[I + 1] : 0u, sub,
+                             [&](uint32_t j) { return __ldg(x + j); });
+        if (on && sub == 0) {
+            const T ri = b[I] - v;
+            r[I] = ri;
+            acc = fma(ri, ri, acc);
+        }
+    }
+    const T t[1] = {acc};
+    double out[1];
+    if (grid_reduce_t<1, 0u>(t, partials, ticket, out) && threadIdx.x == 0) *rr_out = out[0];
+}
+
+template <class T>
+__global__ void k_pcg_start_s(const T *__restrict__ r, const T *__restrict__ b,
+                              const T *__restrict__ Dinv, T *__restrict__ z, uint64_t n,
+                              PcgScalars *S, double *partials) {
+    T t[3] = {(T)0, (T)0, (T)0};  // rz, rr, bb
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const T ri = r[i], zi = Dinv[i] * ri;
+        z[i] = zi;
+        t[0] = fma(ri, zi, t[0]);
+        t[1] = fma(ri, ri, t[1]);
+        if (b) t[2] = fma(b[i], b[i], t[2]);
+    }
+    double out[3];
+    if (grid_reduce_t<3, 0u>(t, partials, &S->cnt_c, out) && threadIdx.x == 0) {
+        S->rz = out[0];
+        S->rr = out[1];
+        if (b) S->bb = out[2];
+        S->beta = 0.0;
+        S->iter = 0;
+        S->status = LMTG_OK;
+        S->done = (out[1] <= S->crit * S->crit * S->bb) ? 1 : 0;
+        if (!isfinite(out[0]) || !isfinite(out[1])) {
+            S->done = 1;
+            S->status = LMTG_ERR_NAN;
+        }
+    }
+}
+
+template <class T>
+__global__ void __launch_bounds__(kRowThreads)
+    k_pcg_spmv_s(const uint32_t *__restrict__ rp, const uint32_t *__restrict__ col,
+                 const T *__restrict__ K, const T *__restrict__ z, const T *__restrict__ pold,
+                 T *__restrict__ pnew, T *__restrict__ q, uint64_t n, PcgScalars *S,
+                 double *partials) {
+    if (*(volatile int *)&S->done) return;
+    const T beta = (T)S->beta;
+    const int lane = threadIdx.x & 31, sub = lane & 7;
+    const uint64_t nq = ((uint64_t)gridDim.x * blockDim.x) >> 3;
+    T acc = (T)0;
+    for (uint64_t base = ((blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5) * 4;
+         base < n; base += nq) {
+        const uint64_t I = base + (lane >> 3);
+        const bool on = I < n;
+        const T qi = csr_row8(col, K, on ? rp[I] : 0u, on ? rp[I + 1] : 0u, sub,
+                              [&](uint32_t j) { return fma(beta, __ldg(pold + j), __ldg(z + j)); });
+        if (on && sub == 0) {
+            const T pn = fma(beta, pold[I], z[I]);
+            pnew[I] = pn;
+            q[I] = qi;
+            acc = fma(pn, qi, acc);
+        }
+    }
+    const T t[1] = {acc};
+    double out[1];
+    if (grid_reduce_t<1, 0u>(t, partials, &S->cnt_a, out) && threadIdx.x == 0) S->pq = out[0];
+}
+
+template <class T>
+__global__ void k_pcg_update_s(T *__restrict__ x, T *__restrict__ r, T *__restrict__ z,
+                               const T *__restrict__ p, const T *__restrict__ q,
+                               const T *__restrict__ Dinv, uint64_t n, PcgScalars *S,
+                               double *partials) {
+    if (*(volatile int *)&S->done) return;
+    const double pq = S->pq;
+    const T alpha = (T)(S->rz / (pq + (pq == 0.0 ? 1.0 : 0.0)));
+    T t[2] = {(T)0, (T)0};
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        x[i] = fma(alpha, p[i], x[i]);
+        const T ri = fma(-alpha, q[i], r[i]);
+        r[i] = ri;
+        const T zi = Dinv[i] * ri;
+        z[i] = zi;
+        t[0] = fma(ri, zi, t[0]);
+        t[1] = fma(ri, ri, t[1]);
+    }
+    double out[2];
+    if (grid_reduce_t<2, 0u>(t, partials, &S->cnt_b, out) && threadIdx.x == 0) {
+        const double rz_old = S->rz;
+        S->iter += 1;
+        S->rr = out[1];
+        S->beta = out[0] / rz_old;
+        S->rz = out[0];
+        if (!isfinite(out[0]) || !isfinite(out[1]) || !isfinite(pq)) {
+            S->status = LMTG_ERR_NAN;
+            S->done = 1;
+        } else if (out[1] <= S->crit * S->crit * S->bb) {
+            S->done = 1;
+        } else if (S->iter >= S->maxit) {
+            S->status = LMTG_ERR_NOT_CONVERGED;
+            S->done = 1;
+        }
+    }
+}
+
+// misfit gradient accumulation for the theta scheme:
+//   g_e -= lambda_e^T Khat_e (theta T_n + (1 - theta) T_{n-1})_e,  Khat_e = int gradN.gradN
+__global__ void k_tri6_grad(const double *__restrict__ pos, const uint32_t *__restrict__ conn,
+                            uint64_t ne, double theta, const double *__restrict__ lam,
+                            const double *__restrict__ Tn, const double *__restrict__ Tm,
+                            double *__restrict__ g) {
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < ne;
+         e += (uint64_t)gridDim.x * blockDim.x) {
+        double xy[6][2], lv[6], wv[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            const uint64_t n = conn[6 * e + k];
+            xy[k][0] = pos[2 * n];
+            xy[k][1] = pos[2 * n + 1];
+            lv[k] = lam[n];
+            wv[k] = theta * Tn[n] + (1.0 - theta) * Tm[n];
+        }
+        double acc = 0.0;
+#pragma unroll 1
+        for (int gp = 0; gp < 6; ++gp) {
+            double N[6], gx[6][2];
+            const double wd = tri6_geom(xy, gp, N, gx);
+            double gl[2] = {0, 0}, gw[2] = {0, 0};
+#pragma unroll
+            for (int k = 0; k < 6; ++k)
+#pragma unroll
+                for (int i = 0; i < 2; ++i) {
+                    gl[i] = fma(lv[k], gx[k][i], gl[i]);
+                    gw[i] = fma(wv[k], gx[k][i], gw[i]);
+                }
+            acc = fma(wd, gl[0] * gw[0] + gl[1] * gw[1], acc);
+        }
+        g[e] -= acc;
+    }
+}
+
+__global__ void k_axpby(const double *__restrict__ a, const double *__restrict__ b, double *c,
+                        uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        c[i] = a[i] - (b ? b[i] : 0.0);
+}
+
+// ---- host -----------------------------------------------------------------------------------
+static int rgrid(lmtg_ctx *c) { return grid_for(c, c->nn * 8, kRowThreads, 8); }
+static int ngrid(lmtg_ctx *c) { return grid_for(c, c->nn, kRowThreads, 8); }
+
+// PCG on A x = b (FP64, Jacobi), warm start from x.  Returns the status.
+static int diff_pcg(lmtg_ctx *c, const double *b, double *x, double tol, int maxit, int *iters) {
+    cudaStream_t s = c->stream;
+    double *r = c->w64[0].p, *z = c->w64[1].p, *p0 = c->w64[2].p, *p1 = c->w64[3].p, *q = c->w64[4].p;
+    PcgScalars init{};
+    init.crit = tol;
+    init.crit_kind = LMTG_CRIT_REL_RESIDUAL;
+    init.maxit = maxit;
+    LMTG_CUDA(cudaMemcpyAsync(c->scal.p, &init, sizeof(init), cudaMemcpyHostToDevice, s));
+    PcgScalars *o = c->scal.p + 1;
+    k_residual_s<double><<<rgrid(c), kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, c->K64.p, x, b, r,
+                                                          c->nn, c->partials.p, &o->cnt_c, &o->rr);
+    k_pcg_start_s<double><<<ngrid(c), kRowThreads, 0, s>>>(r, b, c->Dinv64.p, z, c->nn, c->scal.p,
+                                                           c->partials.p);
+    LMTG_CUDA(cudaMemsetAsync(p0, 0, sizeof(double) * c->nn, s));
+    LMTG_CUDA(cudaGetLastError());
+    c->launches += 2;
+    constexpr int kPairs = 8;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    LMTG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    for (int k = 0; k < kPairs; ++k) {
+        k_pcg_spmv_s<double><<<rgrid(c), kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, c->K64.p, z, p0,
+                                                              p1, q, c->nn, c->scal.p, c->partials.p);
+        k_pcg_update_s<double><<<ngrid(c), kRowThreads, 0, s>>>(x, r, z, p1, q, c->Dinv64.p, c->nn,
+                                                                c->scal.p, c->partials.p);
+        k_pcg_spmv_s<double><<<rgrid(c), kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, c->K64.p, z, p1,
+                                                              p0, q, c->nn, c->scal.p, c->partials.p);
+        k_pcg_update_s<double><<<ngrid(c), kRowThreads, 0, s>>>(x, r, z, p0, q, c->Dinv64.p, c->nn,
+                                                                c->scal.p, c->partials.p);
+    }
+    cudaError_t ce = cudaStreamEndCapture(s, &graph);
+    if (ce != cudaSuccess) throw Error{LMTG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce)};
+    ce = cudaGraphInstantiate(&exec, graph, 0);
+    if (ce != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        throw Error{LMTG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce)};
+    }
+    bool finished = false;
+    LMTG_CUDA(cudaMemcpyAsync(c->h_scal, c->scal.p, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
+    LMTG_CUDA(cudaStreamSynchronize(s));
+    finished = c->h_scal[0].done != 0;
+    const int max_chunks = maxit / (2 * kPairs) + 2;
+    for (int ch = 0; ch < max_chunks && !finished; ++ch) {
+        ce = cudaGraphLaunch(exec, s);
+        c->launches += 4 * kPairs;
+        if (ce == cudaSuccess)
+            ce = cudaMemcpyAsync(c->h_scal, c->scal.p, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s);
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+        if (ce != cudaSuccess) {
+            cudaGraphExecDestroy(exec);
+            cudaGraphDestroy(graph);
+            throw Error{LMTG_ERR_CUDA, std::string("pcg chunk: ") + cudaGetErrorString(ce)};
+        }
+        finished = c->h_scal[0].done != 0;
+    }
+    cudaGraphExecDestroy(exec);
+    cudaGraphDestroy(graph);
+    *iters = c->h_scal[0].iter;
+    return finished ? c->h_scal[0].status : LMTG_ERR_NOT_CONVERGED;
+}
+
+// rhs = B T (FP64)
+static void diff_rhs(lmtg_ctx *c, const double *T, double *rhs) {
+    k_spmv_s<double><<<rgrid(c), kRowThreads, 0, c->stream>>>(c->bptr.p, c->bcol.p, c->B64.p, T, rhs,
+                                                              c->nn);
+    LMTG_CUDA(cudaGetLastError());
+    c->launches += 1;
+}
+
+// one step T_next = A^-1 B T (warm start from T)
+static int diff_step(lmtg_ctx *c, const double *T, double *Tn, double tol, int maxit, int *it) {
+    diff_rhs(c, T, c->F.p);
+    if (Tn != T)
+        LMTG_CUDA(cudaMemcpyAsync(Tn, T, sizeof(double) * c->nn, cudaMemcpyDeviceToDevice, c->stream));
+    return diff_pcg(c, c->F.p, Tn, tol, maxit, it);
+}
+
+void diff_setup(lmtg_ctx *c, const double *k, uint64_t nk, double rho_c, double dt, double theta,
+                uint64_t nbnd, const uint32_t *bnd, double penalty) {
+    LMTG_CHECK(c->elem_type == LMTG_ELEM_TRIANGLE6, LMTG_ERR_STATE, "diffusion needs a Triangle_6 mesh");
+    LMTG_CHECK(nk == 1 || nk == c->ne, LMTG_ERR_ARG, "conductivity needs 1 or ne values");
+    LMTG_CHECK(rho_c > 0 && dt > 0 && theta >= 0 && theta <= 1, LMTG_ERR_ARG, "rho_c, dt > 0, theta in [0,1]");
+    cudaStream_t s = c->stream;
+    if (!c->allocated) {
+        build_pattern(c);
+        c->nnz_lower = (c->nnzb - c->nn) / 2 + c->nn;
+        c->K64.alloc(c->nnzb);
+        c->B64.alloc(c->nnzb);
+        c->K32.alloc(c->nnzb);
+        c->Ke64.alloc(c->ne * kTriPairs);
+        c->KeB64.alloc(c->ne * kTriPairs);
+        c->F.alloc(c->nn);
+        c->u.alloc(c->nn);
+        c->Dinv64.alloc(c->nn);
+        for (auto &w : c->w64) w.alloc(c->nn);
+        LMTG_CUDA(cudaMemsetAsync(c->u.p, 0, c->u.bytes(), s));
+        c->allocated = true;
+    }
+    c->E.alloc(nk);
+    LMTG_CUDA(cudaMemcpyAsync(c->E.p, k, nk * 8, cudaMemcpyHostToDevice, s));
+    c->E_per_elem = nk > 1;
+    c->rho_c = rho_c;
+    c->dt = dt;
+    c->theta = theta;
+    k_tri6_diff<<<grid_for(c, c->ne, 128, 16), 128, 0, s>>>(c->pos.p, c->conn.p, c->E.p, c->E_per_elem,
+                                                            1.0 / rho_c, dt, theta, c->ne, c->Ke64.p,
+                                                            c->KeB64.p);
+    k_assemble_s<<<grid_for(c, c->nnzb, 256, 8), 256, 0, s>>>(c->gptr.p, c->gsrc.p, c->Ke64.p,
+                                                              c->KeB64.p, c->nnzb, c->K64.p, c->B64.p,
+                                                              c->K32.p);
+    LMTG_CUDA(cudaGetLastError());
+    c->launches += 2;
+    if (nbnd) {
+        upload_u32(c, c->cdof, bnd, nbnd);
+        DBuf<unsigned long long> md;
+        md.alloc(1);
+        if (c->penalty_scale > 0.0) {
+            unsigned long long bits;
+            memcpy(&bits, &c->penalty_scale, sizeof(bits));
+            LMTG_CUDA(cudaMemcpyAsync(md.p, &bits, sizeof(bits), cudaMemcpyHostToDevice, s));
+        } else {
+            LMTG_CUDA(cudaMemsetAsync(md.p, 0, 8, s));
+            k_max_diag_s<<<grid_for(c, c->nn, 256), 256, 0, s>>>(c->bdiag.p, c->K64.p, c->nn, md.p);
+            c->launches += 1;
+        }
+        k_penalty_s<<<grid_for(c, nbnd, 256), 256, 0, s>>>(c->bdiag.p, c->K64.p, c->K32.p, c->cdof.p,
+                                                          nbnd, penalty, md.p);
+        c->launches += 1;
+        unsigned long long bits = 0;
+        LMTG_CUDA(cudaMemcpyAsync(&bits, md.p, 8, cudaMemcpyDeviceToHost, s));
+        LMTG_CUDA(cudaStreamSynchronize(s));
+        memcpy(&c->max_diag, &bits, 8);
+    }
+    k_jacobi_s<double><<<grid_for(c, c->nn, 256), 256, 0, s>>>(c->bdiag.p, c->K64.p, c->nn, c->Dinv64.p,
+                                                               c->K32.p);
+    LMTG_CUDA(cudaGetLastError());
+    c->launches += 1;
+    LMTG_CUDA(cudaStreamSynchronize(s));
+    c->have64 = true;
+}
+
+int diff_run(lmtg_ctx *c, int nsteps, double tol, int maxit, lmtg_solve_stats *st) {
+    int total = 0, status = LMTG_OK;
+    for (int n = 0; n < nsteps && status == LMTG_OK; ++n) {
+        int it = 0;
+        status = diff_step(c, c->u.p, c->u.p, tol, maxit, &it);
+        total += it;
+    }
+    st->iterations = total;
+    st->outer_iterations = nsteps;
+    return status;
+}
+
+// Final-time misfit J = 1/2 |T_N - target|^2 and dJ/dk_e (k = conductivity; a = k / rho_c) with
+// checkpoints every `ck` steps: the forward sweep keeps T at steps 0, ck, 2ck, ...; the backward
+// sweep recomputes each segment's states from its checkpoint, then walks the adjoint
+//   A lambda_N = T_N - target,   A lambda_n = B lambda_{n+1},
+//   dJ/da_e = -sum_n lambda_n^T Khat_e (theta T_n + (1 - theta) T_{n-1}).
+int diff_adjoint(lmtg_ctx *c, int nsteps, int ck, const double *target_dev, double tol, int maxit,
+                 double *J, std::vector<double> &grad, lmtg_solve_stats *st) {
+    cudaStream_t s = c->stream;
+    const uint64_t nn = c->nn;
+    const int nck = nsteps / ck + 1;
+    DBuf<double> ckpt, seg, lam, lam2, g;
+    ckpt.alloc((uint64_t)nck * nn);
+    seg.alloc((uint64_t)(ck + 1) * nn);
+    lam.alloc(nn);
+    lam2.alloc(nn);
+    g.alloc(c->ne);
+    LMTG_CUDA(cudaMemsetAsync(g.p, 0, c->ne * 8, s));
+    int total = 0, status = LMTG_OK, it = 0;
+    // forward with checkpoints (u holds T_0 on entry)
+    LMTG_CUDA(cudaMemcpyAsync(ckpt.p, c->u.p, nn * 8, cudaMemcpyDeviceToDevice, s));
+    for (int n = 1; n <= nsteps && status == LMTG_OK; ++n) {
+        status = diff_step(c, c->u.p, c->u.p, tol, maxit, &it);
+        total += it;
+        if (n % ck == 0) LMTG_CUDA(cudaMemcpyAsync(ckpt.p + (uint64_t)(n / ck) * nn, c->u.p, nn * 8,
+                                                   cudaMemcpyDeviceToDevice, s));
+    }
+    if (status != LMTG_OK) return status;
+    // objective and the final adjoint
+    k_axpby<<<ngrid(c), kRowThreads, 0, s>>>(c->u.p, target_dev, c->w64[5].p, nn);
+    c->launches += 1;
+    {
+        std::vector<double> d(nn);
+        LMTG_CUDA(cudaMemcpyAsync(d.data(), c->w64[5].p, nn * 8, cudaMemcpyDeviceToHost, s));
+        LMTG_CUDA(cudaStreamSynchronize(s));
+        double acc = 0;
+        for (double v : d) acc += v * v;
+        *J = 0.5 * acc;
+    }
+    LMTG_CUDA(cudaMemsetAsync(lam.p, 0, nn * 8, s));
+    status = diff_pcg(c, c->w64[5].p, lam.p, tol, maxit, &it);
+    total += it;
+    if (status != LMTG_OK) return status;
+    // backward over segments
+    for (int seg_start = ((nsteps - 1) / ck) * ck; seg_start >= 0 && status == LMTG_OK; seg_start -= ck) {
+        const int seg_end = std::min(seg_start + ck, nsteps);
+        LMTG_CUDA(cudaMemcpyAsync(seg.p, ckpt.p + (uint64_t)(seg_start / ck) * nn, nn * 8,
+                                  cudaMemcpyDeviceToDevice, s));
+        for (int n = seg_start + 1; n <= seg_end && status == LMTG_OK; ++n) {
+            status = diff_step(c, seg.p + (uint64_t)(n - 1 - seg_start) * nn,
+                               seg.p + (uint64_t)(n - seg_start) * nn, tol, maxit, &it);
+            total += it;
+        }
+        for (int n = seg_end; n > seg_start && status == LMTG_OK; --n) {
+            const double *Tn = seg.p + (uint64_t)(n - seg_start) * nn;
+            const double *Tm = seg.p + (uint64_t)(n - 1 - seg_start) * nn;
+            k_tri6_grad<<<grid_for(c, c->ne, 128, 16), 128, 0, s>>>(c->pos.p, c->conn.p, c->ne,
+                                                                    c->theta, lam.p, Tn, Tm, g.p);
+            c->launches += 1;
+            if (n > 1) {  // lambda_{n-1}: A lambda_{n-1} = B lambda_n
+                diff_rhs(c, lam.p, lam2.p);
+                LMTG_CUDA(cudaMemcpyAsync(lam.p, lam2.p, nn * 8, cudaMemcpyDeviceToDevice, s));
+                status = diff_pcg(c, lam2.p, lam.p, tol, maxit, &it);
+                total += it;
+            }
+        }
+    }
+    grad.resize(c->ne);
+    LMTG_CUDA(cudaMemcpyAsync(grad.data(), g.p, c->ne * 8, cudaMemcpyDeviceToHost, s));
+    LMTG_CUDA(cudaStreamSynchronize(s));
+    // dJ/dk = dJ/da / rho_c
+    for (double &v : grad) v /= c->rho_c;
+    st->iterations = total;
+    st->outer_iterations = nsteps;
+    return status;
+}
+
+}  // namespace lmtg
+
+using namespace lmtg;
+
+namespace {
+
+template <class F>
+int guard_d(lmtg_ctx *c, F &&f) {
+    if (!c) return LMTG_ERR_ARG;
+    try {
+        cudaError_t e = cudaSetDevice(c->device);
+        if (e != cudaSuccess) throw Error{LMTG_ERR_CUDA, cudaGetErrorString(e)};
+        int s = f();
+        if (s == LMTG_OK) c->err.clear();
+        return s;
+    } catch (const Error &e) {
+        c->err = e.msg;
+        return e.status;
+    } catch (const std::bad_alloc &) {
+        c->err = "host allocation failed";
+        return LMTG_ERR_NOMEM;
+    } catch (const std::exception &e) {
+        c->err = e.what();
+        return LMTG_ERR_CUDA;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int lmtg_make_rect_triangle6(const double X0[2], const double X1[2], const uint32_t nbp[2],
+                             uint64_t *nn_out, uint64_t *ne_out, double *pos, uint32_t *conn) {
+    if (!X0 || !X1 || !nbp || !nn_out || !ne_out) return LMTG_ERR_ARG;
+    const uint64_t nx = nbp[0], ny = nbp[1];
+    if (nx < 2 || ny < 2) return LMTG_ERR_ARG;
+    const uint64_t gx = 2 * nx - 1, gy = 2 * ny - 1;
+    if (gx * gy >= (1ull << 32)) return LMTG_ERR_UNSUPPORTED;
+    *nn_out = gx * gy;
+    *ne_out = 2 * (nx - 1) * (ny - 1);
+    if (!pos || !conn) return LMTG_OK;
+    // half-step grid of Rectilinear_iterator (accumulated, x fastest), make_rect.h:148-150
+    std::vector<double> ax[2];
+    for (int d = 0; d < 2; ++d) {
+        const double lo = std::fmin(X0[d], X1[d]), hi = std::fmax(X0[d], X1[d]);
+        const double inc = (hi - lo) / ((double)nbp[d] - 1.0) * .5;
+        const double step = inc + (inc == 0.0 ? 1.0 : 0.0), upper = hi + step * 0.5;
+        const uint64_t want = d ? gy : gx;
+        for (double p = lo; p < upper; p += step) {
+            if (ax[d].size() == want) return LMTG_ERR_ARG;
+            ax[d].push_back(p);
+        }
+        if (ax[d].size() != want) return LMTG_ERR_ARG;
+    }
+    uint64_t n = 0;
+    for (uint64_t j = 0; j < gy; ++j)
+        for (uint64_t i = 0; i < gx; ++i, ++n) {
+            pos[2 * n] = ax[0][i];
+            pos[2 * n + 1] = ax[1][j];
+        }
+    // two triangles per cell, make_rect.h:153-167
+    uint64_t e = 0;
+    const uint64_t r = 2 * nx - 1;
+    for (uint64_t i = 0; i + 1 < ny; ++i)
+        for (uint64_t j = 0; j + 1 < nx; ++j) {
+            const uint64_t b = 2 * i * r + 2 * j;
+            const uint64_t p[9] = {b, b + 1, b + 2, b + r, b + 1 + r, b + 2 + r,
+                                   b + 2 * r, b + 1 + 2 * r, b + 2 + 2 * r};
+            const uint64_t t1[6] = {p[0], p[2], p[6], p[1], p[4], p[3]};
+            const uint64_t t2[6] = {p[2], p[8], p[6], p[5], p[7], p[4]};
+            for (int a = 0; a < 6; ++a) conn[6 * e + a] = (uint32_t)t1[a];
+            ++e;
+            for (int a = 0; a < 6; ++a) conn[6 * e + a] = (uint32_t)t2[a];
+            ++e;
+        }
+    return LMTG_OK;
+}
+
+int lmtg_diff_mesh_set(lmtg_ctx *c, uint64_t nn, const double *pos, uint64_t ne,
+                       const uint32_t *conn) {
+    return guard_d(c, [&] {
+        LMTG_CHECK(pos && conn && nn > 0 && ne > 0, LMTG_ERR_ARG, "empty mesh");
+        LMTG_CHECK(nn < (1ull << 32), LMTG_ERR_UNSUPPORTED, "more than 2^32 nodes");
+        for (uint64_t q = 0; q < 6 * ne; ++q) LMTG_CHECK(conn[q] < nn, LMTG_ERR_ARG, "node id >= nn");
+        c->elem_type = LMTG_ELEM_TRIANGLE6;
+        c->npe = 6;
+        c->nnu = 1;
+        c->npairs = 21;
+        c->nn = nn;
+        c->ne = ne;
+        c->n = nn;
+        c->pos.alloc(2 * nn);
+        LMTG_CUDA(cudaMemcpyAsync(c->pos.p, pos, 16 * nn, cudaMemcpyHostToDevice, c->stream));
+        upload_u32(c, c->conn, conn, 6 * ne);
+        c->allocated = c->have64 = c->have32 = c->have_vec = false;
+        LMTG_CUDA(cudaStreamSynchronize(c->stream));
+        return LMTG_OK;
+    });
+}
+
+int lmtg_diff_setup(lmtg_ctx *c, const double *k, uint64_t nk, double rho_c, double dt,
+                    double theta, uint64_t nbnd, const uint32_t *bnd, double penalty) {
+    return guard_d(c, [&] {
+        LMTG_CHECK(k && (nbnd == 0 || bnd), LMTG_ERR_ARG, "null arrays");
+        for (uint64_t q = 0; q < nbnd; ++q) LMTG_CHECK(bnd[q] < c->nn, LMTG_ERR_ARG, "node id >= nn");
+        LMTG_CHECK(nbnd == 0 || penalty > 0, LMTG_ERR_UNSUPPORTED, "penalty constraints only");
+        diff_setup(c, k, nk, rho_c, dt, theta, nbnd, bnd, penalty);
+        return LMTG_OK;
+    });
+}
+
+int lmtg_diff_set_state(lmtg_ctx *c, const double *T) {
+    return guard_d(c, [&] {
+        LMTG_CHECK(c->allocated && c->elem_type == LMTG_ELEM_TRIANGLE6 && T, LMTG_ERR_STATE, "setup first");
+        LMTG_CUDA(cudaMemcpyAsync(c->u.p, T, c->nn * 8, cudaMemcpyHostToDevice, c->stream));
+        LMTG_CUDA(cudaStreamSynchronize(c->stream));
+        return LMTG_OK;
+    });
+}
+
+int lmtg_diff_get_state(lmtg_ctx *c, double *T) {
+    return guard_d(c, [&] {
+        LMTG_CHECK(c->allocated && c->elem_type == LMTG_ELEM_TRIANGLE6 && T, LMTG_ERR_STATE, "setup first");
+        LMTG_CUDA(cudaMemcpyAsync(T, c->u.p, c->nn * 8, cudaMemcpyDeviceToHost, c->stream));
+        LMTG_CUDA(cudaStreamSynchronize(c->stream));
+        return LMTG_OK;
+    });
+}
+
+int lmtg_diff_run(lmtg_ctx *c, int nsteps, double tol, int maxit, lmtg_solve_stats *st) {
+    lmtg_solve_stats local{};
+    if (!st) st = &local;
+    memset(st, 0, sizeof(*st));
+    return guard_d(c, [&] {
+        LMTG_CHECK(c->have64 && c->elem_type == LMTG_ELEM_TRIANGLE6, LMTG_ERR_STATE, "setup first");
+        LMTG_CHECK(nsteps >= 0 && maxit > 0, LMTG_ERR_ARG, "nsteps >= 0, maxit > 0");
+        cudaEvent_t e0, e1;
+        LMTG_CUDA(cudaEventCreate(&e0));
+        LMTG_CUDA(cudaEventCreate(&e1));
+        LMTG_CUDA(cudaEventRecord(e0, c->stream));
+        int s = diff_run(c, nsteps, tol, maxit, st);
+        LMTG_CUDA(cudaEventRecord(e1, c->stream));
+        LMTG_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        st->device_ms = ms;
+        st->status = s;
+        if (s != LMTG_OK) c->err = lmtg_status_string(s);
+        return s;
+    });
+}
+
+int lmtg_diff_adjoint_misfit(lmtg_ctx *c, int nsteps, int ck, const double *target, double tol,
+                             int maxit, double *J, double *dJdk, lmtg_solve_stats *st) {
+    lmtg_solve_stats local{};
+    if (!st) st = &local;
+    memset(st, 0, sizeof(*st));
+    return guard_d(c, [&] {
+        LMTG_CHECK(c->have64 && c->elem_type == LMTG_ELEM_TRIANGLE6, LMTG_ERR_STATE, "setup first");
+        LMTG_CHECK(nsteps > 0 && ck > 0 && maxit > 0 && J && dJdk, LMTG_ERR_ARG, "bad arguments");
+        DBuf<double> t;
+        if (target) {
+            t.alloc(c->nn);
+            LMTG_CUDA(cudaMemcpyAsync(t.p, target, c->nn * 8, cudaMemcpyHostToDevice, c->stream));
+        }
+        cudaEvent_t e0, e1;
+        LMTG_CUDA(cudaEventCreate(&e0));
+        LMTG_CUDA(cudaEventCreate(&e1));
+        LMTG_CUDA(cudaEventRecord(e0, c->stream));
+        std::vector<double> g;
+        int s = diff_adjoint(c, nsteps, ck, t.p, tol, maxit, J, g, st);
+        LMTG_CUDA(cudaEventRecord(e1, c->stream));
+        LMTG_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        st->device_ms = ms;
+        st->status = s;
+        if (s != LMTG_OK) {
+            c->err = std::string("diffusion adjoint: ") + lmtg_status_string(s);
+            return s;
+        }
+        memcpy(dJdk, g.data(), c->ne * 8);
+        return LMTG_OK;
+    });
+}
+
+int lmtg_diff_get_matrices(lmtg_ctx *c, uint64_t *rowptr, uint32_t *col, double *A, double *B) {
+    return guard_d(c, [&] {
+        LMTG_CHECK(c->have64 && c->elem_type == LMTG_ELEM_TRIANGLE6, LMTG_ERR_STATE, "setup first");
+        LMTG_CHECK(rowptr && col && A && B, LMTG_ERR_ARG, "null output");
+        std::vector<uint32_t> bptr(c->nn + 1), bcol(c->nnzb);
+        std::vector<double> hA(c->nnzb), hB(c->nnzb);
+        LMTG_CUDA(cudaMemcpy(bptr.data(), c->bptr.p, bptr.size() * 4, cudaMemcpyDeviceToHost));
+        LMTG_CUDA(cudaMemcpy(bcol.data(), c->bcol.p, bcol.size() * 4, cudaMemcpyDeviceToHost));
+        LMTG_CUDA(cudaMemcpy(hA.data(), c->K64.p, hA.size() * 8, cudaMemcpyDeviceToHost));
+        LMTG_CUDA(cudaMemcpy(hB.data(), c->B64.p, hB.size() * 8, cudaMemcpyDeviceToHost));
+        uint64_t w = 0;
+        rowptr[0] = 0;
+        for (uint64_t i = 0; i < c->nn; ++i) {
+            for (uint32_t q = bptr[i]; q < bptr[i + 1]; ++q) {
+                if (bcol[q] > i) break;
+                col[w] = bcol[q];
+                A[w] = hA[q];
+                B[w] = hB[q];
+                ++w;
+            }
+            rowptr[i + 1] = w;
+        }
+        return LMTG_OK;
+    });
+}
+
+}  // extern "C"

@@ -115,6 +115,11 @@ struct lmtg_ctx {
     // values
     lmtg::DBuf<double> Ke64, K64, F, u, Dinv64;
     lmtg::DBuf<double> adj_rhs, adj_lam, grad;  // adjoint workspace
+
+    // heat diffusion (Triangle_6, one unknown per node): K64 holds A = M/dt + theta K,
+    // B64 holds B = M/dt - (1 - theta) K, K32 the FP32 copy of A; Ke64 / KeB64 the element blocks
+    lmtg::DBuf<double> B64, KeB64;
+    double rho_c = 1.0, dt = 0.0, theta = 0.5;
     lmtg::DBuf<float> Ke32, K32, Dinv32;
     bool have64 = false, have32 = false, have_vec = false;
     double max_diag = 0;
@@ -154,6 +159,19 @@ void copy_k64_to_k32(lmtg_ctx *c);
 
 // ---- adjoint (adjoint.cu) ----
 void launch_grad_E(lmtg_ctx *c, const double *a, const double *b, double *g);
+
+// ---- heat diffusion (diffusion.cu) ----
+void diff_setup(lmtg_ctx *c, const double *k, uint64_t nk, double rho_c, double dt, double theta,
+                uint64_t nbnd, const uint32_t *bnd, double penalty);
+int diff_run(lmtg_ctx *c, int nsteps, double tol, int maxit, lmtg_solve_stats *st);
+int diff_adjoint(lmtg_ctx *c, int nsteps, int ck, const double *target_dev, double tol, int maxit,
+                 double *J, std::vector<double> &grad, lmtg_solve_stats *st);
+
+template <class T>
+inline void upload_u32(lmtg_ctx *c, DBuf<T> &d, const T *h, size_t n) {
+    d.alloc(n);
+    if (n) LMTG_CUDA(cudaMemcpyAsync(d.p, h, n * sizeof(T), cudaMemcpyHostToDevice, c->stream));
+}
 
 // ---- solver (solver.cu) ----
 void spmv64(lmtg_ctx *c, const double *x, double *y);

@@ -565,6 +565,141 @@ int orc_tri6_traction(uint64_t nfaces, const uint32_t *faces, const double *pos,
 }
 
 /* ------------------------------------------------------------------------------------------
+ * Heat diffusion (formulations/formulation_difftherm.py:24-30) on Triangle_6.
+ * make_rect(m, Triangle_6(), X0, X1, nb_points) -- include/mesh/make_rect.h:141-170: nodes on
+ * the (2 nx - 1) x (2 ny - 1) half-step grid created by Rectilinear_iterator (accumulated
+ * coordinates, x fastest), incr = (X1 - X0) / (nb_points - 1) * 0.5; two triangles per cell.
+ * ------------------------------------------------------------------------------------------ */
+int orc_make_rect_triangle6(const double X0_[2], const double X1_[2], const uint32_t nbp[2],
+                            uint64_t *nn_out, uint64_t *ne_out, double *pos, uint32_t *conn) {
+    const uint32_t nx = nbp[0], ny = nbp[1];
+    if (nx < 2 || ny < 2) return -1;
+    const uint64_t gx = 2ull * nx - 1, gy = 2ull * ny - 1;
+    *nn_out = gx * gy;
+    *ne_out = 2ull * (nx - 1) * (ny - 1);
+    if (!pos || !conn) return 0;
+    double c[2][8192 * 2];
+    uint64_t cnt[2] = {0, 0};
+    for (int d = 0; d < 2; ++d) {
+        const double lo = X0_[d] < X1_[d] ? X0_[d] : X1_[d], hi = X0_[d] < X1_[d] ? X1_[d] : X0_[d];
+        const double inc = (hi - lo) / ((double)nbp[d] - 1.0) * .5;
+        const double step = inc + (inc == 0.0 ? 1.0 : 0.0), upper = hi + step * 0.5;
+        for (double p = lo; p < upper; p += step) {
+            if (cnt[d] >= (d ? gy : gx) || cnt[d] >= 16384) return -1;
+            c[d][cnt[d]++] = p;
+        }
+    }
+    if (cnt[0] != gx || cnt[1] != gy) return -1;
+    uint64_t n = 0;
+    for (uint64_t j = 0; j < gy; ++j)
+        for (uint64_t i = 0; i < gx; ++i, ++n) {
+            pos[2 * n] = c[0][i];
+            pos[2 * n + 1] = c[1][j];
+        }
+    uint64_t e = 0;
+    for (uint64_t i = 0; i + 1 < ny; ++i)
+        for (uint64_t j = 0; j + 1 < nx; ++j) {
+            const uint64_t b = 2 * i * (2 * nx - 1) + 2 * j, r = 2 * nx - 1;
+            const uint64_t p[9] = {b, b + 1, b + 2, b + r, b + 1 + r, b + 2 + r, b + 2 * r, b + 1 + 2 * r, b + 2 + 2 * r};
+            const uint64_t t1[6] = {p[0], p[2], p[6], p[1], p[4], p[3]};
+            const uint64_t t2[6] = {p[2], p[8], p[6], p[5], p[7], p[4]};
+            for (int a = 0; a < 6; ++a) conn[6 * e + a] = (uint32_t)t1[a];
+            ++e;
+            for (int a = 0; a < 6; ++a) conn[6 * e + a] = (uint32_t)t2[a];
+            ++e;
+        }
+    return 0;
+}
+
+/* 6-point rule of the Python element description used when the formulation integrates the
+ * element in closed form (integration_totale, formulations/element_Triangle_6.py:92-99). */
+int orc_gauss_triangle_6pt(double *w, double *xi) {
+    const double a = 0.445948490915965, b = 0.091576213509771;
+    const double wa = 0.111690794839005, wb = 0.054975871827661;
+    const double t[6][3] = {{wa, a, a}, {wa, 1.0 - 2.0 * a, a}, {wa, a, 1.0 - 2.0 * a},
+                            {wb, b, b}, {wb, 1.0 - 2.0 * b, b}, {wb, b, 1.0 - 2.0 * b}};
+    for (int g = 0; g < 6; ++g) {
+        w[g] = t[g][0];
+        xi[2 * g] = t[g][1];
+        xi[2 * g + 1] = t[g][2];
+    }
+    return 6;
+}
+
+static void tri6_shape(double u, double v, double N[6], double dN[6][2]) {
+    const double X0 = 1 - u - v;
+    N[0] = X0 * (2 * X0 - 1); N[1] = u * (2 * u - 1); N[2] = v * (2 * v - 1);
+    N[3] = 4 * X0 * u;        N[4] = 4 * u * v;       N[5] = 4 * v * X0;
+    dN[0][0] = -(4 * X0 - 1); dN[0][1] = -(4 * X0 - 1);
+    dN[1][0] = 4 * u - 1;     dN[1][1] = 0;
+    dN[2][0] = 0;             dN[2][1] = 4 * v - 1;
+    dN[3][0] = 4 * (X0 - u);  dN[3][1] = -4 * u;
+    dN[4][0] = 4 * v;         dN[4][1] = 4 * u;
+    dN[5][0] = -4 * v;        dN[5][1] = 4 * (X0 - v);
+}
+
+/* Element matrices of the diffusion weak form a grad T . grad v + T' v: stiffness
+ * Ke = int a gradN_i . gradN_j (a = conductivity / (density * heat capacity), given directly)
+ * and mass Me = int N_i N_j, both 6x6 row-major. */
+void orc_triangle6_diff_km(const double *xy, double a, double *Ke, double *Me) {
+    double w[6], xi[12];
+    orc_gauss_triangle_6pt(w, xi);
+    memset(Ke, 0, sizeof(double) * 36);
+    memset(Me, 0, sizeof(double) * 36);
+    for (int g = 0; g < 6; ++g) {
+        double N[6], dN[6][2];
+        tri6_shape(xi[2 * g], xi[2 * g + 1], N, dN);
+        double J[2][2] = {{0, 0}, {0, 0}};
+        for (int k = 0; k < 6; ++k)
+            for (int i = 0; i < 2; ++i)
+                for (int j = 0; j < 2; ++j) J[i][j] += xy[2 * k + i] * dN[k][j];
+        const double det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+        const double Ji[2][2] = {{J[1][1] / det, -J[0][1] / det}, {-J[1][0] / det, J[0][0] / det}};
+        double gx[6][2];
+        for (int k = 0; k < 6; ++k)
+            for (int i = 0; i < 2; ++i) gx[k][i] = Ji[0][i] * dN[k][0] + Ji[1][i] * dN[k][1];
+        const double f = w[g] * det;
+        for (int i = 0; i < 6; ++i)
+            for (int j = 0; j < 6; ++j) {
+                Ke[6 * i + j] += f * a * (gx[i][0] * gx[j][0] + gx[i][1] * gx[j][1]);
+                Me[6 * i + j] += f * N[i] * N[j];
+            }
+    }
+}
+
+/* Theta-scheme matrices A = M/dt + theta K and B = M/dt - (1-theta) K on the structural lower
+ * pattern (nnu = 1).  theta = 1/2 is the reference's time integration: the residual evaluated
+ * at the midpoint of [t_n, t_n+1] with the unknown interpolated linearly
+ * (formal_lf/formulation.py:506-509, formal_lf/extrapolation.py:21-40,
+ * formal_lf/gauss_integration.py:52-63, left/right_time_integration 0/1). */
+int orc_assemble_diff(uint64_t nn, uint64_t ne, const double *pos, const uint32_t *conn,
+                      const double *a, int a_per_elem, double rho_c, double dt, double theta,
+                      const uint64_t *rowptr, const uint32_t *col, double *A, double *B) {
+    memset(A, 0, sizeof(double) * rowptr[nn]);
+    memset(B, 0, sizeof(double) * rowptr[nn]);
+    double xy[12], Ke[36], Me[36];
+    for (uint64_t e = 0; e < ne; ++e) {
+        const uint32_t *c = conn + 6 * e;
+        for (int k = 0; k < 6; ++k) {
+            xy[2 * k] = pos[2 * (uint64_t)c[k]];
+            xy[2 * k + 1] = pos[2 * (uint64_t)c[k] + 1];
+        }
+        /* diffusivity a = conductivity / (density * heat capacity) (formulation_difftherm.py:25) */
+        orc_triangle6_diff_km(xy, a[a_per_elem ? e : 0] / rho_c, Ke, Me);
+        for (int i = 0; i < 6; ++i)
+            for (int j = 0; j < 6; ++j) {
+                const uint64_t r = c[i], s = c[j];
+                if (s > r) continue;
+                const uint64_t p = find_col(rowptr, col, r, (uint32_t)s);
+                if (p == (uint64_t)-1) return -2;
+                A[p] += Me[6 * i + j] / dt + theta * Ke[6 * i + j];
+                B[p] += Me[6 * i + j] / dt - (1.0 - theta) * Ke[6 * i + j];
+            }
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------------------------
  * Skyline (envelope) Cholesky, used as the oracle's direct solver in place of the vendored
  * LDL (include/util/solveLDL.cpp:44-125): same factorization mathematics, no ordering.
  * ------------------------------------------------------------------------------------------ */

@@ -46,6 +46,10 @@ int orc_make_rect_hexa(const double X0[3], const double X1[3], const uint32_t nb
 int orc_make_rect_tetra10(const double X0[3], const double X1[3], const uint32_t nb_points[3],
                           uint64_t *nn, uint64_t *ne, double *pos, uint32_t *conn);
 
+/* Structured Triangle_6 mesh (2 triangles per cell), pos nn*2.  Two-phase like Tetra_10. */
+int orc_make_rect_triangle6(const double X0[2], const double X1[2], const uint32_t nb_points[2],
+                            uint64_t *nn, uint64_t *ne, double *pos, uint32_t *conn);
+
 /* ---------------- Gauss tables (reference C++ tables, 12-digit constants) ---------------- */
 /* Returns number of points; w[np], xi[np*dim]. */
 int orc_gauss_hexa_order2(double *w, double *xi);
@@ -65,6 +69,10 @@ double orc_tetra10_elast_gp(const double *xyz, double E, double nu, double w, co
                             double *Ke);
 void orc_tetra10_elast_ke(const double *xyz, double E, double nu, double *Ke);
 
+/* Triangle_6 heat diffusion: stiffness a grad.grad and mass N N (6x6 each, 6-point rule). */
+int orc_gauss_triangle_6pt(double *w, double *xi);
+void orc_triangle6_diff_km(const double *xy, double a, double *Ke, double *Me);
+
 /* ---------------- pattern / assembly ---------------- */
 /* Structural lower pattern (node-pair product x nnu^2, j<=i).  rowptr has n+1 entries.
  * Phase 1: col==NULL returns nnz in *nnz (rowptr filled).  Phase 2 fills col. */
@@ -76,6 +84,13 @@ int orc_pattern_lower(uint64_t nn, int nnu, uint64_t ne, int npe, const uint32_t
 int orc_assemble_elast(int npe, uint64_t nn, uint64_t ne, const double *pos, const uint32_t *conn,
                        const double *E, int E_per_elem, double nu,
                        const uint64_t *rowptr, const uint32_t *col, double *val);
+
+/* Theta-scheme matrices A = M/dt + theta K, B = M/dt - (1-theta) K on the lower pattern of a
+ * Triangle_6 mesh (nnu = 1); K uses the diffusivity conductivity / rho_c (a has ne or 1 values
+ * of the conductivity). */
+int orc_assemble_diff(uint64_t nn, uint64_t ne, const double *pos, const uint32_t *conn,
+                      const double *a, int a_per_elem, double rho_c, double dt, double theta,
+                      const uint64_t *rowptr, const uint32_t *col, double *A, double *B);
 
 /* Consistent nodal loads of a uniform traction on Quad4 faces (4 node ids per face,
  * order-2 quad rule).  F has nn*3 entries and is accumulated. */

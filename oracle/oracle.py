@@ -253,3 +253,76 @@ def elasticity_problem(nb_points, E=210000.0, nu=0.3, pen=1e5, traction=(1.0, 0.
     md = penalty(rowptr, col, val, F, dofs, np.ones(dofs.shape[0]), np.zeros(dofs.shape[0]), pen)
     return dict(pos=pos, conn=conn, rowptr=rowptr, col=col, val=val, F=F, faces=faces, dofs=dofs,
                 max_diag=md, E=E, nu=nu, penalty=pen)
+
+
+# ---------------------------------------------------------------------------------------------
+# heat diffusion on Triangle_6 (formulations/formulation_difftherm.py)
+# ---------------------------------------------------------------------------------------------
+def make_rect_triangle6(nb_points, X0=(0.0, 0.0), X1=(1.0, 1.0)):
+    nbp = np.asarray(nb_points if np.ndim(nb_points) else [nb_points] * 2, dtype=np.uint32)
+    x0 = np.asarray(X0, dtype=np.float64)
+    x1 = np.asarray(X1, dtype=np.float64)
+    nn, ne = ctypes.c_uint64(), ctypes.c_uint64()
+    L = lib()
+    L.orc_make_rect_triangle6(_p(x0, _f64p), _p(x1, _f64p), _p(nbp, _u32p), ctypes.byref(nn),
+                              ctypes.byref(ne), None, None)
+    pos = np.zeros((nn.value, 2))
+    conn = np.zeros((ne.value, 6), dtype=np.uint32)
+    rc = L.orc_make_rect_triangle6(_p(x0, _f64p), _p(x1, _f64p), _p(nbp, _u32p), ctypes.byref(nn),
+                                   ctypes.byref(ne), _p(pos, _f64p), _p(conn, _u32p))
+    if rc:
+        raise RuntimeError("orc_make_rect_triangle6 failed: %d" % rc)
+    return pos, conn
+
+
+def triangle6_km(xy, a):
+    xy = np.ascontiguousarray(xy, dtype=np.float64)
+    Ke, Me = np.zeros((6, 6)), np.zeros((6, 6))
+    lib().orc_triangle6_diff_km(_p(xy, _f64p), ctypes.c_double(a), _p(Ke, _f64p), _p(Me, _f64p))
+    return Ke, Me
+
+
+def assemble_diff(pos, conn, k, rho_c, dt, theta, rowptr, col):
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    conn = np.ascontiguousarray(conn, dtype=np.uint32)
+    k = np.ascontiguousarray(np.atleast_1d(k), dtype=np.float64)
+    A, B = np.zeros(col.shape[0]), np.zeros(col.shape[0])
+    rc = lib().orc_assemble_diff(ctypes.c_uint64(pos.shape[0]), ctypes.c_uint64(conn.shape[0]),
+                                 _p(pos, _f64p), _p(conn, _u32p), _p(k, _f64p),
+                                 ctypes.c_int(1 if k.shape[0] > 1 else 0), ctypes.c_double(rho_c),
+                                 ctypes.c_double(dt), ctypes.c_double(theta), _p(rowptr, _u64p),
+                                 _p(col, _u32p), _p(A, _f64p), _p(B, _f64p))
+    if rc:
+        raise RuntimeError("orc_assemble_diff failed: %d" % rc)
+    return A, B
+
+
+def boundary_nodes_2d(pos, eps=1e-9):
+    return np.nonzero((pos[:, 0] < eps) | (pos[:, 1] < eps) | (pos[:, 0] > 1 - eps) | (pos[:, 1] > 1 - eps))[0]
+
+
+def gaussian_bump(pos, centre=(0.5, 0.5), sigma=0.1):
+    d2 = (pos[:, 0] - centre[0]) ** 2 + (pos[:, 1] - centre[1]) ** 2
+    return np.exp(-d2 / (2 * sigma * sigma))
+
+
+def diffusion_problem(nb_points, k=1.0, rho_c=1.0, dt=1e-4, theta=0.5, pen=1e5):
+    """Heat diffusion on the unit square of Triangle_6: theta-scheme matrices (A with the penalty
+    T = 0 on the boundary, max|diag A| scale), the Gaussian-bump initial field."""
+    pos, conn = make_rect_triangle6(nb_points)
+    rowptr, col = pattern_lower(pos.shape[0], 1, conn)
+    A, B = assemble_diff(pos, conn, k, rho_c, dt, theta, rowptr, col)
+    bnd = boundary_nodes_2d(pos)
+    md = penalty(rowptr, col, A, None, bnd, np.ones(bnd.shape[0]), np.zeros(bnd.shape[0]), pen)
+    return dict(pos=pos, conn=conn, rowptr=rowptr, col=col, A=A, B=B, bnd=bnd, max_diag=md,
+                T0=gaussian_bump(pos), k=k, rho_c=rho_c, dt=dt, theta=theta, penalty=pen)
+
+
+def diffusion_run(P, nsteps, T0=None):
+    """CPU theta-scheme: A T_{n+1} = B T_n with the direct solver; returns all states."""
+    T = np.array(P["T0"] if T0 is None else T0, dtype=np.float64)
+    states = [T.copy()]
+    for _ in range(nsteps):
+        T = skyline_solve(P["rowptr"], P["col"], P["A"], spmv(P["rowptr"], P["col"], P["B"], T))
+        states.append(T.copy())
+    return states

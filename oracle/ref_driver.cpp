@@ -17,6 +17,7 @@
  * (formal_lf/calculate_matrix.py:86-98): for each Gauss point, matrix(i,j) += tmp for j >= i.
  *
  * Usage: ref_driver hexa|tetra10 <nb_points> <E> <nu> <penalty> <outdir>
+ *        ref_driver tri6 <nb_points> <conductivity> <rho_c> <dt> <theta> <penalty> <outdir>
  * Writes little-endian raw arrays: pos.f64 conn.u32 rowptr.u64 col.u32 val.f64 F.f64
  * u_ldl.f64 u_icpcg.f64 lam_ldl.f64 (LDL solution of K lambda = u_ldl) and info.txt.
  */
@@ -52,7 +53,91 @@ static void read_mesh(TM &m, int npe, std::vector<double> &pos, std::vector<unsi
             conn[npe * e + a] = m.node_list.number(*m.elem_list[e]->node_virtual(a));
 }
 
+/* Heat diffusion on Triangle_6: mesh, theta-scheme matrices A and B in the reference's Sym
+ * SparseLine storage (oracle element integrand, per-element scatter), penalty on the boundary,
+ * and one step A T1 = B T0 solved with the reference's LDL.
+ * usage: ref_driver tri6 <nb_points> <conductivity> <rho_c> <dt> <theta> <penalty> <outdir> */
+static int run_tri6(int argc, char **argv) {
+    if (argc != 9) return 1;
+    unsigned nbp = atoi(argv[2]);
+    double k = atof(argv[3]), rho_c = atof(argv[4]), dt = atof(argv[5]), theta = atof(argv[6]),
+           penalty = atof(argv[7]);
+    std::string out = argv[8];
+    typedef Mesh<MeshCaracStd<2, 2, 0, double, 2> > TM; /* nb=0, degree 2 -> Triangle_6 */
+    TM m;
+    make_rect(m, Triangle_6(), TM::Pvec(0, 0), TM::Pvec(1, 1), TM::Pvec(nbp, nbp));
+    unsigned nn = m.node_list.size(), ne = m.elem_list.size();
+    std::vector<double> pos(2 * nn);
+    for (unsigned i = 0; i < nn; ++i)
+        for (int d = 0; d < 2; ++d) pos[2 * i + d] = m.node_list[i].pos[d];
+    std::vector<unsigned> conn(6 * ne);
+    for (unsigned e = 0; e < ne; ++e)
+        for (int a = 0; a < 6; ++a) conn[6 * e + a] = m.node_list.number(*m.elem_list[e]->node_virtual(a));
+    Mat<double, Sym<>, SparseLine<> > A(nn, nn), B(nn, nn);
+    for (unsigned e = 0; e < ne; ++e) {
+        double xy[12], Ke[36], Me[36];
+        for (int a = 0; a < 6; ++a)
+            for (int d = 0; d < 2; ++d) xy[2 * a + d] = pos[2 * conn[6 * e + a] + d];
+        orc_triangle6_diff_km(xy, k / rho_c, Ke, Me);
+        for (int i = 0; i < 6; ++i)
+            for (int j = i; j < 6; ++j) {
+                A(conn[6 * e + i], conn[6 * e + j]) += Me[6 * i + j] / dt + theta * Ke[6 * i + j];
+                B(conn[6 * e + i], conn[6 * e + j]) += Me[6 * i + j] / dt - (1 - theta) * Ke[6 * i + j];
+            }
+    }
+    /* T = 0 on the boundary: penalty constraints node[i].temperature on A */
+    double max_diag = max(abs(A.diag()));
+    for (unsigned i = 0; i < nn; ++i) {
+        const double x = pos[2 * i], y = pos[2 * i + 1];
+        if (x < 1e-9 || y < 1e-9 || x > 1 - 1e-9 || y > 1 - 1e-9) A(i, i) += max_diag * penalty;
+    }
+    std::vector<double> T0(nn), T1(nn);
+    for (unsigned i = 0; i < nn; ++i) {
+        const double dx = pos[2 * i] - 0.5, dy = pos[2 * i + 1] - 0.5;
+        T0[i] = exp(-(dx * dx + dy * dy) / (2 * 0.1 * 0.1));
+    }
+    Vec<double> t0, rhs;
+    t0.resize(nn);
+    for (unsigned i = 0; i < nn; ++i) t0[i] = T0[i];
+    rhs = B * t0;
+    Mat<double, Sym<>, SparseLine<> > Ac = A;
+    LDL_solver ldl;
+    ldl.get_factorization(Ac, false);
+    ldl.solve(rhs);
+    for (unsigned i = 0; i < nn; ++i) T1[i] = rhs[i];
+    std::vector<unsigned long long> rowptr(nn + 1, 0), rowptrB(nn + 1, 0);
+    std::vector<unsigned> col, colB;
+    std::vector<double> val, valB;
+    for (unsigned i = 0; i < nn; ++i) {
+        for (unsigned q = 0; q < A.data[i].indices.size(); ++q) {
+            col.push_back(A.data[i].indices[q]);
+            val.push_back(A.data[i].data[q]);
+        }
+        rowptr[i + 1] = col.size();
+        for (unsigned q = 0; q < B.data[i].indices.size(); ++q) {
+            colB.push_back(B.data[i].indices[q]);
+            valB.push_back(B.data[i].data[q]);
+        }
+        rowptrB[i + 1] = colB.size();
+    }
+    dump(out + "/pos.f64", pos);
+    dump(out + "/conn.u32", conn);
+    dump(out + "/rowptr.u64", rowptr);
+    dump(out + "/col.u32", col);
+    dump(out + "/val.f64", val);
+    dump(out + "/rowptrB.u64", rowptrB);
+    dump(out + "/colB.u32", colB);
+    dump(out + "/valB.f64", valB);
+    dump(out + "/T0.f64", T0);
+    dump(out + "/T1.f64", T1);
+    FILE *f = fopen((out + "/info.txt").c_str(), "w");
+    fprintf(f, "nn %u\nne %u\nnnz %zu\nmax_diag %.17g\n", nn, ne, col.size(), max_diag);
+    fclose(f);
+    return 0;
+}
+
 int main(int argc, char **argv) {
+    if (argc >= 2 && std::string(argv[1]) == "tri6") return run_tri6(argc, argv);
     if (argc != 7 || (std::string(argv[1]) != "hexa" && std::string(argv[1]) != "tetra10")) {
         fprintf(stderr, "usage: ref_driver hexa|tetra10 <nb_points> <E> <nu> <penalty> <outdir>\n");
         return 1;

@@ -6,6 +6,10 @@ penalty constraints, LDL and IC(0)-PCG, built by oracle/build_ref.sh from the LM
 workload of the reference's example -- unit cube of Hexa8 or Tetra_10, penalty clamp
 of x = 0, uniform traction (1,0,0) on x = 1 -- and stores its outputs as compressed npz.
 
+For heat diffusion (formulation difftherm) on Triangle_6 it records the mesh, the Crank-Nicolson
+matrices A = M/dt + K/2 (with the boundary penalty) and B = M/dt - K/2 in the reference's storage,
+and one step A T1 = B T0 solved by the reference's LDL.
+
 Also records the known-answer vectors of the reference's solver unit tests
 (tests/include/containers/conjugate_gradient_test.cpp:15-71) as JSON.
 
@@ -49,6 +53,24 @@ def run_case(name, elem, nbp, E, nu, pen):
                                           nnz=int(info["nnz"])))))
 
 
+def run_tri6(name, nbp, k, rho_c, dt, theta, pen):
+    """Heat diffusion on Triangle_6: mesh, A and B (lower CSR, penalty on A) and one LDL step."""
+    drv = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
+    with tempfile.TemporaryDirectory() as d:
+        subprocess.check_call([drv, "tri6", str(nbp), repr(k), repr(rho_c), repr(dt), repr(theta),
+                               repr(pen), d])
+        r = lambda f, t: np.fromfile(os.path.join(d, f), dtype=t)
+        info = dict(l.split() for l in open(os.path.join(d, "info.txt")))
+        np.savez_compressed(
+            os.path.join(HERE, name + ".npz"),
+            pos=r("pos.f64", np.float64).reshape(-1, 2), conn=r("conn.u32", np.uint32).reshape(-1, 6),
+            rowptr=r("rowptr.u64", np.uint64), col=r("col.u32", np.uint32), A=r("val.f64", np.float64),
+            rowptrB=r("rowptrB.u64", np.uint64), colB=r("colB.u32", np.uint32), B=r("valB.f64", np.float64),
+            T0=r("T0.f64", np.float64), T1=r("T1.f64", np.float64),
+            meta=np.array(json.dumps(dict(nb_points=nbp, k=k, rho_c=rho_c, dt=dt, theta=theta, penalty=pen,
+                                          max_diag=float(info["max_diag"])))))
+
+
 def cg_known_answers():
     # conjugate_gradient_0: 3x3 Sym matrix, b = (3,4,5), x = (11,2,4)
     # conjugate_gradient_1: 10x10 Sym matrix, b given, solution from Maple (s_Maple)
@@ -81,6 +103,8 @@ if __name__ == "__main__":
     for c in CASES:
         run_case(*c)
         print("wrote", c[0])
+    run_tri6("tri6_8x8_cn", 9, 1.0, 1.0, 1e-3, 0.5, 1e5)
+    print("wrote tri6_8x8_cn")
     with open(os.path.join(HERE, "cg_known_answers.json"), "w") as f:
         json.dump(cg_known_answers(), f, indent=1)
     print("wrote cg_known_answers.json")

@@ -84,3 +84,12 @@ def test_make_rect_tetra10_matches_oracle(nbp):
     pos_o, conn_o = O.make_rect_tetra10(nbp)
     assert np.array_equal(pos, pos_o)
     assert np.array_equal(conn, conn_o)
+
+
+@pytest.mark.parametrize("nbp", [(2, 2), (9, 9), (5, 7)])
+def test_make_rect_triangle6_matches_oracle(nbp):
+    from lmtpp_gb300.diffusion import make_rect_triangle6
+    pos, conn = make_rect_triangle6(nbp)
+    pos_o, conn_o = O.make_rect_triangle6(nbp)
+    assert np.array_equal(pos, pos_o)
+    assert np.array_equal(conn, conn_o)

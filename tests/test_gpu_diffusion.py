@@ -1,0 +1,90 @@
+"""Transient heat diffusion (Triangle_6, theta scheme) on the GPU against the oracle and the
+reference's fixture; the adjoint gradient against central differences and checkpoint-free runs."""
+import json
+import os
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from lmtpp_gb300.diffusion import Diffusion, boundary_nodes, make_rect_triangle6
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def csr(rowptr, col, val, n):
+    return sp.csr_matrix((val, col.astype(np.int64), rowptr.astype(np.int64)), shape=(n, n))
+
+
+def test_diffusion_matrices_and_step_match_reference(golden_dir):
+    g = np.load(os.path.join(golden_dir, "tri6_8x8_cn.npz"))
+    m = json.loads(str(g["meta"]))
+    pos, conn = make_rect_triangle6(m["nb_points"])
+    assert np.array_equal(pos, g["pos"]) and np.array_equal(conn, g["conn"])
+    d = Diffusion(pos, conn)
+    d.setup(m["k"], rho_c=m["rho_c"], dt=m["dt"], theta=m["theta"], dirichlet=boundary_nodes(pos),
+            penalty=m["penalty"])
+    rowptr, col, A, B = d.get_matrices()
+    n = pos.shape[0]
+    Ar = csr(g["rowptr"], g["col"], g["A"], n)
+    Br = csr(g["rowptrB"], g["colB"], g["B"], n)
+    Ag, Bg = csr(rowptr, col, A, n), csr(rowptr, col, B, n)
+    assert abs(Ar - Ag).max() <= 1e-12 * abs(Ar).max()
+    assert abs(Br - Bg).max() <= 1e-12 * abs(Br).max()
+    assert d.get_penalty_scale() == pytest.approx(m["max_diag"], rel=1e-12)
+    d.set_state(g["T0"])
+    d.run(1, tol=1e-14)
+    T1 = d.get_state()
+    assert np.linalg.norm(T1 - g["T1"]) <= 1e-10 * np.linalg.norm(g["T1"])
+    d.close()
+
+
+@pytest.mark.parametrize("theta", [0.5, 1.0])
+def test_diffusion_multistep_matches_oracle(theta):
+    rng = np.random.default_rng(4)
+    P0 = O.diffusion_problem(17, theta=theta)
+    k = np.exp(0.3 * rng.standard_normal(P0["conn"].shape[0]))
+    P = O.diffusion_problem(17, k=k, theta=theta)
+    states = O.diffusion_run(P, 10)
+    d = Diffusion(P["pos"], P["conn"])
+    d.setup(k, rho_c=1.0, dt=1e-4, theta=theta, dirichlet=boundary_nodes(P["pos"]), penalty=1e5)
+    d.set_state(P["T0"])
+    st = d.run(10, tol=1e-14)
+    T = d.get_state()
+    assert np.linalg.norm(T - states[-1]) <= 1e-10 * np.linalg.norm(states[-1]), st
+    d.close()
+
+
+def test_diffusion_adjoint_checkpoints_and_central_differences():
+    rng = np.random.default_rng(9)
+    pos, conn = make_rect_triangle6(9)
+    ne = conn.shape[0]
+    k = np.exp(0.3 * rng.standard_normal(ne))
+    T0 = O.gaussian_bump(pos)
+    target = rng.standard_normal(pos.shape[0]) * 0.05
+    d = Diffusion(pos, conn)
+    bnd = boundary_nodes(pos)
+    d.setup(k, rho_c=1.0, dt=1e-3, theta=1.0, dirichlet=bnd, penalty=1e5)
+    d.set_penalty_scale(d.get_penalty_scale())  # held fixed, as the gradient assumes
+    nsteps = 12
+    J, g = d.adjoint_misfit(T0, target, nsteps, checkpoint_every=5, tol=1e-14)
+    J1, g1 = d.adjoint_misfit(T0, target, nsteps, checkpoint_every=1, tol=1e-14)
+    assert J == pytest.approx(J1, rel=1e-13)
+    assert np.linalg.norm(g - g1) <= 1e-10 * np.linalg.norm(g1)
+
+    def Jof(kk):
+        d.setup(kk, rho_c=1.0, dt=1e-3, theta=1.0, dirichlet=bnd, penalty=1e5)
+        d.set_state(T0)
+        d.run(nsteps, tol=1e-15)
+        r = d.get_state() - target
+        return 0.5 * r @ r
+
+    for e in rng.choice(ne, 5, replace=False):
+        h = 1e-4 * k[e]
+        kp, km = k.copy(), k.copy()
+        kp[e] += h
+        km[e] -= h
+        fd = (Jof(kp) - Jof(km)) / (2 * h)
+        assert fd == pytest.approx(g[e], rel=1e-5, abs=1e-9 * np.abs(g).max()), (e, fd, g[e])
+    d.close()

@@ -123,3 +123,23 @@ def test_oracle_adjoint_solve_matches_reference_ldl(golden_dir):
     P = O.elasticity_problem(m["nb_points"], E=m["E"], nu=m["nu"], pen=m["penalty"])
     lam = O.skyline_solve(P["rowptr"], P["col"], P["val"], g["u_ldl"])
     assert np.linalg.norm(lam - g["lam_ldl"]) <= 1e-12 * np.linalg.norm(g["lam_ldl"])
+
+
+def test_oracle_diffusion_matches_reference_runtime(golden_dir):
+    """Triangle_6 heat diffusion: mesh, Crank-Nicolson matrices (penalty on A) and one LDL step."""
+    g = np.load(os.path.join(golden_dir, "tri6_8x8_cn.npz"))
+    m = json.loads(str(g["meta"]))
+    P = O.diffusion_problem(m["nb_points"], k=m["k"], rho_c=m["rho_c"], dt=m["dt"], theta=m["theta"],
+                            pen=m["penalty"])
+    assert np.array_equal(P["pos"], g["pos"]) and np.array_equal(P["conn"], g["conn"])
+    n = P["pos"].shape[0]
+    A = csr(g["rowptr"], g["col"], g["A"], n)
+    B = csr(g["rowptrB"], g["colB"], g["B"], n)
+    Ao = csr(P["rowptr"], P["col"], P["A"], n)
+    Bo = csr(P["rowptr"], P["col"], P["B"], n)
+    assert abs(A - Ao).max() <= 1e-12 * abs(Ao).max()
+    assert abs(B - Bo).max() <= 1e-12 * abs(Bo).max()
+    assert P["max_diag"] == pytest.approx(m["max_diag"], rel=1e-14)
+    np.testing.assert_allclose(P["T0"], g["T0"], rtol=1e-15, atol=0)  # exp() of two libms
+    T1 = O.diffusion_run(P, 1)[1]
+    assert np.linalg.norm(T1 - g["T1"]) <= 1e-12 * np.linalg.norm(g["T1"])
