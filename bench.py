@@ -49,7 +49,9 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--fd", type=int, default=32, help="elements checked by central differences (adjoint mode)")
-    p.add_argument("--mode", default="bench", choices=["bench", "profile", "solve", "adjoint"],
+    p.add_argument("--steps-t", type=int, default=100, help="time steps (transient mode)")
+    p.add_argument("--ckpt", type=int, default=10, help="checkpoint interval (transient mode)")
+    p.add_argument("--mode", default="bench", choices=["bench", "profile", "solve", "adjoint", "transient"],
                    help="profile: time the PCG kernels once on --side (small ncu case); "
                         "solve: one assemble + mixed solve at --tol (launch-list case)")
     p.add_argument("--tol", type=float, default=1e-10)
@@ -426,8 +428,53 @@ def run_adjoint(args):
     print(json.dumps(out), flush=True)
 
 
+def run_transient(args):
+    """Transient heat diffusion: unit square of 2 x N^2 Triangle_6 (default N = 1024: 2,097,152
+    elements, 4,198,401 nodes), conductivity lognormal (log-std 0.3, default_rng(seed)), rho_c = 1,
+    implicit Euler (theta = 1), dt = 1e-4, 100 steps, T = 0 on the boundary (penalty), Gaussian-bump
+    initial field (centre (0.5, 0.5), sigma 0.1); then the final-time misfit to a seeded target and
+    its adjoint gradient w.r.t. the 2.1 M conductivities with checkpoints every --ckpt steps."""
+    import torch
+    from lmtpp_gb300.diffusion import Diffusion, boundary_nodes, make_rect_triangle6
+    N = args.side
+    pos, conn = make_rect_triangle6(N + 1)
+    rng = np.random.default_rng(SEED)
+    k = np.exp(0.3 * rng.standard_normal(conn.shape[0]))
+    d2 = (pos[:, 0] - 0.5) ** 2 + (pos[:, 1] - 0.5) ** 2
+    T0 = np.exp(-d2 / (2 * 0.1 * 0.1))
+    target = T0 * (1.0 + 0.1 * rng.standard_normal(pos.shape[0]))
+    d = Diffusion(pos, conn)
+    bnd = boundary_nodes(pos)
+    t0 = time.perf_counter()
+    d.setup(k, rho_c=1.0, dt=1e-4, theta=1.0, dirichlet=bnd, penalty=1e5)
+    d.set_penalty_scale(d.get_penalty_scale())
+    setup_s = time.perf_counter() - t0
+    d.set_state(T0)
+    d.run(2, tol=1e-10)  # warm-up (graph capture, caches)
+    d.set_state(T0)
+    torch.cuda.synchronize()
+    st_f = d.run(args.steps_t, tol=1e-10)
+    J, g = d.adjoint_misfit(T0, target, args.steps_t, checkpoint_every=args.ckpt, tol=1e-10)
+    st_a = d.last_stats
+    d.close()
+    out = {"mode": "transient",
+           "workload": "Triangle_6 heat diffusion 2 x %d^2 (%d elements, %d nodes), lognormal "
+                       "conductivity (log-std 0.3, seed %d), implicit Euler, dt 1e-4, %d steps, "
+                       "T=0 on the boundary (penalty), Gaussian-bump T0" % (N, conn.shape[0], pos.shape[0],
+                                                                          SEED, args.steps_t),
+           "setup_s": setup_s, "forward_ms": st_f["device_ms"], "forward_pcg_iters": st_f["iterations"],
+           "adjoint_ms": st_a["device_ms"], "adjoint_pcg_iters_incl_recompute": st_a["iterations"],
+           "adjoint_ratio_vs_forward": st_a["device_ms"] / st_f["device_ms"],
+           "checkpoint_every": args.ckpt, "J": J, "grad_norm": float(np.linalg.norm(g))}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
+    if args.mode == "transient":
+        if args.side == 128:
+            args.side = 1024
+        return run_transient(args)
     if args.cpu_side == 0:
         args.cpu_side = 24 if args.elem == "hexa8" else 8
     if args.mode == "adjoint":
