@@ -449,23 +449,45 @@ def run_transient(args):
     d.setup(k, rho_c=1.0, dt=1e-4, theta=1.0, dirichlet=bnd, penalty=1e5)
     d.set_penalty_scale(d.get_penalty_scale())
     setup_s = time.perf_counter() - t0
-    d.set_state(T0)
-    d.run(2, tol=1e-10)  # warm-up (graph capture, caches)
-    d.set_state(T0)
-    torch.cuda.synchronize()
-    st_f = d.run(args.steps_t, tol=1e-10)
-    J, g = d.adjoint_misfit(T0, target, args.steps_t, checkpoint_every=args.ckpt, tol=1e-10)
-    st_a = d.last_stats
-    d.close()
     out = {"mode": "transient",
            "workload": "Triangle_6 heat diffusion 2 x %d^2 (%d elements, %d nodes), lognormal "
                        "conductivity (log-std 0.3, seed %d), implicit Euler, dt 1e-4, %d steps, "
                        "T=0 on the boundary (penalty), Gaussian-bump T0" % (N, conn.shape[0], pos.shape[0],
                                                                           SEED, args.steps_t),
-           "setup_s": setup_s, "forward_ms": st_f["device_ms"], "forward_pcg_iters": st_f["iterations"],
-           "adjoint_ms": st_a["device_ms"], "adjoint_pcg_iters_incl_recompute": st_a["iterations"],
-           "adjoint_ratio_vs_forward": st_a["device_ms"] / st_f["device_ms"],
-           "checkpoint_every": args.ckpt, "J": J, "grad_norm": float(np.linalg.norm(g))}
+           "setup_s": setup_s}
+    finals = {}
+    for solver in ("fp64", "mixed"):
+        d.set_solver(solver)
+        d.set_state(T0)
+        d.run(2, tol=1e-10)  # warm-up (graph capture, caches)
+        d.set_state(T0)
+        torch.cuda.synchronize()
+        st_f = d.run(args.steps_t, tol=1e-10)
+        finals[solver] = d.get_state()
+        out["forward_ms_" + solver] = st_f["device_ms"]
+        out["forward_pcg_iters_" + solver] = st_f["iterations"]
+    out["forward_speedup_mixed"] = out["forward_ms_fp64"] / out["forward_ms_mixed"]
+    out["final_state_rel_diff_mixed_vs_fp64"] = float(np.linalg.norm(finals["mixed"] - finals["fp64"]) /
+                                                       np.linalg.norm(finals["fp64"]))
+    # the adjoint call runs its own forward sweep; backward = call - that forward
+    grads = {}
+    for ck in sorted({1, args.ckpt}):
+        J, g = d.adjoint_misfit(T0, target, args.steps_t, checkpoint_every=ck, tol=1e-10)
+        st_a = d.last_stats
+        grads[ck] = g
+        key = "adjoint_ck%d_" % ck
+        out[key + "ms"] = st_a["device_ms"]
+        out[key + "pcg_iters"] = st_a["iterations"]
+        out[key + "backward_ratio_vs_forward"] = (st_a["device_ms"] - out["forward_ms_mixed"]) / \
+            out["forward_ms_mixed"]
+        out["J"] = J
+        out["grad_norm"] = float(np.linalg.norm(g))
+    if len(grads) == 2:
+        out["grad_rel_diff_ck1_vs_ck%d" % args.ckpt] = float(np.linalg.norm(grads[1] - grads[args.ckpt]) /
+                                                             np.linalg.norm(grads[1]))
+    out["adjoint_solver"] = "mixed"
+    out["checkpoint_bytes_ck1"] = (args.steps_t + 1) * pos.shape[0] * 8
+    d.close()
     print(json.dumps(out), flush=True)
 
 

@@ -222,16 +222,20 @@ int lmtg_diff_mesh_set(lmtg_ctx *ctx, uint64_t nn, const double *pos, uint64_t n
  * Builds the pattern (first call), the element matrices and A, B. */
 int lmtg_diff_setup(lmtg_ctx *ctx, const double *k, uint64_t nk, double rho_c, double dt,
                     double theta, uint64_t nbnd, const uint32_t *bnd_nodes, double penalty);
+/* Linear solver of every time step (and of the adjoint): LMTG_SOLVE_PCG_F64 (default, FP64
+ * Jacobi-PCG) or LMTG_SOLVE_MIXED_IR (FP32 Jacobi-PCG with FP64 residual replacement). */
+int lmtg_diff_set_solver(lmtg_ctx *ctx, int mode);
 /* Temperature state (nn doubles). */
 int lmtg_diff_set_state(lmtg_ctx *ctx, const double *T);
 int lmtg_diff_get_state(lmtg_ctx *ctx, double *T);
-/* nsteps time steps from the current state, each solved by FP64 Jacobi-PCG to the relative
- * residual tol (warm start from the previous state). */
+/* nsteps time steps from the current state, each solved to the relative
+ * residual tol (warm start from the previous state) with the solver of lmtg_diff_set_solver. */
 int lmtg_diff_run(lmtg_ctx *ctx, int nsteps, double tol, int maxit, lmtg_solve_stats *stats);
 /* Final-time misfit J = 1/2 |T_N - target|^2 of nsteps steps from the current state and its
  * adjoint gradient w.r.t. every element's conductivity (ne doubles into dJdk), with forward
  * states checkpointed every `checkpoint_every` steps and recomputed per segment in the backward
- * sweep (no reference counterpart).  The penalty scale is held constant.  Leaves T_N as state. */
+ * sweep; checkpoint_every = 1 keeps all nsteps + 1 states and recomputes none (no reference
+ * counterpart).  The penalty scale is held constant.  Leaves T_N as state. */
 int lmtg_diff_adjoint_misfit(lmtg_ctx *ctx, int nsteps, int checkpoint_every, const double *target,
                              double tol, int maxit, double *J, double *dJdk,
                              lmtg_solve_stats *stats);

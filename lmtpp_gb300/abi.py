@@ -62,6 +62,7 @@ _SIGS = {
     "lmtg_make_rect_triangle6": (_i, [_vp, _vp, _vp, ctypes.POINTER(_u64), ctypes.POINTER(_u64), _vp, _vp]),
     "lmtg_diff_mesh_set": (_i, [_vp, _u64, _vp, _u64, _vp]),
     "lmtg_diff_setup": (_i, [_vp, _vp, _u64, _d, _d, _d, _u64, _vp, _d]),
+    "lmtg_diff_set_solver": (_i, [_vp, _i]),
     "lmtg_diff_set_state": (_i, [_vp, _vp]),
     "lmtg_diff_get_state": (_i, [_vp, _vp]),
     "lmtg_diff_run": (_i, [_vp, _i, _d, _i, ctypes.POINTER(SolveStats)]),

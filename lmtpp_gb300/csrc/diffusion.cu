@@ -162,15 +162,67 @@ __global__ void k_jacobi_s(const uint32_t *__restrict__ bdiag, const double *__r
     }
 }
 
-// ---- scalar CSR kernels: 8 lanes per row, 4 rows per warp --------------------------------
+// ---- scalar CSR kernels: one warp per 32 consecutive rows, entries streamed --------------
+// The warp walks the contiguous entry range of its 32 rows in tiles of kTile entries: lane l
+// takes entries t0 + 32k + l (coalesced K / col loads, every lane busy whatever the row
+// lengths), all loads of a tile issued before the products are formed; the products go to a
+// per-warp shared tile and each lane then sums the part of its own row inside the tile, in
+// column order.  Rows average ~11.5 entries here, so 8-lanes-per-row kept too few loads in
+// flight and left the kernel latency-bound.
+constexpr int kTileChunks = 8;
+constexpr int kTile = 32 * kTileChunks;
+constexpr int kRowWarps = kRowThreads / 32;
+
+// 32-row chunks of this CTA: a contiguous range, its warps interleaved over it
+struct ChunkRange {
+    uint64_t first, end;
+};
+__device__ __forceinline__ ChunkRange cta_chunks(uint64_t n) {
+    const uint64_t nch = (n + 31) / 32;
+    const uint64_t per = (nch + gridDim.x - 1) / gridDim.x;
+    const uint64_t b = (uint64_t)blockIdx.x * per;
+    return {b < nch ? b : nch, b + per < nch ? b + per : nch};
+}
+
+// Row sums of K x~ for rows r0 .. r0+31 (x~_j = xf(j)); returns lane l's row sum (0 past n).
 template <class T, class XF>
-__device__ __forceinline__ T csr_row8(const uint32_t *__restrict__ col, const T *__restrict__ K,
-                                      uint32_t rb, uint32_t re, int sub, XF xf) {
+__device__ __forceinline__ T csr_stream32(const uint32_t *__restrict__ rp, const uint32_t *__restrict__ col,
+                                          const T *__restrict__ K, uint64_t r0, uint64_t n, T *tile,
+                                          XF xf) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t I = r0 + lane;
+    const uint32_t rs = __ldg(rp + (I < n ? I : n));
+    uint32_t re = __shfl_down_sync(0xffffffffu, rs, 1);
+    if (lane == 31) re = __ldg(rp + (r0 + 32 < n ? r0 + 32 : n));
+    const uint32_t e0 = __shfl_sync(0xffffffffu, rs, 0);
+    const uint32_t e1 = __shfl_sync(0xffffffffu, re, 31);
     T acc = (T)0;
-    for (uint32_t q = rb + sub; q < re; q += 8) acc = fma(__ldg(K + q), xf(__ldg(col + q)), acc);
-    acc += __shfl_xor_sync(0xffffffffu, acc, 4);
-    acc += __shfl_xor_sync(0xffffffffu, acc, 2);
-    acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+    for (uint32_t t0 = e0; t0 < e1; t0 += kTile) {
+        const uint32_t nck = (e1 - t0 + 31) / 32;  // live chunks of this tile (warp-uniform)
+        uint32_t cj[kTileChunks];
+        T kv[kTileChunks];
+#pragma unroll
+        for (int k = 0; k < kTileChunks; ++k) {
+            if (k < nck) {
+                const uint32_t q = t0 + 32 * k + lane;
+                const bool on = q < e1;
+                cj[k] = on ? __ldg(col + q) : 0u;
+                kv[k] = on ? __ldg(K + q) : (T)0;
+            }
+        }
+        T xv[kTileChunks];
+#pragma unroll
+        for (int k = 0; k < kTileChunks; ++k)
+            if (k < nck) xv[k] = t0 + 32 * k + lane < e1 ? xf(cj[k]) : (T)0;
+#pragma unroll
+        for (int k = 0; k < kTileChunks; ++k)
+            if (k < nck) tile[32 * k + lane] = kv[k] * xv[k];
+        __syncwarp();
+        const uint32_t lo = rs > t0 ? rs : t0;
+        const uint32_t hi = re < t0 + kTile ? re : t0 + kTile;
+        for (uint32_t q = lo; q < hi; ++q) acc += tile[q - t0];
+        __syncwarp();
+    }
     return acc;
 }
 
@@ -178,15 +230,13 @@ template <class T>
 __global__ void __launch_bounds__(kRowThreads)
     k_spmv_s(const uint32_t *__restrict__ rp, const uint32_t *__restrict__ col,
              const T *__restrict__ K, const T *__restrict__ x, T *__restrict__ y, uint64_t n) {
-    const int lane = threadIdx.x & 31, sub = lane & 7;
-    const uint64_t nq = ((uint64_t)gridDim.x * blockDim.x) >> 3;
-    for (uint64_t base = ((blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5) * 4;
-         base < n; base += nq) {
-        const uint64_t I = base + (lane >> 3);
-        const bool on = I < n;
-        const T v = csr_row8(col, K, on ? rp[I] : 0u, on ? rp[I + 1] : 0u, sub,
-                             [&](uint32_t j) { return __ldg(x + j); });
-        if (on && sub == 0) y[I] = v;
+    __shared__ T tiles[kRowWarps][kTile];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const ChunkRange cr = cta_chunks(n);
+    for (uint64_t ch = cr.first + w; ch < cr.end; ch += kRowWarps) {
+        const T v = csr_stream32(rp, col, K, ch * 32, n, tiles[w], [&](uint32_t j) { return __ldg(x + j); });
+        const uint64_t I = ch * 32 + lane;
+        if (I < n) y[I] = v;
     }
 }
 
@@ -195,16 +245,14 @@ __global__ void __launch_bounds__(kRowThreads)
     k_residual_s(const uint32_t *__restrict__ rp, const uint32_t *__restrict__ col,
                  const T *__restrict__ K, const T *__restrict__ x, const T *__restrict__ b,
                  T *__restrict__ r, uint64_t n, double *partials, unsigned *ticket, double *rr_out) {
-    const int lane = threadIdx.x & 31, sub = lane & 7;
-    const uint64_t nq = ((uint64_t)gridDim.x * blockDim.x) >> 3;
+    __shared__ T tiles[kRowWarps][kTile];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const ChunkRange cr = cta_chunks(n);
     T acc = (T)0;
-    for (uint64_t base = ((blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5) * 4;
-         base < n; base += nq) {
-        const uint64_t I = base + (lane >> 3);
-        const bool on = I < n;
-        const T v = csr_row8(col, K, on ? rp[I] : 0u, on ? rp[I + 1] : 0u, sub,
-                             [&](uint32_t j) { return __ldg(x + j); });
-        if (on && sub == 0) {
+    for (uint64_t ch = cr.first + w; ch < cr.end; ch += kRowWarps) {
+        const T v = csr_stream32(rp, col, K, ch * 32, n, tiles[w], [&](uint32_t j) { return __ldg(x + j); });
+        const uint64_t I = ch * 32 + lane;
+        if (I < n) {
             const T ri = b[I] - v;
             r[I] = ri;
             acc = fma(ri, ri, acc);
@@ -244,28 +292,34 @@ __global__ void k_pcg_start_s(const T *__restrict__ r, const T *__restrict__ b,
     }
 }
 
+// p = z + beta p (beta = 0 on a fresh start): its own pass, so that the SpMV gathers one vector
+// and the FP64 pipe forms no z + beta p per matrix entry
+template <class T>
+__global__ void k_pcg_dir_s(const T *__restrict__ z, T *__restrict__ p, uint64_t n, const PcgScalars *S) {
+    if (*(volatile const int *)&S->done) return;
+    const T beta = (T)S->beta;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        p[i] = beta != (T)0 ? fma(beta, p[i], z[i]) : z[i];
+}
+
+// q = K p and p.q
 template <class T>
 __global__ void __launch_bounds__(kRowThreads)
     k_pcg_spmv_s(const uint32_t *__restrict__ rp, const uint32_t *__restrict__ col,
-                 const T *__restrict__ K, const T *__restrict__ z, const T *__restrict__ pold,
-                 T *__restrict__ pnew, T *__restrict__ q, uint64_t n, PcgScalars *S,
-                 double *partials) {
+                 const T *__restrict__ K, const T *__restrict__ p, T *__restrict__ q, uint64_t n,
+                 PcgScalars *S, double *partials) {
     if (*(volatile int *)&S->done) return;
-    const T beta = (T)S->beta;
-    const int lane = threadIdx.x & 31, sub = lane & 7;
-    const uint64_t nq = ((uint64_t)gridDim.x * blockDim.x) >> 3;
+    __shared__ T tiles[kRowWarps][kTile];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const ChunkRange cr = cta_chunks(n);
     T acc = (T)0;
-    for (uint64_t base = ((blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5) * 4;
-         base < n; base += nq) {
-        const uint64_t I = base + (lane >> 3);
-        const bool on = I < n;
-        const T qi = csr_row8(col, K, on ? rp[I] : 0u, on ? rp[I + 1] : 0u, sub,
-                              [&](uint32_t j) { return fma(beta, __ldg(pold + j), __ldg(z + j)); });
-        if (on && sub == 0) {
-            const T pn = fma(beta, pold[I], z[I]);
-            pnew[I] = pn;
+    for (uint64_t ch = cr.first + w; ch < cr.end; ch += kRowWarps) {
+        const T qi = csr_stream32(rp, col, K, ch * 32, n, tiles[w], [&](uint32_t j) { return __ldg(p + j); });
+        const uint64_t I = ch * 32 + lane;
+        if (I < n) {
             q[I] = qi;
-            acc = fma(pn, qi, acc);
+            acc = fma(p[I], qi, acc);
         }
     }
     const T t[1] = {acc};
@@ -355,39 +409,72 @@ __global__ void k_axpby(const double *__restrict__ a, const double *__restrict__
 }
 
 // ---- host -----------------------------------------------------------------------------------
-static int rgrid(lmtg_ctx *c) { return grid_for(c, c->nn * 8, kRowThreads, 8); }
+// row kernels: one resident wave (each CTA owns a contiguous range of 32-row chunks)
+template <class KF>
+static int rgrid(lmtg_ctx *c, KF kernel) {
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, kRowThreads, 0) != cudaSuccess || nb < 1)
+        nb = 1;
+    return grid_for(c, c->nn, kRowThreads, nb);
+}
 static int ngrid(lmtg_ctx *c) { return grid_for(c, c->nn, kRowThreads, 8); }
 
-// PCG on A x = b (FP64, Jacobi), warm start from x.  Returns the status.
-static int diff_pcg(lmtg_ctx *c, const double *b, double *x, double tol, int maxit, int *iters) {
+__global__ void k_dot_s(const double *__restrict__ a, const double *__restrict__ b, uint64_t n,
+                        double *partials, unsigned *ticket, double *out_p) {
+    double v[1] = {0.0};
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        v[0] = fma(a[i], b[i], v[0]);
+    double out[1];
+    if (grid_reduce<1, 0u>(v, partials, ticket, out) && threadIdx.x == 0) *out_p = out[0];
+}
+
+// PCG (Jacobi) on K x = b in precision T, from the current x (x_zero: x is 0, r = b).  b_norm2 >= 0
+// gives |b|^2 for the relative test; beta_den > 0 continues the search direction held in p
+// (reliable update).  Returns the status; *iters the iterations.
+template <class T>
+static int diff_pcg_t(lmtg_ctx *c, const T *K, const T *Dinv, const T *b, T *x, T *r, T *z, T *p, T *q,
+                      bool x_zero, double tol, int maxit, double b_norm2, double beta_den, int *iters) {
     cudaStream_t s = c->stream;
-    double *r = c->w64[0].p, *z = c->w64[1].p, *p0 = c->w64[2].p, *p1 = c->w64[3].p, *q = c->w64[4].p;
     PcgScalars init{};
     init.crit = tol;
     init.crit_kind = LMTG_CRIT_REL_RESIDUAL;
     init.maxit = maxit;
+    init.bb = b_norm2 >= 0 ? b_norm2 : 0.0;
     LMTG_CUDA(cudaMemcpyAsync(c->scal.p, &init, sizeof(init), cudaMemcpyHostToDevice, s));
     PcgScalars *o = c->scal.p + 1;
-    k_residual_s<double><<<rgrid(c), kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, c->K64.p, x, b, r,
-                                                          c->nn, c->partials.p, &o->cnt_c, &o->rr);
-    k_pcg_start_s<double><<<ngrid(c), kRowThreads, 0, s>>>(r, b, c->Dinv64.p, z, c->nn, c->scal.p,
-                                                           c->partials.p);
-    LMTG_CUDA(cudaMemsetAsync(p0, 0, sizeof(double) * c->nn, s));
+    if (x_zero) {
+        LMTG_CUDA(cudaMemcpyAsync(r, b, sizeof(T) * c->nn, cudaMemcpyDeviceToDevice, s));
+    } else {
+        k_residual_s<T><<<rgrid(c, k_residual_s<T>), kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, K, x, b, r,
+                                                                          c->nn, c->partials.p, &o->cnt_c,
+                                                                          &o->rr);
+        c->launches += 1;
+    }
+    k_pcg_start_s<T><<<ngrid(c), kRowThreads, 0, s>>>(r, b_norm2 >= 0 ? nullptr : b, Dinv, z, c->nn,
+                                                      c->scal.p, c->partials.p);
+    c->launches += 1;
     LMTG_CUDA(cudaGetLastError());
-    c->launches += 2;
-    constexpr int kPairs = 8;
+    if (beta_den > 0.0) {
+        // continue the previous direction: beta = rz_new / beta_den (set after the start kernel)
+        PcgScalars h{};
+        LMTG_CUDA(cudaMemcpyAsync(&h, c->scal.p, sizeof(h), cudaMemcpyDeviceToHost, s));
+        LMTG_CUDA(cudaStreamSynchronize(s));
+        const double beta = h.rz / beta_den;
+        LMTG_CUDA(cudaMemcpyAsync(&c->scal.p->beta, &beta, sizeof(double), cudaMemcpyHostToDevice, s));
+        LMTG_CUDA(cudaStreamSynchronize(s));
+    }
+    constexpr int kIters = 16;  // iterations per graph launch
+    const int gr = rgrid(c, k_pcg_spmv_s<T>);
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     LMTG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    for (int k = 0; k < kPairs; ++k) {
-        k_pcg_spmv_s<double><<<rgrid(c), kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, c->K64.p, z, p0,
-                                                              p1, q, c->nn, c->scal.p, c->partials.p);
-        k_pcg_update_s<double><<<ngrid(c), kRowThreads, 0, s>>>(x, r, z, p1, q, c->Dinv64.p, c->nn,
-                                                                c->scal.p, c->partials.p);
-        k_pcg_spmv_s<double><<<rgrid(c), kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, c->K64.p, z, p1,
-                                                              p0, q, c->nn, c->scal.p, c->partials.p);
-        k_pcg_update_s<double><<<ngrid(c), kRowThreads, 0, s>>>(x, r, z, p0, q, c->Dinv64.p, c->nn,
-                                                                c->scal.p, c->partials.p);
+    for (int k = 0; k < kIters; ++k) {
+        k_pcg_dir_s<T><<<ngrid(c), kRowThreads, 0, s>>>(z, p, c->nn, c->scal.p);
+        k_pcg_spmv_s<T><<<gr, kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, K, p, q, c->nn, c->scal.p,
+                                                   c->partials.p);
+        k_pcg_update_s<T><<<ngrid(c), kRowThreads, 0, s>>>(x, r, z, p, q, Dinv, c->nn, c->scal.p,
+                                                           c->partials.p);
     }
     cudaError_t ce = cudaStreamEndCapture(s, &graph);
     if (ce != cudaSuccess) throw Error{LMTG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce)};
@@ -396,14 +483,13 @@ static int diff_pcg(lmtg_ctx *c, const double *b, double *x, double tol, int max
         cudaGraphDestroy(graph);
         throw Error{LMTG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce)};
     }
-    bool finished = false;
     LMTG_CUDA(cudaMemcpyAsync(c->h_scal, c->scal.p, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
     LMTG_CUDA(cudaStreamSynchronize(s));
-    finished = c->h_scal[0].done != 0;
-    const int max_chunks = maxit / (2 * kPairs) + 2;
+    bool finished = c->h_scal[0].done != 0;
+    const int max_chunks = maxit / kIters + 2;
     for (int ch = 0; ch < max_chunks && !finished; ++ch) {
         ce = cudaGraphLaunch(exec, s);
-        c->launches += 4 * kPairs;
+        c->launches += 3 * kIters;
         if (ce == cudaSuccess)
             ce = cudaMemcpyAsync(c->h_scal, c->scal.p, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s);
         if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
@@ -420,9 +506,77 @@ static int diff_pcg(lmtg_ctx *c, const double *b, double *x, double tol, int max
     return finished ? c->h_scal[0].status : LMTG_ERR_NOT_CONVERGED;
 }
 
+static int diff_pcg64(lmtg_ctx *c, const double *b, double *x, double tol, int maxit, int *iters) {
+    return diff_pcg_t<double>(c, c->K64.p, c->Dinv64.p, b, x, c->w64[0].p, c->w64[1].p, c->w64[2].p,
+                              c->w64[3].p, false, tol, maxit, -1.0, 0.0, iters);
+}
+
+// FP32-inner / FP64-refined solve of A x = b with reliable updates (the elasticity solver's
+// scheme on the scalar matrices): FP32 Jacobi-PCG segments on A32 d = r / s, each ending after a
+// 10x reduction of its recursive residual; x += s d and r = b - A x in FP64; the search
+// direction is kept across the residual replacement.
+static int diff_mixed(lmtg_ctx *c, const double *b, double *x, double tol, int maxit, int *iters) {
+    cudaStream_t st = c->stream;
+    double *r64 = c->w64[0].p;
+    float *b32 = c->w32[0].p, *d32 = c->w32[1].p, *r32 = c->w32[2].p, *z32 = c->w32[3].p,
+          *p32 = c->w32[4].p, *q32 = c->w32[5].p;
+    PcgScalars *o = c->scal.p + 1;
+    auto read_rr = [&]() {
+        double v = 0;
+        LMTG_CUDA(cudaMemcpyAsync(&v, &o->rr, 8, cudaMemcpyDeviceToHost, st));
+        LMTG_CUDA(cudaStreamSynchronize(st));
+        return v;
+    };
+    k_dot_s<<<ngrid(c), kRowThreads, 0, st>>>(b, b, c->nn, c->partials.p, &o->cnt_c, &o->rr);
+    c->launches += 1;
+    const double bb = read_rr();
+    constexpr double kDelta = 0.1;
+    int total = 0, status = LMTG_OK, outer = 0;
+    double s_prev = 0, rz_prev = 0, rel_prev = 0;
+    bool have_dir = false;
+    for (;;) {
+        k_residual_s<double><<<rgrid(c, k_residual_s<double>), kRowThreads, 0, st>>>(c->bptr.p, c->bcol.p, c->K64.p, x, b, r64,
+                                                               c->nn, c->partials.p, &o->cnt_c, &o->rr);
+        c->launches += 1;
+        const double rr = read_rr();
+        const double rel = bb > 0 ? std::sqrt(rr / bb) : std::sqrt(rr);
+        if (!std::isfinite(rel)) { status = LMTG_ERR_NAN; break; }
+        if (rel <= tol || rr == 0.0) break;
+        if (total >= maxit || outer >= 400) { status = LMTG_ERR_NOT_CONVERGED; break; }
+        if (have_dir && rel > 0.5 * rel_prev) have_dir = false;
+        const double sc = std::sqrt(rr);
+        k_scale_to32<<<ngrid(c), kRowThreads, 0, st>>>(r64, 1.0 / sc, b32, c->nn);
+        LMTG_CUDA(cudaMemsetAsync(d32, 0, sizeof(float) * c->nn, st));
+        c->launches += 1;
+        const double beta_den = have_dir ? rz_prev * (s_prev / sc) : 0.0;
+        double eta = 0.5 * tol / rel;
+        if (eta < kDelta) eta = kDelta;
+        int it = 0;
+        const int s2 = diff_pcg_t<float>(c, c->K32.p, c->Dinv32.p, b32, d32, r32, z32, p32, q32, true,
+                                         eta, maxit - total, 1.0, beta_den, &it);
+        total += it;
+        ++outer;
+        if (s2 == LMTG_ERR_NAN) { status = s2; break; }
+        rz_prev = c->h_scal[0].beta != 0.0 ? c->h_scal[0].rz / c->h_scal[0].beta : 0.0;
+        s_prev = sc;
+        rel_prev = rel;
+        have_dir = it > 0 && rz_prev > 0.0;
+        k_axpy_64_32<<<ngrid(c), kRowThreads, 0, st>>>(x, sc, d32, c->nn);
+        LMTG_CUDA(cudaGetLastError());
+        c->launches += 1;
+    }
+    *iters = total;
+    return status;
+}
+
+static int diff_pcg(lmtg_ctx *c, const double *b, double *x, double tol, int maxit, int *iters) {
+    return c->diff_mode == LMTG_SOLVE_MIXED_IR ? diff_mixed(c, b, x, tol, maxit, iters)
+                                               : diff_pcg64(c, b, x, tol, maxit, iters);
+}
+
 // rhs = B T (FP64)
 static void diff_rhs(lmtg_ctx *c, const double *T, double *rhs) {
-    k_spmv_s<double><<<rgrid(c), kRowThreads, 0, c->stream>>>(c->bptr.p, c->bcol.p, c->B64.p, T, rhs,
+    k_spmv_s<double><<<rgrid(c, k_spmv_s<double>), kRowThreads, 0, c->stream>>>(c->bptr.p, c->bcol.p, c->B64.p, T, rhs,
                                                               c->nn);
     LMTG_CUDA(cudaGetLastError());
     c->launches += 1;
@@ -453,7 +607,9 @@ void diff_setup(lmtg_ctx *c, const double *k, uint64_t nk, double rho_c, double 
         c->F.alloc(c->nn);
         c->u.alloc(c->nn);
         c->Dinv64.alloc(c->nn);
+        c->Dinv32.alloc(c->nn);
         for (auto &w : c->w64) w.alloc(c->nn);
+        for (auto &w : c->w32) w.alloc(c->nn);
         LMTG_CUDA(cudaMemsetAsync(c->u.p, 0, c->u.bytes(), s));
         c->allocated = true;
     }
@@ -494,8 +650,10 @@ void diff_setup(lmtg_ctx *c, const double *k, uint64_t nk, double rho_c, double 
     }
     k_jacobi_s<double><<<grid_for(c, c->nn, 256), 256, 0, s>>>(c->bdiag.p, c->K64.p, c->nn, c->Dinv64.p,
                                                                c->K32.p);
+    k_jacobi_s<float><<<grid_for(c, c->nn, 256), 256, 0, s>>>(c->bdiag.p, c->K64.p, c->nn, c->Dinv32.p,
+                                                              nullptr);
     LMTG_CUDA(cudaGetLastError());
-    c->launches += 1;
+    c->launches += 2;
     LMTG_CUDA(cudaStreamSynchronize(s));
     c->have64 = true;
 }
@@ -524,7 +682,7 @@ int diff_adjoint(lmtg_ctx *c, int nsteps, int ck, const double *target_dev, doub
     const int nck = nsteps / ck + 1;
     DBuf<double> ckpt, seg, lam, lam2, g;
     ckpt.alloc((uint64_t)nck * nn);
-    seg.alloc((uint64_t)(ck + 1) * nn);
+    if (ck > 1) seg.alloc((uint64_t)(ck + 1) * nn);  // ck == 1: every state is a checkpoint
     lam.alloc(nn);
     lam2.alloc(nn);
     g.alloc(c->ne);
@@ -557,16 +715,21 @@ int diff_adjoint(lmtg_ctx *c, int nsteps, int ck, const double *target_dev, doub
     // backward over segments
     for (int seg_start = ((nsteps - 1) / ck) * ck; seg_start >= 0 && status == LMTG_OK; seg_start -= ck) {
         const int seg_end = std::min(seg_start + ck, nsteps);
-        LMTG_CUDA(cudaMemcpyAsync(seg.p, ckpt.p + (uint64_t)(seg_start / ck) * nn, nn * 8,
-                                  cudaMemcpyDeviceToDevice, s));
-        for (int n = seg_start + 1; n <= seg_end && status == LMTG_OK; ++n) {
-            status = diff_step(c, seg.p + (uint64_t)(n - 1 - seg_start) * nn,
-                               seg.p + (uint64_t)(n - seg_start) * nn, tol, maxit, &it);
-            total += it;
+        // the segment's states: recomputed from its checkpoint, or the checkpoints themselves
+        const double *states = ckpt.p + (uint64_t)seg_start * nn;
+        if (ck > 1) {
+            LMTG_CUDA(cudaMemcpyAsync(seg.p, ckpt.p + (uint64_t)(seg_start / ck) * nn, nn * 8,
+                                      cudaMemcpyDeviceToDevice, s));
+            for (int n = seg_start + 1; n <= seg_end && status == LMTG_OK; ++n) {
+                status = diff_step(c, seg.p + (uint64_t)(n - 1 - seg_start) * nn,
+                                   seg.p + (uint64_t)(n - seg_start) * nn, tol, maxit, &it);
+                total += it;
+            }
+            states = seg.p;
         }
         for (int n = seg_end; n > seg_start && status == LMTG_OK; --n) {
-            const double *Tn = seg.p + (uint64_t)(n - seg_start) * nn;
-            const double *Tm = seg.p + (uint64_t)(n - 1 - seg_start) * nn;
+            const double *Tn = states + (uint64_t)(n - seg_start) * nn;
+            const double *Tm = states + (uint64_t)(n - 1 - seg_start) * nn;
             k_tri6_grad<<<grid_for(c, c->ne, 128, 16), 128, 0, s>>>(c->pos.p, c->conn.p, c->ne,
                                                                     c->theta, lam.p, Tn, Tm, g.p);
             c->launches += 1;
@@ -695,6 +858,14 @@ int lmtg_diff_setup(lmtg_ctx *c, const double *k, uint64_t nk, double rho_c, dou
         for (uint64_t q = 0; q < nbnd; ++q) LMTG_CHECK(bnd[q] < c->nn, LMTG_ERR_ARG, "node id >= nn");
         LMTG_CHECK(nbnd == 0 || penalty > 0, LMTG_ERR_UNSUPPORTED, "penalty constraints only");
         diff_setup(c, k, nk, rho_c, dt, theta, nbnd, bnd, penalty);
+        return LMTG_OK;
+    });
+}
+
+int lmtg_diff_set_solver(lmtg_ctx *c, int mode) {
+    return guard_d(c, [&] {
+        LMTG_CHECK(mode == LMTG_SOLVE_PCG_F64 || mode == LMTG_SOLVE_MIXED_IR, LMTG_ERR_ARG, "unknown mode");
+        c->diff_mode = mode;
         return LMTG_OK;
     });
 }

@@ -120,6 +120,7 @@ struct lmtg_ctx {
     // B64 holds B = M/dt - (1 - theta) K, K32 the FP32 copy of A; Ke64 / KeB64 the element blocks
     lmtg::DBuf<double> B64, KeB64;
     double rho_c = 1.0, dt = 0.0, theta = 0.5;
+    int diff_mode = LMTG_SOLVE_PCG_F64;
     lmtg::DBuf<float> Ke32, K32, Dinv32;
     bool have64 = false, have32 = false, have_vec = false;
     double max_diag = 0;

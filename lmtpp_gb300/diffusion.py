@@ -60,6 +60,11 @@ class Diffusion:
                                             float(theta), bnd.shape[0], abi.ptr(bnd) if bnd.size else None,
                                             float(penalty)), self._ctx, "diff_setup")
 
+    def set_solver(self, mode):
+        """'fp64' (FP64 Jacobi-PCG) or 'mixed' (FP32 PCG with FP64 residual replacement)."""
+        m = {"fp64": abi.SOLVE_PCG_F64, "mixed": abi.SOLVE_MIXED_IR}[mode]
+        abi.check(self._lib.lmtg_diff_set_solver(self._ctx, m), self._ctx, "set_solver")
+
     def set_penalty_scale(self, max_diag):
         abi.check(self._lib.lmtg_set_penalty_scale(self._ctx, float(max_diag)), self._ctx, "penalty scale")
 

@@ -88,3 +88,37 @@ def test_diffusion_adjoint_checkpoints_and_central_differences():
         fd = (Jof(kp) - Jof(km)) / (2 * h)
         assert fd == pytest.approx(g[e], rel=1e-5, abs=1e-9 * np.abs(g).max()), (e, fd, g[e])
     d.close()
+
+
+@pytest.mark.parametrize("theta", [0.5, 1.0])
+def test_diffusion_mixed_solver_matches_oracle(theta):
+    """FP32-inner steps with FP64 residual replacement reach the FP64 solution: 1e-8 relative."""
+    rng = np.random.default_rng(5)
+    P0 = O.diffusion_problem(17, theta=theta)
+    k = np.exp(0.3 * rng.standard_normal(P0["conn"].shape[0]))
+    P = O.diffusion_problem(17, k=k, theta=theta)
+    states = O.diffusion_run(P, 10)
+    d = Diffusion(P["pos"], P["conn"])
+    d.setup(k, rho_c=1.0, dt=1e-4, theta=theta, dirichlet=boundary_nodes(P["pos"]), penalty=1e5)
+    d.set_solver("mixed")
+    d.set_state(P["T0"])
+    st = d.run(10, tol=1e-12)
+    T = d.get_state()
+    assert np.linalg.norm(T - states[-1]) <= 1e-8 * np.linalg.norm(states[-1]), st
+    d.close()
+
+
+def test_diffusion_mixed_adjoint_matches_fp64():
+    rng = np.random.default_rng(11)
+    pos, conn = make_rect_triangle6(13)
+    k = np.exp(0.3 * rng.standard_normal(conn.shape[0]))
+    T0 = O.gaussian_bump(pos)
+    target = rng.standard_normal(pos.shape[0]) * 0.05
+    d = Diffusion(pos, conn)
+    d.setup(k, rho_c=1.0, dt=1e-3, theta=0.5, dirichlet=boundary_nodes(pos), penalty=1e5)
+    J64, g64 = d.adjoint_misfit(T0, target, 8, checkpoint_every=3, tol=1e-13)
+    d.set_solver("mixed")
+    J32, g32 = d.adjoint_misfit(T0, target, 8, checkpoint_every=3, tol=1e-13)
+    assert J32 == pytest.approx(J64, rel=1e-9)
+    assert np.linalg.norm(g32 - g64) <= 1e-8 * np.linalg.norm(g64)
+    d.close()
