@@ -51,7 +51,8 @@ def parse():
     p.add_argument("--fd", type=int, default=32, help="elements checked by central differences (adjoint mode)")
     p.add_argument("--steps-t", type=int, default=100, help="time steps (transient mode)")
     p.add_argument("--ckpt", type=int, default=10, help="checkpoint interval (transient mode)")
-    p.add_argument("--mode", default="bench", choices=["bench", "profile", "solve", "adjoint", "transient"],
+    p.add_argument("--nsys", type=int, default=256, help="meshes in the batch (batch mode)")
+    p.add_argument("--mode", default="bench", choices=["bench", "profile", "solve", "adjoint", "transient", "batch"],
                    help="profile: time the PCG kernels once on --side (small ncu case); "
                         "solve: one assemble + mixed solve at --tol (launch-list case)")
     p.add_argument("--tol", type=float, default=1e-10)
@@ -491,8 +492,72 @@ def run_transient(args):
     print(json.dumps(out), flush=True)
 
 
+def run_batch(args):
+    """Batched elasticity: --nsys (256) Hexa8 cubes with side n ~ U{8..32} elements
+    (rng.integers(8, 33)), E ~ U[5e4, 3e5], nu ~ U[0.2, 0.4] per cube (default_rng(seed), drawn in
+    that order), clamped on x = 0 (penalty 1e5 x the cube's max|diag|), four right-hand sides:
+    unit tractions +x, +y, +z on x = 1 and a N(0, 1) nodal load (same generator, after the
+    materials).  All pairs solved to a 1e-10 FP64 relative residual, mixed and FP64."""
+    import torch
+    from lmtpp_gb300 import make_rect_hexa, x1_faces_hexa
+    from lmtpp_gb300.batch import BatchFormulation
+    rng = np.random.default_rng(SEED)
+    sides = rng.integers(8, 33, args.nsys)
+    E = rng.uniform(5e4, 3e5, args.nsys)
+    nu = rng.uniform(0.2, 0.4, args.nsys)
+    meshes = [make_rect_hexa((int(n) + 1,) * 3) for n in sides]
+    t0 = time.perf_counter()
+    bf = BatchFormulation(meshes)
+    bf.set_materials(E, nu)
+    clamped = np.nonzero(bf.pos[:, 0] < 1e-6)[0]
+    bf.add_constraints((3 * clamped[:, None] + np.arange(3)[None, :]).ravel(), 1e5)
+    bf.assemble(True, False, mixed=True)
+    faces = x1_faces_hexa(bf.pos, bf.conn)
+    B = np.zeros((4, bf.n))
+    for r in range(3):
+        bf.set_nodal_loads(np.zeros(bf.n))
+        t = np.zeros(3)
+        t[r] = 1.0
+        bf.add_skin_traction(faces, t)
+        bf.assemble(False, True)
+        B[r] = bf.get_sollicitation()
+    B[3] = rng.standard_normal(bf.n)
+    setup_s = time.perf_counter() - t0
+    out = {"mode": "batch",
+           "workload": "%d Hexa8 cubes, side ~ U{8..32} (seed %d), E ~ U[5e4,3e5], nu ~ U[0.2,0.4], "
+                       "clamped x=0 (penalty 1e5), 4 RHS (+x/+y/+z unit traction on x=1, N(0,1) nodal)"
+                       % (args.nsys, SEED),
+           "dofs": bf.n, "elements": bf.ne, "setup_s": setup_s, "tol": args.tol}
+    for mode in ("mixed", "fp64"):
+        bf.solve_batch(B, mode=mode, tol=args.tol)  # warm-up: autotuner, buffers, caches
+        torch.cuda.synchronize()
+        w0 = time.perf_counter()
+        X, st, its = bf.solve_batch(B, mode=mode, tol=args.tol)
+        wall = time.perf_counter() - w0
+        out["solve_ms_" + mode] = st["device_ms"]
+        out["e2e_wall_ms_" + mode] = wall * 1e3
+        out["max_pair_iters_" + mode] = int(its.max())
+        out["segments_" + mode] = st["outer_iterations"]
+        out["worst_rel_residual_" + mode] = st["rel_residual"]
+        out["dof_rhs_per_s_" + mode] = 4 * bf.n / (st["device_ms"] * 1e-3)
+        if mode == "mixed":
+            big, small = int(np.argmax(sides)), int(np.argmin(sides))
+            out["iters_side%d" % sides[big]] = its[big].tolist()
+            out["iters_side%d" % sides[small]] = its[small].tolist()
+            Xm = X
+    out["speedup_mixed_vs_fp64"] = out["solve_ms_fp64"] / out["solve_ms_mixed"]
+    out["mixed_vs_fp64_max_rel_diff"] = float(max(np.linalg.norm(Xm[r] - X[r]) / np.linalg.norm(X[r])
+                                                 for r in range(4)))
+    out["autotuner"] = bf.batch_info()
+    out["launches"] = bf.launch_count()
+    bf.close()
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
+    if args.mode == "batch":
+        return run_batch(args)
     if args.mode == "transient":
         if args.side == 128:
             args.side = 1024

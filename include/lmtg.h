@@ -242,6 +242,39 @@ int lmtg_diff_adjoint_misfit(lmtg_ctx *ctx, int nsteps, int checkpoint_every, co
 /* A and B as lower CSR (rowptr nn+1, col/A/B nnz_lower = (blocks - nn)/2 + nn entries). */
 int lmtg_diff_get_matrices(lmtg_ctx *ctx, uint64_t *rowptr, uint32_t *col, double *A, double *B);
 
+/* ---- batches of independent meshes (no reference counterpart as one call: the reference
+ * solves one Formulation per mesh and one right-hand side per solve,
+ * include/formulation/formulation_ancestor.h:64) ----
+ * The context's mesh is the concatenation of nsys meshes: system m owns the node range
+ * [node_off[m], node_off[m+1]) (node_off[0] = 0, node_off[nsys] = nn) and no element couples two
+ * ranges.  The penalty scale max|diag| is then taken per system.  Call after lmtg_mesh_set. */
+int lmtg_batch_set(lmtg_ctx *ctx, uint32_t nsys, const uint64_t *node_off);
+/* Per-element Poisson ratios (n_nu = ne), replacing the single value of lmtg_material_set
+ * (which returns the context to a single ratio: call this one after it). */
+int lmtg_material_set_nu(lmtg_ctx *ctx, const double *nu, uint64_t n_nu);
+/* nrhs (1..4) right-hand sides, B[r * ndof + i] (host); resets the batch solution to 0. */
+int lmtg_batch_set_rhs(lmtg_ctx *ctx, int nrhs, const double *B);
+/* Solves every (system, rhs) pair to |b - K x|_2 <= tol |b|_2 (FP64 true residual of that pair)
+ * with block-Jacobi PCG: LMTG_SOLVE_PCG_F64 or LMTG_SOLVE_MIXED_IR (FP32 inner, FP64 residual
+ * replacement; needs LMTG_ASM_MAT32).  maxit bounds the iterations of every pair.  stats: the
+ * largest pair iteration count, FP32 segments, and the worst final relative residual;
+ * pair_iters (optional, nsys * nrhs ints, system-major) the iterations of each pair. */
+int lmtg_batch_solve(lmtg_ctx *ctx, int mode, double tol, int maxit, double timeout_s,
+                     lmtg_solve_stats *stats, int *pair_iters);
+/* The solutions, X[r * ndof + i] (nrhs x ndof doubles, host). */
+int lmtg_batch_get_result(lmtg_ctx *ctx, double *X);
+/* The autotuner's choice: rows per tile, SpMV variant (0 plain, 1 next row prefetched), tile
+ * count, and the SpMV time of each candidate (8 doubles, ms, variant-major over tile sizes
+ * 16, 32, 64, 128 rows; 0 = not tried; optional).  A tile is one warp's work. */
+int lmtg_batch_info(lmtg_ctx *ctx, int *tile_rows, int *variant, uint64_t *ntiles, double *tuned_ms);
+/* Fixed rows per tile (0: autotune) and SpMV variant (-1: autotune) of the batch solver. */
+int lmtg_batch_set_options(lmtg_ctx *ctx, int tile_rows, int variant);
+
+/* Mixed-precision solvers (lmtg_solve_system, lmtg_batch_solve, the diffusion steps): the
+ * recursive-residual reduction of each FP32 segment before the FP64 residual replacement,
+ * in (0, 1); default 0.01.  No reference counterpart. */
+int lmtg_set_inner_reduction(lmtg_ctx *ctx, double inner_reduction);
+
 /* Sizes of the current problem. */
 int lmtg_get_sizes(lmtg_ctx *ctx, uint64_t *nn, uint64_t *ne, uint64_t *ndof, uint64_t *nnz_blocks);
 

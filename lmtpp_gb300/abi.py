@@ -74,6 +74,14 @@ _SIGS = {
     "lmtg_adjoint_grad": (_i, [_vp, _i, _vp, _vp, _i, _d, _i, _d, ctypes.POINTER(_d), _vp,
                                ctypes.POINTER(SolveStats)]),
     "lmtg_get_stream": (_i, [_vp, ctypes.POINTER(_vp)]),
+    "lmtg_batch_set": (_i, [_vp, ctypes.c_uint32, _vp]),
+    "lmtg_material_set_nu": (_i, [_vp, _vp, _u64]),
+    "lmtg_batch_set_rhs": (_i, [_vp, _i, _vp]),
+    "lmtg_batch_solve": (_i, [_vp, _i, _d, _i, _d, ctypes.POINTER(SolveStats), _vp]),
+    "lmtg_batch_get_result": (_i, [_vp, _vp]),
+    "lmtg_batch_info": (_i, [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(_u64), _vp]),
+    "lmtg_batch_set_options": (_i, [_vp, _i, _i]),
+    "lmtg_set_inner_reduction": (_i, [_vp, _d]),
     "lmtg_residual_norm_noalloc": (_i, [_vp, _u64, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.POINTER(_d)]),
     "lmtg_profile_pcg_kernels": (_i, [_vp, _i, _i, ctypes.POINTER(_d), ctypes.POINTER(_d)]),
 }

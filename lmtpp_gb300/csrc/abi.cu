@@ -145,6 +145,7 @@ int lmtg_destroy(lmtg_ctx *c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->h_scal) cudaFreeHost(c->h_scal);
+    batch_free(c);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;  // DBuf destructors free device memory
     return LMTG_OK;
@@ -312,8 +313,118 @@ int lmtg_material_set(lmtg_ctx *c, const double *E, uint64_t nE, double nu) {
         upload(c, c->E, E, nE);
         c->E_per_elem = nE > 1 ? 1 : 0;
         c->nu = nu;
+        c->nu_per_elem = 0;  // lmtg_material_set_nu afterwards for per-element ratios
         c->have64 = c->have32 = false;
         LMTG_CUDA(cudaStreamSynchronize(c->stream));
+        return LMTG_OK;
+    });
+}
+
+int lmtg_material_set_nu(lmtg_ctx *c, const double *nu, uint64_t n_nu) {
+    return guard(c, [&] {
+        LMTG_CHECK(c->ne > 0, LMTG_ERR_STATE, "mesh_set first");
+        LMTG_CHECK(nu && n_nu == c->ne, LMTG_ERR_ARG, "nu needs ne values");
+        for (uint64_t e = 0; e < n_nu; ++e)
+            LMTG_CHECK(nu[e] > -1.0 && nu[e] < 0.5, LMTG_ERR_ARG, "poisson_ratio out of (-1, 0.5)");
+        upload(c, c->nuv, nu, n_nu);
+        c->nu_per_elem = 1;
+        c->have64 = c->have32 = false;
+        LMTG_CUDA(cudaStreamSynchronize(c->stream));
+        return LMTG_OK;
+    });
+}
+
+int lmtg_batch_set(lmtg_ctx *c, uint32_t nsys, const uint64_t *node_off) {
+    return guard(c, [&] {
+        LMTG_CHECK(c->ne > 0 && c->nnu == 3, LMTG_ERR_STATE, "elasticity mesh_set first");
+        LMTG_CHECK(nsys > 0 && node_off, LMTG_ERR_ARG, "nsys > 0 and node_off needed");
+        LMTG_CHECK(node_off[0] == 0 && node_off[nsys] == c->nn, LMTG_ERR_ARG, "node_off must span 0..nn");
+        std::vector<uint32_t> sys(c->nn);
+        for (uint32_t m = 0; m < nsys; ++m) {
+            LMTG_CHECK(node_off[m + 1] > node_off[m], LMTG_ERR_ARG, "empty or decreasing node range");
+            for (uint64_t i = node_off[m]; i < node_off[m + 1]; ++i) sys[i] = m;
+        }
+        for (uint64_t e = 0; e < c->ne; ++e) {
+            const uint32_t m = sys[c->h_conn[e * c->npe]];
+            for (int k = 1; k < c->npe; ++k)
+                LMTG_CHECK(sys[c->h_conn[e * c->npe + k]] == m, LMTG_ERR_ARG, "an element couples two systems");
+        }
+        c->h_sys_node_off.assign(node_off, node_off + nsys + 1);
+        upload_u32(c, c->sys_of_node, sys.data(), sys.size());
+        c->nsys = nsys;
+        c->h_sys_max_diag.assign(nsys, 0.0);
+        batch_free(c);
+        c->have64 = c->have32 = false;
+        LMTG_CUDA(cudaStreamSynchronize(c->stream));
+        return LMTG_OK;
+    });
+}
+
+int lmtg_batch_set_rhs(lmtg_ctx *c, int nrhs, const double *B) {
+    return guard(c, [&] {
+        LMTG_CHECK(nrhs >= 1 && nrhs <= 4 && B, LMTG_ERR_ARG, "1..4 right-hand sides");
+        batch_set_rhs(c, nrhs, B);
+        return LMTG_OK;
+    });
+}
+
+int lmtg_batch_solve(lmtg_ctx *c, int mode, double tol, int maxit, double timeout_s, lmtg_solve_stats *st,
+                     int *pair_iters) {
+    lmtg_solve_stats local{};
+    if (!st) st = &local;
+    memset(st, 0, sizeof(*st));
+    int s = guard(c, [&] {
+        LMTG_CHECK(maxit > 0 && tol > 0, LMTG_ERR_ARG, "maxit > 0, tol > 0");
+        cudaEvent_t e0, e1;
+        LMTG_CUDA(cudaEventCreate(&e0));
+        LMTG_CUDA(cudaEventCreate(&e1));
+        LMTG_CUDA(cudaEventRecord(e0, c->stream));
+        const int status = batch_solve(c, mode, tol, maxit, timeout_s, st, pair_iters);
+        LMTG_CUDA(cudaEventRecord(e1, c->stream));
+        LMTG_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        st->device_ms = ms;
+        if (status != LMTG_OK) c->err = lmtg_status_string(status);
+        return status;
+    });
+    st->status = s;
+    return s;
+}
+
+int lmtg_batch_get_result(lmtg_ctx *c, double *X) {
+    return guard(c, [&] {
+        LMTG_CHECK(X, LMTG_ERR_ARG, "null output");
+        batch_get_result(c, X);
+        return LMTG_OK;
+    });
+}
+
+int lmtg_batch_info(lmtg_ctx *c, int *tile_rows, int *variant, uint64_t *ntiles, double *tuned_ms) {
+    return guard(c, [&] {
+        batch_info(c, tile_rows, variant, ntiles, tuned_ms);
+        return LMTG_OK;
+    });
+}
+
+int lmtg_set_inner_reduction(lmtg_ctx *c, double inner_reduction) {
+    return guard(c, [&] {
+        LMTG_CHECK(inner_reduction > 0 && inner_reduction < 1, LMTG_ERR_ARG, "inner_reduction in (0, 1)");
+        c->inner_reduction = inner_reduction;
+        return LMTG_OK;
+    });
+}
+
+int lmtg_batch_set_options(lmtg_ctx *c, int tile_rows, int variant) {
+    return guard(c, [&] {
+        LMTG_CHECK(tile_rows == 0 || tile_rows == 16 || tile_rows == 32 || tile_rows == 64 || tile_rows == 128,
+                   LMTG_ERR_ARG, "tile_rows: 0 (autotune), 16, 32, 64 or 128");
+        LMTG_CHECK(variant >= -1 && variant <= 1, LMTG_ERR_ARG, "variant: -1 (autotune), 0 or 1");
+        c->batch_tile_rows = tile_rows;
+        c->batch_variant = variant;
+        batch_free(c);  // re-tune at the next solve
         return LMTG_OK;
     });
 }

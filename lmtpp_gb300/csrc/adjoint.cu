@@ -26,13 +26,14 @@ namespace lmtg {
 
 template <class EL>
 __global__ void __launch_bounds__(128)
-    k_grad_E(const double *__restrict__ pos, const uint32_t *__restrict__ conn, double nu,
-             uint64_t ne, const double *__restrict__ a, const double *__restrict__ b,
-             double *__restrict__ g) {
+    k_grad_E(const double *__restrict__ pos, const uint32_t *__restrict__ conn, double nu0,
+             const double *__restrict__ nuv, uint64_t ne, const double *__restrict__ a,
+             const double *__restrict__ b, double *__restrict__ g) {
     constexpr int NPE = EL::npe;
-    const double lh = nu / ((1.0 + nu) * (1.0 - 2.0 * nu)), mh = 1.0 / (2.0 * (1.0 + nu));
     for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < ne;
          e += (uint64_t)gridDim.x * blockDim.x) {
+        const double nu = nuv ? nuv[e] : nu0;
+        const double lh = nu / ((1.0 + nu) * (1.0 - 2.0 * nu)), mh = 1.0 / (2.0 * (1.0 + nu));
         uint32_t nd[NPE];
         double xyz[NPE][3];
 #pragma unroll
@@ -99,9 +100,11 @@ void launch_grad_E(lmtg_ctx *c, const double *a, const double *b, double *g) {
     const int T = 128;
     const int grid = grid_for(c, c->ne, T, 16);
     if (c->elem_type == LMTG_ELEM_HEXA8)
-        k_grad_E<Hexa8><<<grid, T, 0, c->stream>>>(c->pos.p, c->conn.p, c->nu, c->ne, a, b, g);
+        k_grad_E<Hexa8><<<grid, T, 0, c->stream>>>(c->pos.p, c->conn.p, c->nu, c->nu_per_elem ? c->nuv.p : nullptr,
+                                                   c->ne, a, b, g);
     else
-        k_grad_E<Tetra10><<<grid, T, 0, c->stream>>>(c->pos.p, c->conn.p, c->nu, c->ne, a, b, g);
+        k_grad_E<Tetra10><<<grid, T, 0, c->stream>>>(c->pos.p, c->conn.p, c->nu, c->nu_per_elem ? c->nuv.p : nullptr,
+                                                   c->ne, a, b, g);
     LMTG_CUDA(cudaGetLastError());
     c->launches += 1;
 }

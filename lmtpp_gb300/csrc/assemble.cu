@@ -12,6 +12,8 @@
 #include <cstring>
 #include <type_traits>
 
+#include <algorithm>
+#include <cstring>
 #include "lmtg_internal.cuh"
 
 namespace lmtg {
@@ -81,27 +83,41 @@ void assemble_matrix(lmtg_ctx *c, bool from64, bool want64, bool want32) {
 // orders like the value and an integer atomicMax is exact.
 template <class T>
 __global__ void k_max_diag(const uint32_t *__restrict__ bptr, const uint32_t *__restrict__ bdiag,
-                           const T *__restrict__ K, uint64_t nn, unsigned long long *out) {
-    double m = 0;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nn;
-         i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t rb = bptr[i], deg = bptr[i + 1] - rb, d = bdiag[i] - rb;
-        m = fmax(m, fmax(fabs((double)K[kidx(rb, deg, d, 0)]),
-                         fmax(fabs((double)K[kidx(rb, deg, d, 4)]), fabs((double)K[kidx(rb, deg, d, 8)]))));
+                           const T *__restrict__ K, uint64_t nn, const uint32_t *__restrict__ sys,
+                           unsigned long long *out) {
+    // grid-stride over whole warps so that every lane reaches the shuffles below
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i0 = blockIdx.x * (uint64_t)blockDim.x + (threadIdx.x & ~31u); i0 < nn; i0 += stride) {
+        const uint64_t i = i0 + (threadIdx.x & 31);
+        double m = 0;
+        uint32_t s = 0;
+        if (i < nn) {
+            const uint32_t rb = bptr[i], deg = bptr[i + 1] - rb, d = bdiag[i] - rb;
+            m = fmax(fabs((double)K[kidx(rb, deg, d, 0)]),
+                     fmax(fabs((double)K[kidx(rb, deg, d, 4)]), fabs((double)K[kidx(rb, deg, d, 8)])));
+            s = sys ? sys[i] : 0u;
+        }
+        // one system per warp (the usual case): one atomic; otherwise one per lane
+        const uint32_t s0 = __shfl_sync(0xffffffffu, s, 0);
+        if (__all_sync(0xffffffffu, i >= nn || s == s0)) {
+            m = warp_max(m);
+            if ((threadIdx.x & 31) == 0) atomicMax(out + s0, (unsigned long long)__double_as_longlong(m));
+        } else if (i < nn) {
+            atomicMax(out + s, (unsigned long long)__double_as_longlong(m));
+        }
     }
-    m = warp_max(m);
-    if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
 }
 
 template <class T>
 __global__ void k_penalty(const uint32_t *__restrict__ bptr, const uint32_t *__restrict__ bdiag, T *K, double *F,
                           const uint32_t *__restrict__ dof, const double *__restrict__ coef,
                           const double *__restrict__ res, uint64_t nc, double penalty,
-                          const unsigned long long *md_bits, bool mat, bool vec) {
-    const double md = __longlong_as_double((long long)*md_bits);
+                          const uint32_t *__restrict__ sys, const unsigned long long *md_bits, bool mat,
+                          bool vec) {
     for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < nc;
          k += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t j = dof[k];
+        const double md = __longlong_as_double((long long)md_bits[sys ? sys[j / 3] : 0u]);
         const double C = coef[k] * md * penalty;
         if (vec) atomicAdd(F + j, C * res[k]);
         if (mat) {
@@ -122,45 +138,61 @@ __global__ void k_round_constrained(const uint32_t *__restrict__ bptr,
     }
 }
 
+// One penalty scale per system of a batch (nsys > 0), else one for the whole matrix.
 void apply_penalty(lmtg_ctx *c, bool mat, bool vec) {
     if (c->nc == 0) return;
+    const uint32_t ns = c->nsys ? c->nsys : 1;
+    const uint32_t *sys = c->nsys ? c->sys_of_node.p : nullptr;
     DBuf<unsigned long long> md;
-    md.alloc(1);
+    md.alloc(ns);
     const int T = 256;
+    auto upload_scales = [&](const std::vector<double> &v) {
+        std::vector<unsigned long long> bits(ns);
+        for (uint32_t m = 0; m < ns; ++m) memcpy(&bits[m], &v[m], sizeof(double));
+        LMTG_CUDA(cudaMemcpyAsync(md.p, bits.data(), ns * sizeof(unsigned long long), cudaMemcpyHostToDevice,
+                                  c->stream));
+        LMTG_CUDA(cudaStreamSynchronize(c->stream));
+    };
     if (mat && c->penalty_scale > 0.0) {
         // caller-fixed scale (held constant for sensitivities w.r.t. the material)
-        unsigned long long bits;
-        memcpy(&bits, &c->penalty_scale, sizeof(bits));
-        LMTG_CUDA(cudaMemcpyAsync(md.p, &bits, sizeof(bits), cudaMemcpyHostToDevice, c->stream));
+        upload_scales(std::vector<double>(ns, c->penalty_scale));
     } else if (mat) {
         // max|diag| of the freshly assembled K, before any constraint (formulation.h:1029-1030)
-        LMTG_CUDA(cudaMemsetAsync(md.p, 0, sizeof(unsigned long long), c->stream));
-        if (c->have64) k_max_diag<double><<<grid_for(c, c->nn, T), T, 0, c->stream>>>(c->bptr.p, c->bdiag.p, c->K64.p, c->nn, md.p);
-        else k_max_diag<float><<<grid_for(c, c->nn, T), T, 0, c->stream>>>(c->bptr.p, c->bdiag.p, c->K32.p, c->nn, md.p);
+        LMTG_CUDA(cudaMemsetAsync(md.p, 0, ns * sizeof(unsigned long long), c->stream));
+        if (c->have64)
+            k_max_diag<double><<<grid_for(c, c->nn, T), T, 0, c->stream>>>(c->bptr.p, c->bdiag.p, c->K64.p, c->nn,
+                                                                           sys, md.p);
+        else
+            k_max_diag<float><<<grid_for(c, c->nn, T), T, 0, c->stream>>>(c->bptr.p, c->bdiag.p, c->K32.p, c->nn,
+                                                                          sys, md.p);
     } else {
         // vector-only assembly reuses the max|diag| of the last matrix assembly
-        unsigned long long bits;
-        memcpy(&bits, &c->max_diag, sizeof(bits));
-        LMTG_CUDA(cudaMemcpyAsync(md.p, &bits, sizeof(bits), cudaMemcpyHostToDevice, c->stream));
+        upload_scales(c->nsys ? c->h_sys_max_diag : std::vector<double>(1, c->max_diag));
     }
     const int g = grid_for(c, c->nc, T);
     if (c->have64) {
         k_penalty<double><<<g, T, 0, c->stream>>>(c->bptr.p, c->bdiag.p, c->K64.p, c->F.p, c->cdof.p, c->ccoef.p,
-                                                  c->cres.p, c->nc, c->penalty, md.p, mat, vec);
+                                                  c->cres.p, c->nc, c->penalty, sys, md.p, mat, vec);
         if (mat && c->have32)
             k_round_constrained<<<g, T, 0, c->stream>>>(c->bptr.p, c->bdiag.p, c->K64.p, c->K32.p, c->cdof.p, c->nc);
     } else {
         k_penalty<float><<<g, T, 0, c->stream>>>(c->bptr.p, c->bdiag.p, c->K32.p, c->F.p, c->cdof.p, c->ccoef.p,
-                                                 c->cres.p, c->nc, c->penalty, md.p, mat, vec);
+                                                 c->cres.p, c->nc, c->penalty, sys, md.p, mat, vec);
     }
     LMTG_CUDA(cudaGetLastError());
     c->launches += ((mat && c->penalty_scale <= 0.0) ? 1 : 0) + 1 + ((mat && c->have64 && c->have32) ? 1 : 0);
-    unsigned long long bits = 0;
-    LMTG_CUDA(cudaMemcpyAsync(&bits, md.p, sizeof(bits), cudaMemcpyDeviceToHost, c->stream));
+    std::vector<unsigned long long> bits(ns);
+    LMTG_CUDA(cudaMemcpyAsync(bits.data(), md.p, ns * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                              c->stream));
     LMTG_CUDA(cudaStreamSynchronize(c->stream));
-    double v;
-    memcpy(&v, &bits, sizeof(v));
-    c->max_diag = v;
+    std::vector<double> v(ns);
+    double vmax = 0;
+    for (uint32_t m = 0; m < ns; ++m) {
+        memcpy(&v[m], &bits[m], sizeof(double));
+        vmax = std::max(vmax, v[m]);
+    }
+    c->max_diag = vmax;
+    if (c->nsys) c->h_sys_max_diag = v;
 }
 
 // ---- block-Jacobi preconditioner: inverse of every 3x3 diagonal block ----

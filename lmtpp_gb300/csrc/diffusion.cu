@@ -513,7 +513,7 @@ static int diff_pcg64(lmtg_ctx *c, const double *b, double *x, double tol, int m
 
 // FP32-inner / FP64-refined solve of A x = b with reliable updates (the elasticity solver's
 // scheme on the scalar matrices): FP32 Jacobi-PCG segments on A32 d = r / s, each ending after a
-// 10x reduction of its recursive residual; x += s d and r = b - A x in FP64; the search
+// reduction of its recursive residual by inner_reduction; x += s d and r = b - A x in FP64; the search
 // direction is kept across the residual replacement.
 static int diff_mixed(lmtg_ctx *c, const double *b, double *x, double tol, int maxit, int *iters) {
     cudaStream_t st = c->stream;
@@ -530,7 +530,7 @@ static int diff_mixed(lmtg_ctx *c, const double *b, double *x, double tol, int m
     k_dot_s<<<ngrid(c), kRowThreads, 0, st>>>(b, b, c->nn, c->partials.p, &o->cnt_c, &o->rr);
     c->launches += 1;
     const double bb = read_rr();
-    constexpr double kDelta = 0.1;
+    const double kDelta = c->inner_reduction;
     int total = 0, status = LMTG_OK, outer = 0;
     double s_prev = 0, rz_prev = 0, rel_prev = 0;
     bool have_dir = false;

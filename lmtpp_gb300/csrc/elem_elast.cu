@@ -34,8 +34,8 @@ struct ElSmem {
 template <class EL, class T, int kTab>
 __global__ void __launch_bounds__(kElWarps * 32)
     k_elast(const double *__restrict__ pos, const uint32_t *__restrict__ conn,
-            const double *__restrict__ E, int E_per_elem, double nu, uint64_t ne,
-            T *__restrict__ Ke) {
+            const double *__restrict__ E, int E_per_elem, double nu0, const double *__restrict__ nuv,
+            uint64_t ne, T *__restrict__ Ke) {
     constexpr int NPE = EL::npe, NGP = EL::ngp, NP = EL::npairs;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     ElSmem<EL, T> &S = reinterpret_cast<ElSmem<EL, T> *>(smem_raw)[threadIdx.x >> 5];
@@ -57,6 +57,7 @@ __global__ void __launch_bounds__(kElWarps * 32)
         if (lane < kElBatch) {
             const uint64_t e = e0 + lane;
             const double Ee = e < ne ? E[E_per_elem ? e : 0] : 0.0;
+            const double nu = (nuv && e < ne) ? nuv[e] : nu0;
             S.lam[lane] = (T)(Ee * nu / ((1.0 + nu) * (1.0 - 2.0 * nu)));
             S.mu[lane] = (T)(Ee / (2.0 * (1.0 + nu)));
         }
@@ -136,13 +137,15 @@ static void launch_t(lmtg_ctx *c, bool fp64) {
         LMTG_CUDA(cudaFuncSetAttribute(k_elast<EL, double, kTab>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
         k_elast<EL, double, kTab><<<grid_for(c, nbatch * 32, threads, 2), threads, sm, c->stream>>>(
-            c->pos.p, c->conn.p, c->E.p, c->E_per_elem, c->nu, c->ne, c->Ke64.p);
+            c->pos.p, c->conn.p, c->E.p, c->E_per_elem, c->nu, c->nu_per_elem ? c->nuv.p : nullptr, c->ne,
+            c->Ke64.p);
     } else {
         const size_t sm = sizeof(ElSmem<EL, float>) * kElWarps;
         LMTG_CUDA(cudaFuncSetAttribute(k_elast<EL, float, kTab>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
         k_elast<EL, float, kTab><<<grid_for(c, nbatch * 32, threads, 4), threads, sm, c->stream>>>(
-            c->pos.p, c->conn.p, c->E.p, c->E_per_elem, c->nu, c->ne, c->Ke32.p);
+            c->pos.p, c->conn.p, c->E.p, c->E_per_elem, c->nu, c->nu_per_elem ? c->nuv.p : nullptr, c->ne,
+            c->Ke32.p);
     }
     LMTG_CUDA(cudaGetLastError());
     c->launches += 1;

@@ -90,6 +90,10 @@ struct PcgScalars {
 
 }  // namespace lmtg
 
+namespace lmtg {
+struct BatchState;  // batch.cu
+}
+
 struct lmtg_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -104,6 +108,18 @@ struct lmtg_ctx {
     lmtg::DBuf<double> E;
     int E_per_elem = 0;
     double nu = 0.3;
+    lmtg::DBuf<double> nuv;  // per-element Poisson ratios (nu_per_elem)
+    int nu_per_elem = 0;
+
+    // batch of independent systems: node ranges [sys_node_off[m], sys_node_off[m+1]) that no
+    // element couples; the penalty scale max|diag| is taken per system
+    uint32_t nsys = 0;
+    std::vector<uint64_t> h_sys_node_off;
+    lmtg::DBuf<uint32_t> sys_of_node;
+    std::vector<double> h_sys_max_diag;
+    lmtg::BatchState *batch = nullptr;
+    int batch_tile_rows = 0;             // 0: autotuned
+    int batch_variant = -1;              // -1: autotuned
     std::vector<double> h_pos;      // host copy of positions (skin loads)
     std::vector<uint32_t> h_conn;   // host copy of connectivity
 
@@ -121,6 +137,9 @@ struct lmtg_ctx {
     lmtg::DBuf<double> B64, KeB64;
     double rho_c = 1.0, dt = 0.0, theta = 0.5;
     int diff_mode = LMTG_SOLVE_PCG_F64;
+    // mixed solvers: recursive-residual reduction of each FP32 segment before the FP64 residual
+    // replacement (lmtg_set_inner_reduction)
+    double inner_reduction = 0.01;
     lmtg::DBuf<float> Ke32, K32, Dinv32;
     bool have64 = false, have32 = false, have_vec = false;
     double max_diag = 0;
@@ -173,6 +192,14 @@ inline void upload_u32(lmtg_ctx *c, DBuf<T> &d, const T *h, size_t n) {
     d.alloc(n);
     if (n) LMTG_CUDA(cudaMemcpyAsync(d.p, h, n * sizeof(T), cudaMemcpyHostToDevice, c->stream));
 }
+
+// ---- batches (batch.cu) ----
+void batch_free(lmtg_ctx *c);
+void batch_set_rhs(lmtg_ctx *c, int nrhs, const double *B_host);
+int batch_solve(lmtg_ctx *c, int mode, double tol, int maxit, double timeout_s, lmtg_solve_stats *st,
+                int *pair_iters);
+void batch_get_result(lmtg_ctx *c, double *X_host);
+void batch_info(lmtg_ctx *c, int *tile_rows, int *variant, uint64_t *ntiles, double *tuned_ms);
 
 // ---- solver (solver.cu) ----
 void spmv64(lmtg_ctx *c, const double *x, double *y);

@@ -219,7 +219,7 @@ int solve_mixed(lmtg_ctx *c, double tol, int maxit, double timeout_s, lmtg_solve
           *pa = c->w32[4].p, *pb = c->w32[5].p;
     float *q32 = reinterpret_cast<float *>(c->w64[1].p);  // FP64 buffer reused as FP32 q
     const double bb = dot64(c, Fb, Fb);
-    constexpr double kDelta = 0.1;  // recursive-residual reduction per segment
+    const double kDelta = c->inner_reduction;  // recursive-residual reduction per segment
     int total = 0, outer = 0, status = LMTG_OK;
     double rel = 0, s_prev = 0, rz_prev = 0, rel_prev = 0;
     bool have_dir = false;

@@ -65,6 +65,11 @@ class Diffusion:
         m = {"fp64": abi.SOLVE_PCG_F64, "mixed": abi.SOLVE_MIXED_IR}[mode]
         abi.check(self._lib.lmtg_diff_set_solver(self._ctx, m), self._ctx, "set_solver")
 
+    def set_inner_reduction(self, inner_reduction):
+        """Recursive-residual reduction of each FP32 segment of the mixed step solver (default 0.01)."""
+        abi.check(self._lib.lmtg_set_inner_reduction(self._ctx, float(inner_reduction)), self._ctx,
+                  "set_inner_reduction")
+
     def set_penalty_scale(self, max_diag):
         abi.check(self._lib.lmtg_set_penalty_scale(self._ctx, float(max_diag)), self._ctx, "penalty scale")
 

@@ -280,6 +280,11 @@ class Formulation:
         return y
 
     # -- sensitivities -------------------------------------------------------------------------
+    def set_inner_reduction(self, inner_reduction):
+        """Recursive-residual reduction of each FP32 segment of the mixed solvers (default 0.01)."""
+        abi.check(self._lib.lmtg_set_inner_reduction(self._ctx, float(inner_reduction)), self._ctx,
+                  "set_inner_reduction")
+
     def set_penalty_scale(self, max_diag):
         """Hold the penalty scale at max_diag (0 = recompute max|diag K| at each assembly)."""
         abi.check(self._lib.lmtg_set_penalty_scale(self._ctx, float(max_diag)), self._ctx, "penalty scale")
