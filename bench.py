@@ -192,9 +192,11 @@ def timed_steps(f, mode, tol, steps, torch, stream):
 
 
 def spmv_bytes(nn, nnzb, s):
-    """Algorithmic bytes of one fused PCG SpMV launch (k_pcg_spmv): K values + block column
-    indices + row pointers, z and p_old read once, p_new and q written once."""
-    return nnzb * (9 * s + 4) + 4 * (nn + 1) + 4 * 3 * nn * s
+    """Algorithmic bytes of one PCG SpMV launch (k_pcg_spmv): K values + block column indices
+    + row pointers, p read once (gathered; 16 B per node padded in FP32, 24 B in FP64) and q
+    written once (3 values per node)."""
+    vs = 4 if s == 4 else 3
+    return nnzb * (9 * s + 4) + 4 * (nn + 1) + vs * nn * s + 3 * nn * s
 
 
 def run_gpu(args, rank, world, local, barrier, allmax):
@@ -329,8 +331,9 @@ def cpu_desc(s):
 
 
 # dram__bytes_read.sum + dram__bytes_write.sum / algorithmic bytes of one k_pcg_spmv<float>
-# launch, ncu capture of the Hexa8 64^3 case (301.4 MB + 8.4 MB over 301.4 MB)
-SPMV32_TRAFFIC_RATIO = (301.365 + 8.372) / 301.365
+# launch, ncu capture of the Hexa8 64^3 case: (293.904 MB + 5.595 MB) over
+# spmv_bytes(274625, 7189057, 4) = 296.350 MB
+SPMV32_TRAFFIC_RATIO = (293.904384 + 5.595136) / 296.350284
 
 METRIC = "time-to-solution at 1e-10 rel. error vs FP64 oracle, mixed vs FP64 CG; asm GB/s"
 

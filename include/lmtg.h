@@ -275,6 +275,13 @@ int lmtg_batch_set_options(lmtg_ctx *ctx, int tile_rows, int variant);
  * in (0, 1); default 0.01.  No reference counterpart. */
 int lmtg_set_inner_reduction(lmtg_ctx *ctx, double inner_reduction);
 
+/* Element fields after the solve (replaces the generated apply_on_elements_after_solve of
+ * elasticity_iso, formulations/formulation_elasticity_iso.py:64-85, run by call_after_solve,
+ * include/formulation/formulation.h:1867-1875): per element, at var_inter = 0.5, out[13 e + k] =
+ * epsilon (k 0..5, tensor shear, 11 22 33 12 13 23), sigma (k 6..11), tr epsilon (k 12).
+ * u: ndof doubles (host), or NULL for the current result. */
+int lmtg_element_fields(lmtg_ctx *ctx, const double *u, double *out);
+
 /* Sizes of the current problem. */
 int lmtg_get_sizes(lmtg_ctx *ctx, uint64_t *nn, uint64_t *ne, uint64_t *ndof, uint64_t *nnz_blocks);
 

@@ -55,6 +55,7 @@ _SIGS = {
     "lmtg_solve_system": (_i, [_vp, _i, _i, _d, _i, _d, ctypes.POINTER(SolveStats)]),
     "lmtg_solve": (_i, [_vp, _i, _i, _d, _i, _d, ctypes.POINTER(SolveStats)]),
     "lmtg_get_result": (_i, [_vp, _vp]),
+    "lmtg_element_fields": (_i, [_vp, _vp, _vp]),
     "lmtg_set_result": (_i, [_vp, _vp]),
     "lmtg_spmv": (_i, [_vp, _i, _vp, _vp]),
     "lmtg_get_sizes": (_i, [_vp, _vp, _vp, _vp, _vp]),

@@ -209,6 +209,26 @@ int lmtg_get_result(lmtg_ctx *c, double *u) {
     });
 }
 
+int lmtg_element_fields(lmtg_ctx *c, const double *u, double *out) {
+    return guard2(c, [&] {
+        LMTG_CHECK(c->allocated && c->nnu == 3, LMTG_ERR_STATE, "elasticity allocate_matrices first");
+        LMTG_CHECK(c->E.p, LMTG_ERR_STATE, "material_set first");
+        LMTG_CHECK(out, LMTG_ERR_ARG, "null output");
+        DBuf<double> ud, od;
+        const double *up = c->u.p;
+        if (u) {
+            ud.alloc(c->n);
+            LMTG_CUDA(cudaMemcpyAsync(ud.p, u, c->n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+            up = ud.p;
+        }
+        od.alloc(13 * c->ne);
+        launch_elem_fields(c, up, od.p);
+        LMTG_CUDA(cudaMemcpyAsync(out, od.p, 13 * c->ne * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        LMTG_CUDA(cudaStreamSynchronize(c->stream));
+        return LMTG_OK;
+    });
+}
+
 int lmtg_set_result(lmtg_ctx *c, const double *u) {
     return guard2(c, [&] {
         LMTG_CHECK(c->allocated && u, LMTG_ERR_STATE, "allocate_matrices first");

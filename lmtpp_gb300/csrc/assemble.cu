@@ -18,61 +18,60 @@
 
 namespace lmtg {
 
+// One warp per node row, one lane per block of the row: the lane walks its block's gather list
+// once, sums the 9 entries of every contribution (transposed when the element pair is (b,a)),
+// then writes component v of its block at kidx(rb, deg, b, v) -- 9 coalesced stores per row.
 template <class TS, bool kW64, bool kW32>
-__global__ void k_assemble(const uint32_t *__restrict__ bptr, uint64_t nn,
-                           const uint32_t *__restrict__ gptr, const uint32_t *__restrict__ gsrc,
-                           const TS *__restrict__ Ke, uint64_t nvals, double *__restrict__ K64,
-                           float *__restrict__ K32) {
-    for (uint64_t idx = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; idx < nvals;
-         idx += (uint64_t)gridDim.x * blockDim.x) {
-        // output position -> (row, component, block) of the planar row layout
-        const uint64_t bi = idx / 9;  // some block of the row that contains idx
-        uint64_t lo = 0, hi = nn;     // row I with bptr[I] <= bi < bptr[I+1]
-        while (hi - lo > 1) {
-            const uint64_t mid = (lo + hi) >> 1;
-            if (__ldg(bptr + mid) <= bi) lo = mid;
-            else hi = mid;
+__global__ void __launch_bounds__(256)
+    k_assemble(const uint32_t *__restrict__ bptr, uint64_t nn, const uint32_t *__restrict__ gptr,
+               const uint32_t *__restrict__ gsrc, const TS *__restrict__ Ke, double *__restrict__ K64,
+               float *__restrict__ K32) {
+    typedef typename std::conditional<sizeof(TS) == 8, double, float>::type Acc;
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t I = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; I < nn; I += nw) {
+        const uint32_t rb = __ldg(bptr + I), deg = __ldg(bptr + I + 1) - rb;
+        for (uint32_t b = lane; b < deg; b += 32) {
+            const uint32_t blk = rb + b, g0 = __ldg(gptr + blk), g1 = __ldg(gptr + blk + 1);
+            Acc s[9];
+#pragma unroll
+            for (int v = 0; v < 9; ++v) s[v] = (Acc)0;
+            for (uint32_t g = g0; g < g1; ++g) {
+                const uint32_t src = __ldg(gsrc + g);
+                const TS *e = Ke + (uint64_t)(src >> 1) * 9;
+                TS m[9];
+#pragma unroll
+                for (int v = 0; v < 9; ++v) m[v] = __ldg(e + v);
+                const bool tr = (src & 1u) != 0;
+#pragma unroll
+                for (int v = 0; v < 9; ++v) s[v] += (Acc)(tr ? m[(v % 3) * 3 + v / 3] : m[v]);
+            }
+#pragma unroll
+            for (int v = 0; v < 9; ++v) {
+                const uint64_t idx = kidx(rb, deg, b, v);
+                if (kW64) K64[idx] = (double)s[v];
+                if (kW32) K32[idx] = (float)s[v];
+            }
         }
-        const uint32_t rb = __ldg(bptr + lo), deg = __ldg(bptr + lo + 1) - rb;
-        const uint64_t off = idx - 9ull * rb;
-        const int v = (int)(off / deg);
-        const uint64_t blk = rb + (off - (uint64_t)v * deg);
-        const int vt = (v % 3) * 3 + v / 3;  // transposed position
-        const uint32_t g0 = gptr[blk], g1 = gptr[blk + 1];
-        typedef typename std::conditional<sizeof(TS) == 8, double, float>::type Acc;
-        Acc s = 0;
-        for (uint32_t g = g0; g < g1; ++g) {
-            const uint32_t src = __ldg(gsrc + g);
-            s += (Acc)Ke[(uint64_t)(src >> 1) * 9 + ((src & 1u) ? vt : v)];
-        }
-        if (kW64) K64[idx] = (double)s;
-        if (kW32) K32[idx] = (float)s;
     }
 }
 
 void assemble_matrix(lmtg_ctx *c, bool from64, bool want64, bool want32) {
-    const uint64_t nvals = c->nnzb * 9;
     const int T = 256;
-    const int grid = grid_for(c, nvals, T, 8);
+    const int grid = grid_for(c, c->nn * 32, T, 8);
     if (from64) {
         if (want64 && want32)
-            k_assemble<double, true, true><<<grid, T, 0, c->stream>>>(c->bptr.p, c->nn, c->gptr.p,
-                                                                      c->gsrc.p, c->Ke64.p, nvals,
-                                                                      c->K64.p, c->K32.p);
+            k_assemble<double, true, true><<<grid, T, 0, c->stream>>>(c->bptr.p, c->nn, c->gptr.p, c->gsrc.p,
+                                                                      c->Ke64.p, c->K64.p, c->K32.p);
         else if (want64)
-            k_assemble<double, true, false><<<grid, T, 0, c->stream>>>(c->bptr.p, c->nn, c->gptr.p,
-                                                                       c->gsrc.p,
-                                                                       c->Ke64.p, nvals, c->K64.p,
-                                                                       nullptr);
+            k_assemble<double, true, false><<<grid, T, 0, c->stream>>>(c->bptr.p, c->nn, c->gptr.p, c->gsrc.p,
+                                                                       c->Ke64.p, c->K64.p, nullptr);
         else
-            k_assemble<double, false, true><<<grid, T, 0, c->stream>>>(c->bptr.p, c->nn, c->gptr.p,
-                                                                       c->gsrc.p,
-                                                                       c->Ke64.p, nvals, nullptr,
-                                                                       c->K32.p);
+            k_assemble<double, false, true><<<grid, T, 0, c->stream>>>(c->bptr.p, c->nn, c->gptr.p, c->gsrc.p,
+                                                                       c->Ke64.p, nullptr, c->K32.p);
     } else {
-        k_assemble<float, false, true><<<grid, T, 0, c->stream>>>(c->bptr.p, c->nn, c->gptr.p,
-                                                                  c->gsrc.p, c->Ke32.p,
-                                                                  nvals, nullptr, c->K32.p);
+        k_assemble<float, false, true><<<grid, T, 0, c->stream>>>(c->bptr.p, c->nn, c->gptr.p, c->gsrc.p,
+                                                                  c->Ke32.p, nullptr, c->K32.p);
     }
     LMTG_CUDA(cudaGetLastError());
     c->launches += 1;

@@ -278,9 +278,10 @@ __global__ void __launch_bounds__(kBThreads)
 }
 
 // Lane <-> (node, rhs) of a warp tile: the rhs is lane & 3 for the whole kernel.
+// The pair (system, rhs) of a lane is fixed within a tile, so per-pair flags and coefficients
+// are read once per tile, and the node loop is unrolled to keep several nodes' loads in flight.
 #define BTILE_PAIRS(t)                                                                      \
-    for (uint32_t I = (t).row0 + ((threadIdx.x & 31) >> 2), r = threadIdx.x & 3; I < (t).row1; \
-         I += 8)
+    _Pragma("unroll 4") for (uint32_t I = (t).row0 + ((threadIdx.x & 31) >> 2); I < (t).row1; I += 8)
 
 // p = z + beta p (beta = 0: p = z) for the running pairs.
 template <class T>
@@ -289,10 +290,10 @@ __global__ void __launch_bounds__(kBThreads) k_b_dir(BDev B, const T *__restrict
     for (uint32_t tile = warp_id(); tile < B.ntiles; tile += warp_count()) {
         const BTile t = B.tiles[tile];
         if (B.sys_done[t.sys]) continue;
+        const uint32_t r = threadIdx.x & 3, k = kBR * t.sys + r;
+        if (B.done[k]) continue;
+        const T beta = pair_coef<T>(B.beta, B.beta32, k);
         BTILE_PAIRS(t) {
-            const uint32_t k = kBR * t.sys + r;
-            if (B.done[k]) continue;
-            const T beta = pair_coef<T>(B.beta, B.beta32, k);
             const uint64_t i = (uint64_t)kBV * I + 3 * r;
 #pragma unroll
             for (int c = 0; c < 3; ++c) p[i + c] = beta != (T)0 ? fma(beta, p[i + c], z[i + c]) : z[i + c];
@@ -332,10 +333,10 @@ __global__ void __launch_bounds__(kBThreads)
         const BTile t = B.tiles[tile];
         if (B.sys_done[t.sys]) continue;  // set only after all of the system's tiles are done
         T acc0 = (T)0, acc1 = (T)0;       // rz, rr
-        BTILE_PAIRS(t) {
-            const uint32_t k = kBR * t.sys + r;
-            if (B.done[k]) continue;
-            const T alpha = pair_coef<T>(B.alpha, B.alpha32, k);
+        const uint32_t r = threadIdx.x & 3, kp = kBR * t.sys + r;
+        const bool run = !B.done[kp];
+        const T alpha = pair_coef<T>(B.alpha, B.alpha32, kp);
+        if (run) BTILE_PAIRS(t) {
             const uint64_t i = (uint64_t)kBV * I + 3 * r;
             T rr3[3], zz[3];
 #pragma unroll
@@ -391,6 +392,7 @@ __global__ void __launch_bounds__(kBThreads)
     for (uint32_t tile = warp_id(); tile < B.ntiles; tile += warp_count()) {
         const BTile t = B.tiles[tile];
         T acc0 = (T)0, acc1 = (T)0;
+        const uint32_t r = threadIdx.x & 3;
         BTILE_PAIRS(t) {
             const uint64_t i = (uint64_t)kBV * I + 3 * r;
             T rr3[3] = {rv_[i], rv_[i + 1], rv_[i + 2]}, zz[3];
@@ -439,6 +441,7 @@ __global__ void __launch_bounds__(kBThreads) k_b_norm2(BDev B, const double *__r
     for (uint32_t tile = warp_id(); tile < B.ntiles; tile += warp_count()) {
         const BTile t = B.tiles[tile];
         double acc = 0.0;
+        const uint32_t r = threadIdx.x & 3;
         BTILE_PAIRS(t) {
             const uint64_t i = (uint64_t)kBV * I + 3 * r;
 #pragma unroll
@@ -455,9 +458,10 @@ __global__ void __launch_bounds__(kBThreads) k_b_norm2(BDev B, const double *__r
 __global__ void k_b_scale(BDev B, const double *__restrict__ r64, float *__restrict__ r32, float *__restrict__ d32) {
     for (uint32_t tile = warp_id(); tile < B.ntiles; tile += warp_count()) {
         const BTile t = B.tiles[tile];
+        const uint32_t r = threadIdx.x & 3;
+        const double s = B.scale[kBR * t.sys + r];
+        const double inv = s > 0.0 ? 1.0 / s : 0.0;
         BTILE_PAIRS(t) {
-            const double s = B.scale[kBR * t.sys + r];
-            const double inv = s > 0.0 ? 1.0 / s : 0.0;
             const uint64_t i = (uint64_t)kBV * I + 3 * r;
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
@@ -472,9 +476,10 @@ __global__ void k_b_scale(BDev B, const double *__restrict__ r64, float *__restr
 __global__ void k_b_axpy(BDev B, double *__restrict__ x, const float *__restrict__ d32) {
     for (uint32_t tile = warp_id(); tile < B.ntiles; tile += warp_count()) {
         const BTile t = B.tiles[tile];
+        const uint32_t r = threadIdx.x & 3;
+        const double s = B.scale[kBR * t.sys + r];
+        if (s == 0.0) continue;
         BTILE_PAIRS(t) {
-            const double s = B.scale[kBR * t.sys + r];
-            if (s == 0.0) continue;
             const uint64_t i = (uint64_t)kBV * I + 3 * r;
 #pragma unroll
             for (int c = 0; c < 3; ++c) x[i + c] = fma(s, (double)d32[i + c], x[i + c]);

@@ -324,7 +324,10 @@ __global__ void __launch_bounds__(kRowThreads)
     }
     const T t[1] = {acc};
     double out[1];
-    if (grid_reduce_t<1, 0u>(t, partials, &S->cnt_a, out) && threadIdx.x == 0) S->pq = out[0];
+    if (grid_reduce_t<1, 0u>(t, partials, &S->cnt_a, out) && threadIdx.x == 0) {
+        S->pq = out[0];
+        S->alpha = S->rz / (out[0] + (out[0] == 0.0 ? 1.0 : 0.0));  // once, not per thread
+    }
 }
 
 template <class T>
@@ -334,7 +337,7 @@ __global__ void k_pcg_update_s(T *__restrict__ x, T *__restrict__ r, T *__restri
                                double *partials) {
     if (*(volatile int *)&S->done) return;
     const double pq = S->pq;
-    const T alpha = (T)(S->rz / (pq + (pq == 0.0 ? 1.0 : 0.0)));
+    const T alpha = (T)S->alpha;
     T t[2] = {(T)0, (T)0};
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
          i += (uint64_t)gridDim.x * blockDim.x) {

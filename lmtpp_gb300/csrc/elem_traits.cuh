@@ -23,6 +23,11 @@ struct Hexa8 {
         const T x = (g == 1 || g == 2 || g == 5 || g == 6) ? gb : ga;
         const T y = (g == 2 || g == 3 || g == 6 || g == 7) ? gb : ga;
         const T z = (g >= 4) ? gb : ga;
+        dN_at(x, y, z, d);
+    }
+    // derivatives at the reference point (x, y, z)
+    template <class T>
+    __device__ static void dN_at(T x, T y, T z, T (&d)[8][3]) {
         const T mx = 1 - x, my = 1 - y, mz = 1 - z;
         d[0][0] = -my * mz; d[0][1] = -mx * mz; d[0][2] = -mx * my;
         d[1][0] = my * mz;  d[1][1] = -x * mz;  d[1][2] = -x * my;
@@ -43,6 +48,11 @@ struct Tetra10 {
     __device__ static void dN(int g, T (&d)[10][3]) {
         const T ta = (T)0.1381966011250105, tb = (T)0.5854101966249685;
         const T x = g == 1 ? tb : ta, y = g == 2 ? tb : ta, z = g == 3 ? tb : ta;
+        dN_at(x, y, z, d);
+    }
+    // derivatives at the reference point (x, y, z)
+    template <class T>
+    __device__ static void dN_at(T x, T y, T z, T (&d)[10][3]) {
         const T X0 = 1 - x - y - z, X1 = x, X2 = y, X3 = z;
         // vertices: d(Xi (2 Xi - 1)) = (4 Xi - 1) dXi, dX0 = (-1,-1,-1)
         const T c0 = 4 * X0 - 1;

@@ -77,6 +77,7 @@ struct PcgScalars {
     double dx_inf;   // |alpha p|_inf of the last update
     double dx_2sq;   // |alpha p|_2^2 of the last update
     double beta;     // current beta (0 on the first iteration)
+    double alpha;    // rz / pq of the current iteration (set with pq)
     double crit;     // threshold of the stopping test
     int crit_kind;   // LMTG_CRIT_*
     int iter;        // iterations done
@@ -179,6 +180,9 @@ void copy_k64_to_k32(lmtg_ctx *c);
 
 // ---- adjoint (adjoint.cu) ----
 void launch_grad_E(lmtg_ctx *c, const double *a, const double *b, double *g);
+
+// ---- element fields after the solve (fields.cu) ----
+void launch_elem_fields(lmtg_ctx *c, const double *u, double *out);
 
 // ---- heat diffusion (diffusion.cu) ----
 void diff_setup(lmtg_ctx *c, const double *k, uint64_t nk, double rho_c, double dt, double theta,

@@ -132,13 +132,10 @@ static int run_pcg(lmtg_ctx *c, const T *K, const T *Dinv, const T *b, T *x, T *
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     LMTG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    for (int k = 0; k < kChunkPairs; ++k) {
-        k_pcg_spmv<T, VS><<<row_grid(c), kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, K, z, p0, p1, q,
-                                                              c->nn, c->scal.p, c->partials.p);
-        k_pcg_update<T, VS><<<node_grid(c), kRowThreads, 0, s>>>(x, r, z, p1, q, Dinv, c->nn,
-                                                                 c->scal.p, c->partials.p);
-        k_pcg_spmv<T, VS><<<row_grid(c), kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, K, z, p1, p0, q,
-                                                              c->nn, c->scal.p, c->partials.p);
+    for (int k = 0; k < 2 * kChunkPairs; ++k) {
+        k_pcg_dir<T, VS><<<node_grid(c), kRowThreads, 0, s>>>(z, p0, c->nn, c->scal.p);
+        k_pcg_spmv<T, VS><<<row_grid(c), kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, K, p0, q, c->nn,
+                                                              c->scal.p, c->partials.p);
         k_pcg_update<T, VS><<<node_grid(c), kRowThreads, 0, s>>>(x, r, z, p0, q, Dinv, c->nn,
                                                                  c->scal.p, c->partials.p);
     }
@@ -158,7 +155,7 @@ static int run_pcg(lmtg_ctx *c, const T *K, const T *Dinv, const T *b, T *x, T *
     if (c->h_scal[0].done) finished = true;
     for (int ch = 0; ch < max_chunks && !finished; ++ch) {
         ce = cudaGraphLaunch(exec, s);
-        c->launches += 4 * kChunkPairs;
+        c->launches += 6 * kChunkPairs;
         if (ce == cudaSuccess)
             ce = cudaMemcpyAsync(c->h_scal, c->scal.p, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s);
         if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
@@ -261,8 +258,7 @@ int solve_mixed(lmtg_ctx *c, double tol, int maxit, double timeout_s, lmtg_solve
             status = s2;
             break;
         }
-        // latest direction: iteration k writes p[(k+1) % 2]; keep it in pa for the next segment
-        if (it & 1) std::swap(pa, pb);
+        // the latest direction stays in pa for the next segment
         // the continued recurrence needs r.z from before the segment's last update:
         // beta_k = rz_{k+1} / rz_k, so rz_k = rz / beta of the final scalars
         rz_prev = c->h_scal[0].beta != 0.0 ? c->h_scal[0].rz / c->h_scal[0].beta : 0.0;
@@ -300,15 +296,16 @@ static void profile_pcg_t(lmtg_ctx *c, const T *K, const T *Dinv, const T *b, T 
     for (auto &e : ev) LMTG_CUDA(cudaEventCreate(&e));
     LMTG_CUDA(cudaEventRecord(ev[0], s));
     for (int k = 0; k < iters; ++k) {
-        T *po = (k & 1) ? p1 : p0, *pn = (k & 1) ? p0 : p1;
-        k_pcg_spmv<T, VS><<<row_grid(c), kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, K, z, po, pn, q,
-                                                              c->nn, c->scal.p, c->partials.p);
+        k_pcg_spmv<T, VS><<<row_grid(c), kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, K, p0, q, c->nn,
+                                                              c->scal.p, c->partials.p);
         LMTG_CUDA(cudaEventRecord(ev[2 * k + 1], s));
-        k_pcg_update<T, VS><<<node_grid(c), kRowThreads, 0, s>>>(x, r, z, pn, q, Dinv, c->nn, c->scal.p,
+        // the rest of the iteration: update, then the next direction
+        k_pcg_update<T, VS><<<node_grid(c), kRowThreads, 0, s>>>(x, r, z, p0, q, Dinv, c->nn, c->scal.p,
                                                              c->partials.p);
+        k_pcg_dir<T, VS><<<node_grid(c), kRowThreads, 0, s>>>(z, p0, c->nn, c->scal.p);
         LMTG_CUDA(cudaEventRecord(ev[2 * k + 2], s));
     }
-    c->launches += 2ull * iters;
+    c->launches += 3ull * iters;
     LMTG_CUDA(cudaGetLastError());
     LMTG_CUDA(cudaEventSynchronize(ev[2 * iters]));
     double a = 0, bsum = 0;

@@ -247,6 +247,14 @@ class Formulation:
         abi.check(self._lib.lmtg_get_result(self._ctx, abi.ptr(u)), self._ctx, "get_result")
         return u
 
+    def element_fields(self, u=None):
+        """call_after_solve: per element (ne x 13) epsilon[6] (tensor shear, 11 22 33 12 13 23),
+        sigma[6] and tr(epsilon) at var_inter = 0.5, from u (default: the current result)."""
+        out = np.zeros((self.ne, 13))
+        uu = None if u is None else np.ascontiguousarray(u, dtype=np.float64)
+        abi.check(self._lib.lmtg_element_fields(self._ctx, abi.ptr(uu), abi.ptr(out)), self._ctx, "element_fields")
+        return {"epsilon": out[:, :6], "sigma": out[:, 6:12], "tr_epsilon": out[:, 12]}
+
     def set_result(self, u):
         u = np.ascontiguousarray(u, dtype=np.float64)
         abi.check(self._lib.lmtg_set_result(self._ctx, abi.ptr(u)), self._ctx, "set_result")

@@ -231,6 +231,53 @@ static double elast_gp(int npe, const double *xyz, const double (*dN)[3], double
     return det;
 }
 
+/* Element fields after the solve (apply_on_elements_after_solve,
+ * formulations/formulation_elasticity_iso.py:64-85): every var_inter is set to 0.5 -- the cube
+ * centre for Hexa8; for Tetra10 the same point (0.5, 0.5, 0.5), which the quadratic field
+ * extrapolates to -- then epsilon = grad_sym_col(dep) (tensor shear, order 11 22 33 12 13 23,
+ * include/codegen/__init__.py:23-42), tr_epsilon = e11 + e22 + e33 and sigma = Kglo epsilon with
+ * Kglo the inverse compliance of hooke_isotrope (formal_lf/material_help.py:116-134).
+ * out: ne x 13 = epsilon[6], sigma[6], tr_epsilon.  nuv (per element) may be NULL. */
+int orc_elem_fields(int npe, uint64_t ne, const double *pos, const uint32_t *conn, const double *E,
+                    int E_per_elem, double nu0, const double *nuv, const double *u, double *out) {
+    if (npe != 8 && npe != 10) return 1;
+    const double xi[3] = {0.5, 0.5, 0.5};
+    double dN[10][3];
+    if (npe == 8) hexa8_dN(xi, (double (*)[3])dN);
+    else tetra10_dN(xi, (double (*)[3])dN);
+    for (uint64_t e = 0; e < ne; ++e) {
+        double J[3][3] = {{0}}, Ji[3][3], det, gu[3][3] = {{0}};
+        for (int a = 0; a < npe; ++a) {
+            const uint32_t n = conn[(uint64_t)npe * e + a];
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) J[i][j] += pos[3 * (uint64_t)n + i] * dN[a][j];
+        }
+        inv3(J, Ji, &det);
+        for (int a = 0; a < npe; ++a) {
+            const uint32_t n = conn[(uint64_t)npe * e + a];
+            double g[3];
+            for (int i = 0; i < 3; ++i) {
+                double s = 0;
+                for (int j = 0; j < 3; ++j) s += Ji[j][i] * dN[a][j];
+                g[i] = s;
+            }
+            for (int k = 0; k < 3; ++k)
+                for (int i = 0; i < 3; ++i) gu[k][i] += u[3 * (uint64_t)n + k] * g[i];  /* du_k/dx_i */
+        }
+        double eps[6] = {gu[0][0], gu[1][1], gu[2][2], 0.5 * (gu[0][1] + gu[1][0]),
+                         0.5 * (gu[0][2] + gu[2][0]), 0.5 * (gu[1][2] + gu[2][1])};
+        const double Ee = E[E_per_elem ? e : 0], nu = nuv ? nuv[e] : nu0;
+        double D[6][6];
+        hooke_energy_matrix(Ee, nu, D);
+        double *o = out + 13 * e;
+        for (int k = 0; k < 6; ++k) o[k] = eps[k];
+        for (int k = 0; k < 3; ++k) o[6 + k] = D[k][0] * eps[0] + D[k][1] * eps[1] + D[k][2] * eps[2];
+        for (int k = 3; k < 6; ++k) o[6 + k] = 0.5 * D[k][k] * eps[k];  /* Kglo shear = (1+nu)/E inverse */
+        o[12] = eps[0] + eps[1] + eps[2];
+    }
+    return 0;
+}
+
 double orc_hexa8_elast_gp(const double *xyz, double E, double nu, double w, const double *xi,
                           double *Ke) {
     double dN[8][3];

@@ -132,6 +132,10 @@ int orc_ic_pcg(uint64_t n, const uint64_t *rowptr, const uint32_t *col, const do
 int orc_cg(uint64_t n, const uint64_t *rowptr, const uint32_t *col, const double *val,
            const double *fac, int precond, const double *b, double *x, int crit_kind,
            double crit, int maxit);
+/* Element fields after the solve at var_inter = 0.5: out ne x 13 = epsilon[6] (tensor shear,
+ * 11 22 33 12 13 23), sigma[6], tr_epsilon (formulation_elasticity_iso.py:64-85). */
+int orc_elem_fields(int npe, uint64_t ne, const double *pos, const uint32_t *conn, const double *E,
+                    int E_per_elem, double nu0, const double *nuv, const double *u, double *out);
 
 #ifdef __cplusplus
 }

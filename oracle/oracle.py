@@ -146,6 +146,24 @@ def assemble_elast(pos, conn, E, nu, rowptr, col):
     return val
 
 
+def elem_fields(pos, conn, E, nu, u):
+    """Element fields after the solve (orc_elem_fields): ne x 13 = epsilon[6], sigma[6],
+    tr_epsilon at var_inter = 0.5.  E: 1 or ne values; nu: scalar or ne values."""
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    conn = np.ascontiguousarray(conn, dtype=np.uint32)
+    E = np.ascontiguousarray(np.atleast_1d(E), dtype=np.float64)
+    nuv = None if np.ndim(nu) == 0 else np.ascontiguousarray(nu, dtype=np.float64)
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    out = np.zeros((conn.shape[0], 13))
+    rc = lib().orc_elem_fields(ctypes.c_int(conn.shape[1]), ctypes.c_uint64(conn.shape[0]), _p(pos, _f64p),
+                               _p(conn, _u32p), _p(E, _f64p), ctypes.c_int(1 if E.shape[0] > 1 else 0),
+                               ctypes.c_double(0.0 if nuv is not None else float(nu)),
+                               None if nuv is None else _p(nuv, _f64p), _p(u, _f64p), _p(out, _f64p))
+    if rc:
+        raise RuntimeError("orc_elem_fields failed: %d" % rc)
+    return out
+
+
 def quad4_traction(faces, pos, t, F):
     faces = np.ascontiguousarray(faces, dtype=np.uint32)
     t = np.asarray(t, dtype=np.float64)

@@ -143,3 +143,18 @@ def test_oracle_diffusion_matches_reference_runtime(golden_dir):
     np.testing.assert_allclose(P["T0"], g["T0"], rtol=1e-15, atol=0)  # exp() of two libms
     T1 = O.diffusion_run(P, 1)[1]
     assert np.linalg.norm(T1 - g["T1"]) <= 1e-12 * np.linalg.norm(g["T1"])
+
+
+def test_oracle_element_fields_patch_test():
+    """A linear displacement gives its exact strain and Hooke stress in every element."""
+    G = np.array([[1e-3, 2e-3, -1e-3], [0.5e-3, -2e-3, 1e-3], [3e-3, 1e-3, 2e-3]])
+    eps = 0.5 * (G + G.T)
+    lam, mu = 2.1e5 * 0.3 / (1.3 * 0.4), 2.1e5 / 2.6
+    sig = lam * np.trace(eps) * np.eye(3) + 2 * mu * eps
+    idx = [(0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2)]
+    for make in (O.make_rect_hexa, O.make_rect_tetra10):
+        pos, conn = make(3)
+        out = O.elem_fields(pos, conn, 2.1e5, 0.3, (pos @ G.T).ravel())
+        assert np.abs(out[:, :6] - [eps[i] for i in idx]).max() <= 1e-15
+        assert np.abs(out[:, 6:12] - [sig[i] for i in idx]).max() <= 1e-10
+        assert np.abs(out[:, 12] - np.trace(G)).max() <= 1e-15
