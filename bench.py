@@ -331,9 +331,9 @@ def cpu_desc(s):
 
 
 # dram__bytes_read.sum + dram__bytes_write.sum / algorithmic bytes of one k_pcg_spmv<float>
-# launch, ncu capture of the Hexa8 64^3 case: (293.904 MB + 5.595 MB) over
+# launch, ncu capture of the Hexa8 64^3 case: (293.433 MB + 4.631 MB) over
 # spmv_bytes(274625, 7189057, 4) = 296.350 MB
-SPMV32_TRAFFIC_RATIO = (293.904384 + 5.595136) / 296.350284
+SPMV32_TRAFFIC_RATIO = (293.433088 + 4.630784) / 296.350284
 
 METRIC = "time-to-solution at 1e-10 rel. error vs FP64 oracle, mixed vs FP64 CG; asm GB/s"
 
@@ -503,14 +503,19 @@ def run_batch(args):
     materials).  All pairs solved to a 1e-10 FP64 relative residual, mixed and FP64."""
     import torch
     from lmtpp_gb300 import make_rect_hexa, x1_faces_hexa
-    from lmtpp_gb300.batch import BatchFormulation
+    from lmtpp_gb300.batch import BatchFormulation, shard
     rng = np.random.default_rng(SEED)
     sides = rng.integers(8, 33, args.nsys)
     E = rng.uniform(5e4, 3e5, args.nsys)
     nu = rng.uniform(0.2, 0.4, args.nsys)
+    # under torchrun the meshes are sharded over the ranks (independent systems: no collective)
+    rank, world, local, barrier, allmax = dist_setup(args.gpus)
+    m0, m1 = shard(3 * (sides + 1) ** 3, rank, world)
+    total_dofs = int(np.sum(3 * (sides.astype(np.int64) + 1) ** 3))
+    sides, E, nu = sides[m0:m1], E[m0:m1], nu[m0:m1]
     meshes = [make_rect_hexa((int(n) + 1,) * 3) for n in sides]
     t0 = time.perf_counter()
-    bf = BatchFormulation(meshes)
+    bf = BatchFormulation(meshes, device=local)
     bf.set_materials(E, nu)
     clamped = np.nonzero(bf.pos[:, 0] < 1e-6)[0]
     bf.add_constraints((3 * clamped[:, None] + np.arange(3)[None, :]).ravel(), 1e5)
@@ -524,25 +529,30 @@ def run_batch(args):
         bf.add_skin_traction(faces, t)
         bf.assemble(False, True)
         B[r] = bf.get_sollicitation()
-    B[3] = rng.standard_normal(bf.n)
+    # N(0,1) nodal load: the same generator after the materials (one rank); a per-rank stream
+    # when the meshes are sharded
+    B[3] = (rng if world == 1 else np.random.default_rng(SEED + 1 + rank)).standard_normal(bf.n)
     setup_s = time.perf_counter() - t0
     out = {"mode": "batch",
            "workload": "%d Hexa8 cubes, side ~ U{8..32} (seed %d), E ~ U[5e4,3e5], nu ~ U[0.2,0.4], "
                        "clamped x=0 (penalty 1e5), 4 RHS (+x/+y/+z unit traction on x=1, N(0,1) nodal)"
                        % (args.nsys, SEED),
-           "dofs": bf.n, "elements": bf.ne, "setup_s": setup_s, "tol": args.tol}
+           "dofs": total_dofs, "dofs_rank0": bf.n, "elements_rank0": bf.ne, "setup_s": setup_s,
+           "tol": args.tol}
     for mode in ("mixed", "fp64"):
         bf.solve_batch(B, mode=mode, tol=args.tol)  # warm-up: autotuner, buffers, caches
         torch.cuda.synchronize()
+        barrier()
         w0 = time.perf_counter()
         X, st, its = bf.solve_batch(B, mode=mode, tol=args.tol)
-        wall = time.perf_counter() - w0
+        wall = allmax(time.perf_counter() - w0)
+        st["device_ms"] = allmax(st["device_ms"])
         out["solve_ms_" + mode] = st["device_ms"]
         out["e2e_wall_ms_" + mode] = wall * 1e3
         out["max_pair_iters_" + mode] = int(its.max())
         out["segments_" + mode] = st["outer_iterations"]
         out["worst_rel_residual_" + mode] = st["rel_residual"]
-        out["dof_rhs_per_s_" + mode] = 4 * bf.n / (st["device_ms"] * 1e-3)
+        out["dof_rhs_per_s_" + mode] = 4 * total_dofs / (st["device_ms"] * 1e-3)  # whole job
         if mode == "mixed":
             big, small = int(np.argmax(sides)), int(np.argmin(sides))
             out["iters_side%d" % sides[big]] = its[big].tolist()
@@ -553,8 +563,11 @@ def run_batch(args):
                                                  for r in range(4)))
     out["autotuner"] = bf.batch_info()
     out["launches"] = bf.launch_count()
+    out["n_gpus"] = world
+    out["scaling"] = "strong"  # the 256 meshes are shared out over the ranks
     bf.close()
-    print(json.dumps(out), flush=True)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
 
 
 def main():

@@ -27,6 +27,20 @@ def concat_meshes(meshes):
     return pos, conn, node_off, elem_off
 
 
+def shard(costs, rank, world):
+    """Contiguous share of a batch for one of `world` replicas: the meshes [a, b) whose
+    cumulative cost (e.g. DOF count) falls in this rank's 1/world of the total.  Every mesh is
+    in exactly one share; no data crosses ranks (the systems are independent)."""
+    c = np.cumsum(np.asarray(costs, dtype=np.float64))
+    if c.size == 0:
+        return 0, 0
+    total = c[-1]
+    cuts = [0] + [int(np.searchsorted(c, total * k / world, side="left")) for k in range(1, world)] + [c.size]
+    for k in range(1, len(cuts)):  # keep the cuts non-decreasing
+        cuts[k] = max(cuts[k], cuts[k - 1])
+    return cuts[rank], cuts[rank + 1]
+
+
 class BatchFormulation(Formulation):
     """Many elasticity_iso formulations (independent meshes of one element type) in one context."""
 

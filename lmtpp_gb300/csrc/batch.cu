@@ -118,9 +118,9 @@ __device__ __forceinline__ T brow(const uint32_t *__restrict__ bcol, const T *__
         if (bl < deg) {
             T m[9];
 #pragma unroll
-            for (int k = 0; k < 9; ++k) m[k] = __ldg(K + kidx(rb, deg, bl, k));
+            for (int k = 0; k < 9; ++k) m[k] = __ldcs(K + kidx(rb, deg, bl, k));
             T xv[kBV];
-            Node12<T>::load(x, __ldg(bcol + rb + bl), xv);
+            Node12<T>::load(x, __ldcs(bcol + rb + bl), xv);
 #pragma unroll
             for (int r = 0; r < kBR; ++r)
                 block_fma(m, xv[3 * r], xv[3 * r + 1], xv[3 * r + 2], a[3 * r], a[3 * r + 1], a[3 * r + 2]);
@@ -143,8 +143,8 @@ __device__ __forceinline__ void row_load(const uint32_t *__restrict__ bptr, cons
     deg = __ldg(bptr + I + 1) - rb;
     const bool on = (uint32_t)lane < deg;
 #pragma unroll
-    for (int k = 0; k < 9; ++k) R.m[k] = on ? __ldg(K + kidx(rb, deg, lane, k)) : (T)0;
-    R.j = on ? __ldg(bcol + rb + lane) : 0u;
+    for (int k = 0; k < 9; ++k) R.m[k] = on ? __ldcs(K + kidx(rb, deg, lane, k)) : (T)0;
+    R.j = on ? __ldcs(bcol + rb + lane) : 0u;  // streamed once: keep L1 for the gathers
 }
 
 // Sum of the four products of a row whose blocks fit the warp (deg <= 32).

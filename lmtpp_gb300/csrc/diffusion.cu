@@ -206,8 +206,8 @@ __device__ __forceinline__ T csr_stream32(const uint32_t *__restrict__ rp, const
             if (k < nck) {
                 const uint32_t q = t0 + 32 * k + lane;
                 const bool on = q < e1;
-                cj[k] = on ? __ldg(col + q) : 0u;
-                kv[k] = on ? __ldg(K + q) : (T)0;
+                cj[k] = on ? __ldcs(col + q) : 0u;  // streamed once: keep L1 for the gathers
+                kv[k] = on ? __ldcs(K + q) : (T)0;
             }
         }
         T xv[kTileChunks];
