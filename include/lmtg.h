@@ -282,6 +282,23 @@ int lmtg_set_inner_reduction(lmtg_ctx *ctx, double inner_reduction);
  * u: ndof doubles (host), or NULL for the current result. */
 int lmtg_element_fields(lmtg_ctx *ctx, const double *u, double *out);
 
+/* Identification of zone moduli by Gauss-Newton (replaces FormulationFit::exec,
+ * include/formulation/FormulationFit.h:17-80, for the elastic_modulus parameter): E_e =
+ * p[zone_of_elem[e]] with nz (1..4) zones; u_exp the measured displacement (ndof), w its
+ * diagonal weight standing for exp_mat (NULL: 1), sens_val the weights of the
+ * sensitivity_after_fit sums (NULL: 1).  Each iteration assembles, solves u (mode
+ * LMTG_SOLVE_PCG_F64 or MIXED_IR, relative residual tol, maxit), solves the nz sensitivities
+ * dU_i = -K^-1 dK/dp_i u, forms M_ij = (w dU_i).dU_j and V_i = (w dU_i).(u_exp - u), adds
+ * levenberg_marq * max|diag M| to the diagonal and updates p += relaxation M^-1 V; it stops when
+ * every |dD_i| < conv or at iteration max_iter (counted from 0, the reference's 20).  p (nz) is
+ * updated in place; history (max|dD| per iteration) and residual_history ((w d).d per
+ * iteration) need max_iter + 1 doubles each (optional); sensitivity (nz, optional). */
+int lmtg_fit_zone_moduli(lmtg_ctx *ctx, uint32_t nz, const uint32_t *zone_of_elem, double *p,
+                         const double *u_exp, const double *w, const double *sens_val,
+                         double relaxation, double levenberg_marq, double conv, int max_iter,
+                         int mode, double tol, int maxit, double *history,
+                         double *residual_history, double *sensitivity, int *n_iter);
+
 /* Sizes of the current problem. */
 int lmtg_get_sizes(lmtg_ctx *ctx, uint64_t *nn, uint64_t *ne, uint64_t *ndof, uint64_t *nnz_blocks);
 

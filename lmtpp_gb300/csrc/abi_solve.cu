@@ -31,6 +31,10 @@ int guard2(lmtg_ctx *c, F &&f) {
     }
 }
 
+}  // namespace
+
+namespace lmtg {
+
 void do_assemble(lmtg_ctx *c, int flags) {
     LMTG_CHECK(c->allocated, LMTG_ERR_STATE, "allocate_matrices first");
     LMTG_CHECK(c->nnu == 3, LMTG_ERR_STATE, "elasticity call on a diffusion context");
@@ -60,7 +64,7 @@ void do_assemble(lmtg_ctx *c, int flags) {
     LMTG_CUDA(cudaStreamSynchronize(c->stream));
 }
 
-}  // namespace
+}  // namespace lmtg
 
 extern "C" {
 

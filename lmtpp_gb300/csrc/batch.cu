@@ -86,24 +86,6 @@ struct Node12<double> {
     }
 };
 
-// Reduce-scatter of 16 values over the warp: afterwards lane L holds the warp total of value
-// (L >> 1) & 15 (each value in two lanes); 16 shuffles instead of 16 x 5.
-template <class T>
-__device__ __forceinline__ T reduce_scatter16(T (&a)[16], int lane) {
-#pragma unroll
-    for (int s = 0; s < 4; ++s) {
-        const int h = 8 >> s, bit = 16 >> s;
-        const bool hi = (lane & bit) != 0;
-#pragma unroll
-        for (int i = 0; i < h; ++i) {
-            const T send = hi ? a[i] : a[i + h];
-            const T keep = hi ? a[i + h] : a[i];
-            a[i] = keep + __shfl_xor_sync(0xffffffffu, send, bit);
-        }
-    }
-    return a[0] + __shfl_xor_sync(0xffffffffu, a[0], 1);
-}
-
 // Row I of K times the four node vectors of x, any number of blocks: lane L (even, L < 24)
 // returns the value of index v = L >> 1 (rhs v / 3, component v % 3).
 template <class T>

@@ -176,6 +176,8 @@ void launch_elem_elast(lmtg_ctx *c, bool fp64);
 void assemble_matrix(lmtg_ctx *c, bool from64, bool want64, bool want32);
 void apply_penalty(lmtg_ctx *c, bool mat, bool vec);
 void build_block_jacobi(lmtg_ctx *c, bool want64, bool want32);
+// element kernel + assembly + penalty + preconditioner for LMTG_ASM_* flags (abi_solve.cu)
+void do_assemble(lmtg_ctx *c, int flags);
 void copy_k64_to_k32(lmtg_ctx *c);
 
 // ---- adjoint (adjoint.cu) ----

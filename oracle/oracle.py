@@ -344,3 +344,59 @@ def diffusion_run(P, nsteps, T0=None):
         T = skyline_solve(P["rowptr"], P["col"], P["A"], spmv(P["rowptr"], P["col"], P["B"], T))
         states.append(T.copy())
     return states
+
+
+# ---------------------------------------------------------------------------------------------
+# identification driver (include/formulation/FormulationFit.h)
+# ---------------------------------------------------------------------------------------------
+def fit_zone_moduli(pos, conn, zone, p0, nu, dofs, pen, F, u_exp, w=None, relaxation=1.0, lm=0.0,
+                    conv=1e-4, max_iter=20, sens_val=None):
+    """Gauss-Newton of FormulationFit::exec (include/formulation/FormulationFit.h:17-80) for the
+    zone moduli p (E_e = p[zone[e]]), with W = diag(w) standing for exp_mat:
+      assemble (penalty max|diag| recomputed, as assemble() does); u = K^-1 F;
+      dU_i = K^-1 (-dK/dp_i u) (the element part; assemble_vector_der_var);
+      M_ij = (W dU_i).dU_j, V_i = (W dU_i).(u_exp - u); a zero diagonal becomes 1;
+      M_ii += max|diag M| lm; dD = M^-1 V; p += relaxation dD;
+      stop when every |dD| < conv or at iteration max_iter (counted from 0);
+      sensitivity_i = sum_c |sens_val_c (M^-1 W dU)_ic|.
+    Direct solves (skyline Cholesky).  Returns dict(p, history, residual_history, sensitivity,
+    iterations)."""
+    zone = np.asarray(zone, dtype=np.int64)
+    p = np.array(p0, dtype=np.float64)
+    nz = p.shape[0]
+    nn = pos.shape[0]
+    n = 3 * nn
+    w = np.ones(n) if w is None else np.asarray(w, dtype=np.float64)
+    sv = np.ones(n) if sens_val is None else np.asarray(sens_val, dtype=np.float64)
+    rowptr, col = pattern_lower(nn, 3, conn)
+    ones = np.ones(dofs.shape[0])
+    zeros = np.zeros(dofs.shape[0])
+    # unit-modulus zone matrices (no penalty): dK/dp_i = K(1 + mask_i) - K(1), K being linear in E
+    # (an E of 0 has no compliance inverse)
+    K1 = assemble_elast(pos, conn, np.ones(conn.shape[0]), nu, rowptr, col)
+    Kz = [assemble_elast(pos, conn, 1.0 + (zone == i), nu, rowptr, col) - K1 for i in range(nz)]
+    hist, res_hist = [], []
+    it = 0
+    while True:
+        val = assemble_elast(pos, conn, p[zone], nu, rowptr, col)
+        Fc = np.array(F, dtype=np.float64)
+        penalty(rowptr, col, val, Fc, dofs, ones, zeros, pen)
+        u = skyline_solve(rowptr, col, val, Fc)
+        dU = np.stack([skyline_solve(rowptr, col, val, -spmv(rowptr, col, Kz[i], u)) for i in range(nz)])
+        d = u_exp - u
+        WdU = dU * w[None, :]
+        M = WdU @ dU.T
+        V = WdU @ d
+        res_hist.append(float(np.sum(w * d * d)))
+        if np.max(np.abs(np.diag(M))) == 0:
+            M[np.diag_indices(nz)] = 1.0
+        if lm:
+            M[np.diag_indices(nz)] += np.max(np.abs(np.diag(M))) * lm
+        Minv = np.linalg.inv(M)
+        dD = Minv @ V
+        hist.append(float(np.max(np.abs(dD))))
+        p += relaxation * dD
+        if np.all(np.abs(dD) < conv) or it == max_iter:
+            sens = np.sum(np.abs(sv[None, :] * (Minv @ WdU)), axis=1)
+            return dict(p=p, history=hist, residual_history=res_hist, sensitivity=sens, iterations=it + 1)
+        it += 1
