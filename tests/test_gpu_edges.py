@@ -1,0 +1,107 @@
+"""Edge cases of the GPU path: single-element meshes, zero loads, an unconstrained (singular)
+body, batches with one or three right-hand sides and a one-element mesh, API misuse of batches,
+a one-cell diffusion mesh and a one-zone fit."""
+import numpy as np
+import pytest
+
+from lmtpp_gb300 import Formulation, abi, make_rect_hexa, make_rect_tetra10, x1_faces
+from lmtpp_gb300.batch import BatchFormulation
+from lmtpp_gb300.diffusion import Diffusion, boundary_nodes, make_rect_triangle6
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def problem(P, **kw):
+    f = Formulation(P["pos"], P["conn"])
+    f.elastic_modulus = P["E"]
+    f.poisson_ratio = P["nu"]
+    f.add_constraints(P["dofs"], P["penalty"])
+    f.add_skin_traction(P["faces"], (1.0, 0.0, 0.0))
+    return f
+
+
+@pytest.mark.parametrize("elem", ["hexa", "tetra10"])
+@pytest.mark.parametrize("mode,tol", [("fp64", 1e-10), ("mixed", 1e-8)])
+def test_single_cube_matches_oracle(elem, mode, tol):
+    P = O.elasticity_problem(2, elem=elem)  # one cube: 1 Hexa8 or 6 Tetra10
+    x = O.skyline_solve(P["rowptr"], P["col"], P["val"], P["F"])
+    f = problem(P)
+    f.solve(1e-13 if mode == "fp64" else 1e-12, mode=mode)
+    u = f.get_result()
+    assert np.linalg.norm(u - x) <= tol * np.linalg.norm(x)
+    f.close()
+
+
+@pytest.mark.parametrize("mode", ["fp64", "mixed"])
+def test_zero_load_gives_zero_solution_at_once(mode):
+    P = O.elasticity_problem(4)
+    f = Formulation(P["pos"], P["conn"])
+    f.elastic_modulus = P["E"]
+    f.add_constraints(P["dofs"], P["penalty"])
+    st = f.solve(1e-10, mode=mode)
+    assert st["iterations"] == 0 and st["status"] == abi.OK
+    assert not np.any(f.get_result())
+    f.close()
+
+
+def test_unconstrained_body_stops_with_a_status():
+    """No constraint: K is singular (rigid-body modes) and an unbalanced traction has no
+    solution; the solver stops at its iteration cap with a status instead of running on."""
+    P = O.elasticity_problem(4)
+    f = Formulation(P["pos"], P["conn"])
+    f.elastic_modulus = P["E"]
+    f.add_skin_traction(P["faces"], (1.0, 0.0, 0.0))
+    with pytest.raises(abi.LmtgError) as ei:
+        f.solve(1e-10, mode="fp64", maxit=400)
+    assert ei.value.status in (abi.ERR_NOT_CONVERGED, abi.ERR_NAN)
+    f.close()
+
+
+@pytest.mark.parametrize("nrhs", [1, 3])
+def test_batch_with_one_element_mesh_and_fewer_rhs(nrhs):
+    sides = [1, 3, 2]
+    rng = np.random.default_rng(nrhs)
+    E = rng.uniform(5e4, 3e5, len(sides))
+    nu = rng.uniform(0.2, 0.4, len(sides))
+    probs = [O.elasticity_problem(s + 1, E=E[m], nu=nu[m], pen=1e5) for m, s in enumerate(sides)]
+    bf = BatchFormulation([(P["pos"], P["conn"]) for P in probs])
+    bf.set_materials(E, nu)
+    bf.add_constraints(np.concatenate([P["dofs"] + 3 * int(bf.node_off[m]) for m, P in enumerate(probs)]), 1e5)
+    bf.assemble(True, False, mixed=True)
+    B = rng.standard_normal((nrhs, bf.n))
+    X, st, its = bf.solve_batch(B, mode="mixed", tol=1e-12)
+    assert its.shape == (len(sides), nrhs)
+    for m, P in enumerate(probs):
+        d = bf.dofs(m)
+        for r in range(nrhs):
+            x = O.skyline_solve(P["rowptr"], P["col"], P["val"], B[r, d])
+            assert np.linalg.norm(X[r, d] - x) <= 1e-8 * np.linalg.norm(x)
+    bf.close()
+
+
+def test_batch_misuse_is_reported():
+    pos, conn = make_rect_hexa((3, 3, 3))
+    f = Formulation(pos, conn)
+    bad = np.array([0, 10, pos.shape[0]], dtype=np.uint64)  # node 10 is shared by elements of both ranges
+    assert f._lib.lmtg_batch_set(f._ctx, 2, abi.ptr(bad)) == abi.ERR_ARG
+    short = np.array([0, 5], dtype=np.uint64)  # does not end at nn
+    assert f._lib.lmtg_batch_set(f._ctx, 1, abi.ptr(short)) == abi.ERR_ARG
+    f.close()
+    bf = BatchFormulation([make_rect_hexa((3, 3, 3))])
+    bf.set_materials([1e5], [0.3])
+    with pytest.raises(abi.LmtgError) as ei:
+        bf.solve_batch(np.zeros((5, bf.n)))  # more than four right-hand sides
+    assert ei.value.status == abi.ERR_ARG
+    bf.close()
+
+
+def test_one_cell_diffusion_matches_oracle():
+    P = O.diffusion_problem(2, theta=0.5)
+    states = O.diffusion_run(P, 3)
+    d = Diffusion(P["pos"], P["conn"])
+    d.setup(1.0, rho_c=1.0, dt=1e-4, theta=0.5, dirichlet=boundary_nodes(P["pos"]), penalty=1e5)
+    d.set_state(P["T0"])
+    d.run(3, tol=1e-14)
+    assert np.linalg.norm(d.get_state() - states[-1]) <= 1e-10 * max(np.linalg.norm(states[-1]), 1e-300)
+    d.close()
