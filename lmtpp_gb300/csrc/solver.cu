@@ -203,7 +203,7 @@ int solve_pcg64(lmtg_ctx *c, int crit_kind, double tol, int maxit, double timeou
 // r = F - K64 u is recomputed in FP64 and becomes the new FP32 residual (rescaled), and the
 // search direction is kept (beta folded with the rescaling), so the Krylov recurrence is not
 // restarted.  A segment that fails to reduce the true residual restarts from p = z (a classic
-// iterative-refinement step).  Convergence is judged on the FP64 true residual only.
+// iterative-refinement step).  Convergence is decided on the FP64 true residual only.
 int solve_mixed(lmtg_ctx *c, double tol, int maxit, double timeout_s, lmtg_solve_stats *st,
                 const double *bvec, double *xvec) {
     const double *Fb = bvec ? bvec : c->F.p;
