@@ -113,7 +113,8 @@ int lmtg_material_set(lmtg_ctx *ctx, const double *E, uint64_t nE, double nu);
  * number of stored scalar entries of the lower triangle (the SparseLine nb_nz()). */
 int lmtg_allocate_matrices(lmtg_ctx *ctx, uint64_t *nnz_lower);
 
-/* Nodal loads f_nodal (n = 3*nn doubles), replacing the current nodal load vector. */
+/* Nodal loads f_nodal (n = 3*nn doubles).  They replace the whole load vector, skin tractions
+ * added before included; lmtg_add_skin_traction adds to it afterwards. */
 int lmtg_set_nodal_loads(lmtg_ctx *ctx, const double *F);
 /* Uniform traction f_surf on skin faces (Quad4 for Hexa8 meshes: nfaces*4 node ids; Triangle_6
  * for Tetra10 meshes: nfaces*6), accumulated into the load vector as consistent nodal loads (the
@@ -122,9 +123,12 @@ int lmtg_set_nodal_loads(lmtg_ctx *ctx, const double *F);
 int lmtg_add_skin_traction(lmtg_ctx *ctx, uint64_t nfaces, const uint32_t *faces,
                            const double traction[3]);
 
-/* Penalty constraints: add_constraint("coef*node[i].dep[d] - res", penalty) for linear
- * single-unknown constraints; assembled as in assemble_constraints (formulation.h:1028-1071):
- * K(j,j) += coef^2 * max|diag K| * penalty, F(j) += coef * max|diag K| * penalty * res. */
+/* Constraints add_constraint("coef*node[i].dep[d] - res", penalty) for linear single-unknown
+ * constraints; assembled as in assemble_constraints (formulation.h:1028-1071):
+ * K(j,j) += coef^2 * max|diag K| * penalty, F(j) += coef * max|diag K| * penalty * res.
+ * penalty == 0 is the reference's exact constraint (Lagrange rows, formulation.h:1072-1088),
+ * applied here by elimination: u_j = res / coef exactly (one exact constraint per DOF, coef != 0;
+ * needs the FP64 matrix assembly; not with the adjoint, the fit or batch solves). */
 int lmtg_set_constraints(lmtg_ctx *ctx, uint64_t nc, const uint32_t *dof, const double *coef,
                          const double *res, double penalty);
 

@@ -4,6 +4,7 @@
 // LMT++'s FormulationAncestor (include/formulation/formulation_ancestor.h:18-262):
 // allocate_matrices -> assemble -> solve_system / solve -> get_result.  Every entry point
 // catches internal errors and returns a status; nothing throws across the ABI.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -482,10 +483,17 @@ int lmtg_set_constraints(lmtg_ctx *c, uint64_t nc, const uint32_t *dof, const do
     return guard(c, [&] {
         LMTG_CHECK(c->n > 0, LMTG_ERR_STATE, "mesh_set first");
         LMTG_CHECK(nc == 0 || (dof && coef && res), LMTG_ERR_ARG, "null constraint arrays");
-        LMTG_CHECK(nc == 0 || penalty != 0.0, LMTG_ERR_UNSUPPORTED,
-                   "Lagrange-multiplier constraints (penalty == 0) are not supported");
-        for (uint64_t k = 0; k < nc; ++k)
+        for (uint64_t k = 0; k < nc; ++k) {
             LMTG_CHECK(dof[k] < c->n, LMTG_ERR_ARG, "constraint dof >= n");
+            // penalty 0: exact constraint coef u = res (the reference's Lagrange rows)
+            LMTG_CHECK(penalty != 0.0 || coef[k] != 0.0, LMTG_ERR_ARG, "exact constraint with coefficient 0");
+        }
+        if (penalty == 0.0 && nc > 1) {  // one exact constraint per DOF
+            std::vector<uint32_t> d(dof, dof + nc);
+            std::sort(d.begin(), d.end());
+            LMTG_CHECK(std::adjacent_find(d.begin(), d.end()) == d.end(), LMTG_ERR_ARG,
+                       "two exact constraints on one DOF");
+        }
         upload(c, c->cdof, dof, nc);
         upload(c, c->ccoef, coef, nc);
         upload(c, c->cres, res, nc);

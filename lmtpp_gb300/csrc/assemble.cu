@@ -137,9 +137,98 @@ __global__ void k_round_constrained(const uint32_t *__restrict__ bptr,
     }
 }
 
+// ---- exact constraints (penalty 0) ----
+// The reference adds Lagrange-multiplier rows for a zero penalty (formulation.h:1072-1088) and
+// needs its LDL solver for the indefinite system.  For constraints coef u_j = res on one
+// unknown each, the same solution follows from elimination, which keeps K SPD for the PCG:
+// u_bar_j = res / coef; F_k -= (K u_bar)_k; rows and columns j of K become zero but for the
+// diagonal; F_j = K_jj u_bar_j.
+__global__ void k_elim_values(const uint32_t *__restrict__ dof, const double *__restrict__ coef,
+                              const double *__restrict__ res, uint64_t nc, double *__restrict__ ubar,
+                              uint8_t *__restrict__ mask) {
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < nc; k += (uint64_t)gridDim.x * blockDim.x) {
+        ubar[dof[k]] = res[k] / coef[k];
+        mask[dof[k]] = 1;
+    }
+}
+
+// warp per node row, lane per block: zero the constrained rows and columns but the diagonal
+template <class T>
+__global__ void k_eliminate(const uint32_t *__restrict__ bptr, const uint32_t *__restrict__ bcol, uint64_t nn,
+                            const uint8_t *__restrict__ mask, T *__restrict__ K, float *__restrict__ K32) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t I = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; I < nn; I += nw) {
+        const uint32_t rb = bptr[I], deg = bptr[I + 1] - rb;
+        const bool mi[3] = {mask[3 * I] != 0, mask[3 * I + 1] != 0, mask[3 * I + 2] != 0};
+        for (uint32_t b = lane; b < deg; b += 32) {
+            const uint64_t J = bcol[rb + b];
+            const bool mj[3] = {mask[3 * J] != 0, mask[3 * J + 1] != 0, mask[3 * J + 2] != 0};
+#pragma unroll
+            for (int v = 0; v < 9; ++v) {
+                const int r = v / 3, cc = v % 3;
+                if ((mi[r] || mj[cc]) && !(J == I && r == cc)) {
+                    const uint64_t idx = kidx(rb, deg, b, v);
+                    if (K) K[idx] = (T)0;
+                    if (K32) K32[idx] = 0.0f;
+                }
+            }
+        }
+    }
+}
+
+__global__ void k_elim_rhs(const double *__restrict__ w, uint64_t n, double *__restrict__ F) {
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x)
+        F[k] -= w[k];
+}
+__global__ void k_elim_rhs_fix(const uint32_t *__restrict__ bptr, const uint32_t *__restrict__ bdiag,
+                               const double *__restrict__ K, const uint32_t *__restrict__ dof, uint64_t nc,
+                               const double *__restrict__ ubar, double *__restrict__ F) {
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < nc; k += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t j = dof[k], I = j / 3, rb = bptr[I];
+        const double kjj = K[kidx(rb, bptr[I + 1] - rb, bdiag[I] - rb, 4 * (j % 3))];
+        F[j] = kjj * ubar[j];
+    }
+}
+
+static void apply_elimination(lmtg_ctx *c, bool mat, bool vec) {
+    LMTG_CHECK(c->have64, LMTG_ERR_UNSUPPORTED, "exact constraints need the FP64 assembly");
+    cudaStream_t s = c->stream;
+    const int T = 256;
+    DBuf<double> ubar;
+    DBuf<uint8_t> mask;
+    ubar.alloc(c->n);
+    mask.alloc(c->n);
+    LMTG_CUDA(cudaMemsetAsync(ubar.p, 0, c->n * sizeof(double), s));
+    LMTG_CUDA(cudaMemsetAsync(mask.p, 0, c->n, s));
+    k_elim_values<<<grid_for(c, c->nc, T), T, 0, s>>>(c->cdof.p, c->ccoef.p, c->cres.p, c->nc, ubar.p, mask.p);
+    c->launches += 1;
+    if (mat) {
+        // coupling of the prescribed values, from the matrix before elimination
+        c->elim_w.alloc(c->n);
+        spmv64(c, ubar.p, c->elim_w.p);
+        k_eliminate<double><<<grid_for(c, c->nn * 32, T, 8), T, 0, s>>>(c->bptr.p, c->bcol.p, c->nn, mask.p,
+                                                                        c->K64.p, c->have32 ? c->K32.p : nullptr);
+        c->launches += 1;
+    }
+    if (vec) {
+        LMTG_CHECK(c->elim_w.p, LMTG_ERR_STATE, "exact constraints: assemble the matrix first");
+        k_elim_rhs<<<grid_for(c, c->n, T), T, 0, s>>>(c->elim_w.p, c->n, c->F.p);
+        k_elim_rhs_fix<<<grid_for(c, c->nc, T), T, 0, s>>>(c->bptr.p, c->bdiag.p, c->K64.p, c->cdof.p, c->nc,
+                                                           ubar.p, c->F.p);
+        c->launches += 2;
+    }
+    LMTG_CUDA(cudaGetLastError());
+    LMTG_CUDA(cudaStreamSynchronize(s));
+}
+
 // One penalty scale per system of a batch (nsys > 0), else one for the whole matrix.
 void apply_penalty(lmtg_ctx *c, bool mat, bool vec) {
     if (c->nc == 0) return;
+    if (c->penalty == 0.0) {
+        apply_elimination(c, mat, vec);
+        return;
+    }
     const uint32_t ns = c->nsys ? c->nsys : 1;
     const uint32_t *sys = c->nsys ? c->sys_of_node.p : nullptr;
     DBuf<unsigned long long> md;

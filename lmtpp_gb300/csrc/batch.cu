@@ -742,6 +742,7 @@ int batch_solve(lmtg_ctx *c, int mode, double tol, int maxit, double timeout_s, 
     batch_prepare(c);
     BatchState &S = *c->batch;
     LMTG_CHECK(S.nrhs > 0, LMTG_ERR_STATE, "lmtg_batch_set_rhs first");
+    LMTG_CHECK(c->penalty != 0.0 || c->nc == 0, LMTG_ERR_UNSUPPORTED, "batch solves with exact (penalty 0) constraints");
     batch_alloc_mode(c, mode);
     const auto t0 = std::chrono::steady_clock::now();
     cudaStream_t s = c->stream;

@@ -171,6 +171,7 @@ int fit_zone_moduli(lmtg_ctx *c, uint32_t nz, const uint32_t *zone_h, double *p,
                     int max_iter, int mode, double tol, int maxit, double *hist, double *res_hist,
                     double *sens, int *n_iter) {
     LMTG_CHECK(c->allocated && c->nnu == 3, LMTG_ERR_STATE, "elasticity allocate_matrices first");
+    LMTG_CHECK(c->penalty != 0.0 || c->nc == 0, LMTG_ERR_UNSUPPORTED, "the fit with exact (penalty 0) constraints");
     LMTG_CHECK(nz >= 1 && nz <= (uint32_t)kFitMaxZones, LMTG_ERR_ARG, "1..4 zones");
     LMTG_CHECK(zone_h && p && uexp_h && max_iter >= 0, LMTG_ERR_ARG, "zones, p and u_exp needed");
     LMTG_CHECK(mode == LMTG_SOLVE_PCG_F64 || mode == LMTG_SOLVE_MIXED_IR, LMTG_ERR_ARG, "unknown mode");

@@ -152,6 +152,7 @@ struct lmtg_ctx {
     lmtg::DBuf<double> ccoef, cres;
     double penalty = 0;
     double penalty_scale = 0;  // > 0: fixed max|diag| used by the penalty instead of recomputing it
+    lmtg::DBuf<double> elim_w;  // exact constraints: K u_bar of the last matrix assembly
 
     // solver workspace
     lmtg::DBuf<double> w64[6];

@@ -90,7 +90,8 @@ def x1_faces(pos, conn, x1=1.0, eps=1e-6):
 
 def x1_faces_hexa(pos, conn, x1=1.0, eps=1e-6):
     """Quad4 skin faces (Hexa child [1,2,6,5], formulations/element_Hexa.py:22-29) on x = x1."""
-    q = conn[:, [1, 2, 6, 5]]
+    cand = np.nonzero(pos[conn[:, 1], 0] > x1 - eps)[0]  # elements whose node 1 lies on the plane
+    q = conn[cand][:, [1, 2, 6, 5]]
     on = np.all(pos[q, 0] > x1 - eps, axis=1)
     return np.ascontiguousarray(q[on], dtype=np.uint32)
 
@@ -161,16 +162,18 @@ class Formulation:
         if node >= self.nn or d > 2:
             raise abi.LmtgError(abi.ERR_ARG, "constraint on a missing node/component")
         # Constraint::res = -(ex with unknowns set to 0) = v  (constraint.h:86)
-        self._constraints.append((3 * node + d, coef, val, float(penalty_value)))
+        self._constraints.append((np.array([3 * node + d], dtype=np.int64), np.array([coef]), np.array([val]),
+                                  float(penalty_value)))
         self._constraints_dirty = True
 
     def add_constraints(self, dofs, penalty_value, coefs=None, res=None):
         """Vectorised add_constraint for many 'node[i].dep[d]' constraints."""
-        dofs = np.asarray(dofs, dtype=np.int64)
-        coefs = np.ones(dofs.shape[0]) if coefs is None else np.asarray(coefs, dtype=np.float64)
-        res = np.zeros(dofs.shape[0]) if res is None else np.asarray(res, dtype=np.float64)
-        for k in range(dofs.shape[0]):
-            self._constraints.append((int(dofs[k]), float(coefs[k]), float(res[k]), float(penalty_value)))
+        dofs = np.asarray(dofs, dtype=np.int64).ravel()
+        coefs = np.ones(dofs.shape[0]) if coefs is None else np.asarray(coefs, dtype=np.float64).ravel()
+        res = np.zeros(dofs.shape[0]) if res is None else np.asarray(res, dtype=np.float64).ravel()
+        if dofs.size and (dofs.min() < 0 or dofs.max() >= self.n):
+            raise abi.LmtgError(abi.ERR_ARG, "constraint on a missing DOF")
+        self._constraints.append((dofs, coefs, res, float(penalty_value)))
         self._constraints_dirty = True
 
     def _sync_constraints(self):
@@ -179,9 +182,9 @@ class Formulation:
         pens = {c[3] for c in self._constraints}
         if len(pens) > 1:
             raise abi.LmtgError(abi.ERR_UNSUPPORTED, "one penalty value per formulation")
-        dof = np.ascontiguousarray([c[0] for c in self._constraints], dtype=np.uint32)
-        coef = np.ascontiguousarray([c[1] for c in self._constraints], dtype=np.float64)
-        res = np.ascontiguousarray([c[2] for c in self._constraints], dtype=np.float64)
+        cat = (lambda k, t: np.ascontiguousarray(np.concatenate([c[k] for c in self._constraints]), dtype=t)
+               if self._constraints else np.zeros(0, dtype=t))
+        dof, coef, res = cat(0, np.uint32), cat(1, np.float64), cat(2, np.float64)
         pen = pens.pop() if pens else 0.0
         abi.check(self._lib.lmtg_set_constraints(self._ctx, dof.shape[0], abi.ptr(dof), abi.ptr(coef),
                                                  abi.ptr(res), pen), self._ctx, "set_constraints")

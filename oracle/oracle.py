@@ -400,3 +400,24 @@ def fit_zone_moduli(pos, conn, zone, p0, nu, dofs, pen, F, u_exp, w=None, relaxa
             sens = np.sum(np.abs(sv[None, :] * (Minv @ WdU)), axis=1)
             return dict(p=p, history=hist, residual_history=res_hist, sensitivity=sens, iterations=it + 1)
         it += 1
+
+
+def eliminate(rowptr, col, val, F, dofs, coef, res):
+    """Exact single-unknown constraints coef u_j = res (the reference's Lagrange rows for a zero
+    penalty, include/formulation/formulation.h:1072-1088) by elimination on the lower CSR, in
+    place: F_k -= (K u_bar)_k, rows and columns j zeroed but the diagonal, F_j = K_jj u_bar_j.
+    The solution of the modified SPD system is the Lagrange solution."""
+    n = rowptr.shape[0] - 1
+    ubar = np.zeros(n)
+    dofs = np.asarray(dofs, dtype=np.int64)
+    ubar[dofs] = np.asarray(res, dtype=np.float64) / np.asarray(coef, dtype=np.float64)
+    F -= spmv(rowptr, col, val, ubar)
+    mask = np.zeros(n, bool)
+    mask[dofs] = True
+    rows = np.repeat(np.arange(n), np.diff(rowptr.astype(np.int64)))
+    cols = col.astype(np.int64)
+    kill = (mask[rows] | mask[cols]) & (rows != cols)
+    val[kill] = 0.0
+    diag = rowptr[1:].astype(np.int64) - 1  # the diagonal is last in each lower row
+    F[dofs] = val[diag[dofs]] * ubar[dofs]
+    return ubar

@@ -105,3 +105,56 @@ def test_one_cell_diffusion_matches_oracle():
     d.run(3, tol=1e-14)
     assert np.linalg.norm(d.get_state() - states[-1]) <= 1e-10 * max(np.linalg.norm(states[-1]), 1e-300)
     d.close()
+
+
+@pytest.mark.parametrize("mode,tol", [("fp64", 1e-10), ("mixed", 1e-8)])
+def test_exact_constraints_by_elimination_match_oracle(mode, tol):
+    """penalty 0 (the reference's Lagrange rows): u_j = res / coef exactly, the rest as the
+    oracle's eliminated direct solve; a vector-only reassembly with new loads keeps it."""
+    P = O.elasticity_problem(5)
+    dofs = P["dofs"]
+    coef = np.where(dofs % 3 == 1, 2.0, 1.0)
+    res = np.where(dofs % 3 == 0, 1e-3, 0.0)
+    f = Formulation(P["pos"], P["conn"])
+    f.elastic_modulus = P["E"]
+    f.poisson_ratio = P["nu"]
+    f.add_constraints(dofs, 0.0, coefs=coef, res=res)
+    f.add_skin_traction(P["faces"], (1.0, 0.0, 0.0))
+    rowptr, col = O.pattern_lower(P["pos"].shape[0], 3, P["conn"])
+    val = O.assemble_elast(P["pos"], P["conn"], P["E"], P["nu"], rowptr, col)
+    F = np.zeros(P["F"].shape[0])
+    O.quad4_traction(P["faces"], P["pos"], (1.0, 0.0, 0.0), F)
+    O.eliminate(rowptr, col, val, F, dofs, coef, res)
+    x = O.skyline_solve(rowptr, col, val, F)
+    f.solve(1e-13 if mode == "fp64" else 1e-12, mode=mode)
+    u = f.get_result()
+    assert np.linalg.norm(u - x) <= tol * np.linalg.norm(x)
+    assert np.abs(u[dofs] - res / coef).max() <= 1e-12 * np.abs(res).max()
+    # the assembled matrix is the oracle's eliminated one
+    rp, cl, v = f.get_mat()
+    assert np.abs(v - val).max() <= 1e-12 * np.abs(val).max()
+    # new loads (set_nodal_loads replaces the whole load vector) through a vector-only assembly
+    rng = np.random.default_rng(1)
+    G = rng.standard_normal(F.shape[0])
+    f.set_nodal_loads(G)
+    f.assemble(False, True, mixed=(mode == "mixed"))
+    f.solve_system(1e-13 if mode == "fp64" else 1e-12, mode=mode)
+    F2 = G.copy()
+    val2 = O.assemble_elast(P["pos"], P["conn"], P["E"], P["nu"], rowptr, col)
+    O.eliminate(rowptr, col, val2, F2, dofs, coef, res)
+    x2 = O.skyline_solve(rowptr, col, val2, F2)
+    assert np.linalg.norm(f.get_result() - x2) <= tol * np.linalg.norm(x2)
+    f.close()
+
+
+def test_exact_constraints_refuse_the_adjoint():
+    P = O.elasticity_problem(3)
+    f = Formulation(P["pos"], P["conn"])
+    f.elastic_modulus = P["E"]
+    f.add_constraints(P["dofs"], 0.0)
+    f.add_skin_traction(P["faces"], (1.0, 0.0, 0.0))
+    f.solve(1e-12, mode="fp64")
+    with pytest.raises(abi.LmtgError) as ei:
+        f.adjoint_grad("compliance")
+    assert ei.value.status == abi.ERR_UNSUPPORTED
+    f.close()

@@ -158,3 +158,29 @@ def test_oracle_element_fields_patch_test():
         assert np.abs(out[:, :6] - [eps[i] for i in idx]).max() <= 1e-15
         assert np.abs(out[:, 6:12] - [sig[i] for i in idx]).max() <= 1e-10
         assert np.abs(out[:, 12] - np.trace(G)).max() <= 1e-15
+
+
+def test_oracle_elimination_equals_lagrange_solution():
+    """Exact constraints (penalty 0): the eliminated SPD system gives the solution of the
+    reference's Lagrange-multiplier system [[K, C^T], [C, 0]] (formulation.h:1072-1088)."""
+    import scipy.sparse.linalg as spla
+    pos, conn = O.make_rect_hexa(4)
+    rowptr, col = O.pattern_lower(pos.shape[0], 3, conn)
+    val = O.assemble_elast(pos, conn, 2.1e5, 0.3, rowptr, col)
+    n = 3 * pos.shape[0]
+    F = np.zeros(n)
+    P = O.elasticity_problem(4)
+    O.quad4_traction(P["faces"], pos, (1.0, 0.3, 0.0), F)
+    dofs = P["dofs"]
+    coef = np.where(dofs % 3 == 1, 2.0, 1.0)
+    res = np.where(dofs % 3 == 0, 1e-3, 0.0)
+    L = csr(rowptr, col, val, n)
+    K = (L + L.T - sp.diags(L.diagonal())).tocsc()
+    C = sp.csr_matrix((coef, (np.arange(dofs.size), dofs)), shape=(dofs.size, n))
+    S = sp.bmat([[K, C.T], [C, None]]).tocsc()
+    x = spla.spsolve(S, np.concatenate([F, res]))[:n]
+    val2, F2 = val.copy(), F.copy()
+    O.eliminate(rowptr, col, val2, F2, dofs, coef, res)
+    u = O.skyline_solve(rowptr, col, val2, F2)
+    assert np.linalg.norm(u - x) <= 1e-10 * np.linalg.norm(x)
+    assert np.abs(u[dofs] - res / coef).max() <= 1e-18
