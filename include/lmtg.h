@@ -129,6 +129,10 @@ int lmtg_add_skin_traction(lmtg_ctx *ctx, uint64_t nfaces, const uint32_t *faces
  * penalty == 0 is the reference's exact constraint (Lagrange rows, formulation.h:1072-1088),
  * applied here by elimination: u_j = res / coef exactly (one exact constraint per DOF, coef != 0;
  * needs the FP64 matrix assembly; not with the adjoint, the fit or batch solves). */
+/* The formulation's levenberg_marquadt term (formulation_ancestor.h:253, applied in
+ * assemble_constraints, formulation.h:1033-1034): K(i,i) += max|diag K| * lm at every matrix
+ * assembly, before the constraints; 0 by default. */
+int lmtg_set_levenberg_marquadt(lmtg_ctx *ctx, double lm);
 int lmtg_set_constraints(lmtg_ctx *ctx, uint64_t nc, const uint32_t *dof, const double *coef,
                          const double *res, double penalty);
 

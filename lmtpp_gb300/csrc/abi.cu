@@ -335,6 +335,15 @@ int lmtg_material_set_nu(lmtg_ctx *c, const double *nu, uint64_t n_nu) {
     });
 }
 
+int lmtg_set_levenberg_marquadt(lmtg_ctx *c, double lm) {
+    return guard(c, [&] {
+        LMTG_CHECK(std::isfinite(lm), LMTG_ERR_ARG, "levenberg_marquadt must be finite");
+        c->levenberg_marquadt = lm;
+        c->have64 = c->have32 = false;
+        return LMTG_OK;
+    });
+}
+
 int lmtg_batch_set(lmtg_ctx *c, uint32_t nsys, const uint64_t *node_off) {
     return guard(c, [&] {
         LMTG_CHECK(c->ne > 0 && c->nnu == 3, LMTG_ERR_STATE, "elasticity mesh_set first");

@@ -222,13 +222,32 @@ static void apply_elimination(lmtg_ctx *c, bool mat, bool vec) {
     LMTG_CUDA(cudaStreamSynchronize(s));
 }
 
-// One penalty scale per system of a batch (nsys > 0), else one for the whole matrix.
-void apply_penalty(lmtg_ctx *c, bool mat, bool vec) {
-    if (c->nc == 0) return;
-    if (c->penalty == 0.0) {
-        apply_elimination(c, mat, vec);
-        return;
+// K(i,i) += max|diag| * levenberg_marquadt on every diagonal entry (formulation.h:1033-1034),
+// with the max|diag| of the node's system
+template <class T>
+__global__ void k_add_diag(const uint32_t *__restrict__ bptr, const uint32_t *__restrict__ bdiag, T *K,
+                           float *K32, uint64_t nn, const uint32_t *__restrict__ sys,
+                           const unsigned long long *md_bits, double lm) {
+    for (uint64_t I = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; I < nn;
+         I += (uint64_t)gridDim.x * blockDim.x) {
+        const double md = __longlong_as_double((long long)md_bits[sys ? sys[I] : 0u]);
+        const uint32_t rb = bptr[I], deg = bptr[I + 1] - rb, d = bdiag[I] - rb;
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            const uint64_t idx = kidx(rb, deg, d, 4 * r);
+            K[idx] = (T)((double)K[idx] + md * lm);
+            if (K32) K32[idx] = (float)K[idx];
+        }
     }
+}
+
+// max|diag| (one per system of a batch, nsys > 0, else one for the whole matrix), the
+// Levenberg-Marquardt diagonal term, then the constraints: penalty terms, or elimination for a
+// zero penalty.
+void apply_penalty(lmtg_ctx *c, bool mat, bool vec) {
+    const bool lm = mat && c->levenberg_marquadt != 0.0;
+    if (c->nc == 0 && !lm) return;
+    const bool exact = c->nc > 0 && c->penalty == 0.0;
     const uint32_t ns = c->nsys ? c->nsys : 1;
     const uint32_t *sys = c->nsys ? c->sys_of_node.p : nullptr;
     DBuf<unsigned long long> md;
@@ -253,22 +272,38 @@ void apply_penalty(lmtg_ctx *c, bool mat, bool vec) {
         else
             k_max_diag<float><<<grid_for(c, c->nn, T), T, 0, c->stream>>>(c->bptr.p, c->bdiag.p, c->K32.p, c->nn,
                                                                           sys, md.p);
+        c->launches += 1;
     } else {
         // vector-only assembly reuses the max|diag| of the last matrix assembly
         upload_scales(c->nsys ? c->h_sys_max_diag : std::vector<double>(1, c->max_diag));
     }
-    const int g = grid_for(c, c->nc, T);
-    if (c->have64) {
-        k_penalty<double><<<g, T, 0, c->stream>>>(c->bptr.p, c->bdiag.p, c->K64.p, c->F.p, c->cdof.p, c->ccoef.p,
-                                                  c->cres.p, c->nc, c->penalty, sys, md.p, mat, vec);
-        if (mat && c->have32)
-            k_round_constrained<<<g, T, 0, c->stream>>>(c->bptr.p, c->bdiag.p, c->K64.p, c->K32.p, c->cdof.p, c->nc);
-    } else {
-        k_penalty<float><<<g, T, 0, c->stream>>>(c->bptr.p, c->bdiag.p, c->K32.p, c->F.p, c->cdof.p, c->ccoef.p,
-                                                 c->cres.p, c->nc, c->penalty, sys, md.p, mat, vec);
+    if (lm) {
+        if (c->have64)
+            k_add_diag<double><<<grid_for(c, c->nn, T), T, 0, c->stream>>>(
+                c->bptr.p, c->bdiag.p, c->K64.p, c->have32 ? c->K32.p : nullptr, c->nn, sys, md.p,
+                c->levenberg_marquadt);
+        else
+            k_add_diag<float><<<grid_for(c, c->nn, T), T, 0, c->stream>>>(c->bptr.p, c->bdiag.p, c->K32.p, nullptr,
+                                                                          c->nn, sys, md.p, c->levenberg_marquadt);
+        c->launches += 1;
+    }
+    if (exact) {
+        apply_elimination(c, mat, vec);
+    } else if (c->nc > 0) {
+        const int g = grid_for(c, c->nc, T);
+        if (c->have64) {
+            k_penalty<double><<<g, T, 0, c->stream>>>(c->bptr.p, c->bdiag.p, c->K64.p, c->F.p, c->cdof.p,
+                                                      c->ccoef.p, c->cres.p, c->nc, c->penalty, sys, md.p, mat, vec);
+            if (mat && c->have32)
+                k_round_constrained<<<g, T, 0, c->stream>>>(c->bptr.p, c->bdiag.p, c->K64.p, c->K32.p, c->cdof.p,
+                                                            c->nc);
+        } else {
+            k_penalty<float><<<g, T, 0, c->stream>>>(c->bptr.p, c->bdiag.p, c->K32.p, c->F.p, c->cdof.p, c->ccoef.p,
+                                                     c->cres.p, c->nc, c->penalty, sys, md.p, mat, vec);
+        }
+        c->launches += 1 + ((mat && c->have64 && c->have32) ? 1 : 0);
     }
     LMTG_CUDA(cudaGetLastError());
-    c->launches += ((mat && c->penalty_scale <= 0.0) ? 1 : 0) + 1 + ((mat && c->have64 && c->have32) ? 1 : 0);
     std::vector<unsigned long long> bits(ns);
     LMTG_CUDA(cudaMemcpyAsync(bits.data(), md.p, ns * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                               c->stream));

@@ -153,6 +153,7 @@ struct lmtg_ctx {
     double penalty = 0;
     double penalty_scale = 0;  // > 0: fixed max|diag| used by the penalty instead of recomputing it
     lmtg::DBuf<double> elim_w;  // exact constraints: K u_bar of the last matrix assembly
+    double levenberg_marquadt = 0;  // K(i,i) += max|diag| * levenberg_marquadt at assembly
 
     // solver workspace
     lmtg::DBuf<double> w64[6];

@@ -123,6 +123,10 @@ class Formulation:
         self._constraints_dirty = False
         self.allocated = False
         self.default_iterative_criterium = 1e-10
+        self.levenberg_marquadt = 0.0  # K += levenberg_marquadt * max|diag K| * Id at assembly
+        self.assume_constant_matrix = False  # solve() reassembles only the vector once K exists
+        self._lm_synced = 0.0
+        self._have_matrix = False
         self.nb_threads_assemble_matrix = 1  # accepted for API parity; the GPU grid replaces it
         self.last_stats = None
 
@@ -207,6 +211,7 @@ class Formulation:
                   "allocate_matrices")
         self.nnz_lower = nnz.value
         self.allocated = True
+        self._have_matrix = False
         self._material_dirty = True
         self._constraints_dirty = bool(self._constraints)
 
@@ -215,12 +220,18 @@ class Formulation:
             self.allocate_matrices()
         self._sync_material()
         self._sync_constraints()
+        if self.levenberg_marquadt != self._lm_synced:
+            abi.check(self._lib.lmtg_set_levenberg_marquadt(self._ctx, float(self.levenberg_marquadt)), self._ctx,
+                      "levenberg_marquadt")
+            self._lm_synced = self.levenberg_marquadt
         flags = 0
         if assemble_mat:
             flags |= abi.ASM_MAT32_NATIVE if native_fp32 else (abi.ASM_MAT64 | (abi.ASM_MAT32 if mixed else 0))
         if assemble_vec:
             flags |= abi.ASM_VEC
         abi.check(self._lib.lmtg_assemble(self._ctx, flags), self._ctx, "assemble")
+        if assemble_mat:
+            self._have_matrix = (mixed or native_fp32, True)
 
     def solve_system(self, iterative_criterium=None, mode="fp64", criterion="rel_residual",
                      maxit=100000, timeout_s=600.0):
@@ -240,8 +251,12 @@ class Formulation:
         return self.last_stats
 
     def solve(self, iterative_criterium=None, mode="fp64", **kw):
-        """solve(): assemble(mat, vec) then solve_system (formulation.h:1517-1568)."""
-        self.assemble(True, True, mixed=(mode == "mixed"))
+        """solve(): assemble(mat, vec) then solve_system (formulation.h:1517-1568); with
+        assume_constant_matrix, a matrix already assembled for this mode is kept."""
+        keep = (self.assume_constant_matrix and self._have_matrix
+                and (mode != "mixed" or self._have_matrix[0]) and not self._material_dirty
+                and not self._constraints_dirty and self.levenberg_marquadt == self._lm_synced)
+        self.assemble(not keep, True, mixed=(mode == "mixed"))
         return self.solve_system(iterative_criterium, mode=mode, **kw)
 
     # -- results ------------------------------------------------------------------------------

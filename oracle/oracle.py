@@ -421,3 +421,10 @@ def eliminate(rowptr, col, val, F, dofs, coef, res):
     diag = rowptr[1:].astype(np.int64) - 1  # the diagonal is last in each lower row
     F[dofs] = val[diag[dofs]] * ubar[dofs]
     return ubar
+
+
+def add_levenberg_marquadt(rowptr, val, max_diag, lm):
+    """K(i,i) += max|diag| * levenberg_marquadt (include/formulation/formulation.h:1033-1034),
+    on the lower CSR (the diagonal is last in each row)."""
+    diag = rowptr[1:].astype(np.int64) - 1
+    val[diag] += max_diag * lm

@@ -158,3 +158,29 @@ def test_exact_constraints_refuse_the_adjoint():
         f.adjoint_grad("compliance")
     assert ei.value.status == abi.ERR_UNSUPPORTED
     f.close()
+
+
+def test_levenberg_marquadt_term_and_constant_matrix():
+    P = O.elasticity_problem(4)
+    f = problem(P)
+    f.levenberg_marquadt = 1e-3
+    f.solve(1e-13, mode="fp64")
+    val = P["val"].copy()
+    O.add_levenberg_marquadt(P["rowptr"], val, P["max_diag"], 1e-3)
+    rp, cl, v = f.get_mat()
+    assert np.abs(v - val).max() <= 1e-12 * np.abs(val).max()
+    x = O.skyline_solve(P["rowptr"], P["col"], val, P["F"])
+    assert np.linalg.norm(f.get_result() - x) <= 1e-10 * np.linalg.norm(x)
+    # assume_constant_matrix: a second solve with new loads reassembles only the vector
+    f.assume_constant_matrix = True
+    n0 = f.launch_count()
+    G = np.random.default_rng(2).standard_normal(P["F"].shape[0])
+    f.set_nodal_loads(G)
+    f.set_result(np.zeros_like(G))
+    f.solve(1e-13, mode="fp64")
+    Fg = G.copy()
+    O.penalty(P["rowptr"], P["col"], val.copy(), Fg, P["dofs"], np.ones(P["dofs"].size), np.zeros(P["dofs"].size),
+              P["penalty"])
+    x2 = O.skyline_solve(P["rowptr"], P["col"], val, Fg)
+    assert np.linalg.norm(f.get_result() - x2) <= 1e-10 * np.linalg.norm(x2)
+    f.close()
