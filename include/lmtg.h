@@ -230,6 +230,16 @@ int lmtg_diff_mesh_set(lmtg_ctx *ctx, uint64_t nn, const double *pos, uint64_t n
  * Builds the pattern (first call), the element matrices and A, B. */
 int lmtg_diff_setup(lmtg_ctx *ctx, const double *k, uint64_t nk, double rho_c, double dt,
                     double theta, uint64_t nbnd, const uint32_t *bnd_nodes, double penalty);
+/* Constant sources of difftherm (formulations/formulation_difftherm.py:26-29): the volume source
+ * Q (nodal field, -Q te dV, applied as M Q) and the nodal source Qs (-Qs te dN); either may be
+ * NULL (nn doubles each).  Added to the right-hand side of every step. */
+int lmtg_diff_set_sources(lmtg_ctx *ctx, const double *Q, const double *Qs);
+/* Skin convection H (T - t0) te dS (formulation_difftherm.py:29) on nedges Bar_3 edges
+ * (3 nodes each: end, end, middle; formulations/element_Bar_3.py), H per edge (nH = nedges) or
+ * one value: adds theta H Ms to A, -(1 - theta) H Ms to B and H t0 int N ds to every step's
+ * right-hand side.  Call after lmtg_diff_setup (which clears it). */
+int lmtg_diff_set_convection(lmtg_ctx *ctx, uint64_t nedges, const uint32_t *edges, const double *H,
+                             uint64_t nH, double t0);
 /* Linear solver of every time step (and of the adjoint): LMTG_SOLVE_PCG_F64 (default, FP64
  * Jacobi-PCG) or LMTG_SOLVE_MIXED_IR (FP32 Jacobi-PCG with FP64 residual replacement). */
 int lmtg_diff_set_solver(lmtg_ctx *ctx, int mode);

@@ -65,6 +65,8 @@ _SIGS = {
     "lmtg_diff_mesh_set": (_i, [_vp, _u64, _vp, _u64, _vp]),
     "lmtg_diff_setup": (_i, [_vp, _vp, _u64, _d, _d, _d, _u64, _vp, _d]),
     "lmtg_diff_set_solver": (_i, [_vp, _i]),
+    "lmtg_diff_set_sources": (_i, [_vp, _vp, _vp]),
+    "lmtg_diff_set_convection": (_i, [_vp, _u64, _vp, _vp, _u64, _d]),
     "lmtg_diff_set_state": (_i, [_vp, _vp]),
     "lmtg_diff_get_state": (_i, [_vp, _vp]),
     "lmtg_diff_run": (_i, [_vp, _i, _d, _i, ctypes.POINTER(SolveStats)]),

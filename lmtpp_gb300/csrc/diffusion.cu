@@ -13,6 +13,7 @@
 //
 // One unknown per node: the node-block pattern of pattern.cu is the scalar CSR pattern; a row
 // holds ~9-19 entries, so the SpMV uses 8 lanes per row (4 rows per warp).
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -585,9 +586,19 @@ static void diff_rhs(lmtg_ctx *c, const double *T, double *rhs) {
     c->launches += 1;
 }
 
-// one step T_next = A^-1 B T (warm start from T)
+__global__ void k_add_vec(double *__restrict__ y, const double *__restrict__ a, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        y[i] += a[i];
+}
+
+// one step T_next = A^-1 (B T + s) (warm start from T); s = the constant source and convection
+// loads (lmtg_diff_set_sources / lmtg_diff_set_convection)
 static int diff_step(lmtg_ctx *c, const double *T, double *Tn, double tol, int maxit, int *it) {
     diff_rhs(c, T, c->F.p);
+    if (c->diff_load.p) {
+        k_add_vec<<<ngrid(c), kRowThreads, 0, c->stream>>>(c->F.p, c->diff_load.p, c->nn);
+        c->launches += 1;
+    }
     if (Tn != T)
         LMTG_CUDA(cudaMemcpyAsync(Tn, T, sizeof(double) * c->nn, cudaMemcpyDeviceToDevice, c->stream));
     return diff_pcg(c, c->F.p, Tn, tol, maxit, it);
@@ -598,6 +609,7 @@ void diff_setup(lmtg_ctx *c, const double *k, uint64_t nk, double rho_c, double 
     LMTG_CHECK(c->elem_type == LMTG_ELEM_TRIANGLE6, LMTG_ERR_STATE, "diffusion needs a Triangle_6 mesh");
     LMTG_CHECK(nk == 1 || nk == c->ne, LMTG_ERR_ARG, "conductivity needs 1 or ne values");
     LMTG_CHECK(rho_c > 0 && dt > 0 && theta >= 0 && theta <= 1, LMTG_ERR_ARG, "rho_c, dt > 0, theta in [0,1]");
+    c->h_diff_conv.clear();  // the matrices are rebuilt: convection has to be set again
     cudaStream_t s = c->stream;
     if (!c->allocated) {
         build_pattern(c);
@@ -659,6 +671,152 @@ void diff_setup(lmtg_ctx *c, const double *k, uint64_t nk, double rho_c, double 
     c->launches += 2;
     LMTG_CUDA(cudaStreamSynchronize(s));
     c->have64 = true;
+}
+
+// pos += val at the given entries of A (K64 and its FP32 copy) and pos -= val_b of B
+__global__ void k_add_entries(const uint64_t *__restrict__ at, const double *__restrict__ va,
+                              const double *__restrict__ vb, uint64_t m, double *A, float *A32, double *B) {
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < m; k += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t q = at[k];
+        A[q] += va[k];
+        A32[q] = (float)A[q];
+        B[q] += vb[k];
+    }
+}
+
+// the constant loads of every step: source + convection parts
+static void diff_update_load(lmtg_ctx *c) {
+    const uint64_t nn = c->nn;
+    const bool any = !c->h_diff_src.empty() || !c->h_diff_conv.empty();
+    if (!any) {
+        c->diff_load.release();
+        return;
+    }
+    std::vector<double> v(nn, 0.0);
+    for (uint64_t i = 0; i < nn && !c->h_diff_src.empty(); ++i) v[i] += c->h_diff_src[i];
+    for (uint64_t i = 0; i < nn && !c->h_diff_conv.empty(); ++i) v[i] += c->h_diff_conv[i];
+    upload_u32(c, c->diff_load, v.data(), nn);
+    LMTG_CUDA(cudaStreamSynchronize(c->stream));
+}
+
+// s = M Q + Qs: the volume source Q (nodal, -Q te dV) and the nodal source Qs (-Qs te dN) of
+// formulations/formulation_difftherm.py:26-29, M the consistent mass matrix
+void diff_set_sources(lmtg_ctx *c, const double *Q, const double *Qs) {
+    LMTG_CHECK(c->allocated && c->elem_type == LMTG_ELEM_TRIANGLE6, LMTG_ERR_STATE, "diff_setup first");
+    cudaStream_t s = c->stream;
+    const uint64_t nn = c->nn;
+    std::vector<double> src(nn, 0.0);
+    if (Q) {
+        DBuf<double> M1, M2, Mv, Bv, q, mq;
+        DBuf<float> M32;
+        M1.alloc(c->ne * kTriPairs);
+        M2.alloc(c->ne * kTriPairs);
+        Mv.alloc(c->nnzb);
+        Bv.alloc(c->nnzb);
+        M32.alloc(c->nnzb);
+        q.alloc(nn);
+        mq.alloc(nn);
+        const double one = 1.0;
+        DBuf<double> a1;
+        upload_u32(c, a1, &one, 1);
+        // conduction 0, dt 1: the element kernel's A part is the mass matrix
+        k_tri6_diff<<<grid_for(c, c->ne, 128, 16), 128, 0, s>>>(c->pos.p, c->conn.p, a1.p, 0, 0.0, 1.0, 1.0, c->ne,
+                                                                M1.p, M2.p);
+        k_assemble_s<<<grid_for(c, c->nnzb, 256, 8), 256, 0, s>>>(c->gptr.p, c->gsrc.p, M1.p, M2.p, c->nnzb, Mv.p,
+                                                                  Bv.p, M32.p);
+        LMTG_CUDA(cudaMemcpyAsync(q.p, Q, nn * 8, cudaMemcpyHostToDevice, s));
+        k_spmv_s<double><<<rgrid(c, k_spmv_s<double>), kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, Mv.p, q.p, mq.p,
+                                                                              nn);
+        LMTG_CUDA(cudaGetLastError());
+        c->launches += 3;
+        LMTG_CUDA(cudaMemcpyAsync(src.data(), mq.p, nn * 8, cudaMemcpyDeviceToHost, s));
+        LMTG_CUDA(cudaStreamSynchronize(s));
+    }
+    if (Qs)
+        for (uint64_t i = 0; i < nn; ++i) src[i] += Qs[i];
+    if (Q || Qs) c->h_diff_src = src;
+    else c->h_diff_src.clear();
+    diff_update_load(c);
+}
+
+// Skin convection H (T - t0) te dS (formulation_difftherm.py:29) on Bar_3 edges (end, end, middle;
+// formulations/element_Bar_3.py), integrated with the 3-point rule of element_Bar_3.py: in the
+// theta scheme A += theta H Ms, B -= (1 - theta) H Ms, and the load H t0 int N ds.
+void diff_set_convection(lmtg_ctx *c, uint64_t nedges, const uint32_t *edges, const double *H, uint64_t nH,
+                         double t0) {
+    LMTG_CHECK(c->allocated && c->elem_type == LMTG_ELEM_TRIANGLE6, LMTG_ERR_STATE, "diff_setup first");
+    LMTG_CHECK(nH == 1 || nH == nedges, LMTG_ERR_ARG, "H needs 1 or nedges values");
+    cudaStream_t s = c->stream;
+    const uint64_t nn = c->nn;
+    std::vector<uint32_t> bp(nn + 1), bc(c->nnzb);
+    LMTG_CUDA(cudaMemcpyAsync(bp.data(), c->bptr.p, (nn + 1) * 4, cudaMemcpyDeviceToHost, s));
+    LMTG_CUDA(cudaMemcpyAsync(bc.data(), c->bcol.p, c->nnzb * 4, cudaMemcpyDeviceToHost, s));
+    LMTG_CUDA(cudaStreamSynchronize(s));
+    const double gx[3] = {0.5 - 0.5 * std::sqrt(3.0 / 5.0), 0.5, 0.5 + 0.5 * std::sqrt(3.0 / 5.0)};
+    const double gw[3] = {5.0 / 18.0, 8.0 / 18.0, 5.0 / 18.0};
+    std::vector<std::pair<uint64_t, double>> ent;
+    std::vector<double> load(nn, 0.0);
+    for (uint64_t e = 0; e < nedges; ++e) {
+        const uint32_t nd[3] = {edges[3 * e], edges[3 * e + 1], edges[3 * e + 2]};
+        for (int k = 0; k < 3; ++k) LMTG_CHECK(nd[k] < nn, LMTG_ERR_ARG, "edge node >= nn");
+        const double h = H[nH == 1 ? 0 : e];
+        double Ms[3][3] = {}, Ns[3] = {};
+        for (int g = 0; g < 3; ++g) {
+            const double X = gx[g];
+            const double N[3] = {2 * (1 - X) * (0.5 - X), 2 * X * (X - 0.5), 4 * (1 - X) * X};
+            const double dN[3] = {4 * X - 3, 4 * X - 1, 4 - 8 * X};
+            double dx = 0, dy = 0;
+            for (int k = 0; k < 3; ++k) {
+                dx += dN[k] * c->h_pos[2 * (uint64_t)nd[k]];
+                dy += dN[k] * c->h_pos[2 * (uint64_t)nd[k] + 1];
+            }
+            const double wj = gw[g] * std::sqrt(dx * dx + dy * dy);
+            for (int a = 0; a < 3; ++a) {
+                Ns[a] += wj * N[a];
+                for (int b = 0; b < 3; ++b) Ms[a][b] += wj * N[a] * N[b];
+            }
+        }
+        for (int a = 0; a < 3; ++a) {
+            load[nd[a]] += h * t0 * Ns[a];
+            for (int b = 0; b < 3; ++b) {
+                const uint32_t i = nd[a], j = nd[b];
+                uint64_t q = bp[i];
+                while (q < bp[i + 1] && bc[q] != j) ++q;
+                LMTG_CHECK(q < bp[i + 1], LMTG_ERR_ARG, "edge nodes are not in one element");
+                ent.push_back({q, h * Ms[a][b]});
+            }
+        }
+    }
+    std::stable_sort(ent.begin(), ent.end(), [](const std::pair<uint64_t, double> &x,
+                                                const std::pair<uint64_t, double> &y) {
+        return x.first < y.first;
+    });  // stable sums: the contributions of one entry in edge order
+    std::vector<uint64_t> at;
+    std::vector<double> va, vb;
+    for (size_t k = 0; k < ent.size();) {
+        const uint64_t q = ent[k].first;
+        double v = 0;
+        for (; k < ent.size() && ent[k].first == q; ++k) v += ent[k].second;
+        at.push_back(q);
+        va.push_back(c->theta * v);
+        vb.push_back(-(1.0 - c->theta) * v);
+    }
+    if (!at.empty()) {
+        DBuf<uint64_t> dat;
+        DBuf<double> dva, dvb;
+        upload_u32(c, dat, at.data(), at.size());
+        upload_u32(c, dva, va.data(), va.size());
+        upload_u32(c, dvb, vb.data(), vb.size());
+        k_add_entries<<<grid_for(c, at.size(), 256), 256, 0, s>>>(dat.p, dva.p, dvb.p, at.size(), c->K64.p, c->K32.p,
+                                                                 c->B64.p);
+        k_jacobi_s<double><<<grid_for(c, nn, 256), 256, 0, s>>>(c->bdiag.p, c->K64.p, nn, c->Dinv64.p, nullptr);
+        k_jacobi_s<float><<<grid_for(c, nn, 256), 256, 0, s>>>(c->bdiag.p, c->K64.p, nn, c->Dinv32.p, nullptr);
+        LMTG_CUDA(cudaGetLastError());
+        c->launches += 3;
+        LMTG_CUDA(cudaStreamSynchronize(s));
+    }
+    c->h_diff_conv = load;
+    diff_update_load(c);
 }
 
 int diff_run(lmtg_ctx *c, int nsteps, double tol, int maxit, lmtg_solve_stats *st) {
@@ -847,6 +1005,10 @@ int lmtg_diff_mesh_set(lmtg_ctx *c, uint64_t nn, const double *pos, uint64_t ne,
         c->n = nn;
         c->pos.alloc(2 * nn);
         LMTG_CUDA(cudaMemcpyAsync(c->pos.p, pos, 16 * nn, cudaMemcpyHostToDevice, c->stream));
+        c->h_pos.assign(pos, pos + 2 * nn);  // skin integrals (convection)
+        c->h_diff_src.clear();
+        c->h_diff_conv.clear();
+        c->diff_load.release();
         upload_u32(c, c->conn, conn, 6 * ne);
         c->allocated = c->have64 = c->have32 = c->have_vec = false;
         LMTG_CUDA(cudaStreamSynchronize(c->stream));
@@ -861,6 +1023,22 @@ int lmtg_diff_setup(lmtg_ctx *c, const double *k, uint64_t nk, double rho_c, dou
         for (uint64_t q = 0; q < nbnd; ++q) LMTG_CHECK(bnd[q] < c->nn, LMTG_ERR_ARG, "node id >= nn");
         LMTG_CHECK(nbnd == 0 || penalty > 0, LMTG_ERR_UNSUPPORTED, "penalty constraints only");
         diff_setup(c, k, nk, rho_c, dt, theta, nbnd, bnd, penalty);
+        return LMTG_OK;
+    });
+}
+
+int lmtg_diff_set_sources(lmtg_ctx *c, const double *Q, const double *Qs) {
+    return guard_d(c, [&] {
+        diff_set_sources(c, Q, Qs);
+        return LMTG_OK;
+    });
+}
+
+int lmtg_diff_set_convection(lmtg_ctx *c, uint64_t nedges, const uint32_t *edges, const double *H, uint64_t nH,
+                             double t0) {
+    return guard_d(c, [&] {
+        LMTG_CHECK(nedges == 0 || (edges && H), LMTG_ERR_ARG, "null arrays");
+        diff_set_convection(c, nedges, edges, H, nH, t0);
         return LMTG_OK;
     });
 }

@@ -138,6 +138,8 @@ struct lmtg_ctx {
     lmtg::DBuf<double> B64, KeB64;
     double rho_c = 1.0, dt = 0.0, theta = 0.5;
     int diff_mode = LMTG_SOLVE_PCG_F64;
+    std::vector<double> h_diff_src, h_diff_conv;  // constant step loads (sources, convection)
+    lmtg::DBuf<double> diff_load;                  // their sum on the device (none: empty)
     // mixed solvers: recursive-residual reduction of each FP32 segment before the FP64 residual
     // replacement (lmtg_set_inner_reduction)
     double inner_reduction = 0.01;

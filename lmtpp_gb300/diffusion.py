@@ -39,6 +39,16 @@ def boundary_nodes(pos, eps=1e-9):
                                            | (pos[:, 1] > 1 - eps))[0], dtype=np.uint32)
 
 
+TRIANGLE6_EDGES = [[0, 1, 3], [1, 2, 4], [2, 0, 5]]  # Bar_3 children (formulations/element_Triangle_6.py:9-13)
+
+
+def edges_on(pos, conn, axis, value, eps=1e-9):
+    """Bar_3 skin edges (end, end, middle) of Triangle_6 elements lying on pos[:, axis] = value."""
+    q = np.asarray(conn)[:, TRIANGLE6_EDGES]  # ne x 3 x 3
+    on = np.all(np.abs(pos[q, axis] - value) < eps, axis=2)
+    return np.ascontiguousarray(q[on], dtype=np.uint32)
+
+
 class Diffusion:
     """Transient heat diffusion on a Triangle_6 mesh, resident on one GPU."""
 
@@ -59,6 +69,20 @@ class Diffusion:
         abi.check(self._lib.lmtg_diff_setup(self._ctx, abi.ptr(k), k.shape[0], float(rho_c), float(dt),
                                             float(theta), bnd.shape[0], abi.ptr(bnd) if bnd.size else None,
                                             float(penalty)), self._ctx, "diff_setup")
+
+    def set_sources(self, Q=None, Qs=None):
+        """Constant volume source Q (nodal field) and nodal source Qs of difftherm."""
+        q = None if Q is None else np.ascontiguousarray(Q, dtype=np.float64)
+        qs = None if Qs is None else np.ascontiguousarray(Qs, dtype=np.float64)
+        abi.check(self._lib.lmtg_diff_set_sources(self._ctx, abi.ptr(q), abi.ptr(qs)), self._ctx, "set_sources")
+
+    def set_convection(self, edges, H, t0=0.0):
+        """Skin convection H (T - t0) on Bar_3 edges (end, end, middle); H: one value or one per
+        edge.  Call after setup()."""
+        e = np.ascontiguousarray(edges, dtype=np.uint32).reshape(-1, 3)
+        h = np.ascontiguousarray(np.atleast_1d(H), dtype=np.float64)
+        abi.check(self._lib.lmtg_diff_set_convection(self._ctx, e.shape[0], abi.ptr(e), abi.ptr(h), h.shape[0],
+                                                     float(t0)), self._ctx, "set_convection")
 
     def set_solver(self, mode):
         """'fp64' (FP64 Jacobi-PCG) or 'mixed' (FP32 PCG with FP64 residual replacement)."""

@@ -336,14 +336,55 @@ def diffusion_problem(nb_points, k=1.0, rho_c=1.0, dt=1e-4, theta=0.5, pen=1e5):
                 T0=gaussian_bump(pos), k=k, rho_c=rho_c, dt=dt, theta=theta, penalty=pen)
 
 
-def diffusion_run(P, nsteps, T0=None):
-    """CPU theta-scheme: A T_{n+1} = B T_n with the direct solver; returns all states."""
+def diffusion_run(P, nsteps, T0=None, load=None):
+    """CPU theta-scheme: A T_{n+1} = B T_n (+ a constant load) with the direct solver; returns
+    all states."""
     T = np.array(P["T0"] if T0 is None else T0, dtype=np.float64)
     states = [T.copy()]
     for _ in range(nsteps):
-        T = skyline_solve(P["rowptr"], P["col"], P["A"], spmv(P["rowptr"], P["col"], P["B"], T))
+        rhs = spmv(P["rowptr"], P["col"], P["B"], T)
+        if load is not None:
+            rhs = rhs + load
+        T = skyline_solve(P["rowptr"], P["col"], P["A"], rhs)
         states.append(T.copy())
     return states
+
+
+def diffusion_sources(P, Q=None, Qs=None):
+    """The step load M Q + Qs of difftherm's sources (formulations/formulation_difftherm.py:26-29):
+    M the consistent Triangle_6 mass matrix (the theta-scheme matrices with k = 0 and dt = 1)."""
+    s = np.zeros(P["pos"].shape[0])
+    if Q is not None:
+        M, _ = assemble_diff(P["pos"], P["conn"], 0.0, 1.0, 1.0, 1.0, P["rowptr"], P["col"])
+        s += spmv(P["rowptr"], P["col"], M, np.asarray(Q, dtype=np.float64))
+    if Qs is not None:
+        s += np.asarray(Qs, dtype=np.float64)
+    return s
+
+
+def diffusion_convection(P, edges, H, t0):
+    """Skin convection H (T - t0) te dS on straight Bar_3 edges (end, end, middle) in closed form:
+    Ms = L/30 [[4, -1, 2], [-1, 4, 2], [2, 2, 16]], int N ds = L [1/6, 1/6, 2/3].  Adds
+    theta H Ms to P["A"] and -(1 - theta) H Ms to P["B"] (lower CSR, in place); returns the load
+    H t0 int N ds."""
+    pos, rowptr, col, th = P["pos"], P["rowptr"], P["col"], P["theta"]
+    H = np.broadcast_to(np.asarray(H, dtype=np.float64), (len(edges),))
+    Ms0 = np.array([[4.0, -1.0, 2.0], [-1.0, 4.0, 2.0], [2.0, 2.0, 16.0]]) / 30.0
+    Ns0 = np.array([1.0, 1.0, 4.0]) / 6.0
+    load = np.zeros(pos.shape[0])
+    for e, nd in enumerate(np.asarray(edges, dtype=np.int64)):
+        L = np.linalg.norm(pos[nd[1]] - pos[nd[0]])
+        load[nd] += H[e] * t0 * L * Ns0
+        for a in range(3):
+            for b in range(3):
+                i, j = nd[a], nd[b]
+                if j > i:
+                    continue
+                q = rowptr[i] + int(np.nonzero(col[rowptr[i]:rowptr[i + 1]] == j)[0][0])
+                v = H[e] * L * Ms0[a, b]
+                P["A"][q] += th * v
+                P["B"][q] -= (1.0 - th) * v
+    return load
 
 
 # ---------------------------------------------------------------------------------------------

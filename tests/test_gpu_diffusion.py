@@ -122,3 +122,40 @@ def test_diffusion_mixed_adjoint_matches_fp64():
     assert J32 == pytest.approx(J64, rel=1e-9)
     assert np.linalg.norm(g32 - g64) <= 1e-8 * np.linalg.norm(g64)
     d.close()
+
+
+@pytest.mark.parametrize("mode,tol", [("fp64", 1e-10), ("mixed", 1e-8)])
+def test_sources_and_convection_match_oracle(mode, tol):
+    """difftherm's other terms: volume source Q (nodal), nodal source Qs, skin convection
+    H (T - t0) on the x = 1 edges; T = 0 on x = 0 only."""
+    from lmtpp_gb300.diffusion import edges_on
+    P = O.diffusion_problem(9, theta=0.5)
+    pos = P["pos"]
+    left = np.nonzero(pos[:, 0] < 1e-9)[0].astype(np.uint32)
+    # the oracle problem with the Dirichlet nodes on x = 0 only
+    rowptr, col = P["rowptr"], P["col"]
+    A, B = O.assemble_diff(pos, P["conn"], 1.0, 1.0, 1e-4, 0.5, rowptr, col)
+    md = O.penalty(rowptr, col, A, None, left, np.ones(left.size), np.zeros(left.size), 1e5)
+    P.update(A=A, B=B)
+    Q = np.sin(np.pi * pos[:, 0]) * np.cos(np.pi * pos[:, 1])
+    Qs = np.zeros(pos.shape[0])
+    Qs[[10, 40, 70]] = [3.0, -1.0, 2.0]
+    edges = edges_on(pos, P["conn"], 0, 1.0)
+    assert edges.shape[0] == 8
+    load = O.diffusion_sources(P, Q, Qs) + O.diffusion_convection(P, edges, 2.5, 0.7)
+    states = O.diffusion_run(P, 6, load=load)
+    d = Diffusion(pos, P["conn"])
+    d.setup(1.0, rho_c=1.0, dt=1e-4, theta=0.5, dirichlet=left, penalty=1e5)
+    assert d.get_penalty_scale() == pytest.approx(md, rel=1e-12)
+    d.set_sources(Q, Qs)
+    d.set_convection(edges, 2.5, 0.7)
+    rp, cl, Ag, Bg = d.get_matrices()
+    n = pos.shape[0]
+    assert abs(csr(rp, cl, Ag, n) - csr(rowptr, col, A, n)).max() <= 1e-12 * np.abs(A).max()
+    assert abs(csr(rp, cl, Bg, n) - csr(rowptr, col, B, n)).max() <= 1e-12 * np.abs(B).max()
+    d.set_solver(mode)
+    d.set_state(P["T0"])
+    d.run(6, tol=1e-14 if mode == "fp64" else 1e-12)
+    T = d.get_state()
+    assert np.linalg.norm(T - states[-1]) <= tol * np.linalg.norm(states[-1])
+    d.close()
