@@ -129,6 +129,13 @@ int lmtg_add_skin_traction(lmtg_ctx *ctx, uint64_t nfaces, const uint32_t *faces
  * penalty == 0 is the reference's exact constraint (Lagrange rows, formulation.h:1072-1088),
  * applied here by elimination: u_j = res / coef exactly (one exact constraint per DOF, coef != 0;
  * needs the FP64 matrix assembly; not with the adjoint, the fit or batch solves). */
+/* Volume force of elasticity_iso (formulations/formulation_elasticity_iso.py:49, static:
+ * dep_tt = 0): F += density f_vol int N dV; f_vol global (3 doubles).  Defaults 0. */
+int lmtg_set_volume_force(lmtg_ctx *ctx, double density, const double f_vol[3]);
+/* Nodal springs dep_imp_coef_0 (formulation_elasticity_iso.py:55-60): K(3I+d,3I+d) += coef[I],
+ * F(3I+d) += coef[I] target[3I+d] (target = lim_cond_0 dep_imp_val_0_0 + lim_cond_1
+ * dep_imp_val_0_1; NULL: 0).  coef NULL removes them. */
+int lmtg_set_nodal_springs(lmtg_ctx *ctx, const double *coef, const double *target);
 /* The formulation's levenberg_marquadt term (formulation_ancestor.h:253, applied in
  * assemble_constraints, formulation.h:1033-1034): K(i,i) += max|diag K| * lm at every matrix
  * assembly, before the constraints; 0 by default. */

@@ -49,6 +49,8 @@ _SIGS = {
     "lmtg_add_skin_traction": (_i, [_vp, _u64, _vp, _vp]),
     "lmtg_set_constraints": (_i, [_vp, _u64, _vp, _vp, _vp, _d]),
     "lmtg_set_levenberg_marquadt": (_i, [_vp, _d]),
+    "lmtg_set_volume_force": (_i, [_vp, _d, _vp]),
+    "lmtg_set_nodal_springs": (_i, [_vp, _vp, _vp]),
     "lmtg_assemble": (_i, [_vp, _i]),
     "lmtg_get_matrix_lower": (_i, [_vp, _vp, _vp, _vp]),
     "lmtg_get_sollicitation": (_i, [_vp, _vp]),

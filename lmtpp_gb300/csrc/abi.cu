@@ -335,6 +335,34 @@ int lmtg_material_set_nu(lmtg_ctx *c, const double *nu, uint64_t n_nu) {
     });
 }
 
+int lmtg_set_volume_force(lmtg_ctx *c, double density, const double f_vol[3]) {
+    return guard(c, [&] {
+        LMTG_CHECK(c->nnu == 3 && c->ne > 0, LMTG_ERR_STATE, "elasticity mesh_set first");
+        LMTG_CHECK(f_vol && std::isfinite(density), LMTG_ERR_ARG, "f_vol needed");
+        c->density = density;
+        for (int i = 0; i < 3; ++i) c->fvol[i] = f_vol[i];
+        c->have_vec = false;
+        return LMTG_OK;
+    });
+}
+
+int lmtg_set_nodal_springs(lmtg_ctx *c, const double *coef, const double *target) {
+    return guard(c, [&] {
+        LMTG_CHECK(c->nnu == 3 && c->ne > 0, LMTG_ERR_STATE, "elasticity mesh_set first");
+        if (!coef) {
+            c->spring_coef.release();
+            c->spring_target.release();
+        } else {
+            upload(c, c->spring_coef, coef, c->nn);
+            if (target) upload(c, c->spring_target, target, c->n);
+            else c->spring_target.release();
+        }
+        c->have64 = c->have32 = c->have_vec = false;
+        LMTG_CUDA(cudaStreamSynchronize(c->stream));
+        return LMTG_OK;
+    });
+}
+
 int lmtg_set_levenberg_marquadt(lmtg_ctx *c, double lm) {
     return guard(c, [&] {
         LMTG_CHECK(std::isfinite(lm), LMTG_ERR_ARG, "levenberg_marquadt must be finite");

@@ -59,6 +59,7 @@ void do_assemble(lmtg_ctx *c, int flags) {
                                   cudaMemcpyHostToDevice, c->stream));
         c->have_vec = true;
     }
+    apply_body_terms(c, mat, vec);
     if (mat || vec) apply_penalty(c, mat, vec);
     if (mat) build_block_jacobi(c, c->have64, c->have32);
     LMTG_CUDA(cudaStreamSynchronize(c->stream));

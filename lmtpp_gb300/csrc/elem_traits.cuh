@@ -25,6 +25,21 @@ struct Hexa8 {
         const T z = (g >= 4) ? gb : ga;
         dN_at(x, y, z, d);
     }
+    // shape functions at the reference point (x, y, z)
+    template <class T>
+    __device__ static void N_at(T x, T y, T z, T (&N)[8]) {
+        const T mx = 1 - x, my = 1 - y, mz = 1 - z;
+        N[0] = mx * my * mz; N[1] = x * my * mz; N[2] = x * y * mz; N[3] = mx * y * mz;
+        N[4] = mx * my * z;  N[5] = x * my * z;  N[6] = x * y * z;  N[7] = mx * y * z;
+    }
+    // Gauss point g of the order-2 rule
+    template <class T>
+    __device__ static void gauss_point(int g, T &x, T &y, T &z) {
+        const T ga = (T)0.211324865405, gb = (T)0.788675134595;
+        x = (g == 1 || g == 2 || g == 5 || g == 6) ? gb : ga;
+        y = (g == 2 || g == 3 || g == 6 || g == 7) ? gb : ga;
+        z = (g >= 4) ? gb : ga;
+    }
     // derivatives at the reference point (x, y, z)
     template <class T>
     __device__ static void dN_at(T x, T y, T z, T (&d)[8][3]) {
@@ -49,6 +64,21 @@ struct Tetra10 {
         const T ta = (T)0.1381966011250105, tb = (T)0.5854101966249685;
         const T x = g == 1 ? tb : ta, y = g == 2 ? tb : ta, z = g == 3 ? tb : ta;
         dN_at(x, y, z, d);
+    }
+    template <class T>
+    __device__ static void N_at(T x, T y, T z, T (&N)[10]) {
+        const T X[4] = {1 - x - y - z, x, y, z};
+#pragma unroll
+        for (int i = 0; i < 4; ++i) N[i] = X[i] * (2 * X[i] - 1);
+        N[4] = 4 * X[0] * X[1]; N[5] = 4 * X[1] * X[2]; N[6] = 4 * X[0] * X[2];
+        N[7] = 4 * X[0] * X[3]; N[8] = 4 * X[1] * X[3]; N[9] = 4 * X[2] * X[3];
+    }
+    template <class T>
+    __device__ static void gauss_point(int g, T &x, T &y, T &z) {
+        const T ta = (T)0.1381966011250105, tb = (T)0.5854101966249685;
+        x = g == 1 ? tb : ta;
+        y = g == 2 ? tb : ta;
+        z = g == 3 ? tb : ta;
     }
     // derivatives at the reference point (x, y, z)
     template <class T>

@@ -92,3 +92,118 @@ void launch_elem_fields(lmtg_ctx *c, const double *u, double *out) {
 }
 
 }  // namespace lmtg
+
+// ---- volume force and nodal springs of elasticity_iso -------------------------------------
+// density * (dep_tt - f_vol) . te dV with dep_tt = 0 (static): F += density f_vol int N_a dV
+// (formulations/formulation_elasticity_iso.py:49), assembled without atomics: node I's
+// elements are the contributions (a, a) of its diagonal block's gather list.
+namespace lmtg {
+
+template <class EL>
+__global__ void k_volume_weights(const double *__restrict__ pos, const uint32_t *__restrict__ conn, uint64_t ne,
+                                 double *__restrict__ w) {
+    constexpr int NPE = EL::npe;
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < ne;
+         e += (uint64_t)gridDim.x * blockDim.x) {
+        double xyz[NPE][3], acc[NPE];
+#pragma unroll
+        for (int a = 0; a < NPE; ++a) {
+            acc[a] = 0.0;
+            const uint64_t n = conn[NPE * e + a];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) xyz[a][i] = pos[3 * n + i];
+        }
+        for (int g = 0; g < EL::ngp; ++g) {
+            double x, y, z, N[NPE], dN[NPE][3], J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+            EL::gauss_point(g, x, y, z);
+            EL::N_at(x, y, z, N);
+            EL::dN_at(x, y, z, dN);
+#pragma unroll
+            for (int a = 0; a < NPE; ++a)
+#pragma unroll
+                for (int i = 0; i < 3; ++i)
+#pragma unroll
+                    for (int j = 0; j < 3; ++j) J[i][j] = fma(xyz[a][i], dN[a][j], J[i][j]);
+            const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+                               J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                               J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+            const double wd = EL::template weight<double>(g) * det;
+#pragma unroll
+            for (int a = 0; a < NPE; ++a) acc[a] = fma(wd, N[a], acc[a]);
+        }
+#pragma unroll
+        for (int a = 0; a < NPE; ++a) w[NPE * e + a] = acc[a];
+    }
+}
+
+template <int NPE, int NPAIRS>
+__global__ void k_volume_force(const uint32_t *__restrict__ bdiag, const uint32_t *__restrict__ gptr,
+                               const uint32_t *__restrict__ gsrc, const double *__restrict__ w, uint64_t nn,
+                               double f0, double f1, double f2, double *__restrict__ F) {
+    for (uint64_t I = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; I < nn;
+         I += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t d = bdiag[I];
+        double s = 0.0;
+        for (uint32_t g = gptr[d]; g < gptr[d + 1]; ++g) {
+            const uint32_t q = gsrc[g] >> 1, e = q / NPAIRS, pr = q - e * NPAIRS;
+            int a = 0;
+            for (int k = 0; k < NPE; ++k) a = pair_index(k, k, NPE) == (int)pr ? k : a;
+            s += w[(uint64_t)NPE * e + a];
+        }
+        F[3 * I] += f0 * s;
+        F[3 * I + 1] += f1 * s;
+        F[3 * I + 2] += f2 * s;
+    }
+}
+
+// dep_imp_coef_0 * dep . te dN (formulation_elasticity_iso.py:55-60): K(3I+d, 3I+d) += coef_I,
+// F(3I+d) += coef_I target(3I+d)
+__global__ void k_springs(const uint32_t *__restrict__ bptr, const uint32_t *__restrict__ bdiag,
+                          const double *__restrict__ coef, const double *__restrict__ target, uint64_t nn,
+                          double *K64, float *K32, double *F, bool mat, bool vec) {
+    for (uint64_t I = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; I < nn;
+         I += (uint64_t)gridDim.x * blockDim.x) {
+        const double k = coef[I];
+        if (k == 0.0) continue;
+        const uint32_t rb = bptr[I], deg = bptr[I + 1] - rb, dd = bdiag[I] - rb;
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            if (mat) {
+                const uint64_t idx = kidx(rb, deg, dd, 4 * r);
+                if (K64) K64[idx] += k;
+                if (K32) K32[idx] = K64 ? (float)K64[idx] : K32[idx] + (float)k;
+            }
+            if (vec && target) F[3 * I + r] += k * target[3 * I + r];
+        }
+    }
+}
+
+void apply_body_terms(lmtg_ctx *c, bool mat, bool vec) {
+    const int T = 256;
+    cudaStream_t s = c->stream;
+    if (vec && c->density != 0.0 && (c->fvol[0] != 0.0 || c->fvol[1] != 0.0 || c->fvol[2] != 0.0)) {
+        DBuf<double> w;
+        w.alloc(c->ne * (uint64_t)c->npe);
+        if (c->elem_type == LMTG_ELEM_HEXA8) {
+            k_volume_weights<Hexa8><<<grid_for(c, c->ne, 128, 16), 128, 0, s>>>(c->pos.p, c->conn.p, c->ne, w.p);
+            k_volume_force<8, Hexa8::npairs><<<grid_for(c, c->nn, T), T, 0, s>>>(
+                c->bdiag.p, c->gptr.p, c->gsrc.p, w.p, c->nn, c->density * c->fvol[0], c->density * c->fvol[1],
+                c->density * c->fvol[2], c->F.p);
+        } else {
+            k_volume_weights<Tetra10><<<grid_for(c, c->ne, 128, 16), 128, 0, s>>>(c->pos.p, c->conn.p, c->ne, w.p);
+            k_volume_force<10, Tetra10::npairs><<<grid_for(c, c->nn, T), T, 0, s>>>(
+                c->bdiag.p, c->gptr.p, c->gsrc.p, w.p, c->nn, c->density * c->fvol[0], c->density * c->fvol[1],
+                c->density * c->fvol[2], c->F.p);
+        }
+        c->launches += 2;
+    }
+    if (c->spring_coef.p && (mat || vec)) {
+        k_springs<<<grid_for(c, c->nn, T), T, 0, s>>>(c->bptr.p, c->bdiag.p, c->spring_coef.p,
+                                                      c->spring_target.p, c->nn, c->have64 ? c->K64.p : nullptr,
+                                                      c->have32 ? c->K32.p : nullptr, c->F.p, mat, vec);
+        c->launches += 1;
+    }
+    LMTG_CUDA(cudaGetLastError());
+}
+
+}  // namespace lmtg

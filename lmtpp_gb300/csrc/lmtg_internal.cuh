@@ -156,6 +156,8 @@ struct lmtg_ctx {
     double penalty_scale = 0;  // > 0: fixed max|diag| used by the penalty instead of recomputing it
     lmtg::DBuf<double> elim_w;  // exact constraints: K u_bar of the last matrix assembly
     double levenberg_marquadt = 0;  // K(i,i) += max|diag| * levenberg_marquadt at assembly
+    double density = 0, fvol[3] = {0, 0, 0};     // volume force density f_vol
+    lmtg::DBuf<double> spring_coef, spring_target;  // nodal dep_imp_coef_0 terms
 
     // solver workspace
     lmtg::DBuf<double> w64[6];
@@ -189,6 +191,8 @@ void launch_grad_E(lmtg_ctx *c, const double *a, const double *b, double *g);
 
 // ---- element fields after the solve (fields.cu) ----
 void launch_elem_fields(lmtg_ctx *c, const double *u, double *out);
+// volume force and nodal springs into K and F at assembly, before the constraints
+void apply_body_terms(lmtg_ctx *c, bool mat, bool vec);
 
 // ---- heat diffusion (diffusion.cu) ----
 void diff_setup(lmtg_ctx *c, const double *k, uint64_t nk, double rho_c, double dt, double theta,

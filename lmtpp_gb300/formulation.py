@@ -306,6 +306,19 @@ class Formulation:
         return y
 
     # -- sensitivities -------------------------------------------------------------------------
+    def set_volume_force(self, f_vol, density=7800.0):
+        """Volume force density * f_vol (formulation_elasticity_iso.py:4,7; density's default
+        7800 as there)."""
+        f = np.ascontiguousarray(f_vol, dtype=np.float64)
+        abi.check(self._lib.lmtg_set_volume_force(self._ctx, float(density), abi.ptr(f)), self._ctx,
+                  "set_volume_force")
+
+    def set_nodal_springs(self, coef, target=None):
+        """dep_imp_coef_0 springs: coef per node, target displacement (3 per node) or 0."""
+        k = None if coef is None else np.ascontiguousarray(coef, dtype=np.float64)
+        t = None if target is None else np.ascontiguousarray(target, dtype=np.float64).ravel()
+        abi.check(self._lib.lmtg_set_nodal_springs(self._ctx, abi.ptr(k), abi.ptr(t)), self._ctx, "set_nodal_springs")
+
     def set_inner_reduction(self, inner_reduction):
         """Recursive-residual reduction of each FP32 segment of the mixed solvers (default 0.01)."""
         abi.check(self._lib.lmtg_set_inner_reduction(self._ctx, float(inner_reduction)), self._ctx,

@@ -231,6 +231,49 @@ static double elast_gp(int npe, const double *xyz, const double (*dN)[3], double
     return det;
 }
 
+/* Shape functions (formulations/element_Hexa.py:61-68, element_Tetra_10.py:27-41). */
+static void hexa8_N(const double *xi, double N[8]) {
+    const double x = xi[0], y = xi[1], z = xi[2], mx = 1 - x, my = 1 - y, mz = 1 - z;
+    const double v[8] = {mx * my * mz, x * my * mz, x * y * mz, mx * y * mz,
+                         mx * my * z,  x * my * z,  x * y * z,  mx * y * z};
+    memcpy(N, v, sizeof(v));
+}
+static void tetra10_N(const double *xi, double N[10]) {
+    const double X[4] = {1 - xi[0] - xi[1] - xi[2], xi[0], xi[1], xi[2]};
+    for (int i = 0; i < 4; ++i) N[i] = X[i] * (2 * X[i] - 1);
+    static const int ed[6][2] = {{0, 1}, {1, 2}, {0, 2}, {0, 3}, {1, 3}, {2, 3}};
+    for (int k = 0; k < 6; ++k) N[4 + k] = 4 * X[ed[k][0]] * X[ed[k][1]];
+}
+
+/* w[e npe + a] = int_e N_a dV with the order-2 rules: the weights of the volume force
+ * density * f_vol . te dV (formulations/formulation_elasticity_iso.py:49). */
+int orc_volume_weights(int npe, uint64_t ne, const double *pos, const uint32_t *conn, double *w) {
+    if (npe != 8 && npe != 10) return 1;
+    double gw[8], gx[24];
+    const int ng = npe == 8 ? orc_gauss_hexa_order2(gw, gx) : orc_gauss_tetra_order2(gw, gx);
+    for (uint64_t e = 0; e < ne; ++e) {
+        for (int a = 0; a < npe; ++a) w[(uint64_t)npe * e + a] = 0.0;
+        for (int g = 0; g < ng; ++g) {
+            double N[10], dN[10][3], J[3][3] = {{0}}, Ji[3][3], det;
+            if (npe == 8) {
+                hexa8_N(gx + 3 * g, N);
+                hexa8_dN(gx + 3 * g, dN);
+            } else {
+                tetra10_N(gx + 3 * g, N);
+                tetra10_dN(gx + 3 * g, dN);
+            }
+            for (int a = 0; a < npe; ++a) {
+                const uint32_t n = conn[(uint64_t)npe * e + a];
+                for (int i = 0; i < 3; ++i)
+                    for (int j = 0; j < 3; ++j) J[i][j] += pos[3 * (uint64_t)n + i] * dN[a][j];
+            }
+            inv3(J, Ji, &det);
+            for (int a = 0; a < npe; ++a) w[(uint64_t)npe * e + a] += gw[g] * det * N[a];
+        }
+    }
+    return 0;
+}
+
 /* Element fields after the solve (apply_on_elements_after_solve,
  * formulations/formulation_elasticity_iso.py:64-85): every var_inter is set to 0.5 -- the cube
  * centre for Hexa8; for Tetra10 the same point (0.5, 0.5, 0.5), which the quadratic field

@@ -132,6 +132,8 @@ int orc_ic_pcg(uint64_t n, const uint64_t *rowptr, const uint32_t *col, const do
 int orc_cg(uint64_t n, const uint64_t *rowptr, const uint32_t *col, const double *val,
            const double *fac, int precond, const double *b, double *x, int crit_kind,
            double crit, int maxit);
+/* int_e N_a dV per element and node (ne x npe): volume-force weights. */
+int orc_volume_weights(int npe, uint64_t ne, const double *pos, const uint32_t *conn, double *w);
 /* Element fields after the solve at var_inter = 0.5: out ne x 13 = epsilon[6] (tensor shear,
  * 11 22 33 12 13 23), sigma[6], tr_epsilon (formulation_elasticity_iso.py:64-85). */
 int orc_elem_fields(int npe, uint64_t ne, const double *pos, const uint32_t *conn, const double *E,

@@ -164,6 +164,21 @@ def elem_fields(pos, conn, E, nu, u):
     return out
 
 
+def volume_force(pos, conn, density, f_vol):
+    """F of the volume force density f_vol . te dV (formulation_elasticity_iso.py:49)."""
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    conn = np.ascontiguousarray(conn, dtype=np.uint32)
+    ne, npe = conn.shape
+    w = np.zeros((ne, npe))
+    rc = lib().orc_volume_weights(ctypes.c_int(npe), ctypes.c_uint64(ne), _p(pos, _f64p), _p(conn, _u32p),
+                                  _p(w, _f64p))
+    if rc:
+        raise RuntimeError("orc_volume_weights failed: %d" % rc)
+    s = np.zeros(pos.shape[0])
+    np.add.at(s, conn.ravel().astype(np.int64), w.ravel())
+    return (density * s[:, None] * np.asarray(f_vol, dtype=np.float64)[None, :]).ravel()
+
+
 def quad4_traction(faces, pos, t, F):
     faces = np.ascontiguousarray(faces, dtype=np.uint32)
     t = np.asarray(t, dtype=np.float64)

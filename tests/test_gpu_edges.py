@@ -184,3 +184,36 @@ def test_levenberg_marquadt_term_and_constant_matrix():
     x2 = O.skyline_solve(P["rowptr"], P["col"], val, Fg)
     assert np.linalg.norm(f.get_result() - x2) <= 1e-10 * np.linalg.norm(x2)
     f.close()
+
+
+@pytest.mark.parametrize("elem", ["hexa", "tetra10"])
+def test_volume_force_and_nodal_springs_match_oracle(elem):
+    """elasticity_iso's density f_vol term and dep_imp_coef_0 springs, on a distorted mesh."""
+    P = O.elasticity_problem(4, elem=elem)
+    pos = P["pos"].copy()
+    rng = np.random.default_rng(4)
+    inner = np.all((pos > 1e-9) & (pos < 1 - 1e-9), axis=1)
+    pos += inner[:, None] * rng.uniform(-0.04, 0.04, pos.shape)
+    nn = pos.shape[0]
+    coef = np.where(rng.random(nn) < 0.2, 1e4, 0.0)
+    target = rng.standard_normal(3 * nn) * 1e-3
+    f = Formulation(pos, P["conn"])
+    f.elastic_modulus = P["E"]
+    f.poisson_ratio = P["nu"]
+    f.add_constraints(P["dofs"], P["penalty"])
+    f.set_volume_force((0.0, -9.81, 1.5), density=7800.0)
+    f.set_nodal_springs(coef, target)
+    f.solve(1e-13, mode="fp64")
+    # oracle: element stiffness + springs on the diagonal, then the penalty
+    rowptr, col = O.pattern_lower(nn, 3, P["conn"])
+    val = O.assemble_elast(pos, P["conn"], P["E"], P["nu"], rowptr, col)
+    diag = rowptr[1:].astype(np.int64) - 1
+    val[diag] += np.repeat(coef, 3)
+    F = O.volume_force(pos, P["conn"], 7800.0, (0.0, -9.81, 1.5)) + np.repeat(coef, 3) * target
+    O.penalty(rowptr, col, val, F, P["dofs"], np.ones(P["dofs"].size), np.zeros(P["dofs"].size), P["penalty"])
+    np.testing.assert_allclose(f.get_sollicitation(), F, rtol=0, atol=1e-12 * np.abs(F).max())
+    rp, cl, v = f.get_mat()
+    assert np.abs(v - val).max() <= 1e-12 * np.abs(val).max()
+    x = O.skyline_solve(rowptr, col, val, F)
+    assert np.linalg.norm(f.get_result() - x) <= 1e-10 * np.linalg.norm(x)
+    f.close()
