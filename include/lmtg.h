@@ -122,6 +122,10 @@ int lmtg_set_nodal_loads(lmtg_ctx *ctx, const double *F);
  * element_Triangle_6.h). */
 int lmtg_add_skin_traction(lmtg_ctx *ctx, uint64_t nfaces, const uint32_t *faces,
                            const double traction[3]);
+/* Skin pressure p dS_normal . te dS (formulation_elasticity_iso.py:60, variable p), on the same
+ * faces: the unit normal is cross(d x/d xi0, d x/d xi1) of the face's node order
+ * (formal_lf/element.py:467-474); outward for the Hexa children.  Adds to the load vector. */
+int lmtg_add_skin_pressure(lmtg_ctx *ctx, uint64_t nfaces, const uint32_t *faces, double p);
 
 /* Constraints add_constraint("coef*node[i].dep[d] - res", penalty) for linear single-unknown
  * constraints; assembled as in assemble_constraints (formulation.h:1028-1071):

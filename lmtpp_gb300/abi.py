@@ -47,6 +47,7 @@ _SIGS = {
     "lmtg_allocate_matrices": (_i, [_vp, ctypes.POINTER(_u64)]),
     "lmtg_set_nodal_loads": (_i, [_vp, _vp]),
     "lmtg_add_skin_traction": (_i, [_vp, _u64, _vp, _vp]),
+    "lmtg_add_skin_pressure": (_i, [_vp, _u64, _vp, _d]),
     "lmtg_set_constraints": (_i, [_vp, _u64, _vp, _vp, _vp, _d]),
     "lmtg_set_levenberg_marquadt": (_i, [_vp, _d]),
     "lmtg_set_volume_force": (_i, [_vp, _d, _vp]),

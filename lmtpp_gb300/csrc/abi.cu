@@ -46,7 +46,7 @@ void upload(lmtg_ctx *c, DBuf<T> &d, const T *h, size_t n) {
 
 // Quad4 consistent loads of a uniform traction, order-2 quad rule of the reference table
 // (include/mesh/element_Quad.h:5-12, abscissae with 12 significant digits, weights 1/4).
-void quad4_loads(const double *pos, const uint32_t *q, const double t[3], double *F) {
+void quad4_loads(const double *pos, const uint32_t *q, const double t[3], double *F, const double *pressure = nullptr) {
     const double A = 0.211324865405, B = 0.788675134595;
     const double gp[4][2] = {{B, B}, {A, B}, {B, A}, {A, A}};
     for (int g = 0; g < 4; ++g) {
@@ -62,15 +62,19 @@ void quad4_loads(const double *pos, const uint32_t *q, const double t[3], double
             }
         const double nx = tu[1] * tv[2] - tu[2] * tv[1], ny = tu[2] * tv[0] - tu[0] * tv[2],
                      nz = tu[0] * tv[1] - tu[1] * tv[0];
-        const double ds = std::sqrt(nx * nx + ny * ny + nz * nz) * 0.25;
+        const double nl = std::sqrt(nx * nx + ny * ny + nz * nz), ds = nl * 0.25;
+        // pressure: p dS_normal, the unit normal cross(d x / d xi0, d x / d xi1) of the face's
+        // node order (formal_lf/element.py:467-474)
+        const double tg[3] = {pressure ? *pressure * nx / nl : t[0], pressure ? *pressure * ny / nl : t[1],
+                              pressure ? *pressure * nz / nl : t[2]};
         for (int a = 0; a < 4; ++a)
-            for (int d = 0; d < 3; ++d) F[3 * (uint64_t)q[a] + d] += N[a] * t[d] * ds;
+            for (int d = 0; d < 3; ++d) F[3 * (uint64_t)q[a] + d] += N[a] * tg[d] * ds;
     }
 }
 
 // Triangle_6 consistent loads of a uniform traction, order-2 rule of the reference table
 // (include/mesh/element_Triangle_6.h:5-15: 3 edge-midpoint points, weights 1/6).
-void tri6_loads(const double *pos, const uint32_t *q, const double t[3], double *F) {
+void tri6_loads(const double *pos, const uint32_t *q, const double t[3], double *F, const double *pressure = nullptr) {
     const double gp[3][2] = {{0.5, 0.0}, {0.5, 0.5}, {0.0, 0.5}};
     for (int g = 0; g < 3; ++g) {
         const double u = gp[g][0], v = gp[g][1], X0 = 1 - u - v;
@@ -86,9 +90,11 @@ void tri6_loads(const double *pos, const uint32_t *q, const double t[3], double 
             }
         const double nx = tu[1] * tv[2] - tu[2] * tv[1], ny = tu[2] * tv[0] - tu[0] * tv[2],
                      nz = tu[0] * tv[1] - tu[1] * tv[0];
-        const double ds = std::sqrt(nx * nx + ny * ny + nz * nz) * 0.16666666666666666667;
+        const double nl = std::sqrt(nx * nx + ny * ny + nz * nz), ds = nl * 0.16666666666666666667;
+        const double tg[3] = {pressure ? *pressure * nx / nl : t[0], pressure ? *pressure * ny / nl : t[1],
+                              pressure ? *pressure * nz / nl : t[2]};
         for (int a = 0; a < 6; ++a)
-            for (int d = 0; d < 3; ++d) F[3 * (uint64_t)q[a] + d] += N[a] * t[d] * ds;
+            for (int d = 0; d < 3; ++d) F[3 * (uint64_t)q[a] + d] += N[a] * tg[d] * ds;
     }
 }
 
@@ -495,6 +501,22 @@ int lmtg_set_nodal_loads(lmtg_ctx *c, const double *F) {
     return guard(c, [&] {
         LMTG_CHECK(c->n > 0 && F, LMTG_ERR_ARG, "mesh_set first / null F");
         c->h_loads.assign(F, F + c->n);
+        return LMTG_OK;
+    });
+}
+
+int lmtg_add_skin_pressure(lmtg_ctx *c, uint64_t nfaces, const uint32_t *faces, double p) {
+    return guard(c, [&] {
+        LMTG_CHECK(c->n > 0 && c->nnu == 3 && (nfaces == 0 || faces), LMTG_ERR_ARG, "bad faces");
+        const int fn = c->elem_type == LMTG_ELEM_HEXA8 ? 4 : 6;
+        for (uint64_t f = 0; f < nfaces; ++f)
+            for (int k = 0; k < fn; ++k) LMTG_CHECK(faces[fn * f + k] < c->nn, LMTG_ERR_ARG, "face node >= nn");
+        const double t0[3] = {0, 0, 0};
+        for (uint64_t f = 0; f < nfaces; ++f) {
+            if (fn == 4) quad4_loads(c->h_pos.data(), faces + 4 * f, t0, c->h_loads.data(), &p);
+            else tri6_loads(c->h_pos.data(), faces + 6 * f, t0, c->h_loads.data(), &p);
+        }
+        c->have_vec = false;
         return LMTG_OK;
     });
 }

@@ -204,6 +204,12 @@ class Formulation:
         abi.check(self._lib.lmtg_add_skin_traction(self._ctx, faces.shape[0], abi.ptr(faces), abi.ptr(t)),
                   self._ctx, "skin traction")
 
+    def add_skin_pressure(self, faces, p):
+        """p dS_normal on skin faces (the unit normal of the face's node order)."""
+        faces = np.ascontiguousarray(faces, dtype=np.uint32)
+        abi.check(self._lib.lmtg_add_skin_pressure(self._ctx, faces.shape[0], abi.ptr(faces), float(p)),
+                  self._ctx, "skin pressure")
+
     # -- the hot path -------------------------------------------------------------------------
     def allocate_matrices(self):
         nnz = ctypes.c_uint64(0)

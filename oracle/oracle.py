@@ -484,3 +484,36 @@ def add_levenberg_marquadt(rowptr, val, max_diag, lm):
     on the lower CSR (the diagonal is last in each row)."""
     diag = rowptr[1:].astype(np.int64) - 1
     val[diag] += max_diag * lm
+
+
+def pressure_loads(faces, pos, p):
+    """Consistent loads of a uniform pressure p dS_normal (formulation_elasticity_iso.py:60) on
+    Quad4 (4 nodes) or Triangle_6 (6 nodes) skin faces: n = unit cross(dx/dxi0, dx/dxi1) of the
+    face node order (formal_lf/element.py:467-474), order-2 rules (element_Quad.h / element_Triangle_6.h)."""
+    faces = np.asarray(faces, dtype=np.int64)
+    F = np.zeros(pos.size)
+    if faces.shape[1] == 4:
+        a, b = 0.211324865405, 0.788675134595
+        pts, w = [(b, b), (a, b), (b, a), (a, a)], 0.25
+        def shape(u, v):
+            N = np.array([(1 - u) * (1 - v), u * (1 - v), u * v, (1 - u) * v])
+            du = np.array([-(1 - v), 1 - v, v, -v])
+            dv = np.array([-(1 - u), -u, u, 1 - u])
+            return N, du, dv
+    else:
+        pts, w = [(0.5, 0.0), (0.5, 0.5), (0.0, 0.5)], 1.0 / 6.0
+        def shape(u, v):
+            X0 = 1 - u - v
+            N = np.array([X0 * (2 * X0 - 1), u * (2 * u - 1), v * (2 * v - 1), 4 * X0 * u, 4 * u * v, 4 * v * X0])
+            du = np.array([-(4 * X0 - 1), 4 * u - 1, 0, 4 * (X0 - u), 4 * v, -4 * v])
+            dv = np.array([-(4 * X0 - 1), 0, 4 * v - 1, -4 * u, 4 * u, 4 * (X0 - v)])
+            return N, du, dv
+    for q in faces:
+        x = pos[q]
+        for (u, v) in pts:
+            N, du, dv = shape(u, v)
+            n = np.cross(du @ x, dv @ x)
+            area = np.linalg.norm(n)
+            for k, node in enumerate(q):
+                F[3 * node:3 * node + 3] += N[k] * p * (n / area) * w * area
+    return F

@@ -104,3 +104,25 @@ def test_batch_autotuner_reports_candidates():
     assert st["rel_residual"] <= 1e-10
     assert info["ntiles"] >= 3
     bf.close()
+
+
+def test_batch_of_tetra10_meshes_matches_oracle():
+    """Tetra10 rows reach 65 blocks: the batched SpMV's wide-row path."""
+    rng = np.random.default_rng(8)
+    sides = [2, 3]
+    E = rng.uniform(5e4, 3e5, 2)
+    nu = rng.uniform(0.2, 0.4, 2)
+    probs = [O.elasticity_problem(s + 1, E=E[m], nu=nu[m], pen=1e5, elem="tetra10") for m, s in enumerate(sides)]
+    bf = BatchFormulation([(P["pos"], P["conn"]) for P in probs])
+    bf.set_materials(E, nu)
+    bf.add_constraints(np.concatenate([P["dofs"] + 3 * int(bf.node_off[m]) for m, P in enumerate(probs)]), 1e5)
+    bf.assemble(True, False, mixed=True)
+    B = rng.standard_normal((4, bf.n))
+    for mode, tol in (("mixed", 1e-8), ("fp64", 1e-10)):
+        X, st, its = bf.solve_batch(B, mode=mode, tol=1e-13 if mode == "fp64" else 1e-12)
+        for m, P in enumerate(probs):
+            d = bf.dofs(m)
+            for r in range(4):
+                x = O.skyline_solve(P["rowptr"], P["col"], P["val"], B[r, d])
+                assert np.linalg.norm(X[r, d] - x) <= tol * np.linalg.norm(x), (mode, m, r)
+    bf.close()

@@ -217,3 +217,26 @@ def test_volume_force_and_nodal_springs_match_oracle(elem):
     x = O.skyline_solve(rowptr, col, val, F)
     assert np.linalg.norm(f.get_result() - x) <= 1e-10 * np.linalg.norm(x)
     f.close()
+
+
+@pytest.mark.parametrize("elem", ["hexa", "tetra10"])
+def test_skin_pressure_matches_oracle(elem):
+    P = O.elasticity_problem(4, elem=elem)
+    pos = P["pos"].copy()
+    rng = np.random.default_rng(6)
+    inner = np.all((pos > 1e-9) & (pos < 1 - 1e-9), axis=1)
+    pos += inner[:, None] * rng.uniform(-0.04, 0.04, pos.shape)
+    f = Formulation(pos, P["conn"])
+    f.elastic_modulus = P["E"]
+    f.add_constraints(P["dofs"], P["penalty"])
+    faces = x1_faces(pos, P["conn"])
+    f.add_skin_pressure(faces, 2.5)
+    f.assemble(True, True)
+    F = f.get_sollicitation()
+    Fo = O.pressure_loads(faces, pos, 2.5)
+    np.testing.assert_allclose(F, Fo, rtol=0, atol=1e-13)
+    if elem == "hexa":  # outward normal on x = 1: the same loads as the traction (p, 0, 0)
+        Ft = np.zeros_like(Fo)
+        O.quad4_traction(faces, pos, (2.5, 0.0, 0.0), Ft)
+        np.testing.assert_allclose(Fo, Ft, rtol=0, atol=1e-13)
+    f.close()
