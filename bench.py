@@ -205,7 +205,7 @@ def timed_steps(f, mode, tol, steps, torch, stream):
 
 
 def spmv_bytes(nn, nnzb, s):
-    """Algorithmic bytes of one PCG SpMV launch (k_pcg_spmv): K values + block column indices
+    """Algorithmic bytes of one PCG SpMV launch (k_pcg_spmv, k_pcg_spmv_bulk): K values + column indices
     + row pointers, p read once (gathered; 16 B per node padded in FP32, 24 B in FP64) and q
     written once (3 values per node)."""
     vs = 4 if s == 4 else 3
@@ -345,10 +345,13 @@ def cpu_desc(s):
                s["t_solve"], s["iters"], s["crit"], s["err"]))
 
 
-# dram__bytes_read.sum + dram__bytes_write.sum / algorithmic bytes of one k_pcg_spmv<float>
-# launch, ncu capture of the Hexa8 64^3 case: (293.433 MB + 4.631 MB) over
-# spmv_bytes(274625, 7189057, 4) = 296.350 MB
-SPMV32_TRAFFIC_RATIO = (293.433088 + 4.630784) / 296.350284
+# dram__bytes_read.sum + dram__bytes_write.sum / algorithmic bytes of one FP32 PCG SpMV
+# launch (k_pcg_spmv_bulk<2, 512, 8, 1, 4>), ncu captures of small cases:
+#   Hexa8 64^3:    (293.262 MB + 4.432 MB) over spmv_bytes(274625, 7189057, 4) = 296.350 MB
+#   Tetra10 24^3:  (132.940 MB + 3.373 MB) over spmv_bytes(117649, 3259585, 4) = 134.148 MB
+SPMV32_KERNEL = "k_pcg_spmv_bulk<2, 512, 8, 1, 4>"
+SPMV32_TRAFFIC_RATIO = {"hexa8": (293.261824 + 4.431616) / 296.350284,
+                        "tetra10": (132.940032 + 3.373312) / 134.148172}
 
 METRIC = "time-to-solution at 1e-10 rel. error vs FP64 oracle, mixed vs FP64 CG; asm GB/s"
 
@@ -645,11 +648,12 @@ def main():
         "warmup": args.warmup, "ms_per_step": r["ms_mixed"], "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64", "data": "synthetic",
         "config": workload_config(args),
-        "roofline": {"bound": "hbm", "kernel": "k_pcg_spmv<float>", "achieved": ach, "peak": hbm,
+        "roofline": {"bound": "hbm", "kernel": SPMV32_KERNEL, "achieved": ach, "peak": hbm,
                      "unit": "GB/s", "frac": ach / hbm,
-                     "traffic": b32 * SPMV32_TRAFFIC_RATIO, "traffic_source": "ncu dram bytes of a "
-                     "64^3 capture scaled by the block count (traffic/algorithmic = %.3f)"
-                     % SPMV32_TRAFFIC_RATIO,
+                     "traffic": b32 * SPMV32_TRAFFIC_RATIO[args.elem],
+                     "traffic_source": "ncu dram bytes of a %s capture scaled by the block count "
+                     "(traffic/algorithmic = %.4f)" % ("64^3" if args.elem == "hexa8" else "24^3",
+                                                       SPMV32_TRAFFIC_RATIO[args.elem]),
                      "peak_source": peak_note, "algorithmic_bytes": b32,
                      "launch_ms": r["spmv32_ms"]},
         "cpu_baseline": {"value": cpu_v, "unit": "s", "cores": 1, "kind": "port", "sample": cpu_desc(s)},

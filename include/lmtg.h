@@ -304,6 +304,12 @@ int lmtg_batch_set_options(lmtg_ctx *ctx, int tile_rows, int variant);
  * in (0, 1); default 0.01.  No reference counterpart. */
 int lmtg_set_inner_reduction(lmtg_ctx *ctx, double inner_reduction);
 
+/* FP32 SpMV of the single-system PCG: 0 = one warp per pair of node rows, the matrix read
+ * straight into registers; 1 (default) and 2 = the matrix streamed through shared memory by
+ * bulk copies (TMA) in a ring of two stages of up to 16 rows, sized for 4 and 5 CTAs per SM.
+ * All give the same q; p.q is summed in a different fixed order.  No reference counterpart. */
+int lmtg_set_spmv_kind(lmtg_ctx *ctx, int kind);
+
 /* Element fields after the solve (replaces the generated apply_on_elements_after_solve of
  * elasticity_iso, formulations/formulation_elasticity_iso.py:64-85, run by call_after_solve,
  * include/formulation/formulation.h:1867-1875): per element, at var_inter = 0.5, out[13 e + k] =

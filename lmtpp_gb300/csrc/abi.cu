@@ -461,6 +461,14 @@ int lmtg_set_inner_reduction(lmtg_ctx *c, double inner_reduction) {
     });
 }
 
+int lmtg_set_spmv_kind(lmtg_ctx *c, int kind) {
+    return guard(c, [&] {
+        LMTG_CHECK(kind >= 0 && kind <= 2, LMTG_ERR_ARG, "spmv kind in 0..2");
+        c->spmv_kind = kind;
+        return LMTG_OK;
+    });
+}
+
 int lmtg_batch_set_options(lmtg_ctx *c, int tile_rows, int variant) {
     return guard(c, [&] {
         LMTG_CHECK(tile_rows == 0 || tile_rows == 16 || tile_rows == 32 || tile_rows == 64 || tile_rows == 128,
@@ -480,7 +488,7 @@ int lmtg_allocate_matrices(lmtg_ctx *c, uint64_t *nnz_lower) {
         build_pattern(c);
         c->Ke64.alloc(c->ne * (uint64_t)c->npairs * 9);
         c->K64.alloc(c->nnzb * 9);
-        c->K32.alloc(c->nnzb * 9);
+        c->K32.alloc(c->nnzb * 9 + 4);  // 16 bytes of slack: bulk copies round their end up
         c->F.alloc(c->n);
         c->u.alloc(c->n);
         c->Dinv64.alloc(c->nn * 9);

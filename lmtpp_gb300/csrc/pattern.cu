@@ -182,6 +182,7 @@ __global__ void k_nbr(const uint32_t *conn, int npe, const uint32_t *incptr, con
         if (over) atomicExch(bad, 2);
         if (!kFill) {
             deg[i] = (uint32_t)m;
+            atomicMax(bad + 1, m);  // widest row
         } else {
             uint32_t o = bptr[i];
             for (int k = 0; k < m; ++k) {
@@ -249,8 +250,8 @@ void build_pattern(lmtg_ctx *c) {
     cudaStream_t s = c->stream;
     const int T = 256;
     DBuf<int> bad;
-    bad.alloc(1);
-    LMTG_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), s));
+    bad.alloc(2);  // [0] error code, [1] blocks in the widest row
+    LMTG_CUDA(cudaMemsetAsync(bad.p, 0, 2 * sizeof(int), s));
 
     DBuf<uint32_t> cnt, incptr, cursor, inc;
     cnt.alloc(nn + 1);
@@ -275,10 +276,12 @@ void build_pattern(lmtg_ctx *c) {
                                                        deg.p, nullptr, nullptr, nullptr, bad.p);
     c->bptr.alloc(nn + 1);
     c->nnzb = exclusive_scan_u32(c, deg.p, c->bptr.p, nn);
-    LMTG_CUDA(cudaMemcpy(&hbad, bad.p, sizeof(int), cudaMemcpyDeviceToHost));
-    LMTG_CHECK(hbad == 0, LMTG_ERR_UNSUPPORTED, "a node has more than 96 neighbour nodes");
+    int hb2[2] = {0, 0};
+    LMTG_CUDA(cudaMemcpy(hb2, bad.p, 2 * sizeof(int), cudaMemcpyDeviceToHost));
+    LMTG_CHECK(hb2[0] == 0, LMTG_ERR_UNSUPPORTED, "a node has more than 96 neighbour nodes");
+    c->max_row_blocks = (uint32_t)hb2[1];
     deg.release();
-    c->bcol.alloc(c->nnzb);
+    c->bcol.alloc(c->nnzb + 4);  // 16 bytes of slack: bulk copies round their end up
     c->bdiag.alloc(nn);
     k_nbr<true><<<grid_for(c, nn, 128), 128, 0, s>>>(c->conn.p, c->npe, incptr.p, inc.p, nn,
                                                       nullptr, c->bptr.p, c->bcol.p, c->bdiag.p,

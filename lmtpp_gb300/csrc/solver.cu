@@ -6,9 +6,10 @@
 // graphs of kChunk iterations; the host only reads the device scalars between chunks.
 #include <chrono>
 #include <cmath>
+#include <type_traits>
 #include <vector>
 
-#include "solver_kernels.cuh"
+#include "spmv_bulk.cuh"
 
 namespace lmtg {
 
@@ -44,6 +45,58 @@ __global__ void k_dot64(const double *__restrict__ a, const double *__restrict__
 
 static int row_grid(lmtg_ctx *c) { return grid_for(c, c->nn * 32, kRowThreads, 8); }
 static int node_grid(lmtg_ctx *c) { return grid_for(c, c->nn, kRowThreads, 8); }
+
+// Bulk-copy SpMV instances, spmv_kind 1, 2 = (stages, blocks per stage, consumer warps,
+// evict-first L2 hint, CTAs per SM the registers are sized for).  Kind 1, the default, held
+// 96% of the measured HBM copy bandwidth on Hexa8 128^3 (0.361 ms against 0.449 ms for the
+// warp-row kernel, kind 0).  The dynamic shared-memory limit and the resident grid are set up
+// once per kind.
+#define LMTG_BULK_KINDS(X)     \
+    X(1, 2, 512, 8, true, 4)   \
+    X(2, 2, 512, 8, true, 5)
+
+template <int kStages, int kCap, int kCons, bool kEF, int kMinB>
+static int bulk_grid(lmtg_ctx *c) {
+    constexpr size_t smem = bulk_smem_bytes<kStages, kCap>();
+    auto fn = k_pcg_spmv_bulk<kStages, kCap, kCons, kEF, kMinB>;
+    LMTG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int nb = 0;
+    LMTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, bulk_threads<kCons>(), smem));
+    return c->sm_count * (nb > 0 ? nb : 1);
+}
+
+static void spmv_setup(lmtg_ctx *c) {
+    if (c->spmv_kind == c->spmv_setup_kind) return;
+    switch (c->spmv_kind) {
+#define LMTG_BULK_SETUP(id, st, cap, cons, ef, minb) \
+    case id: c->spmv_grid = bulk_grid<st, cap, cons, ef, minb>(c); break;
+        LMTG_BULK_KINDS(LMTG_BULK_SETUP)
+#undef LMTG_BULK_SETUP
+        default: c->spmv_grid = row_grid(c); break;
+    }
+    c->spmv_setup_kind = c->spmv_kind;
+}
+
+// q = K p, pq and alpha of one PCG iteration (FP64: the warp-row kernel; FP32: spmv_kind)
+template <class T, int VS>
+static void launch_pcg_spmv(lmtg_ctx *c, const T *K, const T *p, T *q, cudaStream_t s) {
+    if constexpr (std::is_same<T, float>::value) {
+        switch (c->spmv_kind) {
+#define LMTG_BULK_LAUNCH(id, st, cap, cons, ef, minb)                                                   \
+    case id:                                                                                              \
+        k_pcg_spmv_bulk<st, cap, cons, ef, minb><<<c->spmv_grid, bulk_threads<cons>(),                      \
+                                                   bulk_smem_bytes<st, cap>(), s>>>(c->bptr.p, c->bcol.p, K, p, q, \
+                                                                                    c->nn, c->scal.p,      \
+                                                                                    c->partials.p);        \
+        return;
+            LMTG_BULK_KINDS(LMTG_BULK_LAUNCH)
+#undef LMTG_BULK_LAUNCH
+            default: break;
+        }
+    }
+    k_pcg_spmv<T, VS><<<row_grid(c), kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, K, p, q, c->nn, c->scal.p,
+                                                          c->partials.p);
+}
 
 void spmv64(lmtg_ctx *c, const double *x, double *y) {
     k_spmv<double><<<row_grid(c), kRowThreads, 0, c->stream>>>(c->bptr.p, c->bcol.p, c->K64.p, x, y,
@@ -103,6 +156,7 @@ static int run_pcg(lmtg_ctx *c, const T *K, const T *Dinv, const T *b, T *x, T *
                    double b_norm2, std::chrono::steady_clock::time_point deadline, bool use_deadline,
                    int *iters, double beta_den = 0.0) {
     cudaStream_t s = c->stream;
+    spmv_setup(c);
     PcgScalars init{};
     init.crit = crit;
     init.crit_kind = crit_kind;
@@ -134,8 +188,7 @@ static int run_pcg(lmtg_ctx *c, const T *K, const T *Dinv, const T *b, T *x, T *
     LMTG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < 2 * kChunkPairs; ++k) {
         k_pcg_dir<T, VS><<<node_grid(c), kRowThreads, 0, s>>>(z, p0, c->nn, c->scal.p);
-        k_pcg_spmv<T, VS><<<row_grid(c), kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, K, p0, q, c->nn,
-                                                              c->scal.p, c->partials.p);
+        launch_pcg_spmv<T, VS>(c, K, p0, q, s);
         k_pcg_update<T, VS><<<node_grid(c), kRowThreads, 0, s>>>(x, r, z, p0, q, Dinv, c->nn,
                                                                  c->scal.p, c->partials.p);
     }
@@ -279,6 +332,7 @@ template <class T>
 static void profile_pcg_t(lmtg_ctx *c, const T *K, const T *Dinv, const T *b, T *x, T *r, T *z,
                           T *p0, T *p1, T *q, int iters, double *spmv_ms, double *update_ms) {
     cudaStream_t s = c->stream;
+    spmv_setup(c);
     PcgScalars init{};
     init.crit = 0.0;  // never met: every launch does the full work
     init.crit_kind = LMTG_CRIT_REL_RESIDUAL;
@@ -296,8 +350,7 @@ static void profile_pcg_t(lmtg_ctx *c, const T *K, const T *Dinv, const T *b, T 
     for (auto &e : ev) LMTG_CUDA(cudaEventCreate(&e));
     LMTG_CUDA(cudaEventRecord(ev[0], s));
     for (int k = 0; k < iters; ++k) {
-        k_pcg_spmv<T, VS><<<row_grid(c), kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, K, p0, q, c->nn,
-                                                              c->scal.p, c->partials.p);
+        launch_pcg_spmv<T, VS>(c, K, p0, q, s);
         LMTG_CUDA(cudaEventRecord(ev[2 * k + 1], s));
         // the rest of the iteration: update, then the next direction
         k_pcg_update<T, VS><<<node_grid(c), kRowThreads, 0, s>>>(x, r, z, p0, q, Dinv, c->nn, c->scal.p,

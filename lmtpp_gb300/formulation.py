@@ -330,6 +330,10 @@ class Formulation:
         abi.check(self._lib.lmtg_set_inner_reduction(self._ctx, float(inner_reduction)), self._ctx,
                   "set_inner_reduction")
 
+    def set_spmv_kind(self, kind):
+        """FP32 PCG SpMV: 0 = warp per row pair, 1 (default), 2 = matrix streamed by bulk copies (TMA)."""
+        abi.check(self._lib.lmtg_set_spmv_kind(self._ctx, int(kind)), self._ctx, "set_spmv_kind")
+
     def set_penalty_scale(self, max_diag):
         """Hold the penalty scale at max_diag (0 = recompute max|diag K| at each assembly)."""
         abi.check(self._lib.lmtg_set_penalty_scale(self._ctx, float(max_diag)), self._ctx, "penalty scale")

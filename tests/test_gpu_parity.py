@@ -154,6 +154,35 @@ def test_tetra10_medium_mesh_fp64_vs_mixed():
     f.close()
 
 
+@pytest.mark.parametrize("kind", [1, 2])
+@pytest.mark.parametrize("elem", ["hexa8", "tetra10"])
+def test_bulk_copy_spmv_solves_like_warp_rows(elem, kind):
+    """The TMA-streamed FP32 SpMV (kinds 1, 2) gives the mixed solve of the warp-row kernel
+    (kind 0) and solves the oracle's system."""
+    if elem == "hexa8":
+        pos, conn = make_rect_hexa(15)
+    else:
+        pos, conn = make_rect_tetra10(9)
+    E = 1e5 * np.exp(np.random.default_rng(5).standard_normal(conn.shape[0]) * 0.5)
+    f = build_problem(pos, conn, E, 0.3, 1e5)
+    f.set_spmv_kind(0)
+    st0 = f.solve(1e-12, mode="mixed")
+    u0 = f.get_result()
+    rowptr, col, val = f.get_mat()
+    F = f.get_sollicitation()
+    assert np.linalg.norm(F - O.spmv(rowptr, col, val, u0)) <= 1e-11 * np.linalg.norm(F), st0
+    f.set_spmv_kind(kind)
+    f.set_result(np.zeros_like(u0))
+    st = f.solve(1e-12, mode="mixed")
+    u = f.get_result()
+    assert np.linalg.norm(u - u0) <= 1e-9 * np.linalg.norm(u0), (st, st0)
+    # deterministic: the same run again gives the same bits
+    f.set_result(np.zeros_like(u0))
+    f.solve(1e-12, mode="mixed")
+    assert np.array_equal(f.get_result(), u)
+    f.close()
+
+
 def test_spmv_matches_oracle():
     P = O.elasticity_problem(9)
     f = build_problem(P["pos"], P["conn"], P["E"], P["nu"], P["penalty"])
