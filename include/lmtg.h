@@ -292,11 +292,15 @@ int lmtg_batch_solve(lmtg_ctx *ctx, int mode, double tol, int maxit, double time
                      lmtg_solve_stats *stats, int *pair_iters);
 /* The solutions, X[r * ndof + i] (nrhs x ndof doubles, host). */
 int lmtg_batch_get_result(lmtg_ctx *ctx, double *X);
-/* The autotuner's choice: rows per tile, SpMV variant (0 plain, 1 next row prefetched), tile
- * count, and the SpMV time of each candidate (8 doubles, ms, variant-major over tile sizes
- * 16, 32, 64, 128 rows; 0 = not tried; optional).  A tile is one warp's work. */
+/* The autotuner's choice: rows per tile, SpMV variant (0 plain, 1 next row prefetched, 2 the
+ * matrix streamed through shared memory by bulk copies, FP32 only), tile count, and the SpMV
+ * time of each candidate (12 doubles, ms, variant-major over tile sizes 16, 32, 64, 128 rows
+ * for variants 0, 1 and 128, 256, 512, 1024 for variant 2; 0 = not tried; optional).  A tile
+ * is one warp's work (variants 0, 1); in variant 2 it is one CTA's SpMV unit, made of 128-row
+ * tiles that the vector kernels take one warp each. */
 int lmtg_batch_info(lmtg_ctx *ctx, int *tile_rows, int *variant, uint64_t *ntiles, double *tuned_ms);
-/* Fixed rows per tile (0: autotune) and SpMV variant (-1: autotune) of the batch solver. */
+/* Fixed rows per tile (0: autotune) and SpMV variant (-1: autotune; 0, 1, 2) of the batch
+ * solver. */
 int lmtg_batch_set_options(lmtg_ctx *ctx, int tile_rows, int variant);
 
 /* Mixed-precision solvers (lmtg_solve_system, lmtg_batch_solve, the diffusion steps): the

@@ -86,7 +86,7 @@ class BatchFormulation(Formulation):
         return X, self.last_stats, its
 
     def set_options(self, tile_rows=0, variant=-1):
-        """Fixed rows per warp tile and SpMV variant; 0 / -1: autotuned."""
+        """Fixed rows per tile and SpMV variant (0, 1, 2 = bulk copies, FP32); 0 / -1: autotuned."""
         abi.check(self._lib.lmtg_batch_set_options(self._ctx, int(tile_rows), int(variant)), self._ctx,
                   "batch_set_options")
 
@@ -94,9 +94,10 @@ class BatchFormulation(Formulation):
         rows = ctypes.c_int()
         var = ctypes.c_int()
         nt = ctypes.c_uint64()
-        ms = np.zeros(8)
+        ms = np.zeros(12)
         abi.check(self._lib.lmtg_batch_info(self._ctx, ctypes.byref(rows), ctypes.byref(var), ctypes.byref(nt),
                                             abi.ptr(ms)), self._ctx, "batch_info")
-        sizes = (16, 32, 64, 128)
+        sizes = ((16, 32, 64, 128), (16, 32, 64, 128), (128, 256, 512, 1024))
         return {"tile_rows": rows.value, "variant": var.value, "ntiles": nt.value,
-                "tuned_spmv_ms": {"v%d_r%d" % (v, r): ms[4 * v + i] for v in (0, 1) for i, r in enumerate(sizes)}}
+                "tuned_spmv_ms": {"v%d_r%d" % (v, r): ms[4 * v + i] for v in (0, 1, 2)
+                                  for i, r in enumerate(sizes[v])}}

@@ -471,9 +471,11 @@ int lmtg_set_spmv_kind(lmtg_ctx *c, int kind) {
 
 int lmtg_batch_set_options(lmtg_ctx *c, int tile_rows, int variant) {
     return guard(c, [&] {
-        LMTG_CHECK(tile_rows == 0 || tile_rows == 16 || tile_rows == 32 || tile_rows == 64 || tile_rows == 128,
-                   LMTG_ERR_ARG, "tile_rows: 0 (autotune), 16, 32, 64 or 128");
-        LMTG_CHECK(variant >= -1 && variant <= 1, LMTG_ERR_ARG, "variant: -1 (autotune), 0 or 1");
+        LMTG_CHECK(variant >= -1 && variant <= 2, LMTG_ERR_ARG, "variant: -1 (autotune), 0, 1 or 2");
+        const bool small = tile_rows == 16 || tile_rows == 32 || tile_rows == 64 || tile_rows == 128;
+        const bool large = tile_rows == 128 || tile_rows == 256 || tile_rows == 512 || tile_rows == 1024;
+        LMTG_CHECK(tile_rows == 0 || (variant == 2 ? large : variant == -1 ? (small || large) : small),
+                   LMTG_ERR_ARG, "tile_rows: 0 (autotune), 16, 32, 64 or 128 (variants 0, 1), 128..1024 (2)");
         c->batch_tile_rows = tile_rows;
         c->batch_variant = variant;
         batch_free(c);  // re-tune at the next solve

@@ -22,9 +22,10 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
-#include "solver_kernels.cuh"
+#include "spmv_bulk.cuh"
 
 namespace lmtg {
 
@@ -41,6 +42,9 @@ struct BTile {
 struct BDev {
     const BTile *tiles;
     uint32_t ntiles;
+    const uint32_t *groups;    // ngroups + 1: k_b_rows_bulk's unit g = tiles [groups[g], groups[g+1])
+    uint32_t ngroups;          //   (consecutive tiles of one system)
+    const uint32_t *sys_g;     // nsys + 1: the units of system m are [sys_g[m], sys_g[m+1])
     const uint32_t *tile_off;  // nsys + 1: tiles of system m are [tile_off[m], tile_off[m+1])
     double *partials;          // ntiles * kBSlots
     unsigned *tk;              // 4 ticket rows of nsys
@@ -51,6 +55,7 @@ struct BDev {
     int *iter, *done, *status;
     int *sys_done;             // nsys
     int *n_active;             // systems with a pair still running
+    int *fault;                // set (LMTG_ERR_TIMEOUT) when a bounded wait of a kernel gave up
     int maxit;
 };
 
@@ -254,6 +259,251 @@ __global__ void __launch_bounds__(kBThreads)
                 B.alpha32[k] = (float)al;
             } else {
                 B.rr[k] = val;
+            }
+        }
+    }
+}
+
+// q = K p and p.q per pair (kMode 0 of k_b_rows) with the matrix streamed through shared memory
+// by bulk copies (TMA): CTAs take tiles round-robin; one producer warp copies the values and
+// column indices of up to 16 rows of the CTA's current tile per stage into a ring of kStages
+// stages (evict-first L2 policy), eight consumer warps take two rows each, read their blocks
+// from shared memory, release the stage and gather the four right-hand sides.  At the last
+// stage of a CTA unit (consecutive tiles of one system) each consumer warp commits its per-rhs
+// partials to its own slot of the unit; the system's last commit sums the slots in a fixed
+// order.  Every wait is bounded; one that
+// gives up sets *B.fault.
+constexpr int kBBulkCons = 8;
+constexpr int kBBulkThreads = 32 * (kBBulkCons + 1);
+constexpr int kBTileSlots = kBBulkCons * kBR;  // partial slots per tile (>= kBSlots)
+static_assert(kBTileSlots >= kBSlots, "partials hold kBSlots values per tile");
+
+// warp_commit for a CTA unit shared by kBBulkCons warps: warp w stores its per-rhs totals of
+// unit g in slot (g, w); the last of the system's warps to commit sums all of the system's
+// slots in order.
+__device__ __forceinline__ bool warp_commit_w(const BDev &B, uint32_t g, uint32_t sys, int w,
+                                              const double (&v)[kBR], unsigned *ticket, double (&tot)[kBR]) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t t0 = B.sys_g[sys], t1 = B.sys_g[sys + 1];
+    const uint32_t nslot = (t1 - t0) * kBBulkCons;
+    unsigned t = 0;
+    if (lane == 0) {
+#pragma unroll
+        for (int i = 0; i < kBR; ++i) B.partials[((size_t)g * kBBulkCons + w) * kBR + i] = v[i];
+        __threadfence();
+        t = atomicInc(ticket + sys, nslot - 1);  // wraps to 0 for the next launch
+    }
+    t = __shfl_sync(0xffffffffu, t, 0);
+    if (t != nslot - 1) return false;
+    __threadfence();
+#pragma unroll
+    for (int i = 0; i < kBR; ++i) {
+        double x = 0.0;
+        for (uint64_t sl = (uint64_t)t0 * kBBulkCons + lane; sl < (uint64_t)t1 * kBBulkCons; sl += 32)
+            x += __ldcg(B.partials + sl * kBR + i);
+        tot[i] = warp_sum(x);
+    }
+    return true;
+}
+
+template <int kStages, int kCap, int kMinB>
+__global__ void __launch_bounds__(kBBulkThreads, kMinB)
+    k_b_rows_bulk(BDev B, const uint32_t *__restrict__ bptr, const uint32_t *__restrict__ bcol,
+                  const float *__restrict__ K, const float *__restrict__ x, float *__restrict__ y) {
+    using St = BulkStage<kCap>;
+    constexpr int kRows = 2 * kBBulkCons;
+    if (*(volatile int *)B.n_active == 0) return;
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ uint64_t full[kStages], empty[kStages];
+    __shared__ uint64_t meta[kStages][4];  // g0, g1, first value, first column
+    __shared__ uint32_t mtile[kStages][2];  // tile, 1 = last stage of the tile
+    __shared__ uint32_t sbp[kStages][kRows + 1];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < kStages; ++i) {
+            bulk::mbar_init(&full[i], 1);
+            bulk::mbar_init(&empty[i], kBBulkCons);
+        }
+        bulk::fence_barrier_init();
+    }
+    __syncthreads();
+    if (warp == kBBulkCons) {
+        // ---------------- producer ----------------
+        uint32_t k = 0;
+        bool failed = false;
+        auto next_slot = [&](int slot) -> bool {
+            if (k < (uint32_t)kStages) return true;
+            const bool ok = bulk::mbar_wait(&empty[slot], ((k / kStages) - 1) & 1u);
+            return __all_sync(0xffffffffu, ok);
+        };
+        for (uint32_t tile = 0, g = blockIdx.x, gcur = 0, tile_end = 0; !failed; ++tile) {
+            if (tile >= tile_end) {  // next unit of this CTA
+                if (g >= B.ngroups) break;
+                tile = B.groups[g];
+                tile_end = B.groups[g + 1];
+                gcur = g;
+                g += gridDim.x;
+            }
+            const BTile t = B.tiles[tile];
+            if (B.sys_done[t.sys]) {  // uniform for the whole launch; a unit is one system
+                tile = tile_end - 1;
+                continue;
+            }
+            uint64_t g0 = t.row0;
+            uint32_t b0 = bptr[g0];
+            while (g0 < t.row1) {
+                const int slot = k % kStages;
+                if (!next_slot(slot)) {
+                    failed = true;
+                    break;
+                }
+                const uint64_t gi = g0 + 1 + lane;
+                const bool in = lane < kRows && gi <= t.row1;
+                const uint32_t bi = in ? bptr[gi] : 0u;
+                const unsigned fits = __ballot_sync(0xffffffffu, in && bi - b0 <= (uint32_t)kCap);
+                const int nrows = __popc(fits);
+                if (nrows == 0) {
+                    failed = true;
+                    break;
+                }
+                const uint32_t b1 = __shfl_sync(0xffffffffu, bi, nrows - 1);
+                if (lane < nrows) sbp[slot][lane + 1] = bi;
+                if (lane == 0) sbp[slot][0] = b0;
+                __syncwarp();
+                if (lane == 0) {
+                    const uint64_t kb0 = (36ull * b0) & ~15ull, kb1 = (36ull * b1 + 15ull) & ~15ull;
+                    const uint64_t cb0 = (4ull * b0) & ~15ull, cb1 = (4ull * b1 + 15ull) & ~15ull;
+                    meta[slot][0] = g0;
+                    meta[slot][1] = g0 + nrows;
+                    meta[slot][2] = kb0 / 4;
+                    meta[slot][3] = cb0 / 4;
+                    mtile[slot][0] = gcur;  // the unit; 1 = its last stage
+                    mtile[slot][1] = (g0 + nrows == t.row1 && tile + 1 == tile_end) ? 1u : 0u;
+                    unsigned char *dst = smem + (size_t)slot * St::kBytes;
+                    const uint64_t pol = bulk::policy_evict_first();
+                    __threadfence_block();
+                    bulk::mbar_arrive_expect_tx(&full[slot], (uint32_t)((kb1 - kb0) + (cb1 - cb0)));
+                    bulk::copy_g2s_hint(dst, reinterpret_cast<const unsigned char *>(K) + kb0, (uint32_t)(kb1 - kb0),
+                                        &full[slot], pol);
+                    bulk::copy_g2s_hint(dst + St::kKBytes, reinterpret_cast<const unsigned char *>(bcol) + cb0,
+                                        (uint32_t)(cb1 - cb0), &full[slot], pol);
+                }
+                g0 += nrows;
+                b0 = b1;
+                ++k;
+            }
+        }
+        if (!failed) {
+            const int slot = k % kStages;
+            if (next_slot(slot)) {
+                if (lane == 0) {  // sentinel: no rows
+                    meta[slot][0] = 0;
+                    meta[slot][1] = 0;
+                    bulk::mbar_arrive(&full[slot]);
+                }
+            } else {
+                failed = true;
+            }
+        }
+        if (failed && lane == 0) {
+            atomicExch(B.fault, LMTG_ERR_TIMEOUT);
+            const uint32_t first = k > (uint32_t)kStages ? k - kStages : 0u;
+            for (uint32_t s2 = first; s2 < k; ++s2) bulk::mbar_wait(&full[s2 % kStages], (s2 / kStages) & 1u);
+        }
+    } else {
+        // ---------------- consumers ----------------
+        const int v = lane >> 1;
+        const bool writer = (lane & 1) == 0 && v < kBV;
+        const int my_r = writer ? v / 3 : -1;
+        float acc = 0.f;
+        for (uint32_t k = 0;; ++k) {
+            const int slot = k % kStages;
+            const bool ok = bulk::mbar_wait(&full[slot], (k / kStages) & 1u);
+            if (!__all_sync(0xffffffffu, ok)) {
+                if (lane == 0) atomicExch(B.fault, LMTG_ERR_TIMEOUT);
+                break;
+            }
+            const uint64_t g0 = meta[slot][0], g1 = meta[slot][1];
+            if (g0 == g1) break;
+            const uint32_t unit = mtile[slot][0];
+            const bool last = mtile[slot][1] != 0;
+            const float *sK = reinterpret_cast<const float *>(smem + (size_t)slot * St::kBytes);
+            const uint32_t *sC = reinterpret_cast<const uint32_t *>(smem + (size_t)slot * St::kBytes + St::kKBytes);
+            const uint64_t kbase = meta[slot][2], cbase = meta[slot][3];
+            const uint64_t I0 = g0 + 2 * warp;
+            const int nmine = I0 >= g1 ? 0 : (I0 + 1 < g1 ? 2 : 1);
+            uint32_t rbv[2] = {0u, 0u}, dv[2] = {0u, 0u};
+            for (int r = 0; r < nmine; ++r) {
+                rbv[r] = sbp[slot][I0 - g0 + r];
+                dv[r] = sbp[slot][I0 - g0 + r + 1] - rbv[r];
+            }
+            if (dv[0] <= 32 && dv[1] <= 32) {
+                // both rows into registers, then the stage goes back
+                RowLd<float> R[2];
+#pragma unroll
+                for (int r = 0; r < 2; ++r) {
+                    const bool on = (uint32_t)lane < dv[r];
+#pragma unroll
+                    for (int c = 0; c < 9; ++c) R[r].m[c] = on ? sK[kidx(rbv[r], dv[r], lane, c) - kbase] : 0.f;
+                    R[r].j = on ? sC[rbv[r] + lane - cbase] : 0u;
+                }
+                __syncwarp();
+                if (lane == 0) bulk::mbar_arrive(&empty[slot]);
+#pragma unroll
+                for (int r = 0; r < 2; ++r) {
+                    if (r < nmine) {
+                        const float val = row_fast(R[r], (uint32_t)lane < dv[r], x, lane);
+                        if (writer) {
+                            const uint64_t i = (uint64_t)kBV * (I0 + r) + v;
+                            y[i] = val;
+                            acc = fmaf(x[i], val, acc);
+                        }
+                    }
+                }
+            } else {
+                for (int r = 0; r < nmine; ++r) {
+                    float a[16];
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) a[i] = 0.f;
+                    for (uint32_t c0 = 0; c0 < dv[r]; c0 += 32) {
+                        const uint32_t bl = c0 + lane;
+                        if (bl < dv[r]) {
+                            float m[9];
+#pragma unroll
+                            for (int c = 0; c < 9; ++c) m[c] = sK[kidx(rbv[r], dv[r], bl, c) - kbase];
+                            float xv[kBV];
+                            Node12<float>::load(x, sC[rbv[r] + bl - cbase], xv);
+#pragma unroll
+                            for (int q4 = 0; q4 < kBR; ++q4)
+                                block_fma(m, xv[3 * q4], xv[3 * q4 + 1], xv[3 * q4 + 2], a[3 * q4], a[3 * q4 + 1],
+                                          a[3 * q4 + 2]);
+                        }
+                    }
+                    const float val = reduce_scatter16(a, lane);
+                    if (writer) {
+                        const uint64_t i = (uint64_t)kBV * (I0 + r) + v;
+                        y[i] = val;
+                        acc = fmaf(x[i], val, acc);
+                    }
+                }
+                __syncwarp();
+                if (lane == 0) bulk::mbar_arrive(&empty[slot]);
+            }
+            if (last) {
+                // this warp's per-rhs totals of the unit, committed without a CTA barrier
+                const BTile t = B.tiles[B.groups[unit]];
+                double sv[kBR], tot[kBR];
+#pragma unroll
+                for (int r = 0; r < kBR; ++r) sv[r] = (double)warp_sum(my_r == r ? acc : 0.f);
+                acc = 0.f;
+                if (warp_commit_w(B, unit, t.sys, warp, sv, B.tk, tot) && lane < kBR) {
+                    const uint32_t kk = kBR * t.sys + lane;
+                    const double val = pick(tot, lane);
+                    B.pq[kk] = val;
+                    const double al = B.rz[kk] / (val + (val == 0.0 ? 1.0 : 0.0));
+                    B.alpha[kk] = al;
+                    B.alpha32[kk] = (float)al;
+                }
             }
         }
     }
@@ -489,7 +739,10 @@ __global__ void k_b_deinterleave(const double *__restrict__ src, double *__restr
 // ---- host ----------------------------------------------------------------------------------
 struct BatchState {
     int tile_rows = 0;
+    int unit_rows = 0;             // k_b_rows_bulk: rows per CTA unit (a multiple of tile_rows)
     std::vector<BTile> h_tiles;
+    std::vector<uint32_t> h_groups, h_sys_g;
+    DBuf<uint32_t> groups, sys_g;
     std::vector<uint32_t> h_tile_off;
     DBuf<BTile> tiles;
     DBuf<uint32_t> tile_off;
@@ -497,13 +750,14 @@ struct BatchState {
     DBuf<unsigned> tk;
     DBuf<double> dscal;  // 9 arrays of 4 nsys doubles
     DBuf<float> fscal;   // alpha32, beta32
-    DBuf<int> iscal;     // iter, done, status (4 nsys each), sys_done (nsys), n_active (1)
-    int *h_active = nullptr;  // pinned
+    DBuf<int> iscal;     // iter, done, status (4 nsys each), sys_done (nsys), n_active, fault
+    int *h_active = nullptr;  // pinned: n_active, fault
     int nrhs = 0;
     DBuf<double> F4, U4, R64, Z64, P64, Q64;
     DBuf<float> R32, Z32, P32, Q32, D32;
-    int pipe = 1;                  // SpMV variant (k_b_rows kPipe)
-    std::vector<double> tuned_ms;  // SpMV ms per candidate (variant-major, tile sizes 32..256)
+    int pipe = 1;                  // SpMV variant: k_b_rows kPipe 0 / 1, 2 = k_b_rows_bulk (FP32)
+    int bulk_grid = 0;             // resident grid of k_b_rows_bulk
+    std::vector<double> tuned_ms;  // SpMV ms per candidate (variant-major, 4 tile sizes each)
     ~BatchState() {
         if (h_active) cudaFreeHost(h_active);
     }
@@ -520,6 +774,9 @@ static BDev bdev(lmtg_ctx *c, int maxit) {
     BDev B{};
     B.tiles = S.tiles.p;
     B.ntiles = (uint32_t)S.h_tiles.size();
+    B.groups = S.groups.p;
+    B.sys_g = S.sys_g.p;
+    B.ngroups = S.h_groups.empty() ? 0u : (uint32_t)S.h_groups.size() - 1;
     B.tile_off = S.tile_off.p;
     B.partials = S.partials.p;
     B.tk = S.tk.p;
@@ -532,6 +789,7 @@ static BDev bdev(lmtg_ctx *c, int maxit) {
     B.beta32 = S.fscal.p + np;
     int *q = S.iscal.p;
     B.iter = q; B.done = q + np; B.status = q + 2 * np; B.sys_done = q + 3 * np; B.n_active = q + 3 * np + c->nsys;
+    B.fault = B.n_active + 1;
     B.maxit = maxit;
     return B;
 }
@@ -548,7 +806,24 @@ static void build_tiles(lmtg_ctx *c, int rows) {
     }
     upload_u32(c, S.tiles, S.h_tiles.data(), S.h_tiles.size());
     upload_u32(c, S.tile_off, S.h_tile_off.data(), S.h_tile_off.size());
-    S.partials.alloc(S.h_tiles.size() * kBSlots);
+    S.partials.alloc(S.h_tiles.size() * kBTileSlots);
+    LMTG_CUDA(cudaStreamSynchronize(c->stream));
+}
+
+// Units of k_b_rows_bulk: runs of `per` consecutive tiles of one system.
+static void build_groups(lmtg_ctx *c, int per) {
+    BatchState &S = *c->batch;
+    S.unit_rows = per * S.tile_rows;
+    S.h_groups.clear();
+    S.h_sys_g.clear();
+    for (uint32_t m = 0; m < c->nsys; ++m) {
+        S.h_sys_g.push_back((uint32_t)S.h_groups.size());
+        for (uint32_t t = S.h_tile_off[m]; t < S.h_tile_off[m + 1]; t += per) S.h_groups.push_back(t);
+    }
+    S.h_sys_g.push_back((uint32_t)S.h_groups.size());
+    S.h_groups.push_back((uint32_t)S.h_tiles.size());
+    upload_u32(c, S.groups, S.h_groups.data(), S.h_groups.size());
+    upload_u32(c, S.sys_g, S.h_sys_g.data(), S.h_sys_g.size());
     LMTG_CUDA(cudaStreamSynchronize(c->stream));
 }
 
@@ -560,9 +835,30 @@ static int bgrid(lmtg_ctx *c, KF kernel) {
     return (int)std::max<uint64_t>(1, std::min<uint64_t>((nt + kBWarps - 1) / kBWarps, (uint64_t)c->sm_count * nb));
 }
 
+constexpr int kBBulkStages = 2, kBBulkCap = 512, kBBulkMinB = 4;
+
+static int bulk_rows_grid(lmtg_ctx *c) {
+    constexpr size_t smem = bulk_smem_bytes<kBBulkStages, kBBulkCap>();
+    auto fn = k_b_rows_bulk<kBBulkStages, kBBulkCap, kBBulkMinB>;
+    LMTG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int nb = 0;
+    LMTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, kBBulkThreads, smem));
+    const uint64_t nt = c->batch->h_groups.size() - 1;  // one CTA per unit at a time
+    return (int)std::max<uint64_t>(1, std::min<uint64_t>(nt, (uint64_t)c->sm_count * (nb > 0 ? nb : 1)));
+}
+
 template <class T, int kMode>
 static void launch_rows(lmtg_ctx *c, const BDev &B, int pipe, const T *K, const T *x, const T *b, T *y,
                         cudaStream_t s) {
+    if constexpr (std::is_same<T, float>::value && kMode == 0) {
+        if (pipe == 2) {
+            k_b_rows_bulk<kBBulkStages, kBBulkCap, kBBulkMinB>
+                <<<c->batch->bulk_grid, kBBulkThreads, bulk_smem_bytes<kBBulkStages, kBBulkCap>(), s>>>(
+                    B, c->bptr.p, c->bcol.p, K, x, y);
+            c->launches += 1;
+            return;
+        }
+    }
     if (pipe)
         k_b_rows<T, kMode, 1><<<bgrid(c, k_b_rows<T, kMode, 1>), kBThreads, 0, s>>>(B, c->bptr.p, c->bcol.p, K, x,
                                                                                       b, y);
@@ -582,21 +878,30 @@ static void autotune(lmtg_ctx *c) {
     DBuf<double> x64, y64;
     if (f32) { x32.alloc(nv); y32.alloc(nv); LMTG_CUDA(cudaMemsetAsync(x32.p, 0, nv * 4, c->stream)); }
     else { x64.alloc(nv); y64.alloc(nv); LMTG_CUDA(cudaMemsetAsync(x64.p, 0, nv * 8, c->stream)); }
-    const int cands[4] = {16, 32, 64, 128};
+    // variants 0, 1: rows per warp tile; variant 2: rows per CTA unit of 128-row tiles (the
+    // vector kernels keep one warp per 128-row tile)
+    const int cands[3][4] = {{16, 32, 64, 128}, {16, 32, 64, 128}, {128, 256, 512, 1024}};
+    constexpr int kUnitTile = 128;
     double best = 1e30;
     int best_rows = 32, best_pipe = 1;
     S.tuned_ms.clear();
     cudaEvent_t e0, e1;
     LMTG_CUDA(cudaEventCreate(&e0));
     LMTG_CUDA(cudaEventCreate(&e1));
-    for (int pipe = 0; pipe < 2; ++pipe) {
-        for (int rows : cands) {
+    for (int pipe = 0; pipe < 3; ++pipe) {
+        for (int rows : cands[pipe]) {
             if ((c->batch_tile_rows > 0 && rows != c->batch_tile_rows) ||
-                (c->batch_variant >= 0 && pipe != c->batch_variant)) {
+                (c->batch_variant >= 0 && pipe != c->batch_variant) || (pipe == 2 && !f32)) {
                 S.tuned_ms.push_back(0.0);
                 continue;
             }
-            build_tiles(c, rows);
+            if (pipe == 2) {
+                if (S.tile_rows != kUnitTile) build_tiles(c, kUnitTile);
+                build_groups(c, rows / kUnitTile);
+                S.bulk_grid = bulk_rows_grid(c);
+            } else {
+                build_tiles(c, rows);
+            }
             BDev B = bdev(c, 1);
             // every system running: sys_done = 0, n_active = nsys
             LMTG_CUDA(cudaMemsetAsync(B.sys_done, 0, sizeof(int) * c->nsys, c->stream));
@@ -625,7 +930,11 @@ static void autotune(lmtg_ctx *c) {
     S.pipe = best_pipe;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    if (best_rows != S.tile_rows) build_tiles(c, best_rows);
+    const int tile = best_pipe == 2 ? kUnitTile : best_rows;
+    if (tile != S.tile_rows) build_tiles(c, tile);
+    build_groups(c, best_pipe == 2 ? best_rows / kUnitTile : 1);
+    S.bulk_grid = bulk_rows_grid(c);
+    LMTG_CUDA(cudaMemsetAsync(bdev(c, 1).fault, 0, sizeof(int), c->stream));
 }
 
 static void batch_prepare(lmtg_ctx *c) {
@@ -638,12 +947,12 @@ static void batch_prepare(lmtg_ctx *c) {
     S.dscal.alloc(9 * np);
     S.fscal.alloc(2 * np);
     LMTG_CUDA(cudaMemsetAsync(S.fscal.p, 0, 2 * np * sizeof(float), c->stream));
-    S.iscal.alloc(3 * np + c->nsys + 1);
+    S.iscal.alloc(3 * np + c->nsys + 2);
     S.tk.alloc(4ull * c->nsys);
     LMTG_CUDA(cudaMemsetAsync(S.dscal.p, 0, 9 * np * sizeof(double), c->stream));
-    LMTG_CUDA(cudaMemsetAsync(S.iscal.p, 0, (3 * np + c->nsys + 1) * sizeof(int), c->stream));
+    LMTG_CUDA(cudaMemsetAsync(S.iscal.p, 0, (3 * np + c->nsys + 2) * sizeof(int), c->stream));
     LMTG_CUDA(cudaMemsetAsync(S.tk.p, 0, 4ull * c->nsys * sizeof(unsigned), c->stream));
-    if (!S.h_active) LMTG_CUDA(cudaMallocHost(&S.h_active, sizeof(int)));
+    if (!S.h_active) LMTG_CUDA(cudaMallocHost(&S.h_active, 2 * sizeof(int)));
     const uint64_t nv = (uint64_t)kBV * c->nn;
     S.F4.alloc(nv);
     S.U4.alloc(nv);
@@ -708,19 +1017,23 @@ static int batch_pcg_run(lmtg_ctx *c, BDev B, const T *K, const T *Dinv, T *x, T
     }
     int status = LMTG_OK;
     BatchState &S = *c->batch;
-    LMTG_CUDA(cudaMemcpyAsync(S.h_active, B.n_active, sizeof(int), cudaMemcpyDeviceToHost, s));
+    LMTG_CUDA(cudaMemcpyAsync(S.h_active, B.n_active, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
     LMTG_CUDA(cudaStreamSynchronize(s));
     const int max_chunks = B.maxit / kBIters + 2;
-    for (int ch = 0; ch < max_chunks && *S.h_active > 0; ++ch) {
+    for (int ch = 0; ch < max_chunks && S.h_active[0] > 0; ++ch) {
         ce = cudaGraphLaunch(exec, s);
         c->launches += 2 * kBIters;  // + the SpMV launches counted at capture
         if (ce == cudaSuccess)
-            ce = cudaMemcpyAsync(S.h_active, B.n_active, sizeof(int), cudaMemcpyDeviceToHost, s);
+            ce = cudaMemcpyAsync(S.h_active, B.n_active, 2 * sizeof(int), cudaMemcpyDeviceToHost, s);
         if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
         if (ce != cudaSuccess) {
             cudaGraphExecDestroy(exec);
             cudaGraphDestroy(graph);
             throw Error{LMTG_ERR_CUDA, std::string("batched pcg: ") + cudaGetErrorString(ce)};
+        }
+        if (S.h_active[1] != 0) {  // a bounded wait of the SpMV gave up: results are not valid
+            status = LMTG_ERR_TIMEOUT;
+            break;
         }
         if (deadline_s > 0 &&
             std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count() > deadline_s) {
@@ -728,7 +1041,7 @@ static int batch_pcg_run(lmtg_ctx *c, BDev B, const T *K, const T *Dinv, T *x, T
             break;
         }
     }
-    if (status == LMTG_OK && *S.h_active > 0) status = LMTG_ERR_NOT_CONVERGED;
+    if (status == LMTG_OK && S.h_active[0] > 0) status = LMTG_ERR_NOT_CONVERGED;
     cudaGraphExecDestroy(exec);
     cudaGraphDestroy(graph);
     return status;
@@ -910,7 +1223,7 @@ void batch_get_result(lmtg_ctx *c, double *X_host) {
 void batch_info(lmtg_ctx *c, int *tile_rows, int *variant, uint64_t *ntiles, double *tuned_ms) {
     batch_prepare(c);
     BatchState &S = *c->batch;
-    if (tile_rows) *tile_rows = S.tile_rows;
+    if (tile_rows) *tile_rows = S.pipe == 2 ? S.unit_rows : S.tile_rows;
     if (variant) *variant = S.pipe;
     if (ntiles) *ntiles = S.h_tiles.size();
     if (tuned_ms)

@@ -95,7 +95,7 @@ def test_batch_equals_single_system_solves():
 def test_batch_autotuner_reports_candidates():
     bf, _, B = build([3, 3, 4], 5, mixed=True)
     info = bf.batch_info()
-    assert info["tile_rows"] in (16, 32, 64, 128) and info["variant"] in (0, 1)
+    assert info["tile_rows"] in (16, 32, 64, 128, 256, 512, 1024) and info["variant"] in (0, 1, 2)
     assert all(v > 0 for v in info["tuned_spmv_ms"].values())
     # a fixed choice is honoured and still solves
     bf.set_options(tile_rows=32, variant=0)
@@ -103,6 +103,29 @@ def test_batch_autotuner_reports_candidates():
     assert bf.batch_info()["tile_rows"] == 32 and bf.batch_info()["variant"] == 0
     assert st["rel_residual"] <= 1e-10
     assert info["ntiles"] >= 3
+    bf.close()
+
+
+@pytest.mark.parametrize("tile_rows", [128, 256, 1024])
+def test_batch_bulk_copy_spmv_matches_oracle_and_warp_tiles(tile_rows):
+    """SpMV variant 2 (matrix streamed by bulk copies, one CTA per tile) solves like the warp
+    tiles (variant 1) and matches the oracle's direct solves; uneven meshes, four rhs."""
+    sides = [2, 6, 3, 5, 2, 4]
+    bf, probs, B = build(sides, 13, mixed=True)
+    bf.set_options(tile_rows=min(tile_rows, 128), variant=1)
+    X1, _, _ = bf.solve_batch(B, mode="mixed", tol=1e-12)
+    bf.set_options(tile_rows=tile_rows, variant=2)
+    X2, st, its = bf.solve_batch(B, mode="mixed", tol=1e-12)
+    assert bf.batch_info()["variant"] == 2 and bf.batch_info()["tile_rows"] == tile_rows
+    assert st["rel_residual"] <= 1e-12, st
+    assert np.linalg.norm(X2 - X1) <= 1e-9 * np.linalg.norm(X1)
+    for m, p in enumerate(probs):
+        P = p["P"]
+        for r in range(4):
+            x = O.skyline_solve(P["rowptr"], P["col"], P["val"], p["F"][r])
+            assert np.linalg.norm(X2[r, bf.dofs(m)] - x) <= 1e-8 * np.linalg.norm(x), (m, r)
+    X3, _, _ = bf.solve_batch(B, mode="mixed", tol=1e-12)
+    assert np.array_equal(X3, X2)  # deterministic
     bf.close()
 
 
@@ -118,6 +141,15 @@ def test_batch_of_tetra10_meshes_matches_oracle():
     bf.add_constraints(np.concatenate([P["dofs"] + 3 * int(bf.node_off[m]) for m, P in enumerate(probs)]), 1e5)
     bf.assemble(True, False, mixed=True)
     B = rng.standard_normal((4, bf.n))
+    for variant in (1, 2):
+        bf.set_options(tile_rows=0, variant=variant)
+        X, st, its = bf.solve_batch(B, mode="mixed", tol=1e-12)
+        for m, P in enumerate(probs):
+            d = bf.dofs(m)
+            for r in range(4):
+                x = O.skyline_solve(P["rowptr"], P["col"], P["val"], B[r, d])
+                assert np.linalg.norm(X[r, d] - x) <= 1e-8 * np.linalg.norm(x), (variant, m, r)
+    bf.set_options(tile_rows=0, variant=-1)
     for mode, tol in (("mixed", 1e-8), ("fp64", 1e-10)):
         X, st, its = bf.solve_batch(B, mode=mode, tol=1e-13 if mode == "fp64" else 1e-12)
         for m, P in enumerate(probs):
