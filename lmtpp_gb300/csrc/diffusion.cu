@@ -14,6 +14,7 @@
 // One unknown per node: the node-block pattern of pattern.cu is the scalar CSR pattern; a row
 // holds ~9-19 entries, so the SpMV uses 8 lanes per row (4 rows per warp).
 #include <algorithm>
+#include <type_traits>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -21,7 +22,7 @@
 #include <new>
 #include <vector>
 
-#include "solver_kernels.cuh"
+#include "spmv_bulk.cuh"
 
 namespace lmtg {
 
@@ -331,6 +332,185 @@ __global__ void __launch_bounds__(kRowThreads)
     }
 }
 
+// q = K p and p.q (FP32) with the matrix streamed through shared memory by bulk copies (TMA).
+// Each CTA owns a contiguous range of 32-row chunks.  One producer warp copies, per stage, the
+// entries (values, columns) and the row pointers of up to 8 chunks whose entries fit kCap into
+// a ring of kStages stages (evict-first L2 policy).  Consumer warp w takes chunk w of a stage:
+// its lanes form the products K_q p[col_q] over the chunk's entries (coalesced, in place), then
+// lane l sums row l's products in column order and the stage goes back.  The products and
+// their order are the ones of csr_stream32, so q is bit-identical to k_pcg_spmv_s; p.q is
+// summed in another fixed order.  Every wait is bounded; one that gives up sets
+// LMTG_ERR_TIMEOUT and done in the PCG scalars.
+constexpr int kSBulkCons = 8;
+constexpr int kSBulkThreads = 32 * (kSBulkCons + 1);
+
+template <int kCap>
+struct SBulkStage {
+    static_assert(kCap % 4 == 0, "16-byte stage parts");
+    static constexpr uint32_t kKBytes = 4u * kCap + 32u;
+    static constexpr uint32_t kCBytes = 4u * kCap + 32u;
+    static constexpr uint32_t kRBytes = 4u * (32 * kSBulkCons + 1) + 32u + 12u;  // rounded to 16
+    static constexpr uint32_t kBytes = kKBytes + kCBytes + kRBytes;
+    static_assert(kRBytes % 16 == 0 && kBytes % 16 == 0, "16-byte stage parts");
+};
+template <int kStages, int kCap>
+constexpr size_t sbulk_smem_bytes() {
+    return (size_t)kStages * SBulkStage<kCap>::kBytes;
+}
+
+template <int kStages, int kCap>
+__global__ void __launch_bounds__(kSBulkThreads, 4)
+    k_pcg_spmv_s_bulk(const uint32_t *__restrict__ rp, const uint32_t *__restrict__ col,
+                      const float *__restrict__ K, const float *__restrict__ p, float *__restrict__ q,
+                      uint64_t n, PcgScalars *S, double *partials) {
+    using St = SBulkStage<kCap>;
+    if (*(volatile int *)&S->done) return;
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ uint64_t full[kStages], empty[kStages];
+    __shared__ uint64_t meta[kStages][4];  // first row, end row, first value index, first rp index
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const ChunkRange cr = cta_chunks(n);
+    const uint64_t row0 = 32 * cr.first, row_end = min(n, 32 * cr.end);
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < kStages; ++i) {
+            bulk::mbar_init(&full[i], 1);
+            bulk::mbar_init(&empty[i], kSBulkCons);
+        }
+        bulk::fence_barrier_init();
+    }
+    __syncthreads();
+    float acc = 0.f;
+    if (warp == kSBulkCons) {
+        // ---------------- producer ----------------
+        uint64_t g0 = row0;
+        uint32_t e0 = row0 < row_end ? rp[row0] : 0u;
+        uint32_t k = 0;
+        bool failed = false;
+        for (;; ++k) {
+            const int slot = k % kStages;
+            if (k >= (uint32_t)kStages) {
+                const bool ok = bulk::mbar_wait(&empty[slot], ((k / kStages) - 1) & 1u);
+                if (!__all_sync(0xffffffffu, ok)) {
+                    failed = true;
+                    break;
+                }
+            }
+            if (g0 >= row_end) {
+                if (lane == 0) {
+                    meta[slot][0] = g0;
+                    meta[slot][1] = g0;
+                    bulk::mbar_arrive(&full[slot]);
+                }
+                break;
+            }
+            // chunk ends g0 + 32 (l + 1) (clamped to row_end) for lanes l < 8
+            const bool in = lane < kSBulkCons && g0 + (uint64_t)(32 * lane) < row_end;
+            const uint64_t ge = min(row_end, g0 + (uint64_t)(32 * (lane + 1)));
+            const uint32_t ei = in ? rp[ge] : 0u;
+            const unsigned fits = __ballot_sync(0xffffffffu, in && ei - e0 <= (uint32_t)kCap);
+            const int nch = __popc(fits);
+            if (nch == 0) {  // a chunk wider than a stage (the host checks this before launching)
+                failed = true;
+                break;
+            }
+            const uint32_t e1 = __shfl_sync(0xffffffffu, ei, nch - 1);
+            const uint64_t g1 = min(row_end, g0 + (uint64_t)(32 * nch));
+            if (lane == 0) {
+                const uint64_t kb0 = (4ull * e0) & ~15ull, kb1 = (4ull * e1 + 15ull) & ~15ull;
+                const uint64_t rb0 = (4ull * g0) & ~15ull, rb1 = (4ull * (g1 + 1) + 15ull) & ~15ull;
+                meta[slot][0] = g0;
+                meta[slot][1] = g1;
+                meta[slot][2] = kb0 / 4;
+                meta[slot][3] = rb0 / 4;
+                unsigned char *dst = smem + (size_t)slot * St::kBytes;
+                const uint64_t pol = bulk::policy_evict_first();
+                __threadfence_block();
+                bulk::mbar_arrive_expect_tx(&full[slot], (uint32_t)(2 * (kb1 - kb0) + (rb1 - rb0)));
+                bulk::copy_g2s_hint(dst, reinterpret_cast<const unsigned char *>(K) + kb0, (uint32_t)(kb1 - kb0),
+                                    &full[slot], pol);
+                bulk::copy_g2s_hint(dst + St::kKBytes, reinterpret_cast<const unsigned char *>(col) + kb0,
+                                    (uint32_t)(kb1 - kb0), &full[slot], pol);
+                bulk::copy_g2s_hint(dst + St::kKBytes + St::kCBytes, reinterpret_cast<const unsigned char *>(rp) + rb0,
+                                    (uint32_t)(rb1 - rb0), &full[slot], pol);
+            }
+            g0 = g1;
+            e0 = e1;
+        }
+        if (failed && lane == 0) {
+            atomicExch(&S->status, LMTG_ERR_TIMEOUT);
+            atomicExch(&S->done, 1);
+            const uint32_t first = k > (uint32_t)kStages ? k - kStages : 0u;
+            for (uint32_t s2 = first; s2 < k; ++s2) bulk::mbar_wait(&full[s2 % kStages], (s2 / kStages) & 1u);
+        }
+    } else {
+        // ---------------- consumers ----------------
+        for (uint32_t k = 0;; ++k) {
+            const int slot = k % kStages;
+            const bool ok = bulk::mbar_wait(&full[slot], (k / kStages) & 1u);
+            if (!__all_sync(0xffffffffu, ok)) {
+                if (lane == 0) {
+                    atomicExch(&S->status, LMTG_ERR_TIMEOUT);
+                    atomicExch(&S->done, 1);
+                }
+                break;
+            }
+            const uint64_t g0 = meta[slot][0], g1 = meta[slot][1];
+            if (g0 == g1) break;
+            float *sK = reinterpret_cast<float *>(smem + (size_t)slot * St::kBytes);
+            const uint32_t *sC = reinterpret_cast<const uint32_t *>(smem + (size_t)slot * St::kBytes + St::kKBytes);
+            const uint32_t *sR =
+                reinterpret_cast<const uint32_t *>(smem + (size_t)slot * St::kBytes + St::kKBytes + St::kCBytes);
+            const uint64_t kbase = meta[slot][2], rbase = meta[slot][3];
+            const uint64_t R0 = g0 + (uint64_t)(32 * warp);
+            if (R0 < g1) {
+                const uint64_t R1 = min(g1, R0 + (uint64_t)32);
+                const uint32_t E0 = sR[R0 - rbase], E1 = sR[R1 - rbase];
+                for (uint32_t t0 = E0; t0 < E1; t0 += kTile) {
+                    float kv[kTileChunks], xv[kTileChunks];
+                    uint32_t cj[kTileChunks];
+#pragma unroll
+                    for (int c = 0; c < kTileChunks; ++c) {
+                        const uint32_t qq = t0 + 32 * c + lane;
+                        const bool on = qq < E1;
+                        kv[c] = on ? sK[qq - kbase] : 0.f;
+                        cj[c] = on ? sC[qq - kbase] : 0u;
+                    }
+#pragma unroll
+                    for (int c = 0; c < kTileChunks; ++c) xv[c] = t0 + 32 * c + lane < E1 ? __ldg(p + cj[c]) : 0.f;
+#pragma unroll
+                    for (int c = 0; c < kTileChunks; ++c) {
+                        const uint32_t qq = t0 + 32 * c + lane;
+                        if (qq < E1) sK[qq - kbase] = kv[c] * xv[c];
+                    }
+                }
+                __syncwarp();
+                const uint64_t I = R0 + lane;
+                float v = 0.f;
+                if (I < R1) {
+                    const uint32_t rs = sR[I - rbase], re = sR[I + 1 - rbase];
+                    for (uint32_t qq = rs; qq < re; ++qq) v += sK[qq - kbase];
+                }
+                __syncwarp();
+                if (lane == 0) bulk::mbar_arrive(&empty[slot]);
+                if (I < R1) {
+                    q[I] = v;
+                    acc = fmaf(p[I], v, acc);
+                }
+            } else {
+                __syncwarp();
+                if (lane == 0) bulk::mbar_arrive(&empty[slot]);
+            }
+        }
+    }
+    __syncthreads();
+    const float t[1] = {acc};
+    double out[1];
+    if (grid_reduce_t<1, 0u>(t, partials, &S->cnt_a, out) && threadIdx.x == 0) {
+        S->pq = out[0];
+        S->alpha = S->rz / (out[0] + (out[0] == 0.0 ? 1.0 : 0.0));
+    }
+}
+
 template <class T>
 __global__ void k_pcg_update_s(T *__restrict__ x, T *__restrict__ r, T *__restrict__ z,
                                const T *__restrict__ p, const T *__restrict__ q,
@@ -470,13 +650,37 @@ static int diff_pcg_t(lmtg_ctx *c, const T *K, const T *Dinv, const T *b, T *x, 
     }
     constexpr int kIters = 16;  // iterations per graph launch
     const int gr = rgrid(c, k_pcg_spmv_s<T>);
+    // FP32: the bulk-copy SpMV unless spmv_kind 0 or a 32-row chunk could exceed a stage
+    constexpr int kSStages = 2, kSCap = 3072;
+    const bool sbulk = std::is_same<T, float>::value && c->spmv_kind != 0 &&
+                       32ull * c->max_row_blocks <= (uint64_t)kSCap;
+    int gr_bulk = 0;
+    if (sbulk) {
+        constexpr size_t smem = sbulk_smem_bytes<kSStages, kSCap>();
+        LMTG_CUDA(cudaFuncSetAttribute(k_pcg_spmv_s_bulk<kSStages, kSCap>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int nb = 0;
+        LMTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_pcg_spmv_s_bulk<kSStages, kSCap>,
+                                                                kSBulkThreads, smem));
+        gr_bulk = c->sm_count * (nb > 0 ? nb : 1);
+    }
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     LMTG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < kIters; ++k) {
         k_pcg_dir_s<T><<<ngrid(c), kRowThreads, 0, s>>>(z, p, c->nn, c->scal.p);
-        k_pcg_spmv_s<T><<<gr, kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, K, p, q, c->nn, c->scal.p,
-                                                   c->partials.p);
+        if constexpr (std::is_same<T, float>::value) {
+            if (sbulk)
+                k_pcg_spmv_s_bulk<kSStages, kSCap>
+                    <<<gr_bulk, kSBulkThreads, sbulk_smem_bytes<kSStages, kSCap>(), s>>>(
+                        c->bptr.p, c->bcol.p, K, p, q, c->nn, c->scal.p, c->partials.p);
+            else
+                k_pcg_spmv_s<T><<<gr, kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, K, p, q, c->nn, c->scal.p,
+                                                           c->partials.p);
+        } else {
+            k_pcg_spmv_s<T><<<gr, kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, K, p, q, c->nn, c->scal.p,
+                                                       c->partials.p);
+        }
         k_pcg_update_s<T><<<ngrid(c), kRowThreads, 0, s>>>(x, r, z, p, q, Dinv, c->nn, c->scal.p,
                                                            c->partials.p);
     }
@@ -616,7 +820,7 @@ void diff_setup(lmtg_ctx *c, const double *k, uint64_t nk, double rho_c, double 
         c->nnz_lower = (c->nnzb - c->nn) / 2 + c->nn;
         c->K64.alloc(c->nnzb);
         c->B64.alloc(c->nnzb);
-        c->K32.alloc(c->nnzb);
+        c->K32.alloc(c->nnzb + 4);  // 16 bytes of slack: bulk copies round their end up
         c->Ke64.alloc(c->ne * kTriPairs);
         c->KeB64.alloc(c->ne * kTriPairs);
         c->F.alloc(c->nn);

@@ -274,7 +274,7 @@ void build_pattern(lmtg_ctx *c) {
     deg.alloc(nn + 1);
     k_nbr<false><<<grid_for(c, nn, 128), 128, 0, s>>>(c->conn.p, c->npe, incptr.p, inc.p, nn,
                                                        deg.p, nullptr, nullptr, nullptr, bad.p);
-    c->bptr.alloc(nn + 1);
+    c->bptr.alloc(nn + 1 + 4);  // 16 bytes of slack: bulk copies round their end up
     c->nnzb = exclusive_scan_u32(c, deg.p, c->bptr.p, nn);
     int hb2[2] = {0, 0};
     LMTG_CUDA(cudaMemcpy(hb2, bad.p, 2 * sizeof(int), cudaMemcpyDeviceToHost));

@@ -108,6 +108,31 @@ def test_diffusion_mixed_solver_matches_oracle(theta):
     d.close()
 
 
+def test_diffusion_bulk_copy_spmv_matches_warp_streamed():
+    """The FP32 step solver with the TMA-streamed CSR SpMV (kind 1) and the warp-streamed one
+    (kind 0): both reach the oracle's states; kind 1 is deterministic."""
+    rng = np.random.default_rng(9)
+    P0 = O.diffusion_problem(33)
+    k = np.exp(0.3 * rng.standard_normal(P0["conn"].shape[0]))
+    P = O.diffusion_problem(33, k=k, theta=1.0)
+    states = O.diffusion_run(P, 6)
+    out = {}
+    for kind in (0, 1, 1):
+        d = Diffusion(P["pos"], P["conn"])
+        d.setup(k, rho_c=1.0, dt=1e-4, theta=1.0, dirichlet=boundary_nodes(P["pos"]), penalty=1e5)
+        d.set_solver("mixed")
+        d.set_spmv_kind(kind)
+        d.set_state(P["T0"])
+        d.run(6, tol=1e-12)
+        T = d.get_state()
+        assert np.linalg.norm(T - states[-1]) <= 1e-8 * np.linalg.norm(states[-1]), kind
+        if kind in out:
+            assert np.array_equal(T, out[kind])
+        out[kind] = T
+        d.close()
+    assert np.linalg.norm(out[1] - out[0]) <= 1e-9 * np.linalg.norm(out[0])
+
+
 def test_diffusion_mixed_adjoint_matches_fp64():
     rng = np.random.default_rng(11)
     pos, conn = make_rect_triangle6(13)
