@@ -314,6 +314,11 @@ int lmtg_set_inner_reduction(lmtg_ctx *ctx, double inner_reduction);
  * All give the same q; p.q is summed in a different fixed order.  No reference counterpart. */
 int lmtg_set_spmv_kind(lmtg_ctx *ctx, int kind);
 
+/* Self-test of the device-side wait bound used by the bulk-copy SpMVs: one thread waits on an
+ * mbarrier that nothing completes.  *status = LMTG_ERR_TIMEOUT when the wait gave up (about
+ * 1 s, *waited_s), and the context stays usable.  No reference counterpart. */
+int lmtg_selftest_bounded_wait(lmtg_ctx *ctx, int *status, double *waited_s);
+
 /* Element fields after the solve (replaces the generated apply_on_elements_after_solve of
  * elasticity_iso, formulations/formulation_elasticity_iso.py:64-85, run by call_after_solve,
  * include/formulation/formulation.h:1867-1875): per element, at var_inter = 0.5, out[13 e + k] =

@@ -12,6 +12,7 @@
 #include <new>
 
 #include "lmtg_internal.cuh"
+#include "spmv_bulk.cuh"
 
 using namespace lmtg;
 
@@ -457,6 +458,36 @@ int lmtg_set_inner_reduction(lmtg_ctx *c, double inner_reduction) {
     return guard(c, [&] {
         LMTG_CHECK(inner_reduction > 0 && inner_reduction < 1, LMTG_ERR_ARG, "inner_reduction in (0, 1)");
         c->inner_reduction = inner_reduction;
+        return LMTG_OK;
+    });
+}
+
+// Self-test of the bound: one thread waits on an mbarrier that nothing arrives on.  out[0] =
+// LMTG_ERR_TIMEOUT if the wait gave up (LMTG_OK if it completed), out[1] = ns waited.
+__global__ void k_selftest_bounded_wait(long long *out) {
+    using namespace lmtg::bulk;
+    __shared__ uint64_t bar;
+    if (threadIdx.x != 0) return;
+    mbar_init(&bar, 1);
+    fence_barrier_init();
+    const uint64_t t0 = globaltimer_ns();
+    const bool ok = mbar_wait(&bar, 0);
+    out[0] = ok ? LMTG_OK : LMTG_ERR_TIMEOUT;
+    out[1] = (long long)(globaltimer_ns() - t0);
+}
+
+int lmtg_selftest_bounded_wait(lmtg_ctx *c, int *status, double *waited_s) {
+    return guard(c, [&] {
+        DBuf<long long> out;
+        out.alloc(2);
+        k_selftest_bounded_wait<<<1, 32, 0, c->stream>>>(out.p);
+        c->launches += 1;
+        LMTG_CUDA(cudaGetLastError());
+        long long h[2] = {0, 0};
+        LMTG_CUDA(cudaMemcpyAsync(h, out.p, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+        LMTG_CUDA(cudaStreamSynchronize(c->stream));
+        if (status) *status = (int)h[0];
+        if (waited_s) *waited_s = 1e-9 * (double)h[1];
         return LMTG_OK;
     });
 }

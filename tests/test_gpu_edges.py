@@ -240,3 +240,22 @@ def test_skin_pressure_matches_oracle(elem):
         O.quad4_traction(faces, pos, (2.5, 0.0, 0.0), Ft)
         np.testing.assert_allclose(Fo, Ft, rtol=0, atol=1e-13)
     f.close()
+
+
+def test_device_wait_bound_gives_up_and_context_stays_usable():
+    """The mbarrier waits of the bulk-copy SpMVs are bounded: a wait that nothing completes
+    returns a timeout status after about a second, and the context then solves as before."""
+    import ctypes
+    P = O.elasticity_problem(4)
+    f = problem(P)
+    st = ctypes.c_int(-1)
+    waited = ctypes.c_double(0.0)
+    abi.check(f._lib.lmtg_selftest_bounded_wait(f._ctx, ctypes.byref(st), ctypes.byref(waited)), f._ctx,
+              "selftest_bounded_wait")
+    assert st.value == abi.ERR_TIMEOUT
+    assert 0.5 <= waited.value <= 10.0, waited.value
+    f.solve(1e-12, mode="mixed")
+    u = f.get_result()
+    x = O.skyline_solve(P["rowptr"], P["col"], P["val"], P["F"])
+    assert np.linalg.norm(u - x) <= 1e-8 * np.linalg.norm(x)
+    f.close()
