@@ -346,6 +346,31 @@ int lmtg_fit_zone_moduli(lmtg_ctx *ctx, uint32_t nz, const uint32_t *zone_of_ele
 /* Sizes of the current problem. */
 int lmtg_get_sizes(lmtg_ctx *ctx, uint64_t *nn, uint64_t *ne, uint64_t *ndof, uint64_t *nnz_blocks);
 
+/* ---- mesh files next to the path (context-free host code, no GPU needed) ---- */
+
+/* Gmsh ASCII format-2 reader (replaces read_msh_2, include/mesh/read_msh_2.h:56-235).  Nodes in
+ * file order (pos: nn x dim, dim 3 for LMTG_ELEM_HEXA8 / LMTG_ELEM_TETRA10, 2 for
+ * LMTG_ELEM_TRIANGLE6); elements of the mesh's dimension in file order, in LMT++'s node order
+ * (Tetra_10: Gmsh's last two edge nodes swapped) and re-ordered by LMT++'s permutation when the
+ * Jacobian at var_inter = 0.5 is negative (permutation_if_jac_neg); lower-dimension elements
+ * (faces, edges, points) skipped; tag[e] = the element's first tag (0 without tags).  Call with
+ * pos = conn = tag = NULL to get nn and ne, then with buffers of those sizes (any may be NULL).
+ * LMTG_ERR_ARG: unreadable or corrupt file, unknown node number; LMTG_ERR_UNSUPPORTED: an
+ * element of the mesh's dimension of another type (mixed meshes). */
+int lmtg_read_msh(const char *path, int elem_type, uint64_t *nn, double *pos, uint64_t *ne, uint32_t *conn,
+                  double *tag);
+
+/* ASCII VTU file with the layout and number formatting of write_mesh_vtk<false>
+ * (include/mesh/write_mesh_vtk.h:434-655): npf point arrays (pnames[f], pncomp[f] components,
+ * pvals[f]: nn x pncomp[f]), then ncf cell arrays (cvals[f]: ne x cncomp[f]) of kind ckind[f]:
+ * 0 = element field, 1 = global field written per element, 2 = unsigned integer (the element
+ * group), each with the reference's separators; then points (z = 0 for 2D meshes), connectivity,
+ * offsets and VTK cell types (12 Hexa8, 24 Tetra10, 22 Triangle6) in LMT++'s node order. */
+int lmtg_write_vtu(const char *path, int elem_type, uint64_t nn, const double *pos, uint64_t ne,
+                   const uint32_t *conn, int npf, const char *const *pnames, const int *pncomp,
+                   const double *const *pvals, int ncf, const char *const *cnames, const int *cncomp,
+                   const int *ckind, const double *const *cvals);
+
 #ifdef __cplusplus
 }
 #endif

@@ -24,6 +24,8 @@ g++ $CFLAGS -std=gnu++98 -fpermissive -I"$SRC/include" -I"$SRC/include/amd" -I"$
 gcc -O2 -std=c99 -c "$HERE/fe_oracle.c" -o "$OUT/obj/fe_oracle.o" &
 g++ $CFLAGS -std=gnu++98 -fpermissive -I"$SRC/include" -I"$SRC/include/amd" -I"$SRC/include/LDL" -I"$HERE" \
     -c "$HERE/ref_driver.cpp" -o "$OUT/obj/ref_driver.o" &
+g++ $CFLAGS -std=gnu++98 -fpermissive -I"$SRC/include" "$HERE/ref_meshio.cpp" -o "$OUT/ref_meshio" &
+g++ $CFLAGS -std=gnu++98 -fpermissive -I"$SRC/include" "$HERE/ref_vtu_elast.cpp" -o "$OUT/ref_vtu_elast" &
 wait
 g++ -o "$OUT/ref_driver" "$OUT"/obj/*.o -lpthread
-echo "build_ref: $OUT/ref_driver"
+echo "build_ref: $OUT/ref_driver $OUT/ref_meshio $OUT/ref_vtu_elast"

@@ -51,3 +51,29 @@ def test_element_fields_of_the_solution_and_patch_test():
     again = f.element_fields()
     assert np.array_equal(again["sigma"], out["sigma"])
     f.close()
+
+
+def test_vtu_of_a_solved_formulation(tmp_path):
+    """write_vtu_elasticity: the displacement and the element fields of the solution, in the
+    layout of LMT++'s elasticity mesh (the writer itself is pinned byte-for-byte on the CPU)."""
+    import xml.etree.ElementTree as ET
+    from lmtpp_gb300 import meshio, x1_faces
+    pos, conn = make_rect_hexa(4)
+    f = Formulation(pos, conn)
+    f.elastic_modulus = 2.1e5
+    f.poisson_ratio = 0.3
+    clamped = np.nonzero(pos[:, 0] < 1e-6)[0]
+    f.add_constraints((3 * clamped[:, None] + np.arange(3)).ravel(), 1e5)
+    f.add_skin_traction(x1_faces(pos, conn), (1.0, 0.0, 0.0))
+    f.solve(1e-12, mode="mixed")
+    out = tmp_path / "sol.vtu"
+    meshio.write_vtu_elasticity(out, f)
+    piece = ET.parse(out).getroot().find("UnstructuredGrid/Piece")
+    arr = {a.get("Name"): np.array(a.text.split(), dtype=float) for a in piece.iter("DataArray") if a.get("Name")}
+    u = f.get_result()
+    assert np.allclose(arr["dep"], u, rtol=1e-5, atol=1e-6 * np.abs(u).max())
+    sig = f.element_fields()["sigma"]
+    assert np.allclose(arr["sigma"].reshape(-1, 6), sig, rtol=1e-5, atol=1e-6 * np.abs(sig).max())
+    assert [a.get("Name") for a in piece.find("CellData")] == [
+        "epsilon", "sigma", "tr_epsilon", "group", "elastic_modulus", "density", "poisson_ratio", "f_vol"]
+    f.close()
