@@ -15,13 +15,20 @@
 // per array with LMT++'s separators (node and global fields: each component followed by a
 // space, and one more space after a vector; element fields: a vector's components each
 // followed by a space, a scalar alone, then two spaces), cell connectivity 8 indices per line.
+#include <sys/stat.h>
+
+#include <charconv>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
-#include <map>
-#include <sstream>
+#include <iterator>
+#include <mutex>
+#include <ostream>
 #include <string>
+#include <string_view>
+#include <unordered_map>
 #include <vector>
 
 #include "lmtg.h"
@@ -88,70 +95,155 @@ struct ParsedMsh {
     uint64_t nn = 0, ne = 0;
 };
 
+// numbers of one line [p, e): blanks are spaces, tabs and '\r'; false when the line has none left
+inline bool next_token(const char *&p, const char *e) {
+    while (p < e && (*p == ' ' || *p == '\t' || *p == '\r')) ++p;
+    return p < e;
+}
+inline bool read_ll(const char *&p, const char *e, long long &v) {
+    if (!next_token(p, e)) return false;
+    char *q = nullptr;
+    v = std::strtoll(p, &q, 10);
+    if (q == p || q > e) return false;
+    p = q;
+    return true;
+}
+inline bool read_d(const char *&p, const char *e, double &v) {
+    if (!next_token(p, e)) return false;
+    char *q = nullptr;
+    v = std::strtod(p, &q);  // correctly rounded, as the stream extraction of the reference
+    if (q == p || q > e) return false;
+    p = q;
+    return true;
+}
+
 int parse_msh(const char *path, int elem_type, ParsedMsh &out) {
     int want_type, npe, dim;
     if (elem_type == LMTG_ELEM_HEXA8) { want_type = 5; npe = 8; dim = 3; }
     else if (elem_type == LMTG_ELEM_TETRA10) { want_type = 11; npe = 10; dim = 3; }
     else if (elem_type == LMTG_ELEM_TRIANGLE6) { want_type = 9; npe = 6; dim = 2; }
     else return LMTG_ERR_ARG;
-    std::ifstream is(path);
+    std::ifstream is(path, std::ios::binary);
     if (!is.is_open()) return LMTG_ERR_ARG;
-    std::map<long long, uint32_t> node_of;  // file number -> index in file order
-    std::string line;
+    std::string buf((std::istreambuf_iterator<char>(is)), std::istreambuf_iterator<char>());
+    std::unordered_map<long long, uint32_t> node_of;  // file number -> index in file order
     int section = 0;  // 1 nodes, 2 elements
-    bool ended = false;
-    while (std::getline(is, line)) {
-        if (line.find("$EndNodes") != std::string::npos) { section = 0; continue; }
-        if (line.find("$EndElements") != std::string::npos) { ended = true; break; }
-        if (line.find("$Nodes") != std::string::npos) { std::getline(is, line); section = 1; continue; }
-        if (line.find("$Elements") != std::string::npos) { std::getline(is, line); section = 2; continue; }
-        if (section == 1) {
-            std::istringstream s(line);
+    bool ended = false, skip_count = false;
+    const char *p0 = buf.c_str(), *end = p0 + buf.size();
+    for (const char *b = p0; b < end && !ended;) {
+        const char *e = static_cast<const char *>(std::memchr(b, '\n', end - b));
+        if (!e) e = end;
+        const std::string_view line(b, e - b);
+        const char *next = e < end ? e + 1 : end;
+        if (skip_count) {  // the count line after $Nodes / $Elements
+            skip_count = false;
+        } else if (line.find("$EndNodes") != std::string_view::npos) {
+            section = 0;
+        } else if (line.find("$EndElements") != std::string_view::npos) {
+            ended = true;
+        } else if (line.find("$Nodes") != std::string_view::npos) {
+            section = 1;
+            skip_count = true;
+        } else if (line.find("$Elements") != std::string_view::npos) {
+            section = 2;
+            skip_count = true;
+        } else if (section == 1) {
+            const char *q = b;
             long long num;
             double x[3] = {0, 0, 0};
-            if (!(s >> num)) return LMTG_ERR_ARG;
+            if (!read_ll(q, e, num)) return LMTG_ERR_ARG;
             for (int k = 0; k < dim; ++k)
-                if (!(s >> x[k])) return LMTG_ERR_ARG;
+                if (!read_d(q, e, x[k])) return LMTG_ERR_ARG;
             node_of[num] = (uint32_t)out.nn++;
             for (int k = 0; k < dim; ++k) out.pos.push_back(x[k]);
         } else if (section == 2) {
-            std::istringstream s(line);
-            long long num;
-            int type, ntags;
-            if (!(s >> num >> type >> ntags) || type < 1 || type > 19 || ntags < 0) return LMTG_ERR_ARG;
-            std::vector<double> tags(ntags);
-            for (int k = 0; k < ntags; ++k)
-                if (!(s >> tags[k])) return LMTG_ERR_ARG;
-            if (kMshDim[type - 1] != dim) continue;  // faces, edges, points of a volume mesh
-            if (type != want_type) return LMTG_ERR_UNSUPPORTED;
-            uint32_t v[10];
-            for (int a = 0; a < kMshNodes[type - 1]; ++a) {
-                long long nb;
-                if (!(s >> nb)) return LMTG_ERR_ARG;
-                auto it = node_of.find(nb);
-                if (it == node_of.end()) return LMTG_ERR_ARG;
-                v[a] = it->second;
+            const char *q = b;
+            long long num, type, ntags;
+            if (!read_ll(q, e, num) || !read_ll(q, e, type) || !read_ll(q, e, ntags) || type < 1 || type > 19 ||
+                ntags < 0 || ntags > 64)
+                return LMTG_ERR_ARG;
+            double tag0 = 0.0;
+            for (long long k = 0; k < ntags; ++k) {
+                double t;
+                if (!read_d(q, e, t)) return LMTG_ERR_ARG;
+                if (k == 0) tag0 = t;
             }
-            if (type == 11) std::swap(v[8], v[9]);
-            if (jacobian_det_half(elem_type, dim, out.pos, v, npe) < 0) {
-                static const int ph[8] = {0, 3, 2, 1, 4, 7, 6, 5};
-                static const int pt[10] = {0, 1, 3, 2, 4, 8, 7, 6, 5, 9};
-                static const int pr[6] = {5, 4, 3, 2, 1, 0};
-                const int *pm = type == 5 ? ph : type == 11 ? pt : pr;
-                uint32_t w[10];
-                for (int a = 0; a < npe; ++a) w[a] = v[pm[a]];
-                for (int a = 0; a < npe; ++a) v[a] = w[a];
+            if (kMshDim[type - 1] == dim) {  // faces, edges, points of the mesh are skipped
+                if (type != want_type) return LMTG_ERR_UNSUPPORTED;
+                uint32_t v[10];
+                for (int a = 0; a < kMshNodes[type - 1]; ++a) {
+                    long long nb;
+                    if (!read_ll(q, e, nb)) return LMTG_ERR_ARG;
+                    auto it = node_of.find(nb);
+                    if (it == node_of.end()) return LMTG_ERR_ARG;
+                    v[a] = it->second;
+                }
+                if (type == 11) std::swap(v[8], v[9]);
+                if (jacobian_det_half(elem_type, dim, out.pos, v, npe) < 0) {
+                    static const int ph[8] = {0, 3, 2, 1, 4, 7, 6, 5};
+                    static const int pt[10] = {0, 1, 3, 2, 4, 8, 7, 6, 5, 9};
+                    static const int pr[6] = {5, 4, 3, 2, 1, 0};
+                    const int *pm = type == 5 ? ph : type == 11 ? pt : pr;
+                    uint32_t w[10];
+                    for (int a = 0; a < npe; ++a) w[a] = v[pm[a]];
+                    for (int a = 0; a < npe; ++a) v[a] = w[a];
+                }
+                out.conn.insert(out.conn.end(), v, v + npe);
+                out.tag.push_back(tag0);
+                ++out.ne;
             }
-            for (int a = 0; a < npe; ++a) out.conn.push_back(v[a]);
-            out.tag.push_back(ntags ? tags[0] : 0.0);
-            ++out.ne;
         }
+        b = next;
     }
     return ended ? LMTG_OK : LMTG_ERR_ARG;
 }
 
-// one value in C++ stream formatting (6 significant digits), as the reference's ostream output
-void put(std::ostream &os, double v) { os << v; }
+// The parse of the last sizing call (lmtg_read_msh with no buffers), reused by the call that
+// fills the buffers when the file is unchanged (same path, element type, size and time).
+struct MshCache {
+    std::mutex mu;
+    bool valid = false;
+    std::string path;
+    int elem_type = 0;
+    long long size = -1, mtime_ns = -1;
+    ParsedMsh m;
+} g_msh_cache;
+
+bool file_stamp(const char *path, long long &size, long long &mtime_ns) {
+    struct stat st;
+    if (stat(path, &st) != 0) return false;
+    size = (long long)st.st_size;
+    mtime_ns = (long long)st.st_mtim.tv_sec * 1000000000ll + st.st_mtim.tv_nsec;
+    return true;
+}
+
+// Text written into memory and to the file at once.  Doubles are formatted as "%g" (6
+// significant digits), which is what a C++ stream with default flags does (the reference's
+// os << value).
+struct Out {
+    std::string s;
+    Out &operator<<(const char *t) { s += t; return *this; }
+    Out &operator<<(char c) { s += c; return *this; }
+    Out &operator<<(uint64_t v) {
+        char b[24];
+        const int n = std::snprintf(b, sizeof b, "%llu", (unsigned long long)v);
+        s.append(b, n);
+        return *this;
+    }
+    Out &operator<<(uint32_t v) { return *this << (uint64_t)v; }
+    Out &operator<<(int v) {
+        char b[16];
+        const int n = std::snprintf(b, sizeof b, "%d", v);
+        s.append(b, n);
+        return *this;
+    }
+};
+void put(Out &os, double v) {
+    char b[32];
+    // std::to_chars with a precision formats as printf's "%.6g" in the "C" locale
+    const auto r = std::to_chars(b, b + sizeof b, v, std::chars_format::general, 6);
+    os.s.append(b, r.ptr - b);
+}
 
 }  // namespace
 
@@ -159,16 +251,36 @@ extern "C" int lmtg_read_msh(const char *path, int elem_type, uint64_t *nn, doub
                              uint32_t *conn, double *tag) {
     try {
         if (!path || !nn || !ne) return LMTG_ERR_ARG;
-        ParsedMsh m;
-        const int rc = parse_msh(path, elem_type, m);
-        if (rc != LMTG_OK) return rc;
         const bool fill = pos || conn || tag;
+        long long size = -1, mtime = -1;
+        if (!file_stamp(path, size, mtime)) return LMTG_ERR_ARG;
+        std::lock_guard<std::mutex> lock(g_msh_cache.mu);
+        MshCache &C = g_msh_cache;
+        if (!(C.valid && C.path == path && C.elem_type == elem_type && C.size == size && C.mtime_ns == mtime)) {
+            C.valid = false;
+            C.m = ParsedMsh();
+            const int rc = parse_msh(path, elem_type, C.m);
+            if (rc != LMTG_OK) {
+                C.m = ParsedMsh();
+                return rc;
+            }
+            C.valid = true;
+            C.path = path;
+            C.elem_type = elem_type;
+            C.size = size;
+            C.mtime_ns = mtime;
+        }
+        const ParsedMsh &m = C.m;
         if (fill && (*nn != m.nn || *ne != m.ne)) return LMTG_ERR_ARG;  // sizes from the first call
         *nn = m.nn;
         *ne = m.ne;
         if (pos && !m.pos.empty()) std::memcpy(pos, m.pos.data(), m.pos.size() * sizeof(double));
         if (conn && !m.conn.empty()) std::memcpy(conn, m.conn.data(), m.conn.size() * sizeof(uint32_t));
         if (tag && !m.tag.empty()) std::memcpy(tag, m.tag.data(), m.tag.size() * sizeof(double));
+        if (fill) {  // the buffers are filled: drop the parse
+            C.valid = false;
+            C.m = ParsedMsh();
+        }
         return LMTG_OK;
     } catch (...) {
         return LMTG_ERR_NOMEM;
@@ -192,8 +304,9 @@ extern "C" int lmtg_write_vtu(const char *path, int elem_type, uint64_t nn, cons
             if (!cnames[f] || cncomp[f] < 1 || ckind[f] < 0 || ckind[f] > 2 || (ne && !cvals[f])) return LMTG_ERR_ARG;
         for (uint64_t i = 0; i < ne * (uint64_t)npe; ++i)
             if (conn[i] >= nn) return LMTG_ERR_ARG;
-        std::ofstream os(path);
-        if (!os.is_open()) return LMTG_ERR_ARG;
+        std::ofstream file(path, std::ios::binary);
+        if (!file.is_open()) return LMTG_ERR_ARG;
+        Out os;
         os << "<?xml version='1.0' ?>\n";
         os << "<VTKFile type='UnstructuredGrid' byte_order='LittleEndian'>\n";
         os << "    <UnstructuredGrid>\n";
@@ -250,7 +363,8 @@ extern "C" int lmtg_write_vtu(const char *path, int elem_type, uint64_t nn, cons
         os << "            <Cells>\n";
         auto list = [&](const char *name, uint64_t count, auto value) {
             os << "                <DataArray Name='" << name << "' type='Int32' format='ascii'>\n";
-            for (uint64_t i = 0; i < count; ++i) os << value(i) << ((i % 8) == 7 || i + 1 == count ? '\n' : ' ');
+            for (uint64_t i = 0; i < count; ++i)
+                os << (uint64_t)value(i) << ((i % 8) == 7 || i + 1 == count ? '\n' : ' ');
             os << "                </DataArray>\n";
         };
         list("connectivity", ne * (uint64_t)npe, [&](uint64_t i) { return conn[i]; });
@@ -263,8 +377,9 @@ extern "C" int lmtg_write_vtu(const char *path, int elem_type, uint64_t nn, cons
         os << "        _\n";
         os << "    </AppendedData>\n";
         os << "</VTKFile>\n";
-        os.close();
-        return os ? LMTG_OK : LMTG_ERR_ARG;
+        file.write(os.s.data(), (std::streamsize)os.s.size());
+        file.close();
+        return file ? LMTG_OK : LMTG_ERR_ARG;
     } catch (...) {
         return LMTG_ERR_NOMEM;
     }

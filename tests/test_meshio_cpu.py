@@ -93,3 +93,29 @@ def test_read_msh_errors(tmp_path):
     _write(tmp_path / "faces.msh", head + "$Elements\n1\n1 2 0 1 2 3\n$EndElements\n")
     pos, conn, tag = meshio.read_msh(tmp_path / "faces.msh", "hexa8")
     assert pos.shape == (4, 3) and conn.shape == (0, 8)
+
+
+REF = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle", "_ref", "ref_meshio")
+
+
+@pytest.mark.skipif(not os.path.exists(REF), reason="the reference's mesh-file driver is built only where its sources are")
+@pytest.mark.parametrize("elem,nb", [("hexa", 17), ("tetra10", 9), ("tri6", 33)])
+def test_reader_and_writer_against_the_reference_at_size(tmp_path, elem, nb):
+    """A larger generated file and mesh than the fixtures, run through the reference's own code."""
+    import subprocess
+    import sys
+    sys.path.insert(0, GOLD)
+    import make_meshio_golden as G
+    from lmtpp_gb300 import make_rect_hexa, make_rect_tetra10
+    pos, conn = {"hexa": make_rect_hexa, "tetra10": make_rect_tetra10, "tri6": make_rect_triangle6}[elem](nb)
+    msh = tmp_path / "m.msh"
+    G.write_msh(str(msh), elem, pos, conn, np.random.default_rng(nb))
+    subprocess.run([REF, "msh", elem, str(msh), str(tmp_path)], check=True)
+    npe, dim = conn.shape[1], pos.shape[1]
+    rpos = np.fromfile(tmp_path / "pos.f64").reshape(-1, dim)
+    rconn = np.fromfile(tmp_path / "conn.u32", dtype=np.uint32).reshape(-1, npe)
+    p2, c2, _ = meshio.read_msh(msh, ELEM[elem])
+    assert np.array_equal(p2, rpos) and np.array_equal(c2, rconn)
+    subprocess.run([REF, "vtu_std", elem, str(nb), str(tmp_path / "r.vtu")], check=True)
+    meshio.write_vtu(tmp_path / "o.vtu", ELEM[elem], pos, conn, [], [("group", np.zeros(conn.shape[0]), meshio.INTEGER)])
+    assert (tmp_path / "o.vtu").read_text() == (tmp_path / "r.vtu").read_text()
