@@ -349,7 +349,9 @@ def cpu_desc(s):
 # launch (k_pcg_spmv_bulk<2, 512, 8, 1, 4>), ncu captures of small cases:
 #   Hexa8 64^3:    (293.262 MB + 4.432 MB) over spmv_bytes(274625, 7189057, 4) = 296.350 MB
 #   Tetra10 24^3:  (132.940 MB + 3.373 MB) over spmv_bytes(117649, 3259585, 4) = 134.148 MB
-SPMV32_KERNEL = "k_pcg_spmv_bulk<2, 512, 8, 1, 4>"
+# Rows wider than 32 blocks (Tetra10) run the 5-CTA instance of the same kernel, which moves
+# the same bytes.
+SPMV32_KERNEL = {"hexa8": "k_pcg_spmv_bulk<2, 512, 8, 1, 4>", "tetra10": "k_pcg_spmv_bulk<2, 512, 8, 1, 5>"}
 SPMV32_TRAFFIC_RATIO = {"hexa8": (293.261824 + 4.431616) / 296.350284,
                         "tetra10": (132.940032 + 3.373312) / 134.148172}
 
@@ -648,7 +650,7 @@ def main():
         "warmup": args.warmup, "ms_per_step": r["ms_mixed"], "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64", "data": "synthetic",
         "config": workload_config(args),
-        "roofline": {"bound": "hbm", "kernel": SPMV32_KERNEL, "achieved": ach, "peak": hbm,
+        "roofline": {"bound": "hbm", "kernel": SPMV32_KERNEL[args.elem], "achieved": ach, "peak": hbm,
                      "unit": "GB/s", "frac": ach / hbm,
                      "traffic": b32 * SPMV32_TRAFFIC_RATIO[args.elem],
                      "traffic_source": "ncu dram bytes of a %s capture scaled by the block count "

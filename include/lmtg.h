@@ -309,9 +309,11 @@ int lmtg_batch_set_options(lmtg_ctx *ctx, int tile_rows, int variant);
 int lmtg_set_inner_reduction(lmtg_ctx *ctx, double inner_reduction);
 
 /* FP32 SpMV of the single-system PCG: 0 = one warp per pair of node rows, the matrix read
- * straight into registers; 1 (default) and 2 = the matrix streamed through shared memory by
- * bulk copies (TMA) in a ring of two stages of up to 16 rows, sized for 4 and 5 CTAs per SM.
- * All give the same q; p.q is summed in a different fixed order.  No reference counterpart. */
+ * straight into registers; 1 and 2 = the matrix streamed through shared memory by bulk copies
+ * (TMA) in a ring of two stages of up to 16 rows, sized for 4 and 5 CTAs per SM; -1 (default)
+ * = 2 when a node row has more than 32 blocks (Tetra10), else 1.  All give the same q; p.q is
+ * summed in a different fixed order.  The diffusion step solver uses its bulk-copy SpMV unless
+ * the kind is 0.  No reference counterpart. */
 int lmtg_set_spmv_kind(lmtg_ctx *ctx, int kind);
 
 /* Self-test of the device-side wait bound used by the bulk-copy SpMVs: one thread waits on an

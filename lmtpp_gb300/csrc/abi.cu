@@ -494,7 +494,7 @@ int lmtg_selftest_bounded_wait(lmtg_ctx *c, int *status, double *waited_s) {
 
 int lmtg_set_spmv_kind(lmtg_ctx *c, int kind) {
     return guard(c, [&] {
-        LMTG_CHECK(kind >= 0 && kind <= 2, LMTG_ERR_ARG, "spmv kind in 0..2");
+        LMTG_CHECK(kind >= -1 && kind <= 2, LMTG_ERR_ARG, "spmv kind in -1..2");
         c->spmv_kind = kind;
         return LMTG_OK;
     });

@@ -128,9 +128,10 @@ struct lmtg_ctx {
     bool allocated = false;
     uint64_t nnzb = 0, nnz_lower = 0, ngather = 0;
     uint32_t max_row_blocks = 0;  // blocks in the widest node row (<= 96)
-    // FP32 PCG SpMV: 0 = warp per row pair, 1 (default), 2 = bulk-copy pipeline (solver.cu);
-    // the grid is set up when the kind changes
-    int spmv_kind = 1, spmv_setup_kind = -1, spmv_grid = 0;
+    // FP32 PCG SpMV: 0 = warp per row pair, 1, 2 = bulk-copy pipeline (solver.cu), -1 (default)
+    // = 2 when a node row has more than 32 blocks, else 1; the grid is set up when the kind
+    // in use changes
+    int spmv_kind = -1, spmv_setup_kind = -2, spmv_grid = 0;
     lmtg::DBuf<uint32_t> bptr, bcol, bdiag, gptr, gsrc;
 
     // values

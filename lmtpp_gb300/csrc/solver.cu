@@ -47,9 +47,9 @@ static int row_grid(lmtg_ctx *c) { return grid_for(c, c->nn * 32, kRowThreads, 8
 static int node_grid(lmtg_ctx *c) { return grid_for(c, c->nn, kRowThreads, 8); }
 
 // Bulk-copy SpMV instances, spmv_kind 1, 2 = (stages, blocks per stage, consumer warps,
-// evict-first L2 hint, CTAs per SM the registers are sized for).  Kind 1, the default, held
-// 96% of the measured HBM copy bandwidth on Hexa8 128^3 (0.361 ms against 0.449 ms for the
-// warp-row kernel, kind 0).  The dynamic shared-memory limit and the resident grid are set up
+// evict-first L2 hint, CTAs per SM the registers are sized for).  Kind 1 held 96% of the
+// measured HBM copy bandwidth on Hexa8 128^3 (0.361 ms against 0.449 ms for the warp-row
+// kernel, kind 0).  The dynamic shared-memory limit and the resident grid are set up
 // once per kind.
 #define LMTG_BULK_KINDS(X)     \
     X(1, 2, 512, 8, true, 4)   \
@@ -65,23 +65,30 @@ static int bulk_grid(lmtg_ctx *c) {
     return c->sm_count * (nb > 0 ? nb : 1);
 }
 
+// the kind in use: -1 picks the 5-CTA instance for wide rows (Tetra10: 0.108 against 0.111 ms
+// at 40^3) and the 4-CTA one otherwise (Hexa8: 0.363 against 0.369 ms at 128^3)
+static int spmv_kind_used(const lmtg_ctx *c) {
+    return c->spmv_kind >= 0 ? c->spmv_kind : (c->max_row_blocks > 32 ? 2 : 1);
+}
+
 static void spmv_setup(lmtg_ctx *c) {
-    if (c->spmv_kind == c->spmv_setup_kind) return;
-    switch (c->spmv_kind) {
+    const int kind = spmv_kind_used(c);
+    if (kind == c->spmv_setup_kind) return;
+    switch (kind) {
 #define LMTG_BULK_SETUP(id, st, cap, cons, ef, minb) \
     case id: c->spmv_grid = bulk_grid<st, cap, cons, ef, minb>(c); break;
         LMTG_BULK_KINDS(LMTG_BULK_SETUP)
 #undef LMTG_BULK_SETUP
         default: c->spmv_grid = row_grid(c); break;
     }
-    c->spmv_setup_kind = c->spmv_kind;
+    c->spmv_setup_kind = kind;
 }
 
 // q = K p, pq and alpha of one PCG iteration (FP64: the warp-row kernel; FP32: spmv_kind)
 template <class T, int VS>
 static void launch_pcg_spmv(lmtg_ctx *c, const T *K, const T *p, T *q, cudaStream_t s) {
     if constexpr (std::is_same<T, float>::value) {
-        switch (c->spmv_kind) {
+        switch (spmv_kind_used(c)) {
 #define LMTG_BULK_LAUNCH(id, st, cap, cons, ef, minb)                                                   \
     case id:                                                                                              \
         k_pcg_spmv_bulk<st, cap, cons, ef, minb><<<c->spmv_grid, bulk_threads<cons>(),                      \

@@ -262,6 +262,45 @@ __global__ void __launch_bounds__(bulk_threads<kCons>(), kMinBlocks)
                     const float q1 = reduce_scatter3(a10, a11, a12, lane);
                     finish(I, q0);
                     if (has1) finish(I + 1, q1);
+                } else if (d0 + d1 <= 96) {
+                    // a wide pair (a Tetra10 vertex row of 65 blocks and its neighbour): the two
+                    // rows' blocks as one list, lane l taking blocks l, l + 32, l + 64, so that
+                    // all of the pair's gathers are in flight before the products
+                    const uint32_t dd = d0 + d1;
+                    float xs[3][3];
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        const uint32_t f = 32 * c + lane;
+                        xs[c][0] = xs[c][1] = xs[c][2] = 0.f;
+                        if (f < dd) {
+                            const uint32_t col = f < d0 ? sC[rb0 + f - cbase] : sC[rb1 + (f - d0) - cbase];
+                            xnode(col, xs[c][0], xs[c][1], xs[c][2]);
+                        }
+                    }
+                    float a00 = 0.f, a01 = 0.f, a02 = 0.f, a10 = 0.f, a11 = 0.f, a12 = 0.f;
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        const uint32_t f = 32 * c + lane;
+                        if (f < dd) {
+                            const bool second = f >= d0;
+                            const uint32_t rb = second ? rb1 : rb0, d = second ? d1 : d0, bl = second ? f - d0 : f;
+                            float m[9];
+#pragma unroll
+                            for (int v = 0; v < 9; ++v) m[v] = sK[kidx(rb, d, bl, v) - kbase];
+                            float t0 = 0.f, t1 = 0.f, t2 = 0.f;
+                            block_fma(m, xs[c][0], xs[c][1], xs[c][2], t0, t1, t2);
+                            a00 += second ? 0.f : t0;
+                            a01 += second ? 0.f : t1;
+                            a02 += second ? 0.f : t2;
+                            a10 += second ? t0 : 0.f;
+                            a11 += second ? t1 : 0.f;
+                            a12 += second ? t2 : 0.f;
+                        }
+                    }
+                    const float q0 = reduce_scatter3(a00, a01, a02, lane);
+                    const float q1 = reduce_scatter3(a10, a11, a12, lane);
+                    finish(I, q0);
+                    if (has1) finish(I + 1, q1);
                 } else {
                     for (int r = 0; r < (has1 ? 2 : 1); ++r) {
                         const uint32_t rb = r ? rb1 : rb0, d = r ? d1 : d0;

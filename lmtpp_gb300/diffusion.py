@@ -95,8 +95,8 @@ class Diffusion:
                   "set_inner_reduction")
 
     def set_spmv_kind(self, kind):
-        """FP32 SpMV of the mixed step solver: 0 = warp-streamed CSR, 1 (default), 2 = the matrix
-        streamed through shared memory by bulk copies (TMA)."""
+        """FP32 SpMV of the mixed step solver: 0 = warp-streamed CSR, any other kind (default -1)
+        = the matrix streamed through shared memory by bulk copies (TMA)."""
         abi.check(self._lib.lmtg_set_spmv_kind(self._ctx, int(kind)), self._ctx, "set_spmv_kind")
 
     def set_penalty_scale(self, max_diag):

@@ -331,7 +331,7 @@ class Formulation:
                   "set_inner_reduction")
 
     def set_spmv_kind(self, kind):
-        """FP32 PCG SpMV: 0 = warp per row pair, 1 (default), 2 = matrix streamed by bulk copies (TMA)."""
+        """FP32 PCG SpMV: 0 = warp per row pair, 1, 2 = matrix streamed by bulk copies (TMA), -1 (default) = by row width."""
         abi.check(self._lib.lmtg_set_spmv_kind(self._ctx, int(kind)), self._ctx, "set_spmv_kind")
 
     def set_penalty_scale(self, max_diag):
