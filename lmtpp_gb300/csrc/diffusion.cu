@@ -300,8 +300,25 @@ template <class T>
 __global__ void k_pcg_dir_s(const T *__restrict__ z, T *__restrict__ p, uint64_t n, const PcgScalars *S) {
     if (*(volatile const int *)&S->done) return;
     const T beta = (T)S->beta;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
-         i += (uint64_t)gridDim.x * blockDim.x)
+    uint64_t i0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+    if constexpr (std::is_same<T, float>::value) {  // four nodes per 16-byte access
+        const uint64_t n4 = n / 4;
+        const float4 *z4 = reinterpret_cast<const float4 *>(z);
+        float4 *p4 = reinterpret_cast<float4 *>(p);
+        for (uint64_t g = i0; g < n4; g += step) {
+            const float4 zz = z4[g];
+            if (beta != 0.f) {
+                const float4 pp = p4[g];
+                p4[g] = make_float4(fmaf(beta, pp.x, zz.x), fmaf(beta, pp.y, zz.y), fmaf(beta, pp.z, zz.z),
+                                    fmaf(beta, pp.w, zz.w));
+            } else {
+                p4[g] = zz;
+            }
+        }
+        i0 += 4 * n4;
+    }
+    for (uint64_t i = i0; i < n; i += step)
         p[i] = beta != (T)0 ? fma(beta, p[i], z[i]) : z[i];
 }
 
@@ -520,8 +537,36 @@ __global__ void k_pcg_update_s(T *__restrict__ x, T *__restrict__ r, T *__restri
     const double pq = S->pq;
     const T alpha = (T)S->alpha;
     T t[2] = {(T)0, (T)0};
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
-         i += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t i0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+    if constexpr (std::is_same<T, float>::value) {  // four nodes per 16-byte access
+        const uint64_t n4 = n / 4;
+        float4 *x4 = reinterpret_cast<float4 *>(x), *r4 = reinterpret_cast<float4 *>(r),
+               *z4 = reinterpret_cast<float4 *>(z);
+        const float4 *p4 = reinterpret_cast<const float4 *>(p), *q4 = reinterpret_cast<const float4 *>(q),
+                     *d4 = reinterpret_cast<const float4 *>(Dinv);
+        for (uint64_t g = i0; g < n4; g += step) {
+            float xv[4], rv[4], pv[4], qv[4], dv[4], zv[4];
+            *reinterpret_cast<float4 *>(xv) = x4[g];
+            *reinterpret_cast<float4 *>(rv) = r4[g];
+            *reinterpret_cast<float4 *>(pv) = p4[g];
+            *reinterpret_cast<float4 *>(qv) = q4[g];
+            *reinterpret_cast<float4 *>(dv) = d4[g];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                xv[k] = fmaf(alpha, pv[k], xv[k]);
+                rv[k] = fmaf(-alpha, qv[k], rv[k]);
+                zv[k] = dv[k] * rv[k];
+                t[0] = fmaf(rv[k], zv[k], t[0]);
+                t[1] = fmaf(rv[k], rv[k], t[1]);
+            }
+            x4[g] = *reinterpret_cast<const float4 *>(xv);
+            r4[g] = *reinterpret_cast<const float4 *>(rv);
+            z4[g] = *reinterpret_cast<const float4 *>(zv);
+        }
+        i0 += 4 * n4;  // the last n % 4 nodes below
+    }
+    for (uint64_t i = i0; i < n; i += step) {
         x[i] = fma(alpha, p[i], x[i]);
         const T ri = fma(-alpha, q[i], r[i]);
         r[i] = ri;
