@@ -353,10 +353,11 @@ __global__ void __launch_bounds__(kRowThreads)
 // Each CTA owns a contiguous range of 32-row chunks.  One producer warp copies, per stage, the
 // entries (values, columns) and the row pointers of up to 8 chunks whose entries fit kCap into
 // a ring of kStages stages (evict-first L2 policy).  Consumer warp w takes chunk w of a stage:
-// its lanes form the products K_q p[col_q] over the chunk's entries (coalesced, in place), then
-// lane l sums row l's products in column order and the stage goes back.  The products and
-// their order are the ones of csr_stream32, so q is bit-identical to k_pcg_spmv_s; p.q is
-// summed in another fixed order.  Every wait is bounded; one that gives up sets
+// lane l sums row l, reading the row's entries from shared memory and gathering p directly
+// (four entries in flight), then the stage goes back.  Forming the products in shared memory
+// first (the warp-streamed layout of csr_stream32) cost 10% more: it doubled the L1 traffic.
+// Each product is rounded and then added in column order, as in csr_stream32, so q is
+// bit-identical to k_pcg_spmv_s; p.q is summed in another fixed order.  Every wait is bounded; one that gives up sets
 // LMTG_ERR_TIMEOUT and done in the PCG scalars.
 constexpr int kSBulkCons = 8;
 constexpr int kSBulkThreads = 32 * (kSBulkCons + 1);
@@ -481,31 +482,12 @@ __global__ void __launch_bounds__(kSBulkThreads, 4)
             const uint64_t R0 = g0 + (uint64_t)(32 * warp);
             if (R0 < g1) {
                 const uint64_t R1 = min(g1, R0 + (uint64_t)32);
-                const uint32_t E0 = sR[R0 - rbase], E1 = sR[R1 - rbase];
-                for (uint32_t t0 = E0; t0 < E1; t0 += kTile) {
-                    float kv[kTileChunks], xv[kTileChunks];
-                    uint32_t cj[kTileChunks];
-#pragma unroll
-                    for (int c = 0; c < kTileChunks; ++c) {
-                        const uint32_t qq = t0 + 32 * c + lane;
-                        const bool on = qq < E1;
-                        kv[c] = on ? sK[qq - kbase] : 0.f;
-                        cj[c] = on ? sC[qq - kbase] : 0u;
-                    }
-#pragma unroll
-                    for (int c = 0; c < kTileChunks; ++c) xv[c] = t0 + 32 * c + lane < E1 ? __ldg(p + cj[c]) : 0.f;
-#pragma unroll
-                    for (int c = 0; c < kTileChunks; ++c) {
-                        const uint32_t qq = t0 + 32 * c + lane;
-                        if (qq < E1) sK[qq - kbase] = kv[c] * xv[c];
-                    }
-                }
-                __syncwarp();
                 const uint64_t I = R0 + lane;
                 float v = 0.f;
                 if (I < R1) {
                     const uint32_t rs = sR[I - rbase], re = sR[I + 1 - rbase];
-                    for (uint32_t qq = rs; qq < re; ++qq) v += sK[qq - kbase];
+#pragma unroll 4
+                    for (uint32_t qq = rs; qq < re; ++qq) v += __fmul_rn(sK[qq - kbase], __ldg(p + sC[qq - kbase]));
                 }
                 __syncwarp();
                 if (lane == 0) bulk::mbar_arrive(&empty[slot]);
