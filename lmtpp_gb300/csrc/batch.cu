@@ -1008,7 +1008,7 @@ template <class T>
 static int batch_pcg_run(lmtg_ctx *c, BDev B, const T *K, const T *Dinv, T *x, T *r, T *z, T *p, T *q,
                          double deadline_s, std::chrono::steady_clock::time_point t0) {
     cudaStream_t s = c->stream;
-    LMTG_CUDA(cudaMemsetAsync(B.n_active, 0, sizeof(int), s));
+    LMTG_CUDA(cudaMemsetAsync(B.n_active, 0, 2 * sizeof(int), s));  // running count and fault word
     k_b_start<T><<<bgrid(c, k_b_start<T>), kBThreads, 0, s>>>(B, r, z, Dinv);
     c->launches += 1;
     LMTG_CUDA(cudaGetLastError());
