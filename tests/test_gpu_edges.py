@@ -259,3 +259,59 @@ def test_device_wait_bound_gives_up_and_context_stays_usable():
     x = O.skyline_solve(P["rowptr"], P["col"], P["val"], P["F"])
     assert np.linalg.norm(u - x) <= 1e-8 * np.linalg.norm(x)
     f.close()
+
+
+def fan_tetra10(M=18):
+    """Tetra10 fan around a central vertex: 2 M tetrahedra (centre, ring_i, ring_i+1, pole), so
+    that the centre's node row holds 5 M + 5 blocks (95 for M = 18; the pattern allows 96)."""
+    ang = 2 * np.pi * np.arange(M) / M
+    verts = [np.zeros(3)] + [np.array([np.cos(a), np.sin(a), 0.0]) for a in ang] + [np.array([0, 0, 1.0]),
+                                                                                       np.array([0, 0, -1.0])]
+    pos = list(verts)
+    mid = {}
+
+    def m(a, b):
+        k = (min(a, b), max(a, b))
+        if k not in mid:
+            mid[k] = len(pos)
+            pos.append(0.5 * (pos[a] + pos[b]))
+        return mid[k]
+    conn = []
+    for i in range(M):
+        r0, r1 = 1 + i, 1 + (i + 1) % M
+        for pole, sgn in ((M + 1, 1.0), (M + 2, -1.0)):
+            v = [0, r0, r1, pole] if sgn > 0 else [0, r1, r0, pole]
+            # LMT++ Tetra_10 edge order: (0,1) (1,2) (0,2) (0,3) (1,3) (2,3)
+            e = [m(v[0], v[1]), m(v[1], v[2]), m(v[0], v[2]), m(v[0], v[3]), m(v[1], v[3]), m(v[2], v[3])]
+            conn.append(v + e)
+    return np.array(pos), np.array(conn, dtype=np.uint32)
+
+
+def test_widest_rows_fan_of_tetra10_matches_oracle():
+    """A node row of 95 blocks (next to the pattern's 96): the bulk-copy SpMV's wide-row paths and
+    the warp-row kernel give the oracle's direct solution."""
+    pos, conn = fan_tetra10(18)
+    nn = pos.shape[0]
+    # orientation: every element's vertex Jacobian positive
+    v = pos[conn[:, :4]]
+    assert (np.einsum("ij,ij->i", v[:, 1] - v[:, 0], np.cross(v[:, 2] - v[:, 0], v[:, 3] - v[:, 0])) > 0).all()
+    rowptr, col = O.pattern_lower(nn, 3, conn)
+    val = O.assemble_elast(pos, conn, 2.1e5, 0.3, rowptr, col)
+    fixed = np.arange(1, 19 + 2)  # the ring and the poles
+    dofs = (3 * fixed[:, None] + np.arange(3)).ravel()
+    F = np.random.default_rng(4).standard_normal(3 * nn)
+    Fo = F.copy()
+    O.penalty(rowptr, col, val, Fo, dofs, np.ones(dofs.shape[0]), np.zeros(dofs.shape[0]), 1e5)
+    x = O.skyline_solve(rowptr, col, val, Fo)
+    for kind in (0, 1, 2):
+        f = Formulation(pos, conn)
+        f.elastic_modulus = 2.1e5
+        f.poisson_ratio = 0.3
+        f.add_constraints(dofs, 1e5)
+        f.allocate_matrices()
+        f.set_nodal_loads(F)
+        f.set_spmv_kind(kind)
+        f.solve(1e-12, mode="mixed")
+        u = f.get_result()
+        assert np.linalg.norm(u - x) <= 1e-8 * np.linalg.norm(x), kind
+        f.close()
