@@ -36,6 +36,7 @@ int guard2(lmtg_ctx *c, F &&f) {
 namespace lmtg {
 
 void do_assemble(lmtg_ctx *c, int flags) {
+    Phase ph("lmtg.assemble");
     LMTG_CHECK(c->allocated, LMTG_ERR_STATE, "allocate_matrices first");
     LMTG_CHECK(c->nnu == 3, LMTG_ERR_STATE, "elasticity call on a diffusion context");
     const bool mat = (flags & (LMTG_ASM_MAT64 | LMTG_ASM_MAT32 | LMTG_ASM_MAT32_NATIVE)) != 0;

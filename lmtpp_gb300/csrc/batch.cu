@@ -1066,6 +1066,7 @@ static int worst(int a, int b) { return a != LMTG_OK ? a : b; }
 // Solves the batch: every pair (system m, rhs r < nrhs) to |b - K x| <= tol |b| in FP64.
 int batch_solve(lmtg_ctx *c, int mode, double tol, int maxit, double timeout_s, lmtg_solve_stats *st,
                 int *pair_iters) {
+    Phase ph("lmtg.batch_solve");
     batch_prepare(c);
     BatchState &S = *c->batch;
     LMTG_CHECK(S.nrhs > 0, LMTG_ERR_STATE, "lmtg_batch_set_rhs first");

@@ -825,6 +825,7 @@ __global__ void k_add_vec(double *__restrict__ y, const double *__restrict__ a, 
 // one step T_next = A^-1 (B T + s) (warm start from T); s = the constant source and convection
 // loads (lmtg_diff_set_sources / lmtg_diff_set_convection)
 static int diff_step(lmtg_ctx *c, const double *T, double *Tn, double tol, int maxit, int *it) {
+    Phase ph("lmtg.diff.step");
     diff_rhs(c, T, c->F.p);
     if (c->diff_load.p) {
         k_add_vec<<<ngrid(c), kRowThreads, 0, c->stream>>>(c->F.p, c->diff_load.p, c->nn);

@@ -15,6 +15,7 @@
 //   Dinv64/Dinv32[nn*9]                                            block-Jacobi inverses
 #pragma once
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 #include <string>
 #include <vector>
@@ -22,6 +23,15 @@
 #include "../../include/lmtg.h"
 
 namespace lmtg {
+
+// NVTX range over a host phase (assembly, a PCG run, a time step...), visible in a timeline
+// profiler; without one attached the calls return at once.
+struct Phase {
+    explicit Phase(const char *name) { nvtxRangePushA(name); }
+    ~Phase() { nvtxRangePop(); }
+    Phase(const Phase &) = delete;
+    Phase &operator=(const Phase &) = delete;
+};
 
 constexpr int kWarp = 32;
 

@@ -243,6 +243,7 @@ __global__ void k_gather(const uint32_t *conn, int npe, int npairs, const uint32
 }
 
 void build_pattern(lmtg_ctx *c) {
+    Phase ph("lmtg.pattern");
     const uint64_t nn = c->nn, ne = c->ne, m = ne * (uint64_t)c->npe;
     LMTG_CHECK(m < (1ull << 32), LMTG_ERR_UNSUPPORTED, "ne * nodes_per_element must be < 2^32");
     LMTG_CHECK((uint64_t)ne * c->npairs * 2 < (1ull << 32), LMTG_ERR_UNSUPPORTED,

@@ -162,6 +162,7 @@ static int run_pcg(lmtg_ctx *c, const T *K, const T *Dinv, const T *b, T *x, T *
                    T *p1, T *q, bool x_is_zero, int crit_kind, double crit, int maxit,
                    double b_norm2, std::chrono::steady_clock::time_point deadline, bool use_deadline,
                    int *iters, double beta_den = 0.0) {
+    Phase ph(sizeof(T) == 4 ? "lmtg.pcg32" : "lmtg.pcg64");
     cudaStream_t s = c->stream;
     spmv_setup(c);
     PcgScalars init{};
@@ -239,6 +240,7 @@ static int run_pcg(lmtg_ctx *c, const T *K, const T *Dinv, const T *b, T *x, T *
 
 int solve_pcg64(lmtg_ctx *c, int crit_kind, double tol, int maxit, double timeout_s,
                 lmtg_solve_stats *st, const double *bvec, double *xvec) {
+    Phase ph("lmtg.solve_pcg64");
     const double *Fb = bvec ? bvec : c->F.p;
     double *ux = xvec ? xvec : c->u.p;
     auto deadline = std::chrono::steady_clock::now() +
@@ -266,6 +268,7 @@ int solve_pcg64(lmtg_ctx *c, int crit_kind, double tol, int maxit, double timeou
 // iterative-refinement step).  Convergence is decided on the FP64 true residual only.
 int solve_mixed(lmtg_ctx *c, double tol, int maxit, double timeout_s, lmtg_solve_stats *st,
                 const double *bvec, double *xvec) {
+    Phase ph("lmtg.solve_mixed");
     const double *Fb = bvec ? bvec : c->F.p;
     double *ux = xvec ? xvec : c->u.p;
     auto deadline = std::chrono::steady_clock::now() +
