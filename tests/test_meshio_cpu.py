@@ -119,3 +119,14 @@ def test_reader_and_writer_against_the_reference_at_size(tmp_path, elem, nb):
     subprocess.run([REF, "vtu_std", elem, str(nb), str(tmp_path / "r.vtu")], check=True)
     meshio.write_vtu(tmp_path / "o.vtu", ELEM[elem], pos, conn, [], [("group", np.zeros(conn.shape[0]), meshio.INTEGER)])
     assert (tmp_path / "o.vtu").read_text() == (tmp_path / "r.vtu").read_text()
+
+
+def test_read_msh_crlf_and_blank_runs(tmp_path):
+    """Windows line ends and runs of blanks parse as the stream extraction of the reference does."""
+    src = open(os.path.join(GOLD, "msh_tetra10.msh")).read()
+    crlf = tmp_path / "crlf.msh"
+    with open(crlf, "w", newline="") as f:
+        f.write(src.replace("\n", "\r\n").replace(" ", " \t "))
+    g = np.load(os.path.join(GOLD, "msh_tetra10.npz"))
+    pos, conn, _ = meshio.read_msh(crlf, "tetra10")
+    assert np.array_equal(pos, g["pos"]) and np.array_equal(conn, g["conn"])
