@@ -130,3 +130,19 @@ def test_read_msh_crlf_and_blank_runs(tmp_path):
     g = np.load(os.path.join(GOLD, "msh_tetra10.npz"))
     pos, conn, _ = meshio.read_msh(crlf, "tetra10")
     assert np.array_equal(pos, g["pos"]) and np.array_equal(conn, g["conn"])
+
+
+def test_write_vtu_empty_mesh_and_bad_arguments(tmp_path):
+    out = tmp_path / "empty.vtu"
+    meshio.write_vtu(out, "hexa8", np.zeros((0, 3)), np.zeros((0, 8), dtype=np.uint32),
+                     [("dep", np.zeros((0, 3)))], [("group", np.zeros(0), meshio.INTEGER)])
+    text = out.read_text()
+    assert "NumberOfPoints='0' NumberOfCells='0'" in text and "Name='dep'" not in text  # as the reference
+    ET.parse(out)
+    pos, conn = make_rect_hexa(2)
+    with pytest.raises(abi.LmtgError) as e:  # a node index past the points
+        meshio.write_vtu(tmp_path / "bad.vtu", "hexa8", pos, conn + 100)
+    assert e.value.status == abi.ERR_ARG
+    with pytest.raises(abi.LmtgError) as e:
+        meshio.write_vtu(tmp_path / "no_dir" / "x.vtu", "hexa8", pos, conn)
+    assert e.value.status == abi.ERR_ARG
