@@ -56,7 +56,7 @@ def to_file_order(elem, conn):
     return c
 
 
-def write_msh(path, elem, pos, conn, rng):
+def write_msh(path, elem, pos, conn, rng, ntags=2):
     nn = pos.shape[0]
     numbers = rng.permutation(np.arange(1, 3 * nn + 1))[:nn] + 100  # unique, non-contiguous
     order = rng.permutation(nn)
@@ -79,7 +79,9 @@ def write_msh(path, elem, pos, conn, rng):
             else:
                 els.append("%d 15 2 7 1 %d" % (k, numbers[conn[e, 0]]))
             k += 1
-        els.append("%d %d 2 %d %d %s" % (k, GMSH[elem], e % 3 + 1, 10 + e, " ".join(str(numbers[j]) for j in fc[e])))
+        tags = [e % 3 + 1, 10 + e, 7][:ntags]
+        els.append("%d %d %d %s%s" % (k, GMSH[elem], ntags, "".join("%d " % t for t in tags),
+                                      " ".join(str(numbers[j]) for j in fc[e])))
         k += 1
     lines += [str(len(els))] + els + ["$EndElements", ""]
     with open(path, "w") as f:

@@ -146,3 +146,25 @@ def test_write_vtu_empty_mesh_and_bad_arguments(tmp_path):
     with pytest.raises(abi.LmtgError) as e:
         meshio.write_vtu(tmp_path / "no_dir" / "x.vtu", "hexa8", pos, conn)
     assert e.value.status == abi.ERR_ARG
+
+
+@pytest.mark.skipif(not os.path.exists(REF), reason="the reference's mesh-file driver is built only where its sources are")
+@pytest.mark.parametrize("ntags", [0, 1, 3])
+@pytest.mark.parametrize("seed", [1, 2])
+def test_reader_against_the_reference_tags_and_seeds(tmp_path, ntags, seed):
+    import subprocess
+    import sys
+    sys.path.insert(0, GOLD)
+    import make_meshio_golden as G
+    for elem, mesh in (("hexa", lambda: make_rect_hexa(4)), ("tetra10", lambda: make_rect_tetra10(3)),
+                       ("tri6", lambda: make_rect_triangle6(5))):
+        pos, conn = mesh()
+        msh = tmp_path / ("%s.msh" % elem)
+        G.write_msh(str(msh), elem, pos, conn, np.random.default_rng(seed), ntags=ntags)
+        subprocess.run([REF, "msh", elem, str(msh), str(tmp_path)], check=True)
+        rpos = np.fromfile(tmp_path / "pos.f64").reshape(-1, pos.shape[1])
+        rconn = np.fromfile(tmp_path / "conn.u32", dtype=np.uint32).reshape(-1, conn.shape[1])
+        p2, c2, tag = meshio.read_msh(msh, ELEM[elem])
+        assert np.array_equal(p2, rpos) and np.array_equal(c2, rconn), (elem, ntags, seed)
+        want = np.arange(conn.shape[0]) % 3 + 1.0 if ntags else np.zeros(conn.shape[0])
+        assert np.array_equal(tag, want)
