@@ -6,8 +6,10 @@
 // shared-memory stages with `cp.async.bulk` (one copy each, completion counted on the stage's
 // "full" mbarrier).  Eight consumer warps take two rows each per stage, read their blocks from
 // shared memory, give the stage back (its "empty" mbarrier) and only then gather p and
-// multiply.  The DRAM stream is thus decoupled from the latency of the p gathers, which in the
-// warp-per-row-pair kernel sit on the same dependency chain as the matrix loads.
+// multiply; a pair holding a row of more than 32 blocks (Tetra10 vertex rows) is taken as one
+// list of up to 96 blocks and gives the stage back after its products.  The DRAM stream is thus
+// decoupled from the latency of the p gathers, which in the warp-per-row-pair kernel sit on the
+// same dependency chain as the matrix loads.
 //
 // Results are the ones of k_pcg_spmv (same q; pq summed in a different fixed order), and they
 // are deterministic: the stage partition depends only on bptr.
