@@ -118,8 +118,9 @@ int lmtg_allocate_matrices(lmtg_ctx *ctx, uint64_t *nnz_lower);
 int lmtg_set_nodal_loads(lmtg_ctx *ctx, const double *F);
 /* Uniform traction f_surf on skin faces (Quad4 for Hexa8 meshes: nfaces*4 node ids; Triangle_6
  * for Tetra10 meshes: nfaces*6), accumulated into the load vector as consistent nodal loads (the
- * add_skin_elem_matrix terms, formulation.h:584-594; order-2 rules of element_Quad.h /
- * element_Triangle_6.h). */
+ * add_skin_elem_matrix terms, formulation.h:584-594), integrated with the rules the reference's
+ * generator bakes into those routines (formal_lf/formulation.py:400-438): gauss_points[3] of
+ * formulations/element_Quad.py, gauss_points[4] of formulations/element_Triangle_6.py. */
 int lmtg_add_skin_traction(lmtg_ctx *ctx, uint64_t nfaces, const uint32_t *faces,
                            const double traction[3]);
 /* Skin pressure p dS_normal . te dS (formulation_elasticity_iso.py:60, variable p), on the same
@@ -127,12 +128,6 @@ int lmtg_add_skin_traction(lmtg_ctx *ctx, uint64_t nfaces, const uint32_t *faces
  * (formal_lf/element.py:467-474); outward for the Hexa children.  Adds to the load vector. */
 int lmtg_add_skin_pressure(lmtg_ctx *ctx, uint64_t nfaces, const uint32_t *faces, double p);
 
-/* Constraints add_constraint("coef*node[i].dep[d] - res", penalty) for linear single-unknown
- * constraints; assembled as in assemble_constraints (formulation.h:1028-1071):
- * K(j,j) += coef^2 * max|diag K| * penalty, F(j) += coef * max|diag K| * penalty * res.
- * penalty == 0 is the reference's exact constraint (Lagrange rows, formulation.h:1072-1088),
- * applied here by elimination: u_j = res / coef exactly (one exact constraint per DOF, coef != 0;
- * needs the FP64 matrix assembly; not with the adjoint, the fit or batch solves). */
 /* Volume force of elasticity_iso (formulations/formulation_elasticity_iso.py:49, static:
  * dep_tt = 0): F += density f_vol int N dV; f_vol global (3 doubles).  Defaults 0. */
 int lmtg_set_volume_force(lmtg_ctx *ctx, double density, const double f_vol[3]);
@@ -144,6 +139,12 @@ int lmtg_set_nodal_springs(lmtg_ctx *ctx, const double *coef, const double *targ
  * assemble_constraints, formulation.h:1033-1034): K(i,i) += max|diag K| * lm at every matrix
  * assembly, before the constraints; 0 by default. */
 int lmtg_set_levenberg_marquadt(lmtg_ctx *ctx, double lm);
+/* Constraints add_constraint("coef*node[i].dep[d] - res", penalty) for linear single-unknown
+ * constraints; assembled as in assemble_constraints (formulation.h:1028-1071):
+ * K(j,j) += coef^2 * max|diag K| * penalty, F(j) += coef * max|diag K| * penalty * res.
+ * penalty == 0 is the reference's exact constraint (Lagrange rows, formulation.h:1072-1088),
+ * applied here by elimination: u_j = res / coef exactly (one exact constraint per DOF, coef != 0;
+ * needs the FP64 matrix assembly; not with the adjoint, the fit or batch solves). */
 int lmtg_set_constraints(lmtg_ctx *ctx, uint64_t nc, const uint32_t *dof, const double *coef,
                          const double *res, double penalty);
 
@@ -216,7 +217,9 @@ int lmtg_profile_pcg_kernels(lmtg_ctx *ctx, int precision, int iters, double *sp
  * callers that cannot call cudaMalloc (device memory owned by their own arena, no allocation
  * allowed between steps).  It allocates nothing: its reduction scratch is a fixed 512 KiB
  * device array, so nn is limited to 524,288 node rows (LMTG_ERR_ARG beyond).  The first call
- * on each device looks up that array's address (make it before any stream capture).  All
+ * on each device looks up that array's address (make it before any stream capture) and keeps
+ * it for the life of the process: a cudaDeviceReset of that device reloads the library's device
+ * code, so a process that resets a device must not call this entry point on it again.  All
  * calls share the array: calls that overlap on the GPU race.  rr_host may be NULL (then the
  * call does not synchronize the stream). */
 int lmtg_residual_norm_noalloc(void *stream, uint64_t nn, const uint32_t *bptr,
@@ -315,6 +318,13 @@ int lmtg_set_inner_reduction(lmtg_ctx *ctx, double inner_reduction);
  * summed in a different fixed order.  The diffusion step solver uses its bulk-copy SpMV unless
  * the kind is 0.  No reference counterpart. */
 int lmtg_set_spmv_kind(lmtg_ctx *ctx, int kind);
+
+/* Test knob of the single-system PCG's bulk-copy SpMV (spmv kinds 1 and 2): with on != 0, every
+ * following PCG run has the SpMV's consumer warps give up at their first wait on a stage, as a
+ * wait that ran out of time does.  The run then ends with LMTG_ERR_TIMEOUT, reported through the
+ * PCG scalars, while the producer lets every copy it issued land before the CTA exits; the
+ * context stays usable.  on = 0 restores normal runs.  No reference counterpart. */
+int lmtg_test_spmv_give_up(lmtg_ctx *ctx, int on);
 
 /* Self-test of the device-side wait bound used by the bulk-copy SpMVs: one thread waits on an
  * mbarrier that nothing completes.  *status = LMTG_ERR_TIMEOUT when the wait gave up (about

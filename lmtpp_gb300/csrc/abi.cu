@@ -45,10 +45,12 @@ void upload(lmtg_ctx *c, DBuf<T> &d, const T *h, size_t n) {
     if (n) LMTG_CUDA(cudaMemcpyAsync(d.p, h, n * sizeof(T), cudaMemcpyHostToDevice, c->stream));
 }
 
-// Quad4 consistent loads of a uniform traction, order-2 quad rule of the reference table
-// (include/mesh/element_Quad.h:5-12, abscissae with 12 significant digits, weights 1/4).
+// Quad4 consistent loads of a uniform traction.  The reference integrates skin terms when it
+// generates add_skin_elem_matrix (formal_lf/formulation.py:400-438, element.integration): with the
+// Python rule of the face element of order >= 2, for Quad gauss_points[3] of
+// formulations/element_Quad.py:70-75, abscissae (1 -+ sqrt(1/3))/2 at full precision, weights 1/4.
 void quad4_loads(const double *pos, const uint32_t *q, const double t[3], double *F, const double *pressure = nullptr) {
-    const double A = 0.211324865405, B = 0.788675134595;
+    const double A = 0.21132486540518711775, B = 0.78867513459481288225;
     const double gp[4][2] = {{B, B}, {A, B}, {B, A}, {A, A}};
     for (int g = 0; g < 4; ++g) {
         const double u = gp[g][0], v = gp[g][1];
@@ -73,11 +75,16 @@ void quad4_loads(const double *pos, const uint32_t *q, const double t[3], double
     }
 }
 
-// Triangle_6 consistent loads of a uniform traction, order-2 rule of the reference table
-// (include/mesh/element_Triangle_6.h:5-15: 3 edge-midpoint points, weights 1/6).
+// Triangle_6 consistent loads of a uniform traction, with the Python rule the reference's
+// generated skin routines integrate by (formal_lf/formulation.py:400-438): gauss_points[4] of
+// formulations/element_Triangle_6.py:92-99, 6 points.
 void tri6_loads(const double *pos, const uint32_t *q, const double t[3], double *F, const double *pressure = nullptr) {
-    const double gp[3][2] = {{0.5, 0.0}, {0.5, 0.5}, {0.0, 0.5}};
-    for (int g = 0; g < 3; ++g) {
+    const double a = 0.445948490915965, b = 0.091576213509771;
+    const double wa = 0.111690794839005, wb = 0.054975871827661;
+    const double gp[6][2] = {{a, a}, {1.0 - 2.0 * a, a}, {a, 1.0 - 2.0 * a},
+                             {b, b}, {1.0 - 2.0 * b, b}, {b, 1.0 - 2.0 * b}};
+    const double gw[6] = {wa, wa, wa, wb, wb, wb};
+    for (int g = 0; g < 6; ++g) {
         const double u = gp[g][0], v = gp[g][1], X0 = 1 - u - v;
         const double N[6] = {X0 * (2 * X0 - 1), u * (2 * u - 1), v * (2 * v - 1),
                              4 * X0 * u,        4 * u * v,       4 * v * X0};
@@ -91,7 +98,7 @@ void tri6_loads(const double *pos, const uint32_t *q, const double t[3], double 
             }
         const double nx = tu[1] * tv[2] - tu[2] * tv[1], ny = tu[2] * tv[0] - tu[0] * tv[2],
                      nz = tu[0] * tv[1] - tu[1] * tv[0];
-        const double nl = std::sqrt(nx * nx + ny * ny + nz * nz), ds = nl * 0.16666666666666666667;
+        const double nl = std::sqrt(nx * nx + ny * ny + nz * nz), ds = nl * gw[g];
         const double tg[3] = {pressure ? *pressure * nx / nl : t[0], pressure ? *pressure * ny / nl : t[1],
                               pressure ? *pressure * nz / nl : t[2]};
         for (int a = 0; a < 6; ++a)
@@ -474,6 +481,13 @@ __global__ void k_selftest_bounded_wait(long long *out) {
     const bool ok = mbar_wait(&bar, 0);
     out[0] = ok ? LMTG_OK : LMTG_ERR_TIMEOUT;
     out[1] = (long long)(globaltimer_ns() - t0);
+}
+
+int lmtg_test_spmv_give_up(lmtg_ctx *c, int on) {
+    return guard(c, [&] {
+        c->test_give_up = on ? 1 : 0;
+        return LMTG_OK;
+    });
 }
 
 int lmtg_selftest_bounded_wait(lmtg_ctx *c, int *status, double *waited_s) {

@@ -395,6 +395,7 @@ __global__ void __launch_bounds__(kBBulkThreads, kMinB)
                 ++k;
             }
         }
+        uint32_t nissued = k;  // stages whose full barrier got its arrival
         if (!failed) {
             const int slot = k % kStages;
             if (next_slot(slot)) {
@@ -403,14 +404,17 @@ __global__ void __launch_bounds__(kBBulkThreads, kMinB)
                     meta[slot][1] = 0;
                     bulk::mbar_arrive(&full[slot]);
                 }
+                nissued = k + 1;
             } else {
                 failed = true;
             }
         }
-        if (failed && lane == 0) {
-            atomicExch(B.fault, LMTG_ERR_TIMEOUT);
-            const uint32_t first = k > (uint32_t)kStages ? k - kStages : 0u;
-            for (uint32_t s2 = first; s2 < k; ++s2) bulk::mbar_wait(&full[s2 % kStages], (s2 / kStages) & 1u);
+        if (lane == 0) {
+            if (failed) atomicExch(B.fault, LMTG_ERR_TIMEOUT);
+            // leave only with no copy in flight: the last stage issued on each slot (complete at
+            // once when the consumers took every stage)
+            const uint32_t first = nissued > (uint32_t)kStages ? nissued - kStages : 0u;
+            for (uint32_t s2 = first; s2 < nissued; ++s2) bulk::mbar_wait(&full[s2 % kStages], (s2 / kStages) & 1u);
         }
     } else {
         // ---------------- consumers ----------------

@@ -402,7 +402,7 @@ __global__ void __launch_bounds__(kSBulkThreads, 4)
         // ---------------- producer ----------------
         uint64_t g0 = row0;
         uint32_t e0 = row0 < row_end ? rp[row0] : 0u;
-        uint32_t k = 0;
+        uint32_t k = 0, nissued = 0;  // stages whose full barrier got its arrival
         bool failed = false;
         for (;; ++k) {
             const int slot = k % kStages;
@@ -419,6 +419,7 @@ __global__ void __launch_bounds__(kSBulkThreads, 4)
                     meta[slot][1] = g0;
                     bulk::mbar_arrive(&full[slot]);
                 }
+                nissued = k + 1;
                 break;
             }
             // chunk ends g0 + 32 (l + 1) (clamped to row_end) for lanes l < 8
@@ -453,12 +454,17 @@ __global__ void __launch_bounds__(kSBulkThreads, 4)
             }
             g0 = g1;
             e0 = e1;
+            nissued = k + 1;
         }
-        if (failed && lane == 0) {
-            atomicExch(&S->status, LMTG_ERR_TIMEOUT);
-            atomicExch(&S->done, 1);
-            const uint32_t first = k > (uint32_t)kStages ? k - kStages : 0u;
-            for (uint32_t s2 = first; s2 < k; ++s2) bulk::mbar_wait(&full[s2 % kStages], (s2 / kStages) & 1u);
+        if (lane == 0) {
+            if (failed) {
+                atomicExch(&S->status, LMTG_ERR_TIMEOUT);
+                atomicExch(&S->done, 1);
+            }
+            // leave only with no copy in flight: the last stage issued on each slot (complete at
+            // once when the consumers took every stage)
+            const uint32_t first = nissued > (uint32_t)kStages ? nissued - kStages : 0u;
+            for (uint32_t s2 = first; s2 < nissued; ++s2) bulk::mbar_wait(&full[s2 % kStages], (s2 / kStages) & 1u);
         }
     } else {
         // ---------------- consumers ----------------

@@ -16,7 +16,11 @@
 //
 // Every mbarrier wait is bounded (about a second of %globaltimer, and an iteration cap).  A
 // wait that gives up sets LMTG_ERR_TIMEOUT and done in the PCG scalars; the producer then
-// waits, bounded again, for its own copies in flight before the CTA exits.
+// waits, bounded again, for its own copies in flight before the CTA exits.  The scalars'
+// test_give_up knob makes the consumers give up at their first wait, which runs that path
+// while every copy completes normally.  The grid-reduction ticket (cnt_a) may stop part-way
+// when a CTA gives up: its count is only right because every PCG run uploads fresh scalars
+// (tickets 0) and the host reads the status before trusting pq or alpha.
 #pragma once
 #include "solver_kernels.cuh"
 
@@ -127,6 +131,7 @@ __global__ void __launch_bounds__(bulk_threads<kCons>(), kMinBlocks)
     static_assert(kBulkStageRows <= 32, "the producer sizes a stage with one warp of bptr loads");
     using St = BulkStage<kCap>;
     if (*(volatile int *)&S->done) return;
+    const bool give_up = S->test_give_up != 0;  // test knob: consumers abandon their first wait
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t full[kStages], empty[kStages];
     __shared__ uint64_t meta[kStages][4];                 // g0, g1, first value, first column
@@ -148,7 +153,7 @@ __global__ void __launch_bounds__(bulk_threads<kCons>(), kMinBlocks)
         // ---------------- producer ----------------
         uint64_t g0 = row0;
         uint32_t b0 = row0 < row_end ? bptr[row0] : 0u;
-        uint32_t k = 0;
+        uint32_t k = 0, nissued = 0;  // stages whose full barrier got its arrival
         for (;; ++k) {
             const int slot = k % kStages;
             if (k >= (uint32_t)kStages) {
@@ -164,6 +169,7 @@ __global__ void __launch_bounds__(bulk_threads<kCons>(), kMinBlocks)
                     meta[slot][1] = g0;
                     bulk::mbar_arrive(&full[slot]);
                 }
+                nissued = k + 1;
                 break;
             }
             const uint64_t gi = g0 + 1 + lane;
@@ -202,15 +208,19 @@ __global__ void __launch_bounds__(bulk_threads<kCons>(), kMinBlocks)
             }
             g0 += nrows;
             b0 = b1;
+            nissued = k + 1;
         }
-        if (timed_out) {
-            if (lane == 0) {
+        if (lane == 0) {
+            if (timed_out) {
                 atomicExch(&S->status, LMTG_ERR_TIMEOUT);
                 atomicExch(&S->done, 1);
-                // copies still in flight: the last stage issued on each slot
-                const uint32_t first = k > (uint32_t)kStages ? k - kStages : 0u;
-                for (uint32_t s = first; s < k; ++s) bulk::mbar_wait(&full[s % kStages], (s / kStages) & 1u);
             }
+            // The CTA leaves only when no copy into its shared memory is in flight: wait (bounded)
+            // for the last stage issued on each slot.  When the consumers took every stage these
+            // phases are complete and each wait returns at once; when they gave up early (a
+            // timeout) the copies are still landing here.
+            const uint32_t first = nissued > (uint32_t)kStages ? nissued - kStages : 0u;
+            for (uint32_t s = first; s < nissued; ++s) bulk::mbar_wait(&full[s % kStages], (s / kStages) & 1u);
         }
     } else {
         // ---------------- consumers ----------------
@@ -223,7 +233,7 @@ __global__ void __launch_bounds__(bulk_threads<kCons>(), kMinBlocks)
         };
         for (uint32_t k = 0;; ++k) {
             const int slot = k % kStages;
-            const bool ok = bulk::mbar_wait(&full[slot], (k / kStages) & 1u);  // every lane acquires
+            const bool ok = !give_up && bulk::mbar_wait(&full[slot], (k / kStages) & 1u);  // every lane acquires
             if (!__all_sync(0xffffffffu, ok)) {
                 timed_out = true;
                 break;

@@ -1,7 +1,12 @@
 #!/bin/sh
-# Builds oracle/_ref/ref_driver from the reference's own sources where they lie (read-only),
-# plus the oracle's element integrand.  Test infrastructure only; outputs go to oracle/_ref/.
-# Needs the LMTpp sources at $LMTPP_SRC (default /root/reference); skipped when absent.
+# Builds the reference drivers of oracle/_ref/ from LMT++'s own sources where they lie (read-only):
+#   ref_codegen  - LMT++'s symbolic engine (include/codegen) driven on the weak forms of the hot
+#                  path; run here, it writes _ref/gen_elem.h, the element routines it emits;
+#   ref_driver   - LMT++'s runtime (make_rect, Sym SparseLine assembly, penalty, LDL, IC(0)-PCG,
+#                  3x3-block IC-PCG) around those routines;
+#   ref_meshio, ref_vtu_elast - LMT++'s mesh reader and VTU writer.
+# Test infrastructure only; outputs go to oracle/_ref/.  The recipe reads the LMTpp sources at
+# $LMTPP_SRC (default /root/reference) and skips everything when they are absent.
 set -e
 HERE="$(cd "$(dirname "$0")" && pwd)"
 SRC="${LMTPP_SRC:-/root/reference}"
@@ -10,22 +15,25 @@ if [ ! -d "$SRC/include" ]; then
   echo "build_ref: no LMTpp sources at $SRC, skipping" >&2
   exit 0
 fi
-mkdir -p "$OUT/obj"
+mkdir -p "$OUT/obj" "$OUT/cg"
 CFLAGS="-O2 -w -DDINT -DDONT_WANT_XML"
+RFLAGS="$CFLAGS -std=gnu++98 -fpermissive -I$SRC/include -I$SRC/include/amd -I$SRC/include/LDL"
 for f in "$SRC"/include/amd/amd_*.c; do
   b=$(basename "$f" .c)
   gcc $CFLAGS -I"$SRC/include/amd" -c "$f" -o "$OUT/obj/$b.o" &
 done
 g++ $CFLAGS -x c++ -I"$SRC/include/amd" -I"$SRC/include/LDL" -c "$SRC/include/LDL/ldl.cpp" -o "$OUT/obj/ldl.o" &
-g++ $CFLAGS -std=gnu++98 -fpermissive -I"$SRC/include" -I"$SRC/include/amd" -I"$SRC/include/LDL" \
-    -c "$SRC/include/util/solveLDL.cpp" -o "$OUT/obj/solveLDL.o" &
-g++ $CFLAGS -std=gnu++98 -fpermissive -I"$SRC/include" -I"$SRC/include/amd" -I"$SRC/include/LDL" \
-    -c "$SRC/include/util/solveLDL_semimorse.cpp" -o "$OUT/obj/solveLDL_semimorse.o" &
-gcc -O2 -std=c99 -c "$HERE/fe_oracle.c" -o "$OUT/obj/fe_oracle.o" &
-g++ $CFLAGS -std=gnu++98 -fpermissive -I"$SRC/include" -I"$SRC/include/amd" -I"$SRC/include/LDL" -I"$HERE" \
-    -c "$HERE/ref_driver.cpp" -o "$OUT/obj/ref_driver.o" &
+g++ $RFLAGS -c "$SRC/include/util/solveLDL.cpp" -o "$OUT/obj/solveLDL.o" &
+g++ $RFLAGS -c "$SRC/include/util/solveLDL_semimorse.cpp" -o "$OUT/obj/solveLDL_semimorse.o" &
+# the symbolic engine (exsolver.cpp needs GSL and is not on this path)
+for f in ex op exvector exmatrix read_ex write_code write_code_language_cpp write_graphviz; do
+  g++ $CFLAGS -std=gnu++98 -fpermissive -I"$SRC/include/codegen" -c "$SRC/include/codegen/$f.cpp" -o "$OUT/cg/$f.o" &
+done
 g++ $CFLAGS -std=gnu++98 -fpermissive -I"$SRC/include" "$HERE/ref_meshio.cpp" -o "$OUT/ref_meshio" &
 g++ $CFLAGS -std=gnu++98 -fpermissive -I"$SRC/include" "$HERE/ref_vtu_elast.cpp" -o "$OUT/ref_vtu_elast" &
 wait
+g++ $CFLAGS -std=gnu++98 -fpermissive -I"$SRC/include/codegen" "$HERE/ref_codegen.cpp" "$OUT"/cg/*.o -o "$OUT/ref_codegen"
+"$OUT/ref_codegen" "$OUT/gen_elem.h"
+g++ $RFLAGS -I"$OUT" -c "$HERE/ref_driver.cpp" -o "$OUT/obj/ref_driver.o"
 g++ -o "$OUT/ref_driver" "$OUT"/obj/*.o -lpthread
-echo "build_ref: $OUT/ref_driver $OUT/ref_meshio $OUT/ref_vtu_elast"
+echo "build_ref: $OUT/ref_driver $OUT/ref_meshio $OUT/ref_vtu_elast (element routines: $OUT/gen_elem.h)"

@@ -89,8 +89,14 @@ int orc_gauss_hexa_order2(double *w, double *xi) {
     return 8;
 }
 
+/* Skin faces are integrated when the reference generates add_skin_elem_matrix
+ * (formal_lf/formulation.py:400-438): with the Python rule of the face element, for Quad
+ * gauss_points[3] of formulations/element_Quad.py:70-75, abscissae (1 -+ sqrt(1/3))/2 at full
+ * precision, weights 1/4. */
+#define QA 0.21132486540518711775
+#define QB 0.78867513459481288225
 int orc_gauss_quad_order2(double *w, double *xi) {
-    static const double t[4][2] = {{GB, GB}, {GA, GB}, {GB, GA}, {GA, GA}};
+    static const double t[4][2] = {{QB, QB}, {QA, QB}, {QB, QA}, {QA, QA}};
     for (int g = 0; g < 4; ++g) {
         w[g] = 0.25;
         xi[2 * g] = t[g][0];
@@ -624,15 +630,18 @@ int orc_make_rect_tetra10(const double X0_[3], const double X1_[3], const uint32
     return next == nn ? 0 : -2;
 }
 
+int orc_gauss_triangle_6pt(double *w, double *xi);
+
 /* Consistent loads of a uniform traction on Triangle_6 faces (6 node ids per face: vertices
- * then mid-edges (01),(12),(20)), order-2 rule of the Triangle_6 table. */
+ * then mid-edges (01),(12),(20)), with the Python rule the generated skin routines integrate by
+ * (formal_lf/formulation.py:400-438; gauss_points[4] of formulations/element_Triangle_6.py:92-99). */
 int orc_tri6_traction(uint64_t nfaces, const uint32_t *faces, const double *pos, const double t[3],
                       double *F) {
-    double w[3], xi[6];
-    orc_gauss_triangle_order2(w, xi);
+    double w[6], xi[12];
+    orc_gauss_triangle_6pt(w, xi);
     for (uint64_t f = 0; f < nfaces; ++f) {
         const uint32_t *q = faces + 6 * f;
-        for (int g = 0; g < 3; ++g) {
+        for (int g = 0; g < 6; ++g) {
             const double u = xi[2 * g], v = xi[2 * g + 1], X0 = 1 - u - v;
             const double N[6] = {X0 * (2 * X0 - 1), u * (2 * u - 1), v * (2 * v - 1),
                                  4 * X0 * u,        4 * u * v,       4 * v * X0};

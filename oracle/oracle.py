@@ -489,19 +489,23 @@ def add_levenberg_marquadt(rowptr, val, max_diag, lm):
 def pressure_loads(faces, pos, p):
     """Consistent loads of a uniform pressure p dS_normal (formulation_elasticity_iso.py:60) on
     Quad4 (4 nodes) or Triangle_6 (6 nodes) skin faces: n = unit cross(dx/dxi0, dx/dxi1) of the
-    face node order (formal_lf/element.py:467-474), order-2 rules (element_Quad.h / element_Triangle_6.h)."""
+    face node order (formal_lf/element.py:467-474), integrated with the Python rules of the face
+    elements as the generated add_skin_elem_matrix does (formal_lf/formulation.py:400-438):
+    element_Quad.py gauss_points[3], element_Triangle_6.py gauss_points[4]."""
     faces = np.asarray(faces, dtype=np.int64)
     F = np.zeros(pos.size)
     if faces.shape[1] == 4:
-        a, b = 0.211324865405, 0.788675134595
-        pts, w = [(b, b), (a, b), (b, a), (a, a)], 0.25
+        a, b = 0.21132486540518711775, 0.78867513459481288225
+        pts, w = [(b, b), (a, b), (b, a), (a, a)], [0.25] * 4
         def shape(u, v):
             N = np.array([(1 - u) * (1 - v), u * (1 - v), u * v, (1 - u) * v])
             du = np.array([-(1 - v), 1 - v, v, -v])
             dv = np.array([-(1 - u), -u, u, 1 - u])
             return N, du, dv
     else:
-        pts, w = [(0.5, 0.0), (0.5, 0.5), (0.0, 0.5)], 1.0 / 6.0
+        a, b = 0.445948490915965, 0.091576213509771
+        pts = [(a, a), (1.0 - 2.0 * a, a), (a, 1.0 - 2.0 * a), (b, b), (1.0 - 2.0 * b, b), (b, 1.0 - 2.0 * b)]
+        w = [0.111690794839005] * 3 + [0.054975871827661] * 3
         def shape(u, v):
             X0 = 1 - u - v
             N = np.array([X0 * (2 * X0 - 1), u * (2 * u - 1), v * (2 * v - 1), 4 * X0 * u, 4 * u * v, 4 * v * X0])
@@ -510,10 +514,10 @@ def pressure_loads(faces, pos, p):
             return N, du, dv
     for q in faces:
         x = pos[q]
-        for (u, v) in pts:
+        for (u, v), wg in zip(pts, w):
             N, du, dv = shape(u, v)
             n = np.cross(du @ x, dv @ x)
             area = np.linalg.norm(n)
             for k, node in enumerate(q):
-                F[3 * node:3 * node + 3] += N[k] * p * (n / area) * w * area
+                F[3 * node:3 * node + 3] += N[k] * p * (n / area) * wg * area
     return F

@@ -1,14 +1,33 @@
-"""Generates the golden fixtures of tests/golden from the reference's own runtime.
+"""Generates the golden fixtures of tests/golden from the reference's own code.
 
-Runs oracle/_ref/ref_driver (LMT++'s make_rect, Sym SparseLine assembly semantics, max|diag|
-penalty constraints, LDL and IC(0)-PCG, built by oracle/build_ref.sh from the LMTpp sources)
-(and the LDL solution of K lambda = u, the adjoint of the misfit 1/2 |u|^2) on the elasticity
-workload of the reference's example -- unit cube of Hexa8 or Tetra_10, penalty clamp
-of x = 0, uniform traction (1,0,0) on x = 1 -- and stores its outputs as compressed npz.
+Runs oracle/_ref/ref_driver, built by oracle/build_ref.sh from the LMTpp sources: LMT++'s
+make_rect, the element routines that LMT++'s Codegen engine writes for the weak forms of
+elasticity_iso and difftherm (oracle/ref_codegen.cpp), its Gauss tables, the Sym SparseLine
+assembly with erase-on-exact-zero, the max|diag| penalty, LDL, IC(0)-PCG and the 3x3-block
+IC(0)-PCG.  Fixtures (compressed npz):
 
-For heat diffusion (formulation difftherm) on Triangle_6 it records the mesh, the Crank-Nicolson
-matrices A = M/dt + K/2 (with the boundary penalty) and B = M/dt - K/2 in the reference's storage,
-and one step A T1 = B T0 solved by the reference's LDL.
+  elem_kernels         distorted single elements (Hexa8, Tetra10 with curved and with straight
+                       edges, nu != 0.3, Triangle_6):
+                       K_e summed over the reference's Gauss table, the skin loads of every face
+                       (f_surf = (0.7,-0.2,0.4), p = 2.5), the difftherm A and B for Crank-Nicolson
+                       and implicit Euler
+  hexa_2x2x2, hexa_10x10x10, tetra10_3x3x3
+                       the elasticity workload of the reference's example (unit cube, penalty clamp
+                       of x = 0, uniform traction (1,0,0) on x = 1): mesh, lower CSR of K, F, the
+                       LDL and IC(0)-PCG solutions, the adjoint LDL solve K lambda = u; for
+                       hexa_10x10x10 also the 3x3-block IC(0)-PCG solution and factor diagonal
+  hexa_16_lognormal    the Hexa8 benchmark family at 16^3: per-element E lognormal (log-std 0.5,
+                       numpy default_rng(20251203), element order), nu 0.3: F, u_ldl, lambda,
+                       the block IC(0)-PCG solution
+  tetra10_10x10x10     the Tetra10 benchmark family at 10^3 cubes: F, u_ldl
+  tri6_8x8_cn          Triangle_6 difftherm, Crank-Nicolson: A, B, one LDL step
+  tri6_32_cn, tri6_32_ie
+                       the transient family at 2 x 32^2: lognormal conductivity (log-std 0.3,
+                       default_rng(20251203)), dt 1e-4, penalty boundary, 10 LDL steps (states 0, 1,
+                       5, 10), A and B, for Crank-Nicolson and implicit Euler
+  batch_cubes          the batch family: cubes of side 3, 5 and 7 with E ~ U[5e4, 3e5] and
+                       nu ~ U[0.2, 0.4] (default_rng(20251203)), four load cases each (+x, +y, +z
+                       unit traction on x = 1, N(0,1) nodal load): F and u_ldl per cube and case
 
 Also records the known-answer vectors of the reference's solver unit tests
 (tests/include/containers/conjugate_gradient_test.cpp:15-71) as JSON.
@@ -26,49 +45,129 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-
-CASES = [  # name, element, nb_points, E, nu, penalty
-    ("hexa_2x2x2", "hexa", 3, 210000.0, 0.3, 1e5),
-    ("hexa_10x10x10", "hexa", 11, 210000.0, 0.3, 1e5),
-    ("tetra10_3x3x3", "tetra10", 4, 210000.0, 0.3, 1e5),
-]
+DRV = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
+SEED = 20251203
 
 
-def run_case(name, elem, nbp, E, nu, pen):
-    drv = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
+def _run(cmd, d, **kw):
+    args = [DRV, cmd] + ["%s=%s" % (k, v) for k, v in kw.items()] + ["out=" + d]
+    subprocess.check_call(args)
+    info = dict(l.split() for l in open(os.path.join(d, "info.txt")))
+    r = lambda f, t: np.fromfile(os.path.join(d, f), dtype=t)
+    return info, r
+
+
+def elast_case(name, elem, nbp, E, nu, pen, dumpK=True, icpcg=True, block_crit=None, efile_E=None,
+               batch_nodal=None):
     npe = 8 if elem == "hexa" else 10
     with tempfile.TemporaryDirectory() as d:
-        subprocess.check_call([drv, elem, str(nbp), repr(E), repr(nu), repr(pen), d])
-        r = lambda f, t: np.fromfile(os.path.join(d, f), dtype=t)
-        info = dict(l.split() for l in open(os.path.join(d, "info.txt")))
-        np.savez_compressed(
-            os.path.join(HERE, name + ".npz"),
-            pos=r("pos.f64", np.float64).reshape(-1, 3), conn=r("conn.u32", np.uint32).reshape(-1, npe),
-            rowptr=r("rowptr.u64", np.uint64), col=r("col.u32", np.uint32), val=r("val.f64", np.float64),
-            F=r("F.f64", np.float64), u_ldl=r("u_ldl.f64", np.float64),
-            u_icpcg=r("u_icpcg.f64", np.float64), lam_ldl=r("lam_ldl.f64", np.float64),
-            meta=np.array(json.dumps(dict(elem=elem, nb_points=nbp, E=E, nu=nu, penalty=pen,
-                                          max_diag=float(info["max_diag"]),
-                                          icpcg_iter=int(info["icpcg_iter"]),
-                                          nnz=int(info["nnz"])))))
+        kw = dict(elem=elem, nbp=nbp, E=repr(E), nu=repr(nu), penalty=repr(pen), dumpK=int(dumpK),
+                  icpcg=int(icpcg))
+        if efile_E is not None:
+            np.asarray(efile_E, dtype=np.float64).tofile(os.path.join(d, "E.f64"))
+            kw["efile"] = os.path.join(d, "E.f64")
+        if block_crit is not None:
+            kw.update(block=1, crit=repr(block_crit))
+        if batch_nodal is not None:
+            np.asarray(batch_nodal, dtype=np.float64).tofile(os.path.join(d, "nodal.f64"))
+            kw.update(batch4=1, nodal=os.path.join(d, "nodal.f64"))
+        info, r = _run("elast", d, **kw)
+        n = int(info["n"])
+        out = dict(F=r("F.f64", np.float64).reshape(-1, n).squeeze(), u_ldl=r("u_ldl.f64", np.float64).reshape(-1, n).squeeze(),
+                   lam_ldl=r("lam_ldl.f64", np.float64))
+        if dumpK:
+            out.update(pos=r("pos.f64", np.float64).reshape(-1, 3), conn=r("conn.u32", np.uint32).reshape(-1, npe),
+                       rowptr=r("rowptr.u64", np.uint64), col=r("col.u32", np.uint32), val=r("val.f64", np.float64))
+        if icpcg:
+            out["u_icpcg"] = r("u_icpcg.f64", np.float64)
+        if block_crit is not None:
+            out["u_block"] = r("u_block.f64", np.float64)
+            out["block_diag"] = r("block_diag.f64", np.float64)
+        meta = dict(elem=elem, nb_points=nbp, E=E, nu=nu, penalty=pen, max_diag=float(info["max_diag"]),
+                    icpcg_iter=int(info["icpcg_iter"]), nnz=int(info["nnz"]), block_crit=block_crit)
+        if efile_E is not None:
+            meta.update(E="lognormal", E_logmean=float(np.log(210000.0)), E_logstd=0.5, seed=SEED)
+        if name is None:
+            return out, meta
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), meta=np.array(json.dumps(meta)), **out)
+        return out, meta
 
 
-def run_tri6(name, nbp, k, rho_c, dt, theta, pen):
-    """Heat diffusion on Triangle_6: mesh, A and B (lower CSR, penalty on A) and one LDL step."""
-    drv = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
+def diff_case(name, nbp, k, rho_c, dt, theta, pen, steps, keep, kfield=None):
     with tempfile.TemporaryDirectory() as d:
-        subprocess.check_call([drv, "tri6", str(nbp), repr(k), repr(rho_c), repr(dt), repr(theta),
-                               repr(pen), d])
-        r = lambda f, t: np.fromfile(os.path.join(d, f), dtype=t)
-        info = dict(l.split() for l in open(os.path.join(d, "info.txt")))
-        np.savez_compressed(
-            os.path.join(HERE, name + ".npz"),
-            pos=r("pos.f64", np.float64).reshape(-1, 2), conn=r("conn.u32", np.uint32).reshape(-1, 6),
-            rowptr=r("rowptr.u64", np.uint64), col=r("col.u32", np.uint32), A=r("val.f64", np.float64),
-            rowptrB=r("rowptrB.u64", np.uint64), colB=r("colB.u32", np.uint32), B=r("valB.f64", np.float64),
-            T0=r("T0.f64", np.float64), T1=r("T1.f64", np.float64),
-            meta=np.array(json.dumps(dict(nb_points=nbp, k=k, rho_c=rho_c, dt=dt, theta=theta, penalty=pen,
-                                          max_diag=float(info["max_diag"])))))
+        kw = dict(nbp=nbp, k=repr(k), rho_c=repr(rho_c), dt=repr(dt), theta=repr(theta), penalty=repr(pen),
+                  steps=steps)
+        if kfield is not None:
+            np.asarray(kfield, dtype=np.float64).tofile(os.path.join(d, "k.f64"))
+            kw["kfile"] = os.path.join(d, "k.f64")
+        info, r = _run("diff", d, **kw)
+        nn = int(info["nn"])
+        states = r("states.f64", np.float64).reshape(steps + 1, nn)
+        out = dict(pos=r("pos.f64", np.float64).reshape(-1, 2), conn=r("conn.u32", np.uint32).reshape(-1, 6),
+                   rowptr=r("rowptr.u64", np.uint64), col=r("col.u32", np.uint32), A=r("val.f64", np.float64),
+                   rowptrB=r("rowptrB.u64", np.uint64), colB=r("colB.u32", np.uint32), B=r("valB.f64", np.float64),
+                   states=states[list(keep)], steps_kept=np.array(keep))
+        if 1 in keep:
+            out.update(T0=states[0], T1=states[1])
+        meta = dict(nb_points=nbp, k=k if kfield is None else "lognormal", rho_c=rho_c, dt=dt, theta=theta,
+                    penalty=pen, steps=steps, max_diag=float(info["max_diag"]))
+        if kfield is not None:
+            meta.update(k_logstd=0.3, seed=SEED)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), meta=np.array(json.dumps(meta)), **out)
+
+
+def elem_kernels():
+    """Single distorted elements through the generated routines."""
+    rng = np.random.default_rng(7)
+    cube = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0], [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]], float)
+    hexa = 0.3 * cube + rng.uniform(-0.02, 0.02, cube.shape)
+    v4 = np.array([[0, 0, 0], [1, 0.1, 0], [0.05, 1, 0.1], [0.1, 0.05, 1.1]]) * 0.4
+    edges = [(0, 1), (1, 2), (0, 2), (0, 3), (1, 3), (2, 3)]  # Tetra_10 nodes 4..9
+    tet = np.vstack([v4, [0.5 * (v4[a] + v4[b]) for a, b in edges]])
+    tet[4:] += rng.uniform(-0.01, 0.01, (6, 3))  # curved edges
+    tri = np.array([[0, 0], [1, 0.1], [0.1, 1], [0.5, 0.06], [0.55, 0.55], [0.04, 0.5]]) * 0.2
+    tri[3:] += rng.uniform(-0.005, 0.005, (3, 2))
+    tets = np.vstack([v4, [0.5 * (v4[a] + v4[b]) for a, b in edges]])  # straight edges
+    res = {"hexa_xyz": hexa, "tetra10_xyz": tet, "tetra10s_xyz": tets, "tri6_xy": tri}
+    cases = {"hexa": (hexa, 123456.0, 0.27), "tetra10": (tet, 210000.0, 0.35),
+             "tetra10s": (tets, 70000.0, 0.21)}
+    with tempfile.TemporaryDirectory() as d:
+        for typ, (xyz, E, nu) in cases.items():
+            xyz.astype(np.float64).tofile(os.path.join(d, "in.f64"))
+            subprocess.check_call([DRV, "elem", "type=" + typ.rstrip("s"), "in=" + os.path.join(d, "in.f64"), "E=" + repr(E),
+                                   "nu=" + repr(nu), "out=" + os.path.join(d, "out.f64")])
+            o = np.fromfile(os.path.join(d, "out.f64"), dtype=np.float64)
+            nd = 3 * xyz.shape[0]
+            res[typ + "_Ke"] = o[:nd * nd].reshape(nd, nd)  # upper triangle (the generated tmp_i_j, j >= i)
+            res[typ + "_skin"] = o[nd * nd:].reshape(-1, nd)
+            res[typ + "_E_nu"] = np.array([E, nu])
+        tri.astype(np.float64).tofile(os.path.join(d, "in.f64"))
+        k, rho_c, dt = 0.7, 1.3, 1e-3
+        subprocess.check_call([DRV, "elem", "type=tri6", "in=" + os.path.join(d, "in.f64"), "k=" + repr(k),
+                               "rho_c=" + repr(rho_c), "dt=" + repr(dt), "out=" + os.path.join(d, "out.f64")])
+        o = np.fromfile(os.path.join(d, "out.f64"), dtype=np.float64).reshape(4, 6, 6)
+        res.update(tri6_A_cn=o[0], tri6_B_cn=o[1], tri6_A_ie=o[2], tri6_B_ie=o[3],
+                   tri6_k_rhoc_dt=np.array([k, rho_c, dt]))
+    res["skin_traction"] = np.array([0.7, -0.2, 0.4])
+    res["skin_pressure"] = np.array(2.5)
+    np.savez_compressed(os.path.join(HERE, "elem_kernels.npz"), **res)
+
+
+def batch_cubes():
+    rng = np.random.default_rng(SEED)
+    sides = [3, 5, 7]
+    E = rng.uniform(5e4, 3e5, len(sides))
+    nu = rng.uniform(0.2, 0.4, len(sides))
+    res = {"sides": np.array(sides), "E": E, "nu": nu}
+    for m, s in enumerate(sides):
+        n = 3 * (s + 1) ** 3
+        g = rng.standard_normal(n)
+        out, meta = elast_case(None, "hexa", s + 1, float(E[m]), float(nu[m]), 1e5, dumpK=False, icpcg=False,
+                               batch_nodal=g)
+        res["F%d" % m] = out["F"]
+        res["u%d" % m] = out["u_ldl"]
+    np.savez_compressed(os.path.join(HERE, "batch_cubes.npz"), meta=np.array(json.dumps(
+        dict(penalty=1e5, seed=SEED, rhs="+x,+y,+z unit traction on x=1; N(0,1) nodal load"))), **res)
 
 
 def cg_known_answers():
@@ -98,14 +197,32 @@ def cg_known_answers():
     }
 
 
-if __name__ == "__main__":
+def main(which):
     subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh")])
-    for c in CASES:
-        run_case(*c)
-        print("wrote", c[0])
-    run_tri6("tri6_8x8_cn", 9, 1.0, 1.0, 1e-3, 0.5, 1e5)
-    print("wrote tri6_8x8_cn")
+    jobs = {
+        "elem_kernels": elem_kernels,
+        "hexa_2x2x2": lambda: elast_case("hexa_2x2x2", "hexa", 3, 210000.0, 0.3, 1e5),
+        "hexa_10x10x10": lambda: elast_case("hexa_10x10x10", "hexa", 11, 210000.0, 0.3, 1e5, block_crit=1e-10),
+        "tetra10_3x3x3": lambda: elast_case("tetra10_3x3x3", "tetra10", 4, 210000.0, 0.3, 1e5),
+        "hexa_16_lognormal": lambda: elast_case(
+            "hexa_16_lognormal", "hexa", 17, 0.0, 0.3, 1e5, dumpK=False, icpcg=False, block_crit=1e-10,
+            efile_E=np.exp(np.log(210000.0) + 0.5 * np.random.default_rng(SEED).standard_normal(16 ** 3))),
+        "tetra10_10x10x10": lambda: elast_case("tetra10_10x10x10", "tetra10", 11, 210000.0, 0.3, 1e5,
+                                               dumpK=False, icpcg=False),
+        "tri6_8x8_cn": lambda: diff_case("tri6_8x8_cn", 9, 1.0, 1.0, 1e-3, 0.5, 1e5, 1, (0, 1)),
+        "tri6_32_cn": lambda: diff_case("tri6_32_cn", 33, 1.0, 1.0, 1e-4, 0.5, 1e5, 10, (0, 1, 5, 10),
+                                        kfield=np.exp(0.3 * np.random.default_rng(SEED).standard_normal(2 * 32 * 32))),
+        "tri6_32_ie": lambda: diff_case("tri6_32_ie", 33, 1.0, 1.0, 1e-4, 1.0, 1e5, 10, (0, 1, 5, 10),
+                                        kfield=np.exp(0.3 * np.random.default_rng(SEED).standard_normal(2 * 32 * 32))),
+        "batch_cubes": batch_cubes,
+    }
+    for name in (which or list(jobs)):
+        jobs[name]()
+        print("wrote", name, flush=True)
     with open(os.path.join(HERE, "cg_known_answers.json"), "w") as f:
         json.dump(cg_known_answers(), f, indent=1)
-    print("wrote cg_known_answers.json")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])
     sys.exit(0)
