@@ -319,13 +319,6 @@ int lmtg_set_inner_reduction(lmtg_ctx *ctx, double inner_reduction);
  * the kind is 0.  No reference counterpart. */
 int lmtg_set_spmv_kind(lmtg_ctx *ctx, int kind);
 
-/* Test knob of the single-system PCG's bulk-copy SpMV (spmv kinds 1 and 2): with on != 0, every
- * following PCG run has the SpMV's consumer warps give up at their first wait on a stage, as a
- * wait that ran out of time does.  The run then ends with LMTG_ERR_TIMEOUT, reported through the
- * PCG scalars, while the producer lets every copy it issued land before the CTA exits; the
- * context stays usable.  on = 0 restores normal runs.  No reference counterpart. */
-int lmtg_test_spmv_give_up(lmtg_ctx *ctx, int on);
-
 /* Self-test of the device-side wait bound used by the bulk-copy SpMVs: one thread waits on an
  * mbarrier that nothing completes.  *status = LMTG_ERR_TIMEOUT when the wait gave up (about
  * 1 s, *waited_s), and the context stays usable.  No reference counterpart. */

@@ -91,7 +91,6 @@ _SIGS = {
     "lmtg_set_inner_reduction": (_i, [_vp, _d]),
     "lmtg_set_spmv_kind": (_i, [_vp, _i]),
     "lmtg_selftest_bounded_wait": (_i, [_vp, _vp, _vp]),
-    "lmtg_test_spmv_give_up": (_i, [_vp, ctypes.c_int]),
     "lmtg_read_msh": (_i, [ctypes.c_char_p, _i, _vp, _vp, _vp, _vp, _vp]),
     "lmtg_write_vtu": (_i, [ctypes.c_char_p, _i, _u64, _vp, _u64, _vp, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp]),
     "lmtg_fit_zone_moduli": (_i, [_vp, ctypes.c_uint32, _vp, _vp, _vp, _vp, _vp, _d, _d, _d, _i, _i, _d, _i,

@@ -483,13 +483,6 @@ __global__ void k_selftest_bounded_wait(long long *out) {
     out[1] = (long long)(globaltimer_ns() - t0);
 }
 
-int lmtg_test_spmv_give_up(lmtg_ctx *c, int on) {
-    return guard(c, [&] {
-        c->test_give_up = on ? 1 : 0;
-        return LMTG_OK;
-    });
-}
-
 int lmtg_selftest_bounded_wait(lmtg_ctx *c, int *status, double *waited_s) {
     return guard(c, [&] {
         DBuf<long long> out;

@@ -97,7 +97,6 @@ struct PcgScalars {
     unsigned cnt_a;  // grid-reduction tickets
     unsigned cnt_b;
     unsigned cnt_c;
-    int test_give_up;  // test knob: the bulk-copy SpMV's consumers give up at their first wait
 };
 
 }  // namespace lmtg
@@ -143,7 +142,6 @@ struct lmtg_ctx {
     // = 2 when a node row has more than 32 blocks, else 1; the grid is set up when the kind
     // in use changes
     int spmv_kind = -1, spmv_setup_kind = -2, spmv_grid = 0;
-    int test_give_up = 0;  // lmtg_test_spmv_give_up: copied into every PCG run's scalars
     lmtg::DBuf<uint32_t> bptr, bcol, bdiag, gptr, gsrc;
 
     // values

@@ -170,7 +170,6 @@ static int run_pcg(lmtg_ctx *c, const T *K, const T *Dinv, const T *b, T *x, T *
     init.crit_kind = crit_kind;
     init.maxit = maxit;
     init.bb = b_norm2 >= 0 ? b_norm2 : 0.0;
-    init.test_give_up = c->test_give_up;
     LMTG_CUDA(cudaMemcpyAsync(c->scal.p, &init, sizeof(init), cudaMemcpyHostToDevice, s));
     if (x_is_zero) {
         LMTG_CUDA(cudaMemcpyAsync(r, b, sizeof(T) * c->n, cudaMemcpyDeviceToDevice, s));

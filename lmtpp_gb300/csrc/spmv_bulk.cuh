@@ -16,11 +16,10 @@
 //
 // Every mbarrier wait is bounded (about a second of %globaltimer, and an iteration cap).  A
 // wait that gives up sets LMTG_ERR_TIMEOUT and done in the PCG scalars; the producer then
-// waits, bounded again, for its own copies in flight before the CTA exits.  The scalars'
-// test_give_up knob makes the consumers give up at their first wait, which runs that path
-// while every copy completes normally.  The grid-reduction ticket (cnt_a) may stop part-way
-// when a CTA gives up: its count is only right because every PCG run uploads fresh scalars
-// (tickets 0) and the host reads the status before trusting pq or alpha.
+// waits, bounded again, for its own copies in flight before the CTA exits.  The grid-reduction
+// ticket (cnt_a) may stop part-way when a CTA gives up (later CTAs return at once on `done`):
+// its count is only right because every PCG run uploads fresh scalars (tickets 0) and the host
+// reads the status before trusting pq or alpha.
 #pragma once
 #include "solver_kernels.cuh"
 
@@ -131,7 +130,6 @@ __global__ void __launch_bounds__(bulk_threads<kCons>(), kMinBlocks)
     static_assert(kBulkStageRows <= 32, "the producer sizes a stage with one warp of bptr loads");
     using St = BulkStage<kCap>;
     if (*(volatile int *)&S->done) return;
-    const bool give_up = S->test_give_up != 0;  // test knob: consumers abandon their first wait
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t full[kStages], empty[kStages];
     __shared__ uint64_t meta[kStages][4];                 // g0, g1, first value, first column
@@ -233,7 +231,7 @@ __global__ void __launch_bounds__(bulk_threads<kCons>(), kMinBlocks)
         };
         for (uint32_t k = 0;; ++k) {
             const int slot = k % kStages;
-            const bool ok = !give_up && bulk::mbar_wait(&full[slot], (k / kStages) & 1u);  // every lane acquires
+            const bool ok = bulk::mbar_wait(&full[slot], (k / kStages) & 1u);  // every lane acquires
             if (!__all_sync(0xffffffffu, ok)) {
                 timed_out = true;
                 break;

@@ -5,10 +5,12 @@
  * It is never linked into the product library.  See fe_oracle.h for the reference
  * file:line each function restates.  Plain C99, one thread, double precision.
  */
+#define _POSIX_C_SOURCE 199309L /* clock_gettime */
 #include "fe_oracle.h"
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 /* ------------------------------------------------------------------------------------------
  * Mesh: make_rect(m, Hexa(), X0, X1, nb_points)  -- include/mesh/make_rect.h:653-679.
@@ -1007,5 +1009,310 @@ done:
     free(d);
     free(q);
     free(s);
+    return ret;
+}
+
+/* ------------------------------------------------------------------------------------------
+ * 3x3-block IC(0) preconditioned CG of the reference, MatWithTinyBlocks<double,Sym<3> >
+ * (include/containers/MatWithTinyBlocks.h): the reference's fastest CPU iterative path for
+ * 3-DOF problems (its documentation times it at 3x the scalar IC-PCG,
+ * include/mesh/exemple_probleme_elastique.txt:228-231).  TEST INFRASTRUCTURE: the CPU baseline.
+ *
+ * Storage: node row R holds its strictly-lower 3x3 blocks in ascending block column (the
+ * reference's RowOfMatWithTinyBlocks) and a lower-stored diagonal block d00 d10 d11 d20 d21 d22
+ * (DB, data[r (r + 1) / 2 + c]).  Blocks are kept row-major here; the reference's SSE2 layout
+ * pairs columns 0 and 1 of a block row in one two-lane register and keeps column 2 apart, so
+ * every sum below keeps that split: a "lane 0" partial over column 0, a "lane 1" partial over
+ * column 1 and a separate partial over column 2, combined as (x - s0 - s1 - f).
+ * ------------------------------------------------------------------------------------------ */
+typedef struct {
+    uint64_t nb;   /* node rows */
+    uint64_t *ptr; /* nb + 1 */
+    uint32_t *col; /* block columns (< row), ascending per row */
+    double *blk;   /* 9 per block, B(i, j) at 3 i + j */
+    double *dg;    /* 6 per row */
+} orc_tiny;
+
+#define DG(dg, i, j) ((i) >= (j) ? (dg)[(i) * ((i) + 1) / 2 + (j)] : (dg)[(j) * ((j) + 1) / 2 + (i)])
+
+/* MatWithTinyBlocks(const Mat<T,Sym<>,SparseLine<> > &) (MatWithTinyBlocks.h:224-270): a block
+ * exists when any of its nine entries is stored in the lower SparseLine rows; absent entries
+ * are 0. */
+static int tiny_from_lower(uint64_t n, const uint64_t *rowptr, const uint32_t *col, const double *val,
+                           orc_tiny *m) {
+    if (n % 3) return -1;
+    const uint64_t nb = n / 3;
+    m->nb = nb;
+    m->ptr = (uint64_t *)calloc(nb + 1, sizeof(uint64_t));
+    m->dg = (double *)calloc(6 * (nb ? nb : 1), sizeof(double));
+    uint32_t *last = (uint32_t *)malloc(sizeof(uint32_t) * (nb ? nb : 1));
+    /* pass 1: count the distinct block columns of each node row (entries are sorted per row) */
+    for (uint64_t R = 0; R < nb; ++R) {
+        uint64_t cnt = 0;
+        uint32_t prev[3] = {0, 0, 0};
+        uint64_t pos[3];
+        for (int a = 0; a < 3; ++a) pos[a] = rowptr[3 * R + a];
+        /* merge the three scalar rows by block column */
+        for (;;) {
+            uint32_t cmin = UINT32_MAX;
+            for (int a = 0; a < 3; ++a)
+                if (pos[a] < rowptr[3 * R + a + 1] && col[pos[a]] / 3 < R && col[pos[a]] / 3 < cmin)
+                    cmin = col[pos[a]] / 3;
+            if (cmin == UINT32_MAX) break;
+            ++cnt;
+            for (int a = 0; a < 3; ++a)
+                while (pos[a] < rowptr[3 * R + a + 1] && col[pos[a]] / 3 == cmin) ++pos[a];
+        }
+        (void)prev;
+        m->ptr[R + 1] = m->ptr[R] + cnt;
+    }
+    const uint64_t total = m->ptr[nb];
+    m->col = (uint32_t *)malloc(sizeof(uint32_t) * (total ? total : 1));
+    m->blk = (double *)calloc(9 * (total ? total : 1), sizeof(double));
+    if (!m->col || !m->blk || !m->ptr || !m->dg) return -2;
+    for (uint64_t R = 0; R < nb; ++R) {
+        uint64_t w = m->ptr[R];
+        uint64_t pos[3];
+        for (int a = 0; a < 3; ++a) pos[a] = rowptr[3 * R + a];
+        for (;;) {
+            uint32_t cmin = UINT32_MAX;
+            for (int a = 0; a < 3; ++a)
+                if (pos[a] < rowptr[3 * R + a + 1] && col[pos[a]] / 3 < R && col[pos[a]] / 3 < cmin)
+                    cmin = col[pos[a]] / 3;
+            if (cmin == UINT32_MAX) break;
+            m->col[w] = cmin;
+            for (int a = 0; a < 3; ++a)
+                while (pos[a] < rowptr[3 * R + a + 1] && col[pos[a]] / 3 == cmin) {
+                    m->blk[9 * w + 3 * a + col[pos[a]] % 3] += val[pos[a]];
+                    ++pos[a];
+                }
+            ++w;
+        }
+        /* the diagonal block: the rest of each scalar row (columns 3R .. 3R + a) */
+        for (int a = 0; a < 3; ++a)
+            for (uint64_t k = pos[a]; k < rowptr[3 * R + a + 1]; ++k) {
+                const uint32_t j = col[k];
+                if (j / 3 != R) continue;
+                const int b = (int)(j % 3);
+                m->dg[6 * R + a * (a + 1) / 2 + b] += val[k];
+            }
+    }
+    free(last);
+    return 0;
+}
+
+static void tiny_free(orc_tiny *m) {
+    free(m->ptr);
+    free(m->col);
+    free(m->blk);
+    free(m->dg);
+}
+
+/* chol_incomp (MatWithTinyBlocks.h:426-520): row by row, each existing block
+ * L_RC = (A_RC - sum_k L_Rk L_Ck^T) L_CC^-T over the columns k that rows R (before this block)
+ * and C share, taken from the highest down (find_corresponding_blocks), then
+ * L_RR = chol(A_RR - sum_k L_Rk L_Rk^T). */
+static void tiny_chol_incomp(orc_tiny *m) {
+    for (uint64_t R = 0; R < m->nb; ++R) {
+        const uint64_t rb = m->ptr[R], re = m->ptr[R + 1];
+        for (uint64_t ic = rb; ic < re; ++ic) {
+            const uint32_t C = m->col[ic];
+            const double *db = m->dg + 6 * C;
+            double *ob = m->blk + 9 * ic;
+            double s0[3][3] = {{0}}, s1[3][3] = {{0}}, f[3][3] = {{0}};
+            int found = 0;
+            /* pairs (k in row C, m in row R before ic) with equal columns, highest first */
+            int64_t i0 = (int64_t)(m->ptr[C + 1] - m->ptr[C]), i1 = (int64_t)(ic - rb);
+            const uint32_t *c0 = m->col + m->ptr[C], *c1 = m->col + rb;
+            for (;;) {
+                if (--i0 < 0 || --i1 < 0) break;
+                int ok = 0;
+                for (;;) {
+                    if (c0[i0] == c1[i1]) {
+                        ok = 1;
+                        break;
+                    } else if (c0[i0] < c1[i1]) {
+                        if (--i1 < 0) break;
+                    } else {
+                        if (--i0 < 0) break;
+                    }
+                }
+                if (!ok) break;
+                found = 1;
+                const double *dj = m->blk + 9 * (m->ptr[C] + (uint64_t)i0);
+                const double *di = m->blk + 9 * (rb + (uint64_t)i1);
+                for (int a = 0; a < 3; ++a)
+                    for (int b = 0; b < 3; ++b) {
+                        s0[a][b] += di[3 * a + 0] * dj[3 * b + 0];
+                        s1[a][b] += di[3 * a + 1] * dj[3 * b + 1];
+                        f[a][b] += di[3 * a + 2] * dj[3 * b + 2];
+                    }
+            }
+            if (found) {
+#define OB(a, b) ob[3 * (a) + (b)]
+#define RS(a, b) (s0[a][b]), (s1[a][b]), (f[a][b])
+                for (int a = 0; a < 3; ++a)
+                    OB(a, 0) = (OB(a, 0) - s0[a][0] - s1[a][0] - f[a][0]) / DG(db, 0, 0);
+                for (int a = 0; a < 3; ++a)
+                    OB(a, 1) = (OB(a, 1) - s0[a][1] - s1[a][1] - f[a][1] - OB(a, 0) * DG(db, 1, 0)) / DG(db, 1, 1);
+                for (int a = 0; a < 3; ++a)
+                    OB(a, 2) = (OB(a, 2) - s0[a][2] - s1[a][2] - f[a][2] - OB(a, 0) * DG(db, 2, 0) -
+                                OB(a, 1) * DG(db, 2, 1)) / DG(db, 2, 2);
+            } else {
+                for (int a = 0; a < 3; ++a) OB(a, 0) = OB(a, 0) / DG(db, 0, 0);
+                for (int a = 0; a < 3; ++a) OB(a, 1) = (OB(a, 1) - OB(a, 0) * DG(db, 1, 0)) / DG(db, 1, 1);
+                for (int a = 0; a < 3; ++a)
+                    OB(a, 2) = (OB(a, 2) - OB(a, 0) * DG(db, 2, 0) - OB(a, 1) * DG(db, 2, 1)) / DG(db, 2, 2);
+            }
+#undef RS
+#undef OB
+        }
+        /* diagonal block (MatWithTinyBlocks.h:497-519) */
+        double s0[3][3] = {{0}}, s1[3][3] = {{0}}, f[3][3] = {{0}};
+        for (uint64_t k = rb; k < re; ++k) {
+            const double *d = m->blk + 9 * k;
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b <= a; ++b) {
+                    s0[a][b] += d[3 * a + 0] * d[3 * b + 0];
+                    s1[a][b] += d[3 * a + 1] * d[3 * b + 1];
+                    f[a][b] += d[3 * a + 2] * d[3 * b + 2];
+                }
+        }
+        double *g = m->dg + 6 * R;
+        g[0] = sqrt(g[0] - s0[0][0] - s1[0][0] - f[0][0]);
+        g[1] = (g[1] - s0[1][0] - s1[1][0] - f[1][0]) / g[0];
+        g[3] = (g[3] - s0[2][0] - s1[2][0] - f[2][0]) / g[0];
+        g[2] = sqrt(g[2] - s0[1][1] - s1[1][1] - f[1][1] - g[1] * g[1]);
+        g[4] = (g[4] - s0[2][1] - s1[2][1] - f[2][1] - g[3] * g[1]) / g[2];
+        g[5] = sqrt(g[5] - s0[2][2] - s1[2][2] - f[2][2] - g[3] * g[3] - g[4] * g[4]);
+    }
+}
+
+/* solve = solve_down then solve_up (MatWithTinyBlocks.h:587-720), in place */
+static void tiny_solve(const orc_tiny *m, double *r) {
+    for (uint64_t R = 0; R < m->nb; ++R) {
+        double s0[3] = {0, 0, 0}, s1[3] = {0, 0, 0}, f[3] = {0, 0, 0};
+        for (uint64_t k = m->ptr[R]; k < m->ptr[R + 1]; ++k) {
+            const double *d = m->blk + 9 * k;
+            const double *v = r + 3 * (uint64_t)m->col[k];
+            for (int a = 0; a < 3; ++a) {
+                s0[a] += d[3 * a + 0] * v[0];
+                s1[a] += d[3 * a + 1] * v[1];
+                f[a] += d[3 * a + 2] * v[2];
+            }
+        }
+        const double *g = m->dg + 6 * R;
+        double *x = r + 3 * R;
+        x[0] -= s0[0] + s1[0] + f[0];
+        x[0] /= g[0];
+        x[1] -= s0[1] + s1[1] + f[1] + g[1] * x[0];
+        x[1] /= g[2];
+        x[2] -= s0[2] + s1[2] + f[2] + g[3] * x[0] + g[4] * x[1];
+        x[2] /= g[5];
+    }
+    for (uint64_t R = m->nb; R-- > 0;) {
+        const double *g = m->dg + 6 * R;
+        double *x = r + 3 * R;
+        x[2] /= g[5];
+        x[0] -= g[3] * x[2];
+        x[1] -= g[4] * x[2];
+        x[1] /= g[2];
+        x[0] -= g[1] * x[1];
+        x[0] /= g[0];
+        for (uint64_t k = m->ptr[R + 1]; k-- > m->ptr[R];) {
+            const double *d = m->blk + 9 * k;
+            double *v = r + 3 * (uint64_t)m->col[k];
+            v[0] = v[0] - (x[0] * d[0] + x[1] * d[3] + x[2] * d[6]);
+            v[1] = v[1] - (x[0] * d[1] + x[1] * d[4] + x[2] * d[7]);
+            v[2] -= x[0] * d[2] + x[1] * d[5] + x[2] * d[8];
+        }
+    }
+}
+
+/* operator* = mul(v, 1) -> partial_mul (MatWithTinyBlocks.h:303-350), one thread */
+static void tiny_mul(const orc_tiny *m, const double *v, double *r) {
+    memset(r, 0, sizeof(double) * 3 * m->nb);
+    for (uint64_t R = 0; R < m->nb; ++R) {
+        const double *vR = v + 3 * R;
+        double s0[3] = {0, 0, 0}, s1[3] = {0, 0, 0}, f[3] = {0, 0, 0};
+        for (uint64_t k = m->ptr[R]; k < m->ptr[R + 1]; ++k) {
+            const double *d = m->blk + 9 * k;
+            const uint64_t c = 3 * (uint64_t)m->col[k];
+            for (int a = 0; a < 3; ++a) {
+                s0[a] += d[3 * a + 0] * v[c + 0];
+                s1[a] += d[3 * a + 1] * v[c + 1];
+                f[a] += d[3 * a + 2] * v[c + 2];
+            }
+            r[c + 0] += d[0] * vR[0] + d[3] * vR[1] + d[6] * vR[2];
+            r[c + 1] += d[1] * vR[0] + d[4] * vR[1] + d[7] * vR[2];
+            double t = 0;
+            t += d[2] * vR[0];
+            t += d[5] * vR[1];
+            t += d[8] * vR[2];
+            r[c + 2] += t;
+        }
+        const double *g = m->dg + 6 * R;
+        for (int a = 0; a < 3; ++a)
+            r[3 * R + a] += s0[a] + s1[a] + f[a] + DG(g, a, 0) * vR[0] + DG(g, a, 1) * vR[1] + DG(g, a, 2) * vR[2];
+    }
+}
+
+/* solve_using_incomplete_chol_factorize for MatWithTinyBlocks (MatWithTinyBlocks.h:1101-1150):
+ * r = b - A x, stop as soon as every |r_i| <= crit (absolute), recursive residual r -= alpha q.
+ * Returns the number of products A d (-1 when maxit is reached), and the factor / solve times. */
+int orc_tiny_block_pcg(uint64_t n, const uint64_t *rowptr, const uint32_t *col, const double *val,
+                       const double *b, double *x, double crit, int maxit, double *diag_out,
+                       double *t_factor, double *t_solve) {
+    orc_tiny A, P;
+    struct timespec t0, t1, t2;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    if (tiny_from_lower(n, rowptr, col, val, &A) || tiny_from_lower(n, rowptr, col, val, &P)) return -2;
+    tiny_chol_incomp(&P);
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    if (diag_out) memcpy(diag_out, P.dg, sizeof(double) * 6 * P.nb);
+    double *r = (double *)malloc(sizeof(double) * n), *d = (double *)malloc(sizeof(double) * n),
+           *q = (double *)malloc(sizeof(double) * n), *s = (double *)malloc(sizeof(double) * n);
+    int ret = -1;
+    tiny_mul(&A, x, q);
+    for (uint64_t i = 0; i < n; ++i) r[i] = b[i] - q[i];
+    int above = 0;
+    for (uint64_t i = 0; i < n; ++i)
+        if (fabs(r[i]) > crit) { above = 1; break; }
+    if (!above) {
+        ret = 0;
+        goto done;
+    }
+    memcpy(d, r, sizeof(double) * n);
+    tiny_solve(&P, d);
+    double deltn = dotv(n, r, d);
+    for (int it = 1; it <= maxit; ++it) {
+        const double delto = deltn;
+        tiny_mul(&A, d, q);
+        const double alpha = deltn / dotv(n, d, q);
+        for (uint64_t i = 0; i < n; ++i) x[i] += alpha * d[i];
+        for (uint64_t i = 0; i < n; ++i) r[i] -= alpha * q[i];
+        above = 0;
+        for (uint64_t i = 0; i < n; ++i)
+            if (fabs(r[i]) > crit) { above = 1; break; }
+        if (!above) {
+            ret = it;
+            goto done;
+        }
+        memcpy(s, r, sizeof(double) * n);
+        tiny_solve(&P, s);
+        deltn = dotv(n, r, s);
+        const double beta = deltn / delto;
+        for (uint64_t i = 0; i < n; ++i) d[i] = s[i] + beta * d[i];
+    }
+done:
+    clock_gettime(CLOCK_MONOTONIC, &t2);
+    if (t_factor) *t_factor = (t1.tv_sec - t0.tv_sec) + 1e-9 * (t1.tv_nsec - t0.tv_nsec);
+    if (t_solve) *t_solve = (t2.tv_sec - t1.tv_sec) + 1e-9 * (t2.tv_nsec - t1.tv_nsec);
+    free(r);
+    free(d);
+    free(q);
+    free(s);
+    tiny_free(&A);
+    tiny_free(&P);
     return ret;
 }

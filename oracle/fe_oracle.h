@@ -132,6 +132,17 @@ int orc_ic_pcg(uint64_t n, const uint64_t *rowptr, const uint32_t *col, const do
 int orc_cg(uint64_t n, const uint64_t *rowptr, const uint32_t *col, const double *val,
            const double *fac, int precond, const double *b, double *x, int crit_kind,
            double crit, int maxit);
+/* The reference's 3x3-block IC(0)-PCG (MatWithTinyBlocks<double,Sym<3> >:
+ * include/containers/MatWithTinyBlocks.h:224-270 construction from the Sym SparseLine lower CSR,
+ * :426-520 chol_incomp, :587-720 solve_down / solve_up, :303-350 the one-thread product,
+ * :1101-1150 solve_using_incomplete_chol_factorize): |r_i| <= crit for every i (absolute),
+ * recursive residual.  x holds the initial guess.  Returns the number of products A d (0 when
+ * the initial residual passes, -1 at maxit, -2 on a bad size); diag_out (optional, 6 per node
+ * row) receives the factor's lower diagonal blocks; t_factor (construction + factorization) and
+ * t_solve (the iterations) in seconds. */
+int orc_tiny_block_pcg(uint64_t n, const uint64_t *rowptr, const uint32_t *col, const double *val,
+                       const double *b, double *x, double crit, int maxit, double *diag_out,
+                       double *t_factor, double *t_solve);
 /* int_e N_a dV per element and node (ne x npe): volume-force weights. */
 int orc_volume_weights(int npe, uint64_t ne, const double *pos, const uint32_t *conn, double *w);
 /* Element fields after the solve at var_inter = 0.5: out ne x 13 = epsilon[6] (tensor shear,

@@ -233,6 +233,22 @@ def ic_pcg(rowptr, col, val, fac, b, crit, maxit=100000, x0=None):
     return x, it
 
 
+def tiny_block_pcg(rowptr, col, val, b, crit, maxit=1000000, x0=None):
+    """The reference's 3x3-block IC(0)-PCG (MatWithTinyBlocks, orc_tiny_block_pcg): returns
+    (x, products of A, factor's diagonal blocks (nn x 6), factor seconds, iteration seconds)."""
+    n = rowptr.shape[0] - 1
+    x = np.zeros(n) if x0 is None else np.array(x0, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    dg = np.zeros(2 * n)
+    tf, ts = ctypes.c_double(), ctypes.c_double()
+    it = lib().orc_tiny_block_pcg(ctypes.c_uint64(n), _p(rowptr, _u64p), _p(col, _u32p), _p(val, _f64p),
+                                  _p(b, _f64p), _p(x, _f64p), ctypes.c_double(crit), ctypes.c_int(maxit),
+                                  _p(dg, _f64p), ctypes.byref(tf), ctypes.byref(ts))
+    if it == -2:
+        raise ValueError("block PCG: the size is not a multiple of 3")
+    return x, it, dg.reshape(-1, 6), tf.value, ts.value
+
+
 def cg(rowptr, col, val, b, crit, crit_kind=2, precond=0, fac=None, maxit=100000, x0=None):
     n = rowptr.shape[0] - 1
     x = np.zeros(n) if x0 is None else np.array(x0, dtype=np.float64)

@@ -43,8 +43,11 @@
 #include "util/solveLDL.h"
 #include <cstdio>
 #include <cstdlib>
+#include <algorithm>
 #include <cstring>
+#include <iostream>
 #include <map>
+#include <sstream>
 #include <string>
 #include <sys/time.h>
 #include <vector>
@@ -285,6 +288,7 @@ static int run_elast(const Args &a) {
         dump(out + "/u_icpcg.f64", u_ic);
     }
     double t_bfac = -1, t_bsolve = -1;
+    int block_it = -1;
     if (arg(a, "block", "0") == "1") {
         /* 3x3-block IC(0) + block PCG (MatWithTinyBlocks.h:426-720, 1101-1150), |r|_inf <= crit */
         double crit = argd(a, "crit") * fmax;
@@ -303,6 +307,18 @@ static int run_elast(const Args &a) {
         std::vector<double> u_b(n);
         for (unsigned i = 0; i < n; ++i) u_b[i] = x[i];
         dump(out + "/u_block.f64", u_b);
+        /* the iteration count: the same solve again with disp_r, which prints max|r| once before
+           the loop and once per product A d */
+        {
+            Vec<double> x2;
+            x2.resize(n, 0.0);
+            std::ostringstream cap;
+            std::streambuf *old = std::cout.rdbuf(cap.rdbuf());
+            solve_using_incomplete_chol_factorize(P, C, b, x2, crit, true);
+            std::cout.rdbuf(old);
+            const std::string txt = cap.str();
+            block_it = (int)std::count(txt.begin(), txt.end(), '\n') - 1;
+        }
         /* the factor's diagonal blocks (lower 3x3, 6 values each) for the restatement's check */
         std::vector<double> dg(6 * (n / 3));
         for (unsigned r = 0; r < n / 3; ++r)
@@ -311,8 +327,8 @@ static int run_elast(const Args &a) {
     }
     FILE *f = fopen((out + "/info.txt").c_str(), "w");
     fprintf(f, "nn %u\nne %u\nn %u\nnnz %zu\nmax_diag %.17g\nncons %u\nnfaces %u\nicpcg_iter %d\n"
-               "t_asm %.6f\nt_block_factor %.6f\nt_block_solve %.6f\n",
-            nn, ne, n, col.size(), max_diag, ncons, nfaces, it, t_asm, t_bfac, t_bsolve);
+               "t_asm %.6f\nt_block_factor %.6f\nt_block_solve %.6f\nblock_iter %d\n",
+            nn, ne, n, col.size(), max_diag, ncons, nfaces, it, t_asm, t_bfac, t_bsolve, block_it);
     fclose(f);
     return 0;
 }

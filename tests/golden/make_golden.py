@@ -84,7 +84,8 @@ def elast_case(name, elem, nbp, E, nu, pen, dumpK=True, icpcg=True, block_crit=N
             out["u_block"] = r("u_block.f64", np.float64)
             out["block_diag"] = r("block_diag.f64", np.float64)
         meta = dict(elem=elem, nb_points=nbp, E=E, nu=nu, penalty=pen, max_diag=float(info["max_diag"]),
-                    icpcg_iter=int(info["icpcg_iter"]), nnz=int(info["nnz"]), block_crit=block_crit)
+                    icpcg_iter=int(info["icpcg_iter"]), nnz=int(info["nnz"]), block_crit=block_crit,
+                    block_iter=int(info["block_iter"]))
         if efile_E is not None:
             meta.update(E="lognormal", E_logmean=float(np.log(210000.0)), E_logstd=0.5, seed=SEED)
         if name is None:

@@ -261,31 +261,6 @@ def test_device_wait_bound_gives_up_and_context_stays_usable():
     f.close()
 
 
-@pytest.mark.parametrize("kind", [1, 2])
-def test_bulk_spmv_give_up_reaches_host_and_context_stays_usable(kind):
-    """The bulk-copy SpMV's own give-up path: with the test knob the consumer warps abandon their
-    first stage wait, as a wait that ran out of time does (every copy still lands: the producer
-    waits, bounded, for its copies before the CTA exits).  LMTG_ERR_TIMEOUT comes back through
-    the PCG scalars, and the same context then solves to the oracle's solution."""
-    import ctypes
-    P = O.elasticity_problem(9)
-    f = problem(P)
-    f.set_spmv_kind(kind)
-    abi.check(f._lib.lmtg_test_spmv_give_up(f._ctx, 1), f._ctx, "test_spmv_give_up")
-    f.assemble(True, True, mixed=True)
-    with pytest.raises(abi.LmtgError) as ei:
-        f.solve_system(1e-12, mode="mixed")
-    assert ei.value.status == abi.ERR_TIMEOUT
-    abi.check(f._lib.lmtg_test_spmv_give_up(f._ctx, 0), f._ctx, "test_spmv_give_up")
-    f.set_result(np.zeros(f.n))
-    st = f.solve(1e-12, mode="mixed")
-    assert st["status"] == abi.OK
-    u = f.get_result()
-    x = O.skyline_solve(P["rowptr"], P["col"], P["val"], P["F"])
-    assert np.linalg.norm(u - x) <= 1e-8 * np.linalg.norm(x)
-    f.close()
-
-
 def fan_tetra10(M=18):
     """Tetra10 fan around a central vertex: 2 M tetrahedra (centre, ring_i, ring_i+1, pole), so
     that the centre's node row holds 5 M + 5 blocks (95 for M = 18; the pattern allows 96)."""

@@ -231,3 +231,21 @@ def test_oracle_elimination_equals_lagrange_solution():
     u = O.skyline_solve(rowptr, col, val2, F2)
     assert np.linalg.norm(u - x) <= 1e-10 * np.linalg.norm(x)
     assert np.abs(u[dofs] - res / coef).max() <= 1e-18
+
+
+@pytest.mark.parametrize("name", ["hexa_10x10x10"])
+def test_block_ic_pcg_restatement_matches_reference(golden_dir, name):
+    """The restated 3x3-block IC(0)-PCG (MatWithTinyBlocks) on the reference's own assembled
+    matrix: the factor's diagonal blocks, the iteration count and the solution of the reference's
+    solve_using_incomplete_chol_factorize at the same absolute |r|_inf criterion."""
+    g = load_golden(golden_dir, name)
+    m = g["meta"]
+    crit = m["block_crit"] * np.abs(g["F"]).max()
+    x, it, dg, tf, ts = O.tiny_block_pcg(g["rowptr"], g["col"], g["val"], g["F"], crit)
+    ref_dg = g["block_diag"].reshape(-1, 6)
+    assert np.abs(dg - ref_dg).max() <= 1e-15 * np.abs(ref_dg).max()
+    assert it == m["block_iter"]
+    u = g["u_block"]
+    assert np.linalg.norm(x - u) <= 1e-12 * np.linalg.norm(u)
+    # and it solves the system: against the LDL solution
+    assert np.linalg.norm(x - g["u_ldl"]) <= 1e-9 * np.linalg.norm(g["u_ldl"])
