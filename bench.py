@@ -12,8 +12,16 @@ computed once, untimed) is <= 1e-10.  The plain FP64 PCG is timed on the same ta
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--side 128]
 
 N > 1 runs N independent replicas (one per GPU, launched by torchrun): the path has no
-data-path exchange to shard on one box.  --impl reference times the CPU restatement of the
-reference's own path (oracle port: assembly + IC(0)-PCG) on a bounded sample.
+data-path exchange to shard on one box.  With N = 1 the line also carries, under "extra", the
+other workload families measured after the headline (--no-extras skips them).
+
+--impl reference times the oracle's restatement of the reference's own CPU path for this
+workload (pattern, assembly with the reference's scatter, max|diag| penalty, 3x3-block IC(0) and
+block PCG -- the reference's solve_system(crit) path for 3-DOF problems) on the FULL workload,
+once and on one thread (the reference's path is sequential): minutes of CPU time, measured and
+not extrapolated, so that arm reports steps = 1 whatever --steps asks.  The reference's C++
+builds only from its sources, which are absent where this runs, so the restatement (pinned to
+the reference build: identical factor, same iteration count) stands in for it.
 """
 import argparse
 import ctypes
@@ -47,9 +55,11 @@ def parse():
     p.add_argument("--elem", default="hexa8", choices=["hexa8", "tetra10"],
                    help="hexa8: N^3 Hexa8 (default N=128); tetra10: N^3 cubes x 6 Tetra10 (N=40)")
     p.add_argument("--cpu-side", type=int, default=0,
-                   help="cubes per side of the CPU sample (default 24 Hexa8 / 8 Tetra10)")
+                   help="cubes per side of the CPU baseline sample (default 48 Hexa8 / 16 Tetra10)")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
+    p.add_argument("--no-extras", action="store_true",
+                   help="skip the other workload families after the headline (adjoint, Tetra10, batch, transient)")
     p.add_argument("--fd", type=int, default=32, help="elements checked by central differences (adjoint mode)")
     p.add_argument("--steps-t", type=int, default=100, help="time steps (transient mode)")
     p.add_argument("--ckpt", type=int, default=10, help="checkpoint interval (transient mode)")
@@ -64,6 +74,12 @@ def parse():
 def lognormal_E(ne, seed=SEED):
     rng = np.random.default_rng(seed)
     return np.exp(np.log(E_MEAN) + E_LOGSTD * rng.standard_normal(ne))
+
+
+def workload_E(elem, ne):
+    """Young's moduli of the workload: lognormal per element for the Hexa8 family, the uniform
+    210000 of the Tetra10 configuration."""
+    return lognormal_E(ne) if elem == "hexa8" else np.full(ne, E_MEAN)
 
 
 def dist_setup(n_gpus):
@@ -217,7 +233,7 @@ def run_gpu(args, rank, world, local, barrier, allmax):
     torch.cuda.set_device(local)
     N = args.side
     pos, conn = make_mesh(args)
-    E = lognormal_E(conn.shape[0])
+    E = workload_E(args.elem, conn.shape[0])
     f = new_problem(pos, conn, E, local)
     stream = torch.cuda.ExternalStream(f.stream_handle(), device=torch.device("cuda", local))
     # FP64 oracle solution (untimed)
@@ -287,62 +303,69 @@ def run_gpu(args, rank, world, local, barrier, allmax):
 
 
 # ------------------------------------------------------------------------------------------
-# CPU arm: the oracle port of the reference's CPU path (assembly with the reference's
-# per-Gauss-point scatter, max|diag| penalty, IC(0) factorization, IC-PCG with the true residual
-# and the |r|_inf test of solve_using_incomplete_chol_factorize), one thread.
+# CPU arm: the oracle's port of the reference's CPU path for 3-DOF problems, on one thread --
+# the structural pattern, the assembly with the reference's per-Gauss-point scatter, the
+# max|diag| penalty, then solve_system(crit) -> MatWithTinyBlocks: the 3x3-block IC(0)
+# factorization and the block PCG with the |r|_inf test of solve_using_incomplete_chol_factorize
+# (include/formulation/formulation.h:1487-1492; include/containers/MatWithTinyBlocks.h:224-720,
+# 1101-1150).  The reference runs this path on one thread: its element scatter is serialized by
+# one mutex and its PCG calls the one-thread product.
 # ------------------------------------------------------------------------------------------
-def cpu_sample(side, elem="hexa8"):
-    """Time-to-solution of the CPU path on a side^3 sample of the same workload family,
-    and its extrapolation to the full workload: assembly scales with the element count,
-    the PCG with element count x iterations (iterations grow like the elements per side)."""
+# |r|_inf <= CPU_CRIT * max|F|: on this family the block PCG's solution then stays within
+# 1e-11 of a 1e-15 solve (measured 2.4e-12 .. 6.6e-12 at 16^3 .. 48^3 with 1e-10; 1e-11 keeps a
+# margin for the larger condition number at 128^3 at a cost of +2% iterations)
+CPU_CRIT = 1e-11
+
+
+def host_info():
+    model = ""
+    try:
+        for l in open("/proc/cpuinfo"):
+            if l.lower().startswith(("model name", "cpu part", "hardware")):
+                model = l.split(":", 1)[1].strip()
+                break
+    except OSError:
+        pass
+    import platform
+    return {"nproc": os.cpu_count(), "cpu": model or platform.processor() or platform.machine(),
+            "machine": platform.machine()}
+
+
+def cpu_reference_run(side, elem="hexa8"):
+    """Time-to-solution of the reference's CPU path on a side^3 mesh of the workload family,
+    measured once (no extrapolation): pattern + assembly + penalty + block IC(0) + block PCG."""
     from oracle import oracle as O
     hexa = elem == "hexa8"
     pos, conn = (O.make_rect_hexa if hexa else O.make_rect_tetra10)(side + 1)
-    E = lognormal_E(conn.shape[0])
-    rowptr, col = O.pattern_lower(pos.shape[0], 3, conn)
+    E = workload_E(elem, conn.shape[0])
     clamped = np.nonzero(pos[:, 0] < 1e-6)[0]
     dofs = (3 * clamped[:, None] + np.arange(3)).ravel()
     faces = O.x1_faces_hexa(pos, conn) if hexa else O.x1_faces_tetra10(pos, conn)
-
-    def assemble():
-        val = O.assemble_elast(pos, conn, E, NU, rowptr, col)
-        F = np.zeros(3 * pos.shape[0])
-        (O.quad4_traction if hexa else O.tri6_traction)(faces, pos, (1.0, 0.0, 0.0), F)
-        O.penalty(rowptr, col, val, F, dofs, np.ones(dofs.shape[0]), np.zeros(dofs.shape[0]), PENALTY)
-        return val, F
-
-    val, F = assemble()
-    fac = O.ic0(rowptr, col, val)
-    ref, _ = O.cg(rowptr, col, val, F, 1e-15, crit_kind=2, precond=0, fac=fac)
-    crit = None
-    for c in (1e-8, 1e-9, 1e-10, 1e-11, 1e-12, 1e-13, 1e-14):
-        x, it = O.ic_pcg(rowptr, col, val, fac, F, c * np.abs(F).max())
-        if it >= 0 and rel_err(x, ref) <= ERR_TARGET:
-            crit = c
-            break
-    if crit is None:
-        raise RuntimeError("CPU IC-PCG never met the error target")
     t0 = time.perf_counter()
-    val, F = assemble()
+    rowptr, col = O.pattern_lower(pos.shape[0], 3, conn)
     t1 = time.perf_counter()
-    fac = O.ic0(rowptr, col, val)
-    x, it = O.ic_pcg(rowptr, col, val, fac, F, crit * np.abs(F).max())
+    val = O.assemble_elast(pos, conn, E, NU, rowptr, col)
+    F = np.zeros(3 * pos.shape[0])
+    (O.quad4_traction if hexa else O.tri6_traction)(faces, pos, (1.0, 0.0, 0.0), F)
+    O.penalty(rowptr, col, val, F, dofs, np.ones(dofs.shape[0]), np.zeros(dofs.shape[0]), PENALTY)
     t2 = time.perf_counter()
-    return {"side": side, "t_asm": t1 - t0, "t_solve": t2 - t1, "iters": it, "crit": crit,
-            "err": rel_err(x, ref), "ne": conn.shape[0], "elem": elem}
+    x, it, _, t_fac, t_pcg = O.tiny_block_pcg(rowptr, col, val, F, CPU_CRIT * np.abs(F).max())
+    t3 = time.perf_counter()
+    Kx = O.spmv(rowptr, col, val, x)
+    return {"side": side, "elem": elem, "ne": conn.shape[0], "ndof": F.shape[0], "t_pattern": t1 - t0,
+            "t_asm": t2 - t1, "t_block_factor": t_fac, "t_block_pcg": t_pcg, "total_s": t3 - t0,
+            "iterations": it, "crit": CPU_CRIT,
+            "rel_residual": float(np.linalg.norm(F - Kx) / np.linalg.norm(F))}
 
 
-def cpu_extrapolate(s, side_full):
-    ne_full = side_full ** 3 * (1 if s["elem"] == "hexa8" else 6)
-    return s["t_asm"] * ne_full / s["ne"] + s["t_solve"] * (side_full / s["side"]) ** 4
-
-
-def cpu_desc(s):
-    return ("%s %d^3 sample of the same workload (lognormal E, penalty clamp, traction): oracle "
-            "port assembly %.3f s + IC(0) + IC-PCG %.3f s (%d it, |r|_inf <= %.0e max|F|, rel err "
-            "%.1e); extrapolated x(ne ratio) for assembly and x(side ratio)^4 for the solve"
-            % ("Hexa8" if s["elem"] == "hexa8" else "Tetra10 (6 per cube)", s["side"], s["t_asm"],
-               s["t_solve"], s["iters"], s["crit"], s["err"]))
+def cpu_desc(s, full):
+    what = "the full workload" if full else "a %d^3 sample of the same workload family" % s["side"]
+    return ("%s (%s), measured once, not scaled: oracle port of the reference's CPU path on one "
+            "thread -- pattern %.2f s + assembly %.2f s + 3x3-block IC(0) %.2f s + block PCG %.2f s "
+            "(%d iterations, |r|_inf <= %.0e max|F|, rel. residual %.1e)"
+            % (what, "Hexa8" if s["elem"] == "hexa8" else "Tetra10, 6 per cube", s["t_pattern"],
+               s["t_asm"], s["t_block_factor"], s["t_block_pcg"], s["iterations"], s["crit"],
+               s["rel_residual"]))
 
 
 # dram__bytes_read.sum + dram__bytes_write.sum / algorithmic bytes of one FP32 PCG SpMV
@@ -364,8 +387,9 @@ def workload_config(args):
         ne, ndof, name = N ** 3, 3 * (N + 1) ** 3, "Hexa8 elasticity %d^3 unit cube" % N
     else:
         ne, ndof, name = 6 * N ** 3, 3 * (2 * N + 1) ** 3, "Tetra10 elasticity %d^3 cubes x 6" % N
-    return {"workload": "%s (%d elements, %d DOF), lognormal E (log-std 0.5, seed %d), nu 0.3, "
-                        "penalty clamp x=0, traction x=1" % (name, ne, ndof, SEED),
+    mat = ("lognormal E (log-std 0.5, seed %d)" % SEED) if args.elem == "hexa8" else "E 210000"
+    return {"workload": "%s (%d elements, %d DOF), %s, nu 0.3, penalty clamp x=0, traction x=1"
+                        % (name, ne, ndof, mat),
             "elements": ne, "dof": ndof, "seed": SEED,
             "error_target": ERR_TARGET, "l2": "inputs larger than L2 (K32 alone > 1 GB)",
             "parallelism": "replicas"}
@@ -374,7 +398,7 @@ def workload_config(args):
 def run_small(args):
     """Single-purpose runs with few launches, for ncu captures."""
     pos, conn = make_mesh(args)
-    f = new_problem(pos, conn, lognormal_E(conn.shape[0]), 0)
+    f = new_problem(pos, conn, workload_E(args.elem, conn.shape[0]), 0)
     out = {"mode": args.mode, "side": args.side, "elem": args.elem}
     if args.mode == "profile":
         f.assemble(True, True, mixed=True)
@@ -388,6 +412,10 @@ def run_small(args):
 
 
 def run_adjoint(args):
+    print(json.dumps(adjoint_extra(args)), flush=True)
+
+
+def adjoint_extra(args):
     """Forward time-to-solution vs adjoint gradient cost (compliance and displacement misfit)
     on the bench workload, and a central-difference check on --fd random elements
     (default_rng(seed + 1)), h = 1e-6 E_e.  J(E +- h) is evaluated through the exact difference
@@ -449,10 +477,14 @@ def run_adjoint(args):
            "fd_max_rel_err_compliance": max(errs_c), "fd_max_rel_err_misfit": max(errs_m),
            "fd_median_rel_err_compliance": float(np.median(errs_c)),
            "fd_median_rel_err_misfit": float(np.median(errs_m))}
-    print(json.dumps(out), flush=True)
+    return out
 
 
 def run_transient(args):
+    print(json.dumps(transient_extra(args)), flush=True)
+
+
+def transient_extra(args, solvers=("fp64", "mixed"), ckpts=None):
     """Transient heat diffusion: unit square of 2 x N^2 Triangle_6 (default N = 1024: 2,097,152
     elements, 4,198,401 nodes), conductivity lognormal (log-std 0.3, default_rng(seed)), rho_c = 1,
     implicit Euler (theta = 1), dt = 1e-4, 100 steps, T = 0 on the boundary (penalty), Gaussian-bump
@@ -480,7 +512,7 @@ def run_transient(args):
                                                                           SEED, args.steps_t),
            "setup_s": setup_s}
     finals = {}
-    for solver in ("fp64", "mixed"):
+    for solver in solvers:
         d.set_solver(solver)
         d.set_state(T0)
         d.run(2, tol=1e-10)  # warm-up (graph capture, caches)
@@ -490,12 +522,13 @@ def run_transient(args):
         finals[solver] = d.get_state()
         out["forward_ms_" + solver] = st_f["device_ms"]
         out["forward_pcg_iters_" + solver] = st_f["iterations"]
-    out["forward_speedup_mixed"] = out["forward_ms_fp64"] / out["forward_ms_mixed"]
-    out["final_state_rel_diff_mixed_vs_fp64"] = float(np.linalg.norm(finals["mixed"] - finals["fp64"]) /
-                                                       np.linalg.norm(finals["fp64"]))
+    if "fp64" in finals:
+        out["forward_speedup_mixed"] = out["forward_ms_fp64"] / out["forward_ms_mixed"]
+        out["final_state_rel_diff_mixed_vs_fp64"] = float(np.linalg.norm(finals["mixed"] - finals["fp64"]) /
+                                                           np.linalg.norm(finals["fp64"]))
     # the adjoint call runs its own forward sweep; backward = call - that forward
     grads = {}
-    for ck in sorted({1, args.ckpt}):
+    for ck in (ckpts or sorted({1, args.ckpt})):
         J, g = d.adjoint_misfit(T0, target, args.steps_t, checkpoint_every=ck, tol=1e-10)
         st_a = d.last_stats
         grads[ck] = g
@@ -512,10 +545,16 @@ def run_transient(args):
     out["adjoint_solver"] = "mixed"
     out["checkpoint_bytes_ck1"] = (args.steps_t + 1) * pos.shape[0] * 8
     d.close()
-    print(json.dumps(out), flush=True)
+    return out
 
 
 def run_batch(args):
+    out = batch_extra(args)
+    if out is not None:
+        print(json.dumps(out), flush=True)
+
+
+def batch_extra(args):
     """Batched elasticity: --nsys (256) Hexa8 cubes with side n ~ U{8..32} elements
     (rng.integers(8, 33)), E ~ U[5e4, 3e5], nu ~ U[0.2, 0.4] per cube (default_rng(seed), drawn in
     that order), clamped on x = 0 (penalty 1e5 x the cube's max|diag|), four right-hand sides:
@@ -586,8 +625,7 @@ def run_batch(args):
     out["n_gpus"] = world
     out["scaling"] = "strong"  # the 256 meshes are shared out over the ranks
     bf.close()
-    if rank == 0:
-        print(json.dumps(out), flush=True)
+    return out if rank == 0 else None
 
 
 def main():
@@ -601,7 +639,7 @@ def main():
     if args.elem == "tetra10" and args.side == 128:
         args.side = 40  # the Tetra10 workload: 40^3 cubes x 6 (1.59 M DOF)
     if args.cpu_side == 0:
-        args.cpu_side = 24 if args.elem == "hexa8" else 8
+        args.cpu_side = 48 if args.elem == "hexa8" else 16
     if args.mode == "adjoint":
         return run_adjoint(args)
     if args.mode != "bench":
@@ -610,18 +648,19 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        samples = []
-        for k in range(args.warmup + args.steps):
-            s = cpu_sample(args.cpu_side, args.elem)
-            if k >= args.warmup:
-                samples.append(cpu_extrapolate(s, args.side))
-        v = statistics.median(samples)
-        line = {"metric": METRIC, "value": v, "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
+        # The reference's CPU path on the full workload, once: a time-to-solution of minutes on
+        # one core is measured, not extrapolated, so this arm runs one step whatever --steps asks
+        # and reports the steps it ran.
+        s = cpu_reference_run(args.side, args.elem)
+        v = s["total_s"]
+        line = {"metric": METRIC, "value": v, "unit": "s", "n_gpus": args.gpus, "steps": 1,
+                "warmup": 0, "steps_requested": args.steps, "warmup_requested": args.warmup,
+                "ms_per_step": v * 1e3, "higher_is_better": False,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                 "config": workload_config(args), "impl": "reference",
                 "cpu_baseline": {"value": v, "unit": "s", "cores": 1, "kind": "port",
-                                 "sample": cpu_desc(s)},
+                                 "sample": cpu_desc(s, True)},
+                "host": host_info(), "reference_run": s,
                 "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
@@ -642,8 +681,8 @@ def main():
     ach64 = b64 / (r["spmv64_ms"] * 1e-3) / 1e9
     # assembly gather bytes: element blocks read, gather indices read, K64 + K32 written
     asm_bytes = r["ne"] * 36 * 9 * 8 + r["ne"] * 64 * 4 + 4 * (r["nnzb"] + 1) + r["nnzb"] * 9 * (8 + 4)
-    s = cpu_sample(args.cpu_side, args.elem)
-    cpu_v = cpu_extrapolate(s, args.side)
+    s = cpu_reference_run(args.cpu_side, args.elem)
+    cpu_v = s["total_s"]
     v = r["ms_mixed"] * 1e-3
     line = {
         "metric": METRIC, "value": v, "unit": "s", "n_gpus": world, "steps": args.steps,
@@ -658,7 +697,8 @@ def main():
                                                        SPMV32_TRAFFIC_RATIO[args.elem]),
                      "peak_source": peak_note, "algorithmic_bytes": b32,
                      "launch_ms": r["spmv32_ms"]},
-        "cpu_baseline": {"value": cpu_v, "unit": "s", "cores": 1, "kind": "port", "sample": cpu_desc(s)},
+        "cpu_baseline": {"value": cpu_v, "unit": "s", "cores": 1, "kind": "port", "sample": cpu_desc(s, False),
+                         "host": host_info()},
         "e2e": ({"value": r["e2e_s"], "unit": "s", "h2d_bytes_per_step": r["h2d"],
                  "d2h_bytes_per_step": r["d2h"], "rel_err": r["e2e_err"]} if "e2e_s" in r else None),
         "gpu_launches": r["launches"],
@@ -671,8 +711,72 @@ def main():
         "asm": {"ms": r["asm_ms"], "gather_bytes": asm_bytes,
                 "GB/s_incl_element_kernel": asm_bytes / (r["asm_ms"] * 1e-3) / 1e9},
         "oracle_solve": r["ref_stats"],
+        "spmv_kind": r.get("spmv_kind"),
     }
+    if world == 1 and not args.no_extras:
+        line["extra"] = run_extras(args)
     print(json.dumps(line), flush=True)
+
+
+def run_extras(args):
+    """The other targets of the workload families, measured on this GPU after the headline:
+    the C3 adjoint (compliance and misfit gradients against the forward solve, 32-element central
+    differences), the Tetra10 40^3 x 6 family (mixed against FP64, its SpMV against the HBM peak),
+    the 256-cube x 4-RHS batch and the 2 x 1024^2 Triangle_6 transient (100 mixed implicit-Euler
+    steps and the adjoint with checkpoints every 10 steps).  Each one's failure is recorded in its
+    key instead of ending the run."""
+    import copy
+    out = {}
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm = peaks.get("hbm_gbs") or 6800.0
+
+    def guarded(name, fn):
+        t0 = time.perf_counter()
+        try:
+            out[name] = fn()
+        except Exception as ex:  # recorded, not fatal: the headline line is already measured
+            out[name] = {"error": "%s: %s" % (type(ex).__name__, ex)}
+        out[name]["wall_s"] = time.perf_counter() - t0
+        print("extra %s: %.1f s" % (name, out[name]["wall_s"]), file=sys.stderr, flush=True)
+
+    def tetra10():
+        a = copy.copy(args)
+        a.elem, a.side, a.steps, a.warmup, a.no_e2e, a.no_fp64 = "tetra10", 40, 2, 1, True, False
+        r = run_gpu(a, 0, 1, 0, (lambda: None), (lambda v: v))
+        b32 = spmv_bytes(r["nn"], r["nnzb"], 4)
+        return {"workload": workload_config(a)["workload"], "mixed_s": r["ms_mixed"] * 1e-3,
+                "fp64_s": r["ms_fp64"] * 1e-3, "mixed_speedup_vs_fp64": r["ms_fp64"] / r["ms_mixed"],
+                "rel_err_mixed": r["err_mixed"], "rel_err_fp64": r["err_fp64"],
+                "iters_mixed": r["stats_mixed"]["iterations"], "iters_fp64": r["stats_fp64"]["iterations"],
+                "spmv32": {"kernel": SPMV32_KERNEL["tetra10"], "launch_ms": r["spmv32_ms"],
+                           "GB/s": b32 / (r["spmv32_ms"] * 1e-3) / 1e9,
+                           "frac": b32 / (r["spmv32_ms"] * 1e-3) / 1e9 / hbm},
+                "spmv_kind": r.get("spmv_kind")}
+
+    def adjoint():
+        a = copy.copy(args)
+        a.elem, a.side, a.tol = "hexa8", 128, ERR_TARGET
+        return adjoint_extra(a)
+
+    def batch():
+        a = copy.copy(args)
+        a.nsys, a.tol, a.gpus = 256, ERR_TARGET, 1
+        return batch_extra(a)
+
+    def transient():
+        a = copy.copy(args)
+        a.side, a.steps_t, a.ckpt = 1024, 100, 10
+        return transient_extra(a, solvers=("mixed",), ckpts=[10])
+
+    guarded("tetra10_40", tetra10)
+    guarded("adjoint_c3", adjoint)
+    guarded("batch_c4", batch)
+    guarded("transient_c5", transient)
+    return out
 
 
 if __name__ == "__main__":

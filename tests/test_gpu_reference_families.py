@@ -6,7 +6,8 @@ the Hexa8 family with lognormal moduli (16^3), the Tetra10 family (10^3 cubes), 
 Triangle_6 family (2 x 32^2, Crank-Nicolson and implicit Euler, 10 steps) and the batch family
 (three cubes x four load cases), each solved by LMT++'s LDL.
 
-Tolerances: element and assembled matrices 1e-12 relative to their largest entry; loads 1e-13;
+Tolerances: element and assembled matrices 1e-12 relative to their largest entry; loads 1e-13
+(single faces) and 1e-14 (assembled, relative to the largest entry);
 FP64 solutions 1e-10 and mixed-precision solutions 1e-8 relative to the LDL solution.
 """
 import json
@@ -130,7 +131,7 @@ def test_hexa_lognormal_family_matches_reference_ldl(golden_dir, mode, tol):
     f.add_skin_traction(x1_faces(pos, conn), (1.0, 0.0, 0.0))
     st = f.solve(1e-14 if mode == "fp64" else 1e-12, mode=mode)
     assert f.get_penalty_scale() == pytest.approx(m["max_diag"], rel=1e-13)
-    np.testing.assert_allclose(f.get_sollicitation(), g["F"], rtol=0, atol=1e-15 * np.abs(g["F"]).max())
+    np.testing.assert_allclose(f.get_sollicitation(), g["F"], rtol=0, atol=1e-14 * np.abs(g["F"]).max())
     u, ref = f.get_result(), g["u_ldl"]
     rel = np.linalg.norm(u - ref) / np.linalg.norm(ref)
     assert rel <= tol, (rel, st)
@@ -160,7 +161,7 @@ def test_tetra10_family_matches_reference_ldl(golden_dir, mode, tol):
     f.add_constraints((3 * clamped[:, None] + np.arange(3)).ravel(), m["penalty"])
     f.add_skin_traction(x1_faces(pos, conn), (1.0, 0.0, 0.0))
     st = f.solve(1e-14 if mode == "fp64" else 1e-12, mode=mode)
-    np.testing.assert_allclose(f.get_sollicitation(), g["F"], rtol=0, atol=1e-15 * np.abs(g["F"]).max())
+    np.testing.assert_allclose(f.get_sollicitation(), g["F"], rtol=0, atol=1e-14 * np.abs(g["F"]).max())
     u, ref = f.get_result(), g["u_ldl"]
     rel = np.linalg.norm(u - ref) / np.linalg.norm(ref)
     assert rel <= tol, (rel, st)
@@ -221,8 +222,8 @@ def test_batch_family_matches_reference_ldl(golden_dir, mode, tol):
         t[r] = 1.0
         bf.add_skin_traction(faces, t)
         bf.assemble(False, True)
-        assert np.abs(bf.get_sollicitation() - B[r]).max() <= 1e-15 * np.abs(B[r]).max()
-    X, st, its = bf.solve_batch(B, mode=mode, tol=1e-14 if mode == "fp64" else 1e-12)
+        assert np.abs(bf.get_sollicitation() - B[r]).max() <= 1e-14 * np.abs(B[r]).max()
+    X, st, its = bf.solve_batch(B, mode=mode, tol=1e-13 if mode == "fp64" else 1e-12)
     for m in range(len(sides)):
         U = g["u%d" % m]
         for r in range(4):
