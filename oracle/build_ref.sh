@@ -16,6 +16,7 @@ if [ ! -d "$SRC/include" ]; then
   exit 0
 fi
 mkdir -p "$OUT/obj" "$OUT/cg"
+echo "$SRC" > "$OUT/lmtpp_src"  # where the sources were found, for the adapter's compile test
 CFLAGS="-O2 -w -DDINT -DDONT_WANT_XML"
 RFLAGS="$CFLAGS -std=gnu++98 -fpermissive -I$SRC/include -I$SRC/include/amd -I$SRC/include/LDL"
 for f in "$SRC"/include/amd/amd_*.c; do
