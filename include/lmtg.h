@@ -348,6 +348,27 @@ int lmtg_fit_zone_moduli(lmtg_ctx *ctx, uint32_t nz, const uint32_t *zone_of_ele
                          int mode, double tol, int maxit, double *history,
                          double *residual_history, double *sensitivity, int *n_iter);
 
+/* Recalage functional (replaces the generated add_elem_matrix / add_nodal_matrix of formulation
+ * recalage, formulations/formulation_recalage.py:1-47, assembled by Formulation::assemble,
+ * include/formulation/formulation.h:1112-1125, nodal terms by add_nodal_matrix at 467-489): the Hessian and minus the gradient at 0 of
+ *   gamma a(V - U, V - U) + (1 - gamma) rho |W - U|^2_L2 + sum_nodes Ud_valid r/(1-r) E |U - Ud|^2
+ * (use_test_functions = False), with the volume terms integrated by the element's Python rule of
+ * order 2 (integration_totale).  Unknowns per node U, V, W then component: DOF 9 I + 3 f + d of
+ * node I, field f (0 U, 1 V, 2 W), component d -- the reference's unknown order with lambd, which
+ * appears in no term, left out.  Needs lmtg_mesh_set (Hexa8 or Tetra10) and lmtg_material_set with
+ * one E and one poisson_ratio; replaces lmtg_allocate_matrices.  Ud: 3 nn doubles, Ud_valid: nn
+ * doubles (both nodal).  omega cancels out of the functional and is only checked non-zero.  After
+ * this call the context holds the 9 nn-unknown system: lmtg_set_constraints takes its DOFs, then
+ * lmtg_recalage_assemble builds it, and lmtg_solve_system / lmtg_get_result /
+ * lmtg_get_matrix_lower / lmtg_get_sollicitation work on it; elasticity assembly, gradients and
+ * element fields refuse it (LMTG_ERR_STATE) until the next lmtg_mesh_set.  On a failure the
+ * mesh must be set again. */
+int lmtg_recalage_setup(lmtg_ctx *ctx, double rho, double omega, double gamma, double r, const double *Ud,
+                        const double *Ud_valid);
+/* Element stiffness and mass blocks, their node-pattern gather, the 9-unknown Hessian and
+ * right-hand side, then the constraints (penalty or exact) and both preconditioners. */
+int lmtg_recalage_assemble(lmtg_ctx *ctx);
+
 /* Sizes of the current problem. */
 int lmtg_get_sizes(lmtg_ctx *ctx, uint64_t *nn, uint64_t *ne, uint64_t *ndof, uint64_t *nnz_blocks);
 

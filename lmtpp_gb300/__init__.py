@@ -12,8 +12,9 @@ from .formulation import (Formulation, make_rect_hexa, make_rect_tetra10, x1_fac
 from .batch import BatchFormulation
 from .fit import FormulationFit
 from .diffusion import Diffusion, make_rect_triangle6
+from .recalage import Recalage
 from . import meshio
 
-__all__ = ["abi", "Formulation", "make_rect_hexa", "make_rect_tetra10", "x1_faces", "x1_faces_hexa",
+__all__ = ["abi", "Recalage", "Formulation", "make_rect_hexa", "make_rect_tetra10", "x1_faces", "x1_faces_hexa",
            "x1_faces_tetra10", "BatchFormulation", "FormulationFit", "Diffusion", "make_rect_triangle6",
            "meshio"]

@@ -63,6 +63,8 @@ _SIGS = {
     "lmtg_set_result": (_i, [_vp, _vp]),
     "lmtg_spmv": (_i, [_vp, _i, _vp, _vp]),
     "lmtg_get_sizes": (_i, [_vp, _vp, _vp, _vp, _vp]),
+    "lmtg_recalage_setup": (_i, [_vp, _d, _d, _d, _d, _vp, _vp]),
+    "lmtg_recalage_assemble": (_i, [_vp]),
     "lmtg_get_launch_count": (_i, [_vp, ctypes.POINTER(_u64)]),
     "lmtg_make_rect_triangle6": (_i, [_vp, _vp, _vp, ctypes.POINTER(_u64), ctypes.POINTER(_u64), _vp, _vp]),
     "lmtg_diff_mesh_set": (_i, [_vp, _u64, _vp, _u64, _vp]),

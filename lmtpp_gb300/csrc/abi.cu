@@ -161,6 +161,7 @@ int lmtg_destroy(lmtg_ctx *c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->h_scal) cudaFreeHost(c->h_scal);
     batch_free(c);
+    recal_free(c);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;  // DBuf destructors free device memory
     return LMTG_OK;
@@ -294,6 +295,7 @@ int lmtg_mesh_set(lmtg_ctx *c, int elem_type, uint64_t nn, const double *pos, ui
         LMTG_CHECK(pos && conn && nn > 0 && ne > 0, LMTG_ERR_ARG, "empty mesh");
         LMTG_CHECK(nn < (1ull << 32), LMTG_ERR_UNSUPPORTED, "more than 2^32 nodes");
         const int npe = elem_type;
+        recal_free(c);
         c->elem_type = elem_type;
         c->npe = npe;
         c->nnu = 3;

@@ -188,6 +188,7 @@ int lmtg_adjoint_grad(lmtg_ctx *c, int objective, const double *target, const do
     memset(st, 0, sizeof(*st));
     return guard3(c, [&] {
         LMTG_CHECK(c->have64 && c->have_vec, LMTG_ERR_STATE, "assemble (FP64) and solve first");
+        LMTG_CHECK(c->nnu == 3, LMTG_ERR_STATE, "elasticity gradient on another formulation's context");
         LMTG_CHECK(dJdE && J, LMTG_ERR_ARG, "null output");
         LMTG_CHECK(c->penalty != 0.0 || c->nc == 0, LMTG_ERR_UNSUPPORTED, "adjoint gradients with exact (penalty 0) constraints");
         LMTG_CHECK(objective == LMTG_OBJ_COMPLIANCE || objective == LMTG_OBJ_MISFIT ||

@@ -103,6 +103,7 @@ struct PcgScalars {
 
 namespace lmtg {
 struct BatchState;  // batch.cu
+struct RecalState;  // recalage.cu
 }
 
 struct lmtg_ctx {
@@ -137,7 +138,8 @@ struct lmtg_ctx {
     // pattern
     bool allocated = false;
     uint64_t nnzb = 0, nnz_lower = 0, ngather = 0;
-    uint32_t max_row_blocks = 0;  // blocks in the widest node row (<= 96)
+    uint32_t max_row_blocks = 0;  // blocks in the widest node row (<= 96; <= 288 on the recalage's
+                                  // virtual pattern, whose FP32 SpMV is then the warp-row kernel)
     // FP32 PCG SpMV: 0 = warp per row pair, 1, 2 = bulk-copy pipeline (solver.cu), -1 (default)
     // = 2 when a node row has more than 32 blocks, else 1; the grid is set up when the kind
     // in use changes
@@ -181,6 +183,10 @@ struct lmtg_ctx {
     lmtg::DBuf<lmtg::PcgScalars> scal;
     lmtg::PcgScalars *h_scal = nullptr;  // pinned mirror
 
+    // recalage functional (recalage.cu): the mesh's node pattern and element blocks, while the
+    // context's pattern and matrices hold the 9-unknown system (nnu = 9)
+    lmtg::RecalState *recal = nullptr;
+
     // number of kernels this context has launched (reported by lmtg_get_launch_count)
     uint64_t launches = 0;
 };
@@ -221,6 +227,9 @@ inline void upload_u32(lmtg_ctx *c, DBuf<T> &d, const T *h, size_t n) {
     d.alloc(n);
     if (n) LMTG_CUDA(cudaMemcpyAsync(d.p, h, n * sizeof(T), cudaMemcpyHostToDevice, c->stream));
 }
+
+// ---- recalage (recalage.cu) ----
+void recal_free(lmtg_ctx *c);
 
 // ---- batches (batch.cu) ----
 void batch_free(lmtg_ctx *c);

@@ -66,8 +66,10 @@ static int bulk_grid(lmtg_ctx *c) {
 }
 
 // the kind in use: -1 picks the 5-CTA instance for wide rows (Tetra10: 0.108 against 0.111 ms
-// at 40^3) and the 4-CTA one otherwise (Hexa8: 0.363 against 0.369 ms at 128^3)
+// at 40^3) and the 4-CTA one otherwise (Hexa8: 0.363 against 0.369 ms at 128^3); rows of more
+// than 96 blocks (the recalage's virtual pattern) always take the warp-row kernel
 static int spmv_kind_used(const lmtg_ctx *c) {
+    if (c->max_row_blocks > 96) return 0;
     return c->spmv_kind >= 0 ? c->spmv_kind : (c->max_row_blocks > 32 ? 2 : 1);
 }
 

@@ -358,6 +358,130 @@ void orc_hexa8_elast_ke(const double *xyz, double E, double nu, double *Ke) {
 }
 
 /* ------------------------------------------------------------------------------------------
+ * recalage (formulations/formulation_recalage.py:25-47): with use_test_functions = False the
+ * generated routines hold the Hessian of
+ *   gamma (sigma(V) - sigma(U)) : K^-1 (sigma(V) - sigma(U)) dV + (1 - gamma) rho |W - U|^2 dV
+ *   + Ud_valid r / (1 - r) E |U - Ud|^2 dN
+ * (formal_lf/calculate_matrix.py:4-61), unknowns per node U, V, W then component.  Since
+ * K^-1 sigma = epsilon, the first term's Hessian is 2 gamma times the elasticity matrix; the
+ * second's is 2 (1 - gamma) rho N_a N_b on the matching components.  The volume part is integrated
+ * by the Python rule of order 2 (integration_totale, formal_lf/formulation.py:549-551): Hexa
+ * gauss_points[2] (formulations/element_Hexa.py:136-146), Tetra_10 gauss_points[2]
+ * (formulations/element_Tetra_10.py:107-113).
+ * ------------------------------------------------------------------------------------------ */
+static uint64_t find_col(const uint64_t *rowptr, const uint32_t *col, uint64_t row, uint32_t c);
+
+static int recal_rule(int npe, double *w, double *xi) {
+    if (npe == 8) {
+        const double a = 1.0 / sqrt(3.0), lo = (1 - a) / 2.0, hi = (1 + a) / 2.0;
+        const double p[8][3] = {{lo, lo, lo}, {hi, lo, lo}, {hi, hi, lo}, {lo, hi, lo},
+                                {lo, lo, hi}, {hi, lo, hi}, {hi, hi, hi}, {lo, hi, hi}};
+        for (int g = 0; g < 8; ++g) {
+            w[g] = 1.0 / 8.0;
+            for (int d = 0; d < 3; ++d) xi[3 * g + d] = p[g][d];
+        }
+        return 8;
+    }
+    const double a = (5.0 - sqrt(5.0)) / 20.0, b = (5.0 + 3.0 * sqrt(5.0)) / 20.0;
+    const double p[4][3] = {{a, a, a}, {b, a, a}, {a, b, a}, {a, a, b}};
+    for (int g = 0; g < 4; ++g) {
+        w[g] = 1.0 / 24.0;
+        for (int d = 0; d < 3; ++d) xi[3 * g + d] = p[g][d];
+    }
+    return 4;
+}
+
+void orc_recalage_ke(int npe, const double *xyz, double E, double nu, double rho, double gamma, double *K) {
+    const int nd = 9 * npe, ns = 3 * npe;
+    double w[8], xi[24], Ks[900], dN[10][3], N[10], M[10][10];
+    const int ngp = recal_rule(npe, w, xi);
+    memset(Ks, 0, sizeof(Ks));
+    memset(M, 0, sizeof(M));
+    for (int g = 0; g < ngp; ++g) {
+        if (npe == 8) {
+            hexa8_dN(xi + 3 * g, (double (*)[3])dN);
+            hexa8_N(xi + 3 * g, N);
+        } else {
+            tetra10_dN(xi + 3 * g, (double (*)[3])dN);
+            tetra10_N(xi + 3 * g, N);
+        }
+        const double det = elast_gp(npe, xyz, (const double (*)[3])dN, E, nu, w[g], Ks);
+        for (int a = 0; a < npe; ++a)
+            for (int b = 0; b < npe; ++b) M[a][b] += w[g] * det * N[a] * N[b];
+    }
+    const double cK = 2.0 * gamma, cM = 2.0 * (1.0 - gamma) * rho;
+    memset(K, 0, sizeof(double) * nd * nd);
+    for (int a = 0; a < npe; ++a)
+        for (int b = 0; b < npe; ++b)
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) {
+                    const double k = Ks[ns * (3 * a + i) + 3 * b + j], m = i == j ? M[a][b] : 0.0;
+                    double *r0 = K + (size_t)nd * (9 * a + i), *r1 = r0 + 3 * nd, *r2 = r0 + 6 * nd;
+                    const int c = 9 * b + j;
+                    r0[c] = cK * k + cM * m;   /* UU */
+                    r0[c + 3] = -cK * k;       /* UV */
+                    r0[c + 6] = -cM * m;       /* UW */
+                    r1[c] = -cK * k;           /* VU */
+                    r1[c + 3] = cK * k;        /* VV */
+                    r2[c] = -cM * m;           /* WU */
+                    r2[c + 6] = cM * m;        /* WW */
+                }
+}
+
+void orc_recalage_nodal(const double ud[3], double valid, double E, double r, double *Kn, double *Fn) {
+    const double c = 2.0 * valid * r / (1.0 - r) * E;
+    memset(Kn, 0, sizeof(double) * 81);
+    memset(Fn, 0, sizeof(double) * 9);
+    for (int d = 0; d < 3; ++d) {
+        Kn[9 * d + d] = c;
+        Fn[d] = c * ud[d];
+    }
+}
+
+/* Scatter of the element Hessians (upper triangle, rows max(i,j) of the Sym storage) and of the
+ * nodal part of every node (add_nodal_matrix) into the lower CSR pattern of nnu = 9. */
+int orc_assemble_recalage(int npe, uint64_t nn, uint64_t ne, const double *pos, const uint32_t *conn, double E,
+                          double nu, double rho, double gamma, double r, const double *Ud, const double *Uv,
+                          const uint64_t *rowptr, const uint32_t *col, double *val, double *F) {
+    if (npe != 8 && npe != 10) return -1;
+    const int nd = 9 * npe;
+    double xyz[30];
+    double *K = (double *)malloc(sizeof(double) * nd * nd);
+    if (!K) return -3;
+    memset(val, 0, sizeof(double) * rowptr[nn * 9]);
+    memset(F, 0, sizeof(double) * nn * 9);
+    for (uint64_t e = 0; e < ne; ++e) {
+        const uint32_t *c = conn + (uint64_t)npe * e;
+        for (int a = 0; a < npe; ++a)
+            for (int d = 0; d < 3; ++d) xyz[3 * a + d] = pos[3 * (uint64_t)c[a] + d];
+        orc_recalage_ke(npe, xyz, E, nu, rho, gamma, K);
+        for (int i = 0; i < nd; ++i)
+            for (int j = i; j < nd; ++j) {
+                const uint64_t gi = 9 * (uint64_t)c[i / 9] + i % 9, gj = 9 * (uint64_t)c[j / 9] + j % 9;
+                const uint64_t row = gi > gj ? gi : gj, cl = gi > gj ? gj : gi;
+                const uint64_t p = find_col(rowptr, col, row, (uint32_t)cl);
+                if (p == (uint64_t)-1) {
+                    free(K);
+                    return -2;
+                }
+                val[p] += K[(size_t)nd * i + j];
+            }
+    }
+    free(K);
+    double Kn[81], Fn[9];
+    for (uint64_t n = 0; n < nn; ++n) {
+        orc_recalage_nodal(Ud + 3 * n, Uv[n], E, r, Kn, Fn);
+        for (int p = 0; p < 9; ++p) {
+            const uint64_t q = find_col(rowptr, col, 9 * n + p, (uint32_t)(9 * n + p));
+            if (q == (uint64_t)-1) return -2;
+            val[q] += Kn[9 * p + p];
+            F[9 * n + p] += Fn[p];
+        }
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------------------------
  * Structural pattern: ResizeMat::GetNZ (include/formulation/formulation.h:200-241) -- every
  * node pair (a,b) of an element gives the nnu x nnu block of DOF pairs; indice_noda[node] =
  * node * nnu (no reordering, formulation.h:283-325).  Restated lower part only.

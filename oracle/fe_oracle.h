@@ -69,6 +69,15 @@ double orc_tetra10_elast_gp(const double *xyz, double E, double nu, double w, co
                             double *Ke);
 void orc_tetra10_elast_ke(const double *xyz, double E, double nu, double *Ke);
 
+/* recalage (formulations/formulation_recalage.py): the element Hessian (9npe x 9npe, row-major,
+ * unknowns per node U, V, W then component; the Python rule of order 2), one node's nodal part
+ * (9 x 9 and 9), and the assembly of both into the lower CSR of orc_pattern_lower(nn, 9, ...). */
+void orc_recalage_ke(int npe, const double *xyz, double E, double nu, double rho, double gamma, double *K);
+void orc_recalage_nodal(const double ud[3], double valid, double E, double r, double *Kn, double *Fn);
+int orc_assemble_recalage(int npe, uint64_t nn, uint64_t ne, const double *pos, const uint32_t *conn, double E,
+                          double nu, double rho, double gamma, double r, const double *Ud, const double *Uv,
+                          const uint64_t *rowptr, const uint32_t *col, double *val, double *F);
+
 /* Triangle_6 heat diffusion: stiffness a grad.grad and mass N N (6x6 each, 6-point rule). */
 int orc_gauss_triangle_6pt(double *w, double *xi);
 void orc_triangle6_diff_km(const double *xy, double a, double *Ke, double *Me);

@@ -146,6 +146,41 @@ def assemble_elast(pos, conn, E, nu, rowptr, col):
     return val
 
 
+def recalage_ke(xyz, E, nu, rho, gamma):
+    """The recalage element Hessian (orc_recalage_ke), 9 npe x 9 npe."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    npe = xyz.shape[0]
+    K = np.zeros((9 * npe, 9 * npe))
+    lib().orc_recalage_ke(ctypes.c_int(npe), _p(xyz, _f64p), ctypes.c_double(E), ctypes.c_double(nu),
+                          ctypes.c_double(rho), ctypes.c_double(gamma), _p(K, _f64p))
+    return K
+
+
+def recalage_nodal(ud, valid, E, r):
+    ud = np.ascontiguousarray(ud, dtype=np.float64)
+    Kn, Fn = np.zeros((9, 9)), np.zeros(9)
+    lib().orc_recalage_nodal(_p(ud, _f64p), ctypes.c_double(valid), ctypes.c_double(E), ctypes.c_double(r),
+                             _p(Kn, _f64p), _p(Fn, _f64p))
+    return Kn, Fn
+
+
+def assemble_recalage(pos, conn, E, nu, rho, gamma, r, Ud, Uv, rowptr, col):
+    """(val, F) of the recalage system on the lower CSR pattern of pattern_lower(nn, 9, conn)."""
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    conn = np.ascontiguousarray(conn, dtype=np.uint32)
+    Ud = np.ascontiguousarray(Ud, dtype=np.float64).reshape(-1)
+    Uv = np.ascontiguousarray(Uv, dtype=np.float64).reshape(-1)
+    nn = pos.shape[0]
+    val, F = np.zeros(col.shape[0]), np.zeros(9 * nn)
+    rc = lib().orc_assemble_recalage(ctypes.c_int(conn.shape[1]), ctypes.c_uint64(nn), ctypes.c_uint64(conn.shape[0]),
+                                     _p(pos, _f64p), _p(conn, _u32p), ctypes.c_double(E), ctypes.c_double(nu),
+                                     ctypes.c_double(rho), ctypes.c_double(gamma), ctypes.c_double(r), _p(Ud, _f64p),
+                                     _p(Uv, _f64p), _p(rowptr, _u64p), _p(col, _u32p), _p(val, _f64p), _p(F, _f64p))
+    if rc:
+        raise RuntimeError("orc_assemble_recalage failed: %d" % rc)
+    return val, F
+
+
 def elem_fields(pos, conn, E, nu, u):
     """Element fields after the solve (orc_elem_fields): ne x 13 = epsilon[6], sigma[6],
     tr_epsilon at var_inter = 0.5.  E: 1 or ne values; nu: scalar or ne values."""

@@ -257,12 +257,16 @@ static Ex trace_sym_col(const ExVector &sigma, const ExVector &epstest) {
     return res;
 }
 
-/* calculate_matrix (calculate_matrix.py:4-61) for a linear form, differentiation branch */
+/* calculate_matrix (calculate_matrix.py:4-61) for a linear form, differentiation branch.  With
+ * test = false (use_test_functions = False) the tests are the unknowns themselves, and the
+ * substitution tests -> 0 concerns the formulation's own test symbols, which an energy does not
+ * contain: nothing is substituted. */
 static void calculate_matrix(const Ex &expr, const std::vector<Ex> &unk, const std::vector<Ex> &tst,
-                             std::vector<std::vector<Ex> > &M, std::vector<Ex> &V) {
+                             std::vector<std::vector<Ex> > &M, std::vector<Ex> &V, bool test = true) {
     MapEx subs_lin, subs_tes;
     for (unsigned i = 0; i < unk.size(); ++i) subs_lin[unk[i]] = number(0.0);
-    for (unsigned i = 0; i < tst.size(); ++i) subs_tes[tst[i]] = number(0.0);
+    if (test)
+        for (unsigned i = 0; i < tst.size(); ++i) subs_tes[tst[i]] = number(0.0);
     M.assign(tst.size(), std::vector<Ex>());
     V.assign(tst.size(), Ex());
     for (unsigned i = 0; i < tst.size(); ++i) {
@@ -533,25 +537,152 @@ static std::string gen_difftherm_tri6(const std::string &fname, double left, dou
     return out.str();
 }
 
+/* recalage (formulations/formulation_recalage.py:25-47): the modified constitutive-relation-error
+ * energy in the unknowns U, V, W (lambd appears in no term and is left out), minimised
+ * (use_test_functions = False: calculate_matrix takes the tests to be the unknowns, so M is the
+ * energy's Hessian and V minus its gradient at 0).  Unknowns per node: U, V, W, then component.
+ * The volume part is integrated by the element's Python rule of order 2 (integration_totale,
+ * formulation.py:549-551; element_Hexa.py gauss_points[2], element_Tetra_10.py gauss_points[2]);
+ * the nodal part (norme_G, dN) is the routine of node 0 (formulation.py:538-546), applied at every
+ * node by add_nodal_matrix. */
+static std::string gen_recalage(const std::string &elem_name, const std::string &fname) {
+    FElem e;
+    init_elem(e, elem_name);
+    const int nn = e.nb_nodes, dim = e.dim;
+    std::vector<Ex> unk;
+    std::vector<std::vector<std::vector<Ex> > > F(3, std::vector<std::vector<Ex> >(dim, std::vector<Ex>(nn)));
+    const char *fld = "UVW";
+    for (int i = 0; i < nn; ++i)
+        for (int f = 0; f < 3; ++f)
+            for (int d = 0; d < dim; ++d) {
+                std::ostringstream o;
+                o << fld[f] << i << "_" << d;
+                F[f][d][i] = sym(o.str());
+                unk.push_back(F[f][d][i]);
+            }
+    std::vector<std::vector<Ex> > udn(dim, std::vector<Ex>(nn));
+    std::vector<Ex> udv(nn);
+    for (int i = 0; i < nn; ++i) {
+        for (int d = 0; d < dim; ++d) udn[d][i] = sym(idx("Ud", dim * i + d));
+        udv[i] = sym(idx("Ud_valid", i));
+    }
+    ExVector U(dim), V(dim), W(dim), Ud(dim);
+    for (int d = 0; d < dim; ++d) {
+        U[d] = nodal_expr(e, F[0][d]);
+        V[d] = nodal_expr(e, F[1][d]);
+        W[d] = nodal_expr(e, F[2][d]);
+        Ud[d] = nodal_expr(e, udn[d]);
+    }
+    const Ex Ud_valid = nodal_expr(e, udv);
+    Ex E = sym("E"), nu = sym("nu"), rho = sym("rho"), omega = sym("omega"), gamma = sym("gamma"), r = sym("r");
+    Ex dV = sym("dV"), dN = sym("dN");
+    ExMatrix K = hooke_isotrope_3d(E, nu);
+    ExVector epsilon_V = grad_sym_col(e, V), epsilon_U = grad_sym_col(e, U);
+    ExVector sigma_V = mul_mv(K, epsilon_V), sigma_U = mul_mv(K, epsilon_U);
+    ExVector gamma_w = rho * omega * W, gamma_u = rho * omega * U;
+    ExMatrix Kinv = K.inverse();
+    ExVector ds = sigma_V - sigma_U, dg = gamma_w - gamma_u, du = U - Ud;
+    /* norme_sigma, norme_gamma, norme_G of formulation_recalage.py:27-32 */
+    Ex res = gamma * (trace_sym_col(ds, mul_mv(Kinv, ds)) * dV);
+    res += (1.0 - gamma) * (1.0 / (rho * pow(omega, 2)) * dot(dg, dg) * dV);
+    res += Ud_valid * r / (1.0 - r) * (E * dot(du, du) * dN);
+    Ex form = 0.0 + 1.0 * res;  /* time integration: no time dependence, one point of weight 1 */
+    /* nodal part: var_inter -> 0, node 0's unknowns only */
+    Ex dN_part = form.diff(dN);
+    {
+        MapEx s0;
+        for (int k = 0; k < e.nvi; ++k) s0[e.vi[k]] = number(0.0L);
+        dN_part = dN_part.subs(s0);
+    }
+    std::vector<Ex> unk0;
+    for (int f = 0; f < 3; ++f)
+        for (int d = 0; d < dim; ++d) unk0.push_back(F[f][d][0]);
+    std::vector<std::vector<Ex> > Mn;
+    std::vector<Ex> Vn;
+    calculate_matrix(dN_part, unk0, unk0, Mn, Vn, false);
+    form = form.subs(dN, number(0.0L));
+    /* volume part, integration_totale: element.integration(form.diff(dV), 2) */
+    Ex expr = form.diff(dV) * e.det_jac;
+    Ex dV_part = 0.0;
+    if (elem_name == "Hexa") {
+        Ex a = 1.0 / sqrt(Ex(3.0));
+        Ex lo = (1.0 - a) / 2.0, hi = (1.0 + a) / 2.0;
+        Ex pts[8][3] = {{lo, lo, lo}, {hi, lo, lo}, {hi, hi, lo}, {lo, hi, lo},
+                        {lo, lo, hi}, {hi, lo, hi}, {hi, hi, hi}, {lo, hi, hi}};
+        for (int g = 0; g < 8; ++g) {
+            MapEx mp;
+            for (int k = 0; k < 3; ++k) mp[e.vi[k]] = pts[g][k];
+            dV_part = dV_part + (1.0 / 8.0) * expr.subs(mp);
+        }
+    } else {
+        Ex s5 = sqrt(Ex(5.0));
+        Ex a = (5.0 - s5) / 20.0, b = (5.0 + 3.0 * s5) / 20.0, pw = Ex(1.0 / 24.0);
+        Ex pts[4][3] = {{a, a, a}, {b, a, a}, {a, b, a}, {a, a, b}};
+        for (int g = 0; g < 4; ++g) {
+            MapEx mp;
+            for (int k = 0; k < 3; ++k) mp[e.vi[k]] = pts[g][k];
+            dV_part = dV_part + pw * expr.subs(mp);
+        }
+    }
+    std::vector<std::vector<Ex> > M;
+    std::vector<Ex> Vv;
+    calculate_matrix(dV_part, unk, unk, M, Vv, false);
+    std::ostringstream out;
+    const int nd = 3 * dim * nn;
+    out << "/* " << elem_name << " recalage: the whole element's Hessian (upper triangle of " << nd << "x" << nd
+        << ", unknowns node-major then U, V, W then component) */\n"
+        << "static void " << fname << "(const double *P, double E, double nu, double rho, double omega,\n"
+        << "    double gamma, double *K) {\n"
+        << "    typedef double T;\n"
+        << write_matrix(M, Vv, true, "K", 0) << "}\n\n"
+        << "/* recalage nodal part (norme_G) of one node: 9x9 upper triangle and the vector */\n"
+        << "static void " << fname << "_nodal(const double *Ud, const double *Ud_valid, double E, double r,\n"
+        << "    double *K, double *F) {\n"
+        << "    typedef double T;\n"
+        << write_matrix(Mn, Vn, true, "K", "F") << "}\n\n";
+    return out.str();
+}
+
+/* Splits the generated text into a header of declarations and a source of definitions: the
+ * definitions are large straight-line functions, compiled once in their own unit. */
+static void split(const std::string &code, std::string &decls, std::string &defs) {
+    std::string::size_type p = 0;
+    defs = code;
+    while ((p = defs.find("static void ", p)) != std::string::npos) {
+        defs.erase(p, 7);  /* "static " */
+        const std::string::size_type q = defs.find(" {\n", p);
+        decls += defs.substr(p, q - p) + ";\n";
+        p = q;
+    }
+}
+
 int main(int argc, char **argv) {
-    if (argc != 2) {
-        fprintf(stderr, "usage: ref_codegen <out.h>\n");
+    if (argc != 4) {
+        fprintf(stderr, "usage: ref_codegen <out.h> <out.cpp> <out_recalage.cpp>\n");
         return 1;
     }
-    std::string s;
-    s += "/* Element routines written by LMT++'s Codegen engine (oracle/ref_codegen.cpp). */\n";
-    s += "#ifndef LMTG_REF_GEN_ELEM_H\n#define LMTG_REF_GEN_ELEM_H\n#include <cmath>\n\n";
-    s += gen_elasticity("Hexa", "gen_hexa8_elast_gp");
-    s += gen_elasticity("Tetra_10", "gen_tetra10_elast_gp");
-    s += gen_difftherm_tri6("gen_tri6_difftherm_cn", 0.0, 1.0);
-    s += gen_difftherm_tri6("gen_tri6_difftherm_ie", 1.0, 1.0);
-    s += "#endif\n";
-    FILE *f = fopen(argv[1], "w");
-    if (!f) {
-        fprintf(stderr, "cannot write %s\n", argv[1]);
-        return 2;
+    std::string code, code_r;
+    code += gen_elasticity("Hexa", "gen_hexa8_elast_gp");
+    code += gen_elasticity("Tetra_10", "gen_tetra10_elast_gp");
+    code += gen_difftherm_tri6("gen_tri6_difftherm_cn", 0.0, 1.0);
+    code += gen_difftherm_tri6("gen_tri6_difftherm_ie", 1.0, 1.0);
+    code_r += gen_recalage("Hexa", "gen_hexa8_recalage");
+    code_r += gen_recalage("Tetra_10", "gen_tetra10_recalage");
+    std::string decls, defs, defs_r;
+    split(code, decls, defs);
+    split(code_r, decls, defs_r);
+    const std::string head = "/* Element routines written by LMT++'s Codegen engine (oracle/ref_codegen.cpp). */\n";
+    const std::string pre = "#include <cmath>\n#include \"gen_elem.h\"\nusing std::pow;\nusing std::sqrt;\n\n";
+    const std::string txt[3] = {head + "#ifndef LMTG_REF_GEN_ELEM_H\n#define LMTG_REF_GEN_ELEM_H\n" + decls + "#endif\n",
+                                head + pre + defs, head + pre + defs_r};
+    for (int k = 0; k < 3; ++k) {
+        FILE *f = fopen(argv[1 + k], "w");
+        if (!f) {
+            fprintf(stderr, "cannot write %s\n", argv[1 + k]);
+            return 2;
+        }
+        fputs(txt[k].c_str(), f);
+        fclose(f);
     }
-    fputs(s.c_str(), f);
-    fclose(f);
     return 0;
 }

@@ -4,7 +4,7 @@
  * Compiled against the reference's headers and its vendored LDL/AMD sources by
  * oracle/build_ref.sh into oracle/_ref/ (never into the product).  Everything that computes a
  * value here is the reference's code:
- *   - the element routines: written by the reference's own Codegen engine (gen_elem.h, produced
+ *   - the element routines: written by the reference's own Codegen engine (gen_elem.cpp, produced
  *     at build time by oracle/ref_codegen.cpp from the weak forms of elasticity_iso and
  *     difftherm), called once per Gauss point of the reference's table
  *     (gauss_point_for_order, include/mesh/element_Hexa.h:5-20, element_Tetra_10.h:5-16) as the
@@ -34,6 +34,11 @@
  *       every face for f_surf = (0.7,-0.2,0.4) and p = 2.5.
  *   ref_driver elem type=tri6 in=path k=.. rho_c=.. dt=.. out=path
  *       One Triangle_6: A and B for Crank-Nicolson, then implicit Euler.
+ *   ref_driver recalage elem=hexa|tetra10 nbp=N E=.. nu=.. rho=.. omega=.. gamma=.. r=.. penalty=.. out=dir
+ *       The recalage functional's system (9 unknowns per node), V clamped on x = 0, LDL solve.
+ *   ref_driver recal_elem type=hexa|tetra10 in=path E=.. nu=.. rho=.. omega=.. gamma=.. r=..
+ *              ud0=.. ud1=.. ud2=.. valid=.. out=path
+ *       One element's recalage Hessian and the nodal routine of one node.
  * Outputs are little-endian raw arrays plus info.txt.
  */
 #include "mesh/meshcaracstd.h"
@@ -412,6 +417,99 @@ static int run_diff(const Args &a) {
     return 0;
 }
 
+/* recalage (formulations/formulation_recalage.py): the generated element Hessian per element and
+ * the generated nodal routine per node, scattered into the reference's Sym SparseLine with 9
+ * unknowns per node (U, V, W, then component); penalty constraints V = 0 on the nodes of x = 0
+ * (the functional alone leaves V - U free up to rigid motions); LDL solve.
+ * Ud(x, y, z) = (0.01 x^2 + 0.002 y, 0.005 x y - 0.001 z, -0.002 z + 0.0005 x z), Ud_valid = 1. */
+static int run_recalage(const Args &a) {
+    const bool tet = arg(a, "elem") == "tetra10";
+    const int npe = tet ? 10 : 8, nd = 9 * npe;
+    unsigned nbp = atoi(arg(a, "nbp").c_str());
+    const double E = argd(a, "E"), nu = argd(a, "nu"), rho = argd(a, "rho"), omega = argd(a, "omega"),
+                 gamma = argd(a, "gamma"), r = argd(a, "r"), penalty = argd(a, "penalty");
+    std::string out = arg(a, "out");
+    std::vector<double> pos;
+    std::vector<unsigned> conn;
+    if (tet) {
+        typedef Mesh<MeshCaracStd<3, 3, 0, double, 2> > TM;
+        TM m;
+        make_rect(m, Tetra_10(), TM::Pvec(0, 0, 0), TM::Pvec(1, 1, 1), TM::Pvec(nbp, nbp, nbp));
+        read_mesh(m, 3, npe, pos, conn);
+    } else {
+        typedef Mesh<MeshCaracStd<3, 3, 1, double, 1> > TM;
+        TM m;
+        make_rect(m, Hexa(), TM::Pvec(0, 0, 0), TM::Pvec(1, 1, 1), TM::Pvec(nbp, nbp, nbp));
+        read_mesh(m, 3, npe, pos, conn);
+    }
+    const unsigned nn = pos.size() / 3, ne = conn.size() / npe, n = 9 * nn;
+    std::vector<double> Ud(3 * nn), valid(nn, 1.0);
+    for (unsigned i = 0; i < nn; ++i) {
+        const double x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
+        Ud[3 * i] = 0.01 * x * x + 0.002 * y;
+        Ud[3 * i + 1] = 0.005 * x * y - 0.001 * z;
+        Ud[3 * i + 2] = -0.002 * z + 0.0005 * x * z;
+    }
+    Mat<double, Sym<>, SparseLine<> > K(n, n);
+    std::vector<double> F(n, 0.0);
+    std::vector<double> Ke(nd * nd);
+    for (unsigned e = 0; e < ne; ++e) {
+        double xyz[30];
+        for (int q = 0; q < npe; ++q)
+            for (int d = 0; d < 3; ++d) xyz[3 * q + d] = pos[3 * conn[npe * e + q] + d];
+        std::fill(Ke.begin(), Ke.end(), 0.0);
+        if (tet) gen_tetra10_recalage(xyz, E, nu, rho, omega, gamma, &Ke[0]);
+        else gen_hexa8_recalage(xyz, E, nu, rho, omega, gamma, &Ke[0]);
+        for (int i = 0; i < nd; ++i)
+            for (int j = i; j < nd; ++j)
+                K(9 * conn[npe * e + i / 9] + i % 9, 9 * conn[npe * e + j / 9] + j % 9) += Ke[nd * i + j];
+    }
+    for (unsigned i = 0; i < nn; ++i) { /* add_nodal_matrix: node 0's routine on every node */
+        double Kn[81] = {0}, Fn[9] = {0};
+        if (tet) gen_tetra10_recalage_nodal(&Ud[3 * i], &valid[i], E, r, Kn, Fn);
+        else gen_hexa8_recalage_nodal(&Ud[3 * i], &valid[i], E, r, Kn, Fn);
+        for (int p = 0; p < 9; ++p) {
+            for (int q = p; q < 9; ++q) K(9 * i + p, 9 * i + q) += Kn[9 * p + q];
+            F[9 * i + p] += Fn[p];
+        }
+    }
+    double max_diag = max(abs(K.diag()));
+    unsigned ncons = 0;
+    for (unsigned i = 0; i < nn; ++i)
+        if (pos[3 * i] < 1e-6)
+            for (int d = 0; d < 3; ++d) {
+                K(9 * i + 3 + d, 9 * i + 3 + d) += max_diag * penalty;
+                ++ncons;
+            }
+    std::vector<unsigned long long> rowptr;
+    std::vector<unsigned> col;
+    std::vector<double> val;
+    export_lower(K, rowptr, col, val);
+    if (arg(a, "dumpK", "1") == "1") {
+        dump(out + "/rowptr.u64", rowptr);
+        dump(out + "/col.u32", col);
+        dump(out + "/val.f64", val);
+    }
+    Mat<double, Sym<>, SparseLine<> > Kc = K;
+    LDL_solver ldl;
+    ldl.get_factorization(Kc, false);
+    Vec<double> sol;
+    sol.resize(n);
+    for (unsigned i = 0; i < n; ++i) sol[i] = F[i];
+    ldl.solve(sol);
+    std::vector<double> u(n);
+    for (unsigned i = 0; i < n; ++i) u[i] = sol[i];
+    dump(out + "/pos.f64", pos);
+    dump(out + "/conn.u32", conn);
+    dump(out + "/F.f64", F);
+    dump(out + "/u_ldl.f64", u);
+    dump(out + "/Ud.f64", Ud);
+    FILE *f = fopen((out + "/info.txt").c_str(), "w");
+    fprintf(f, "nn %u\nne %u\nn %u\nnnz %zu\nmax_diag %.17g\nncons %u\n", nn, ne, n, col.size(), max_diag, ncons);
+    fclose(f);
+    return 0;
+}
+
 /* One element through the generated routines. */
 static int run_elem(const Args &a) {
     std::string type = arg(a, "type"), out = arg(a, "out");
@@ -436,12 +534,33 @@ static int run_elem(const Args &a) {
     return 0;
 }
 
+/* One element through the generated recalage routines: the element Hessian (upper triangle,
+ * 9 npe x 9 npe), then the nodal routine's 9 x 9 upper triangle and vector for Ud = (ud0, ud1, ud2),
+ * Ud_valid = valid. */
+static int run_recal_elem(const Args &a) {
+    const bool tet = arg(a, "type") == "tetra10";
+    const int npe = tet ? 10 : 8, nd = 9 * npe;
+    std::vector<double> xyz = load_f64(arg(a, "in"), 3 * npe);
+    std::vector<double> res(nd * nd + 81 + 9, 0.0);
+    const double E = argd(a, "E"), nu = argd(a, "nu"), rho = argd(a, "rho"), omega = argd(a, "omega"),
+                 gamma = argd(a, "gamma"), r = argd(a, "r");
+    if (tet) gen_tetra10_recalage(&xyz[0], E, nu, rho, omega, gamma, &res[0]);
+    else gen_hexa8_recalage(&xyz[0], E, nu, rho, omega, gamma, &res[0]);
+    const double ud[3] = {argd(a, "ud0"), argd(a, "ud1"), argd(a, "ud2")}, valid = argd(a, "valid");
+    if (tet) gen_tetra10_recalage_nodal(ud, &valid, E, r, &res[nd * nd], &res[nd * nd + 81]);
+    else gen_hexa8_recalage_nodal(ud, &valid, E, r, &res[nd * nd], &res[nd * nd + 81]);
+    dump(arg(a, "out"), res);
+    return 0;
+}
+
 int main(int argc, char **argv) {
     std::string cmd = argc >= 2 ? argv[1] : "";
     Args a = parse(argc, argv);
     if (cmd == "elast") return run_elast(a);
     if (cmd == "diff") return run_diff(a);
     if (cmd == "elem") return run_elem(a);
-    fprintf(stderr, "usage: ref_driver elast|diff|elem key=value ...\n");
+    if (cmd == "recalage") return run_recalage(a);
+    if (cmd == "recal_elem") return run_recal_elem(a);
+    fprintf(stderr, "usage: ref_driver elast|diff|elem|recalage|recal_elem key=value ...\n");
     return 1;
 }

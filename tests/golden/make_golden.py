@@ -25,6 +25,12 @@ IC(0)-PCG.  Fixtures (compressed npz):
                        the transient family at 2 x 32^2: lognormal conductivity (log-std 0.3,
                        default_rng(20251203)), dt 1e-4, penalty boundary, 10 LDL steps (states 0, 1,
                        5, 10), A and B, for Crank-Nicolson and implicit Euler
+  recal_elem           the recalage routines on the distorted Hexa8 and curved Tetra10 of
+                       elem_kernels: element Hessian (upper triangle) and one node's nodal part
+  recal_hexa_3, recal_tetra10_2, recal_hexa_8
+                       the recalage system on the unit cube (3^3 Hexa8, 2^3 Tetra10 cubes, 8^3
+                       Hexa8), E 2, nu 0.3, rho 1.5, omega 3, gamma 0.4, r 0.3, Ud a fixed quadratic
+                       field, Ud_valid 1, V clamped on x = 0 by penalty 1e5: lower CSR, F, LDL solution
   batch_cubes          the batch family: cubes of side 3, 5 and 7 with E ~ U[5e4, 3e5] and
                        nu ~ U[0.2, 0.4] (default_rng(20251203)), four load cases each (+x, +y, +z
                        unit traction on x = 1, N(0,1) nodal load): F and u_ldl per cube and case
@@ -154,6 +160,47 @@ def elem_kernels():
     np.savez_compressed(os.path.join(HERE, "elem_kernels.npz"), **res)
 
 
+RECAL = dict(E=2.0, nu=0.3, rho=1.5, omega=3.0, gamma=0.4, r=0.3)
+
+
+def recal_case(name, elem, nbp, pen, dumpK=True):
+    """The recalage system of the unit cube (V clamped on x = 0 by penalty) and its LDL solution."""
+    npe = 8 if elem == "hexa" else 10
+    with tempfile.TemporaryDirectory() as d:
+        kw = dict(elem=elem, nbp=nbp, penalty=repr(pen), dumpK=int(dumpK), **{k: repr(v) for k, v in RECAL.items()})
+        info, r = _run("recalage", d, **kw)
+        out = dict(pos=r("pos.f64", np.float64).reshape(-1, 3), conn=r("conn.u32", np.uint32).reshape(-1, npe),
+                   F=r("F.f64", np.float64), u_ldl=r("u_ldl.f64", np.float64), Ud=r("Ud.f64", np.float64))
+        if dumpK:
+            out.update(rowptr=r("rowptr.u64", np.uint64), col=r("col.u32", np.uint32), val=r("val.f64", np.float64))
+        meta = dict(elem=elem, nb_points=nbp, penalty=pen, max_diag=float(info["max_diag"]), nnz=int(info["nnz"]),
+                    ncons=int(info["ncons"]), **RECAL)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), meta=np.array(json.dumps(meta)), **out)
+
+
+def recal_elem():
+    """Single distorted elements through the generated recalage routines."""
+    ek = np.load(os.path.join(HERE, "elem_kernels.npz"))
+    res = dict(params=np.array([RECAL[k] for k in ("E", "nu", "rho", "omega", "gamma", "r")]),
+               ud=np.array([0.013, -0.004, 0.021]), valid=np.array(0.8))
+    with tempfile.TemporaryDirectory() as d:
+        for typ in ("hexa", "tetra10"):
+            xyz = ek[typ + "_xyz"]
+            xyz.astype(np.float64).tofile(os.path.join(d, "in.f64"))
+            args = [DRV, "recal_elem", "type=" + typ, "in=" + os.path.join(d, "in.f64"),
+                    "out=" + os.path.join(d, "out.f64"), "valid=0.8"]
+            args += ["%s=%r" % (k, v) for k, v in RECAL.items()]
+            args += ["ud%d=%r" % (i, float(v)) for i, v in enumerate(res["ud"])]
+            subprocess.check_call(args)
+            o = np.fromfile(os.path.join(d, "out.f64"), dtype=np.float64)
+            nd = 9 * xyz.shape[0]
+            res[typ + "_xyz"] = xyz
+            res[typ + "_K"] = o[:nd * nd].reshape(nd, nd)  # upper triangle
+            res[typ + "_Kn"] = o[nd * nd:nd * nd + 81].reshape(9, 9)
+            res[typ + "_Fn"] = o[nd * nd + 81:]
+    np.savez_compressed(os.path.join(HERE, "recal_elem.npz"), **res)
+
+
 def batch_cubes():
     rng = np.random.default_rng(SEED)
     sides = [3, 5, 7]
@@ -216,6 +263,10 @@ def main(which):
         "tri6_32_ie": lambda: diff_case("tri6_32_ie", 33, 1.0, 1.0, 1e-4, 1.0, 1e5, 10, (0, 1, 5, 10),
                                         kfield=np.exp(0.3 * np.random.default_rng(SEED).standard_normal(2 * 32 * 32))),
         "batch_cubes": batch_cubes,
+        "recal_elem": recal_elem,
+        "recal_hexa_3": lambda: recal_case("recal_hexa_3", "hexa", 4, 1e5),
+        "recal_tetra10_2": lambda: recal_case("recal_tetra10_2", "tetra10", 3, 1e5),
+        "recal_hexa_8": lambda: recal_case("recal_hexa_8", "hexa", 9, 1e5, dumpK=False),
     }
     for name in (which or list(jobs)):
         jobs[name]()

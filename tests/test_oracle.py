@@ -249,3 +249,49 @@ def test_block_ic_pcg_restatement_matches_reference(golden_dir, name):
     assert np.linalg.norm(x - u) <= 1e-12 * np.linalg.norm(u)
     # and it solves the system: against the LDL solution
     assert np.linalg.norm(x - g["u_ldl"]) <= 1e-9 * np.linalg.norm(g["u_ldl"])
+
+
+def test_recalage_element_restatement_matches_generated_code(golden_dir):
+    """orc_recalage_ke / orc_recalage_nodal against the routines LMT++'s Codegen engine writes for
+    formulation recalage (use_test_functions = False, integration_totale, order 2)."""
+    g = np.load(os.path.join(golden_dir, "recal_elem.npz"))
+    E, nu, rho, omega, gamma, r = g["params"]
+    for t in ("hexa", "tetra10"):
+        K = O.recalage_ke(g[t + "_xyz"], E, nu, rho, gamma)
+        Kr = g[t + "_K"]  # upper triangle
+        assert np.allclose(np.triu(K), Kr, rtol=0, atol=1e-14 * np.abs(Kr).max())
+        assert np.allclose(K, K.T, rtol=0, atol=1e-15 * np.abs(K).max())
+        Kn, Fn = O.recalage_nodal(g["ud"], float(g["valid"]), E, r)
+        assert np.allclose(np.triu(Kn), g[t + "_Kn"], rtol=1e-15, atol=0)
+        assert np.allclose(Fn, g[t + "_Fn"], rtol=1e-15, atol=0)
+        assert np.any(Fn != 0)
+
+
+@pytest.mark.parametrize("name", ["recal_hexa_3", "recal_tetra10_2"])
+def test_recalage_assembly_matches_reference(golden_dir, name):
+    """The assembled recalage system (element Hessians + nodal parts + penalty V = 0 on x = 0)
+    against the reference's Sym SparseLine, and the LDL solution where it is unique: all of it on
+    Hexa8; on Tetra10 the order-2 rule makes the quadratic element's mass matrix rank-deficient,
+    so W is defined up to that null space and only U and V are compared."""
+    g = load_golden(golden_dir, name)
+    m = g["meta"]
+    pos, conn = g["pos"], g["conn"]
+    nn, n = pos.shape[0], 9 * pos.shape[0]
+    rp, col = O.pattern_lower(nn, 9, conn)
+    val, F = O.assemble_recalage(pos, conn, m["E"], m["nu"], m["rho"], m["gamma"], m["r"], g["Ud"], np.ones(nn),
+                                 rp, col)
+    dofs = np.array([9 * i + 3 + d for i in np.nonzero(pos[:, 0] < 1e-6)[0] for d in range(3)])
+    md = O.penalty(rp, col, val, F, dofs, np.ones(dofs.size), np.zeros(dofs.size), m["penalty"])
+    assert md == pytest.approx(m["max_diag"], rel=1e-15)
+    A = csr(g["rowptr"], g["col"], g["val"], n).toarray()
+    B = csr(rp, col, val, n).toarray()
+    assert np.allclose(A, B, rtol=0, atol=1e-15 * np.abs(A).max())
+    assert np.allclose(F, g["F"], rtol=0, atol=1e-15 * np.abs(g["F"]).max())
+    S = B + np.tril(B, -1).T
+    u = np.linalg.solve(S, F) if m["elem"] == "hexa" else np.linalg.lstsq(S, F, rcond=None)[0]
+    assert np.abs(S @ g["u_ldl"] - F).max() <= 1e-12 * np.abs(F).max()
+    d = (u - g["u_ldl"]).reshape(nn, 3, 3)
+    sc = np.abs(g["u_ldl"]).max()
+    assert np.abs(d[:, :2]).max() <= 1e-8 * sc
+    if m["elem"] == "hexa":
+        assert np.abs(d).max() <= 1e-10 * sc
