@@ -53,6 +53,10 @@ extern "C" {
 #define LMTG_SOLVE_PCG_F64 0  /* plain FP64 block-Jacobi PCG */
 #define LMTG_SOLVE_MIXED_IR 1 /* FP32 inner PCG wrapped in FP64 iterative refinement */
 
+/* ---- preconditioners of the FP32 inner PCG (lmtg_set_preconditioner) ---- */
+#define LMTG_PREC_BLOCK_JACOBI 0 /* inverse 3x3 diagonal blocks */
+#define LMTG_PREC_AMG 1          /* aggregation multigrid V-cycle (the default) */
+
 /* ---- stopping criteria ---- */
 #define LMTG_CRIT_REL_RESIDUAL 0   /* |b - K u|_2 <= tol |b|_2 */
 #define LMTG_CRIT_NORM_INF_DELTA 1 /* |alpha d|_inf <= tol (ConvergenceCriteriumNormInfDelta,
@@ -368,6 +372,23 @@ int lmtg_recalage_setup(lmtg_ctx *ctx, double rho, double omega, double gamma, d
 /* Element stiffness and mass blocks, their node-pattern gather, the 9-unknown Hessian and
  * right-hand side, then the constraints (penalty or exact) and both preconditioners. */
 int lmtg_recalage_assemble(lmtg_ctx *ctx);
+
+/* Preconditioner of the FP32 inner PCG of the mixed solve (LMTG_SOLVE_MIXED_IR), standing in
+ * for the reference's sequential incomplete Cholesky (include/containers/matinvsparse.h:201-261,
+ * MatWithTinyBlocks.h:426-585).  LMTG_PREC_AMG (default): one V-cycle of an unsmoothed-aggregation
+ * multigrid whose coarse spaces carry the six rigid-body modes per aggregate, damped block-Jacobi
+ * smoothing, a dense coarsest level; used for single-system Hexa8 / Tetra10 elasticity of at
+ * least 3,000 unknowns, block Jacobi otherwise (batches, recalage, small systems).  Its structure
+ * is built at the first mixed solve after lmtg_allocate_matrices or lmtg_set_constraints (nodes
+ * with a constraint stay out of the coarse spaces), its numeric part at the first mixed solve
+ * after each matrix assembly.  LMTG_PREC_BLOCK_JACOBI: the inverse 3x3 diagonal blocks.  The
+ * FP64 PCG always uses block Jacobi. */
+int lmtg_set_preconditioner(lmtg_ctx *ctx, int kind);
+/* The multigrid hierarchy built for the last mixed solve (levels = 0 when none): per level
+ * (up to 8) unknowns, stored blocks, damped-Jacobi weight and lambda_max(D^-1 K); the host time
+ * of the structure setup and of the last numeric setup.  Any output may be NULL. */
+int lmtg_amg_info(lmtg_ctx *ctx, int *levels, uint64_t ndof[8], uint64_t nnz_blocks[8], double omega[8],
+                  double lambda_max[8], double *structure_ms, double *numeric_ms);
 
 /* Sizes of the current problem. */
 int lmtg_get_sizes(lmtg_ctx *ctx, uint64_t *nn, uint64_t *ne, uint64_t *ndof, uint64_t *nnz_blocks);

@@ -16,6 +16,7 @@ ELEM_HEXA8, ELEM_TETRA10, ELEM_TRIANGLE6 = 8, 10, 6
 ASM_MAT64, ASM_MAT32, ASM_VEC, ASM_MAT32_NATIVE = 1, 2, 4, 8
 SOLVE_PCG_F64, SOLVE_MIXED_IR = 0, 1
 CRIT_REL_RESIDUAL, CRIT_NORM_INF_DELTA, CRIT_NORM2_DELTA, CRIT_ABS_RESIDUAL_INF = 0, 1, 2, 3
+PREC_BLOCK_JACOBI, PREC_AMG = 0, 1
 OBJ_COMPLIANCE, OBJ_MISFIT, OBJ_LINEAR = 0, 1, 2
 
 _vp = ctypes.c_void_p
@@ -64,6 +65,8 @@ _SIGS = {
     "lmtg_spmv": (_i, [_vp, _i, _vp, _vp]),
     "lmtg_get_sizes": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "lmtg_recalage_setup": (_i, [_vp, _d, _d, _d, _d, _vp, _vp]),
+    "lmtg_set_preconditioner": (_i, [_vp, _i]),
+    "lmtg_amg_info": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "lmtg_recalage_assemble": (_i, [_vp]),
     "lmtg_get_launch_count": (_i, [_vp, ctypes.POINTER(_u64)]),
     "lmtg_make_rect_triangle6": (_i, [_vp, _vp, _vp, ctypes.POINTER(_u64), ctypes.POINTER(_u64), _vp, _vp]),

@@ -12,6 +12,7 @@
 #include <new>
 
 #include "lmtg_internal.cuh"
+#include "amg.cuh"
 #include "spmv_bulk.cuh"
 
 using namespace lmtg;
@@ -162,6 +163,7 @@ int lmtg_destroy(lmtg_ctx *c) {
     if (c->h_scal) cudaFreeHost(c->h_scal);
     batch_free(c);
     recal_free(c);
+    amg_free(c);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;  // DBuf destructors free device memory
     return LMTG_OK;
@@ -296,6 +298,7 @@ int lmtg_mesh_set(lmtg_ctx *c, int elem_type, uint64_t nn, const double *pos, ui
         LMTG_CHECK(nn < (1ull << 32), LMTG_ERR_UNSUPPORTED, "more than 2^32 nodes");
         const int npe = elem_type;
         recal_free(c);
+        amg_free(c);
         c->elem_type = elem_type;
         c->npe = npe;
         c->nnu = 3;
@@ -315,6 +318,7 @@ int lmtg_mesh_set(lmtg_ctx *c, int elem_type, uint64_t nn, const double *pos, ui
         c->nu = 0.33;
         c->allocated = c->have64 = c->have32 = c->have_vec = false;
         c->nc = 0;
+        c->h_cdof.clear();
         c->penalty = 0;
         c->h_loads.assign(c->n, 0.0);
         LMTG_CUDA(cudaStreamSynchronize(c->stream));
@@ -390,6 +394,7 @@ int lmtg_set_levenberg_marquadt(lmtg_ctx *c, double lm) {
 
 int lmtg_batch_set(lmtg_ctx *c, uint32_t nsys, const uint64_t *node_off) {
     return guard(c, [&] {
+        amg_free(c);
         LMTG_CHECK(c->ne > 0 && c->nnu == 3, LMTG_ERR_STATE, "elasticity mesh_set first");
         LMTG_CHECK(nsys > 0 && node_off, LMTG_ERR_ARG, "nsys > 0 and node_off needed");
         LMTG_CHECK(node_off[0] == 0 && node_off[nsys] == c->nn, LMTG_ERR_ARG, "node_off must span 0..nn");
@@ -509,6 +514,22 @@ int lmtg_set_spmv_kind(lmtg_ctx *c, int kind) {
     });
 }
 
+int lmtg_set_preconditioner(lmtg_ctx *c, int kind) {
+    return guard(c, [&] {
+        LMTG_CHECK(kind == LMTG_PREC_BLOCK_JACOBI || kind == LMTG_PREC_AMG, LMTG_ERR_ARG, "unknown preconditioner");
+        c->precond = kind;
+        return LMTG_OK;
+    });
+}
+
+int lmtg_amg_info(lmtg_ctx *c, int *levels, uint64_t *ndof, uint64_t *nnz_blocks, double *omega,
+                  double *lambda_max, double *structure_ms, double *numeric_ms) {
+    return guard(c, [&] {
+        amg_info(c, levels, ndof, nnz_blocks, omega, lambda_max, structure_ms, numeric_ms);
+        return LMTG_OK;
+    });
+}
+
 int lmtg_batch_set_options(lmtg_ctx *c, int tile_rows, int variant) {
     return guard(c, [&] {
         LMTG_CHECK(variant >= -1 && variant <= 2, LMTG_ERR_ARG, "variant: -1 (autotune), 0, 1 or 2");
@@ -527,6 +548,7 @@ int lmtg_allocate_matrices(lmtg_ctx *c, uint64_t *nnz_lower) {
     return guard(c, [&] {
         LMTG_CHECK(c->ne > 0, LMTG_ERR_STATE, "mesh_set first");
         LMTG_CHECK(c->nnu == 3, LMTG_ERR_STATE, "elasticity call on a diffusion context");
+        amg_free(c);
         build_pattern(c);
         c->Ke64.alloc(c->ne * (uint64_t)c->npairs * 9);
         c->K64.alloc(c->nnzb * 9);
@@ -604,6 +626,8 @@ int lmtg_set_constraints(lmtg_ctx *c, uint64_t nc, const uint32_t *dof, const do
                        "two exact constraints on one DOF");
         }
         upload(c, c->cdof, dof, nc);
+        c->h_cdof.assign(dof, dof + nc);
+        amg_free(c);  // constrained nodes stay out of the multigrid's coarse spaces
         upload(c, c->ccoef, coef, nc);
         upload(c, c->cres, res, nc);
         c->nc = nc;

@@ -62,7 +62,10 @@ void do_assemble(lmtg_ctx *c, int flags) {
     }
     apply_body_terms(c, mat, vec);
     if (mat || vec) apply_penalty(c, mat, vec);
-    if (mat) build_block_jacobi(c, c->have64, c->have32);
+    if (mat) {
+        build_block_jacobi(c, c->have64, c->have32);
+        ++c->mat_version;
+    }
     LMTG_CUDA(cudaStreamSynchronize(c->stream));
 }
 

@@ -1,0 +1,1082 @@
+// amg.cu -- aggregation multigrid preconditioner for the FP32 inner PCG of elasticity.
+//
+// The reference preconditions its CG with a sequential incomplete Cholesky
+// (include/containers/matinvsparse.h:201-261, 3x3-block variant
+// include/containers/MatWithTinyBlocks.h:426-585), which has no parallel form; block Jacobi, its
+// stand-in here, needs O(mesh side) iterations (2,388 at Hexa8 128^3).  This file replaces z = P r
+// by one V-cycle of an unsmoothed-aggregation multigrid whose coarse spaces hold the rigid-body
+// modes, so that the iteration count stays nearly flat with the mesh size.
+//
+// Hierarchy (structure built once per pattern and constraint set, on the host):
+//   level 0   the context's 3x3-block matrix K32 (planar rows, kidx), its block-Jacobi Dinv32
+//   level l+1 aggregates of level-l nodes: a root node with all its free neighbours, then the
+//             leftovers joined to a neighbouring aggregate, then the rest grouped around a free
+//             node.  Nodes carrying a constraint are left out (the smoother alone handles them).
+//   Q_l       per level-l node a b x 6 block of the tentative prolongator: the six rigid-body modes
+//             of the aggregate (three translations, three rotations about its centroid at level 0;
+//             the coarse modes R at deeper levels) orthonormalised per aggregate (Gram-Schmidt in
+//             FP64); a mode that the aggregate cannot carry (one node, or nodes on a line) gives a
+//             zero column, and the coarse unknown it would define is a decoupled unit diagonal.
+//   K_{l+1}   = Q_l^T K_l Q_l (Galerkin), 6x6 blocks, through gather lists: for every coarse block
+//             the level-l blocks that sum into it, in a fixed order (one thread per coarse block,
+//             no atomics, deterministic).
+//   coarsest  (<= 300 unknowns): a dense inverse, computed on the host in FP64, applied in FP32.
+// Numeric setup after every matrix assembly: the Galerkin products, the 6x6 block-Jacobi
+// inverses, and per level the damped-Jacobi weight omega = 1.6 / lambda_max(D^-1 K) (lambda_max by
+// ten power steps; the weight of a degree-1 Chebyshev smoother on [lambda/30, 1.1 lambda]).
+//
+// V-cycle (z = M r), per level: x = omega D^-1 r; res = r - K x; restrict Q^T res; recurse;
+// x += Q e; x' = x + omega D^-1 (r - K x).  The same smoother before and after makes M symmetric,
+// as the conjugate gradient needs.  At level 0 the first smoothing step is fused into the PCG's
+// update kernel and the last one writes z and forms r.z and beta.  Every kernel returns at once
+// once the PCG's `done` flag is set, so the cycle runs inside the captured iteration chunks.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <thread>
+#include <vector>
+
+#include "amg.cuh"
+#include "spmv_bulk.cuh"
+
+namespace lmtg {
+
+namespace {
+
+constexpr uint32_t kNone = 0xffffffffu;
+constexpr int kMaxLevels = 8;
+constexpr uint64_t kCoarsestDofs = 300;
+
+// planar 6x6 block rows: component v (row-major) of local block b of a row starting at block rb
+__host__ __device__ __forceinline__ uint64_t kidx6(uint32_t rb, uint32_t deg, uint32_t b, int v) {
+    return 36ull * rb + (uint64_t)v * deg + b;
+}
+
+template <int B>
+__host__ __device__ __forceinline__ uint64_t kidxb(uint32_t rb, uint32_t deg, uint32_t b, int v) {
+    return (uint64_t)(B * B) * rb + (uint64_t)v * deg + b;
+}
+
+__device__ __forceinline__ bool done(const PcgScalars *S) { return S && *(volatile const int *)&S->done; }
+
+// ---------------------------------------------------------------------------------------------
+// numeric setup kernels
+// ---------------------------------------------------------------------------------------------
+
+// Coarse block (I, J) = sum over its gather list of Q_i^T K_ij Q_j.  One thread per coarse block;
+// g[2e] = fine block index, g[2e+1] = its fine row.  A coarse diagonal entry that sums to exactly
+// zero (a mode the aggregate cannot carry) becomes 1, a decoupled unknown.
+template <int B>
+__global__ void __launch_bounds__(128)
+    k_galerkin(const uint32_t *__restrict__ fbptr, const uint32_t *__restrict__ fbcol, const float *__restrict__ fK,
+               const float *__restrict__ Q, const uint32_t *__restrict__ cbptr, const uint32_t *__restrict__ cbcol,
+               uint64_t cnn, const uint32_t *__restrict__ gptr, const uint32_t *__restrict__ gsrc,
+               float *__restrict__ cK) {
+    const uint64_t nb = cbptr[cnn];
+    for (uint64_t cb = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; cb < nb; cb += (uint64_t)gridDim.x * blockDim.x) {
+        float C[36];
+#pragma unroll
+        for (int v = 0; v < 36; ++v) C[v] = 0.f;
+        for (uint32_t e = gptr[cb]; e < gptr[cb + 1]; ++e) {
+            const uint32_t k = gsrc[2 * (uint64_t)e], i = gsrc[2 * (uint64_t)e + 1];
+            const uint32_t rb = fbptr[i], deg = fbptr[i + 1] - rb, j = fbcol[k];
+            float A[B * B];
+#pragma unroll
+            for (int v = 0; v < B * B; ++v) A[v] = fK[kidxb<B>(rb, deg, k - rb, v)];
+            const float *Qi = Q + (uint64_t)i * B * 6, *Qj = Q + (uint64_t)j * B * 6;
+            float T[B * 6];  // A Q_j
+#pragma unroll
+            for (int r = 0; r < B; ++r)
+#pragma unroll
+                for (int c = 0; c < 6; ++c) {
+                    float s = 0.f;
+#pragma unroll
+                    for (int m = 0; m < B; ++m) s = fmaf(A[r * B + m], __ldg(Qj + m * 6 + c), s);
+                    T[r * 6 + c] = s;
+                }
+#pragma unroll
+            for (int r = 0; r < B; ++r) {
+                float q[6];
+#pragma unroll
+                for (int a = 0; a < 6; ++a) q[a] = __ldg(Qi + r * 6 + a);
+#pragma unroll
+                for (int a = 0; a < 6; ++a)
+#pragma unroll
+                    for (int c = 0; c < 6; ++c) C[a * 6 + c] = fmaf(q[a], T[r * 6 + c], C[a * 6 + c]);
+            }
+        }
+        // row of this coarse block (binary search on cbptr) to place it in the planar layout
+        uint64_t lo = 0, hi = cnn;
+        while (hi - lo > 1) {
+            const uint64_t mid = (lo + hi) / 2;
+            if (cbptr[mid] <= cb) lo = mid;
+            else hi = mid;
+        }
+        const uint32_t rb = cbptr[lo], deg = cbptr[lo + 1] - rb;
+        if (cbcol[cb] == lo)
+#pragma unroll
+            for (int a = 0; a < 6; ++a)
+                if (C[a * 7] == 0.f) C[a * 7] = 1.f;
+#pragma unroll
+        for (int v = 0; v < 36; ++v) cK[kidx6(rb, deg, (uint32_t)(cb - rb), v)] = C[v];
+    }
+}
+
+// Inverse of every 6x6 diagonal block (Gauss-Jordan with partial pivoting, FP64).
+__global__ void k_block_inv6(const uint32_t *__restrict__ bptr, const uint32_t *__restrict__ bdiag,
+                             const float *__restrict__ K, uint64_t nn, float *__restrict__ Dinv) {
+    for (uint64_t I = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; I < nn; I += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t rb = bptr[I], deg = bptr[I + 1] - rb, d = bdiag[I] - rb;
+        double a[6][12];
+        for (int r = 0; r < 6; ++r)
+            for (int c = 0; c < 6; ++c) {
+                a[r][c] = (double)K[kidx6(rb, deg, d, 6 * r + c)];
+                a[r][6 + c] = r == c ? 1.0 : 0.0;
+            }
+        bool ok = true;
+        for (int c = 0; c < 6 && ok; ++c) {
+            int p = c;
+            for (int r = c + 1; r < 6; ++r)
+                if (fabs(a[r][c]) > fabs(a[p][c])) p = r;
+            if (a[p][c] == 0.0) {
+                ok = false;
+                break;
+            }
+            if (p != c)
+                for (int k = 0; k < 12; ++k) {
+                    const double t = a[c][k];
+                    a[c][k] = a[p][k];
+                    a[p][k] = t;
+                }
+            const double iv = 1.0 / a[c][c];
+            for (int k = 0; k < 12; ++k) a[c][k] *= iv;
+            for (int r = 0; r < 6; ++r)
+                if (r != c) {
+                    const double f = a[r][c];
+                    if (f != 0.0)
+                        for (int k = 0; k < 12; ++k) a[r][k] -= f * a[c][k];
+                }
+        }
+        for (int r = 0; r < 6; ++r)
+            for (int c = 0; c < 6; ++c) Dinv[36 * I + 6 * r + c] = ok ? (float)a[r][6 + c] : (r == c ? 1.f : 0.f);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// row products
+// ---------------------------------------------------------------------------------------------
+
+// (K x)_I for a 3x3-block row, x padded to 4 per node: returns the reduce_scatter3 layout
+__device__ __forceinline__ float row3(const uint32_t *__restrict__ bcol, const float *__restrict__ K, uint32_t rb,
+                                      uint32_t re, int lane, const float *__restrict__ x) {
+    return bsr3_row_lanes(bcol, K, rb, re, lane, [&](uint64_t J, float &a, float &b, float &c) {
+        NodeVec<float, 4>::load(x, J, a, b, c);
+    });
+}
+
+// (K x)_I for a 6x6-block row, x padded to 8 per node: every lane ends with the 6 sums
+__device__ __forceinline__ void row6(const uint32_t *__restrict__ bcol, const float *__restrict__ K, uint32_t rb,
+                                     uint32_t re, int lane, const float *__restrict__ x, float (&a)[6]) {
+    const uint32_t deg = re - rb;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) a[k] = 0.f;
+    for (uint32_t b0 = 0; b0 < deg; b0 += 32) {
+        const uint32_t bl = b0 + lane;
+        if (bl < deg) {
+            const uint32_t J = __ldg(bcol + rb + bl);
+            const float4 u = __ldg(reinterpret_cast<const float4 *>(x) + 2 * (uint64_t)J);
+            const float4 w = __ldg(reinterpret_cast<const float4 *>(x) + 2 * (uint64_t)J + 1);
+            const float xv[6] = {u.x, u.y, u.z, u.w, w.x, w.y};
+#pragma unroll
+            for (int r = 0; r < 6; ++r)
+#pragma unroll
+                for (int c = 0; c < 6; ++c) a[r] = fmaf(__ldg(K + kidx6(rb, deg, bl, 6 * r + c)), xv[c], a[r]);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) a[k] = warp_sum(a[k]);
+}
+
+// ---------------------------------------------------------------------------------------------
+// cycle kernels
+// ---------------------------------------------------------------------------------------------
+
+// x = omega D^-1 r (6x6 blocks; r packed 6, x padded 8)
+__global__ void k_amg_bj6(const float *__restrict__ Dinv, const float *__restrict__ r, float *__restrict__ x,
+                          float omega, uint64_t nn, const PcgScalars *S) {
+    if (done(S)) return;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < 6 * nn; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t I = i / 6;
+        const int c = (int)(i - 6 * I);
+        const float *D = Dinv + 36 * I + 6 * c;
+        const float *rv = r + 6 * I;
+        float s = 0.f;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) s = fmaf(D[k], rv[k], s);
+        x[8 * I + c] = omega * s;
+    }
+}
+
+// res = r - K x (r == nullptr: res = -K x), warp per row
+template <int B>
+__global__ void __launch_bounds__(kRowThreads)
+    k_amg_res(const uint32_t *__restrict__ bptr, const uint32_t *__restrict__ bcol, const float *__restrict__ K,
+              const float *__restrict__ x, const float *__restrict__ r, float *__restrict__ res, uint64_t nn,
+              const PcgScalars *S) {
+    if (done(S)) return;
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t I = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; I < nn; I += nw) {
+        if (B == 3) {
+            const float a = row3(bcol, K, bptr[I], bptr[I + 1], lane, x);
+            if ((lane & 7) == 0 && lane < 24) {
+                const uint64_t i = 3 * I + (lane >> 3);
+                res[i] = (r ? r[i] : 0.f) - a;
+            }
+        } else {
+            float a[6];
+            row6(bcol, K, bptr[I], bptr[I + 1], lane, x, a);
+            if (lane < 6) {
+                float v = a[0];
+#pragma unroll
+                for (int k = 1; k < 6; ++k) v = lane == k ? a[k] : v;
+                const uint64_t i = 6 * I + lane;
+                res[i] = (r ? r[i] : 0.f) - v;
+            }
+        }
+    }
+}
+
+// Post-smoothing x_out = x + omega D^-1 (r - K x), warp per row.  With S_rz (level 0 inside the
+// PCG) x_out is the PCG's z, and r.z is reduced: rz and beta are set (beta = rz / rz_old, or on a
+// start rz / beta_den when beta_den > 0, else 0).
+template <int B>
+__global__ void __launch_bounds__(kRowThreads)
+    k_amg_post(const uint32_t *__restrict__ bptr, const uint32_t *__restrict__ bcol, const float *__restrict__ K,
+               const float *__restrict__ Dinv, const float *__restrict__ x, const float *__restrict__ r,
+               float *__restrict__ xo, float omega, uint64_t nn, PcgScalars *S, bool with_rz, int start,
+               double beta_den, double *partials) {
+    if (done(S)) return;
+    constexpr int VS = B == 3 ? 4 : 8;
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    float rz = 0.f;
+    for (uint64_t I = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; I < nn; I += nw) {
+        float d[B];
+        if (B == 3) {
+            const float a = row3(bcol, K, bptr[I], bptr[I + 1], lane, x);
+            d[0] = __shfl_sync(0xffffffffu, a, 0);
+            d[1] = __shfl_sync(0xffffffffu, a, 8);
+            d[2] = __shfl_sync(0xffffffffu, a, 16);
+        } else {
+            float a[6];
+            row6(bcol, K, bptr[I], bptr[I + 1], lane, x, a);
+#pragma unroll
+            for (int k = 0; k < B; ++k) d[k] = a[k < 6 ? k : 0];
+        }
+#pragma unroll
+        for (int k = 0; k < B; ++k) d[k] = r[(uint64_t)B * I + k] - d[k];
+        if (lane < B) {
+            const float *D = Dinv + (uint64_t)B * B * I + B * lane;
+            float s = 0.f;
+#pragma unroll
+            for (int k = 0; k < B; ++k) s = fmaf(D[k], d[k], s);
+            const float z = x[(uint64_t)VS * I + lane] + omega * s;
+            xo[(uint64_t)VS * I + lane] = z;
+            rz = fmaf(r[(uint64_t)B * I + lane], z, rz);
+        }
+    }
+    if (!with_rz) return;
+    const float t[1] = {rz};
+    double out[1];
+    if (grid_reduce_t<1, 0u>(t, partials, &S->cnt_d, out) && threadIdx.x == 0) {
+        if (start) {
+            S->beta = beta_den > 0.0 ? out[0] / beta_den : 0.0;
+        } else {
+            S->beta = out[0] / S->rz;
+        }
+        S->rz = out[0];
+        if (!isfinite(out[0])) {
+            S->status = LMTG_ERR_NAN;
+            S->done = 1;
+        }
+    }
+}
+
+// rc = Q^T res per aggregate (warp per aggregate)
+template <int B>
+__global__ void __launch_bounds__(kRowThreads)
+    k_amg_restrict(const uint32_t *__restrict__ aptr, const uint32_t *__restrict__ anode, const float *__restrict__ Q,
+                   const float *__restrict__ res, float *__restrict__ rc, uint64_t na, const PcgScalars *S) {
+    if (done(S)) return;
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t a = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; a < na; a += nw) {
+        float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        for (uint32_t k = aptr[a] + lane; k < aptr[a + 1]; k += 32) {
+            const uint32_t i = anode[k];
+            const float *q = Q + (uint64_t)i * B * 6;
+#pragma unroll
+            for (int r = 0; r < B; ++r) {
+                const float v = res[(uint64_t)B * i + r];
+#pragma unroll
+                for (int c = 0; c < 6; ++c) acc[c] = fmaf(q[6 * r + c], v, acc[c]);
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 6; ++c) acc[c] = warp_sum(acc[c]);
+        if (lane < 6) {
+            float v = acc[0];
+#pragma unroll
+            for (int c = 1; c < 6; ++c) v = lane == c ? acc[c] : v;
+            rc[6 * a + lane] = v;
+        }
+    }
+}
+
+// x += Q e[agg] per node (e with stride ES per coarse node)
+template <int B, int ES>
+__global__ void k_amg_prolong(const uint32_t *__restrict__ agg, const float *__restrict__ Q, const float *__restrict__ e,
+                              float *__restrict__ x, uint64_t nn, const PcgScalars *S) {
+    if (done(S)) return;
+    constexpr int VS = B == 3 ? 4 : 8;
+    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < (uint64_t)B * nn;
+         t += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t i = t / B;
+        const int r = (int)(t - (uint64_t)B * i);
+        const uint32_t a = agg[i];
+        if (a == kNone) continue;
+        const float *q = Q + (i * B + r) * 6;
+        const float *ev = e + (uint64_t)ES * a;
+        float s = 0.f;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) s = fmaf(q[c], ev[c], s);
+        x[(uint64_t)VS * i + r] += s;
+    }
+}
+
+// e = Cinv r on the coarsest level (warp per row)
+__global__ void k_amg_dense(const float *__restrict__ Cinv, const float *__restrict__ r, float *__restrict__ e, int n,
+                            const PcgScalars *S) {
+    if (done(S)) return;
+    const int lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < n; row += nw) {
+        float s = 0.f;
+        for (int k = lane; k < n; k += 32) s = fmaf(Cinv[(uint64_t)row * n + k], r[k], s);
+        s = warp_sum(s);
+        if (lane == 0) e[row] = s;
+    }
+}
+
+// one power step for lambda_max(D^-1 K): w = D^-1 K v (v, w padded); |w|^2 and v.w reduced
+template <int B>
+__global__ void __launch_bounds__(kRowThreads)
+    k_amg_power(const uint32_t *__restrict__ bptr, const uint32_t *__restrict__ bcol, const float *__restrict__ K,
+                const float *__restrict__ Dinv, const float *__restrict__ v, float *__restrict__ w, uint64_t nn,
+                double *partials, unsigned *ticket, double *out2) {
+    constexpr int VS = B == 3 ? 4 : 8;
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    float ww = 0.f, vw = 0.f;
+    for (uint64_t I = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; I < nn; I += nw) {
+        float d[B];
+        if (B == 3) {
+            const float a = row3(bcol, K, bptr[I], bptr[I + 1], lane, v);
+            d[0] = __shfl_sync(0xffffffffu, a, 0);
+            d[1] = __shfl_sync(0xffffffffu, a, 8);
+            d[2] = __shfl_sync(0xffffffffu, a, 16);
+        } else {
+            float a[6];
+            row6(bcol, K, bptr[I], bptr[I + 1], lane, v, a);
+#pragma unroll
+            for (int k = 0; k < B; ++k) d[k] = a[k < 6 ? k : 0];
+        }
+        if (lane < B) {
+            const float *D = Dinv + (uint64_t)B * B * I + B * lane;
+            float s = 0.f;
+#pragma unroll
+            for (int k = 0; k < B; ++k) s = fmaf(D[k], d[k], s);
+            w[(uint64_t)VS * I + lane] = s;
+            ww = fmaf(s, s, ww);
+            vw = fmaf(v[(uint64_t)VS * I + lane], s, vw);
+        }
+    }
+    const float t[2] = {ww, vw};
+    double out[2];
+    if (grid_reduce_t<2, 0u>(t, partials, ticket, out) && threadIdx.x == 0) {
+        out2[0] = out[0];
+        out2[1] = out[1];
+    }
+}
+
+// v = s w (padded vectors), or a deterministic pseudo-random start in [-1, 1) when w == nullptr
+__global__ void k_amg_scale(float *__restrict__ v, const float *__restrict__ w, float s, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        if (w) {
+            v[i] = s * w[i];
+        } else {
+            uint32_t h = (uint32_t)(i * 2654435761ull) ^ 0x9e3779b9u;
+            h ^= h >> 16;
+            h *= 0x7feb352du;
+            h ^= h >> 15;
+            v[i] = (float)(h & 0xffffff) * (2.0f / 16777216.0f) - 1.0f;
+        }
+    }
+}
+
+// Level-0 epilogues of the bulk-copy SpMV (spmv_bulk.cuh), which streams K32 at the HBM rate:
+//   EpiRes   res = r - K x
+//   EpiPost  z = x + omega D^-1 (r - K x), r.z reduced -> rz, beta (start: rz / beta_den or 0)
+struct EpiRes {
+    const float *r;
+    float *res;
+    static constexpr bool kReduce = false;
+    __device__ __forceinline__ void row(uint64_t I, float qi, int lane, const float *, float &) const {
+        if ((lane & 7) == 0 && lane < 24) {
+            const uint64_t i = 3 * I + (lane >> 3);
+            res[i] = r[i] - qi;
+        }
+    }
+    __device__ static unsigned *ticket(PcgScalars *S) { return &S->cnt_d; }
+    __device__ void final(PcgScalars *, double) const {}
+};
+
+struct EpiPost {
+    const float *r, *D;
+    float *z;
+    float omega;
+    int start;
+    double beta_den;
+    static constexpr bool kReduce = true;
+    __device__ __forceinline__ void row(uint64_t I, float qi, int lane, const float *__restrict__ x, float &acc) const {
+        const float v0 = __shfl_sync(0xffffffffu, qi, 0), v1 = __shfl_sync(0xffffffffu, qi, 8),
+                    v2 = __shfl_sync(0xffffffffu, qi, 16);
+        if (lane < 3) {
+            const float d0 = r[3 * I] - v0, d1 = r[3 * I + 1] - v1, d2 = r[3 * I + 2] - v2;
+            const float *Dr = D + 9 * I + 3 * lane;
+            const float zc = x[4 * I + lane] + omega * (Dr[0] * d0 + Dr[1] * d1 + Dr[2] * d2);
+            z[4 * I + lane] = zc;
+            acc = fmaf(r[3 * I + lane], zc, acc);
+        }
+    }
+    __device__ static unsigned *ticket(PcgScalars *S) { return &S->cnt_d; }
+    __device__ void final(PcgScalars *S, double v) const {
+        S->beta = start ? (beta_den > 0.0 ? v / beta_den : 0.0) : v / S->rz;
+        S->rz = v;
+        if (!isfinite(v)) {
+            S->status = LMTG_ERR_NAN;
+            S->done = 1;
+        }
+    }
+};
+
+// one instance of the bulk kernel per (stage shape, epilogue); its resident grid is set up once
+template <int kSt, int kCap, int kCons, bool kEF, int kMinB, class Epi>
+struct Bulk0 {
+    static int &grid() {
+        static int g = 0;
+        return g;
+    }
+    static void setup(lmtg_ctx *c) {
+        if (grid()) return;
+        constexpr size_t smem = bulk_smem_bytes<kSt, kCap>();
+        auto fn = k_pcg_spmv_bulk<kSt, kCap, kCons, kEF, kMinB, Epi>;
+        LMTG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int nb = 0;
+        LMTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, bulk_threads<kCons>(), smem));
+        grid() = c->sm_count * (nb > 0 ? nb : 1);
+    }
+    static void launch(lmtg_ctx *c, const float *x, Epi epi, cudaStream_t s) {
+        k_pcg_spmv_bulk<kSt, kCap, kCons, kEF, kMinB, Epi><<<grid(), bulk_threads<kCons>(), bulk_smem_bytes<kSt, kCap>(), s>>>(
+            c->bptr.p, c->bcol.p, c->K32.p, x, epi, c->nn, c->scal.p, c->partials.p);
+    }
+};
+// the shapes of the PCG's own SpMV: 4 CTAs per SM for rows of <= 32 blocks, 5 for wider rows
+template <class Epi> using Bulk0N = Bulk0<2, 512, 8, true, 4, Epi>;
+template <class Epi> using Bulk0W = Bulk0<2, 512, 8, true, 5, Epi>;
+
+template <class Epi>
+static void bulk0_launch(lmtg_ctx *c, const float *x, Epi epi, cudaStream_t s) {
+    if (c->max_row_blocks > 32) Bulk0W<Epi>::launch(c, x, epi, s);
+    else Bulk0N<Epi>::launch(c, x, epi, s);
+}
+
+static void bulk0_setup(lmtg_ctx *c) {
+    if (c->max_row_blocks > 32) {
+        Bulk0W<EpiRes>::setup(c);
+        Bulk0W<EpiPost>::setup(c);
+    } else {
+        Bulk0N<EpiRes>::setup(c);
+        Bulk0N<EpiPost>::setup(c);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// host structure setup
+// ---------------------------------------------------------------------------------------------
+
+struct HostLevel {
+    int b = 3;
+    uint64_t nn = 0;
+    std::vector<uint32_t> bptr, bcol, bdiag;  // level pattern (levels >= 1; level 0 from the device)
+};
+
+// standard aggregation of a node graph; skip[i] = node left out
+static uint64_t aggregate(uint64_t nn, const std::vector<uint32_t> &bptr, const std::vector<uint32_t> &bcol,
+                          const std::vector<uint8_t> &skip, std::vector<uint32_t> &agg) {
+    agg.assign(nn, kNone);
+    const uint32_t kFree = kNone, kSkip = kNone - 1;
+    for (uint64_t i = 0; i < nn; ++i)
+        if (!skip.empty() && skip[i]) agg[i] = kSkip;
+    uint64_t na = 0;
+    // pass 1: roots whose neighbours are all free
+    for (uint64_t i = 0; i < nn; ++i) {
+        if (agg[i] != kFree) continue;
+        bool ok = true;
+        for (uint32_t k = bptr[i]; k < bptr[i + 1] && ok; ++k) {
+            const uint32_t j = bcol[k];
+            if (j != i && agg[j] != kFree && agg[j] != kSkip) ok = false;
+        }
+        if (!ok) continue;
+        for (uint32_t k = bptr[i]; k < bptr[i + 1]; ++k)
+            if (agg[bcol[k]] == kFree) agg[bcol[k]] = (uint32_t)na;
+        agg[i] = (uint32_t)na++;
+    }
+    // pass 2: leftovers join the neighbouring aggregate they have most links to (first on ties)
+    std::vector<uint32_t> cand;
+    std::vector<uint32_t> add(nn, kFree);
+    for (uint64_t i = 0; i < nn; ++i) {
+        if (agg[i] != kFree) continue;
+        cand.clear();
+        for (uint32_t k = bptr[i]; k < bptr[i + 1]; ++k) {
+            const uint32_t a = agg[bcol[k]];
+            if (a < kSkip) cand.push_back(a);
+        }
+        if (cand.empty()) continue;
+        uint32_t best = cand[0];
+        int bestn = 0;
+        for (size_t u = 0; u < cand.size(); ++u) {
+            int m = 0;
+            for (size_t w = 0; w < cand.size(); ++w) m += cand[w] == cand[u];
+            if (m > bestn) {
+                bestn = m;
+                best = cand[u];
+            }
+        }
+        add[i] = best;
+    }
+    for (uint64_t i = 0; i < nn; ++i)
+        if (add[i] != kFree) agg[i] = add[i];
+    // pass 3: the rest, grouped around a free node with its free neighbours
+    for (uint64_t i = 0; i < nn; ++i) {
+        if (agg[i] != kFree) continue;
+        for (uint32_t k = bptr[i]; k < bptr[i + 1]; ++k)
+            if (agg[bcol[k]] == kFree) agg[bcol[k]] = (uint32_t)na;
+        agg[i] = (uint32_t)na++;
+    }
+    for (uint64_t i = 0; i < nn; ++i)
+        if (agg[i] == kSkip) agg[i] = kNone;
+    return na;
+}
+
+// Tentative prolongator of one level: Q (nn x b x 6, row-major per node) and the coarse modes
+// Bc (na x 6 x 6) from the level's modes Bf (nn x b x 6), orthonormalised per aggregate.
+static void tentative(int b, uint64_t nn, uint64_t na, const std::vector<uint32_t> &aptr,
+                      const std::vector<uint32_t> &anode, const std::vector<double> &Bf, std::vector<float> &Q,
+                      std::vector<double> &Bc) {
+    Q.assign(nn * b * 6, 0.f);
+    Bc.assign(na * 36, 0.0);
+    const unsigned nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    auto work = [&](uint64_t a0, uint64_t a1) {
+        std::vector<double> M;
+        for (uint64_t a = a0; a < a1; ++a) {
+            const uint32_t n0 = aptr[a], m = aptr[a + 1] - n0;
+            const size_t rows = (size_t)m * b;
+            M.assign(rows * 6, 0.0);
+            for (uint32_t t = 0; t < m; ++t) {
+                const uint32_t i = anode[n0 + t];
+                for (int r = 0; r < b; ++r)
+                    for (int c = 0; c < 6; ++c) M[((size_t)t * b + r) * 6 + c] = Bf[((size_t)i * b + r) * 6 + c];
+            }
+            double R[6][6] = {{0}};
+            double norm0[6];
+            for (int c = 0; c < 6; ++c) {
+                double s = 0;
+                for (size_t q = 0; q < rows; ++q) s += M[q * 6 + c] * M[q * 6 + c];
+                norm0[c] = std::sqrt(s);
+            }
+            for (int c = 0; c < 6; ++c) {
+                for (int pass = 0; pass < 2; ++pass)  // Gram-Schmidt, twice for orthogonality
+                    for (int p = 0; p < c; ++p) {
+                        double s = 0;
+                        for (size_t q = 0; q < rows; ++q) s += M[q * 6 + p] * M[q * 6 + c];
+                        R[p][c] += s;
+                        for (size_t q = 0; q < rows; ++q) M[q * 6 + c] -= s * M[q * 6 + p];
+                    }
+                double s = 0;
+                for (size_t q = 0; q < rows; ++q) s += M[q * 6 + c] * M[q * 6 + c];
+                s = std::sqrt(s);
+                if (s <= 1e-10 * norm0[c] || s == 0.0) {  // a mode the aggregate cannot carry
+                    for (size_t q = 0; q < rows; ++q) M[q * 6 + c] = 0.0;
+                    R[c][c] = 0.0;
+                } else {
+                    R[c][c] = s;
+                    for (size_t q = 0; q < rows; ++q) M[q * 6 + c] /= s;
+                }
+            }
+            for (uint32_t t = 0; t < m; ++t) {
+                const uint32_t i = anode[n0 + t];
+                for (int r = 0; r < b; ++r)
+                    for (int c = 0; c < 6; ++c) Q[((size_t)i * b + r) * 6 + c] = (float)M[((size_t)t * b + r) * 6 + c];
+            }
+            for (int r = 0; r < 6; ++r)
+                for (int c = 0; c < 6; ++c) Bc[a * 36 + r * 6 + c] = R[r][c];
+        }
+    };
+    std::vector<std::thread> th;
+    const uint64_t per = (na + nt - 1) / nt;
+    for (unsigned t = 0; t < nt; ++t) {
+        const uint64_t a0 = t * per, a1 = std::min<uint64_t>(na, a0 + per);
+        if (a0 < a1) th.emplace_back(work, a0, a1);
+    }
+    for (auto &t : th) t.join();
+}
+
+// Coarse pattern (sorted distinct aggregate columns per aggregate row) and the Galerkin gather
+// lists (fine block, fine row) per coarse block, in the order aggregate nodes x row blocks.
+static void coarse_pattern(uint64_t na, const std::vector<uint32_t> &aptr, const std::vector<uint32_t> &anode,
+                           const std::vector<uint32_t> &fbptr, const std::vector<uint32_t> &fbcol,
+                           const std::vector<uint32_t> &agg, std::vector<uint32_t> &cbptr,
+                           std::vector<uint32_t> &cbcol, std::vector<uint32_t> &cbdiag, std::vector<uint32_t> &gptr,
+                           std::vector<uint32_t> &gsrc) {
+    const unsigned nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    const uint64_t per = (na + nt - 1) / nt;
+    std::vector<uint32_t> cdeg(na), cnt(na);
+    // per-aggregate distinct columns, sorted (mark[J] = the last aggregate that listed J)
+    auto distinct = [&](uint64_t a, std::vector<uint32_t> &cols, std::vector<uint32_t> &mark, uint32_t *nent) {
+        cols.clear();
+        uint32_t e = 0;
+        for (uint32_t t = aptr[a]; t < aptr[a + 1]; ++t) {
+            const uint32_t i = anode[t];
+            for (uint32_t k = fbptr[i]; k < fbptr[i + 1]; ++k) {
+                const uint32_t J = agg[fbcol[k]];
+                if (J == kNone) continue;
+                ++e;
+                if (mark[J] != (uint32_t)a) {
+                    mark[J] = (uint32_t)a;
+                    cols.push_back(J);
+                }
+            }
+        }
+        std::sort(cols.begin(), cols.end());
+        if (nent) *nent = e;
+    };
+    {
+        std::vector<std::thread> th;
+        for (unsigned t = 0; t < nt; ++t) {
+            const uint64_t a0 = t * per, a1 = std::min<uint64_t>(na, a0 + per);
+            if (a0 >= a1) continue;
+            th.emplace_back([&, a0, a1] {
+                std::vector<uint32_t> cols, mark(na, kNone);
+                for (uint64_t a = a0; a < a1; ++a) {
+                    distinct(a, cols, mark, &cnt[a]);
+                    cdeg[a] = (uint32_t)cols.size();
+                }
+            });
+        }
+        for (auto &t : th) t.join();
+    }
+    cbptr.assign(na + 1, 0);
+    std::vector<uint64_t> eoff(na + 1, 0);
+    for (uint64_t a = 0; a < na; ++a) {
+        cbptr[a + 1] = cbptr[a] + cdeg[a];
+        eoff[a + 1] = eoff[a] + cnt[a];
+    }
+    if (eoff[na] >= (1ull << 32)) throw Error{LMTG_ERR_UNSUPPORTED, "amg: Galerkin lists over 2^32 entries"};
+    cbcol.assign(cbptr[na] + 4, 0);
+    cbdiag.assign(na, 0);
+    gptr.assign(cbptr[na] + 1, 0);
+    gsrc.assign(2 * eoff[na], 0);
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < nt; ++t) {
+        const uint64_t a0 = t * per, a1 = std::min<uint64_t>(na, a0 + per);
+        if (a0 >= a1) continue;
+        th.emplace_back([&, a0, a1] {
+            std::vector<uint32_t> cols, slotcnt, slotpos, mark(na, kNone);
+            for (uint64_t a = a0; a < a1; ++a) {
+                distinct(a, cols, mark, nullptr);
+                const uint32_t rb = cbptr[a], deg = (uint32_t)cols.size();
+                for (uint32_t s = 0; s < deg; ++s) {
+                    cbcol[rb + s] = cols[s];
+                    if (cols[s] == a) cbdiag[a] = rb + s;
+                }
+                slotcnt.assign(deg, 0);
+                auto slot_of = [&](uint32_t J) {
+                    return (uint32_t)(std::lower_bound(cols.begin(), cols.end(), J) - cols.begin());
+                };
+                for (uint32_t t2 = aptr[a]; t2 < aptr[a + 1]; ++t2) {
+                    const uint32_t i = anode[t2];
+                    for (uint32_t k = fbptr[i]; k < fbptr[i + 1]; ++k) {
+                        const uint32_t J = agg[fbcol[k]];
+                        if (J != kNone) ++slotcnt[slot_of(J)];
+                    }
+                }
+                slotpos.assign(deg, 0);
+                uint64_t off = eoff[a];
+                for (uint32_t s = 0; s < deg; ++s) {
+                    gptr[rb + s] = (uint32_t)off;
+                    slotpos[s] = (uint32_t)off;
+                    off += slotcnt[s];
+                }
+                for (uint32_t t2 = aptr[a]; t2 < aptr[a + 1]; ++t2) {
+                    const uint32_t i = anode[t2];
+                    for (uint32_t k = fbptr[i]; k < fbptr[i + 1]; ++k) {
+                        const uint32_t J = agg[fbcol[k]];
+                        if (J == kNone) continue;
+                        const uint32_t p = slotpos[slot_of(J)]++;
+                        gsrc[2 * (uint64_t)p] = k;
+                        gsrc[2 * (uint64_t)p + 1] = i;
+                    }
+                }
+            }
+        });
+    }
+    for (auto &t : th) t.join();
+    gptr[cbptr[na]] = (uint32_t)eoff[na];
+}
+
+template <class T>
+static void upload(DBuf<T> &d, const std::vector<T> &h, cudaStream_t s) {
+    d.alloc(h.size());
+    if (!h.empty()) LMTG_CUDA(cudaMemcpyAsync(d.p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+}
+
+}  // namespace
+
+void amg_free(lmtg_ctx *c) {
+    delete c->amg;
+    c->amg = nullptr;
+}
+
+bool amg_applicable(const lmtg_ctx *c) {
+    return c->precond == LMTG_PREC_AMG && c->nnu == 3 && !c->recal && c->nsys == 0 && c->n >= 3000 &&
+           (c->elem_type == LMTG_ELEM_HEXA8 || c->elem_type == LMTG_ELEM_TETRA10);
+}
+
+// Structure of the hierarchy: aggregates, tentative prolongators, coarse patterns and gather lists.
+static void amg_build_structure(lmtg_ctx *c) {
+    Phase ph("lmtg.amg.structure");
+    auto t0 = std::chrono::steady_clock::now();
+    cudaStream_t s = c->stream;
+    std::unique_ptr<AmgState> A(new AmgState());
+    // level 0 pattern from the device
+    HostLevel cur;
+    cur.b = 3;
+    cur.nn = c->nn;
+    cur.bptr.resize(c->nn + 1);
+    cur.bcol.resize(c->nnzb);
+    LMTG_CUDA(cudaMemcpyAsync(cur.bptr.data(), c->bptr.p, 4 * (c->nn + 1), cudaMemcpyDeviceToHost, s));
+    LMTG_CUDA(cudaMemcpyAsync(cur.bcol.data(), c->bcol.p, 4 * c->nnzb, cudaMemcpyDeviceToHost, s));
+    LMTG_CUDA(cudaStreamSynchronize(s));
+    // nodes with a constraint stay out of the coarse spaces
+    std::vector<uint8_t> skip(c->nn, 0);
+    if (c->h_cdof.size() == c->nc)
+        for (uint32_t d : c->h_cdof)
+            if (d / 3 < c->nn) skip[d / 3] = 1;
+    // rigid-body modes about the mesh centroid (nodes x 3 x 6)
+    std::vector<double> Bf(c->nn * 18, 0.0);
+    {
+        double cen[3] = {0, 0, 0};
+        for (uint64_t i = 0; i < c->nn; ++i)
+            for (int d = 0; d < 3; ++d) cen[d] += c->h_pos[3 * i + d];
+        for (int d = 0; d < 3; ++d) cen[d] /= (double)c->nn;
+        for (uint64_t i = 0; i < c->nn; ++i) {
+            const double x = c->h_pos[3 * i] - cen[0], y = c->h_pos[3 * i + 1] - cen[1], z = c->h_pos[3 * i + 2] - cen[2];
+            double *m = &Bf[i * 18];
+            m[0 * 6 + 0] = 1;
+            m[1 * 6 + 1] = 1;
+            m[2 * 6 + 2] = 1;
+            // rotations about z, x, y: (-y, x, 0), (0, -z, y), (z, 0, -x)
+            m[0 * 6 + 3] = -y;
+            m[1 * 6 + 3] = x;
+            m[1 * 6 + 4] = -z;
+            m[2 * 6 + 4] = y;
+            m[0 * 6 + 5] = z;
+            m[2 * 6 + 5] = -x;
+        }
+    }
+    for (int l = 0;; ++l) {
+        std::unique_ptr<AmgLevel> L(new AmgLevel());
+        L->b = cur.b;
+        L->nn = cur.nn;
+        L->nnzb = cur.bptr[cur.nn];
+        const int VS = cur.b == 3 ? 4 : 8;
+        L->xa.alloc(VS * cur.nn);
+        L->xb.alloc(VS * cur.nn);
+        L->res.alloc(cur.b * cur.nn + 4);
+        if (l > 0) {
+            L->r.alloc(cur.b * cur.nn + 4);
+            upload(L->bptr, cur.bptr, s);
+            upload(L->bcol, cur.bcol, s);
+            upload(L->bdiag, cur.bdiag, s);
+            L->K.alloc(36 * L->nnzb);
+            L->Dinv.alloc(36 * cur.nn);
+        }
+        const bool coarsest = (uint64_t)cur.b * cur.nn <= kCoarsestDofs || l + 1 >= kMaxLevels;
+        if (coarsest) {
+            A->levels.push_back(std::move(L));
+            break;
+        }
+        std::vector<uint32_t> agg;
+        const uint64_t na = aggregate(cur.nn, cur.bptr, cur.bcol, l == 0 ? skip : std::vector<uint8_t>(), agg);
+        if (na == 0 || na * 2 > cur.nn) {  // no useful coarsening left: this level is the coarsest
+            A->levels.push_back(std::move(L));
+            break;
+        }
+        std::vector<uint32_t> aptr(na + 1, 0), anode;
+        for (uint64_t i = 0; i < cur.nn; ++i)
+            if (agg[i] != kNone) ++aptr[agg[i] + 1];
+        for (uint64_t a = 0; a < na; ++a) aptr[a + 1] += aptr[a];
+        anode.resize(aptr[na]);
+        {
+            std::vector<uint32_t> pos(aptr.begin(), aptr.end() - 1);
+            for (uint64_t i = 0; i < cur.nn; ++i)
+                if (agg[i] != kNone) anode[pos[agg[i]]++] = (uint32_t)i;
+        }
+        std::vector<float> Q;
+        std::vector<double> Bc;
+        tentative(cur.b, cur.nn, na, aptr, anode, Bf, Q, Bc);
+        HostLevel nxt;
+        nxt.b = 6;
+        nxt.nn = na;
+        std::vector<uint32_t> gptr, gsrc;
+        coarse_pattern(na, aptr, anode, cur.bptr, cur.bcol, agg, nxt.bptr, nxt.bcol, nxt.bdiag, gptr, gsrc);
+        L->nagg = na;
+        upload(L->agg, agg, s);
+        upload(L->aptr, aptr, s);
+        upload(L->anode, anode, s);
+        upload(L->Q, Q, s);
+        upload(L->gptr, gptr, s);
+        upload(L->gsrc, gsrc, s);
+        LMTG_CUDA(cudaStreamSynchronize(s));
+        A->levels.push_back(std::move(L));
+        Bf.swap(Bc);
+        cur = std::move(nxt);
+    }
+    // coarsest dense buffers; no hierarchy (block Jacobi instead) with a single level or a
+    // coarsest level too large for a dense inverse
+    AmgLevel &C = *A->levels.back();
+    const uint64_t nc = (uint64_t)C.b * C.nn;
+    A->nc = (A->levels.size() > 1 && nc <= 2000) ? (int)nc : 0;
+    if (A->nc) A->Cinv.alloc((size_t)A->nc * A->nc);
+    A->structure_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    c->amg = A.release();
+}
+
+// Numeric setup after an assembly: Galerkin products, block inverses, smoother weights, dense
+// coarsest inverse.
+static void amg_numeric(lmtg_ctx *c) {
+    Phase ph("lmtg.amg.numeric");
+    auto t0 = std::chrono::steady_clock::now();
+    AmgState &A = *c->amg;
+    cudaStream_t s = c->stream;
+    const size_t nl = A.levels.size();
+    for (size_t l = 0; l + 1 < nl; ++l) {
+        AmgLevel &F = *A.levels[l], &C = *A.levels[l + 1];
+        const uint32_t *fbptr = l == 0 ? c->bptr.p : F.bptr.p;
+        const uint32_t *fbcol = l == 0 ? c->bcol.p : F.bcol.p;
+        const float *fK = l == 0 ? c->K32.p : F.K.p;
+        const uint64_t ncb = C.nnzb;
+        const int g = grid_for(c, ncb, 128, 16);
+        if (F.b == 3)
+            k_galerkin<3><<<g, 128, 0, s>>>(fbptr, fbcol, fK, F.Q.p, C.bptr.p, C.bcol.p, C.nn, F.gptr.p, F.gsrc.p, C.K.p);
+        else
+            k_galerkin<6><<<g, 128, 0, s>>>(fbptr, fbcol, fK, F.Q.p, C.bptr.p, C.bcol.p, C.nn, F.gptr.p, F.gsrc.p, C.K.p);
+        k_block_inv6<<<grid_for(c, C.nn, 128), 128, 0, s>>>(C.bptr.p, C.bdiag.p, C.K.p, C.nn, C.Dinv.p);
+        LMTG_CUDA(cudaGetLastError());
+        c->launches += 2;
+    }
+    // smoother weights: omega = 1 / theta of a degree-1 Chebyshev on [lmax/30, 1.1 lmax]
+    PcgScalars *o = c->scal.p + 1;
+    double *out2 = reinterpret_cast<double *>(&o->pq);  // pq, rr: two doubles of the outer slot
+    for (size_t l = 0; l + 1 < nl; ++l) {
+        AmgLevel &L = *A.levels[l];
+        const int VS = L.b == 3 ? 4 : 8;
+        const uint64_t nv = (uint64_t)VS * L.nn;
+        const uint32_t *bp = l == 0 ? c->bptr.p : L.bptr.p, *bc = l == 0 ? c->bcol.p : L.bcol.p;
+        const float *K = l == 0 ? c->K32.p : L.K.p, *D = l == 0 ? c->Dinv32.p : L.Dinv.p;
+        k_amg_scale<<<grid_for(c, nv, 256), 256, 0, s>>>(L.xa.p, nullptr, 1.f, nv);  // random start
+        c->launches += 1;
+        // power steps v -> w = D^-1 K v, v normalised from the second step on: lambda ~ |w|
+        double lam = 0, h[2] = {0, 0};
+        float scale = 1.f;
+        for (int it = 0; it < 10; ++it) {
+            float *v = (it & 1) ? L.xb.p : L.xa.p, *w = (it & 1) ? L.xa.p : L.xb.p;
+            if (it > 0) k_amg_scale<<<grid_for(c, nv, 256), 256, 0, s>>>(v, v, scale, nv);
+            const int g = grid_for(c, L.nn * 32, kRowThreads, 8);
+            if (L.b == 3)
+                k_amg_power<3><<<g, kRowThreads, 0, s>>>(bp, bc, K, D, v, w, L.nn, c->partials.p, &o->cnt_c, out2);
+            else
+                k_amg_power<6><<<g, kRowThreads, 0, s>>>(bp, bc, K, D, v, w, L.nn, c->partials.p, &o->cnt_c, out2);
+            LMTG_CUDA(cudaGetLastError());
+            LMTG_CUDA(cudaMemcpyAsync(h, out2, sizeof(h), cudaMemcpyDeviceToHost, s));
+            LMTG_CUDA(cudaStreamSynchronize(s));
+            c->launches += it > 0 ? 2 : 1;
+            if (it > 0) lam = std::sqrt(h[0]);
+            scale = h[0] > 0 ? (float)(1.0 / std::sqrt(h[0])) : 1.f;
+        }
+        const double hi = 1.1 * lam, lo = hi / 30.0;
+        L.lambda = lam;
+        L.omega = lam > 0 ? (float)(2.0 / (hi + lo)) : 1.f;
+    }
+    // dense inverse of the coarsest level (FP64 Gauss-Jordan with partial pivoting on the host;
+    // a pivot below 1e-13 of the largest diagonal makes that unknown decoupled)
+    {
+        AmgLevel &C = *A.levels.back();
+        const int n = A.nc;
+        std::vector<uint32_t> bp(C.nn + 1), bc(C.nnzb);
+        std::vector<float> K(36 * C.nnzb);
+        LMTG_CUDA(cudaMemcpyAsync(bp.data(), C.bptr.p, 4 * bp.size(), cudaMemcpyDeviceToHost, s));
+        LMTG_CUDA(cudaMemcpyAsync(bc.data(), C.bcol.p, 4 * bc.size(), cudaMemcpyDeviceToHost, s));
+        LMTG_CUDA(cudaMemcpyAsync(K.data(), C.K.p, 4 * K.size(), cudaMemcpyDeviceToHost, s));
+        LMTG_CUDA(cudaStreamSynchronize(s));
+        std::vector<double> M((size_t)n * 2 * n, 0.0);
+        const size_t w = 2 * (size_t)n;
+        for (uint64_t I = 0; I < C.nn; ++I) {
+            const uint32_t rb = bp[I], deg = bp[I + 1] - rb;
+            for (uint32_t b = 0; b < deg; ++b)
+                for (int r = 0; r < 6; ++r)
+                    for (int cc = 0; cc < 6; ++cc)
+                        M[(6 * I + r) * w + 6 * (size_t)bc[rb + b] + cc] = K[kidx6(rb, deg, b, 6 * r + cc)];
+        }
+        double dmax = 0;
+        for (int i = 0; i < n; ++i) {
+            dmax = std::max(dmax, std::fabs(M[i * w + i]));
+            M[i * w + n + i] = 1.0;
+        }
+        std::vector<char> dead(n, 0);
+        for (int col = 0; col < n; ++col) {
+            int p = col;
+            for (int r = col + 1; r < n; ++r)
+                if (std::fabs(M[r * w + col]) > std::fabs(M[p * w + col])) p = r;
+            if (std::fabs(M[p * w + col]) <= 1e-13 * dmax) {
+                dead[col] = 1;
+                continue;
+            }
+            if (p != col)
+                for (size_t k = 0; k < w; ++k) std::swap(M[col * w + k], M[p * w + k]);
+            const double iv = 1.0 / M[col * w + col];
+            for (size_t k = 0; k < w; ++k) M[col * w + k] *= iv;
+            for (int r = 0; r < n; ++r) {
+                if (r == col) continue;
+                const double f = M[r * w + col];
+                if (f == 0.0) continue;
+                for (size_t k = col; k < w; ++k) M[r * w + k] -= f * M[col * w + k];
+            }
+        }
+        std::vector<float> Ci((size_t)n * n);
+        for (int r = 0; r < n; ++r)
+            for (int k = 0; k < n; ++k)
+                Ci[(size_t)r * n + k] = (dead[r] || dead[k]) ? 0.f : (float)M[r * w + n + k];
+        LMTG_CUDA(cudaMemcpyAsync(A.Cinv.p, Ci.data(), 4 * Ci.size(), cudaMemcpyHostToDevice, s));
+        LMTG_CUDA(cudaStreamSynchronize(s));
+    }
+    A.version = c->mat_version;
+    A.numeric_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+bool amg_prepare(lmtg_ctx *c) {
+    if (!amg_applicable(c)) return false;
+    LMTG_CHECK(c->have32, LMTG_ERR_STATE, "amg: FP32 matrix not assembled");
+    if (!c->amg) amg_build_structure(c);
+    if (c->amg->nc == 0) return false;
+    bulk0_setup(c);
+    if (c->amg->version != c->mat_version) amg_numeric(c);
+    return true;
+}
+
+// Level-0 smoothing weight (the update kernel applies the first smoothing step itself).
+float amg_omega0(const lmtg_ctx *c) { return c->amg->levels[0]->omega; }
+float *amg_xa0(const lmtg_ctx *c) { return c->amg->levels[0]->xa.p; }
+
+// The cycle after the update kernel: r (level-0 residual, packed) -> z (padded), rz and beta.
+void amg_launch_cycle(lmtg_ctx *c, const float *r, float *z, cudaStream_t s, int start, double beta_den) {
+    AmgState &A = *c->amg;
+    PcgScalars *S = c->scal.p;
+    const size_t nl = A.levels.size();
+    // down: residual and restriction
+    for (size_t l = 0; l + 1 < nl; ++l) {
+        AmgLevel &L = *A.levels[l], &N = *A.levels[l + 1];
+        const float *rl = l == 0 ? r : L.r.p;
+        const uint32_t *bp = l == 0 ? c->bptr.p : L.bptr.p, *bc = l == 0 ? c->bcol.p : L.bcol.p;
+        const float *K = l == 0 ? c->K32.p : L.K.p;
+        const int g = grid_for(c, L.nn * 32, kRowThreads, 8);
+        if (l > 0) {
+            k_amg_bj6<<<grid_for(c, 6 * L.nn, 256), 256, 0, s>>>(L.Dinv.p, rl, L.xa.p, L.omega, L.nn, S);
+            c->launches += 1;
+        }
+        if (L.b == 3) {
+            bulk0_launch(c, L.xa.p, EpiRes{rl, L.res.p}, s);
+            k_amg_restrict<3><<<grid_for(c, L.nagg * 32, kRowThreads, 8), kRowThreads, 0, s>>>(L.aptr.p, L.anode.p, L.Q.p,
+                                                                                            L.res.p, N.r.p, L.nagg, S);
+        } else {
+            k_amg_res<6><<<g, kRowThreads, 0, s>>>(bp, bc, K, L.xa.p, rl, L.res.p, L.nn, S);
+            k_amg_restrict<6><<<grid_for(c, L.nagg * 32, kRowThreads, 8), kRowThreads, 0, s>>>(L.aptr.p, L.anode.p, L.Q.p,
+                                                                                            L.res.p, N.r.p, L.nagg, S);
+        }
+        c->launches += 2;
+    }
+    // coarsest
+    {
+        AmgLevel &C = *A.levels.back();
+        k_amg_dense<<<grid_for(c, (uint64_t)A.nc * 32, 256, 4), 256, 0, s>>>(A.Cinv.p, C.r.p, C.res.p, A.nc, S);
+        c->launches += 1;
+    }
+    // up: prolongation and post-smoothing
+    for (size_t l = nl - 1; l-- > 0;) {
+        AmgLevel &L = *A.levels[l], &N = *A.levels[l + 1];
+        const bool ncoarsest = l + 2 == nl;
+        const float *e = ncoarsest ? N.res.p : N.xb.p;
+        const int tb = 256;
+        if (L.b == 3) {
+            if (ncoarsest)
+                k_amg_prolong<3, 6><<<grid_for(c, 3 * L.nn, tb), tb, 0, s>>>(L.agg.p, L.Q.p, e, L.xa.p, L.nn, S);
+            else
+                k_amg_prolong<3, 8><<<grid_for(c, 3 * L.nn, tb), tb, 0, s>>>(L.agg.p, L.Q.p, e, L.xa.p, L.nn, S);
+        } else {
+            if (ncoarsest)
+                k_amg_prolong<6, 6><<<grid_for(c, 6 * L.nn, tb), tb, 0, s>>>(L.agg.p, L.Q.p, e, L.xa.p, L.nn, S);
+            else
+                k_amg_prolong<6, 8><<<grid_for(c, 6 * L.nn, tb), tb, 0, s>>>(L.agg.p, L.Q.p, e, L.xa.p, L.nn, S);
+        }
+        const int g = grid_for(c, L.nn * 32, kRowThreads, 8);
+        if (l == 0)
+            bulk0_launch(c, L.xa.p, EpiPost{r, c->Dinv32.p, z, L.omega, start, beta_den}, s);
+        else
+            k_amg_post<6><<<g, kRowThreads, 0, s>>>(L.bptr.p, L.bcol.p, L.K.p, L.Dinv.p, L.xa.p, L.r.p, L.xb.p, L.omega,
+                                                    L.nn, S, false, 0, 0.0, c->partials.p);
+        c->launches += 2;
+    }
+    LMTG_CUDA(cudaGetLastError());
+}
+
+void amg_info(const lmtg_ctx *c, int *levels, uint64_t *ndof, uint64_t *nnzb, double *omega, double *lambda,
+              double *structure_ms, double *numeric_ms) {
+    const AmgState *A = c->amg;
+    const int nl = A ? (int)A->levels.size() : 0;
+    if (levels) *levels = nl;
+    for (int l = 0; l < kMaxLevels; ++l) {
+        const AmgLevel *L = l < nl ? A->levels[l].get() : nullptr;
+        if (ndof) ndof[l] = L ? L->b * L->nn : 0;
+        if (nnzb) nnzb[l] = L ? L->nnzb : 0;
+        if (omega) omega[l] = L ? L->omega : 0.0;
+        if (lambda) lambda[l] = L ? L->lambda : 0.0;
+    }
+    if (structure_ms) *structure_ms = A ? A->structure_ms : 0.0;
+    if (numeric_ms) *numeric_ms = A ? A->numeric_ms : 0.0;
+}
+
+}  // namespace lmtg

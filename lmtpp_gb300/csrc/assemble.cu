@@ -373,6 +373,7 @@ void copy_k64_to_k32(lmtg_ctx *c) {
     LMTG_CUDA(cudaGetLastError());
     c->launches += 1;
     c->have32 = true;
+    ++c->mat_version;
 }
 
 }  // namespace lmtg

@@ -1235,6 +1235,7 @@ int lmtg_diff_mesh_set(lmtg_ctx *c, uint64_t nn, const double *pos, uint64_t ne,
         LMTG_CHECK(nn < (1ull << 32), LMTG_ERR_UNSUPPORTED, "more than 2^32 nodes");
         for (uint64_t q = 0; q < 6 * ne; ++q) LMTG_CHECK(conn[q] < nn, LMTG_ERR_ARG, "node id >= nn");
         recal_free(c);
+        amg_free(c);
         c->elem_type = LMTG_ELEM_TRIANGLE6;
         c->npe = 6;
         c->nnu = 1;

@@ -97,6 +97,7 @@ struct PcgScalars {
     unsigned cnt_a;  // grid-reduction tickets
     unsigned cnt_b;
     unsigned cnt_c;
+    unsigned cnt_d;
 };
 
 }  // namespace lmtg
@@ -104,6 +105,7 @@ struct PcgScalars {
 namespace lmtg {
 struct BatchState;  // batch.cu
 struct RecalState;  // recalage.cu
+struct AmgState;    // amg.cu
 }
 
 struct lmtg_ctx {
@@ -187,6 +189,14 @@ struct lmtg_ctx {
     // context's pattern and matrices hold the 9-unknown system (nnu = 9)
     lmtg::RecalState *recal = nullptr;
 
+    // preconditioner of the FP32 inner PCG (LMTG_PREC_*): the aggregation multigrid (amg.cu) is
+    // built on the first mixed solve after the pattern or the constraints changed, and its
+    // numeric part again after every matrix assembly (mat_version)
+    int precond = LMTG_PREC_AMG;
+    lmtg::AmgState *amg = nullptr;
+    uint64_t mat_version = 0;
+    std::vector<uint32_t> h_cdof;  // host copy of the constrained DOFs
+
     // number of kernels this context has launched (reported by lmtg_get_launch_count)
     uint64_t launches = 0;
 };
@@ -230,6 +240,9 @@ inline void upload_u32(lmtg_ctx *c, DBuf<T> &d, const T *h, size_t n) {
 
 // ---- recalage (recalage.cu) ----
 void recal_free(lmtg_ctx *c);
+
+// ---- aggregation multigrid (amg.cu) ----
+void amg_free(lmtg_ctx *c);
 
 // ---- batches (batch.cu) ----
 void batch_free(lmtg_ctx *c);

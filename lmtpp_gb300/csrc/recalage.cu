@@ -236,6 +236,7 @@ void recal_setup(lmtg_ctx *c, double rho, double omega, double gamma, double r, 
     LMTG_CHECK(rho > 0 && omega != 0 && r < 1, LMTG_ERR_ARG, "recalage: rho > 0, omega != 0, r < 1");
     LMTG_CHECK(Ud && Ud_valid, LMTG_ERR_ARG, "recalage: null Ud or Ud_valid");
     cudaStream_t s = c->stream;
+    amg_free(c);
     RecalState *R = new RecalState();
     c->recal = R;
     LMTG_CUDA(cudaMemcpy(&R->E, c->E.p, sizeof(double), cudaMemcpyDeviceToHost));
@@ -299,6 +300,7 @@ void recal_setup(lmtg_ctx *c, double rho, double omega, double gamma, double r, 
     c->have64 = c->have32 = c->have_vec = false;
     c->nnu = 9;  // elasticity-only calls (assembly, gradients, fields) refuse this context
     c->nc = 0;   // constraints are given on the 9-unknown system, after this call
+    c->h_cdof.clear();
 }
 
 void recal_assemble(lmtg_ctx *c) {
@@ -327,6 +329,7 @@ void recal_assemble(lmtg_ctx *c) {
     copy_k64_to_k32(c);
     c->have32 = true;
     build_block_jacobi(c, true, true);
+    ++c->mat_version;
     LMTG_CUDA(cudaStreamSynchronize(s));
 }
 

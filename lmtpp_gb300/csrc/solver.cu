@@ -9,6 +9,7 @@
 #include <type_traits>
 #include <vector>
 
+#include "amg.cuh"
 #include "spmv_bulk.cuh"
 
 namespace lmtg {
@@ -58,7 +59,7 @@ static int node_grid(lmtg_ctx *c) { return grid_for(c, c->nn, kRowThreads, 8); }
 template <int kStages, int kCap, int kCons, bool kEF, int kMinB>
 static int bulk_grid(lmtg_ctx *c) {
     constexpr size_t smem = bulk_smem_bytes<kStages, kCap>();
-    auto fn = k_pcg_spmv_bulk<kStages, kCap, kCons, kEF, kMinB>;
+    auto fn = k_pcg_spmv_bulk<kStages, kCap, kCons, kEF, kMinB, EpiPcg>;
     LMTG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int nb = 0;
     LMTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, bulk_threads<kCons>(), smem));
@@ -93,10 +94,9 @@ static void launch_pcg_spmv(lmtg_ctx *c, const T *K, const T *p, T *q, cudaStrea
         switch (spmv_kind_used(c)) {
 #define LMTG_BULK_LAUNCH(id, st, cap, cons, ef, minb)                                                   \
     case id:                                                                                              \
-        k_pcg_spmv_bulk<st, cap, cons, ef, minb><<<c->spmv_grid, bulk_threads<cons>(),                      \
-                                                   bulk_smem_bytes<st, cap>(), s>>>(c->bptr.p, c->bcol.p, K, p, q, \
-                                                                                    c->nn, c->scal.p,      \
-                                                                                    c->partials.p);        \
+        k_pcg_spmv_bulk<st, cap, cons, ef, minb, EpiPcg><<<c->spmv_grid, bulk_threads<cons>(),              \
+                                                           bulk_smem_bytes<st, cap>(), s>>>(              \
+            c->bptr.p, c->bcol.p, K, p, EpiPcg{q}, c->nn, c->scal.p, c->partials.p);                       \
         return;
             LMTG_BULK_KINDS(LMTG_BULK_LAUNCH)
 #undef LMTG_BULK_LAUNCH
@@ -151,6 +151,110 @@ static double dot64(lmtg_ctx *c, const double *a, const double *b) {
     return read_double(c, &o->rr);
 }
 
+// Multigrid-preconditioned FP32 PCG: the start and update kernels leave z to the cycle
+// (amg.cu), whose last kernel forms z, r.z and beta.  Both write the cycle's first smoothing
+// step xa = omega D^-1 r (padded 4 per node).
+__global__ void k_pcg_start_amg(const float *__restrict__ r, const float *__restrict__ b,
+                                const float *__restrict__ Dinv, float *__restrict__ xa, float omega, uint64_t nn,
+                                PcgScalars *S, double *partials) {
+    float t[3] = {0.f, 0.f, 0.f};  // rr, bb, rinf
+    for (uint64_t I = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; I < nn;
+         I += (uint64_t)gridDim.x * blockDim.x) {
+        const float *D = Dinv + 9 * I;
+        const float r0 = r[3 * I], r1 = r[3 * I + 1], r2 = r[3 * I + 2];
+        xa[4 * I] = omega * (D[0] * r0 + D[1] * r1 + D[2] * r2);
+        xa[4 * I + 1] = omega * (D[3] * r0 + D[4] * r1 + D[5] * r2);
+        xa[4 * I + 2] = omega * (D[6] * r0 + D[7] * r1 + D[8] * r2);
+        t[0] += r0 * r0 + r1 * r1 + r2 * r2;
+        if (b) {
+            const float b0 = b[3 * I], b1 = b[3 * I + 1], b2 = b[3 * I + 2];
+            t[1] += b0 * b0 + b1 * b1 + b2 * b2;
+        }
+        t[2] = fmaxf(t[2], fmaxf(fabsf(r0), fmaxf(fabsf(r1), fabsf(r2))));
+    }
+    double out[3];
+    if (grid_reduce_t<3, 4u>(t, partials, &S->cnt_c, out) && threadIdx.x == 0) {
+        S->rr = out[0];
+        if (b) S->bb = out[1];
+        S->iter = 0;
+        S->status = LMTG_OK;
+        S->done = 0;
+        if (S->crit_kind == LMTG_CRIT_REL_RESIDUAL && out[0] <= S->crit * S->crit * S->bb) S->done = 1;
+        if (S->crit_kind == LMTG_CRIT_ABS_RESIDUAL_INF && out[2] <= S->crit) S->done = 1;
+        if (!isfinite(out[0])) {
+            S->done = 1;
+            S->status = LMTG_ERR_NAN;
+        }
+    }
+}
+
+__global__ void k_pcg_update_amg(float *__restrict__ x, float *__restrict__ r, const float *__restrict__ p,
+                                 const float *__restrict__ q, const float *__restrict__ Dinv, float *__restrict__ xa,
+                                 float omega, uint64_t nn, PcgScalars *S, double *partials) {
+    if (*(volatile int *)&S->done) return;
+    const double pq = S->pq;
+    const float alpha = (float)S->alpha;
+    float t[4] = {0.f, 0.f, 0.f, 0.f};  // rr, dx2, dxinf, rinf
+    for (uint64_t I = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; I < nn;
+         I += (uint64_t)gridDim.x * blockDim.x) {
+        float rv[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const uint64_t i = 3 * I + c;
+            const float dx = alpha * p[4 * I + c];
+            x[i] += dx;
+            rv[c] = fmaf(-alpha, q[i], r[i]);
+            r[i] = rv[c];
+            t[1] = fmaf(dx, dx, t[1]);
+            t[2] = fmaxf(t[2], fabsf(dx));
+            t[3] = fmaxf(t[3], fabsf(rv[c]));
+        }
+        const float *D = Dinv + 9 * I;
+        xa[4 * I] = omega * (D[0] * rv[0] + D[1] * rv[1] + D[2] * rv[2]);
+        xa[4 * I + 1] = omega * (D[3] * rv[0] + D[4] * rv[1] + D[5] * rv[2]);
+        xa[4 * I + 2] = omega * (D[6] * rv[0] + D[7] * rv[1] + D[8] * rv[2]);
+        t[0] += rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
+    }
+    double out[4];
+    if (grid_reduce_t<4, (4u | 8u)>(t, partials, &S->cnt_b, out) && threadIdx.x == 0) {
+        S->iter += 1;
+        S->rr = out[0];
+        S->dx_2sq = out[1];
+        S->dx_inf = out[2];
+        bool conv = false;
+        switch (S->crit_kind) {
+            case LMTG_CRIT_REL_RESIDUAL: conv = out[0] <= S->crit * S->crit * S->bb; break;
+            case LMTG_CRIT_NORM_INF_DELTA: conv = out[2] <= S->crit; break;
+            case LMTG_CRIT_NORM2_DELTA: conv = sqrt(out[1]) < S->crit; break;
+            case LMTG_CRIT_ABS_RESIDUAL_INF: conv = out[3] <= S->crit; break;
+        }
+        if (!isfinite(out[0]) || !isfinite(pq)) {
+            S->status = LMTG_ERR_NAN;
+            S->done = 1;
+        } else if (conv) {
+            S->done = 1;
+        } else if (S->iter >= S->maxit) {
+            S->status = LMTG_ERR_NOT_CONVERGED;
+            S->done = 1;
+        }
+    }
+}
+
+// A captured chunk of PCG iterations, kept across the segments of one mixed solve (its kernel
+// arguments -- buffers, scalars, smoother weights -- do not change between segments).
+struct ChunkGraph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    uint64_t launches = 0;  // kernels per chunk
+    ChunkGraph() = default;
+    ChunkGraph(const ChunkGraph &) = delete;
+    ChunkGraph &operator=(const ChunkGraph &) = delete;
+    ~ChunkGraph() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+    }
+};
+
 struct PcgBufs {
     void *x, *r, *z, *p0, *p1, *q;
 };
@@ -163,7 +267,7 @@ template <class T>
 static int run_pcg(lmtg_ctx *c, const T *K, const T *Dinv, const T *b, T *x, T *r, T *z, T *p0,
                    T *p1, T *q, bool x_is_zero, int crit_kind, double crit, int maxit,
                    double b_norm2, std::chrono::steady_clock::time_point deadline, bool use_deadline,
-                   int *iters, double beta_den = 0.0) {
+                   int *iters, double beta_den = 0.0, bool use_amg = false, ChunkGraph *keep = nullptr) {
     Phase ph(sizeof(T) == 4 ? "lmtg.pcg32" : "lmtg.pcg64");
     cudaStream_t s = c->stream;
     spmv_setup(c);
@@ -182,9 +286,19 @@ static int run_pcg(lmtg_ctx *c, const T *K, const T *Dinv, const T *b, T *x, T *
         c->launches += 1;
     }
     constexpr int VS = GatherStride<T>::value;
-    k_pcg_start<T, VS><<<node_grid(c), kRowThreads, 0, s>>>(r, b_norm2 >= 0 ? nullptr : b, Dinv, z,
-                                                             c->nn, c->scal.p, c->partials.p,
-                                                             beta_den);
+    bool amg = false;
+    if constexpr (std::is_same<T, float>::value) {
+        amg = use_amg;
+        if (amg) {
+            k_pcg_start_amg<<<node_grid(c), kRowThreads, 0, s>>>(r, b_norm2 >= 0 ? nullptr : b, Dinv, amg_xa0(c),
+                                                                 amg_omega0(c), c->nn, c->scal.p, c->partials.p);
+            amg_launch_cycle(c, r, z, s, 1, beta_den);
+        }
+    }
+    if (!amg)
+        k_pcg_start<T, VS><<<node_grid(c), kRowThreads, 0, s>>>(r, b_norm2 >= 0 ? nullptr : b, Dinv, z,
+                                                                 c->nn, c->scal.p, c->partials.p,
+                                                                 beta_den);
     if (beta_den <= 0.0) {
         LMTG_CUDA(cudaMemsetAsync(p0, 0, sizeof(T) * VS * c->nn, s));
         LMTG_CUDA(cudaMemsetAsync(p1, 0, sizeof(T) * VS * c->nn, s));
@@ -192,49 +306,57 @@ static int run_pcg(lmtg_ctx *c, const T *K, const T *Dinv, const T *b, T *x, T *
     LMTG_CUDA(cudaGetLastError());
     c->launches += 1;
 
-    // capture one chunk: pairs of iterations alternating the p buffers
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    LMTG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    for (int k = 0; k < 2 * kChunkPairs; ++k) {
-        k_pcg_dir<T, VS><<<node_grid(c), kRowThreads, 0, s>>>(z, p0, c->nn, c->scal.p);
-        launch_pcg_spmv<T, VS>(c, K, p0, q, s);
-        k_pcg_update<T, VS><<<node_grid(c), kRowThreads, 0, s>>>(x, r, z, p0, q, Dinv, c->nn,
-                                                                 c->scal.p, c->partials.p);
+    // capture one chunk of iterations (or reuse the caller's): 2 kChunkPairs iterations, 8 with
+    // the multigrid cycle, whose segments take fewer iterations and more kernels each
+    ChunkGraph local;
+    ChunkGraph &cg = keep ? *keep : local;
+    const int chunk_iters = amg ? 8 : 2 * kChunkPairs;
+    if (!cg.exec) {
+        LMTG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        const uint64_t launches0 = c->launches;
+        for (int k = 0; k < chunk_iters; ++k) {
+            k_pcg_dir<T, VS><<<node_grid(c), kRowThreads, 0, s>>>(z, p0, c->nn, c->scal.p);
+            launch_pcg_spmv<T, VS>(c, K, p0, q, s);
+            if constexpr (std::is_same<T, float>::value) {
+                if (amg) {
+                    k_pcg_update_amg<<<node_grid(c), kRowThreads, 0, s>>>(x, r, p0, q, Dinv, amg_xa0(c), amg_omega0(c),
+                                                                          c->nn, c->scal.p, c->partials.p);
+                    amg_launch_cycle(c, r, z, s, 0, 0.0);
+                    continue;
+                }
+            }
+            k_pcg_update<T, VS><<<node_grid(c), kRowThreads, 0, s>>>(x, r, z, p0, q, Dinv, c->nn,
+                                                                     c->scal.p, c->partials.p);
+        }
+        // kernels of one chunk (the cycle's launches were counted while capturing)
+        cg.launches = 3 * chunk_iters + (c->launches - launches0);
+        c->launches = launches0;
+        cudaError_t ce = cudaStreamEndCapture(s, &cg.graph);
+        if (ce != cudaSuccess) throw Error{LMTG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce)};
+        ce = cudaGraphInstantiate(&cg.exec, cg.graph, 0);
+        if (ce != cudaSuccess) throw Error{LMTG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce)};
     }
-    cudaError_t ce = cudaStreamEndCapture(s, &graph);
-    if (ce != cudaSuccess) throw Error{LMTG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce)};
-    ce = cudaGraphInstantiate(&exec, graph, 0);
-    if (ce != cudaSuccess) {
-        cudaGraphDestroy(graph);
-        throw Error{LMTG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce)};
-    }
+    cudaGraphExec_t exec = cg.exec;
     int status = LMTG_OK;
-    const int max_chunks = maxit / (2 * kChunkPairs) + 2;
+    const int max_chunks = maxit / chunk_iters + 2;
     bool finished = false;
     // check the initial test before the first chunk
     LMTG_CUDA(cudaMemcpyAsync(c->h_scal, c->scal.p, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
     LMTG_CUDA(cudaStreamSynchronize(s));
     if (c->h_scal[0].done) finished = true;
     for (int ch = 0; ch < max_chunks && !finished; ++ch) {
-        ce = cudaGraphLaunch(exec, s);
-        c->launches += 6 * kChunkPairs;
+        cudaError_t ce = cudaGraphLaunch(exec, s);
+        c->launches += cg.launches;
         if (ce == cudaSuccess)
             ce = cudaMemcpyAsync(c->h_scal, c->scal.p, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s);
         if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
-        if (ce != cudaSuccess) {
-            cudaGraphExecDestroy(exec);
-            cudaGraphDestroy(graph);
-            throw Error{LMTG_ERR_CUDA, std::string("pcg chunk: ") + cudaGetErrorString(ce)};
-        }
+        if (ce != cudaSuccess) throw Error{LMTG_ERR_CUDA, std::string("pcg chunk: ") + cudaGetErrorString(ce)};
         if (c->h_scal[0].done) finished = true;
         else if (use_deadline && std::chrono::steady_clock::now() > deadline) {
             status = LMTG_ERR_TIMEOUT;
             break;
         }
     }
-    cudaGraphExecDestroy(exec);
-    cudaGraphDestroy(graph);
     *iters = c->h_scal[0].iter;
     if (status == LMTG_OK) status = finished ? c->h_scal[0].status : LMTG_ERR_NOT_CONVERGED;
     return status;
@@ -281,6 +403,8 @@ int solve_mixed(lmtg_ctx *c, double tol, int maxit, double timeout_s, lmtg_solve
           *pa = c->w32[4].p, *pb = c->w32[5].p;
     float *q32 = reinterpret_cast<float *>(c->w64[1].p);  // FP64 buffer reused as FP32 q
     const double bb = dot64(c, Fb, Fb);
+    const bool amg = amg_prepare(c);
+    ChunkGraph chunk;  // captured at the first segment, replayed by the others
     const double kDelta = c->inner_reduction;  // recursive-residual reduction per segment
     int total = 0, outer = 0, status = LMTG_OK;
     double rel = 0, s_prev = 0, rz_prev = 0, rel_prev = 0;
@@ -316,7 +440,7 @@ int solve_mixed(lmtg_ctx *c, double tol, int maxit, double timeout_s, lmtg_solve
         int it = 0;
         int s2 = run_pcg<float>(c, c->K32.p, c->Dinv32.p, b32, d32, r32, z32, pa, pb, q32, true,
                                 LMTG_CRIT_REL_RESIDUAL, eta, maxit - total, 1.0, deadline,
-                                timeout_s > 0, &it, beta_den);
+                                timeout_s > 0, &it, beta_den, amg, &chunk);
         total += it;
         ++outer;
         if (s2 == LMTG_ERR_NAN || s2 == LMTG_ERR_TIMEOUT) {
@@ -326,7 +450,9 @@ int solve_mixed(lmtg_ctx *c, double tol, int maxit, double timeout_s, lmtg_solve
         // the latest direction stays in pa for the next segment
         // the continued recurrence needs r.z from before the segment's last update:
         // beta_k = rz_{k+1} / rz_k, so rz_k = rz / beta of the final scalars
-        rz_prev = c->h_scal[0].beta != 0.0 ? c->h_scal[0].rz / c->h_scal[0].beta : 0.0;
+        // (with the multigrid cycle the last update skips the cycle, so rz is still rz_k)
+        if (amg) rz_prev = c->h_scal[0].rz;
+        else rz_prev = c->h_scal[0].beta != 0.0 ? c->h_scal[0].rz / c->h_scal[0].beta : 0.0;
         s_prev = sc;
         rel_prev = rel;
         have_dir = it > 0 && rz_prev > 0.0;

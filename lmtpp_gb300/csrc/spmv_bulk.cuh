@@ -120,10 +120,31 @@ constexpr size_t bulk_smem_bytes() {
     return (size_t)kStages * BulkStage<kCap>::kBytes;
 }
 
-template <int kStages, int kCap, int kCons, bool kEvictFirst, int kMinBlocks>
+// Row epilogues of the bulk-copy SpMV.  row() receives the row sums in the reduce_scatter3
+// layout (lane 8c holds component c of row I; every lane of the warp calls it) and may add to
+// the thread's partial `acc`; with kReduce the partials are reduced over the grid on ticket()
+// and final() runs once with the total.
+//   EpiPcg   q = K p and p.q -> pq, alpha (the PCG's SpMV)
+struct EpiPcg {
+    float *q;
+    static constexpr bool kReduce = true;
+    __device__ __forceinline__ void row(uint64_t I, float qi, int lane, const float *__restrict__ p, float &acc) const {
+        if ((lane & 7) == 0 && lane < 24) {
+            q[3 * I + (lane >> 3)] = qi;
+            acc = fmaf(p[4 * I + (lane >> 3)], qi, acc);
+        }
+    }
+    __device__ static unsigned *ticket(PcgScalars *S) { return &S->cnt_a; }
+    __device__ void final(PcgScalars *S, double v) const {
+        S->pq = v;
+        S->alpha = S->rz / (v + (v == 0.0 ? 1.0 : 0.0));
+    }
+};
+
+template <int kStages, int kCap, int kCons, bool kEvictFirst, int kMinBlocks, class Epi = EpiPcg>
 __global__ void __launch_bounds__(bulk_threads<kCons>(), kMinBlocks)
     k_pcg_spmv_bulk(const uint32_t *__restrict__ bptr, const uint32_t *__restrict__ bcol,
-                    const float *__restrict__ K, const float *__restrict__ p, float *__restrict__ q,
+                    const float *__restrict__ K, const float *__restrict__ p, Epi epi,
                     uint64_t nn, PcgScalars *S, double *partials) {
     constexpr int VS = 4;
     constexpr int kBulkConsumers = kCons, kBulkStageRows = 2 * kCons;
@@ -223,12 +244,7 @@ __global__ void __launch_bounds__(bulk_threads<kCons>(), kMinBlocks)
     } else {
         // ---------------- consumers ----------------
         auto xnode = [&](uint64_t J, float &a, float &b, float &c) { NodeVec<float, VS>::load(p, J, a, b, c); };
-        auto finish = [&](uint64_t I, float qi) {
-            if ((lane & 7) == 0 && lane < 24) {
-                q[3 * I + (lane >> 3)] = qi;
-                acc = fmaf(p[VS * I + (lane >> 3)], qi, acc);
-            }
-        };
+        auto finish = [&](uint64_t I, float qi) { epi.row(I, qi, lane, p, acc); };
         for (uint32_t k = 0;; ++k) {
             const int slot = k % kStages;
             const bool ok = bulk::mbar_wait(&full[slot], (k / kStages) & 1u);  // every lane acquires
@@ -360,11 +376,10 @@ __global__ void __launch_bounds__(bulk_threads<kCons>(), kMinBlocks)
         }
     }
     __syncthreads();
-    const float tacc[1] = {acc};
-    double out[1];
-    if (grid_reduce_t<1, 0u>(tacc, partials, &S->cnt_a, out) && threadIdx.x == 0) {
-        S->pq = out[0];
-        S->alpha = S->rz / (out[0] + (out[0] == 0.0 ? 1.0 : 0.0));
+    if constexpr (Epi::kReduce) {
+        const float tacc[1] = {acc};
+        double out[1];
+        if (grid_reduce_t<1, 0u>(tacc, partials, Epi::ticket(S), out) && threadIdx.x == 0) epi.final(S, out[0]);
     }
 }
 
