@@ -213,7 +213,11 @@ def timed_steps(f, mode, tol, steps, torch, stream):
     torch.cuda.synchronize()
     n0 = f.launch_count()
     ev0.record(stream)
-    stats = [one_solve(f, mode, tol) for _ in range(steps)]
+    stats = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        stats.append(one_solve(f, mode, tol))
+        stats[-1]["step_wall_ms"] = (time.perf_counter() - t0) * 1e3
     ev1.record(stream)
     ev1.synchronize()
     torch.cuda.synchronize()
@@ -255,6 +259,8 @@ def run_gpu(args, rank, world, local, barrier, allmax):
     ms_m = allmax(ms_m)
     err_final = rel_err(f.get_result(), u_ref)
     res = {"ms_mixed": ms_m, "tol_mixed": tol_m, "err_mixed": err_final, "stats_mixed": stats_m[-1],
+           "steps_mixed": [{"wall_ms": s["step_wall_ms"], "solve_device_ms": s["device_ms"],
+                            "iterations": s["iterations"]} for s in stats_m],
            "launches": launches, "clocks": clk.summary(), "ref_stats": st_ref}
     if not args.no_fp64:
         ms_d, stats_d, _ = timed_steps(f, "fp64", tol_d, 1, torch, stream)
@@ -264,6 +270,7 @@ def run_gpu(args, rank, world, local, barrier, allmax):
     one_solve(f, "mixed", tol_m)
     spmv32_ms, upd32_ms = f.profile_pcg_kernels(precision=1, iters=30)
     spmv64_ms, upd64_ms = f.profile_pcg_kernels(precision=0, iters=10)
+    res.update(spmv_info=f.spmv_info(), amg=f.amg_info(), amg_stage_ms=f.profile_amg_kernels(iters=20))
     from lmtpp_gb300 import abi as _abi
     nn_, ne_, n_, nnzb = (ctypes.c_uint64() for _ in range(4))
     f._lib.lmtg_get_sizes(f._ctx, ctypes.byref(nn_), ctypes.byref(ne_), ctypes.byref(n_), ctypes.byref(nnzb))
@@ -377,8 +384,35 @@ def cpu_desc(s, full):
 SPMV32_KERNEL = {"hexa8": "k_pcg_spmv_bulk<2, 512, 8, 1, 4>", "tetra10": "k_pcg_spmv_bulk<2, 512, 8, 1, 5>"}
 SPMV32_TRAFFIC_RATIO = {"hexa8": (293.261824 + 4.431616) / 296.350284,
                         "tetra10": (132.940032 + 3.373312) / 134.148172}
+# the same ratio for the multigrid's level-0 residual and smoothing launches (ncu captures below)
+STAGE_TRAFFIC_RATIO = {}
 
 METRIC = "time-to-solution at 1e-10 rel. error vs FP64 oracle, mixed vs FP64 CG; asm GB/s"
+
+# Level-0 stages of one multigrid-preconditioned FP32 iteration and their algorithmic bytes per
+# launch (nn nodes, nnzb 3x3 blocks; FP32 values, u32 indices, vectors gathered as 16-byte nodes):
+#   the three bulk-copy SpMVs stream K32 + columns + row pointers and gather one vector (base),
+#   smoothing reads r and D^-1 (36 B per node) and writes z, the residual reads r and writes res.
+STAGE_KERNEL = {"spmv": "EpiPcg", "residual0": "EpiRes", "smooth0": "EpiPost"}
+
+
+def stage_bytes(nn, nnzb, amg=None):
+    base = nnzb * 40 + 4 * (nn + 1) + 16 * nn
+    b = {"direction": 48 * nn, "spmv": base + 12 * nn, "update": 128 * nn, "residual0": base + 24 * nn,
+         "restrict0": 88 * nn, "prolong0": 108 * nn, "smooth0": base + 64 * nn}
+    coarse = 0
+    if amg and amg.get("levels", 0) > 1:
+        nl = amg["levels"]
+        for l in range(1, nl):
+            n6 = amg["ndof"][l] // 6
+            if l == nl - 1:
+                coarse += 4 * amg["ndof"][l] ** 2 + 8 * amg["ndof"][l]  # dense inverse and vectors
+            else:
+                # two 6x6-block passes (residual, smoothing: 144 B values + 4 B column per block),
+                # block-Jacobi, restriction and prolongation vectors
+                coarse += 2 * (148 * amg["nnz_blocks"][l] + 4 * (n6 + 1)) + 400 * n6
+    b["coarse"] = coarse
+    return b
 
 
 def workload_config(args):
@@ -704,6 +738,7 @@ def main():
         "gpu_launches": r["launches"],
         "clocks": r["clocks"],
         "rel_err": r["err_mixed"], "tol_mixed": r["tol_mixed"], "iters_mixed": r["stats_mixed"],
+        "steps_mixed": r["steps_mixed"],
         "fp64_pcg_s": r.get("ms_fp64", float("nan")) * 1e-3, "fp64_tol": r.get("tol_fp64"),
         "fp64_rel_err": r.get("err_fp64"), "iters_fp64": r.get("stats_fp64"),
         "mixed_speedup_vs_fp64": (r["ms_fp64"] / r["ms_mixed"]) if "ms_fp64" in r else None,
@@ -711,8 +746,28 @@ def main():
         "asm": {"ms": r["asm_ms"], "gather_bytes": asm_bytes,
                 "GB/s_incl_element_kernel": asm_bytes / (r["asm_ms"] * 1e-3) / 1e9},
         "oracle_solve": r["ref_stats"],
-        "spmv_kind": r.get("spmv_kind"),
+        "spmv_kind": r["spmv_info"]["kind"], "spmv_autotune_ms": r["spmv_info"]["tune_ms"],
+        "amg": r["amg"],
     }
+    st_ms = r["amg_stage_ms"]
+    if any(st_ms.values()):
+        sb = stage_bytes(r["nn"], r["nnzb"], r["amg"])
+        inst = "2, 512, 8, 1, %d" % (5 if r["spmv_info"]["kind"] == 2 else 4)
+        stages = {k: {"ms": st_ms[k], "algorithmic_bytes": sb[k],
+                      "GB/s": sb[k] / (st_ms[k] * 1e-3) / 1e9 if st_ms[k] > 0 else None} for k in st_ms}
+        it_ms, it_b = sum(st_ms.values()), sum(sb.values())
+        dom = max(STAGE_KERNEL, key=lambda k: st_ms[k])
+        achd = sb[dom] / (st_ms[dom] * 1e-3) / 1e9
+        line["roofline"] = {
+            "bound": "hbm", "kernel": "k_pcg_spmv_bulk<%s, %s>" % (inst, STAGE_KERNEL[dom]), "achieved": achd,
+            "peak": hbm, "unit": "GB/s", "frac": achd / hbm,
+            "traffic": sb[dom] * STAGE_TRAFFIC_RATIO.get((args.elem, dom), SPMV32_TRAFFIC_RATIO[args.elem]),
+            "traffic_source": "ncu dram bytes of a %s capture of this kernel scaled by the block count"
+                              % ("64^3" if args.elem == "hexa8" else "24^3"),
+            "peak_source": peak_note, "algorithmic_bytes": sb[dom], "launch_ms": st_ms[dom],
+            "pcg_spmv": line["roofline"]}
+        line["iteration"] = {"ms": it_ms, "algorithmic_bytes": it_b, "GB/s": it_b / (it_ms * 1e-3) / 1e9,
+                             "frac": it_b / (it_ms * 1e-3) / 1e9 / hbm, "stages": stages}
     if world == 1 and not args.no_extras:
         line["extra"] = run_extras(args)
     print(json.dumps(line), flush=True)
@@ -755,7 +810,8 @@ def run_extras(args):
                 "spmv32": {"kernel": SPMV32_KERNEL["tetra10"], "launch_ms": r["spmv32_ms"],
                            "GB/s": b32 / (r["spmv32_ms"] * 1e-3) / 1e9,
                            "frac": b32 / (r["spmv32_ms"] * 1e-3) / 1e9 / hbm},
-                "spmv_kind": r.get("spmv_kind")}
+                "spmv_kind": r["spmv_info"]["kind"], "spmv_autotune_ms": r["spmv_info"]["tune_ms"],
+                "amg": r["amg"], "amg_stage_ms": r["amg_stage_ms"]}
 
     def adjoint():
         a = copy.copy(args)

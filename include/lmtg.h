@@ -386,9 +386,22 @@ int lmtg_recalage_assemble(lmtg_ctx *ctx);
 int lmtg_set_preconditioner(lmtg_ctx *ctx, int kind);
 /* The multigrid hierarchy built for the last mixed solve (levels = 0 when none): per level
  * (up to 8) unknowns, stored blocks, damped-Jacobi weight and lambda_max(D^-1 K); the host time
- * of the structure setup and of the last numeric setup.  Any output may be NULL. */
+ * of the structure setup, of the last numeric setup, and of the structure setup's phases
+ * (pattern copy and rigid-body modes, aggregation, tentative prolongators, coarse patterns and
+ * gather lists, uploads).  Any output may be NULL. */
 int lmtg_amg_info(lmtg_ctx *ctx, int *levels, uint64_t ndof[8], uint64_t nnz_blocks[8], double omega[8],
-                  double lambda_max[8], double *structure_ms, double *numeric_ms);
+                  double lambda_max[8], double *structure_ms, double *numeric_ms, double structure_phase_ms[5]);
+
+/* FP32 SpMV kind in use for this context's solves (0 warp-row, 1 / 2 bulk copies with 4 / 5 CTAs
+ * per SM), the autotuned kind (-1 before the first FP32 solve of the pattern, or when
+ * lmtg_set_spmv_kind pinned one) and the autotuner's per-kind launch times (ms, 0 = not timed). */
+int lmtg_spmv_info(lmtg_ctx *ctx, int *kind_in_use, int *tuned, double tune_ms[3]);
+/* Device time (ms, CUDA events) of each stage of one multigrid-preconditioned FP32 iteration,
+ * averaged over `iters` iterations on the assembled system: [0] SpMV q = K p, [1] update with
+ * the first smoothing step, [2] level-0 residual, [3] restriction, [4] coarse levels, [5]
+ * prolongation, [6] level-0 smoothing forming z, [7] direction update.  All 0 without a
+ * hierarchy. */
+int lmtg_profile_amg_kernels(lmtg_ctx *ctx, int iters, double ms[8]);
 
 /* Sizes of the current problem. */
 int lmtg_get_sizes(lmtg_ctx *ctx, uint64_t *nn, uint64_t *ne, uint64_t *ndof, uint64_t *nnz_blocks);

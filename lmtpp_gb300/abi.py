@@ -66,7 +66,9 @@ _SIGS = {
     "lmtg_get_sizes": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "lmtg_recalage_setup": (_i, [_vp, _d, _d, _d, _d, _vp, _vp]),
     "lmtg_set_preconditioner": (_i, [_vp, _i]),
-    "lmtg_amg_info": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "lmtg_amg_info": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "lmtg_spmv_info": (_i, [_vp, _vp, _vp, _vp]),
+    "lmtg_profile_amg_kernels": (_i, [_vp, _i, _vp]),
     "lmtg_recalage_assemble": (_i, [_vp]),
     "lmtg_get_launch_count": (_i, [_vp, ctypes.POINTER(_u64)]),
     "lmtg_make_rect_triangle6": (_i, [_vp, _vp, _vp, ctypes.POINTER(_u64), ctypes.POINTER(_u64), _vp, _vp]),

@@ -510,6 +510,26 @@ int lmtg_set_spmv_kind(lmtg_ctx *c, int kind) {
     return guard(c, [&] {
         LMTG_CHECK(kind >= -1 && kind <= 2, LMTG_ERR_ARG, "spmv kind in -1..2");
         c->spmv_kind = kind;
+        if (kind == -1) c->spmv_tuned = -1;  // tune again at the next FP32 solve
+        return LMTG_OK;
+    });
+}
+
+int lmtg_spmv_info(lmtg_ctx *c, int *kind_in_use, int *tuned, double tune_ms[3]) {
+    return guard(c, [&] {
+        if (kind_in_use) *kind_in_use = spmv_kind_in_use(c);
+        if (tuned) *tuned = c->spmv_tuned;
+        if (tune_ms)
+            for (int k = 0; k < 3; ++k) tune_ms[k] = c->spmv_tune_ms[k];
+        return LMTG_OK;
+    });
+}
+
+int lmtg_profile_amg_kernels(lmtg_ctx *c, int iters, double ms[8]) {
+    return guard(c, [&] {
+        LMTG_CHECK(ms && iters > 0, LMTG_ERR_ARG, "bad arguments");
+        LMTG_CHECK(c->have_vec && c->have32, LMTG_ERR_STATE, "assemble the system (FP32 matrix) first");
+        profile_amg(c, iters, ms);
         return LMTG_OK;
     });
 }
@@ -523,9 +543,9 @@ int lmtg_set_preconditioner(lmtg_ctx *c, int kind) {
 }
 
 int lmtg_amg_info(lmtg_ctx *c, int *levels, uint64_t *ndof, uint64_t *nnz_blocks, double *omega,
-                  double *lambda_max, double *structure_ms, double *numeric_ms) {
+                  double *lambda_max, double *structure_ms, double *numeric_ms, double *structure_phase_ms) {
     return guard(c, [&] {
-        amg_info(c, levels, ndof, nnz_blocks, omega, lambda_max, structure_ms, numeric_ms);
+        amg_info(c, levels, ndof, nnz_blocks, omega, lambda_max, structure_ms, numeric_ms, structure_phase_ms);
         return LMTG_OK;
     });
 }
@@ -550,6 +570,8 @@ int lmtg_allocate_matrices(lmtg_ctx *c, uint64_t *nnz_lower) {
         LMTG_CHECK(c->nnu == 3, LMTG_ERR_STATE, "elasticity call on a diffusion context");
         amg_free(c);
         build_pattern(c);
+        c->spmv_tuned = -1;
+        c->spmv_setup_kind = -2;
         c->Ke64.alloc(c->ne * (uint64_t)c->npairs * 9);
         c->K64.alloc(c->nnzb * 9);
         c->K32.alloc(c->nnzb * 9 + 4);  // 16 bytes of slack: bulk copies round their end up

@@ -18,12 +18,12 @@
 //             FP64); a mode that the aggregate cannot carry (one node, or nodes on a line) gives a
 //             zero column, and the coarse unknown it would define is a decoupled unit diagonal.
 //   K_{l+1}   = Q_l^T K_l Q_l (Galerkin), 6x6 blocks, through gather lists: for every coarse block
-//             the level-l blocks that sum into it, in a fixed order (one thread per coarse block,
+//             the level-l blocks that sum into it, in a fixed order (one warp per coarse block,
 //             no atomics, deterministic).
 //   coarsest  (<= 300 unknowns): a dense inverse, computed on the host in FP64, applied in FP32.
 // Numeric setup after every matrix assembly: the Galerkin products, the 6x6 block-Jacobi
 // inverses, and per level the damped-Jacobi weight omega = 1.6 / lambda_max(D^-1 K) (lambda_max by
-// ten power steps; the weight of a degree-1 Chebyshev smoother on [lambda/30, 1.1 lambda]).
+// eight power steps; the weight of a degree-1 Chebyshev smoother on [lambda/30, 1.1 lambda]).
 //
 // V-cycle (z = M r), per level: x = omega D^-1 r; res = r - K x; restrict Q^T res; recurse;
 // x += Q e; x' = x + omega D^-1 (r - K x).  The same smoother before and after makes M symmetric,
@@ -65,21 +65,24 @@ __device__ __forceinline__ bool done(const PcgScalars *S) { return S && *(volati
 // numeric setup kernels
 // ---------------------------------------------------------------------------------------------
 
-// Coarse block (I, J) = sum over its gather list of Q_i^T K_ij Q_j.  One thread per coarse block;
-// g[2e] = fine block index, g[2e+1] = its fine row.  A coarse diagonal entry that sums to exactly
+// Coarse block (I, J) = sum over its gather list of Q_i^T K_ij Q_j.  One warp per coarse block,
+// its lanes over the list (g[2e] = fine block index, g[2e+1] = its fine row), then a butterfly sum
+// of the 36 values (fixed order: deterministic).  A coarse diagonal entry that sums to exactly
 // zero (a mode the aggregate cannot carry) becomes 1, a decoupled unknown.
 template <int B>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(256)
     k_galerkin(const uint32_t *__restrict__ fbptr, const uint32_t *__restrict__ fbcol, const float *__restrict__ fK,
                const float *__restrict__ Q, const uint32_t *__restrict__ cbptr, const uint32_t *__restrict__ cbcol,
                uint64_t cnn, const uint32_t *__restrict__ gptr, const uint32_t *__restrict__ gsrc,
                float *__restrict__ cK) {
     const uint64_t nb = cbptr[cnn];
-    for (uint64_t cb = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; cb < nb; cb += (uint64_t)gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t cb = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; cb < nb; cb += nw) {
         float C[36];
 #pragma unroll
         for (int v = 0; v < 36; ++v) C[v] = 0.f;
-        for (uint32_t e = gptr[cb]; e < gptr[cb + 1]; ++e) {
+        for (uint32_t e = gptr[cb] + lane; e < gptr[cb + 1]; e += 32) {
             const uint32_t k = gsrc[2 * (uint64_t)e], i = gsrc[2 * (uint64_t)e + 1];
             const uint32_t rb = fbptr[i], deg = fbptr[i + 1] - rb, j = fbcol[k];
             float A[B * B];
@@ -107,6 +110,8 @@ __global__ void __launch_bounds__(128)
                     for (int c = 0; c < 6; ++c) C[a * 6 + c] = fmaf(q[a], T[r * 6 + c], C[a * 6 + c]);
             }
         }
+#pragma unroll
+        for (int v = 0; v < 36; ++v) C[v] = warp_sum(C[v]);
         // row of this coarse block (binary search on cbptr) to place it in the planar layout
         uint64_t lo = 0, hi = cnn;
         while (hi - lo > 1) {
@@ -119,8 +124,14 @@ __global__ void __launch_bounds__(128)
 #pragma unroll
             for (int a = 0; a < 6; ++a)
                 if (C[a * 7] == 0.f) C[a * 7] = 1.f;
+        // lane v writes value v (and lanes 0..3 also value 32 + lane)
+        float mine = C[0], extra = C[32];
 #pragma unroll
-        for (int v = 0; v < 36; ++v) cK[kidx6(rb, deg, (uint32_t)(cb - rb), v)] = C[v];
+        for (int v = 1; v < 32; ++v) mine = lane == v ? C[v] : mine;
+#pragma unroll
+        for (int v = 33; v < 36; ++v) extra = lane == v - 32 ? C[v] : extra;
+        cK[kidx6(rb, deg, (uint32_t)(cb - rb), lane)] = mine;
+        if (lane < 4) cK[kidx6(rb, deg, (uint32_t)(cb - rb), 32 + lane)] = extra;
     }
 }
 
@@ -473,6 +484,27 @@ struct EpiPost {
     }
 };
 
+//   EpiPower w = D^-1 K v, |w|^2 reduced into out (a power step for lambda_max; runs on the outer
+//            scalar slot, whose `done` stays 0)
+struct EpiPower {
+    const float *D;
+    float *w;
+    double *out;
+    static constexpr bool kReduce = true;
+    __device__ __forceinline__ void row(uint64_t I, float qi, int lane, const float *, float &acc) const {
+        const float v0 = __shfl_sync(0xffffffffu, qi, 0), v1 = __shfl_sync(0xffffffffu, qi, 8),
+                    v2 = __shfl_sync(0xffffffffu, qi, 16);
+        if (lane < 3) {
+            const float *Dr = D + 9 * I + 3 * lane;
+            const float wc = Dr[0] * v0 + Dr[1] * v1 + Dr[2] * v2;
+            w[4 * I + lane] = wc;
+            acc = fmaf(wc, wc, acc);
+        }
+    }
+    __device__ static unsigned *ticket(PcgScalars *S) { return &S->cnt_d; }
+    __device__ void final(PcgScalars *, double v) const { *out = v; }
+};
+
 // one instance of the bulk kernel per (stage shape, epilogue); its resident grid is set up once
 template <int kSt, int kCap, int kCons, bool kEF, int kMinB, class Epi>
 struct Bulk0 {
@@ -489,43 +521,82 @@ struct Bulk0 {
         LMTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, bulk_threads<kCons>(), smem));
         grid() = c->sm_count * (nb > 0 ? nb : 1);
     }
-    static void launch(lmtg_ctx *c, const float *x, Epi epi, cudaStream_t s) {
+    static void launch(lmtg_ctx *c, const float *x, Epi epi, cudaStream_t s, PcgScalars *S) {
         k_pcg_spmv_bulk<kSt, kCap, kCons, kEF, kMinB, Epi><<<grid(), bulk_threads<kCons>(), bulk_smem_bytes<kSt, kCap>(), s>>>(
-            c->bptr.p, c->bcol.p, c->K32.p, x, epi, c->nn, c->scal.p, c->partials.p);
+            c->bptr.p, c->bcol.p, c->K32.p, x, epi, c->nn, S, c->partials.p);
     }
 };
 // the shapes of the PCG's own SpMV: 4 CTAs per SM for rows of <= 32 blocks, 5 for wider rows
 template <class Epi> using Bulk0N = Bulk0<2, 512, 8, true, 4, Epi>;
 template <class Epi> using Bulk0W = Bulk0<2, 512, 8, true, 5, Epi>;
 
-template <class Epi>
-static void bulk0_launch(lmtg_ctx *c, const float *x, Epi epi, cudaStream_t s) {
-    if (c->max_row_blocks > 32) Bulk0W<Epi>::launch(c, x, epi, s);
-    else Bulk0N<Epi>::launch(c, x, epi, s);
-}
-
+// the level-0 residual / smoothing products follow the PCG's SpMV kind (1: 4 CTAs per SM,
+// 2: 5, 0: the warp-row kernels k_amg_res<3> / k_amg_post<3>); set up outside graph capture
 static void bulk0_setup(lmtg_ctx *c) {
-    if (c->max_row_blocks > 32) {
-        Bulk0W<EpiRes>::setup(c);
-        Bulk0W<EpiPost>::setup(c);
-    } else {
+    const int kind = spmv_kind_in_use(c);
+    if (kind == 1) {
         Bulk0N<EpiRes>::setup(c);
         Bulk0N<EpiPost>::setup(c);
+        Bulk0N<EpiPower>::setup(c);
+    } else if (kind == 2) {
+        Bulk0W<EpiRes>::setup(c);
+        Bulk0W<EpiPost>::setup(c);
+        Bulk0W<EpiPower>::setup(c);
     }
+}
+
+template <class Epi>
+static void bulk0_launch(lmtg_ctx *c, const float *x, Epi epi, cudaStream_t s, PcgScalars *S = nullptr) {
+    if (!S) S = c->scal.p;
+    if (spmv_kind_in_use(c) == 2) Bulk0W<Epi>::launch(c, x, epi, s, S);
+    else Bulk0N<Epi>::launch(c, x, epi, s, S);
 }
 
 // ---------------------------------------------------------------------------------------------
 // host structure setup
 // ---------------------------------------------------------------------------------------------
 
+// Host array without value-initialisation (the buffers here are filled completely, or only
+// their filled part is read).
+template <class T>
+struct HBuf {
+    std::unique_ptr<T[]> p;
+    size_t n = 0;
+    void alloc(size_t k) {
+        p.reset(k ? new T[k] : nullptr);
+        n = k;
+    }
+    T &operator[](size_t i) { return p[i]; }
+    const T &operator[](size_t i) const { return p[i]; }
+    T *data() { return p.get(); }
+    const T *data() const { return p.get(); }
+    size_t size() const { return n; }
+};
+
 struct HostLevel {
     int b = 3;
     uint64_t nn = 0;
-    std::vector<uint32_t> bptr, bcol, bdiag;  // level pattern (levels >= 1; level 0 from the device)
+    std::vector<uint32_t> bptr, bdiag;  // level pattern (level 0: copied from the device)
+    HBuf<uint32_t> bcol;
 };
 
+static unsigned host_threads() { return std::max(1u, std::min(16u, std::thread::hardware_concurrency())); }
+
+// runs f(a0, a1) on contiguous ranges of [0, n) in parallel
+template <class F>
+static void parallel_ranges(uint64_t n, F f) {
+    const unsigned nt = host_threads();
+    const uint64_t per = (n + nt - 1) / nt;
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < nt; ++t) {
+        const uint64_t a0 = t * per, a1 = std::min<uint64_t>(n, a0 + per);
+        if (a0 < a1) th.emplace_back(f, a0, a1, t);
+    }
+    for (auto &t : th) t.join();
+}
+
 // standard aggregation of a node graph; skip[i] = node left out
-static uint64_t aggregate(uint64_t nn, const std::vector<uint32_t> &bptr, const std::vector<uint32_t> &bcol,
+static uint64_t aggregate(uint64_t nn, const std::vector<uint32_t> &bptr, const HBuf<uint32_t> &bcol,
                           const std::vector<uint8_t> &skip, std::vector<uint32_t> &agg) {
     agg.assign(nn, kNone);
     const uint32_t kFree = kNone, kSkip = kNone - 1;
@@ -582,25 +653,20 @@ static uint64_t aggregate(uint64_t nn, const std::vector<uint32_t> &bptr, const 
     return na;
 }
 
-// Tentative prolongator of one level: Q (nn x b x 6, row-major per node) and the coarse modes
-// Bc (na x 6 x 6) from the level's modes Bf (nn x b x 6), orthonormalised per aggregate.
-static void tentative(int b, uint64_t nn, uint64_t na, const std::vector<uint32_t> &aptr,
-                      const std::vector<uint32_t> &anode, const std::vector<double> &Bf, std::vector<float> &Q,
-                      std::vector<double> &Bc) {
-    Q.assign(nn * b * 6, 0.f);
+// Tentative prolongator of one level: Q (b x 6 per aggregated node, row-major) and the coarse
+// modes Bc (na x 6 x 6), from the level's modes mode(i, m) -> the b x 6 block of node i in m,
+// orthonormalised per aggregate.
+template <class ModeF>
+static void tentative(int b, uint64_t na, const std::vector<uint32_t> &aptr, const std::vector<uint32_t> &anode,
+                      ModeF mode, HBuf<float> &Q, std::vector<double> &Bc) {
     Bc.assign(na * 36, 0.0);
-    const unsigned nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-    auto work = [&](uint64_t a0, uint64_t a1) {
+    parallel_ranges(na, [&](uint64_t a0, uint64_t a1, unsigned) {
         std::vector<double> M;
         for (uint64_t a = a0; a < a1; ++a) {
             const uint32_t n0 = aptr[a], m = aptr[a + 1] - n0;
             const size_t rows = (size_t)m * b;
-            M.assign(rows * 6, 0.0);
-            for (uint32_t t = 0; t < m; ++t) {
-                const uint32_t i = anode[n0 + t];
-                for (int r = 0; r < b; ++r)
-                    for (int c = 0; c < 6; ++c) M[((size_t)t * b + r) * 6 + c] = Bf[((size_t)i * b + r) * 6 + c];
-            }
+            M.resize(rows * 6);
+            for (uint32_t t = 0; t < m; ++t) mode(anode[n0 + t], &M[(size_t)t * b * 6]);
             double R[6][6] = {{0}};
             double norm0[6];
             for (int c = 0; c < 6; ++c) {
@@ -635,60 +701,57 @@ static void tentative(int b, uint64_t nn, uint64_t na, const std::vector<uint32_
             for (int r = 0; r < 6; ++r)
                 for (int c = 0; c < 6; ++c) Bc[a * 36 + r * 6 + c] = R[r][c];
         }
-    };
-    std::vector<std::thread> th;
-    const uint64_t per = (na + nt - 1) / nt;
-    for (unsigned t = 0; t < nt; ++t) {
-        const uint64_t a0 = t * per, a1 = std::min<uint64_t>(na, a0 + per);
-        if (a0 < a1) th.emplace_back(work, a0, a1);
-    }
-    for (auto &t : th) t.join();
+    });
 }
 
 // Coarse pattern (sorted distinct aggregate columns per aggregate row) and the Galerkin gather
 // lists (fine block, fine row) per coarse block, in the order aggregate nodes x row blocks.
 static void coarse_pattern(uint64_t na, const std::vector<uint32_t> &aptr, const std::vector<uint32_t> &anode,
-                           const std::vector<uint32_t> &fbptr, const std::vector<uint32_t> &fbcol,
-                           const std::vector<uint32_t> &agg, std::vector<uint32_t> &cbptr,
-                           std::vector<uint32_t> &cbcol, std::vector<uint32_t> &cbdiag, std::vector<uint32_t> &gptr,
-                           std::vector<uint32_t> &gsrc) {
-    const unsigned nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-    const uint64_t per = (na + nt - 1) / nt;
+                           const std::vector<uint32_t> &fbptr, const HBuf<uint32_t> &fbcol,
+                           const std::vector<uint32_t> &agg, std::vector<uint32_t> &cbptr, HBuf<uint32_t> &cbcol,
+                           std::vector<uint32_t> &cbdiag, HBuf<uint32_t> &gptr, HBuf<uint32_t> &gsrc) {
+    const unsigned nt = host_threads();
+    // pass 1 (per thread): each aggregate's sorted distinct columns and per-column entry counts
+    struct Arena {
+        std::vector<uint32_t> cols, cnt;
+    };
+    std::vector<Arena> arena(nt);
     std::vector<uint32_t> cdeg(na), cnt(na);
-    // per-aggregate distinct columns, sorted (mark[J] = the last aggregate that listed J)
-    auto distinct = [&](uint64_t a, std::vector<uint32_t> &cols, std::vector<uint32_t> &mark, uint32_t *nent) {
-        cols.clear();
-        uint32_t e = 0;
-        for (uint32_t t = aptr[a]; t < aptr[a + 1]; ++t) {
-            const uint32_t i = anode[t];
-            for (uint32_t k = fbptr[i]; k < fbptr[i + 1]; ++k) {
-                const uint32_t J = agg[fbcol[k]];
-                if (J == kNone) continue;
-                ++e;
-                if (mark[J] != (uint32_t)a) {
-                    mark[J] = (uint32_t)a;
-                    cols.push_back(J);
+    std::vector<uint64_t> aoff(na);
+    parallel_ranges(na, [&](uint64_t a0, uint64_t a1, unsigned t) {
+        Arena &ar = arena[t];
+        std::vector<uint32_t> mark(na, kNone), cols;
+        for (uint64_t a = a0; a < a1; ++a) {
+            cols.clear();
+            uint32_t e = 0;
+            for (uint32_t u = aptr[a]; u < aptr[a + 1]; ++u) {
+                const uint32_t i = anode[u];
+                for (uint32_t k = fbptr[i]; k < fbptr[i + 1]; ++k) {
+                    const uint32_t J = agg[fbcol[k]];
+                    if (J == kNone) continue;
+                    ++e;
+                    if (mark[J] != (uint32_t)a) {
+                        mark[J] = (uint32_t)a;
+                        cols.push_back(J);
+                    }
+                }
+            }
+            std::sort(cols.begin(), cols.end());
+            aoff[a] = ar.cols.size();
+            cdeg[a] = (uint32_t)cols.size();
+            cnt[a] = e;
+            ar.cols.insert(ar.cols.end(), cols.begin(), cols.end());
+            ar.cnt.resize(ar.cols.size(), 0);
+            uint32_t *sc = ar.cnt.data() + aoff[a];
+            for (uint32_t u = aptr[a]; u < aptr[a + 1]; ++u) {
+                const uint32_t i = anode[u];
+                for (uint32_t k = fbptr[i]; k < fbptr[i + 1]; ++k) {
+                    const uint32_t J = agg[fbcol[k]];
+                    if (J != kNone) ++sc[std::lower_bound(cols.begin(), cols.end(), J) - cols.begin()];
                 }
             }
         }
-        std::sort(cols.begin(), cols.end());
-        if (nent) *nent = e;
-    };
-    {
-        std::vector<std::thread> th;
-        for (unsigned t = 0; t < nt; ++t) {
-            const uint64_t a0 = t * per, a1 = std::min<uint64_t>(na, a0 + per);
-            if (a0 >= a1) continue;
-            th.emplace_back([&, a0, a1] {
-                std::vector<uint32_t> cols, mark(na, kNone);
-                for (uint64_t a = a0; a < a1; ++a) {
-                    distinct(a, cols, mark, &cnt[a]);
-                    cdeg[a] = (uint32_t)cols.size();
-                }
-            });
-        }
-        for (auto &t : th) t.join();
-    }
+    });
     cbptr.assign(na + 1, 0);
     std::vector<uint64_t> eoff(na + 1, 0);
     for (uint64_t a = 0; a < na; ++a) {
@@ -696,55 +759,39 @@ static void coarse_pattern(uint64_t na, const std::vector<uint32_t> &aptr, const
         eoff[a + 1] = eoff[a] + cnt[a];
     }
     if (eoff[na] >= (1ull << 32)) throw Error{LMTG_ERR_UNSUPPORTED, "amg: Galerkin lists over 2^32 entries"};
-    cbcol.assign(cbptr[na] + 4, 0);
+    cbcol.alloc(cbptr[na] + 4);
+    for (int k = 0; k < 4; ++k) cbcol[cbptr[na] + k] = 0;
     cbdiag.assign(na, 0);
-    gptr.assign(cbptr[na] + 1, 0);
-    gsrc.assign(2 * eoff[na], 0);
-    std::vector<std::thread> th;
-    for (unsigned t = 0; t < nt; ++t) {
-        const uint64_t a0 = t * per, a1 = std::min<uint64_t>(na, a0 + per);
-        if (a0 >= a1) continue;
-        th.emplace_back([&, a0, a1] {
-            std::vector<uint32_t> cols, slotcnt, slotpos, mark(na, kNone);
-            for (uint64_t a = a0; a < a1; ++a) {
-                distinct(a, cols, mark, nullptr);
-                const uint32_t rb = cbptr[a], deg = (uint32_t)cols.size();
-                for (uint32_t s = 0; s < deg; ++s) {
-                    cbcol[rb + s] = cols[s];
-                    if (cols[s] == a) cbdiag[a] = rb + s;
-                }
-                slotcnt.assign(deg, 0);
-                auto slot_of = [&](uint32_t J) {
-                    return (uint32_t)(std::lower_bound(cols.begin(), cols.end(), J) - cols.begin());
-                };
-                for (uint32_t t2 = aptr[a]; t2 < aptr[a + 1]; ++t2) {
-                    const uint32_t i = anode[t2];
-                    for (uint32_t k = fbptr[i]; k < fbptr[i + 1]; ++k) {
-                        const uint32_t J = agg[fbcol[k]];
-                        if (J != kNone) ++slotcnt[slot_of(J)];
-                    }
-                }
-                slotpos.assign(deg, 0);
-                uint64_t off = eoff[a];
-                for (uint32_t s = 0; s < deg; ++s) {
-                    gptr[rb + s] = (uint32_t)off;
-                    slotpos[s] = (uint32_t)off;
-                    off += slotcnt[s];
-                }
-                for (uint32_t t2 = aptr[a]; t2 < aptr[a + 1]; ++t2) {
-                    const uint32_t i = anode[t2];
-                    for (uint32_t k = fbptr[i]; k < fbptr[i + 1]; ++k) {
-                        const uint32_t J = agg[fbcol[k]];
-                        if (J == kNone) continue;
-                        const uint32_t p = slotpos[slot_of(J)]++;
-                        gsrc[2 * (uint64_t)p] = k;
-                        gsrc[2 * (uint64_t)p + 1] = i;
-                    }
+    gptr.alloc(cbptr[na] + 1);
+    gsrc.alloc(2 * eoff[na]);
+    // pass 2: columns, gather-list offsets and the gather lists themselves
+    parallel_ranges(na, [&](uint64_t a0, uint64_t a1, unsigned t) {
+        const Arena &ar = arena[t];
+        std::vector<uint32_t> slotpos;
+        for (uint64_t a = a0; a < a1; ++a) {
+            const uint32_t *cols = ar.cols.data() + aoff[a], *sc = ar.cnt.data() + aoff[a];
+            const uint32_t rb = cbptr[a], deg = cdeg[a];
+            slotpos.resize(deg);
+            uint64_t off = eoff[a];
+            for (uint32_t u = 0; u < deg; ++u) {
+                cbcol[rb + u] = cols[u];
+                if (cols[u] == a) cbdiag[a] = rb + u;
+                gptr[rb + u] = (uint32_t)off;
+                slotpos[u] = (uint32_t)off;
+                off += sc[u];
+            }
+            for (uint32_t u = aptr[a]; u < aptr[a + 1]; ++u) {
+                const uint32_t i = anode[u];
+                for (uint32_t k = fbptr[i]; k < fbptr[i + 1]; ++k) {
+                    const uint32_t J = agg[fbcol[k]];
+                    if (J == kNone) continue;
+                    const uint32_t p = slotpos[std::lower_bound(cols, cols + deg, J) - cols]++;
+                    gsrc[2 * (uint64_t)p] = k;
+                    gsrc[2 * (uint64_t)p + 1] = i;
                 }
             }
-        });
-    }
-    for (auto &t : th) t.join();
+        }
+    });
     gptr[cbptr[na]] = (uint32_t)eoff[na];
 }
 
@@ -752,6 +799,11 @@ template <class T>
 static void upload(DBuf<T> &d, const std::vector<T> &h, cudaStream_t s) {
     d.alloc(h.size());
     if (!h.empty()) LMTG_CUDA(cudaMemcpyAsync(d.p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+}
+template <class T>
+static void upload(DBuf<T> &d, const HBuf<T> &h, cudaStream_t s) {
+    d.alloc(h.size());
+    if (h.size()) LMTG_CUDA(cudaMemcpyAsync(d.p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s));
 }
 
 }  // namespace
@@ -772,12 +824,18 @@ static void amg_build_structure(lmtg_ctx *c) {
     auto t0 = std::chrono::steady_clock::now();
     cudaStream_t s = c->stream;
     std::unique_ptr<AmgState> A(new AmgState());
+    auto tp = t0;
+    auto phase = [&](int k) {
+        const auto now = std::chrono::steady_clock::now();
+        A->phase_ms[k] += std::chrono::duration<double, std::milli>(now - tp).count();
+        tp = now;
+    };
     // level 0 pattern from the device
     HostLevel cur;
     cur.b = 3;
     cur.nn = c->nn;
     cur.bptr.resize(c->nn + 1);
-    cur.bcol.resize(c->nnzb);
+    cur.bcol.alloc(c->nnzb);
     LMTG_CUDA(cudaMemcpyAsync(cur.bptr.data(), c->bptr.p, 4 * (c->nn + 1), cudaMemcpyDeviceToHost, s));
     LMTG_CUDA(cudaMemcpyAsync(cur.bcol.data(), c->bcol.p, 4 * c->nnzb, cudaMemcpyDeviceToHost, s));
     LMTG_CUDA(cudaStreamSynchronize(s));
@@ -786,28 +844,22 @@ static void amg_build_structure(lmtg_ctx *c) {
     if (c->h_cdof.size() == c->nc)
         for (uint32_t d : c->h_cdof)
             if (d / 3 < c->nn) skip[d / 3] = 1;
-    // rigid-body modes about the mesh centroid (nodes x 3 x 6)
-    std::vector<double> Bf(c->nn * 18, 0.0);
-    {
-        double cen[3] = {0, 0, 0};
-        for (uint64_t i = 0; i < c->nn; ++i)
-            for (int d = 0; d < 3; ++d) cen[d] += c->h_pos[3 * i + d];
-        for (int d = 0; d < 3; ++d) cen[d] /= (double)c->nn;
-        for (uint64_t i = 0; i < c->nn; ++i) {
-            const double x = c->h_pos[3 * i] - cen[0], y = c->h_pos[3 * i + 1] - cen[1], z = c->h_pos[3 * i + 2] - cen[2];
-            double *m = &Bf[i * 18];
-            m[0 * 6 + 0] = 1;
-            m[1 * 6 + 1] = 1;
-            m[2 * 6 + 2] = 1;
-            // rotations about z, x, y: (-y, x, 0), (0, -z, y), (z, 0, -x)
-            m[0 * 6 + 3] = -y;
-            m[1 * 6 + 3] = x;
-            m[1 * 6 + 4] = -z;
-            m[2 * 6 + 4] = y;
-            m[0 * 6 + 5] = z;
-            m[2 * 6 + 5] = -x;
-        }
-    }
+    // level-0 modes: translations and rotations about the mesh centroid, per node
+    double cen[3] = {0, 0, 0};
+    for (uint64_t i = 0; i < c->nn; ++i)
+        for (int d = 0; d < 3; ++d) cen[d] += c->h_pos[3 * i + d];
+    for (int d = 0; d < 3; ++d) cen[d] /= (double)c->nn;
+    const double *hp = c->h_pos.data();
+    auto rigid_modes = [hp, cen](uint32_t i, double *m) {
+        const double x = hp[3 * (size_t)i] - cen[0], y = hp[3 * (size_t)i + 1] - cen[1], z = hp[3 * (size_t)i + 2] - cen[2];
+        // rows x, y, z; columns: translations x, y, z, rotations about z, x, y
+        const double v[18] = {1, 0, 0, -y, 0, z,  //
+                              0, 1, 0, x, -z, 0,  //
+                              0, 0, 1, 0, y, -x};
+        std::memcpy(m, v, sizeof(v));
+    };
+    std::vector<double> Bf;  // modes of the current level (levels >= 1: 6 x 6 per node)
+    phase(0);
     for (int l = 0;; ++l) {
         std::unique_ptr<AmgLevel> L(new AmgLevel());
         L->b = cur.b;
@@ -831,7 +883,9 @@ static void amg_build_structure(lmtg_ctx *c) {
             break;
         }
         std::vector<uint32_t> agg;
+        phase(4);
         const uint64_t na = aggregate(cur.nn, cur.bptr, cur.bcol, l == 0 ? skip : std::vector<uint8_t>(), agg);
+        phase(1);
         if (na == 0 || na * 2 > cur.nn) {  // no useful coarsening left: this level is the coarsest
             A->levels.push_back(std::move(L));
             break;
@@ -846,14 +900,23 @@ static void amg_build_structure(lmtg_ctx *c) {
             for (uint64_t i = 0; i < cur.nn; ++i)
                 if (agg[i] != kNone) anode[pos[agg[i]]++] = (uint32_t)i;
         }
-        std::vector<float> Q;
+        HBuf<float> Q;
+        Q.alloc(cur.nn * cur.b * 6);  // rows of nodes in no aggregate are never read
         std::vector<double> Bc;
-        tentative(cur.b, cur.nn, na, aptr, anode, Bf, Q, Bc);
+        if (l == 0) {
+            tentative(3, na, aptr, anode, rigid_modes, Q, Bc);
+        } else {
+            const double *bf = Bf.data();
+            tentative(6, na, aptr, anode, [bf](uint32_t i, double *m) { std::memcpy(m, bf + 36 * (size_t)i, 36 * sizeof(double)); },
+                      Q, Bc);
+        }
+        phase(2);
         HostLevel nxt;
         nxt.b = 6;
         nxt.nn = na;
-        std::vector<uint32_t> gptr, gsrc;
+        HBuf<uint32_t> gptr, gsrc;
         coarse_pattern(na, aptr, anode, cur.bptr, cur.bcol, agg, nxt.bptr, nxt.bcol, nxt.bdiag, gptr, gsrc);
+        phase(3);
         L->nagg = na;
         upload(L->agg, agg, s);
         upload(L->aptr, aptr, s);
@@ -862,6 +925,7 @@ static void amg_build_structure(lmtg_ctx *c) {
         upload(L->gptr, gptr, s);
         upload(L->gsrc, gsrc, s);
         LMTG_CUDA(cudaStreamSynchronize(s));
+        phase(4);
         A->levels.push_back(std::move(L));
         Bf.swap(Bc);
         cur = std::move(nxt);
@@ -890,11 +954,11 @@ static void amg_numeric(lmtg_ctx *c) {
         const uint32_t *fbcol = l == 0 ? c->bcol.p : F.bcol.p;
         const float *fK = l == 0 ? c->K32.p : F.K.p;
         const uint64_t ncb = C.nnzb;
-        const int g = grid_for(c, ncb, 128, 16);
+        const int g = grid_for(c, ncb * 32, 256, 8);
         if (F.b == 3)
-            k_galerkin<3><<<g, 128, 0, s>>>(fbptr, fbcol, fK, F.Q.p, C.bptr.p, C.bcol.p, C.nn, F.gptr.p, F.gsrc.p, C.K.p);
+            k_galerkin<3><<<g, 256, 0, s>>>(fbptr, fbcol, fK, F.Q.p, C.bptr.p, C.bcol.p, C.nn, F.gptr.p, F.gsrc.p, C.K.p);
         else
-            k_galerkin<6><<<g, 128, 0, s>>>(fbptr, fbcol, fK, F.Q.p, C.bptr.p, C.bcol.p, C.nn, F.gptr.p, F.gsrc.p, C.K.p);
+            k_galerkin<6><<<g, 256, 0, s>>>(fbptr, fbcol, fK, F.Q.p, C.bptr.p, C.bcol.p, C.nn, F.gptr.p, F.gsrc.p, C.K.p);
         k_block_inv6<<<grid_for(c, C.nn, 128), 128, 0, s>>>(C.bptr.p, C.bdiag.p, C.K.p, C.nn, C.Dinv.p);
         LMTG_CUDA(cudaGetLastError());
         c->launches += 2;
@@ -913,11 +977,15 @@ static void amg_numeric(lmtg_ctx *c) {
         // power steps v -> w = D^-1 K v, v normalised from the second step on: lambda ~ |w|
         double lam = 0, h[2] = {0, 0};
         float scale = 1.f;
-        for (int it = 0; it < 10; ++it) {
+        const bool bulk = l == 0 && spmv_kind_in_use(c) != 0;
+        if (bulk) bulk0_setup(c);
+        for (int it = 0; it < 8; ++it) {
             float *v = (it & 1) ? L.xb.p : L.xa.p, *w = (it & 1) ? L.xa.p : L.xb.p;
             if (it > 0) k_amg_scale<<<grid_for(c, nv, 256), 256, 0, s>>>(v, v, scale, nv);
             const int g = grid_for(c, L.nn * 32, kRowThreads, 8);
-            if (L.b == 3)
+            if (bulk)
+                bulk0_launch(c, v, EpiPower{D, w, out2}, s, o);
+            else if (L.b == 3)
                 k_amg_power<3><<<g, kRowThreads, 0, s>>>(bp, bc, K, D, v, w, L.nn, c->partials.p, &o->cnt_c, out2);
             else
                 k_amg_power<6><<<g, kRowThreads, 0, s>>>(bp, bc, K, D, v, w, L.nn, c->partials.p, &o->cnt_c, out2);
@@ -993,7 +1061,6 @@ bool amg_prepare(lmtg_ctx *c) {
     LMTG_CHECK(c->have32, LMTG_ERR_STATE, "amg: FP32 matrix not assembled");
     if (!c->amg) amg_build_structure(c);
     if (c->amg->nc == 0) return false;
-    bulk0_setup(c);
     if (c->amg->version != c->mat_version) amg_numeric(c);
     return true;
 }
@@ -1003,10 +1070,18 @@ float amg_omega0(const lmtg_ctx *c) { return c->amg->levels[0]->omega; }
 float *amg_xa0(const lmtg_ctx *c) { return c->amg->levels[0]->xa.p; }
 
 // The cycle after the update kernel: r (level-0 residual, packed) -> z (padded), rz and beta.
-void amg_launch_cycle(lmtg_ctx *c, const float *r, float *z, cudaStream_t s, int start, double beta_den) {
+// ev (profiling only) receives events after the level-0 residual, the level-0 restriction, the
+// coarse levels, the level-0 prolongation and the level-0 smoothing.
+void amg_launch_cycle(lmtg_ctx *c, const float *r, float *z, cudaStream_t s, int start, double beta_den,
+                      cudaEvent_t *ev) {
     AmgState &A = *c->amg;
     PcgScalars *S = c->scal.p;
     const size_t nl = A.levels.size();
+    const bool warp_rows = spmv_kind_in_use(c) == 0;
+    if (!warp_rows) bulk0_setup(c);
+    auto mark = [&](int k) {
+        if (ev) LMTG_CUDA(cudaEventRecord(ev[k], s));
+    };
     // down: residual and restriction
     for (size_t l = 0; l + 1 < nl; ++l) {
         AmgLevel &L = *A.levels[l], &N = *A.levels[l + 1];
@@ -1019,9 +1094,12 @@ void amg_launch_cycle(lmtg_ctx *c, const float *r, float *z, cudaStream_t s, int
             c->launches += 1;
         }
         if (L.b == 3) {
-            bulk0_launch(c, L.xa.p, EpiRes{rl, L.res.p}, s);
+            if (warp_rows) k_amg_res<3><<<g, kRowThreads, 0, s>>>(bp, bc, K, L.xa.p, rl, L.res.p, L.nn, S);
+            else bulk0_launch(c, L.xa.p, EpiRes{rl, L.res.p}, s);
+            mark(0);
             k_amg_restrict<3><<<grid_for(c, L.nagg * 32, kRowThreads, 8), kRowThreads, 0, s>>>(L.aptr.p, L.anode.p, L.Q.p,
                                                                                             L.res.p, N.r.p, L.nagg, S);
+            mark(1);
         } else {
             k_amg_res<6><<<g, kRowThreads, 0, s>>>(bp, bc, K, L.xa.p, rl, L.res.p, L.nn, S);
             k_amg_restrict<6><<<grid_for(c, L.nagg * 32, kRowThreads, 8), kRowThreads, 0, s>>>(L.aptr.p, L.anode.p, L.Q.p,
@@ -1042,6 +1120,7 @@ void amg_launch_cycle(lmtg_ctx *c, const float *r, float *z, cudaStream_t s, int
         const float *e = ncoarsest ? N.res.p : N.xb.p;
         const int tb = 256;
         if (L.b == 3) {
+            mark(2);
             if (ncoarsest)
                 k_amg_prolong<3, 6><<<grid_for(c, 3 * L.nn, tb), tb, 0, s>>>(L.agg.p, L.Q.p, e, L.xa.p, L.nn, S);
             else
@@ -1053,9 +1132,15 @@ void amg_launch_cycle(lmtg_ctx *c, const float *r, float *z, cudaStream_t s, int
                 k_amg_prolong<6, 8><<<grid_for(c, 6 * L.nn, tb), tb, 0, s>>>(L.agg.p, L.Q.p, e, L.xa.p, L.nn, S);
         }
         const int g = grid_for(c, L.nn * 32, kRowThreads, 8);
-        if (l == 0)
-            bulk0_launch(c, L.xa.p, EpiPost{r, c->Dinv32.p, z, L.omega, start, beta_den}, s);
-        else
+        if (l == 0) {
+            mark(3);
+            if (warp_rows)
+                k_amg_post<3><<<g, kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, c->K32.p, c->Dinv32.p, L.xa.p, r, z,
+                                                        L.omega, L.nn, S, true, start, beta_den, c->partials.p);
+            else
+                bulk0_launch(c, L.xa.p, EpiPost{r, c->Dinv32.p, z, L.omega, start, beta_den}, s);
+            mark(4);
+        } else
             k_amg_post<6><<<g, kRowThreads, 0, s>>>(L.bptr.p, L.bcol.p, L.K.p, L.Dinv.p, L.xa.p, L.r.p, L.xb.p, L.omega,
                                                     L.nn, S, false, 0, 0.0, c->partials.p);
         c->launches += 2;
@@ -1064,7 +1149,7 @@ void amg_launch_cycle(lmtg_ctx *c, const float *r, float *z, cudaStream_t s, int
 }
 
 void amg_info(const lmtg_ctx *c, int *levels, uint64_t *ndof, uint64_t *nnzb, double *omega, double *lambda,
-              double *structure_ms, double *numeric_ms) {
+              double *structure_ms, double *numeric_ms, double *phase_ms) {
     const AmgState *A = c->amg;
     const int nl = A ? (int)A->levels.size() : 0;
     if (levels) *levels = nl;
@@ -1077,6 +1162,8 @@ void amg_info(const lmtg_ctx *c, int *levels, uint64_t *ndof, uint64_t *nnzb, do
     }
     if (structure_ms) *structure_ms = A ? A->structure_ms : 0.0;
     if (numeric_ms) *numeric_ms = A ? A->numeric_ms : 0.0;
+    if (phase_ms)
+        for (int k = 0; k < 5; ++k) phase_ms[k] = A ? A->phase_ms[k] : 0.0;
 }
 
 }  // namespace lmtg

@@ -33,6 +33,9 @@ struct AmgState {
     DBuf<float> Cinv;       // its inverse, row-major
     uint64_t version = ~0ull;  // matrix version of the numeric setup
     double structure_ms = 0, numeric_ms = 0;
+    // host time of the structure setup by phase: pattern copy and modes, aggregation, tentative
+    // prolongators, coarse patterns and gather lists, uploads
+    double phase_ms[5] = {0, 0, 0, 0, 0};
 };
 
 void amg_free(lmtg_ctx *c);
@@ -42,8 +45,9 @@ bool amg_applicable(const lmtg_ctx *c);
 bool amg_prepare(lmtg_ctx *c);
 float amg_omega0(const lmtg_ctx *c);
 float *amg_xa0(const lmtg_ctx *c);
-void amg_launch_cycle(lmtg_ctx *c, const float *r, float *z, cudaStream_t s, int start, double beta_den);
+void amg_launch_cycle(lmtg_ctx *c, const float *r, float *z, cudaStream_t s, int start, double beta_den,
+                      cudaEvent_t *ev = nullptr);
 void amg_info(const lmtg_ctx *c, int *levels, uint64_t *ndof, uint64_t *nnzb, double *omega, double *lambda,
-              double *structure_ms, double *numeric_ms);
+              double *structure_ms, double *numeric_ms, double *phase_ms);
 
 }  // namespace lmtg

@@ -142,10 +142,12 @@ struct lmtg_ctx {
     uint64_t nnzb = 0, nnz_lower = 0, ngather = 0;
     uint32_t max_row_blocks = 0;  // blocks in the widest node row (<= 96; <= 288 on the recalage's
                                   // virtual pattern, whose FP32 SpMV is then the warp-row kernel)
-    // FP32 PCG SpMV: 0 = warp per row pair, 1, 2 = bulk-copy pipeline (solver.cu), -1 (default)
-    // = 2 when a node row has more than 32 blocks, else 1; the grid is set up when the kind
-    // in use changes
+    // FP32 PCG SpMV: 0 = warp per row pair, 1, 2 = bulk-copy pipeline (solver.cu) with 4 / 5 CTAs
+    // per SM, -1 (default) = autotuned; the grid is set up when the kind in use changes
     int spmv_kind = -1, spmv_setup_kind = -2, spmv_grid = 0;
+    // autotuned kind for spmv_kind -1 (timed at the first FP32 PCG run of a pattern; -1 = not yet)
+    int spmv_tuned = -1;
+    double spmv_tune_ms[3] = {0, 0, 0};
     lmtg::DBuf<uint32_t> bptr, bcol, bdiag, gptr, gsrc;
 
     // values
@@ -261,6 +263,10 @@ int solve_pcg64(lmtg_ctx *c, int crit_kind, double tol, int maxit, double timeou
 int solve_mixed(lmtg_ctx *c, double tol, int maxit, double timeout_s, lmtg_solve_stats *st,
                 const double *b = nullptr, double *x = nullptr);
 void profile_pcg(lmtg_ctx *c, bool fp32, int iters, double *spmv_ms, double *update_ms);
+// FP32 SpMV kind in use (0 warp-row, 1, 2 bulk copies)
+int spmv_kind_in_use(const lmtg_ctx *c);
+// per-stage device times of the multigrid-preconditioned FP32 iteration (amg.cu stages)
+void profile_amg(lmtg_ctx *c, int iters, double *ms);
 
 // ---- utilities (pattern.cu) ----
 // Exclusive scan of u32 counts into u32 offsets (out has count+1 entries); returns the total.

@@ -284,6 +284,7 @@ void recal_setup(lmtg_ctx *c, double rho, double omega, double gamma, double r, 
     c->nnz_lower = 9ull * (nnzb_v - nv) / 2 + 6ull * nv;
     c->max_row_blocks *= 3;  // above 96 the FP32 solves take the warp-row SpMV, which strides over any width
     c->spmv_setup_kind = -2;
+    c->spmv_tuned = -1;
     c->K64.alloc(nnzb_v * 9);
     c->K32.alloc(nnzb_v * 9 + 4);
     c->F.alloc(c->n);

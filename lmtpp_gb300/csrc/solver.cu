@@ -71,8 +71,12 @@ static int bulk_grid(lmtg_ctx *c) {
 // than 96 blocks (the recalage's virtual pattern) always take the warp-row kernel
 static int spmv_kind_used(const lmtg_ctx *c) {
     if (c->max_row_blocks > 96) return 0;
-    return c->spmv_kind >= 0 ? c->spmv_kind : (c->max_row_blocks > 32 ? 2 : 1);
+    if (c->spmv_kind >= 0) return c->spmv_kind;
+    if (c->spmv_tuned >= 0) return c->spmv_tuned;
+    return c->max_row_blocks > 32 ? 2 : 1;
 }
+
+int spmv_kind_in_use(const lmtg_ctx *c) { return spmv_kind_used(c); }
 
 static void spmv_setup(lmtg_ctx *c) {
     const int kind = spmv_kind_used(c);
@@ -118,6 +122,43 @@ void spmv32(lmtg_ctx *c, const float *x, float *y) {
                                                               c->nn);
     LMTG_CUDA(cudaGetLastError());
     c->launches += 1;
+}
+
+// FP32 SpMV autotuner (spmv_kind -1): at the first FP32 PCG run of a pattern every kind the
+// pattern admits -- 0 the warp-row kernel, 1 and 2 the bulk-copy pipeline with the resident grid
+// sized for 4 or 5 CTAs per SM -- is timed with CUDA events over three launches on the assembled
+// K32 (after one untimed launch), and the fastest is kept for the context's later solves.  Runs
+// with the scalars of a fresh PCG run (done = 0); p and q are scratch at that point.
+static void spmv_autotune(lmtg_ctx *c, const float *K, const float *p, float *q) {
+    cudaStream_t s = c->stream;
+    cudaEvent_t e0, e1;
+    LMTG_CUDA(cudaEventCreate(&e0));
+    LMTG_CUDA(cudaEventCreate(&e1));
+    int best = -1;
+    double best_ms = 0;
+    for (int k = 0; k < 3; ++k) {
+        c->spmv_tune_ms[k] = 0;
+        if (k > 0 && c->max_row_blocks > 96) continue;
+        c->spmv_tuned = k;
+        spmv_setup(c);
+        launch_pcg_spmv<float, 4>(c, K, p, q, s);
+        LMTG_CUDA(cudaEventRecord(e0, s));
+        for (int r = 0; r < 3; ++r) launch_pcg_spmv<float, 4>(c, K, p, q, s);
+        LMTG_CUDA(cudaEventRecord(e1, s));
+        LMTG_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        LMTG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        c->spmv_tune_ms[k] = ms / 3.0;
+        c->launches += 4;
+        if (best < 0 || ms / 3.0 < best_ms) {
+            best = k;
+            best_ms = ms / 3.0;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    c->spmv_tuned = best;
+    spmv_setup(c);
 }
 
 // Second scalar slot (index 1) serves the outer loop and standalone reductions.
@@ -277,6 +318,9 @@ static int run_pcg(lmtg_ctx *c, const T *K, const T *Dinv, const T *b, T *x, T *
     init.maxit = maxit;
     init.bb = b_norm2 >= 0 ? b_norm2 : 0.0;
     LMTG_CUDA(cudaMemcpyAsync(c->scal.p, &init, sizeof(init), cudaMemcpyHostToDevice, s));
+    if constexpr (std::is_same<T, float>::value) {
+        if (c->spmv_kind < 0 && c->spmv_tuned < 0 && beta_den <= 0.0) spmv_autotune(c, K, p0, q);
+    }
     if (x_is_zero) {
         LMTG_CUDA(cudaMemcpyAsync(r, b, sizeof(T) * c->n, cudaMemcpyDeviceToDevice, s));
     } else {
@@ -526,6 +570,62 @@ void profile_pcg(lmtg_ctx *c, bool fp32, int iters, double *spmv_ms, double *upd
                              c->w32[4].p, c->w32[5].p, reinterpret_cast<float *>(c->w64[1].p), iters,
                              spmv_ms, update_ms);
     }
+}
+
+// Device time per stage of the multigrid-preconditioned FP32 iteration, averaged over `iters`
+// iterations run on the scaled load vector with a criterion that never stops them: ms[0] the
+// PCG's SpMV, [1] the update (with the first smoothing step), [2] the level-0 residual, [3] the
+// restriction, [4] the coarse levels, [5] the prolongation, [6] the level-0 smoothing (z, r.z),
+// [7] the direction update.  All zero when the context has no hierarchy.
+void profile_amg(lmtg_ctx *c, int iters, double *ms) {
+    for (int k = 0; k < 8; ++k) ms[k] = 0;
+    if (!amg_prepare(c)) return;
+    cudaStream_t s = c->stream;
+    spmv_setup(c);
+    float *b32 = c->w32[0].p, *x = c->w32[1].p, *r = c->w32[2].p, *z = c->w32[3].p, *p0 = c->w32[4].p;
+    float *q = reinterpret_cast<float *>(c->w64[1].p);
+    const double bb = dot64(c, c->F.p, c->F.p);
+    k_scale_to32<<<node_grid(c), kRowThreads, 0, s>>>(c->F.p, bb > 0 ? 1.0 / std::sqrt(bb) : 1.0, b32, c->n);
+    PcgScalars init{};
+    init.crit = 0.0;
+    init.crit_kind = LMTG_CRIT_REL_RESIDUAL;
+    init.maxit = 1 << 30;
+    init.bb = 1.0;
+    LMTG_CUDA(cudaMemcpyAsync(c->scal.p, &init, sizeof(init), cudaMemcpyHostToDevice, s));
+    LMTG_CUDA(cudaMemsetAsync(x, 0, sizeof(float) * c->n, s));
+    LMTG_CUDA(cudaMemcpyAsync(r, b32, sizeof(float) * c->n, cudaMemcpyDeviceToDevice, s));
+    LMTG_CUDA(cudaMemsetAsync(p0, 0, sizeof(float) * 4 * c->nn, s));
+    k_pcg_start_amg<<<node_grid(c), kRowThreads, 0, s>>>(r, nullptr, c->Dinv32.p, amg_xa0(c), amg_omega0(c), c->nn,
+                                                         c->scal.p, c->partials.p);
+    amg_launch_cycle(c, r, z, s, 1, 0.0);
+    c->launches += 2;
+    std::vector<cudaEvent_t> ev(9 * iters);
+    for (auto &e : ev) LMTG_CUDA(cudaEventCreate(&e));
+    const uint64_t l0 = c->launches;
+    for (int it = 0; it < iters; ++it) {
+        cudaEvent_t *e = &ev[9 * it];
+        LMTG_CUDA(cudaEventRecord(e[0], s));
+        k_pcg_dir<float, 4><<<node_grid(c), kRowThreads, 0, s>>>(z, p0, c->nn, c->scal.p);
+        LMTG_CUDA(cudaEventRecord(e[1], s));
+        launch_pcg_spmv<float, 4>(c, c->K32.p, p0, q, s);
+        LMTG_CUDA(cudaEventRecord(e[2], s));
+        k_pcg_update_amg<<<node_grid(c), kRowThreads, 0, s>>>(x, r, p0, q, c->Dinv32.p, amg_xa0(c), amg_omega0(c),
+                                                              c->nn, c->scal.p, c->partials.p);
+        LMTG_CUDA(cudaEventRecord(e[3], s));
+        amg_launch_cycle(c, r, z, s, 0, 0.0, e + 4);
+    }
+    c->launches += 3ull * iters;
+    (void)l0;
+    LMTG_CUDA(cudaGetLastError());
+    LMTG_CUDA(cudaEventSynchronize(ev[9 * iters - 1]));
+    static const int from[8] = {1, 2, 3, 4, 5, 6, 7, 0}, to[8] = {2, 3, 4, 5, 6, 7, 8, 1};
+    for (int it = 0; it < iters; ++it)
+        for (int k = 0; k < 8; ++k) {
+            float m = 0;
+            cudaEventElapsedTime(&m, ev[9 * it + from[k]], ev[9 * it + to[k]]);
+            ms[k] += m / iters;
+        }
+    for (auto &e : ev) cudaEventDestroy(e);
 }
 
 }  // namespace lmtg

@@ -330,8 +330,45 @@ class Formulation:
         abi.check(self._lib.lmtg_set_inner_reduction(self._ctx, float(inner_reduction)), self._ctx,
                   "set_inner_reduction")
 
+    def set_preconditioner(self, kind):
+        """'amg' (default: aggregation multigrid V-cycle) or 'block_jacobi' for the FP32 inner PCG of
+        the mixed solve; the FP64 PCG always uses block Jacobi."""
+        k = {"block_jacobi": abi.PREC_BLOCK_JACOBI, "amg": abi.PREC_AMG}[kind]
+        abi.check(self._lib.lmtg_set_preconditioner(self._ctx, k), self._ctx, "set_preconditioner")
+
+    def amg_info(self):
+        """The multigrid hierarchy of the last mixed solve: per level unknowns, stored blocks,
+        smoothing weight and lambda_max(D^-1 K); host setup times (structure, last numeric)."""
+        lv = ctypes.c_int()
+        nd, nb = (ctypes.c_uint64 * 8)(), (ctypes.c_uint64 * 8)()
+        om, la = (ctypes.c_double * 8)(), (ctypes.c_double * 8)()
+        sm, nm = ctypes.c_double(), ctypes.c_double()
+        ph = (ctypes.c_double * 5)()
+        abi.check(self._lib.lmtg_amg_info(self._ctx, ctypes.byref(lv), nd, nb, om, la, ctypes.byref(sm),
+                                          ctypes.byref(nm), ph), self._ctx, "amg_info")
+        n = lv.value
+        return {"levels": n, "ndof": list(nd)[:n], "nnz_blocks": list(nb)[:n], "omega": list(om)[:n],
+                "lambda_max": list(la)[:n], "structure_ms": sm.value, "numeric_ms": nm.value,
+                "structure_phase_ms": dict(zip(["pattern_modes", "aggregation", "tentative", "coarse_pattern",
+                                                "uploads"], list(ph)))}
+
+    def spmv_info(self):
+        """FP32 SpMV kind in use, the autotuned kind and the autotuner's per-kind times (ms)."""
+        k, t = ctypes.c_int(), ctypes.c_int()
+        ms = (ctypes.c_double * 3)()
+        abi.check(self._lib.lmtg_spmv_info(self._ctx, ctypes.byref(k), ctypes.byref(t), ms), self._ctx, "spmv_info")
+        return {"kind": k.value, "tuned": t.value, "tune_ms": list(ms)}
+
+    def profile_amg_kernels(self, iters=10):
+        """Per-stage device times (ms) of one multigrid-preconditioned FP32 iteration."""
+        ms = (ctypes.c_double * 8)()
+        abi.check(self._lib.lmtg_profile_amg_kernels(self._ctx, int(iters), ms), self._ctx, "profile_amg_kernels")
+        names = ["spmv", "update", "residual0", "restrict0", "coarse", "prolong0", "smooth0", "direction"]
+        return dict(zip(names, list(ms)))
+
     def set_spmv_kind(self, kind):
-        """FP32 PCG SpMV: 0 = warp per row pair, 1, 2 = matrix streamed by bulk copies (TMA), -1 (default) = by row width."""
+        """FP32 PCG SpMV: 0 = warp per row pair, 1, 2 = matrix streamed by bulk copies (TMA) with 4 / 5 CTAs per
+        SM, -1 (default) = autotuned at the first FP32 solve."""
         abi.check(self._lib.lmtg_set_spmv_kind(self._ctx, int(kind)), self._ctx, "set_spmv_kind")
 
     def set_penalty_scale(self, max_diag):
