@@ -1,0 +1,152 @@
+"""The FP32 inner PCG's preconditioners and SpMV autotuner against the reference's LDL solutions.
+
+Both preconditioners of the mixed solve -- the aggregation multigrid (default) and block Jacobi --
+must reach the reference's LDL solution of the C3 family (Hexa8 16^3, lognormal E) and of the C2
+family (Tetra10 10^3 cubes) at 1e-8; the multigrid must need far fewer iterations; new
+assemblies (numeric setup again) and constraint changes (structure again) must keep it right;
+results are bit-identical across repeated solves with the kind fixed.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from lmtpp_gb300 import Formulation, make_rect_hexa, make_rect_tetra10, x1_faces
+
+pytestmark = pytest.mark.gpu
+
+
+def load(golden_dir, name):
+    g = np.load(os.path.join(golden_dir, name + ".npz"))
+    d = {k: g[k] for k in g.files}
+    d["meta"] = json.loads(str(d["meta"]))
+    return d
+
+
+def c3_family(g):
+    m = g["meta"]
+    pos, conn = make_rect_hexa(m["nb_points"])
+    E = np.exp(m["E_logmean"] + m["E_logstd"] * np.random.default_rng(m["seed"]).standard_normal(conn.shape[0]))
+    f = Formulation(pos, conn)
+    f.elastic_modulus = E
+    f.poisson_ratio = m["nu"]
+    clamped = np.nonzero(pos[:, 0] < 1e-6)[0]
+    f.add_constraints((3 * clamped[:, None] + np.arange(3)).ravel(), m["penalty"])
+    f.add_skin_traction(x1_faces(pos, conn), (1.0, 0.0, 0.0))
+    f.allocate_matrices()
+    return f, pos, conn
+
+
+def rel(u, ref):
+    return np.linalg.norm(u - ref) / np.linalg.norm(ref)
+
+
+def test_both_preconditioners_reach_the_reference_solution(golden_dir):
+    g = load(golden_dir, "hexa_16_lognormal")
+    f, _, _ = c3_family(g)
+    its = {}
+    for prec in ("block_jacobi", "amg"):
+        f.set_preconditioner(prec)
+        f.set_result(np.zeros(f.n))
+        st = f.solve(1e-12, mode="mixed")
+        assert st["status"] == 0
+        assert rel(f.get_result(), g["u_ldl"]) <= 1e-8, prec
+        its[prec] = st["iterations"]
+    info = f.amg_info()
+    assert info["levels"] >= 2 and info["ndof"][0] == f.n
+    assert all(0.0 < w < 2.0 / lam for w, lam in zip(info["omega"][:-1], info["lambda_max"][:-1]))
+    assert its["amg"] * 4 < its["block_jacobi"], its
+    f.close()
+
+
+def test_amg_tetra10_family(golden_dir):
+    g = load(golden_dir, "tetra10_10x10x10")
+    m = g["meta"]
+    pos, conn = make_rect_tetra10(m["nb_points"])
+    f = Formulation(pos, conn)
+    f.elastic_modulus = m["E"]
+    f.poisson_ratio = m["nu"]
+    clamped = np.nonzero(pos[:, 0] < 1e-6)[0]
+    f.add_constraints((3 * clamped[:, None] + np.arange(3)).ravel(), m["penalty"])
+    f.add_skin_traction(x1_faces(pos, conn), (1.0, 0.0, 0.0))
+    st = f.solve(1e-12, mode="mixed")
+    assert st["status"] == 0
+    assert rel(f.get_result(), g["u_ldl"]) <= 1e-8
+    assert f.amg_info()["levels"] >= 2
+    f.close()
+
+
+def test_amg_numeric_and_structure_setup_follow_the_system(golden_dir):
+    """A new assembly (other moduli) runs the numeric setup again; new constraints rebuild the
+    structure; both solves match a block-Jacobi solve of the same system."""
+    g = load(golden_dir, "hexa_16_lognormal")
+    f, pos, conn = c3_family(g)
+    f.solve(1e-12, mode="mixed")
+    n0 = f.amg_info()["numeric_ms"]
+    assert n0 > 0
+    f.elastic_modulus = np.full(conn.shape[0], 70000.0)
+    f.set_result(np.zeros(f.n))
+    f.solve(1e-12, mode="mixed")
+    u_amg = f.get_result()
+    f.set_preconditioner("block_jacobi")
+    f.set_result(np.zeros(f.n))
+    f.solve(1e-12, mode="mixed")
+    assert rel(u_amg, f.get_result()) <= 1e-9
+    # a prescribed displacement on x = 1 as well (new constraints: the structure leaves those nodes out)
+    f.set_preconditioner("amg")
+    x1 = np.nonzero(pos[:, 0] > 1 - 1e-6)[0]
+    f.add_constraints((3 * x1[:, None]).ravel(), 1e5, res=np.full(x1.size, 1e-3))
+    f.set_result(np.zeros(f.n))
+    st = f.solve(1e-12, mode="mixed")
+    assert st["status"] == 0
+    u_amg = f.get_result()
+    # the prescribed displacements make the penalised system far worse conditioned: the solution
+    # is checked through its residual in the assembled matrix, and against block Jacobi loosely
+    rp, col, val = f.get_mat()
+    L = sp.csr_matrix((val, col.astype(np.int64), rp.astype(np.int64)), shape=(f.n, f.n))
+    K = L + sp.tril(L, -1).T
+    F = f.get_sollicitation()
+    assert np.linalg.norm(F - K @ u_amg) <= 1e-11 * np.linalg.norm(F)
+    f.set_preconditioner("block_jacobi")
+    f.set_result(np.zeros(f.n))
+    f.solve(1e-12, mode="mixed")
+    assert rel(u_amg, f.get_result()) <= 1e-5
+    f.close()
+
+
+def test_amg_solves_are_deterministic_and_profiled(golden_dir):
+    g = load(golden_dir, "hexa_16_lognormal")
+    f, _, _ = c3_family(g)
+    out = []
+    for _ in range(2):
+        f.set_result(np.zeros(f.n))
+        f.solve(1e-12, mode="mixed")
+        out.append(f.get_result())
+    assert np.array_equal(out[0], out[1])
+    sp = f.spmv_info()
+    assert sp["kind"] in (0, 1, 2) and sp["tuned"] == sp["kind"]
+    assert min(t for t in sp["tune_ms"] if t > 0) == pytest.approx(sp["tune_ms"][sp["kind"]])
+    stages = f.profile_amg_kernels(iters=3)
+    assert all(v > 0 for v in stages.values()), stages
+    # a pinned kind is kept
+    f.set_spmv_kind(0)
+    f.set_result(np.zeros(f.n))
+    f.solve(1e-12, mode="mixed")
+    assert f.spmv_info()["kind"] == 0
+    assert rel(f.get_result(), g["u_ldl"]) <= 1e-8
+    f.close()
+
+
+def test_small_systems_use_block_jacobi():
+    pos, conn = make_rect_hexa(4)
+    f = Formulation(pos, conn)
+    f.elastic_modulus, f.poisson_ratio = 210000.0, 0.3
+    clamped = np.nonzero(pos[:, 0] < 1e-6)[0]
+    f.add_constraints((3 * clamped[:, None] + np.arange(3)).ravel(), 1e5)
+    f.add_skin_traction(x1_faces(pos, conn), (1.0, 0.0, 0.0))
+    st = f.solve(1e-12, mode="mixed")
+    assert st["status"] == 0
+    assert f.amg_info()["levels"] == 0
+    f.close()
