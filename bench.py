@@ -384,8 +384,13 @@ def cpu_desc(s, full):
 SPMV32_KERNEL = {"hexa8": "k_pcg_spmv_bulk<2, 512, 8, 1, 4>", "tetra10": "k_pcg_spmv_bulk<2, 512, 8, 1, 5>"}
 SPMV32_TRAFFIC_RATIO = {"hexa8": (293.261824 + 4.431616) / 296.350284,
                         "tetra10": (132.940032 + 3.373312) / 134.148172}
-# the same ratio for the multigrid's level-0 residual and smoothing launches (ncu captures below)
-STAGE_TRAFFIC_RATIO = {}
+# the same ratio for the multigrid's level-0 residual and smoothing launches, ncu captures of
+# Hexa8 64^3 (profiles/ncu_amg_level0_hexa8_64.md):
+#   EpiRes:  (296.566016 MB + 3.514880 MB) over 299.645784 MB
+#   EpiPost: (307.288064 MB + 0.907520 MB) over 310.630784 MB
+STAGE_TRAFFIC_RATIO = {("hexa8", "residual0"): (296.566016 + 3.514880) / 299.645784,
+                       ("hexa8", "smooth0"): (307.288064 + 0.907520) / 310.630784,
+                       ("hexa8", "spmv"): (293.261824 + 4.431616) / 296.350284}
 
 METRIC = "time-to-solution at 1e-10 rel. error vs FP64 oracle, mixed vs FP64 CG; asm GB/s"
 

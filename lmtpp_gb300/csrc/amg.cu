@@ -22,13 +22,15 @@
 //             no atomics, deterministic).
 //   coarsest  (<= 300 unknowns): a dense inverse, computed on the host in FP64, applied in FP32.
 // Numeric setup after every matrix assembly: the Galerkin products, the 6x6 block-Jacobi
-// inverses, and per level the damped-Jacobi weight omega = 1.6 / lambda_max(D^-1 K) (lambda_max by
-// eight power steps; the weight of a degree-1 Chebyshev smoother on [lambda/30, 1.1 lambda]).
+// inverses, and per level the damped-Jacobi weight omega = 1.47 / lambda_max(D^-1 K) (lambda_max by
+// twelve power steps, which approach it from below; the weight of a degree-1 Chebyshev smoother on
+// [h/30, h], h = 1.2 lambda).
 //
 // V-cycle (z = M r), per level: x = omega D^-1 r; res = r - K x; restrict Q^T res; recurse;
 // x += Q e; x' = x + omega D^-1 (r - K x).  The same smoother before and after makes M symmetric,
 // as the conjugate gradient needs.  At level 0 the first smoothing step is fused into the PCG's
-// update kernel and the last one writes z and forms r.z and beta.  Every kernel returns at once
+// update kernel and the last one writes z and forms r.z and beta; at the coarser levels the
+// first smoothing step is fused into the restriction that produces the level's right-hand side.  Every kernel returns at once
 // once the PCG's `done` flag is set, so the cycle runs inside the captured iteration chunks.
 #include <algorithm>
 #include <chrono>
@@ -214,22 +216,6 @@ __device__ __forceinline__ void row6(const uint32_t *__restrict__ bcol, const fl
 // cycle kernels
 // ---------------------------------------------------------------------------------------------
 
-// x = omega D^-1 r (6x6 blocks; r packed 6, x padded 8)
-__global__ void k_amg_bj6(const float *__restrict__ Dinv, const float *__restrict__ r, float *__restrict__ x,
-                          float omega, uint64_t nn, const PcgScalars *S) {
-    if (done(S)) return;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < 6 * nn; i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t I = i / 6;
-        const int c = (int)(i - 6 * I);
-        const float *D = Dinv + 36 * I + 6 * c;
-        const float *rv = r + 6 * I;
-        float s = 0.f;
-#pragma unroll
-        for (int k = 0; k < 6; ++k) s = fmaf(D[k], rv[k], s);
-        x[8 * I + c] = omega * s;
-    }
-}
-
 // res = r - K x (r == nullptr: res = -K x), warp per row
 template <int B>
 __global__ void __launch_bounds__(kRowThreads)
@@ -316,11 +302,13 @@ __global__ void __launch_bounds__(kRowThreads)
     }
 }
 
-// rc = Q^T res per aggregate (warp per aggregate)
+// rc = Q^T res per aggregate (warp per aggregate); with Dc, also the coarse level's first
+// smoothing step xc = omega_c Dc^-1 rc (padded 8), which needs nothing but rc
 template <int B>
 __global__ void __launch_bounds__(kRowThreads)
     k_amg_restrict(const uint32_t *__restrict__ aptr, const uint32_t *__restrict__ anode, const float *__restrict__ Q,
-                   const float *__restrict__ res, float *__restrict__ rc, uint64_t na, const PcgScalars *S) {
+                   const float *__restrict__ res, float *__restrict__ rc, uint64_t na, const float *__restrict__ Dc,
+                   float omega_c, float *__restrict__ xc, const PcgScalars *S) {
     if (done(S)) return;
     const int lane = threadIdx.x & 31;
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -343,6 +331,13 @@ __global__ void __launch_bounds__(kRowThreads)
 #pragma unroll
             for (int c = 1; c < 6; ++c) v = lane == c ? acc[c] : v;
             rc[6 * a + lane] = v;
+            if (Dc) {
+                const float *D = Dc + 36 * a + 6 * lane;
+                float x = 0.f;
+#pragma unroll
+                for (int k = 0; k < 6; ++k) x = fmaf(D[k], acc[k], x);
+                xc[8 * a + lane] = omega_c * x;
+            }
         }
     }
 }
@@ -445,11 +440,14 @@ struct EpiRes {
     const float *r;
     float *res;
     static constexpr bool kReduce = false;
-    __device__ __forceinline__ void row(uint64_t I, float qi, int lane, const float *, float &) const {
-        if ((lane & 7) == 0 && lane < 24) {
-            const uint64_t i = 3 * I + (lane >> 3);
-            res[i] = r[i] - qi;
-        }
+    struct Pre {
+        float r;
+    };
+    __device__ __forceinline__ Pre pre(uint64_t I, int lane, const float *) const {
+        return {((lane & 7) == 0 && lane < 24) ? r[3 * I + (lane >> 3)] : 0.f};
+    }
+    __device__ __forceinline__ void row(uint64_t I, float qi, int lane, const float *, float &, const Pre &pr) const {
+        if ((lane & 7) == 0 && lane < 24) res[3 * I + (lane >> 3)] = pr.r - qi;
     }
     __device__ static unsigned *ticket(PcgScalars *S) { return &S->cnt_d; }
     __device__ void final(PcgScalars *, double) const {}
@@ -462,15 +460,26 @@ struct EpiPost {
     int start;
     double beta_den;
     static constexpr bool kReduce = true;
-    __device__ __forceinline__ void row(uint64_t I, float qi, int lane, const float *__restrict__ x, float &acc) const {
+    struct Pre {
+        float r0, r1, r2, x, d0, d1, d2;
+    };
+    __device__ __forceinline__ Pre pre(uint64_t I, int lane, const float *__restrict__ x) const {
+        Pre p{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        if (lane < 3) {
+            const float *Dr = D + 9 * I + 3 * lane;
+            p = {r[3 * I], r[3 * I + 1], r[3 * I + 2], x[4 * I + lane], Dr[0], Dr[1], Dr[2]};
+        }
+        return p;
+    }
+    __device__ __forceinline__ void row(uint64_t I, float qi, int lane, const float *, float &acc,
+                                        const Pre &p) const {
         const float v0 = __shfl_sync(0xffffffffu, qi, 0), v1 = __shfl_sync(0xffffffffu, qi, 8),
                     v2 = __shfl_sync(0xffffffffu, qi, 16);
         if (lane < 3) {
-            const float d0 = r[3 * I] - v0, d1 = r[3 * I + 1] - v1, d2 = r[3 * I + 2] - v2;
-            const float *Dr = D + 9 * I + 3 * lane;
-            const float zc = x[4 * I + lane] + omega * (Dr[0] * d0 + Dr[1] * d1 + Dr[2] * d2);
+            const float zc = p.x + omega * (p.d0 * (p.r0 - v0) + p.d1 * (p.r1 - v1) + p.d2 * (p.r2 - v2));
             z[4 * I + lane] = zc;
-            acc = fmaf(r[3 * I + lane], zc, acc);
+            const float rc = lane == 0 ? p.r0 : (lane == 1 ? p.r1 : p.r2);
+            acc = fmaf(rc, zc, acc);
         }
     }
     __device__ static unsigned *ticket(PcgScalars *S) { return &S->cnt_d; }
@@ -491,12 +500,23 @@ struct EpiPower {
     float *w;
     double *out;
     static constexpr bool kReduce = true;
-    __device__ __forceinline__ void row(uint64_t I, float qi, int lane, const float *, float &acc) const {
+    struct Pre {
+        float d0, d1, d2;
+    };
+    __device__ __forceinline__ Pre pre(uint64_t I, int lane, const float *) const {
+        Pre p{0.f, 0.f, 0.f};
+        if (lane < 3) {
+            const float *Dr = D + 9 * I + 3 * lane;
+            p = {Dr[0], Dr[1], Dr[2]};
+        }
+        return p;
+    }
+    __device__ __forceinline__ void row(uint64_t I, float qi, int lane, const float *, float &acc,
+                                        const Pre &p) const {
         const float v0 = __shfl_sync(0xffffffffu, qi, 0), v1 = __shfl_sync(0xffffffffu, qi, 8),
                     v2 = __shfl_sync(0xffffffffu, qi, 16);
         if (lane < 3) {
-            const float *Dr = D + 9 * I + 3 * lane;
-            const float wc = Dr[0] * v0 + Dr[1] * v1 + Dr[2] * v2;
+            const float wc = p.d0 * v0 + p.d1 * v1 + p.d2 * v2;
             w[4 * I + lane] = wc;
             acc = fmaf(wc, wc, acc);
         }
@@ -528,7 +548,12 @@ struct Bulk0 {
 };
 // the shapes of the PCG's own SpMV: 4 CTAs per SM for rows of <= 32 blocks, 5 for wider rows
 template <class Epi> using Bulk0N = Bulk0<2, 512, 8, true, 4, Epi>;
-template <class Epi> using Bulk0W = Bulk0<2, 512, 8, true, 5, Epi>;
+// (the smoothing and power epilogues keep 4 CTAs per SM for wide rows too: at 5 their prefetched
+// operands spill)
+template <class Epi> struct WideMinB { static constexpr int v = 5; };
+template <> struct WideMinB<EpiPost> { static constexpr int v = 4; };
+template <> struct WideMinB<EpiPower> { static constexpr int v = 4; };
+template <class Epi> using Bulk0W = Bulk0<2, 512, 8, true, WideMinB<Epi>::v, Epi>;
 
 // the level-0 residual / smoothing products follow the PCG's SpMV kind (1: 4 CTAs per SM,
 // 2: 5, 0: the warp-row kernels k_amg_res<3> / k_amg_post<3>); set up outside graph capture
@@ -963,7 +988,7 @@ static void amg_numeric(lmtg_ctx *c) {
         LMTG_CUDA(cudaGetLastError());
         c->launches += 2;
     }
-    // smoother weights: omega = 1 / theta of a degree-1 Chebyshev on [lmax/30, 1.1 lmax]
+    // smoother weights: omega = 1 / theta of a degree-1 Chebyshev on [h/30, h], h = 1.2 lmax
     PcgScalars *o = c->scal.p + 1;
     double *out2 = reinterpret_cast<double *>(&o->pq);  // pq, rr: two doubles of the outer slot
     for (size_t l = 0; l + 1 < nl; ++l) {
@@ -979,7 +1004,7 @@ static void amg_numeric(lmtg_ctx *c) {
         float scale = 1.f;
         const bool bulk = l == 0 && spmv_kind_in_use(c) != 0;
         if (bulk) bulk0_setup(c);
-        for (int it = 0; it < 8; ++it) {
+        for (int it = 0; it < 12; ++it) {
             float *v = (it & 1) ? L.xb.p : L.xa.p, *w = (it & 1) ? L.xa.p : L.xb.p;
             if (it > 0) k_amg_scale<<<grid_for(c, nv, 256), 256, 0, s>>>(v, v, scale, nv);
             const int g = grid_for(c, L.nn * 32, kRowThreads, 8);
@@ -996,7 +1021,7 @@ static void amg_numeric(lmtg_ctx *c) {
             if (it > 0) lam = std::sqrt(h[0]);
             scale = h[0] > 0 ? (float)(1.0 / std::sqrt(h[0])) : 1.f;
         }
-        const double hi = 1.1 * lam, lo = hi / 30.0;
+        const double hi = 1.2 * lam, lo = hi / 30.0;
         L.lambda = lam;
         L.omega = lam > 0 ? (float)(2.0 / (hi + lo)) : 1.f;
     }
@@ -1089,21 +1114,20 @@ void amg_launch_cycle(lmtg_ctx *c, const float *r, float *z, cudaStream_t s, int
         const uint32_t *bp = l == 0 ? c->bptr.p : L.bptr.p, *bc = l == 0 ? c->bcol.p : L.bcol.p;
         const float *K = l == 0 ? c->K32.p : L.K.p;
         const int g = grid_for(c, L.nn * 32, kRowThreads, 8);
-        if (l > 0) {
-            k_amg_bj6<<<grid_for(c, 6 * L.nn, 256), 256, 0, s>>>(L.Dinv.p, rl, L.xa.p, L.omega, L.nn, S);
-            c->launches += 1;
-        }
+        // the next level's first smoothing step rides on the restriction (not on the coarsest)
+        const bool ncoarsest = l + 2 == nl;
+        const float *Dn = ncoarsest ? nullptr : N.Dinv.p;
         if (L.b == 3) {
             if (warp_rows) k_amg_res<3><<<g, kRowThreads, 0, s>>>(bp, bc, K, L.xa.p, rl, L.res.p, L.nn, S);
             else bulk0_launch(c, L.xa.p, EpiRes{rl, L.res.p}, s);
             mark(0);
-            k_amg_restrict<3><<<grid_for(c, L.nagg * 32, kRowThreads, 8), kRowThreads, 0, s>>>(L.aptr.p, L.anode.p, L.Q.p,
-                                                                                            L.res.p, N.r.p, L.nagg, S);
+            k_amg_restrict<3><<<grid_for(c, L.nagg * 32, kRowThreads, 8), kRowThreads, 0, s>>>(
+                L.aptr.p, L.anode.p, L.Q.p, L.res.p, N.r.p, L.nagg, Dn, N.omega, N.xa.p, S);
             mark(1);
         } else {
             k_amg_res<6><<<g, kRowThreads, 0, s>>>(bp, bc, K, L.xa.p, rl, L.res.p, L.nn, S);
-            k_amg_restrict<6><<<grid_for(c, L.nagg * 32, kRowThreads, 8), kRowThreads, 0, s>>>(L.aptr.p, L.anode.p, L.Q.p,
-                                                                                            L.res.p, N.r.p, L.nagg, S);
+            k_amg_restrict<6><<<grid_for(c, L.nagg * 32, kRowThreads, 8), kRowThreads, 0, s>>>(
+                L.aptr.p, L.anode.p, L.Q.p, L.res.p, N.r.p, L.nagg, Dn, N.omega, N.xa.p, S);
         }
         c->launches += 2;
     }

@@ -120,15 +120,19 @@ constexpr size_t bulk_smem_bytes() {
     return (size_t)kStages * BulkStage<kCap>::kBytes;
 }
 
-// Row epilogues of the bulk-copy SpMV.  row() receives the row sums in the reduce_scatter3
-// layout (lane 8c holds component c of row I; every lane of the warp calls it) and may add to
-// the thread's partial `acc`; with kReduce the partials are reduced over the grid on ticket()
-// and final() runs once with the total.
+// Row epilogues of the bulk-copy SpMV.  pre() loads what the epilogue of row I needs before the
+// row's products (its loads then overlap the gathers); row() receives the row sums in the
+// reduce_scatter3 layout (lane 8c holds component c of row I; every lane of the warp calls it)
+// and may add to the thread's partial `acc`; with kReduce the partials are reduced over the grid
+// on ticket() and final() runs once with the total.
 //   EpiPcg   q = K p and p.q -> pq, alpha (the PCG's SpMV)
 struct EpiPcg {
     float *q;
     static constexpr bool kReduce = true;
-    __device__ __forceinline__ void row(uint64_t I, float qi, int lane, const float *__restrict__ p, float &acc) const {
+    struct Pre {};
+    __device__ __forceinline__ Pre pre(uint64_t, int, const float *) const { return {}; }
+    __device__ __forceinline__ void row(uint64_t I, float qi, int lane, const float *__restrict__ p, float &acc,
+                                        const Pre &) const {
         if ((lane & 7) == 0 && lane < 24) {
             q[3 * I + (lane >> 3)] = qi;
             acc = fmaf(p[4 * I + (lane >> 3)], qi, acc);
@@ -244,7 +248,8 @@ __global__ void __launch_bounds__(bulk_threads<kCons>(), kMinBlocks)
     } else {
         // ---------------- consumers ----------------
         auto xnode = [&](uint64_t J, float &a, float &b, float &c) { NodeVec<float, VS>::load(p, J, a, b, c); };
-        auto finish = [&](uint64_t I, float qi) { epi.row(I, qi, lane, p, acc); };
+        using Pre = typename Epi::Pre;
+        auto finish = [&](uint64_t I, float qi, const Pre &pr) { epi.row(I, qi, lane, p, acc, pr); };
         for (uint32_t k = 0;; ++k) {
             const int slot = k % kStages;
             const bool ok = bulk::mbar_wait(&full[slot], (k / kStages) & 1u);  // every lane acquires
@@ -265,6 +270,7 @@ __global__ void __launch_bounds__(bulk_threads<kCons>(), kMinBlocks)
                 const uint32_t rb0 = sbp[slot][li], re0 = sbp[slot][li + 1];
                 const uint32_t rb1 = has1 ? re0 : 0u, re1 = has1 ? sbp[slot][li + 2] : 0u;
                 const uint32_t d0 = re0 - rb0, d1 = re1 - rb1;
+                const Pre pre0 = epi.pre(I, lane, p), pre1 = has1 ? epi.pre(I + 1, lane, p) : Pre{};
                 if (d0 <= 32 && d1 <= 32) {
                     float m0[9], m1[9];
                     const bool on0 = (uint32_t)lane < d0, on1 = (uint32_t)lane < d1;
@@ -286,8 +292,8 @@ __global__ void __launch_bounds__(bulk_threads<kCons>(), kMinBlocks)
                     block_fma(m1, x10, x11, x12, a10, a11, a12);
                     const float q0 = reduce_scatter3(a00, a01, a02, lane);
                     const float q1 = reduce_scatter3(a10, a11, a12, lane);
-                    finish(I, q0);
-                    if (has1) finish(I + 1, q1);
+                    finish(I, q0, pre0);
+                    if (has1) finish(I + 1, q1, pre1);
                 } else if (d0 + d1 <= 96) {
                     // a wide pair (a Tetra10 vertex row of 65 blocks and its neighbour): the two
                     // rows' blocks as one list, lane l taking blocks l, l + 32, l + 64, so that
@@ -325,8 +331,8 @@ __global__ void __launch_bounds__(bulk_threads<kCons>(), kMinBlocks)
                     }
                     const float q0 = reduce_scatter3(a00, a01, a02, lane);
                     const float q1 = reduce_scatter3(a10, a11, a12, lane);
-                    finish(I, q0);
-                    if (has1) finish(I + 1, q1);
+                    finish(I, q0, pre0);
+                    if (has1) finish(I + 1, q1, pre1);
                 } else {
                     for (int r = 0; r < (has1 ? 2 : 1); ++r) {
                         const uint32_t rb = r ? rb1 : rb0, d = r ? d1 : d0;
@@ -361,7 +367,7 @@ __global__ void __launch_bounds__(bulk_threads<kCons>(), kMinBlocks)
                                 block_fma(m, x0, x1, x2, a0, a1, a2);
                             }
                         }
-                        finish(I + r, reduce_scatter3(a0, a1, a2, lane));
+                        finish(I + r, reduce_scatter3(a0, a1, a2, lane), r ? pre1 : pre0);
                     }
                 }
             }
