@@ -50,6 +50,8 @@ namespace {
 constexpr uint32_t kNone = 0xffffffffu;
 constexpr int kMaxLevels = 8;
 constexpr uint64_t kCoarsestDofs = 300;
+// the coarse correction is scaled by this factor (over-correction of unsmoothed aggregation)
+constexpr float kCoarseScale = 1.5f;
 
 // planar 6x6 block rows: component v (row-major) of local block b of a row starting at block rb
 __host__ __device__ __forceinline__ uint64_t kidx6(uint32_t rb, uint32_t deg, uint32_t b, int v) {
@@ -359,7 +361,7 @@ __global__ void k_amg_prolong(const uint32_t *__restrict__ agg, const float *__r
         float s = 0.f;
 #pragma unroll
         for (int c = 0; c < 6; ++c) s = fmaf(q[c], ev[c], s);
-        x[(uint64_t)VS * i + r] += s;
+        x[(uint64_t)VS * i + r] += kCoarseScale * s;
     }
 }
 
