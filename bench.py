@@ -65,7 +65,7 @@ def parse():
     p.add_argument("--ckpt", type=int, default=10, help="checkpoint interval (transient mode)")
     p.add_argument("--nsys", type=int, default=256, help="meshes in the batch (batch mode)")
     p.add_argument("--mode", default="bench", choices=["bench", "profile", "solve", "adjoint", "transient", "batch"],
-                   help="profile: time the PCG kernels once on --side (small ncu case); "
+                   help="profile: time the PCG and multigrid kernels once on --side, outside graphs (small ncu case); "
                         "solve: one assemble + mixed solve at --tol (launch-list case)")
     p.add_argument("--tol", type=float, default=1e-10)
     return p.parse_args()
@@ -443,6 +443,7 @@ def run_small(args):
         f.assemble(True, True, mixed=True)
         out["spmv32_ms"], out["upd32_ms"] = f.profile_pcg_kernels(precision=1, iters=5)
         out["spmv64_ms"], out["upd64_ms"] = f.profile_pcg_kernels(precision=0, iters=3)
+        out["amg_stage_ms"] = f.profile_amg_kernels(iters=3)  # the multigrid's stages, outside graphs
     else:
         out["stats"] = one_solve(f, "mixed", args.tol)
     out["launches"] = f.launch_count()
