@@ -17,9 +17,8 @@
 //             the coarse modes R at deeper levels) orthonormalised per aggregate (Gram-Schmidt in
 //             FP64); a mode that the aggregate cannot carry (one node, or nodes on a line) gives a
 //             zero column, and the coarse unknown it would define is a decoupled unit diagonal.
-//   K_{l+1}   = Q_l^T K_l Q_l (Galerkin), 6x6 blocks, through gather lists: for every coarse block
-//             the level-l blocks that sum into it, in a fixed order (one warp per coarse block,
-//             no atomics, deterministic).
+//   K_{l+1}   = Q_l^T K_l Q_l (Galerkin), 6x6 blocks: one warp per aggregate streams its nodes'
+//             rows and sums every coarse entry in one fixed order (no atomics, deterministic).
 //   coarsest  (<= 300 unknowns): a dense inverse, computed on the host in FP64, applied in FP32.
 // Numeric setup after every matrix assembly: the Galerkin products, the 6x6 block-Jacobi
 // inverses, and per level the damped-Jacobi weight omega = 1.47 / lambda_max(D^-1 K) (lambda_max by
@@ -69,73 +68,106 @@ __device__ __forceinline__ bool done(const PcgScalars *S) { return S && *(volati
 // numeric setup kernels
 // ---------------------------------------------------------------------------------------------
 
-// Coarse block (I, J) = sum over its gather list of Q_i^T K_ij Q_j.  One warp per coarse block,
-// its lanes over the list (g[2e] = fine block index, g[2e+1] = its fine row), then a butterfly sum
-// of the 36 values (fixed order: deterministic).  A coarse diagonal entry that sums to exactly
-// zero (a mode the aggregate cannot carry) becomes 1, a decoupled unknown.
+// Coarse row I of Q^T K Q, one warp per aggregate I.  The warp takes the fine blocks of the
+// aggregate's rows 32 at a time (lane = block; aggregate-node order, then row order); each lane
+// forms its block's 6x6 product Q_i^T K_ij Q_j and its slot in the coarse row (the position of
+// agg(j) among the row's sorted columns) and stages them in shared memory; then the staged
+// products are added to the row's accumulator in lane order, the lanes splitting the 36 entries.
+// Every coarse entry is summed in one fixed order (deterministic, no atomics).  A coarse diagonal entry that sums to
+// exactly zero (a mode the aggregate cannot carry) becomes 1, a decoupled unknown.
+constexpr int kGalMaxDeg = 128;  // widest coarse row the shared accumulator may hold
+constexpr int kGalWarps = 8;
+// shared memory of one warp for coarse rows of at most cap blocks: acc[cap][36], stage[32][36], slot[32]
+__host__ __device__ constexpr size_t gal_warp_bytes(int cap) { return 4u * (36u * cap + 36u * 32u + 32u); }
+
 template <int B>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(32 * kGalWarps)
     k_galerkin(const uint32_t *__restrict__ fbptr, const uint32_t *__restrict__ fbcol, const float *__restrict__ fK,
+               const uint32_t *__restrict__ agg, const uint32_t *__restrict__ aptr, const uint32_t *__restrict__ anode,
                const float *__restrict__ Q, const uint32_t *__restrict__ cbptr, const uint32_t *__restrict__ cbcol,
-               uint64_t cnn, const uint32_t *__restrict__ gptr, const uint32_t *__restrict__ gsrc,
-               float *__restrict__ cK) {
-    const uint64_t nb = cbptr[cnn];
+               uint64_t na, int cap, float *__restrict__ cK) {
+    extern __shared__ __align__(16) unsigned char gal_raw[];
+    float *wbase = reinterpret_cast<float *>(gal_raw + (threadIdx.x >> 5) * gal_warp_bytes(cap));
+    float(*acc)[36] = reinterpret_cast<float(*)[36]>(wbase);
+    float(*stage)[36] = reinterpret_cast<float(*)[36]>(wbase + 36 * cap);
+    int *slots = reinterpret_cast<int *>(wbase + 36 * cap + 36 * 32);
     const int lane = threadIdx.x & 31;
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    for (uint64_t cb = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; cb < nb; cb += nw) {
-        float C[36];
+    for (uint64_t a = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; a < na; a += nw) {
+        const uint32_t crb = cbptr[a], cdeg = cbptr[a + 1] - crb;
+        const uint32_t *crow = cbcol + crb;
+        for (uint32_t t = lane; t < cdeg * 36; t += 32) (&acc[0][0])[t] = 0.f;
+        __syncwarp();
+        for (uint32_t u = aptr[a]; u < aptr[a + 1]; ++u) {
+            const uint32_t i = anode[u];
+            const uint32_t rb = fbptr[i], deg = fbptr[i + 1] - rb;
+            const float *Qi = Q + (uint64_t)i * B * 6;
+            for (uint32_t c0 = 0; c0 < deg; c0 += 32) {
+                const uint32_t bl = c0 + lane;
+                int slot = -1;
+                if (bl < deg) {
+                    const uint32_t j = fbcol[rb + bl], J = agg[j];
+                    if (J != kNone) {
+                        uint32_t lo = 0, hi = cdeg;  // J is in the row: lower_bound finds it
+                        while (lo < hi) {
+                            const uint32_t mid = (lo + hi) >> 1;
+                            if (crow[mid] < J) lo = mid + 1;
+                            else hi = mid;
+                        }
+                        slot = (int)lo;
+                        float A[B * B];
 #pragma unroll
-        for (int v = 0; v < 36; ++v) C[v] = 0.f;
-        for (uint32_t e = gptr[cb] + lane; e < gptr[cb + 1]; e += 32) {
-            const uint32_t k = gsrc[2 * (uint64_t)e], i = gsrc[2 * (uint64_t)e + 1];
-            const uint32_t rb = fbptr[i], deg = fbptr[i + 1] - rb, j = fbcol[k];
-            float A[B * B];
+                        for (int v = 0; v < B * B; ++v) A[v] = fK[kidxb<B>(rb, deg, bl, v)];
+                        const float *Qj = Q + (uint64_t)j * B * 6;
+                        float T[B * 6];  // A Q_j
 #pragma unroll
-            for (int v = 0; v < B * B; ++v) A[v] = fK[kidxb<B>(rb, deg, k - rb, v)];
-            const float *Qi = Q + (uint64_t)i * B * 6, *Qj = Q + (uint64_t)j * B * 6;
-            float T[B * 6];  // A Q_j
+                        for (int r = 0; r < B; ++r)
 #pragma unroll
-            for (int r = 0; r < B; ++r)
+                            for (int c = 0; c < 6; ++c) {
+                                float s = 0.f;
 #pragma unroll
-                for (int c = 0; c < 6; ++c) {
-                    float s = 0.f;
+                                for (int m = 0; m < B; ++m) s = fmaf(A[r * B + m], __ldg(Qj + m * 6 + c), s);
+                                T[r * 6 + c] = s;
+                            }
+                        float C[36];
 #pragma unroll
-                    for (int m = 0; m < B; ++m) s = fmaf(A[r * B + m], __ldg(Qj + m * 6 + c), s);
-                    T[r * 6 + c] = s;
+                        for (int v = 0; v < 36; ++v) C[v] = 0.f;
+#pragma unroll
+                        for (int r = 0; r < B; ++r) {
+                            float q[6];
+#pragma unroll
+                            for (int x = 0; x < 6; ++x) q[x] = __ldg(Qi + r * 6 + x);
+#pragma unroll
+                            for (int x = 0; x < 6; ++x)
+#pragma unroll
+                                for (int c = 0; c < 6; ++c) C[x * 6 + c] = fmaf(q[x], T[r * 6 + c], C[x * 6 + c]);
+                        }
+#pragma unroll
+                        for (int v = 0; v < 36; ++v) stage[lane][v] = C[v];
+                    }
                 }
-#pragma unroll
-            for (int r = 0; r < B; ++r) {
-                float q[6];
-#pragma unroll
-                for (int a = 0; a < 6; ++a) q[a] = __ldg(Qi + r * 6 + a);
-#pragma unroll
-                for (int a = 0; a < 6; ++a)
-#pragma unroll
-                    for (int c = 0; c < 6; ++c) C[a * 6 + c] = fmaf(q[a], T[r * 6 + c], C[a * 6 + c]);
+                slots[lane] = slot;
+                __syncwarp();
+                // staged products added in lane order, the 36 entries of each by the warp's lanes
+                const int nl = min(32u, deg - c0);
+                for (int l = 0; l < nl; ++l) {
+                    const int sl = slots[l];
+                    if (sl >= 0) {
+                        acc[sl][lane] += stage[l][lane];
+                        if (lane < 4) acc[sl][32 + lane] += stage[l][32 + lane];
+                    }
+                }
+                __syncwarp();
             }
         }
-#pragma unroll
-        for (int v = 0; v < 36; ++v) C[v] = warp_sum(C[v]);
-        // row of this coarse block (binary search on cbptr) to place it in the planar layout
-        uint64_t lo = 0, hi = cnn;
-        while (hi - lo > 1) {
-            const uint64_t mid = (lo + hi) / 2;
-            if (cbptr[mid] <= cb) lo = mid;
-            else hi = mid;
+        for (uint32_t t = lane; t < cdeg * 36; t += 32) {
+            const uint32_t sl = t / 36;
+            const int v = (int)(t - 36 * sl);
+            float x = acc[sl][v];
+            if (crow[sl] == a && v % 7 == 0 && x == 0.f) x = 1.f;
+            cK[kidx6(crb, cdeg, sl, v)] = x;
         }
-        const uint32_t rb = cbptr[lo], deg = cbptr[lo + 1] - rb;
-        if (cbcol[cb] == lo)
-#pragma unroll
-            for (int a = 0; a < 6; ++a)
-                if (C[a * 7] == 0.f) C[a * 7] = 1.f;
-        // lane v writes value v (and lanes 0..3 also value 32 + lane)
-        float mine = C[0], extra = C[32];
-#pragma unroll
-        for (int v = 1; v < 32; ++v) mine = lane == v ? C[v] : mine;
-#pragma unroll
-        for (int v = 33; v < 36; ++v) extra = lane == v - 32 ? C[v] : extra;
-        cK[kidx6(rb, deg, (uint32_t)(cb - rb), lane)] = mine;
-        if (lane < 4) cK[kidx6(rb, deg, (uint32_t)(cb - rb), 32 + lane)] = extra;
+        __syncwarp();
     }
 }
 
@@ -731,95 +763,50 @@ static void tentative(int b, uint64_t na, const std::vector<uint32_t> &aptr, con
     });
 }
 
-// Coarse pattern (sorted distinct aggregate columns per aggregate row) and the Galerkin gather
-// lists (fine block, fine row) per coarse block, in the order aggregate nodes x row blocks.
+// Coarse pattern: the sorted distinct aggregate columns of every aggregate row.
 static void coarse_pattern(uint64_t na, const std::vector<uint32_t> &aptr, const std::vector<uint32_t> &anode,
                            const std::vector<uint32_t> &fbptr, const HBuf<uint32_t> &fbcol,
                            const std::vector<uint32_t> &agg, std::vector<uint32_t> &cbptr, HBuf<uint32_t> &cbcol,
-                           std::vector<uint32_t> &cbdiag, HBuf<uint32_t> &gptr, HBuf<uint32_t> &gsrc) {
+                           std::vector<uint32_t> &cbdiag) {
     const unsigned nt = host_threads();
-    // pass 1 (per thread): each aggregate's sorted distinct columns and per-column entry counts
-    struct Arena {
-        std::vector<uint32_t> cols, cnt;
-    };
-    std::vector<Arena> arena(nt);
-    std::vector<uint32_t> cdeg(na), cnt(na);
+    std::vector<std::vector<uint32_t>> arena(nt);  // per thread: its aggregates' columns, in order
+    std::vector<uint32_t> cdeg(na);
     std::vector<uint64_t> aoff(na);
     parallel_ranges(na, [&](uint64_t a0, uint64_t a1, unsigned t) {
-        Arena &ar = arena[t];
+        std::vector<uint32_t> &ar = arena[t];
         std::vector<uint32_t> mark(na, kNone), cols;
         for (uint64_t a = a0; a < a1; ++a) {
             cols.clear();
-            uint32_t e = 0;
             for (uint32_t u = aptr[a]; u < aptr[a + 1]; ++u) {
                 const uint32_t i = anode[u];
                 for (uint32_t k = fbptr[i]; k < fbptr[i + 1]; ++k) {
                     const uint32_t J = agg[fbcol[k]];
-                    if (J == kNone) continue;
-                    ++e;
-                    if (mark[J] != (uint32_t)a) {
+                    if (J != kNone && mark[J] != (uint32_t)a) {
                         mark[J] = (uint32_t)a;
                         cols.push_back(J);
                     }
                 }
             }
             std::sort(cols.begin(), cols.end());
-            aoff[a] = ar.cols.size();
+            aoff[a] = ar.size();
             cdeg[a] = (uint32_t)cols.size();
-            cnt[a] = e;
-            ar.cols.insert(ar.cols.end(), cols.begin(), cols.end());
-            ar.cnt.resize(ar.cols.size(), 0);
-            uint32_t *sc = ar.cnt.data() + aoff[a];
-            for (uint32_t u = aptr[a]; u < aptr[a + 1]; ++u) {
-                const uint32_t i = anode[u];
-                for (uint32_t k = fbptr[i]; k < fbptr[i + 1]; ++k) {
-                    const uint32_t J = agg[fbcol[k]];
-                    if (J != kNone) ++sc[std::lower_bound(cols.begin(), cols.end(), J) - cols.begin()];
-                }
-            }
+            ar.insert(ar.end(), cols.begin(), cols.end());
         }
     });
     cbptr.assign(na + 1, 0);
-    std::vector<uint64_t> eoff(na + 1, 0);
-    for (uint64_t a = 0; a < na; ++a) {
-        cbptr[a + 1] = cbptr[a] + cdeg[a];
-        eoff[a + 1] = eoff[a] + cnt[a];
-    }
-    if (eoff[na] >= (1ull << 32)) throw Error{LMTG_ERR_UNSUPPORTED, "amg: Galerkin lists over 2^32 entries"};
+    for (uint64_t a = 0; a < na; ++a) cbptr[a + 1] = cbptr[a] + cdeg[a];
     cbcol.alloc(cbptr[na] + 4);
     for (int k = 0; k < 4; ++k) cbcol[cbptr[na] + k] = 0;
     cbdiag.assign(na, 0);
-    gptr.alloc(cbptr[na] + 1);
-    gsrc.alloc(2 * eoff[na]);
-    // pass 2: columns, gather-list offsets and the gather lists themselves
     parallel_ranges(na, [&](uint64_t a0, uint64_t a1, unsigned t) {
-        const Arena &ar = arena[t];
-        std::vector<uint32_t> slotpos;
-        for (uint64_t a = a0; a < a1; ++a) {
-            const uint32_t *cols = ar.cols.data() + aoff[a], *sc = ar.cnt.data() + aoff[a];
-            const uint32_t rb = cbptr[a], deg = cdeg[a];
-            slotpos.resize(deg);
-            uint64_t off = eoff[a];
-            for (uint32_t u = 0; u < deg; ++u) {
-                cbcol[rb + u] = cols[u];
-                if (cols[u] == a) cbdiag[a] = rb + u;
-                gptr[rb + u] = (uint32_t)off;
-                slotpos[u] = (uint32_t)off;
-                off += sc[u];
+        const std::vector<uint32_t> &ar = arena[t];
+        for (uint64_t a = a0; a < a1; ++a)
+            for (uint32_t u = 0; u < cdeg[a]; ++u) {
+                const uint32_t J = ar[aoff[a] + u];
+                cbcol[cbptr[a] + u] = J;
+                if (J == a) cbdiag[a] = cbptr[a] + u;
             }
-            for (uint32_t u = aptr[a]; u < aptr[a + 1]; ++u) {
-                const uint32_t i = anode[u];
-                for (uint32_t k = fbptr[i]; k < fbptr[i + 1]; ++k) {
-                    const uint32_t J = agg[fbcol[k]];
-                    if (J == kNone) continue;
-                    const uint32_t p = slotpos[std::lower_bound(cols, cols + deg, J) - cols]++;
-                    gsrc[2 * (uint64_t)p] = k;
-                    gsrc[2 * (uint64_t)p + 1] = i;
-                }
-            }
-        }
     });
-    gptr[cbptr[na]] = (uint32_t)eoff[na];
 }
 
 template <class T>
@@ -941,16 +928,14 @@ static void amg_build_structure(lmtg_ctx *c) {
         HostLevel nxt;
         nxt.b = 6;
         nxt.nn = na;
-        HBuf<uint32_t> gptr, gsrc;
-        coarse_pattern(na, aptr, anode, cur.bptr, cur.bcol, agg, nxt.bptr, nxt.bcol, nxt.bdiag, gptr, gsrc);
+        coarse_pattern(na, aptr, anode, cur.bptr, cur.bcol, agg, nxt.bptr, nxt.bcol, nxt.bdiag);
+        for (uint64_t a = 0; a < na; ++a) A->max_cdeg = std::max<uint32_t>(A->max_cdeg, nxt.bptr[a + 1] - nxt.bptr[a]);
         phase(3);
         L->nagg = na;
         upload(L->agg, agg, s);
         upload(L->aptr, aptr, s);
         upload(L->anode, anode, s);
         upload(L->Q, Q, s);
-        upload(L->gptr, gptr, s);
-        upload(L->gsrc, gsrc, s);
         LMTG_CUDA(cudaStreamSynchronize(s));
         phase(4);
         A->levels.push_back(std::move(L));
@@ -961,7 +946,12 @@ static void amg_build_structure(lmtg_ctx *c) {
     // coarsest level too large for a dense inverse
     AmgLevel &C = *A->levels.back();
     const uint64_t nc = (uint64_t)C.b * C.nn;
-    A->nc = (A->levels.size() > 1 && nc <= 2000) ? (int)nc : 0;
+    A->nc = (A->levels.size() > 1 && nc <= 2000 && A->max_cdeg <= (uint32_t)kGalMaxDeg) ? (int)nc : 0;
+    if (A->nc) {
+        const int smem = (int)(kGalWarps * gal_warp_bytes((int)((A->max_cdeg + 7) & ~7u)));
+        LMTG_CUDA(cudaFuncSetAttribute(k_galerkin<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        LMTG_CUDA(cudaFuncSetAttribute(k_galerkin<6>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    }
     if (A->nc) A->Cinv.alloc((size_t)A->nc * A->nc);
     A->structure_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     c->amg = A.release();
@@ -980,12 +970,15 @@ static void amg_numeric(lmtg_ctx *c) {
         const uint32_t *fbptr = l == 0 ? c->bptr.p : F.bptr.p;
         const uint32_t *fbcol = l == 0 ? c->bcol.p : F.bcol.p;
         const float *fK = l == 0 ? c->K32.p : F.K.p;
-        const uint64_t ncb = C.nnzb;
-        const int g = grid_for(c, ncb * 32, 256, 8);
+        const int cap = (int)((A.max_cdeg + 7) & ~7u);
+        const size_t smem = kGalWarps * gal_warp_bytes(cap);
+        const int g = grid_for(c, F.nagg * 32, 32 * kGalWarps, 8);
         if (F.b == 3)
-            k_galerkin<3><<<g, 256, 0, s>>>(fbptr, fbcol, fK, F.Q.p, C.bptr.p, C.bcol.p, C.nn, F.gptr.p, F.gsrc.p, C.K.p);
+            k_galerkin<3><<<g, 32 * kGalWarps, smem, s>>>(fbptr, fbcol, fK, F.agg.p, F.aptr.p, F.anode.p, F.Q.p, C.bptr.p,
+                                                          C.bcol.p, F.nagg, cap, C.K.p);
         else
-            k_galerkin<6><<<g, 256, 0, s>>>(fbptr, fbcol, fK, F.Q.p, C.bptr.p, C.bcol.p, C.nn, F.gptr.p, F.gsrc.p, C.K.p);
+            k_galerkin<6><<<g, 32 * kGalWarps, smem, s>>>(fbptr, fbcol, fK, F.agg.p, F.aptr.p, F.anode.p, F.Q.p, C.bptr.p,
+                                                          C.bcol.p, F.nagg, cap, C.K.p);
         k_block_inv6<<<grid_for(c, C.nn, 128), 128, 0, s>>>(C.bptr.p, C.bdiag.p, C.K.p, C.nn, C.Dinv.p);
         LMTG_CUDA(cudaGetLastError());
         c->launches += 2;

@@ -24,7 +24,6 @@ struct AmgLevel {
     DBuf<uint32_t> agg;          // node -> aggregate (0xffffffff: in none)
     DBuf<uint32_t> aptr, anode;  // aggregate -> nodes
     DBuf<float> Q;               // tentative prolongator, b x 6 per node (row-major)
-    DBuf<uint32_t> gptr, gsrc;   // coarse block -> (fine block, fine row) pairs
 };
 
 struct AmgState {
@@ -32,6 +31,7 @@ struct AmgState {
     int nc = 0;             // unknowns of the dense coarsest level (0: no hierarchy)
     DBuf<float> Cinv;       // its inverse, row-major
     uint64_t version = ~0ull;  // matrix version of the numeric setup
+    uint32_t max_cdeg = 0;     // widest coarse row over the levels
     double structure_ms = 0, numeric_ms = 0;
     // host time of the structure setup by phase: pattern copy and modes, aggregation, tentative
     // prolongators, coarse patterns and gather lists, uploads
