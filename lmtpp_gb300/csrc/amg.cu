@@ -171,6 +171,101 @@ __global__ void __launch_bounds__(32 * kGalWarps)
     }
 }
 
+// Tentative prolongator of one level on the device, one warp per aggregate: the aggregate's
+// modes (level 0: translations and rotations about `cen` from the node positions; deeper: the
+// previous level's coarse modes Bf, 6 x 6 per node) as a rows x 6 matrix, rows spread over the
+// lanes (row lane + 32 k), orthonormalised by Gram-Schmidt twice in FP64 with warp sums; a column
+// that falls below 1e-10 of its original norm is dropped (zero).  Writes Q (b x 6 per node, FP32)
+// and the coarse modes Bc = R (6 x 6 per aggregate).  rows <= 32 kTentRows (checked on the host).
+constexpr int kTentRows = 10;
+template <int B>
+__global__ void __launch_bounds__(128)
+    k_tentative(const uint32_t *__restrict__ aptr, const uint32_t *__restrict__ anode, uint64_t na,
+                const double *__restrict__ pos, double cx, double cy, double cz, const double *__restrict__ Bf,
+                float *__restrict__ Q, double *__restrict__ Bc) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t a = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; a < na; a += nw) {
+        const uint32_t n0 = aptr[a], rows = (aptr[a + 1] - n0) * B;
+        double M[kTentRows][6];
+#pragma unroll
+        for (int k = 0; k < kTentRows; ++k) {
+            const uint32_t r = lane + 32 * k;
+#pragma unroll
+            for (int c = 0; c < 6; ++c) M[k][c] = 0.0;
+            if (r < rows) {
+                const uint32_t i = anode[n0 + r / B];
+                const int rr = (int)(r % B);
+                if (B == 3) {
+                    const double x = pos[3 * (uint64_t)i] - cx, y = pos[3 * (uint64_t)i + 1] - cy,
+                                 z = pos[3 * (uint64_t)i + 2] - cz;
+                    // columns: translations x, y, z, rotations about z, x, y
+                    M[k][rr] = 1.0;
+                    M[k][3] = rr == 0 ? -y : (rr == 1 ? x : 0.0);
+                    M[k][4] = rr == 1 ? -z : (rr == 2 ? y : 0.0);
+                    M[k][5] = rr == 0 ? z : (rr == 2 ? -x : 0.0);
+                } else {
+#pragma unroll
+                    for (int c = 0; c < 6; ++c) M[k][c] = Bf[36 * (uint64_t)i + 6 * rr + c];
+                }
+            }
+        }
+        double R[6][6];
+#pragma unroll
+        for (int p = 0; p < 6; ++p)
+#pragma unroll
+            for (int c = 0; c < 6; ++c) R[p][c] = 0.0;
+        double norm0[6];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            double t = 0.0;
+#pragma unroll
+            for (int k = 0; k < kTentRows; ++k) t += M[k][c] * M[k][c];
+            norm0[c] = sqrt(warp_sum(t));
+        }
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+#pragma unroll
+            for (int pass = 0; pass < 2; ++pass)
+#pragma unroll
+                for (int p = 0; p < c; ++p) {
+                    double t = 0.0;
+#pragma unroll
+                    for (int k = 0; k < kTentRows; ++k) t += M[k][p] * M[k][c];
+                    t = warp_sum(t);
+                    R[p][c] += t;
+#pragma unroll
+                    for (int k = 0; k < kTentRows; ++k) M[k][c] -= t * M[k][p];
+                }
+            double t = 0.0;
+#pragma unroll
+            for (int k = 0; k < kTentRows; ++k) t += M[k][c] * M[k][c];
+            const double nrm = sqrt(warp_sum(t));
+            const bool drop = nrm <= 1e-10 * norm0[c] || nrm == 0.0;
+            R[c][c] = drop ? 0.0 : nrm;
+            const double inv = drop ? 0.0 : 1.0 / nrm;
+#pragma unroll
+            for (int k = 0; k < kTentRows; ++k) M[k][c] *= inv;
+        }
+#pragma unroll
+        for (int k = 0; k < kTentRows; ++k) {
+            const uint32_t r = lane + 32 * k;
+            if (r < rows) {
+                const uint32_t i = anode[n0 + r / B];
+                const int rr = (int)(r % B);
+#pragma unroll
+                for (int c = 0; c < 6; ++c) Q[((uint64_t)i * B + rr) * 6 + c] = (float)M[k][c];
+            }
+        }
+        for (int v = lane; v < 36; v += 32) {
+            double x = R[0][0];
+#pragma unroll
+            for (int u = 1; u < 36; ++u) x = v == u ? R[u / 6][u % 6] : x;
+            Bc[36 * a + v] = x;
+        }
+    }
+}
+
 // Inverse of every 6x6 diagonal block (Gauss-Jordan with partial pivoting, FP64).
 __global__ void k_block_inv6(const uint32_t *__restrict__ bptr, const uint32_t *__restrict__ bdiag,
                              const float *__restrict__ K, uint64_t nn, float *__restrict__ Dinv) {
@@ -872,7 +967,7 @@ static void amg_build_structure(lmtg_ctx *c) {
                               0, 0, 1, 0, y, -x};
         std::memcpy(m, v, sizeof(v));
     };
-    std::vector<double> Bf;  // modes of the current level (levels >= 1: 6 x 6 per node)
+    DBuf<double> Bf_dev;  // modes of the current level (levels >= 1: 6 x 6 per node), on the device
     phase(0);
     for (int l = 0;; ++l) {
         std::unique_ptr<AmgLevel> L(new AmgLevel());
@@ -914,15 +1009,43 @@ static void amg_build_structure(lmtg_ctx *c) {
             for (uint64_t i = 0; i < cur.nn; ++i)
                 if (agg[i] != kNone) anode[pos[agg[i]]++] = (uint32_t)i;
         }
-        HBuf<float> Q;
-        Q.alloc(cur.nn * cur.b * 6);  // rows of nodes in no aggregate are never read
-        std::vector<double> Bc;
-        if (l == 0) {
-            tentative(3, na, aptr, anode, rigid_modes, Q, Bc);
+        // tentative prolongator: on the device (one warp per aggregate) when every aggregate fits
+        // the kernel's 320 rows, else on the host
+        uint32_t maxm = 0;
+        for (uint64_t a = 0; a < na; ++a) maxm = std::max(maxm, aptr[a + 1] - aptr[a]);
+        upload(L->aptr, aptr, s);
+        upload(L->anode, anode, s);
+        L->Q.alloc(cur.nn * cur.b * 6);  // rows of nodes in no aggregate are never read
+        DBuf<double> Bc_dev;
+        Bc_dev.alloc(na * 36);
+        if ((uint64_t)maxm * cur.b <= 32u * kTentRows) {
+            const int g = grid_for(c, na * 32, 128, 8);
+            if (l == 0)
+                k_tentative<3><<<g, 128, 0, s>>>(L->aptr.p, L->anode.p, na, c->pos.p, cen[0], cen[1], cen[2], nullptr,
+                                                 L->Q.p, Bc_dev.p);
+            else
+                k_tentative<6><<<g, 128, 0, s>>>(L->aptr.p, L->anode.p, na, nullptr, 0, 0, 0, Bf_dev.p, L->Q.p,
+                                                 Bc_dev.p);
+            LMTG_CUDA(cudaGetLastError());
+            c->launches += 1;
         } else {
-            const double *bf = Bf.data();
-            tentative(6, na, aptr, anode, [bf](uint32_t i, double *m) { std::memcpy(m, bf + 36 * (size_t)i, 36 * sizeof(double)); },
-                      Q, Bc);
+            HBuf<float> Q;
+            Q.alloc(cur.nn * cur.b * 6);
+            std::vector<double> Bc;
+            if (l == 0) {
+                tentative(3, na, aptr, anode, rigid_modes, Q, Bc);
+            } else {
+                std::vector<double> Bf(36 * cur.nn);
+                LMTG_CUDA(cudaMemcpyAsync(Bf.data(), Bf_dev.p, Bf.size() * 8, cudaMemcpyDeviceToHost, s));
+                LMTG_CUDA(cudaStreamSynchronize(s));
+                const double *bf = Bf.data();
+                tentative(6, na, aptr, anode,
+                          [bf](uint32_t i, double *m) { std::memcpy(m, bf + 36 * (size_t)i, 36 * sizeof(double)); }, Q,
+                          Bc);
+            }
+            LMTG_CUDA(cudaMemcpyAsync(L->Q.p, Q.data(), Q.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+            LMTG_CUDA(cudaMemcpyAsync(Bc_dev.p, Bc.data(), Bc.size() * 8, cudaMemcpyHostToDevice, s));
+            LMTG_CUDA(cudaStreamSynchronize(s));
         }
         phase(2);
         HostLevel nxt;
@@ -933,13 +1056,11 @@ static void amg_build_structure(lmtg_ctx *c) {
         phase(3);
         L->nagg = na;
         upload(L->agg, agg, s);
-        upload(L->aptr, aptr, s);
-        upload(L->anode, anode, s);
-        upload(L->Q, Q, s);
         LMTG_CUDA(cudaStreamSynchronize(s));
         phase(4);
         A->levels.push_back(std::move(L));
-        Bf.swap(Bc);
+        std::swap(Bf_dev.p, Bc_dev.p);
+        std::swap(Bf_dev.n, Bc_dev.n);
         cur = std::move(nxt);
     }
     // coarsest dense buffers; no hierarchy (block Jacobi instead) with a single level or a
