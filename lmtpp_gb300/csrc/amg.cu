@@ -345,12 +345,14 @@ __device__ __forceinline__ void row6(const uint32_t *__restrict__ bcol, const fl
 // cycle kernels
 // ---------------------------------------------------------------------------------------------
 
-// res = r - K x (r == nullptr: res = -K x), warp per row
+// res = r - K x (r == nullptr: res = -K x), warp per row; with D (6x6 levels), also the first
+// smoothing step of a cycle on that residual, xpre = omega D^-1 res (padded 8)
 template <int B>
 __global__ void __launch_bounds__(kRowThreads)
     k_amg_res(const uint32_t *__restrict__ bptr, const uint32_t *__restrict__ bcol, const float *__restrict__ K,
               const float *__restrict__ x, const float *__restrict__ r, float *__restrict__ res, uint64_t nn,
-              const PcgScalars *S) {
+              const PcgScalars *S, const float *__restrict__ D = nullptr, float omega = 0.f,
+              float *__restrict__ xpre = nullptr) {
     if (done(S)) return;
     const int lane = threadIdx.x & 31;
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -370,6 +372,13 @@ __global__ void __launch_bounds__(kRowThreads)
                 for (int k = 1; k < 6; ++k) v = lane == k ? a[k] : v;
                 const uint64_t i = 6 * I + lane;
                 res[i] = (r ? r[i] : 0.f) - v;
+                if (D) {
+                    const float *Dr = D + 36 * I + 6 * lane;
+                    float xp = 0.f;
+#pragma unroll
+                    for (int k = 0; k < 6; ++k) xp = fmaf(Dr[k], (r ? r[6 * I + k] : 0.f) - a[k], xp);
+                    xpre[8 * I + lane] = omega * xp;
+                }
             }
         }
     }
@@ -471,10 +480,10 @@ __global__ void __launch_bounds__(kRowThreads)
     }
 }
 
-// x += Q e[agg] per node (e with stride ES per coarse node)
+// x += Q (e + e2)[agg] per node (e, e2 with stride ES per coarse node; e2 may be null)
 template <int B, int ES>
 __global__ void k_amg_prolong(const uint32_t *__restrict__ agg, const float *__restrict__ Q, const float *__restrict__ e,
-                              float *__restrict__ x, uint64_t nn, const PcgScalars *S) {
+                              const float *__restrict__ e2, float *__restrict__ x, uint64_t nn, const PcgScalars *S) {
     if (done(S)) return;
     constexpr int VS = B == 3 ? 4 : 8;
     for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < (uint64_t)B * nn;
@@ -486,8 +495,14 @@ __global__ void k_amg_prolong(const uint32_t *__restrict__ agg, const float *__r
         const float *q = Q + (i * B + r) * 6;
         const float *ev = e + (uint64_t)ES * a;
         float s = 0.f;
+        if (e2) {
+            const float *ev2 = e2 + (uint64_t)ES * a;
 #pragma unroll
-        for (int c = 0; c < 6; ++c) s = fmaf(q[c], ev[c], s);
+            for (int c = 0; c < 6; ++c) s = fmaf(q[c], ev[c] + ev2[c], s);
+        } else {
+#pragma unroll
+            for (int c = 0; c < 6; ++c) s = fmaf(q[c], ev[c], s);
+        }
         x[(uint64_t)VS * i + r] += kCoarseScale * s;
     }
 }
@@ -978,6 +993,10 @@ static void amg_build_structure(lmtg_ctx *c) {
         L->xa.alloc(VS * cur.nn);
         L->xb.alloc(VS * cur.nn);
         L->res.alloc(cur.b * cur.nn + 4);
+        if (l == 1) {
+            L->r2.alloc(cur.b * cur.nn + 4);
+            L->xb2.alloc(8 * cur.nn);
+        }
         if (l > 0) {
             L->r.alloc(cur.b * cur.nn + 4);
             upload(L->bptr, cur.bptr, s);
@@ -1210,7 +1229,40 @@ bool amg_prepare(lmtg_ctx *c) {
 float amg_omega0(const lmtg_ctx *c) { return c->amg->levels[0]->omega; }
 float *amg_xa0(const lmtg_ctx *c) { return c->amg->levels[0]->xa.p; }
 
+// Cycle of a level l >= 1 on the right-hand side rhs (packed 6), its first smoothing step
+// already in L.xa (fused into the caller's restriction or residual); the result goes to out
+// (padded 8; packed 6 on the coarsest, the dense solve).
+static void coarse_cycle(lmtg_ctx *c, AmgState &A, size_t l, const float *rhs, float *out, cudaStream_t s,
+                         PcgScalars *S) {
+    const size_t nl = A.levels.size();
+    AmgLevel &L = *A.levels[l];
+    if (l + 1 == nl) {
+        k_amg_dense<<<grid_for(c, (uint64_t)A.nc * 32, 256, 4), 256, 0, s>>>(A.Cinv.p, rhs, out, A.nc, S);
+        c->launches += 1;
+        return;
+    }
+    AmgLevel &N = *A.levels[l + 1];
+    const bool ncoarsest = l + 2 == nl;
+    const int g = grid_for(c, L.nn * 32, kRowThreads, 8);
+    k_amg_res<6><<<g, kRowThreads, 0, s>>>(L.bptr.p, L.bcol.p, L.K.p, L.xa.p, rhs, L.res.p, L.nn, S);
+    k_amg_restrict<6><<<grid_for(c, L.nagg * 32, kRowThreads, 8), kRowThreads, 0, s>>>(
+        L.aptr.p, L.anode.p, L.Q.p, L.res.p, N.r.p, L.nagg, ncoarsest ? nullptr : N.Dinv.p, N.omega, N.xa.p, S);
+    float *e = ncoarsest ? N.res.p : N.xb.p;
+    coarse_cycle(c, A, l + 1, N.r.p, e, s, S);
+    const int tb = 256;
+    if (ncoarsest)
+        k_amg_prolong<6, 6><<<grid_for(c, 6 * L.nn, tb), tb, 0, s>>>(L.agg.p, L.Q.p, e, nullptr, L.xa.p, L.nn, S);
+    else
+        k_amg_prolong<6, 8><<<grid_for(c, 6 * L.nn, tb), tb, 0, s>>>(L.agg.p, L.Q.p, e, nullptr, L.xa.p, L.nn, S);
+    k_amg_post<6><<<g, kRowThreads, 0, s>>>(L.bptr.p, L.bcol.p, L.K.p, L.Dinv.p, L.xa.p, rhs, out, L.omega, L.nn, S,
+                                            false, 0, 0.0, c->partials.p);
+    c->launches += 4;
+}
+
 // The cycle after the update kernel: r (level-0 residual, packed) -> z (padded), rz and beta.
+// Level 0's coarse correction runs level 1's cycle twice (the second on the residual the first
+// leaves): with unsmoothed aggregation this brings the multilevel cycle close to the two-level
+// method's convergence for one more level-1 residual and cycle.
 // ev (profiling only) receives events after the level-0 residual, the level-0 restriction, the
 // coarse levels, the level-0 prolongation and the level-0 smoothing.
 void amg_launch_cycle(lmtg_ctx *c, const float *r, float *z, cudaStream_t s, int start, double beta_den,
@@ -1218,73 +1270,47 @@ void amg_launch_cycle(lmtg_ctx *c, const float *r, float *z, cudaStream_t s, int
     AmgState &A = *c->amg;
     PcgScalars *S = c->scal.p;
     const size_t nl = A.levels.size();
-    const bool warp_rows = spmv_kind_in_use(c) == 0;
+    const bool warp_rows = spmv_kind_in_use(c) == 0;  // the level-0 products follow the PCG's kind
     if (!warp_rows) bulk0_setup(c);
     auto mark = [&](int k) {
         if (ev) LMTG_CUDA(cudaEventRecord(ev[k], s));
     };
-    // down: residual and restriction
-    for (size_t l = 0; l + 1 < nl; ++l) {
-        AmgLevel &L = *A.levels[l], &N = *A.levels[l + 1];
-        const float *rl = l == 0 ? r : L.r.p;
-        const uint32_t *bp = l == 0 ? c->bptr.p : L.bptr.p, *bc = l == 0 ? c->bcol.p : L.bcol.p;
-        const float *K = l == 0 ? c->K32.p : L.K.p;
-        const int g = grid_for(c, L.nn * 32, kRowThreads, 8);
-        // the next level's first smoothing step rides on the restriction (not on the coarsest)
-        const bool ncoarsest = l + 2 == nl;
-        const float *Dn = ncoarsest ? nullptr : N.Dinv.p;
-        if (L.b == 3) {
-            if (warp_rows) k_amg_res<3><<<g, kRowThreads, 0, s>>>(bp, bc, K, L.xa.p, rl, L.res.p, L.nn, S);
-            else bulk0_launch(c, L.xa.p, EpiRes{rl, L.res.p}, s);
-            mark(0);
-            k_amg_restrict<3><<<grid_for(c, L.nagg * 32, kRowThreads, 8), kRowThreads, 0, s>>>(
-                L.aptr.p, L.anode.p, L.Q.p, L.res.p, N.r.p, L.nagg, Dn, N.omega, N.xa.p, S);
-            mark(1);
-        } else {
-            k_amg_res<6><<<g, kRowThreads, 0, s>>>(bp, bc, K, L.xa.p, rl, L.res.p, L.nn, S);
-            k_amg_restrict<6><<<grid_for(c, L.nagg * 32, kRowThreads, 8), kRowThreads, 0, s>>>(
-                L.aptr.p, L.anode.p, L.Q.p, L.res.p, N.r.p, L.nagg, Dn, N.omega, N.xa.p, S);
-        }
-        c->launches += 2;
-    }
-    // coarsest
-    {
-        AmgLevel &C = *A.levels.back();
-        k_amg_dense<<<grid_for(c, (uint64_t)A.nc * 32, 256, 4), 256, 0, s>>>(A.Cinv.p, C.r.p, C.res.p, A.nc, S);
+    AmgLevel &L = *A.levels[0], &N = *A.levels[1];
+    const int g0 = grid_for(c, L.nn * 32, kRowThreads, 8);
+    const bool ncoarsest = nl == 2;
+    // level 0: residual of the first smoothing step (written by the update kernel), restriction
+    // with level 1's first smoothing step
+    if (warp_rows) k_amg_res<3><<<g0, kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, c->K32.p, L.xa.p, r, L.res.p, L.nn, S);
+    else bulk0_launch(c, L.xa.p, EpiRes{r, L.res.p}, s);
+    mark(0);
+    k_amg_restrict<3><<<grid_for(c, L.nagg * 32, kRowThreads, 8), kRowThreads, 0, s>>>(
+        L.aptr.p, L.anode.p, L.Q.p, L.res.p, N.r.p, L.nagg, ncoarsest ? nullptr : N.Dinv.p, N.omega, N.xa.p, S);
+    mark(1);
+    c->launches += 2;
+    float *e = ncoarsest ? N.res.p : N.xb.p, *e2 = nullptr;
+    coarse_cycle(c, A, 1, N.r.p, e, s, S);
+    if (!ncoarsest) {
+        // second level-1 cycle on r1 - K1 e (the residual kernel also forms its first smoothing step)
+        k_amg_res<6><<<grid_for(c, N.nn * 32, kRowThreads, 8), kRowThreads, 0, s>>>(
+            N.bptr.p, N.bcol.p, N.K.p, e, N.r.p, N.r2.p, N.nn, S, N.Dinv.p, N.omega, N.xa.p);
         c->launches += 1;
+        coarse_cycle(c, A, 1, N.r2.p, N.xb2.p, s, S);
+        e2 = N.xb2.p;
     }
-    // up: prolongation and post-smoothing
-    for (size_t l = nl - 1; l-- > 0;) {
-        AmgLevel &L = *A.levels[l], &N = *A.levels[l + 1];
-        const bool ncoarsest = l + 2 == nl;
-        const float *e = ncoarsest ? N.res.p : N.xb.p;
-        const int tb = 256;
-        if (L.b == 3) {
-            mark(2);
-            if (ncoarsest)
-                k_amg_prolong<3, 6><<<grid_for(c, 3 * L.nn, tb), tb, 0, s>>>(L.agg.p, L.Q.p, e, L.xa.p, L.nn, S);
-            else
-                k_amg_prolong<3, 8><<<grid_for(c, 3 * L.nn, tb), tb, 0, s>>>(L.agg.p, L.Q.p, e, L.xa.p, L.nn, S);
-        } else {
-            if (ncoarsest)
-                k_amg_prolong<6, 6><<<grid_for(c, 6 * L.nn, tb), tb, 0, s>>>(L.agg.p, L.Q.p, e, L.xa.p, L.nn, S);
-            else
-                k_amg_prolong<6, 8><<<grid_for(c, 6 * L.nn, tb), tb, 0, s>>>(L.agg.p, L.Q.p, e, L.xa.p, L.nn, S);
-        }
-        const int g = grid_for(c, L.nn * 32, kRowThreads, 8);
-        if (l == 0) {
-            mark(3);
-            if (warp_rows)
-                k_amg_post<3><<<g, kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, c->K32.p, c->Dinv32.p, L.xa.p, r, z,
-                                                        L.omega, L.nn, S, true, start, beta_den, c->partials.p);
-            else
-                bulk0_launch(c, L.xa.p, EpiPost{r, c->Dinv32.p, z, L.omega, start, beta_den}, s);
-            mark(4);
-        } else
-            k_amg_post<6><<<g, kRowThreads, 0, s>>>(L.bptr.p, L.bcol.p, L.K.p, L.Dinv.p, L.xa.p, L.r.p, L.xb.p, L.omega,
-                                                    L.nn, S, false, 0, 0.0, c->partials.p);
-        c->launches += 2;
-    }
+    mark(2);
+    const int tb = 256;
+    if (ncoarsest)
+        k_amg_prolong<3, 6><<<grid_for(c, 3 * L.nn, tb), tb, 0, s>>>(L.agg.p, L.Q.p, e, nullptr, L.xa.p, L.nn, S);
+    else
+        k_amg_prolong<3, 8><<<grid_for(c, 3 * L.nn, tb), tb, 0, s>>>(L.agg.p, L.Q.p, e, e2, L.xa.p, L.nn, S);
+    mark(3);
+    if (warp_rows)
+        k_amg_post<3><<<g0, kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, c->K32.p, c->Dinv32.p, L.xa.p, r, z, L.omega,
+                                                 L.nn, S, true, start, beta_den, c->partials.p);
+    else
+        bulk0_launch(c, L.xa.p, EpiPost{r, c->Dinv32.p, z, L.omega, start, beta_den}, s);
+    mark(4);
+    c->launches += 2;
     LMTG_CUDA(cudaGetLastError());
 }
 

@@ -19,6 +19,7 @@ struct AmgLevel {
     DBuf<float> r;                     // right-hand side (packed b per node), levels >= 1
     DBuf<float> xa, xb;                // iterates, padded to 4 (level 0) or 8 per node
     DBuf<float> res;                   // residual (packed); on the coarsest, its solution
+    DBuf<float> r2, xb2;               // level 1: right-hand side and result of its second cycle
     // transfer to the next coarser level
     uint64_t nagg = 0;
     DBuf<uint32_t> agg;          // node -> aggregate (0xffffffff: in none)
