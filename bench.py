@@ -407,15 +407,20 @@ def stage_bytes(nn, nnzb, amg=None):
          "restrict0": 88 * nn, "prolong0": 108 * nn, "smooth0": base + 64 * nn}
     coarse = 0
     if amg and amg.get("levels", 0) > 1:
+        # Each level's coarse correction runs the next level's cycle twice (once on the dense
+        # coarsest): level l >= 1 is visited 2^l times per iteration.  A visit makes two 6x6-block
+        # passes (residual, smoothing: 144 B values + 4 B column per block) with their block-Jacobi,
+        # restriction and prolongation vectors; between a level's two visits one more residual
+        # pass (with the next first smoothing step) runs, 2^(l-1) times; the dense coarsest reads
+        # its inverse once per visit of the level above.
         nl = amg["levels"]
-        for l in range(1, nl):
+        visits = [1] + [2 ** l for l in range(1, nl - 1)]
+        for l in range(1, nl - 1):
             n6 = amg["ndof"][l] // 6
-            if l == nl - 1:
-                coarse += 4 * amg["ndof"][l] ** 2 + 8 * amg["ndof"][l]  # dense inverse and vectors
-            else:
-                # two 6x6-block passes (residual, smoothing: 144 B values + 4 B column per block),
-                # block-Jacobi, restriction and prolongation vectors
-                coarse += 2 * (148 * amg["nnz_blocks"][l] + 4 * (n6 + 1)) + 400 * n6
+            rows = 148 * amg["nnz_blocks"][l] + 4 * (n6 + 1)
+            coarse += visits[l] * (2 * rows + 400 * n6) + visits[l - 1] * (rows + 256 * n6)
+        nc = amg["ndof"][nl - 1]
+        coarse += visits[nl - 2] * (4 * nc ** 2 + 8 * nc)
     b["coarse"] = coarse
     return b
 

@@ -40,6 +40,7 @@
 #include <vector>
 
 #include "amg.cuh"
+#include "amg_bulk6.cuh"
 #include "spmv_bulk.cuh"
 
 namespace lmtg {
@@ -48,7 +49,9 @@ namespace {
 
 constexpr uint32_t kNone = 0xffffffffu;
 constexpr int kMaxLevels = 8;
+constexpr int kPowerSteps = 12;  // power steps for lambda_max(D^-1 K) per level
 constexpr uint64_t kCoarsestDofs = 300;
+constexpr uint64_t kDenseMaxDofs = 2000;  // largest coarsest level (its dense inverse) accepted
 // the coarse correction is scaled by this factor (over-correction of unsmoothed aggregation)
 constexpr float kCoarseScale = 1.5f;
 
@@ -521,14 +524,23 @@ __global__ void k_amg_dense(const float *__restrict__ Cinv, const float *__restr
     }
 }
 
-// one power step for lambda_max(D^-1 K): w = D^-1 K v (v, w padded); |w|^2 and v.w reduced
+// 1 / |v| from the previous power step's |w|^2 (v is that w), 1 on the first step
+__device__ __forceinline__ float power_scale(const double *prev) {
+    if (!prev) return 1.f;
+    const float p = (float)*prev;
+    return p > 0.f ? rsqrtf(p) : 1.f;
+}
+
+// one power step for lambda_max(D^-1 K): w = D^-1 K v / |v| (v, w padded; |v|^2 is the previous
+// step's |w|^2 in prev); |w|^2 and v.w reduced into out2
 template <int B>
 __global__ void __launch_bounds__(kRowThreads)
     k_amg_power(const uint32_t *__restrict__ bptr, const uint32_t *__restrict__ bcol, const float *__restrict__ K,
                 const float *__restrict__ Dinv, const float *__restrict__ v, float *__restrict__ w, uint64_t nn,
-                double *partials, unsigned *ticket, double *out2) {
+                double *partials, unsigned *ticket, const double *prev, double *out2) {
     constexpr int VS = B == 3 ? 4 : 8;
     const int lane = threadIdx.x & 31;
+    const float sc = power_scale(prev);
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     float ww = 0.f, vw = 0.f;
     for (uint64_t I = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; I < nn; I += nw) {
@@ -549,6 +561,7 @@ __global__ void __launch_bounds__(kRowThreads)
             float s = 0.f;
 #pragma unroll
             for (int k = 0; k < B; ++k) s = fmaf(D[k], d[k], s);
+            s *= sc;
             w[(uint64_t)VS * I + lane] = s;
             ww = fmaf(s, s, ww);
             vw = fmaf(v[(uint64_t)VS * I + lane], s, vw);
@@ -637,11 +650,12 @@ struct EpiPost {
     }
 };
 
-//   EpiPower w = D^-1 K v, |w|^2 reduced into out (a power step for lambda_max; runs on the outer
-//            scalar slot, whose `done` stays 0)
+//   EpiPower w = D^-1 K v / |v|, |w|^2 reduced into out (a power step for lambda_max, |v|^2 the
+//            previous step's |w|^2 in prev; runs on the outer scalar slot, whose `done` stays 0)
 struct EpiPower {
     const float *D;
     float *w;
+    const double *prev;
     double *out;
     static constexpr bool kReduce = true;
     struct Pre {
@@ -660,7 +674,7 @@ struct EpiPower {
         const float v0 = __shfl_sync(0xffffffffu, qi, 0), v1 = __shfl_sync(0xffffffffu, qi, 8),
                     v2 = __shfl_sync(0xffffffffu, qi, 16);
         if (lane < 3) {
-            const float wc = p.d0 * v0 + p.d1 * v1 + p.d2 * v2;
+            const float wc = (p.d0 * v0 + p.d1 * v1 + p.d2 * v2) * power_scale(prev);
             w[4 * I + lane] = wc;
             acc = fmaf(wc, wc, acc);
         }
@@ -719,6 +733,54 @@ static void bulk0_launch(lmtg_ctx *c, const float *x, Epi epi, cudaStream_t s, P
     if (!S) S = c->scal.p;
     if (spmv_kind_in_use(c) == 2) Bulk0W<Epi>::launch(c, x, epi, s, S);
     else Bulk0N<Epi>::launch(c, x, epi, s, S);
+}
+
+// 6x6 levels of at least this many blocks stream their matrix with the bulk-copy kernel
+// (amg_bulk6.cuh); smaller ones stay L2-resident and keep the warp-per-row kernels
+constexpr uint64_t kBulk6MinBlocks = 1ull << 18;
+
+template <class Epi>
+struct Bulk6 {
+    static constexpr int kSt = 3, kCap = 224, kCons = 8, kMinB = 2;
+    static int &grid() {
+        static int g = 0;
+        return g;
+    }
+    static void setup(lmtg_ctx *c) {
+        if (grid()) return;
+        constexpr size_t smem = bulk6_smem_bytes<kSt, kCap>();
+        auto fn = k_amg6_bulk<kSt, kCap, kCons, kMinB, Epi>;
+        LMTG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int nb = 0;
+        LMTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 32 * (kCons + 1), smem));
+        grid() = c->sm_count * (nb > 0 ? nb : 1);
+    }
+    static void launch(const AmgLevel &L, const float *x, Epi epi, cudaStream_t s, PcgScalars *S) {
+        k_amg6_bulk<kSt, kCap, kCons, kMinB, Epi><<<grid(), 32 * (kCons + 1), bulk6_smem_bytes<kSt, kCap>(), s>>>(
+            L.bptr.p, L.bcol.p, L.K.p, x, epi, L.nn, S);
+    }
+};
+
+// res = r - K x on a 6x6 level; with D also xpre = omega D^-1 res
+static void level_res(lmtg_ctx *c, const AmgLevel &L, const float *x, const float *r, float *res, const float *D,
+                      float omega, float *xpre, cudaStream_t s, PcgScalars *S) {
+    if (L.bulk)
+        Bulk6<Epi6Res>::launch(L, x, Epi6Res{r, res, D, omega, xpre}, s, S);
+    else
+        k_amg_res<6><<<grid_for(c, L.nn * 32, kRowThreads, 8), kRowThreads, 0, s>>>(L.bptr.p, L.bcol.p, L.K.p, x, r,
+                                                                                    res, L.nn, S, D, omega, xpre);
+    c->launches += 1;
+}
+
+// xo = x + omega D^-1 (r - K x) on a 6x6 level
+static void level_post(lmtg_ctx *c, const AmgLevel &L, const float *x, const float *r, float *xo, cudaStream_t s,
+                       PcgScalars *S) {
+    if (L.bulk)
+        Bulk6<Epi6Post>::launch(L, x, Epi6Post{r, L.Dinv.p, x, xo, L.omega}, s, S);
+    else
+        k_amg_post<6><<<grid_for(c, L.nn * 32, kRowThreads, 8), kRowThreads, 0, s>>>(
+            L.bptr.p, L.bcol.p, L.K.p, L.Dinv.p, x, r, xo, L.omega, L.nn, S, false, 0, 0.0, c->partials.p);
+    c->launches += 1;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -993,7 +1055,7 @@ static void amg_build_structure(lmtg_ctx *c) {
         L->xa.alloc(VS * cur.nn);
         L->xb.alloc(VS * cur.nn);
         L->res.alloc(cur.b * cur.nn + 4);
-        if (l == 1) {
+        if (l >= 1) {
             L->r2.alloc(cur.b * cur.nn + 4);
             L->xb2.alloc(8 * cur.nn);
         }
@@ -1086,13 +1148,27 @@ static void amg_build_structure(lmtg_ctx *c) {
     // coarsest level too large for a dense inverse
     AmgLevel &C = *A->levels.back();
     const uint64_t nc = (uint64_t)C.b * C.nn;
-    A->nc = (A->levels.size() > 1 && nc <= 2000 && A->max_cdeg <= (uint32_t)kGalMaxDeg) ? (int)nc : 0;
+    A->nc = (A->levels.size() > 1 && nc <= kDenseMaxDofs && A->max_cdeg <= (uint32_t)kGalMaxDeg) ? (int)nc : 0;
     if (A->nc) {
-        const int smem = (int)(kGalWarps * gal_warp_bytes((int)((A->max_cdeg + 7) & ~7u)));
+        // the functions' dynamic shared-memory ceilings are process-wide: set for the widest rows
+        // any context may launch with, not this hierarchy's
+        const int smem = (int)(kGalWarps * gal_warp_bytes(kGalMaxDeg));
         LMTG_CUDA(cudaFuncSetAttribute(k_galerkin<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         LMTG_CUDA(cudaFuncSetAttribute(k_galerkin<6>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        // large 6x6 levels (not the coarsest, which is solved densely) stream by bulk copies;
+        // their rows hold at most kGalMaxDeg blocks, within a stage
+        static_assert(kGalMaxDeg <= Bulk6<Epi6Res>::kCap, "a coarse row must fit a bulk-copy stage");
+        for (size_t l = 1; l + 1 < A->levels.size(); ++l) {
+            AmgLevel &L = *A->levels[l];
+            L.bulk = L.nnzb >= kBulk6MinBlocks;
+            if (L.bulk) {
+                Bulk6<Epi6Res>::setup(c);
+                Bulk6<Epi6Post>::setup(c);
+            }
+        }
     }
     if (A->nc) A->Cinv.alloc((size_t)A->nc * A->nc);
+    A->power.alloc(2 * kPowerSteps * kMaxLevels);
     A->structure_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     c->amg = A.release();
 }
@@ -1123,9 +1199,11 @@ static void amg_numeric(lmtg_ctx *c) {
         LMTG_CUDA(cudaGetLastError());
         c->launches += 2;
     }
-    // smoother weights: omega = 1 / theta of a degree-1 Chebyshev on [h/30, h], h = 1.2 lmax
+    // smoother weights: omega = 1 / theta of a degree-1 Chebyshev on [h/30, h], h = 1.2 lmax.
+    // kPowerSteps power steps per level from a pseudo-random start, each normalising its input by
+    // the previous step's norm on the device: every level's steps are queued back to back and
+    // read once.
     PcgScalars *o = c->scal.p + 1;
-    double *out2 = reinterpret_cast<double *>(&o->pq);  // pq, rr: two doubles of the outer slot
     for (size_t l = 0; l + 1 < nl; ++l) {
         AmgLevel &L = *A.levels[l];
         const int VS = L.b == 3 ? 4 : 8;
@@ -1134,31 +1212,34 @@ static void amg_numeric(lmtg_ctx *c) {
         const float *K = l == 0 ? c->K32.p : L.K.p, *D = l == 0 ? c->Dinv32.p : L.Dinv.p;
         k_amg_scale<<<grid_for(c, nv, 256), 256, 0, s>>>(L.xa.p, nullptr, 1.f, nv);  // random start
         c->launches += 1;
-        // power steps v -> w = D^-1 K v, v normalised from the second step on: lambda ~ |w|
-        double lam = 0, h[2] = {0, 0};
-        float scale = 1.f;
         const bool bulk = l == 0 && spmv_kind_in_use(c) != 0;
         if (bulk) bulk0_setup(c);
-        for (int it = 0; it < 12; ++it) {
+        for (int it = 0; it < kPowerSteps; ++it) {
             float *v = (it & 1) ? L.xb.p : L.xa.p, *w = (it & 1) ? L.xa.p : L.xb.p;
-            if (it > 0) k_amg_scale<<<grid_for(c, nv, 256), 256, 0, s>>>(v, v, scale, nv);
+            double *out2 = A.power.p + 2 * (kPowerSteps * l + it);
+            const double *prev = it ? out2 - 2 : nullptr;
             const int g = grid_for(c, L.nn * 32, kRowThreads, 8);
             if (bulk)
-                bulk0_launch(c, v, EpiPower{D, w, out2}, s, o);
+                bulk0_launch(c, v, EpiPower{D, w, prev, out2}, s, o);
             else if (L.b == 3)
-                k_amg_power<3><<<g, kRowThreads, 0, s>>>(bp, bc, K, D, v, w, L.nn, c->partials.p, &o->cnt_c, out2);
+                k_amg_power<3><<<g, kRowThreads, 0, s>>>(bp, bc, K, D, v, w, L.nn, c->partials.p, &o->cnt_c, prev, out2);
             else
-                k_amg_power<6><<<g, kRowThreads, 0, s>>>(bp, bc, K, D, v, w, L.nn, c->partials.p, &o->cnt_c, out2);
+                k_amg_power<6><<<g, kRowThreads, 0, s>>>(bp, bc, K, D, v, w, L.nn, c->partials.p, &o->cnt_c, prev, out2);
             LMTG_CUDA(cudaGetLastError());
-            LMTG_CUDA(cudaMemcpyAsync(h, out2, sizeof(h), cudaMemcpyDeviceToHost, s));
-            LMTG_CUDA(cudaStreamSynchronize(s));
-            c->launches += it > 0 ? 2 : 1;
-            if (it > 0) lam = std::sqrt(h[0]);
-            scale = h[0] > 0 ? (float)(1.0 / std::sqrt(h[0])) : 1.f;
+            c->launches += 1;
         }
-        const double hi = 1.2 * lam, lo = hi / 30.0;
-        L.lambda = lam;
-        L.omega = lam > 0 ? (float)(2.0 / (hi + lo)) : 1.f;
+    }
+    {
+        std::vector<double> h(2 * kPowerSteps * (nl - 1));
+        LMTG_CUDA(cudaMemcpyAsync(h.data(), A.power.p, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, s));
+        LMTG_CUDA(cudaStreamSynchronize(s));
+        for (size_t l = 0; l + 1 < nl; ++l) {
+            AmgLevel &L = *A.levels[l];
+            const double lam = std::sqrt(std::max(0.0, h[2 * (kPowerSteps * l + kPowerSteps - 1)]));
+            const double hi = 1.2 * lam, lo = hi / 30.0;
+            L.lambda = lam;
+            L.omega = lam > 0 ? (float)(2.0 / (hi + lo)) : 1.f;
+        }
     }
     // dense inverse of the coarsest level (FP64 Gauss-Jordan with partial pivoting on the host;
     // a pivot below 1e-13 of the largest diagonal makes that unknown decoupled)
@@ -1229,6 +1310,31 @@ bool amg_prepare(lmtg_ctx *c) {
 float amg_omega0(const lmtg_ctx *c) { return c->amg->levels[0]->omega; }
 float *amg_xa0(const lmtg_ctx *c) { return c->amg->levels[0]->xa.p; }
 
+static void coarse_cycle(lmtg_ctx *c, AmgState &A, size_t l, const float *rhs, float *out, cudaStream_t s,
+                         PcgScalars *S);
+
+// Coarse correction of level l: level l+1's cycle on N.r (its first smoothing step already in
+// N.xa, fused into the restriction).  On the dense coarsest one solve (e, packed 6); otherwise
+// two cycles, the second on the residual N.r - K e the first leaves (e, e2 padded 8; a W-cycle
+// below level 0, which with unsmoothed aggregation brings the multilevel cycle close to the
+// two-level method's convergence).
+static void coarse_correction(lmtg_ctx *c, AmgState &A, size_t l, cudaStream_t s, PcgScalars *S, float *&e,
+                              float *&e2) {
+    const size_t nl = A.levels.size();
+    AmgLevel &N = *A.levels[l + 1];
+    if (l + 2 == nl) {
+        e = N.res.p;
+        e2 = nullptr;
+        coarse_cycle(c, A, l + 1, N.r.p, e, s, S);
+        return;
+    }
+    e = N.xb.p;
+    e2 = N.xb2.p;
+    coarse_cycle(c, A, l + 1, N.r.p, e, s, S);
+    level_res(c, N, e, N.r.p, N.r2.p, N.Dinv.p, N.omega, N.xa.p, s, S);
+    coarse_cycle(c, A, l + 1, N.r2.p, e2, s, S);
+}
+
 // Cycle of a level l >= 1 on the right-hand side rhs (packed 6), its first smoothing step
 // already in L.xa (fused into the caller's restriction or residual); the result goes to out
 // (padded 8; packed 6 on the coarsest, the dense solve).
@@ -1243,26 +1349,21 @@ static void coarse_cycle(lmtg_ctx *c, AmgState &A, size_t l, const float *rhs, f
     }
     AmgLevel &N = *A.levels[l + 1];
     const bool ncoarsest = l + 2 == nl;
-    const int g = grid_for(c, L.nn * 32, kRowThreads, 8);
-    k_amg_res<6><<<g, kRowThreads, 0, s>>>(L.bptr.p, L.bcol.p, L.K.p, L.xa.p, rhs, L.res.p, L.nn, S);
+    level_res(c, L, L.xa.p, rhs, L.res.p, nullptr, 0.f, nullptr, s, S);
     k_amg_restrict<6><<<grid_for(c, L.nagg * 32, kRowThreads, 8), kRowThreads, 0, s>>>(
         L.aptr.p, L.anode.p, L.Q.p, L.res.p, N.r.p, L.nagg, ncoarsest ? nullptr : N.Dinv.p, N.omega, N.xa.p, S);
-    float *e = ncoarsest ? N.res.p : N.xb.p;
-    coarse_cycle(c, A, l + 1, N.r.p, e, s, S);
+    float *e, *e2;
+    coarse_correction(c, A, l, s, S, e, e2);
     const int tb = 256;
     if (ncoarsest)
         k_amg_prolong<6, 6><<<grid_for(c, 6 * L.nn, tb), tb, 0, s>>>(L.agg.p, L.Q.p, e, nullptr, L.xa.p, L.nn, S);
     else
-        k_amg_prolong<6, 8><<<grid_for(c, 6 * L.nn, tb), tb, 0, s>>>(L.agg.p, L.Q.p, e, nullptr, L.xa.p, L.nn, S);
-    k_amg_post<6><<<g, kRowThreads, 0, s>>>(L.bptr.p, L.bcol.p, L.K.p, L.Dinv.p, L.xa.p, rhs, out, L.omega, L.nn, S,
-                                            false, 0, 0.0, c->partials.p);
-    c->launches += 4;
+        k_amg_prolong<6, 8><<<grid_for(c, 6 * L.nn, tb), tb, 0, s>>>(L.agg.p, L.Q.p, e, e2, L.xa.p, L.nn, S);
+    level_post(c, L, L.xa.p, rhs, out, s, S);
+    c->launches += 2;
 }
 
 // The cycle after the update kernel: r (level-0 residual, packed) -> z (padded), rz and beta.
-// Level 0's coarse correction runs level 1's cycle twice (the second on the residual the first
-// leaves): with unsmoothed aggregation this brings the multilevel cycle close to the two-level
-// method's convergence for one more level-1 residual and cycle.
 // ev (profiling only) receives events after the level-0 residual, the level-0 restriction, the
 // coarse levels, the level-0 prolongation and the level-0 smoothing.
 void amg_launch_cycle(lmtg_ctx *c, const float *r, float *z, cudaStream_t s, int start, double beta_den,
@@ -1287,16 +1388,8 @@ void amg_launch_cycle(lmtg_ctx *c, const float *r, float *z, cudaStream_t s, int
         L.aptr.p, L.anode.p, L.Q.p, L.res.p, N.r.p, L.nagg, ncoarsest ? nullptr : N.Dinv.p, N.omega, N.xa.p, S);
     mark(1);
     c->launches += 2;
-    float *e = ncoarsest ? N.res.p : N.xb.p, *e2 = nullptr;
-    coarse_cycle(c, A, 1, N.r.p, e, s, S);
-    if (!ncoarsest) {
-        // second level-1 cycle on r1 - K1 e (the residual kernel also forms its first smoothing step)
-        k_amg_res<6><<<grid_for(c, N.nn * 32, kRowThreads, 8), kRowThreads, 0, s>>>(
-            N.bptr.p, N.bcol.p, N.K.p, e, N.r.p, N.r2.p, N.nn, S, N.Dinv.p, N.omega, N.xa.p);
-        c->launches += 1;
-        coarse_cycle(c, A, 1, N.r2.p, N.xb2.p, s, S);
-        e2 = N.xb2.p;
-    }
+    float *e, *e2;
+    coarse_correction(c, A, 0, s, S, e, e2);
     mark(2);
     const int tb = 256;
     if (ncoarsest)

@@ -19,7 +19,8 @@ struct AmgLevel {
     DBuf<float> r;                     // right-hand side (packed b per node), levels >= 1
     DBuf<float> xa, xb;                // iterates, padded to 4 (level 0) or 8 per node
     DBuf<float> res;                   // residual (packed); on the coarsest, its solution
-    DBuf<float> r2, xb2;               // level 1: right-hand side and result of its second cycle
+    DBuf<float> r2, xb2;               // levels >= 1: right-hand side and result of a second cycle
+    bool bulk = false;                 // row products by the bulk-copy kernel (large 6x6 levels)
     // transfer to the next coarser level
     uint64_t nagg = 0;
     DBuf<uint32_t> agg;          // node -> aggregate (0xffffffff: in none)
@@ -31,6 +32,7 @@ struct AmgState {
     std::vector<std::unique_ptr<AmgLevel>> levels;
     int nc = 0;             // unknowns of the dense coarsest level (0: no hierarchy)
     DBuf<float> Cinv;       // its inverse, row-major
+    DBuf<double> power;     // |w|^2 and v.w of every power step, per level
     uint64_t version = ~0ull;  // matrix version of the numeric setup
     uint32_t max_cdeg = 0;     // widest coarse row over the levels
     double structure_ms = 0, numeric_ms = 0;

@@ -578,6 +578,7 @@ void profile_pcg(lmtg_ctx *c, bool fp32, int iters, double *spmv_ms, double *upd
 // restriction, [4] the coarse levels, [5] the prolongation, [6] the level-0 smoothing (z, r.z),
 // [7] the direction update.  All zero when the context has no hierarchy.
 void profile_amg(lmtg_ctx *c, int iters, double *ms) {
+    Phase ph("lmtg.amg.profile");
     for (int k = 0; k < 8; ++k) ms[k] = 0;
     if (!amg_prepare(c)) return;
     cudaStream_t s = c->stream;

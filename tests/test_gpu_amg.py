@@ -150,3 +150,36 @@ def test_small_systems_use_block_jacobi():
     assert st["status"] == 0
     assert f.amg_info()["levels"] == 0
     f.close()
+
+
+def test_large_coarse_levels_stream_by_bulk_copies():
+    """Hexa8 72^3 (1.17 M DOF): level 1 holds more than 2^18 6x6 blocks, so its residual and
+    smoothing products run on the bulk-copy kernel; the mixed solve must reach its FP64 residual
+    target, agree with the block-Jacobi solve and repeat bit for bit."""
+    pos, conn = make_rect_hexa(73)
+    E = np.exp(np.log(210000.0) + 0.5 * np.random.default_rng(7).standard_normal(conn.shape[0]))
+    f = Formulation(pos, conn)
+    f.elastic_modulus = E
+    f.poisson_ratio = 0.3
+    clamped = np.nonzero(pos[:, 0] < 1e-6)[0]
+    f.add_constraints((3 * clamped[:, None] + np.arange(3)).ravel(), 1e5)
+    f.add_skin_traction(x1_faces(pos, conn), (1.0, 0.0, 0.0))
+    f.allocate_matrices()
+    out = []
+    for _ in range(2):
+        f.set_result(np.zeros(f.n))
+        st = f.solve(1e-10, mode="mixed")
+        assert st["status"] == 0
+        out.append(f.get_result())
+    assert np.array_equal(out[0], out[1])
+    info = f.amg_info()
+    assert info["levels"] >= 3 and info["nnz_blocks"][1] >= 1 << 18, info
+    F = f.get_sollicitation()
+    assert np.linalg.norm(F - f.spmv(out[0])) <= 1.01e-10 * np.linalg.norm(F)
+    its = st["iterations"]
+    f.set_preconditioner("block_jacobi")
+    f.set_result(np.zeros(f.n))
+    st = f.solve(1e-10, mode="mixed")
+    assert st["status"] == 0 and its * 10 < st["iterations"]
+    assert rel(out[0], f.get_result()) <= 1e-7
+    f.close()
