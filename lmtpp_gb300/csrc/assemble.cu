@@ -4,11 +4,10 @@
 // global assembly mutex (formal_lf/calculate_matrix.py:86-98, include/containers/vec_mt.h:39-62)
 // and assemble_constraints (include/formulation/formulation.h:1028-1071).
 //
-// Assembly: one thread per stored value of K (BSR 3x3, full symmetric pattern).  It walks the
-// block's gather list (element order, built once by pattern.cu) and sums the element block
-// entries, transposed when the element pair is (b,a) with a > b.  No atomics, no search, a
-// deterministic summation order.  FP64 assembly can write the FP32 inner operator in the same
-// pass (rounded from the FP64 sum).
+// Assembly: each stored 3x3 block of K (BSR, full symmetric pattern) is the sum of the element
+// blocks its gather list names (element order, built once by pattern.cu), transposed when the
+// element pair is (b,a) with a > b.  No atomics, no search, a deterministic summation order.
+// FP64 assembly can write the FP32 inner operator in the same pass (rounded from the FP64 sum).
 #include <cstring>
 #include <type_traits>
 
@@ -18,46 +17,159 @@
 
 namespace lmtg {
 
-// One warp per node row, one lane per block of the row: the lane walks its block's gather list
-// once, sums the 9 entries of every contribution (transposed when the element pair is (b,a)),
-// then writes component v of its block at kidx(rb, deg, b, v) -- 9 coalesced stores per row.
+// IEEE round-to-nearest-even double -> float on the integer pipe (GB300 issues FP64 and its
+// conversions at 2 lanes per clock per SM): finite values in the normal float range are rounded
+// from the bit pattern, zeros and double subnormals give a signed zero, and the rest (float
+// subnormals, overflow, inf, nan) go through the conversion instruction.  Results equal the
+// conversion's.
+__device__ __forceinline__ float d2f_rn(double d) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+    const int ef = (int)((b >> 52) & 0x7ffu);
+    if (ef == 0) return __uint_as_float(sign);
+    const int e = ef - 1023 + 127;
+    if (e <= 0 || e >= 255) return (float)d;
+    const unsigned long long man = b & 0xfffffffffffffull;
+    unsigned keep = (unsigned)(man >> 29);
+    const unsigned rem = (unsigned)man & 0x1fffffffu;
+    keep += (rem > 0x10000000u || (rem == 0x10000000u && (keep & 1u))) ? 1u : 0u;
+    return __uint_as_float(sign | (((unsigned)e << 23) + keep));  // a mantissa carry bumps the exponent
+}
+
+template <class A>
+__device__ __forceinline__ float to_f32(A v) {
+    if constexpr (sizeof(A) == 8) return d2f_rn(v);
+    else return v;
+}
+
+// One warp per node row, its blocks 32 at a time (a group).  The contributions of a group's
+// blocks are one contiguous range of the gather list, so the warp first copies the group's
+// element records (up to kAsmChunk) into shared memory -- lane t loads value t % 9 of record
+// t / 9, all loads independent.  The sums are then spread evenly over the lanes: the group's
+// 9 x (records) addends, ordered by (block, component, contribution), are cut into 32 equal
+// ranges and each lane sums its range in order, closing every output it completes; an output
+// that straddles two lanes is the earlier lane's partial plus the later lane's.  Every lane
+// issues the same number of adds whatever the blocks' contribution counts (1 to 8 on a Hexa8
+// grid), which matters on GB300's narrow FP64 pipe.  Groups with more records than a chunk or
+// an output longer than a lane's range (Tetra10 vertex rows), or a block without contributions,
+// take the per-block walk instead: lane b sums block b's records in element order.  Either way the order is fixed: results are
+// deterministic.  Component v of a block goes to kidx(rb, deg, b, v): coalesced stores.
+constexpr int kAsmWarps = 4, kAsmChunk = 64;  // 28 KB of static shared memory per CTA (FP64)
+
 template <class TS, bool kW64, bool kW32>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(32 * kAsmWarps)
     k_assemble(const uint32_t *__restrict__ bptr, uint64_t nn, const uint32_t *__restrict__ gptr,
                const uint32_t *__restrict__ gsrc, const TS *__restrict__ Ke, double *__restrict__ K64,
                float *__restrict__ K32) {
     typedef typename std::conditional<sizeof(TS) == 8, double, float>::type Acc;
-    const int lane = threadIdx.x & 31;
+    __shared__ TS rec[kAsmWarps][kAsmChunk * 9];
+    __shared__ Acc outs[kAsmWarps][32 * 9];
+    __shared__ uint32_t ofs[kAsmWarps][33];
+    __shared__ unsigned char trf[kAsmWarps][kAsmChunk];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    TS *R = rec[warp];
+    Acc *Out = outs[warp];
+    uint32_t *O = ofs[warp];
+    unsigned char *Tr = trf[warp];
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    auto store = [&](uint32_t rb, uint32_t deg, uint32_t b, const Acc (&s)[9]) {
+#pragma unroll
+        for (int v = 0; v < 9; ++v) {
+            const uint64_t idx = kidx(rb, deg, b, v);
+            if (kW64) K64[idx] = (double)s[v];
+            if (kW32) K32[idx] = to_f32(s[v]);
+        }
+    };
     for (uint64_t I = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; I < nn; I += nw) {
         const uint32_t rb = __ldg(bptr + I), deg = __ldg(bptr + I + 1) - rb;
-        for (uint32_t b = lane; b < deg; b += 32) {
-            const uint32_t blk = rb + b, g0 = __ldg(gptr + blk), g1 = __ldg(gptr + blk + 1);
-            Acc s[9];
+        for (uint32_t bg = 0; bg < deg; bg += 32) {
+            const uint32_t nb = min(32u, deg - bg);
+            const bool on = (uint32_t)lane < nb;
+            const uint32_t gs = __ldg(gptr + rb + bg), ge = __ldg(gptr + rb + bg + nb);
+            const uint32_t my0 = on ? __ldg(gptr + rb + bg + lane) : 0u;
+            const uint32_t my1 = on ? __ldg(gptr + rb + bg + lane + 1) : 0u;
+            const uint32_t nrec = ge - gs, W = 9 * nrec, P = (W + 31) / 32;
+            const uint32_t maxcnt = __reduce_max_sync(0xffffffffu, my1 - my0);
+            const uint32_t mincnt = __reduce_min_sync(0xffffffffu, on ? my1 - my0 : ~0u);
+            if (nrec <= (uint32_t)kAsmChunk && maxcnt <= P && mincnt > 0) {
+#pragma unroll 6
+                for (uint32_t t = lane; t < W; t += 32) {
+                    const uint32_t k = t / 9, v = t - 9 * k;
+                    const uint32_t src = __ldg(gsrc + gs + k);
+                    R[t] = __ldg(Ke + (uint64_t)(src >> 1) * 9 + v);
+                    if (v == 0) Tr[k] = (unsigned char)(src & 1u);
+                }
+                if (on) O[lane] = my0 - gs;
+                if (lane == 0) O[nb] = nrec;
+                __syncwarp();
+                // this lane's addends [j0, j1): output (b, v) holds addends 9 O[b] + v cnt_b + c
+                const uint32_t j0 = min(W, lane * P), j1 = min(W, j0 + P);
+                Acc s = (Acc)0, head = (Acc)0, tail = (Acc)0;
+                uint32_t head_id = ~0u, tail_id = ~0u;
+                if (j0 < j1) {
+                    uint32_t b = 0;
+                    while (9 * O[b + 1] <= j0) ++b;
+                    uint32_t cnt = O[b + 1] - O[b], rel = j0 - 9 * O[b];
+                    uint32_t v = rel / cnt, c = rel - v * cnt;
+                    bool first_partial = c != 0;  // the first output began in the previous lane
+                    for (uint32_t j = j0; j < j1; ++j) {
+                        const uint32_t k = O[b] + c;
+                        const uint32_t vv = Tr[k] ? (v % 3) * 3 + v / 3 : v;
+                        const Acc x = (Acc)R[9 * k + vv];
+                        s = c == 0 ? x : s + x;
+                        if (c + 1 == cnt) {  // output (b, v) complete
+                            if (first_partial) {
+                                head = s;
+                                head_id = 9 * b + v;
+                                first_partial = false;
+                            } else {
+                                Out[9 * b + v] = s;
+                            }
+                            c = 0;
+                            if (++v == 9) {
+                                v = 0;
+                                ++b;
+                                cnt = b < nb ? O[b + 1] - O[b] : 1u;
+                            }
+                        } else {
+                            ++c;
+                        }
+                    }
+                    if (c != 0) {  // the last output continues in the next lane
+                        tail = s;
+                        tail_id = 9 * b + v;
+                    }
+                }
+                const Acc prev = __shfl_up_sync(0xffffffffu, tail, 1);
+                const uint32_t prev_id = __shfl_up_sync(0xffffffffu, tail_id, 1);
+                if (lane > 0 && head_id != ~0u && prev_id == head_id) Out[head_id] = prev + head;
+                __syncwarp();
+                if (on) {
+                    Acc o[9];
 #pragma unroll
-            for (int v = 0; v < 9; ++v) s[v] = (Acc)0;
-            for (uint32_t g = g0; g < g1; ++g) {
-                const uint32_t src = __ldg(gsrc + g);
-                const TS *e = Ke + (uint64_t)(src >> 1) * 9;
-                TS m[9];
+                    for (int v = 0; v < 9; ++v) o[v] = Out[9 * lane + v];
+                    store(rb, deg, bg + lane, o);
+                }
+                __syncwarp();
+            } else if (on) {
+                Acc o[9];
 #pragma unroll
-                for (int v = 0; v < 9; ++v) m[v] = __ldg(e + v);
-                const bool tr = (src & 1u) != 0;
+                for (int v = 0; v < 9; ++v) o[v] = (Acc)0;
+                for (uint32_t g = my0; g < my1; ++g) {
+                    const uint32_t src = __ldg(gsrc + g);
+                    const TS *e = Ke + (uint64_t)(src >> 1) * 9;
+                    const bool tr = (src & 1u) != 0;
 #pragma unroll
-                for (int v = 0; v < 9; ++v) s[v] += (Acc)(tr ? m[(v % 3) * 3 + v / 3] : m[v]);
-            }
-#pragma unroll
-            for (int v = 0; v < 9; ++v) {
-                const uint64_t idx = kidx(rb, deg, b, v);
-                if (kW64) K64[idx] = (double)s[v];
-                if (kW32) K32[idx] = (float)s[v];
+                    for (int v = 0; v < 9; ++v) o[v] += (Acc)__ldg(e + (tr ? (v % 3) * 3 + v / 3 : v));
+                }
+                store(rb, deg, bg + lane, o);
             }
         }
     }
 }
 
 void assemble_matrix(lmtg_ctx *c, bool from64, bool want64, bool want32) {
-    const int T = 256;
+    const int T = 32 * kAsmWarps;
     const int grid = grid_for(c, c->nn * 32, T, 8);
     if (from64) {
         if (want64 && want32)
