@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "amg.cuh"
+#include "residual_dd.cuh"
 #include "spmv_bulk.cuh"
 
 namespace lmtg {
@@ -181,6 +182,60 @@ static double residual(lmtg_ctx *c, const T *K, const T *x, const T *b, T *r) {
     LMTG_CUDA(cudaGetLastError());
     c->launches += 1;
     return read_double(c, &o->rr);
+}
+
+__global__ void k_scale32(float *__restrict__ v, float s, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        v[i] *= s;
+}
+
+// the float-float residual kernel's shape: 3 stages of up to 256 blocks, 8 consumer warps, 3 CTAs
+// per SM (59 KB of shared memory each)
+constexpr int kResStages = 3, kResCap = 256, kResCons = 8, kResMinB = 3;
+
+// Refinement residual of the mixed solver: b32 = r / |r| for r = F - K64 u, returns |r|^2.  With
+// ff the float-float bulk-copy kernel (residual_dd.cuh) forms r to ~2^-48 relative accuracy off
+// the FP64 pipe; otherwise, and for patterns with rows wider than its stage, the FP64 warp-row
+// kernel into r64.
+static double refinement_residual(lmtg_ctx *c, const double *u, const double *Fb, double bb, float *b32,
+                                  double *r64, bool ff) {
+    PcgScalars *o = outer_slot(c);
+    cudaStream_t s = c->stream;
+    if (!ff || c->max_row_blocks > (uint32_t)kResCap) {
+        const double rr = residual<double>(c, c->K64.p, u, Fb, r64);
+        if (rr > 0) {
+            k_scale_to32<<<node_grid(c), kRowThreads, 0, s>>>(r64, 1.0 / std::sqrt(rr), b32, c->n);
+            c->launches += 1;
+        }
+        return rr;
+    }
+    static int grid = 0;
+    constexpr size_t smem = res64_smem_bytes<kResStages, kResCap>();
+    auto fn = k_residual_ff<kResStages, kResCap, kResCons, kResMinB>;
+    if (!grid) {
+        LMTG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int nb = 0;
+        LMTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 32 * (kResCons + 1), smem));
+        grid = c->sm_count * (nb > 0 ? nb : 1);
+    }
+    // a power of two near 1 / rms(F) keeps the squares of small residuals in the float range
+    const double rms = std::sqrt(bb / (double)(c->n ? c->n : 1));
+    const int e = (rms > 0 && std::isfinite(rms)) ? std::max(-100, std::min(100, std::ilogb(rms))) : 0;
+    const float rscale = std::ldexp(1.0f, -e);
+    LMTG_CUDA(cudaMemsetAsync(&o->status, 0, sizeof(int), s));
+    fn<<<grid, 32 * (kResCons + 1), smem, s>>>(c->bptr.p, c->bcol.p, c->K64.p, u, Fb, rscale, b32, c->nn,
+                                                c->partials.p, o);
+    LMTG_CUDA(cudaGetLastError());
+    c->launches += 1;
+    PcgScalars h;
+    LMTG_CUDA(cudaMemcpyAsync(&h, o, sizeof(h), cudaMemcpyDeviceToHost, s));
+    LMTG_CUDA(cudaStreamSynchronize(s));
+    LMTG_CHECK(h.status != LMTG_ERR_TIMEOUT, LMTG_ERR_TIMEOUT, "residual: a bulk-copy wait gave up");
+    if (h.rr > 0) {
+        k_scale32<<<node_grid(c), kRowThreads, 0, s>>>(b32, (float)(1.0 / std::sqrt(h.rr)), c->n);
+        c->launches += 1;
+    }
+    return h.rr * std::ldexp(1.0, 2 * e);
 }
 
 static double dot64(lmtg_ctx *c, const double *a, const double *b) {
@@ -449,14 +504,27 @@ int solve_mixed(lmtg_ctx *c, double tol, int maxit, double timeout_s, lmtg_solve
     const double bb = dot64(c, Fb, Fb);
     const bool amg = amg_prepare(c);
     ChunkGraph chunk;  // captured at the first segment, replayed by the others
-    const double kDelta = c->inner_reduction;  // recursive-residual reduction per segment
+    const double kDelta = inner_reduction_for(c, amg);  // recursive-residual reduction per segment
     int total = 0, outer = 0, status = LMTG_OK;
     double rel = 0, s_prev = 0, rz_prev = 0, rel_prev = 0;
     bool have_dir = false;
     const int max_outer = 400;
+    // Float-float residuals (32x the FP64 rounding) while the residual is above kFFMinRel of |F|,
+    // where their rounding stays four orders below it; below, and to decide convergence or when
+    // a float-float residual shows no progress, the FP64 residual takes over for the rest of the
+    // solve.  (Near the float-float floor the residual is mostly rounding, and a segment that
+    // continues its search direction on it can diverge.)
+    constexpr double kFFMinRel = 1e-9;
+    bool ff = true;
     for (;;) {
-        const double rr = residual<double>(c, c->K64.p, ux, Fb, r64);
+        double rr = refinement_residual(c, ux, Fb, bb, b32, r64, ff);  // b32 = r / |r|
         rel = bb > 0 ? std::sqrt(rr / bb) : std::sqrt(rr);
+        if (ff && (!std::isfinite(rel) || rel <= tol || rel < kFFMinRel || rr == 0.0 ||
+                   (outer > 0 && rel > 0.5 * rel_prev))) {
+            ff = false;
+            rr = refinement_residual(c, ux, Fb, bb, b32, r64, false);
+            rel = bb > 0 ? std::sqrt(rr / bb) : std::sqrt(rr);
+        }
         if (!std::isfinite(rel)) {
             status = LMTG_ERR_NAN;
             break;
@@ -473,8 +541,6 @@ int solve_mixed(lmtg_ctx *c, double tol, int maxit, double timeout_s, lmtg_solve
         // a segment that did not reduce the true residual by 2x restarts the direction
         if (have_dir && rel > 0.5 * rel_prev) have_dir = false;
         const double sc = std::sqrt(rr);
-        k_scale_to32<<<node_grid(c), kRowThreads, 0, c->stream>>>(r64, 1.0 / sc, b32, c->n);
-        c->launches += 1;
         LMTG_CUDA(cudaMemsetAsync(d32, 0, sizeof(float) * c->n, c->stream));
         const double f = have_dir ? s_prev / sc : 0.0;
         const double beta_den = have_dir ? rz_prev * f : 0.0;
