@@ -15,6 +15,7 @@
 // points from shared memory and writing the 3x3 block.  Output layout Ke[e][pair][3][3]
 // (pairs a<=b): consecutive lanes write consecutive 72/36-byte blocks.
 #include "elem_traits.cuh"
+#include "ffloat.cuh"
 
 namespace lmtg {
 
@@ -126,6 +127,174 @@ __global__ void __launch_bounds__(kElWarps * 32)
     }
 }
 
+// ---- FP64 element matrices in float-float arithmetic ----
+// The same mapping and algebra as k_elast, every FP64 operation replaced by its float-float
+// counterpart (ffloat.cuh): GB300's FP64 pipe made k_elast<double> its bound (92% busy).  The
+// Jacobian is formed from the node coordinates relative to the element's first node, taken in
+// FP64 (the shape-function gradients sum to zero, so this is the same Jacobian), so that no
+// coordinate offset cancels in the 48-bit arithmetic; the reference-cell gradients and weights
+// come from FP64 tables split on the host.  Entries reach about 1e-14 of the largest, and are
+// written as FP64.
+
+// reference-cell gradients at the Gauss points and the weights, as float-float pairs
+__constant__ ff::f2 c_dNff[2][8][10][3];
+__constant__ ff::f2 c_wff[2];
+
+template <class EL>
+struct ElSmemFF {
+    ff::f2 d[kElBatch][3 * EL::npe];              // node coordinates minus the first node's
+    ff::f2 G[kElBatch][EL::ngp][EL::npe][3];      // [element][gauss point][node][dim]
+    ff::f2 GW[kElBatch][EL::ngp][EL::npe][3];     // w * detJ * G
+    ff::f2 lam[kElBatch], mu[kElBatch];
+};
+
+template <class EL, int kTab>
+__global__ void __launch_bounds__(kElWarps * 32)
+    k_elast_ff(const double *__restrict__ pos, const uint32_t *__restrict__ conn, const double *__restrict__ E,
+               int E_per_elem, ff::f2 flam, ff::f2 fmu, double nu0, const double *__restrict__ nuv, uint64_t ne,
+               double *__restrict__ Ke) {
+    constexpr int NPE = EL::npe, NGP = EL::ngp, NP = EL::npairs;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    ElSmemFF<EL> &S = reinterpret_cast<ElSmemFF<EL> *>(smem_raw)[threadIdx.x >> 5];
+    // the gradient table in shared memory: lanes read it at different Gauss points
+    __shared__ ff::f2 dN[NGP][NPE][3];
+    for (int t = threadIdx.x; t < NGP * NPE * 3; t += blockDim.x) {
+        const int g = t / (NPE * 3), a = (t / 3) % NPE, j = t % 3;
+        dN[g][a][j] = c_dNff[kTab][g][a][j];
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const uint64_t nbatch = (ne + kElBatch - 1) / kElBatch;
+    const uint64_t warp0 = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+
+    for (uint64_t batch = warp0; batch < nbatch; batch += nwarps) {
+        const uint64_t e0 = batch * kElBatch;
+        // node coordinates relative to the element's first node
+        for (int t = lane; t < kElBatch * 3 * NPE; t += 32) {
+            const int le = t / (3 * NPE), r = t % (3 * NPE);
+            const uint64_t e = e0 + le;
+            ff::f2 v{0.f, 0.f};
+            // the FP64 difference is exact for nodes within a factor 2 of the first (Sterbenz)
+            if (e < ne) v = ff::split(pos[3ull * conn[e * NPE + r / 3] + r % 3] - pos[3ull * conn[e * NPE] + r % 3]);
+            S.d[le][r] = v;
+        }
+        if (lane < kElBatch) {
+            const uint64_t e = e0 + lane;
+            const ff::f2 Ee = ff::split(e < ne ? E[E_per_elem ? e : 0] : 0.0);
+            if (nuv && e < ne) {  // per-element Poisson ratio: the factors in FP64
+                const double nu = nuv[e];
+                S.lam[lane] = ff::mul(Ee, ff::split(nu / ((1.0 + nu) * (1.0 - 2.0 * nu))));
+                S.mu[lane] = ff::mul(Ee, ff::split(1.0 / (2.0 * (1.0 + nu))));
+            } else {
+                S.lam[lane] = ff::mul(Ee, flam);
+                S.mu[lane] = ff::mul(Ee, fmu);
+            }
+        }
+        __syncwarp();
+        // phase 1: geometry per (element, Gauss point)
+        for (int t = lane; t < kElBatch * NGP; t += 32) {
+            const int le = t / NGP, g = t % NGP;
+            ff::f2 J[3][3];
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) {
+                    ff::Dot acc;
+#pragma unroll
+                    for (int a = 1; a < NPE; ++a) acc.add(S.d[le][3 * a + i], dN[g][a][j]);
+                    J[i][j] = acc.get();
+                }
+            auto cof = [&](int r0, int c0, int r1, int c1) {  // J[r0][c0] J[r1][c1] - J[r0][c1] J[r1][c0]
+                ff::Dot acc;
+                acc.add(J[r0][c0], J[r1][c1]);
+                acc.add(ff::neg(J[r0][c1]), J[r1][c0]);
+                return acc.get();
+            };
+            const ff::f2 c00 = cof(1, 1, 2, 2), c01 = cof(1, 2, 2, 0), c02 = cof(1, 0, 2, 1);
+            ff::Dot dacc;
+            dacc.add(J[0][0], c00);
+            dacc.add(J[0][1], c01);
+            dacc.add(J[0][2], c02);
+            const ff::f2 det = dacc.get();
+            const ff::f2 id = ff::recip(det);
+            // Ji[j][i]: gradient g_i = sum_j Ji[j][i] dN_j (the inverse's transpose, as in k_elast)
+            const ff::f2 Ji[3][3] = {
+                {ff::mul(c00, id), ff::mul(cof(0, 2, 2, 1), id), ff::mul(cof(0, 1, 1, 2), id)},
+                {ff::mul(c01, id), ff::mul(cof(0, 0, 2, 2), id), ff::mul(cof(0, 2, 1, 0), id)},
+                {ff::mul(c02, id), ff::mul(cof(0, 1, 2, 0), id), ff::mul(cof(0, 0, 1, 1), id)}};
+            const ff::f2 wdet = ff::mul(c_wff[kTab], det);
+#pragma unroll
+            for (int a = 0; a < NPE; ++a)
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+                    ff::Dot acc;
+                    acc.add(Ji[0][i], dN[g][a][0]);
+                    acc.add(Ji[1][i], dN[g][a][1]);
+                    acc.add(Ji[2][i], dN[g][a][2]);
+                    const ff::f2 gi = acc.get();
+                    S.G[le][g][a][i] = gi;
+                    S.GW[le][g][a][i] = ff::mul(wdet, gi);
+                }
+        }
+        __syncwarp();
+        // phase 2: node-pair blocks
+        for (int t = lane; t < kElBatch * NP; t += 32) {
+            const int le = t / NP, p = t - le * NP;
+            const uint64_t e = e0 + le;
+            if (e >= ne) break;
+            const int a = c_pair_a[kTab][p], b = c_pair_b[kTab][p];
+            ff::Dot A[3][3];
+#pragma unroll
+            for (int g = 0; g < NGP; ++g) {
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+                    const ff::f2 wa = S.GW[le][g][a][i];
+#pragma unroll
+                    for (int j = 0; j < 3; ++j) A[i][j].add(wa, S.G[le][g][b][j]);
+                }
+            }
+            ff::f2 Af[3][3];
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) Af[i][j] = A[i][j].get();
+            const ff::f2 lam = S.lam[le], mu = S.mu[le];
+            const ff::f2 tr = ff::add(ff::add(Af[0][0], Af[1][1]), Af[2][2]);
+            double *o = Ke + (e * NP + p) * 9;
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) {
+                    ff::Dot acc;
+                    acc.add(lam, Af[i][j]);
+                    acc.add(mu, Af[j][i]);
+                    if (i == j) acc.add(mu, tr);
+                    o[3 * i + j] = ff::to_double(acc.get());
+                }
+        }
+        __syncwarp();
+    }
+}
+
+// FP64 table of the reference-cell gradients at the Gauss points, split into float-float pairs
+// on the host (hi = the float nearest to the value, lo = the float nearest to the rest)
+template <class EL>
+static void ff_tables(ff::f2 (&dn)[8][10][3], ff::f2 &w) {
+    auto sp = [](double v) {
+        const float hi = (float)v;
+        return ff::f2{hi, (float)(v - (double)hi)};
+    };
+    for (int g = 0; g < EL::ngp; ++g) {
+        double x, y, z, d[EL::npe][3];
+        EL::template gauss_point<double>(g, x, y, z);
+        EL::template dN_at<double>(x, y, z, d);
+        for (int a = 0; a < EL::npe; ++a)
+            for (int j = 0; j < 3; ++j) dn[g][a][j] = sp(d[a][j]);
+    }
+    w = sp(EL::template weight<double>(0));
+}
+
 static bool g_pairs_ready[64] = {false};
 
 template <class EL, int kTab>
@@ -133,12 +302,16 @@ static void launch_t(lmtg_ctx *c, bool fp64) {
     const int threads = kElWarps * 32;
     const uint64_t nbatch = (c->ne + kElBatch - 1) / kElBatch;
     if (fp64) {
-        const size_t sm = sizeof(ElSmem<EL, double>) * kElWarps;
-        LMTG_CUDA(cudaFuncSetAttribute(k_elast<EL, double, kTab>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        k_elast<EL, double, kTab><<<grid_for(c, nbatch * 32, threads, 2), threads, sm, c->stream>>>(
-            c->pos.p, c->conn.p, c->E.p, c->E_per_elem, c->nu, c->nu_per_elem ? c->nuv.p : nullptr, c->ne,
-            c->Ke64.p);
+        const size_t sm = sizeof(ElSmemFF<EL>) * kElWarps;
+        LMTG_CUDA(cudaFuncSetAttribute(k_elast_ff<EL, kTab>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        const double nu = c->nu;
+        auto sp = [](double v) {
+            const float hi = (float)v;
+            return ff::f2{hi, (float)(v - (double)hi)};
+        };
+        k_elast_ff<EL, kTab><<<grid_for(c, nbatch * 32, threads, 2), threads, sm, c->stream>>>(
+            c->pos.p, c->conn.p, c->E.p, c->E_per_elem, sp(nu / ((1.0 + nu) * (1.0 - 2.0 * nu))),
+            sp(1.0 / (2.0 * (1.0 + nu))), c->nu, c->nu_per_elem ? c->nuv.p : nullptr, c->ne, c->Ke64.p);
     } else {
         const size_t sm = sizeof(ElSmem<EL, float>) * kElWarps;
         LMTG_CUDA(cudaFuncSetAttribute(k_elast<EL, float, kTab>,
@@ -164,6 +337,11 @@ void launch_elem_elast(lmtg_ctx *c, bool fp64) {
                 }
         LMTG_CUDA(cudaMemcpyToSymbol(c_pair_a, pa, sizeof(pa)));
         LMTG_CUDA(cudaMemcpyToSymbol(c_pair_b, pb, sizeof(pb)));
+        static ff::f2 dn[2][8][10][3], w[2];
+        ff_tables<Hexa8>(dn[0], w[0]);
+        ff_tables<Tetra10>(dn[1], w[1]);
+        LMTG_CUDA(cudaMemcpyToSymbol(c_dNff, dn, sizeof(dn)));
+        LMTG_CUDA(cudaMemcpyToSymbol(c_wff, w, sizeof(w)));
         g_pairs_ready[c->device & 63] = true;
     }
     if (c->elem_type == LMTG_ELEM_HEXA8) launch_t<Hexa8, 0>(c, fp64);

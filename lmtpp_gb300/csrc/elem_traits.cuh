@@ -16,9 +16,9 @@ namespace lmtg {
 struct Hexa8 {
     static constexpr int npe = 8, ngp = 8, npairs = 36;
     template <class T>
-    __device__ static T weight(int) { return (T)0.125; }
+    __host__ __device__ static T weight(int) { return (T)0.125; }
     template <class T>
-    __device__ static void dN(int g, T (&d)[8][3]) {
+    __host__ __device__ static void dN(int g, T (&d)[8][3]) {
         const T ga = (T)0.211324865405, gb = (T)0.788675134595;
         const T x = (g == 1 || g == 2 || g == 5 || g == 6) ? gb : ga;
         const T y = (g == 2 || g == 3 || g == 6 || g == 7) ? gb : ga;
@@ -27,14 +27,14 @@ struct Hexa8 {
     }
     // shape functions at the reference point (x, y, z)
     template <class T>
-    __device__ static void N_at(T x, T y, T z, T (&N)[8]) {
+    __host__ __device__ static void N_at(T x, T y, T z, T (&N)[8]) {
         const T mx = 1 - x, my = 1 - y, mz = 1 - z;
         N[0] = mx * my * mz; N[1] = x * my * mz; N[2] = x * y * mz; N[3] = mx * y * mz;
         N[4] = mx * my * z;  N[5] = x * my * z;  N[6] = x * y * z;  N[7] = mx * y * z;
     }
     // Gauss point g of the order-2 rule
     template <class T>
-    __device__ static void gauss_point(int g, T &x, T &y, T &z) {
+    __host__ __device__ static void gauss_point(int g, T &x, T &y, T &z) {
         const T ga = (T)0.211324865405, gb = (T)0.788675134595;
         x = (g == 1 || g == 2 || g == 5 || g == 6) ? gb : ga;
         y = (g == 2 || g == 3 || g == 6 || g == 7) ? gb : ga;
@@ -42,7 +42,7 @@ struct Hexa8 {
     }
     // derivatives at the reference point (x, y, z)
     template <class T>
-    __device__ static void dN_at(T x, T y, T z, T (&d)[8][3]) {
+    __host__ __device__ static void dN_at(T x, T y, T z, T (&d)[8][3]) {
         const T mx = 1 - x, my = 1 - y, mz = 1 - z;
         d[0][0] = -my * mz; d[0][1] = -mx * mz; d[0][2] = -mx * my;
         d[1][0] = my * mz;  d[1][1] = -x * mz;  d[1][2] = -x * my;
@@ -58,15 +58,15 @@ struct Hexa8 {
 struct Tetra10 {
     static constexpr int npe = 10, ngp = 4, npairs = 55;
     template <class T>
-    __device__ static T weight(int) { return (T)0.041666666666666666667; }
+    __host__ __device__ static T weight(int) { return (T)0.041666666666666666667; }
     template <class T>
-    __device__ static void dN(int g, T (&d)[10][3]) {
+    __host__ __device__ static void dN(int g, T (&d)[10][3]) {
         const T ta = (T)0.1381966011250105, tb = (T)0.5854101966249685;
         const T x = g == 1 ? tb : ta, y = g == 2 ? tb : ta, z = g == 3 ? tb : ta;
         dN_at(x, y, z, d);
     }
     template <class T>
-    __device__ static void N_at(T x, T y, T z, T (&N)[10]) {
+    __host__ __device__ static void N_at(T x, T y, T z, T (&N)[10]) {
         const T X[4] = {1 - x - y - z, x, y, z};
 #pragma unroll
         for (int i = 0; i < 4; ++i) N[i] = X[i] * (2 * X[i] - 1);
@@ -74,7 +74,7 @@ struct Tetra10 {
         N[7] = 4 * X[0] * X[3]; N[8] = 4 * X[1] * X[3]; N[9] = 4 * X[2] * X[3];
     }
     template <class T>
-    __device__ static void gauss_point(int g, T &x, T &y, T &z) {
+    __host__ __device__ static void gauss_point(int g, T &x, T &y, T &z) {
         const T ta = (T)0.1381966011250105, tb = (T)0.5854101966249685;
         x = g == 1 ? tb : ta;
         y = g == 2 ? tb : ta;
@@ -82,7 +82,7 @@ struct Tetra10 {
     }
     // derivatives at the reference point (x, y, z)
     template <class T>
-    __device__ static void dN_at(T x, T y, T z, T (&d)[10][3]) {
+    __host__ __device__ static void dN_at(T x, T y, T z, T (&d)[10][3]) {
         const T X0 = 1 - x - y - z, X1 = x, X2 = y, X3 = z;
         // vertices: d(Xi (2 Xi - 1)) = (4 Xi - 1) dXi, dX0 = (-1,-1,-1)
         const T c0 = 4 * X0 - 1;

@@ -16,37 +16,12 @@
 // consumer warp w takes row w of a stage, lane b its block b (wider rows in chunks of 32).
 // Waits are bounded; a wait that gives up sets LMTG_ERR_TIMEOUT in the scalar slot's status.
 #pragma once
+#include "ffloat.cuh"
 #include "spmv_bulk.cuh"
 
 namespace lmtg {
 
 namespace ff {
-
-// d = hi + lo: hi the leading 24 significant bits (truncated), lo the next 29 rounded to float;
-// zeros and values below 2^-126 give zeros (lo is dropped below 2^-74), on the integer pipe
-__device__ __forceinline__ void split(double d, float &hi, float &lo) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
-    const unsigned top = (unsigned)(b >> 32), sign = top & 0x80000000u;
-    const int ef = (int)((top >> 20) & 0x7ffu);
-    const int eh = ef - 896;  // float exponent field of hi
-    if (eh <= 0) {
-        hi = __uint_as_float(sign);
-        lo = 0.f;
-        return;
-    }
-    hi = __uint_as_float(sign | ((unsigned)eh << 23) | ((unsigned)(b >> 29) & 0x7fffffu));
-    const unsigned rem = (unsigned)b & 0x1fffffffu;
-    const int el = ef - 948;  // float exponent field of 2^(ef - 1075), the remainder's unit
-    lo = (el > 0 && rem) ? __uint_as_float(sign | __float_as_uint(__uint2float_rn(rem) * __uint_as_float((unsigned)el << 23)))
-                         : 0.f;
-}
-
-// s + e = a + b exactly (Knuth's two-sum)
-__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
-    s = a + b;
-    const float bb = s - a;
-    e = (a - (s - bb)) + (b - bb);
-}
 
 // running compensated sum (s, c) += (ph + pl) for a product split as ph + pl
 __device__ __forceinline__ void acc(float &s, float &c, float ph, float pl) {
@@ -56,7 +31,7 @@ __device__ __forceinline__ void acc(float &s, float &c, float ph, float pl) {
 }
 
 // (ah + al) (bh + bl) as ph + pl (the lo * lo term dropped)
-__device__ __forceinline__ void mul(float ah, float al, float bh, float bl, float &ph, float &pl) {
+__device__ __forceinline__ void mul_parts(float ah, float al, float bh, float bl, float &ph, float &pl) {
     ph = ah * bh;
     pl = fmaf(ah, bh, -ph);
     pl = fmaf(ah, bl, pl);
@@ -211,8 +186,8 @@ __global__ void __launch_bounds__(32 * (kCons + 1), kMinBlocks)
             if (I < g1) {
                 const uint32_t rb = sbp[slot][warp], d = sbp[slot][warp + 1] - rb;
                 // the row's right-hand side, loaded before the products
-                float bh = 0.f, bl = 0.f;
-                if ((lane & 7) == 0 && lane < 24) ff::split(b[3 * I + (lane >> 3)], bh, bl);
+                ff::f2 bs{0.f, 0.f};
+                if ((lane & 7) == 0 && lane < 24) bs = ff::split(b[3 * I + (lane >> 3)]);
                 float s[3] = {0.f, 0.f, 0.f}, c[3] = {0.f, 0.f, 0.f};
                 for (uint32_t c0 = 0; c0 < d; c0 += 32) {
                     const uint32_t bl_ = c0 + lane;
@@ -230,16 +205,16 @@ __global__ void __launch_bounds__(32 * (kCons + 1), kMinBlocks)
                         released = true;
                     }
                     if (on) {
-                        float xh[3], xl[3];
+                        ff::f2 xs[3];
 #pragma unroll
-                        for (int j = 0; j < 3; ++j) ff::split(__ldg(x + 3 * (uint64_t)J + j), xh[j], xl[j]);
+                        for (int j = 0; j < 3; ++j) xs[j] = ff::split(__ldg(x + 3 * (uint64_t)J + j));
 #pragma unroll
                         for (int r = 0; r < 3; ++r)
 #pragma unroll
                             for (int j = 0; j < 3; ++j) {
-                                float kh, kl, ph, pl;
-                                ff::split(m[3 * r + j], kh, kl);
-                                ff::mul(kh, kl, xh[j], xl[j], ph, pl);
+                                const ff::f2 kv = ff::split(m[3 * r + j]);
+                                float ph, pl;
+                                ff::mul_parts(kv.h, kv.l, xs[j].h, xs[j].l, ph, pl);
                                 ff::acc(s[r], c[r], ph, pl);
                             }
                     }
@@ -249,8 +224,8 @@ __global__ void __launch_bounds__(32 * (kCons + 1), kMinBlocks)
                 if ((lane & 7) == 0 && lane < 24) {
                     // r = b - q with b = bh + bl, q = qs + qc
                     float rh, e;
-                    ff::two_sum(bh, -qs, rh, e);
-                    const float ri = (rh + (e + (bl - qc))) * rscale;
+                    ff::two_sum(bs.h, -qs, rh, e);
+                    const float ri = (rh + (e + (bs.l - qc))) * rscale;
                     r32[3 * I + (lane >> 3)] = ri;
                     racc = fmaf(ri, ri, racc);
                 }

@@ -97,6 +97,31 @@ def test_element_matrices_match_oracle_on_distorted_mesh():
     f.close()
 
 
+@pytest.mark.parametrize("elem", ["hexa", "tetra10"])
+def test_element_matrices_of_a_small_mesh_far_from_the_origin(elem):
+    """The FP64 element matrices are formed in 48-bit float-float arithmetic from the node
+    coordinates relative to each element's first node: a 1e-2-sized distorted mesh moved to
+    (1000, -500, 250) keeps 1e-12 of the oracle's matrices (the oracle is given the same
+    translated element, where its own FP64 arithmetic has no offset to cancel)."""
+    make, ke = (make_rect_hexa, O.hexa8_ke) if elem == "hexa" else (make_rect_tetra10, O.tetra10_ke)
+    pos, conn = make(4)
+    rng = np.random.default_rng(11)
+    inner = np.all((pos > 1e-9) & (pos < 1 - 1e-9), axis=1)
+    pos = (pos + inner[:, None] * rng.uniform(-0.03, 0.03, pos.shape)) * 1e-2 + np.array([1000.0, -500.0, 250.0])
+    E = rng.uniform(5e4, 3e5, conn.shape[0])
+    f = Formulation(pos, conn)
+    f.elastic_modulus = E
+    f.poisson_ratio = 0.29
+    f.allocate_matrices()
+    f.assemble(True, False)
+    Ke = f.element_matrices(0, conn.shape[0])
+    for e in range(conn.shape[0]):
+        xyz = pos[conn[e]]
+        Ko = ke(xyz - xyz[0], E[e], 0.29)
+        assert np.abs(Ke[e] - Ko).max() <= 1e-12 * np.abs(Ko).max(), e
+    f.close()
+
+
 @pytest.mark.parametrize("name", ["hexa_2x2x2", "hexa_10x10x10", "tetra10_3x3x3"])
 @pytest.mark.parametrize("mode,tol", [("fp64", 1e-10), ("mixed", 1e-8)])
 def test_solution_matches_reference_ldl(golden_dir, name, mode, tol):
