@@ -312,8 +312,8 @@ int lmtg_batch_set_options(lmtg_ctx *ctx, int tile_rows, int variant);
 
 /* Mixed-precision solvers (lmtg_solve_system, lmtg_batch_solve, the diffusion steps): the
  * recursive-residual reduction of each FP32 segment before the FP64 residual replacement,
- * in (0, 1); 0 (default) = 1e-3 for the multigrid-preconditioned single-system solve, 0.01 for
- * the block-Jacobi solvers.  No reference counterpart. */
+ * in (0, 1); default 0.01 (1e-3 saved one refinement step on Hexa8 128^3 but made the
+ * continued-direction segments on Tetra10 40^3 stall).  No reference counterpart. */
 int lmtg_set_inner_reduction(lmtg_ctx *ctx, double inner_reduction);
 
 /* FP32 SpMV of the single-system PCG: 0 = one warp per pair of node rows, the matrix read

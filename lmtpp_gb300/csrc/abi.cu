@@ -470,7 +470,7 @@ int lmtg_batch_info(lmtg_ctx *c, int *tile_rows, int *variant, uint64_t *ntiles,
 
 int lmtg_set_inner_reduction(lmtg_ctx *c, double inner_reduction) {
     return guard(c, [&] {
-        LMTG_CHECK(inner_reduction >= 0 && inner_reduction < 1, LMTG_ERR_ARG, "inner_reduction in [0, 1)");
+        LMTG_CHECK(inner_reduction > 0 && inner_reduction < 1, LMTG_ERR_ARG, "inner_reduction in (0, 1)");
         c->inner_reduction = inner_reduction;
         return LMTG_OK;
     });

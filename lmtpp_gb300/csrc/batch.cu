@@ -1131,7 +1131,7 @@ int batch_solve(lmtg_ctx *c, int mode, double tol, int maxit, double timeout_s, 
         // FP32 segments with FP64 residual replacement, per pair (the single-system scheme):
         // each segment reduces its recursive residual by inner_reduction (or to the remaining target), the
         // direction is kept across the replacement while the true residual keeps halving.
-        const double kDelta = inner_reduction_for(c, false);
+        const double kDelta = c->inner_reduction;
         std::vector<double> s_prev(np, 0.0), rz_prev(np, 0.0), rel_prev(np, 0.0), sc(np), den(np), rzv(np), bt(np);
         std::vector<int> have_dir(np, 0);
         for (;;) {

@@ -771,7 +771,7 @@ static int diff_mixed(lmtg_ctx *c, const double *b, double *x, double tol, int m
     k_dot_s<<<ngrid(c), kRowThreads, 0, st>>>(b, b, c->nn, c->partials.p, &o->cnt_c, &o->rr);
     c->launches += 1;
     const double bb = read_rr();
-    const double kDelta = inner_reduction_for(c, false);
+    const double kDelta = c->inner_reduction;
     int total = 0, status = LMTG_OK, outer = 0;
     double s_prev = 0, rz_prev = 0, rel_prev = 0;
     bool have_dir = false;

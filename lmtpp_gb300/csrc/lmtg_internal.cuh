@@ -162,8 +162,8 @@ struct lmtg_ctx {
     std::vector<double> h_diff_src, h_diff_conv;  // constant step loads (sources, convection)
     lmtg::DBuf<double> diff_load;                  // their sum on the device (none: empty)
     // mixed solvers: recursive-residual reduction of each FP32 segment before the FP64 residual
-    // replacement (lmtg_set_inner_reduction; 0 = the solver's default, inner_reduction_for)
-    double inner_reduction = 0.0;
+    // replacement (lmtg_set_inner_reduction)
+    double inner_reduction = 0.01;
     lmtg::DBuf<float> Ke32, K32, Dinv32;
     bool have64 = false, have32 = false, have_vec = false;
     double max_diag = 0;
@@ -265,12 +265,6 @@ int solve_mixed(lmtg_ctx *c, double tol, int maxit, double timeout_s, lmtg_solve
 void profile_pcg(lmtg_ctx *c, bool fp32, int iters, double *spmv_ms, double *update_ms);
 // FP32 SpMV kind in use (0 warp-row, 1, 2 bulk copies)
 int spmv_kind_in_use(const lmtg_ctx *c);
-// Recursive-residual reduction of a mixed solver's FP32 segments: the value set by
-// lmtg_set_inner_reduction, else 1e-3 for the multigrid-preconditioned single-system solve (one
-// FP64 residual fewer at Hexa8 128^3, same FP32 iterations) and 1e-2 for the block-Jacobi ones.
-inline double inner_reduction_for(const lmtg_ctx *c, bool multigrid) {
-    return c->inner_reduction > 0 ? c->inner_reduction : (multigrid ? 1e-3 : 1e-2);
-}
 // per-stage device times of the multigrid-preconditioned FP32 iteration (amg.cu stages)
 void profile_amg(lmtg_ctx *c, int iters, double *ms);
 

@@ -504,7 +504,7 @@ int solve_mixed(lmtg_ctx *c, double tol, int maxit, double timeout_s, lmtg_solve
     const double bb = dot64(c, Fb, Fb);
     const bool amg = amg_prepare(c);
     ChunkGraph chunk;  // captured at the first segment, replayed by the others
-    const double kDelta = inner_reduction_for(c, amg);  // recursive-residual reduction per segment
+    const double kDelta = c->inner_reduction;  // recursive-residual reduction per segment
     int total = 0, outer = 0, status = LMTG_OK;
     double rel = 0, s_prev = 0, rz_prev = 0, rel_prev = 0;
     bool have_dir = false;

@@ -326,8 +326,7 @@ class Formulation:
         abi.check(self._lib.lmtg_set_nodal_springs(self._ctx, abi.ptr(k), abi.ptr(t)), self._ctx, "set_nodal_springs")
 
     def set_inner_reduction(self, inner_reduction):
-        """Recursive-residual reduction of each FP32 segment of the mixed solvers (0, the default: 1e-3
-        with the multigrid preconditioner, 0.01 with block Jacobi)."""
+        """Recursive-residual reduction of each FP32 segment of the mixed solvers (default 0.01)."""
         abi.check(self._lib.lmtg_set_inner_reduction(self._ctx, float(inner_reduction)), self._ctx,
                   "set_inner_reduction")
 
