@@ -6,10 +6,11 @@
 // and the row sums are formed in float-float arithmetic: each product K_ij x_j by the FMA-exact
 // two-product of the high parts plus the cross terms, accumulated with the error-free two-sum
 // and a running compensation (the compensated dot product of Ogita, Rump and Oishi, 2005).
-// The relative error of a sum is a few units of 2^-48, against the FP64 sum's 2^-53: at the
-// refinement's residuals (down to 1e-11 of |b|) the difference is four orders of magnitude
-// below the residual itself.  The residual is consumed only as the FP32 right-hand side of the
-// next segment and through |r|^2, so it is written rounded to float.
+// The relative error of a sum is a few units of 2^-48, against the FP64 sum's 2^-53; the mixed
+// solver uses this kernel while the residual is above 1e-9 of |b|, where that rounding stays
+// orders of magnitude below the residual, and the FP64 kernel below.  The residual is consumed
+// only as the FP32 right-hand side of the next segment and through |r|^2, so it is written
+// rounded to float.
 //
 // The matrix streams through shared memory by bulk copies (TMA), as in the FP32 bulk-copy SpMV:
 // one producer warp moves runs of up to kCons rows (at most kCap blocks) into a ring of stages;
