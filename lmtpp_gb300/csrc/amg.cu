@@ -67,6 +67,32 @@ __host__ __device__ __forceinline__ uint64_t kidxb(uint32_t rb, uint32_t deg, ui
 
 __device__ __forceinline__ bool done(const PcgScalars *S) { return S && *(volatile const int *)&S->done; }
 
+// Programmatic dependent launch: a cycle kernel launched with launch_pdl may be scheduled while
+// the previous kernel of the stream finishes.  It first waits until that kernel has completed
+// and its writes are visible (griddepcontrol.wait, a hardware wait, a no-op without the launch
+// attribute), then lets its own successor be scheduled (launch_dependents).  The cycle's coarse
+// levels are chains of short dependent launches; this hides part of each launch's latency.
+__device__ __forceinline__ void pdl_wait_trigger() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+template <class... KArgs, class... Args>
+static void launch_pdl(void (*kernel)(KArgs...), unsigned grid, unsigned block, size_t smem, cudaStream_t s,
+                       Args... args) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    LMTG_CUDA(cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...));
+}
+
 // ---------------------------------------------------------------------------------------------
 // numeric setup kernels
 // ---------------------------------------------------------------------------------------------
@@ -356,6 +382,7 @@ __global__ void __launch_bounds__(kRowThreads)
               const float *__restrict__ x, const float *__restrict__ r, float *__restrict__ res, uint64_t nn,
               const PcgScalars *S, const float *__restrict__ D = nullptr, float omega = 0.f,
               float *__restrict__ xpre = nullptr) {
+    pdl_wait_trigger();
     if (done(S)) return;
     const int lane = threadIdx.x & 31;
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -396,6 +423,7 @@ __global__ void __launch_bounds__(kRowThreads)
                const float *__restrict__ Dinv, const float *__restrict__ x, const float *__restrict__ r,
                float *__restrict__ xo, float omega, uint64_t nn, PcgScalars *S, bool with_rz, int start,
                double beta_den, double *partials) {
+    pdl_wait_trigger();
     if (done(S)) return;
     constexpr int VS = B == 3 ? 4 : 8;
     const int lane = threadIdx.x & 31;
@@ -450,6 +478,7 @@ __global__ void __launch_bounds__(kRowThreads)
     k_amg_restrict(const uint32_t *__restrict__ aptr, const uint32_t *__restrict__ anode, const float *__restrict__ Q,
                    const float *__restrict__ res, float *__restrict__ rc, uint64_t na, const float *__restrict__ Dc,
                    float omega_c, float *__restrict__ xc, const PcgScalars *S) {
+    pdl_wait_trigger();
     if (done(S)) return;
     const int lane = threadIdx.x & 31;
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -487,6 +516,7 @@ __global__ void __launch_bounds__(kRowThreads)
 template <int B, int ES>
 __global__ void k_amg_prolong(const uint32_t *__restrict__ agg, const float *__restrict__ Q, const float *__restrict__ e,
                               const float *__restrict__ e2, float *__restrict__ x, uint64_t nn, const PcgScalars *S) {
+    pdl_wait_trigger();
     if (done(S)) return;
     constexpr int VS = B == 3 ? 4 : 8;
     for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < (uint64_t)B * nn;
@@ -513,6 +543,7 @@ __global__ void k_amg_prolong(const uint32_t *__restrict__ agg, const float *__r
 // e = Cinv r on the coarsest level (warp per row)
 __global__ void k_amg_dense(const float *__restrict__ Cinv, const float *__restrict__ r, float *__restrict__ e, int n,
                             const PcgScalars *S) {
+    pdl_wait_trigger();
     if (done(S)) return;
     const int lane = threadIdx.x & 31;
     const int nw = (gridDim.x * blockDim.x) >> 5;
@@ -637,6 +668,8 @@ struct EpiPost {
             z[4 * I + lane] = zc;
             const float rc = lane == 0 ? p.r0 : (lane == 1 ? p.r1 : p.r2);
             acc = fmaf(rc, zc, acc);
+        } else if (lane == 3) {
+            z[4 * I + 3] = 0.f;  // the padding too: whole 16-byte nodes, no partially written sectors
         }
     }
     __device__ static unsigned *ticket(PcgScalars *S) { return &S->cnt_d; }
@@ -756,8 +789,8 @@ struct Bulk6 {
         grid() = c->sm_count * (nb > 0 ? nb : 1);
     }
     static void launch(const AmgLevel &L, const float *x, Epi epi, cudaStream_t s, PcgScalars *S) {
-        k_amg6_bulk<kSt, kCap, kCons, kMinB, Epi><<<grid(), 32 * (kCons + 1), bulk6_smem_bytes<kSt, kCap>(), s>>>(
-            L.bptr.p, L.bcol.p, L.K.p, x, epi, L.nn, S);
+        launch_pdl(k_amg6_bulk<kSt, kCap, kCons, kMinB, Epi>, grid(), 32 * (kCons + 1), bulk6_smem_bytes<kSt, kCap>(),
+                   s, L.bptr.p, L.bcol.p, L.K.p, x, epi, L.nn, S);
     }
 };
 
@@ -767,8 +800,8 @@ static void level_res(lmtg_ctx *c, const AmgLevel &L, const float *x, const floa
     if (L.bulk)
         Bulk6<Epi6Res>::launch(L, x, Epi6Res{r, res, D, omega, xpre}, s, S);
     else
-        k_amg_res<6><<<grid_for(c, L.nn * 32, kRowThreads, 8), kRowThreads, 0, s>>>(L.bptr.p, L.bcol.p, L.K.p, x, r,
-                                                                                    res, L.nn, S, D, omega, xpre);
+        launch_pdl(k_amg_res<6>, grid_for(c, L.nn * 32, kRowThreads, 8), kRowThreads, 0, s, L.bptr.p, L.bcol.p,
+                   L.K.p, x, r, res, L.nn, S, D, omega, xpre);
     c->launches += 1;
 }
 
@@ -778,8 +811,8 @@ static void level_post(lmtg_ctx *c, const AmgLevel &L, const float *x, const flo
     if (L.bulk)
         Bulk6<Epi6Post>::launch(L, x, Epi6Post{r, L.Dinv.p, x, xo, L.omega}, s, S);
     else
-        k_amg_post<6><<<grid_for(c, L.nn * 32, kRowThreads, 8), kRowThreads, 0, s>>>(
-            L.bptr.p, L.bcol.p, L.K.p, L.Dinv.p, x, r, xo, L.omega, L.nn, S, false, 0, 0.0, c->partials.p);
+        launch_pdl(k_amg_post<6>, grid_for(c, L.nn * 32, kRowThreads, 8), kRowThreads, 0, s, L.bptr.p, L.bcol.p,
+                   L.K.p, L.Dinv.p, x, r, xo, L.omega, L.nn, S, false, 0, 0.0, c->partials.p);
     c->launches += 1;
 }
 
@@ -1343,22 +1376,23 @@ static void coarse_cycle(lmtg_ctx *c, AmgState &A, size_t l, const float *rhs, f
     const size_t nl = A.levels.size();
     AmgLevel &L = *A.levels[l];
     if (l + 1 == nl) {
-        k_amg_dense<<<grid_for(c, (uint64_t)A.nc * 32, 256, 4), 256, 0, s>>>(A.Cinv.p, rhs, out, A.nc, S);
+        launch_pdl(k_amg_dense, grid_for(c, (uint64_t)A.nc * 32, 256, 4), 256, 0, s, A.Cinv.p, rhs, out, A.nc, S);
         c->launches += 1;
         return;
     }
     AmgLevel &N = *A.levels[l + 1];
     const bool ncoarsest = l + 2 == nl;
     level_res(c, L, L.xa.p, rhs, L.res.p, nullptr, 0.f, nullptr, s, S);
-    k_amg_restrict<6><<<grid_for(c, L.nagg * 32, kRowThreads, 8), kRowThreads, 0, s>>>(
-        L.aptr.p, L.anode.p, L.Q.p, L.res.p, N.r.p, L.nagg, ncoarsest ? nullptr : N.Dinv.p, N.omega, N.xa.p, S);
+    launch_pdl(k_amg_restrict<6>, grid_for(c, L.nagg * 32, kRowThreads, 8), kRowThreads, 0, s, L.aptr.p, L.anode.p,
+               L.Q.p, L.res.p, N.r.p, L.nagg, ncoarsest ? nullptr : N.Dinv.p, N.omega, N.xa.p, S);
     float *e, *e2;
     coarse_correction(c, A, l, s, S, e, e2);
     const int tb = 256;
     if (ncoarsest)
-        k_amg_prolong<6, 6><<<grid_for(c, 6 * L.nn, tb), tb, 0, s>>>(L.agg.p, L.Q.p, e, nullptr, L.xa.p, L.nn, S);
+        launch_pdl(k_amg_prolong<6, 6>, grid_for(c, 6 * L.nn, tb), tb, 0, s, L.agg.p, L.Q.p, e, nullptr, L.xa.p, L.nn,
+                   S);
     else
-        k_amg_prolong<6, 8><<<grid_for(c, 6 * L.nn, tb), tb, 0, s>>>(L.agg.p, L.Q.p, e, e2, L.xa.p, L.nn, S);
+        launch_pdl(k_amg_prolong<6, 8>, grid_for(c, 6 * L.nn, tb), tb, 0, s, L.agg.p, L.Q.p, e, e2, L.xa.p, L.nn, S);
     level_post(c, L, L.xa.p, rhs, out, s, S);
     c->launches += 2;
 }
@@ -1393,9 +1427,10 @@ void amg_launch_cycle(lmtg_ctx *c, const float *r, float *z, cudaStream_t s, int
     mark(2);
     const int tb = 256;
     if (ncoarsest)
-        k_amg_prolong<3, 6><<<grid_for(c, 3 * L.nn, tb), tb, 0, s>>>(L.agg.p, L.Q.p, e, nullptr, L.xa.p, L.nn, S);
+        launch_pdl(k_amg_prolong<3, 6>, grid_for(c, 3 * L.nn, tb), tb, 0, s, L.agg.p, L.Q.p, e, nullptr, L.xa.p, L.nn,
+                   S);
     else
-        k_amg_prolong<3, 8><<<grid_for(c, 3 * L.nn, tb), tb, 0, s>>>(L.agg.p, L.Q.p, e, e2, L.xa.p, L.nn, S);
+        launch_pdl(k_amg_prolong<3, 8>, grid_for(c, 3 * L.nn, tb), tb, 0, s, L.agg.p, L.Q.p, e, e2, L.xa.p, L.nn, S);
     mark(3);
     if (warp_rows)
         k_amg_post<3><<<g0, kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, c->K32.p, c->Dinv32.p, L.xa.p, r, z, L.omega,

@@ -134,6 +134,9 @@ __global__ void __launch_bounds__(32 * (kCons + 1), kMinBlocks)
                 const float *__restrict__ x, Epi epi, uint64_t nn, PcgScalars *S) {
     static_assert(kCons >= 1 && kCons <= 31, "the producer sizes a stage with one warp of bptr loads");
     using St = Bulk6Stage<kCap>;
+    // programmatic dependent launch (see the multigrid's launch_pdl): wait for the previous
+    // kernel's writes.  No early trigger: its successor starts when this stream ends
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     if (S && *(volatile int *)&S->done) return;
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t full[kStages], empty[kStages];

@@ -14,8 +14,6 @@
 // that loads the library holds this array until the process exits.  All calls share it and it
 // keeps the last call's contents, so calls that overlap on the GPU (different streams, or
 // different host threads) race and must be serialized by the caller.
-#include <mutex>
-
 #include "solver_kernels.cuh"
 
 namespace {
@@ -29,10 +27,6 @@ constexpr size_t kScratchBytes = kPartialsBytes + 256;  // + ticket (u32) and re
 // Device code may name this array directly; host code must use the address obtained with
 // cudaGetSymbolAddress (the host-side name is only a stand-in, not a device address).
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
-
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mutex;
-unsigned char *g_scratch_addr[kMaxDevices] = {nullptr};
 
 // One node row per warp, one block per 8 rows (no grid stride: one partial per block).
 __global__ void __launch_bounds__(lmtg::kRowThreads)
@@ -58,18 +52,13 @@ __global__ void __launch_bounds__(lmtg::kRowThreads)
     if (lmtg::grid_reduce<1, 0u>(v, partials, ticket, out) && threadIdx.x == 0) *rr_out = out[0];
 }
 
-// Per-device set-up, done by the first call on each device with that device current.
+// The scratch array's address in the current device's context, looked up on every call (no
+// allocation; cheap): a cached address would go stale after a device reset or a new primary
+// context reloads the module.
 int scratch_for_current_device(unsigned char **out) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return LMTG_ERR_CUDA;
-    if (dev < 0 || dev >= kMaxDevices) return LMTG_ERR_UNSUPPORTED;
-    std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_addr[dev]) {
-        void *p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return LMTG_ERR_CUDA;
-        g_scratch_addr[dev] = static_cast<unsigned char *>(p);
-    }
-    *out = g_scratch_addr[dev];
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return LMTG_ERR_CUDA;
+    *out = static_cast<unsigned char *>(p);
     return LMTG_OK;
 }
 

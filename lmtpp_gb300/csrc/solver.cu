@@ -258,9 +258,10 @@ __global__ void k_pcg_start_amg(const float *__restrict__ r, const float *__rest
          I += (uint64_t)gridDim.x * blockDim.x) {
         const float *D = Dinv + 9 * I;
         const float r0 = r[3 * I], r1 = r[3 * I + 1], r2 = r[3 * I + 2];
-        xa[4 * I] = omega * (D[0] * r0 + D[1] * r1 + D[2] * r2);
-        xa[4 * I + 1] = omega * (D[3] * r0 + D[4] * r1 + D[5] * r2);
-        xa[4 * I + 2] = omega * (D[6] * r0 + D[7] * r1 + D[8] * r2);
+        // whole 16-byte nodes (zero padding): no partially written sectors
+        reinterpret_cast<float4 *>(xa)[I] = make_float4(omega * (D[0] * r0 + D[1] * r1 + D[2] * r2),
+                                                        omega * (D[3] * r0 + D[4] * r1 + D[5] * r2),
+                                                        omega * (D[6] * r0 + D[7] * r1 + D[8] * r2), 0.f);
         t[0] += r0 * r0 + r1 * r1 + r2 * r2;
         if (b) {
             const float b0 = b[3 * I], b1 = b[3 * I + 1], b2 = b[3 * I + 2];
@@ -294,10 +295,12 @@ __global__ void k_pcg_update_amg(float *__restrict__ x, float *__restrict__ r, c
     for (uint64_t I = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; I < nn;
          I += (uint64_t)gridDim.x * blockDim.x) {
         float rv[3];
+        const float4 p4 = reinterpret_cast<const float4 *>(p)[I];
+        const float pv[3] = {p4.x, p4.y, p4.z};
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             const uint64_t i = 3 * I + c;
-            const float dx = alpha * p[4 * I + c];
+            const float dx = alpha * pv[c];
             x[i] += dx;
             rv[c] = fmaf(-alpha, q[i], r[i]);
             r[i] = rv[c];
@@ -306,9 +309,9 @@ __global__ void k_pcg_update_amg(float *__restrict__ x, float *__restrict__ r, c
             t[3] = fmaxf(t[3], fabsf(rv[c]));
         }
         const float *D = Dinv + 9 * I;
-        xa[4 * I] = omega * (D[0] * rv[0] + D[1] * rv[1] + D[2] * rv[2]);
-        xa[4 * I + 1] = omega * (D[3] * rv[0] + D[4] * rv[1] + D[5] * rv[2]);
-        xa[4 * I + 2] = omega * (D[6] * rv[0] + D[7] * rv[1] + D[8] * rv[2]);
+        reinterpret_cast<float4 *>(xa)[I] = make_float4(omega * (D[0] * rv[0] + D[1] * rv[1] + D[2] * rv[2]),
+                                                        omega * (D[3] * rv[0] + D[4] * rv[1] + D[5] * rv[2]),
+                                                        omega * (D[6] * rv[0] + D[7] * rv[1] + D[8] * rv[2]), 0.f);
         t[0] += rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
     }
     double out[4];
