@@ -55,7 +55,7 @@ extern "C" {
 
 /* ---- preconditioners of the FP32 inner PCG (lmtg_set_preconditioner) ---- */
 #define LMTG_PREC_BLOCK_JACOBI 0 /* inverse 3x3 diagonal blocks */
-#define LMTG_PREC_AMG 1          /* aggregation multigrid V-cycle (the default) */
+#define LMTG_PREC_AMG 1          /* aggregation multigrid W-cycle (the default) */
 
 /* ---- stopping criteria ---- */
 #define LMTG_CRIT_REL_RESIDUAL 0   /* |b - K u|_2 <= tol |b|_2 */
@@ -376,9 +376,10 @@ int lmtg_recalage_assemble(lmtg_ctx *ctx);
 
 /* Preconditioner of the FP32 inner PCG of the mixed solve (LMTG_SOLVE_MIXED_IR), standing in
  * for the reference's sequential incomplete Cholesky (include/containers/matinvsparse.h:201-261,
- * MatWithTinyBlocks.h:426-585).  LMTG_PREC_AMG (default): one V-cycle of an unsmoothed-aggregation
- * multigrid whose coarse spaces carry the six rigid-body modes per aggregate, damped block-Jacobi
- * smoothing, a dense coarsest level; used for single-system Hexa8 / Tetra10 elasticity of at
+ * MatWithTinyBlocks.h:426-585).  LMTG_PREC_AMG (default): one W-cycle of an unsmoothed-aggregation
+ * multigrid (every level above the coarsest visits the next level twice) whose coarse spaces
+ * carry the six rigid-body modes per aggregate, damped block-Jacobi smoothing, a dense coarsest
+ * level; used for single-system Hexa8 / Tetra10 elasticity of at
  * least 3,000 unknowns, block Jacobi otherwise (batches, recalage, small systems).  Its structure
  * is built at the first mixed solve after lmtg_allocate_matrices or lmtg_set_constraints (nodes
  * with a constraint stay out of the coarse spaces), its numeric part at the first mixed solve

@@ -4,8 +4,8 @@
 // (include/containers/matinvsparse.h:201-261, 3x3-block variant
 // include/containers/MatWithTinyBlocks.h:426-585), which has no parallel form; block Jacobi, its
 // stand-in here, needs O(mesh side) iterations (2,388 at Hexa8 128^3).  This file replaces z = P r
-// by one V-cycle of an unsmoothed-aggregation multigrid whose coarse spaces hold the rigid-body
-// modes, so that the iteration count stays nearly flat with the mesh size.
+// by one W-cycle of an unsmoothed-aggregation multigrid whose coarse spaces hold the rigid-body
+// modes, so that the iteration count stays nearly flat with the mesh size (41 at Hexa8 128^3).
 //
 // Hierarchy (structure built once per pattern and constraint set, on the host):
 //   level 0   the context's 3x3-block matrix K32 (planar rows, kidx), its block-Jacobi Dinv32
@@ -25,12 +25,15 @@
 // twelve power steps, which approach it from below; the weight of a degree-1 Chebyshev smoother on
 // [h/30, h], h = 1.2 lambda).
 //
-// V-cycle (z = M r), per level: x = omega D^-1 r; res = r - K x; restrict Q^T res; recurse;
-// x += Q e; x' = x + omega D^-1 (r - K x).  The same smoother before and after makes M symmetric,
-// as the conjugate gradient needs.  At level 0 the first smoothing step is fused into the PCG's
-// update kernel and the last one writes z and forms r.z and beta; at the coarser levels the
-// first smoothing step is fused into the restriction that produces the level's right-hand side.  Every kernel returns at once
-// once the PCG's `done` flag is set, so the cycle runs inside the captured iteration chunks.
+// W-cycle (z = M r), per level: x = omega D^-1 r; res = r - K x; restrict Q^T res; the coarse
+// correction e (the next level's cycle run twice, the second time on the residual the first
+// leaves; one dense solve on the coarsest); x += 1.5 Q e; x' = x + omega D^-1 (r - K x).  The
+// same smoother before and after makes M symmetric, as the conjugate gradient needs.  At level 0
+// the first smoothing step is fused into the PCG's update kernel and the last one writes z and
+// forms r.z and beta; at the coarser levels the first smoothing step is fused into the
+// restriction (or residual) that produces the level's right-hand side.  Large 6x6 levels stream
+// their matrix by bulk copies (amg_bulk6.cuh).  Every kernel returns at once once the PCG's
+// `done` flag is set, so the cycle runs inside the captured iteration chunks.
 #include <algorithm>
 #include <chrono>
 #include <cmath>

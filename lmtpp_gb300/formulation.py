@@ -331,7 +331,7 @@ class Formulation:
                   "set_inner_reduction")
 
     def set_preconditioner(self, kind):
-        """'amg' (default: aggregation multigrid V-cycle) or 'block_jacobi' for the FP32 inner PCG of
+        """'amg' (default: aggregation multigrid W-cycle) or 'block_jacobi' for the FP32 inner PCG of
         the mixed solve; the FP64 PCG always uses block Jacobi."""
         k = {"block_jacobi": abi.PREC_BLOCK_JACOBI, "amg": abi.PREC_AMG}[kind]
         abi.check(self._lib.lmtg_set_preconditioner(self._ctx, k), self._ctx, "set_preconditioner")
