@@ -112,12 +112,44 @@ constexpr int kGalWarps = 8;
 // shared memory of one warp for coarse rows of at most cap blocks: acc[cap][36], stage[32][36], slot[32]
 __host__ __device__ constexpr size_t gal_warp_bytes(int cap) { return 4u * (36u * cap + 36u * 32u + 32u); }
 
+// Slot of every fine block (I, J) in its coarse row: the position of agg(J) among the sorted
+// columns of agg(I)'s row (kNoSlot when J is in no aggregate).  Depends only on the patterns and
+// the aggregation: computed once per structure, read by every Galerkin product.
+constexpr uint8_t kNoSlot = 0xff;
+static_assert(kGalMaxDeg < kNoSlot, "coarse slots fit a byte");
+
+__global__ void k_gal_slots(const uint32_t *__restrict__ fbptr, const uint32_t *__restrict__ fbcol,
+                            const uint32_t *__restrict__ agg, uint64_t nn, const uint32_t *__restrict__ cbptr,
+                            const uint32_t *__restrict__ cbcol, uint8_t *__restrict__ gslot) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t i = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; i < nn; i += nw) {
+        const uint32_t a = agg[i];
+        const uint32_t rb = fbptr[i], deg = fbptr[i + 1] - rb;
+        for (uint32_t bl = lane; bl < deg; bl += 32) {
+            uint8_t slot = kNoSlot;
+            const uint32_t J = agg[fbcol[rb + bl]];
+            if (a != kNone && J != kNone) {
+                const uint32_t crb = cbptr[a], cdeg = cbptr[a + 1] - crb;
+                uint32_t lo = 0, hi = cdeg;  // J is in the row: lower_bound finds it
+                while (lo < hi) {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    if (cbcol[crb + mid] < J) lo = mid + 1;
+                    else hi = mid;
+                }
+                slot = (uint8_t)lo;
+            }
+            gslot[rb + bl] = slot;
+        }
+    }
+}
+
 template <int B>
 __global__ void __launch_bounds__(32 * kGalWarps)
     k_galerkin(const uint32_t *__restrict__ fbptr, const uint32_t *__restrict__ fbcol, const float *__restrict__ fK,
                const uint32_t *__restrict__ agg, const uint32_t *__restrict__ aptr, const uint32_t *__restrict__ anode,
                const float *__restrict__ Q, const uint32_t *__restrict__ cbptr, const uint32_t *__restrict__ cbcol,
-               uint64_t na, int cap, float *__restrict__ cK) {
+               const uint8_t *__restrict__ gslot, uint64_t na, int cap, float *__restrict__ cK) {
     extern __shared__ __align__(16) unsigned char gal_raw[];
     float *wbase = reinterpret_cast<float *>(gal_raw + (threadIdx.x >> 5) * gal_warp_bytes(cap));
     float(*acc)[36] = reinterpret_cast<float(*)[36]>(wbase);
@@ -138,15 +170,9 @@ __global__ void __launch_bounds__(32 * kGalWarps)
                 const uint32_t bl = c0 + lane;
                 int slot = -1;
                 if (bl < deg) {
-                    const uint32_t j = fbcol[rb + bl], J = agg[j];
-                    if (J != kNone) {
-                        uint32_t lo = 0, hi = cdeg;  // J is in the row: lower_bound finds it
-                        while (lo < hi) {
-                            const uint32_t mid = (lo + hi) >> 1;
-                            if (crow[mid] < J) lo = mid + 1;
-                            else hi = mid;
-                        }
-                        slot = (int)lo;
+                    const uint32_t j = fbcol[rb + bl], gs = gslot[rb + bl];
+                    if (gs != kNoSlot) {
+                        slot = (int)gs;
                         float A[B * B];
 #pragma unroll
                         for (int v = 0; v < B * B; ++v) A[v] = fK[kidxb<B>(rb, deg, bl, v)];
@@ -1203,7 +1229,19 @@ static void amg_build_structure(lmtg_ctx *c) {
             }
         }
     }
-    if (A->nc) A->Cinv.alloc((size_t)A->nc * A->nc);
+    if (A->nc) {
+        A->Cinv.alloc((size_t)A->nc * A->nc);
+        // coarse slots of every fine block, read by each numeric setup's Galerkin products
+        for (size_t l = 0; l + 1 < A->levels.size(); ++l) {
+            AmgLevel &F = *A->levels[l], &C = *A->levels[l + 1];
+            F.gslot.alloc(F.nnzb);
+            k_gal_slots<<<grid_for(c, F.nn * 32, kRowThreads, 8), kRowThreads, 0, s>>>(
+                l == 0 ? c->bptr.p : F.bptr.p, l == 0 ? c->bcol.p : F.bcol.p, F.agg.p, F.nn, C.bptr.p, C.bcol.p,
+                F.gslot.p);
+            LMTG_CUDA(cudaGetLastError());
+            c->launches += 1;
+        }
+    }
     A->power.alloc(2 * kPowerSteps * kMaxLevels);
     A->structure_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     c->amg = A.release();
@@ -1227,10 +1265,10 @@ static void amg_numeric(lmtg_ctx *c) {
         const int g = grid_for(c, F.nagg * 32, 32 * kGalWarps, 8);
         if (F.b == 3)
             k_galerkin<3><<<g, 32 * kGalWarps, smem, s>>>(fbptr, fbcol, fK, F.agg.p, F.aptr.p, F.anode.p, F.Q.p, C.bptr.p,
-                                                          C.bcol.p, F.nagg, cap, C.K.p);
+                                                          C.bcol.p, F.gslot.p, F.nagg, cap, C.K.p);
         else
             k_galerkin<6><<<g, 32 * kGalWarps, smem, s>>>(fbptr, fbcol, fK, F.agg.p, F.aptr.p, F.anode.p, F.Q.p, C.bptr.p,
-                                                          C.bcol.p, F.nagg, cap, C.K.p);
+                                                          C.bcol.p, F.gslot.p, F.nagg, cap, C.K.p);
         k_block_inv6<<<grid_for(c, C.nn, 128), 128, 0, s>>>(C.bptr.p, C.bdiag.p, C.K.p, C.nn, C.Dinv.p);
         LMTG_CUDA(cudaGetLastError());
         c->launches += 2;

@@ -26,6 +26,7 @@ struct AmgLevel {
     DBuf<uint32_t> agg;          // node -> aggregate (0xffffffff: in none)
     DBuf<uint32_t> aptr, anode;  // aggregate -> nodes
     DBuf<float> Q;               // tentative prolongator, b x 6 per node (row-major)
+    DBuf<uint8_t> gslot;         // per fine block: slot of its coarse block in the coarse row
 };
 
 struct AmgState {
