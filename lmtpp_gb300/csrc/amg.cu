@@ -511,32 +511,39 @@ __global__ void __launch_bounds__(kRowThreads)
     if (done(S)) return;
     const int lane = threadIdx.x & 31;
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const int cc = lane >> 2;  // lane 4c ends with component c of the reduce-scatter
+    const bool own = (lane & 3) == 0;
     for (uint64_t a = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; a < na; a += nw) {
+        // the coarse block-Jacobi row, loaded before the products
+        float d[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        if (Dc && own && cc < 6) {
+#pragma unroll
+            for (int k = 0; k < 6; ++k) d[k] = Dc[36 * a + 6 * cc + k];
+        }
         float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         for (uint32_t k = aptr[a] + lane; k < aptr[a + 1]; k += 32) {
             const uint32_t i = anode[k];
-            const float *q = Q + (uint64_t)i * B * 6;
+            // the node's prolongator rows as 8-byte pairs (B x 6 floats at 8-byte aligned offsets)
+            const float2 *q2 = reinterpret_cast<const float2 *>(Q + (uint64_t)i * B * 6);
 #pragma unroll
             for (int r = 0; r < B; ++r) {
                 const float v = res[(uint64_t)B * i + r];
-#pragma unroll
-                for (int c = 0; c < 6; ++c) acc[c] = fmaf(q[6 * r + c], v, acc[c]);
+                const float2 q01 = q2[3 * r], q23 = q2[3 * r + 1], q45 = q2[3 * r + 2];
+                acc[0] = fmaf(q01.x, v, acc[0]);
+                acc[1] = fmaf(q01.y, v, acc[1]);
+                acc[2] = fmaf(q23.x, v, acc[2]);
+                acc[3] = fmaf(q23.y, v, acc[3]);
+                acc[4] = fmaf(q45.x, v, acc[4]);
+                acc[5] = fmaf(q45.y, v, acc[5]);
             }
         }
+        const float t = reduce_scatter6(acc, lane);
+        if (own && cc < 6) rc[6 * a + cc] = t;
+        if (Dc) {
+            float x = 0.f;
 #pragma unroll
-        for (int c = 0; c < 6; ++c) acc[c] = warp_sum(acc[c]);
-        if (lane < 6) {
-            float v = acc[0];
-#pragma unroll
-            for (int c = 1; c < 6; ++c) v = lane == c ? acc[c] : v;
-            rc[6 * a + lane] = v;
-            if (Dc) {
-                const float *D = Dc + 36 * a + 6 * lane;
-                float x = 0.f;
-#pragma unroll
-                for (int k = 0; k < 6; ++k) x = fmaf(D[k], acc[k], x);
-                xc[8 * a + lane] = omega_c * x;
-            }
+            for (int k = 0; k < 6; ++k) x = fmaf(d[k], __shfl_sync(0xffffffffu, t, 4 * k), x);
+            if (own) xc[8 * a + cc] = cc < 6 ? omega_c * x : 0.f;  // padding too: whole 32-byte nodes
         }
     }
 }
@@ -554,7 +561,9 @@ __global__ void k_amg_prolong(const uint32_t *__restrict__ agg, const float *__r
         const int r = (int)(t - (uint64_t)B * i);
         const uint32_t a = agg[i];
         if (a == kNone) continue;
-        const float *q = Q + (i * B + r) * 6;
+        const float2 *q2 = reinterpret_cast<const float2 *>(Q + (i * B + r) * 6);  // 8-byte aligned rows
+        const float2 q01 = q2[0], q23 = q2[1], q45 = q2[2];
+        const float q[6] = {q01.x, q01.y, q23.x, q23.y, q45.x, q45.y};
         const float *ev = e + (uint64_t)ES * a;
         float s = 0.f;
         if (e2) {
