@@ -285,6 +285,8 @@ __global__ void k_pcg_start_amg(const float *__restrict__ r, const float *__rest
     }
 }
 
+constexpr int kUpdNodes = 2;  // nodes a thread takes per step in k_pcg_update_amg (4: 128 registers, slower)
+
 __global__ void k_pcg_update_amg(float *__restrict__ x, float *__restrict__ r, const float *__restrict__ p,
                                  const float *__restrict__ q, const float *__restrict__ Dinv, float *__restrict__ xa,
                                  float omega, uint64_t nn, PcgScalars *S, double *partials) {
@@ -292,27 +294,56 @@ __global__ void k_pcg_update_amg(float *__restrict__ x, float *__restrict__ r, c
     const double pq = S->pq;
     const float alpha = (float)S->alpha;
     float t[4] = {0.f, 0.f, 0.f, 0.f};  // rr, dx2, dxinf, rinf
-    for (uint64_t I = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; I < nn;
-         I += (uint64_t)gridDim.x * blockDim.x) {
-        float rv[3];
-        const float4 p4 = reinterpret_cast<const float4 *>(p)[I];
-        const float pv[3] = {p4.x, p4.y, p4.z};
+    // kUpdNodes nodes per step (I, I + stride, ...), every load issued before the arithmetic
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t I0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; I0 < nn; I0 += kUpdNodes * stride) {
+        uint64_t Is[kUpdNodes];
+        bool on[kUpdNodes];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            const uint64_t i = 3 * I + c;
-            const float dx = alpha * pv[c];
-            x[i] += dx;
-            rv[c] = fmaf(-alpha, q[i], r[i]);
-            r[i] = rv[c];
-            t[1] = fmaf(dx, dx, t[1]);
-            t[2] = fmaxf(t[2], fabsf(dx));
-            t[3] = fmaxf(t[3], fabsf(rv[c]));
+        for (int u = 0; u < kUpdNodes; ++u) {
+            Is[u] = I0 + u * stride;
+            on[u] = Is[u] < nn;
         }
-        const float *D = Dinv + 9 * I;
-        reinterpret_cast<float4 *>(xa)[I] = make_float4(omega * (D[0] * rv[0] + D[1] * rv[1] + D[2] * rv[2]),
-                                                        omega * (D[3] * rv[0] + D[4] * rv[1] + D[5] * rv[2]),
-                                                        omega * (D[6] * rv[0] + D[7] * rv[1] + D[8] * rv[2]), 0.f);
-        t[0] += rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
+        float xv[kUpdNodes][3], rv0[kUpdNodes][3], qv[kUpdNodes][3], pv[kUpdNodes][3], D[kUpdNodes][9];
+#pragma unroll
+        for (int u = 0; u < kUpdNodes; ++u) {
+            if (!on[u]) continue;
+            const uint64_t I = Is[u];
+            const float4 p4 = reinterpret_cast<const float4 *>(p)[I];
+            pv[u][0] = p4.x;
+            pv[u][1] = p4.y;
+            pv[u][2] = p4.z;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                xv[u][c] = x[3 * I + c];
+                rv0[u][c] = r[3 * I + c];
+                qv[u][c] = q[3 * I + c];
+            }
+#pragma unroll
+            for (int k = 0; k < 9; ++k) D[u][k] = Dinv[9 * I + k];
+        }
+#pragma unroll
+        for (int u = 0; u < kUpdNodes; ++u) {
+            if (!on[u]) continue;
+            const uint64_t I = Is[u];
+            float rv[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float dx = alpha * pv[u][c];
+                x[3 * I + c] = xv[u][c] + dx;
+                rv[c] = fmaf(-alpha, qv[u][c], rv0[u][c]);
+                r[3 * I + c] = rv[c];
+                t[1] = fmaf(dx, dx, t[1]);
+                t[2] = fmaxf(t[2], fabsf(dx));
+                t[3] = fmaxf(t[3], fabsf(rv[c]));
+            }
+            const float *Du = D[u];
+            reinterpret_cast<float4 *>(xa)[I] =
+                make_float4(omega * (Du[0] * rv[0] + Du[1] * rv[1] + Du[2] * rv[2]),
+                            omega * (Du[3] * rv[0] + Du[4] * rv[1] + Du[5] * rv[2]),
+                            omega * (Du[6] * rv[0] + Du[7] * rv[1] + Du[8] * rv[2]), 0.f);
+            t[0] += rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
+        }
     }
     double out[4];
     if (grid_reduce_t<4, (4u | 8u)>(t, partials, &S->cnt_b, out) && threadIdx.x == 0) {

@@ -291,9 +291,25 @@ template <class T, int VS>
 __global__ void k_pcg_dir(const T *__restrict__ z, T *__restrict__ p, uint64_t nn, const PcgScalars *S) {
     if (*(volatile const int *)&S->done) return;
     const T beta = (T)S->beta;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < VS * nn;
-         i += (uint64_t)gridDim.x * blockDim.x)
-        p[i] = beta != (T)0 ? fma(beta, p[i], z[i]) : z[i];
+    if constexpr (sizeof(T) == 4 && VS == 4) {  // whole 16-byte nodes
+        const float4 *z4 = reinterpret_cast<const float4 *>(z);
+        float4 *p4 = reinterpret_cast<float4 *>(p);
+        for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nn;
+             i += (uint64_t)gridDim.x * blockDim.x) {
+            const float4 zv = z4[i];
+            if (beta != (T)0) {
+                const float4 pv = p4[i];
+                p4[i] = make_float4(fmaf(beta, pv.x, zv.x), fmaf(beta, pv.y, zv.y), fmaf(beta, pv.z, zv.z),
+                                    fmaf(beta, pv.w, zv.w));
+            } else {
+                p4[i] = zv;
+            }
+        }
+    } else {
+        for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < VS * nn;
+             i += (uint64_t)gridDim.x * blockDim.x)
+            p[i] = beta != (T)0 ? fma(beta, p[i], z[i]) : z[i];
+    }
 }
 
 // Matrix values and column indices are read once per SpMV: they are loaded with the
