@@ -27,7 +27,7 @@ struct Hexa8 {
     }
     // shape functions at the reference point (x, y, z)
     template <class T>
-    __host__ __device__ static void N_at(T x, T y, T z, T (&N)[8]) {
+    __device__ static void N_at(T x, T y, T z, T (&N)[8]) {
         const T mx = 1 - x, my = 1 - y, mz = 1 - z;
         N[0] = mx * my * mz; N[1] = x * my * mz; N[2] = x * y * mz; N[3] = mx * y * mz;
         N[4] = mx * my * z;  N[5] = x * my * z;  N[6] = x * y * z;  N[7] = mx * y * z;
@@ -66,7 +66,7 @@ struct Tetra10 {
         dN_at(x, y, z, d);
     }
     template <class T>
-    __host__ __device__ static void N_at(T x, T y, T z, T (&N)[10]) {
+    __device__ static void N_at(T x, T y, T z, T (&N)[10]) {
         const T X[4] = {1 - x - y - z, x, y, z};
 #pragma unroll
         for (int i = 0; i < 4; ++i) N[i] = X[i] * (2 * X[i] - 1);
