@@ -697,33 +697,50 @@ static int diff_pcg_t(lmtg_ctx *c, const T *K, const T *Dinv, const T *b, T *x, 
                                                                 kSBulkThreads, smem));
         gr_bulk = c->sm_count * (nb > 0 ? nb : 1);
     }
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    LMTG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    for (int k = 0; k < kIters; ++k) {
-        k_pcg_dir_s<T><<<ngrid(c), kRowThreads, 0, s>>>(z, p, c->nn, c->scal.p);
-        if constexpr (std::is_same<T, float>::value) {
-            if (sbulk)
-                k_pcg_spmv_s_bulk<kSStages, kSCap>
-                    <<<gr_bulk, kSBulkThreads, sbulk_smem_bytes<kSStages, kSCap>(), s>>>(
-                        c->bptr.p, c->bcol.p, K, p, q, c->nn, c->scal.p, c->partials.p);
-            else
+    // the chunk graph of this precision, reused while it was captured on the same buffers
+    DiffGraph &dg = c->diff_graph[std::is_same<T, float>::value ? 1 : 0];
+    const void *key[9] = {K, Dinv, b, x, r, z, p, q, reinterpret_cast<const void *>((uintptr_t)sbulk)};
+    bool cached = dg.exec != nullptr;
+    for (int i = 0; i < 9 && cached; ++i) cached = dg.key[i] == key[i];
+    if (!cached) {
+        if (dg.exec) cudaGraphExecDestroy(dg.exec);
+        if (dg.graph) cudaGraphDestroy(dg.graph);
+        dg.exec = nullptr;
+        dg.graph = nullptr;
+    }
+    cudaGraph_t graph = dg.graph;
+    cudaGraphExec_t exec = dg.exec;
+    if (!cached) {
+        LMTG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        for (int k = 0; k < kIters; ++k) {
+            k_pcg_dir_s<T><<<ngrid(c), kRowThreads, 0, s>>>(z, p, c->nn, c->scal.p);
+            if constexpr (std::is_same<T, float>::value) {
+                if (sbulk)
+                    k_pcg_spmv_s_bulk<kSStages, kSCap>
+                        <<<gr_bulk, kSBulkThreads, sbulk_smem_bytes<kSStages, kSCap>(), s>>>(
+                            c->bptr.p, c->bcol.p, K, p, q, c->nn, c->scal.p, c->partials.p);
+                else
+                    k_pcg_spmv_s<T><<<gr, kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, K, p, q, c->nn, c->scal.p,
+                                                               c->partials.p);
+            } else {
                 k_pcg_spmv_s<T><<<gr, kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, K, p, q, c->nn, c->scal.p,
                                                            c->partials.p);
-        } else {
-            k_pcg_spmv_s<T><<<gr, kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, K, p, q, c->nn, c->scal.p,
-                                                       c->partials.p);
+            }
+            k_pcg_update_s<T><<<ngrid(c), kRowThreads, 0, s>>>(x, r, z, p, q, Dinv, c->nn, c->scal.p,
+                                                               c->partials.p);
         }
-        k_pcg_update_s<T><<<ngrid(c), kRowThreads, 0, s>>>(x, r, z, p, q, Dinv, c->nn, c->scal.p,
-                                                           c->partials.p);
+        cudaError_t ce = cudaStreamEndCapture(s, &graph);
+        if (ce != cudaSuccess) throw Error{LMTG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce)};
+        ce = cudaGraphInstantiate(&exec, graph, 0);
+        if (ce != cudaSuccess) {
+            cudaGraphDestroy(graph);
+            throw Error{LMTG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce)};
+        }
+        dg.graph = graph;
+        dg.exec = exec;
+        for (int i = 0; i < 9; ++i) dg.key[i] = key[i];
     }
-    cudaError_t ce = cudaStreamEndCapture(s, &graph);
-    if (ce != cudaSuccess) throw Error{LMTG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce)};
-    ce = cudaGraphInstantiate(&exec, graph, 0);
-    if (ce != cudaSuccess) {
-        cudaGraphDestroy(graph);
-        throw Error{LMTG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce)};
-    }
+    cudaError_t ce = cudaSuccess;
     LMTG_CUDA(cudaMemcpyAsync(c->h_scal, c->scal.p, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
     LMTG_CUDA(cudaStreamSynchronize(s));
     bool finished = c->h_scal[0].done != 0;
@@ -735,16 +752,21 @@ static int diff_pcg_t(lmtg_ctx *c, const T *K, const T *Dinv, const T *b, T *x, 
             ce = cudaMemcpyAsync(c->h_scal, c->scal.p, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s);
         if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
         if (ce != cudaSuccess) {
-            cudaGraphExecDestroy(exec);
-            cudaGraphDestroy(graph);
+            diff_graphs_free(c);
             throw Error{LMTG_ERR_CUDA, std::string("pcg chunk: ") + cudaGetErrorString(ce)};
         }
         finished = c->h_scal[0].done != 0;
     }
-    cudaGraphExecDestroy(exec);
-    cudaGraphDestroy(graph);
     *iters = c->h_scal[0].iter;
     return finished ? c->h_scal[0].status : LMTG_ERR_NOT_CONVERGED;
+}
+
+void diff_graphs_free(lmtg_ctx *c) {
+    for (DiffGraph &dg : c->diff_graph) {
+        if (dg.exec) cudaGraphExecDestroy(dg.exec);
+        if (dg.graph) cudaGraphDestroy(dg.graph);
+        dg = DiffGraph{};
+    }
 }
 
 static int diff_pcg64(lmtg_ctx *c, const double *b, double *x, double tol, int maxit, int *iters) {
@@ -1236,6 +1258,7 @@ int lmtg_diff_mesh_set(lmtg_ctx *c, uint64_t nn, const double *pos, uint64_t ne,
         for (uint64_t q = 0; q < 6 * ne; ++q) LMTG_CHECK(conn[q] < nn, LMTG_ERR_ARG, "node id >= nn");
         recal_free(c);
         amg_free(c);
+        diff_graphs_free(c);
         c->elem_type = LMTG_ELEM_TRIANGLE6;
         c->npe = 6;
         c->nnu = 1;

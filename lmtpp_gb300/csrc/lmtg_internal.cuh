@@ -108,6 +108,16 @@ struct RecalState;  // recalage.cu
 struct AmgState;    // amg.cu
 }
 
+namespace lmtg {
+// A captured chunk of the diffusion PCG, replayed by later solves while its arguments (the
+// buffers it was captured on) are the same.
+struct DiffGraph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    const void *key[9] = {};
+};
+}  // namespace lmtg
+
 struct lmtg_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -164,6 +174,7 @@ struct lmtg_ctx {
     // mixed solvers: recursive-residual reduction of each FP32 segment before the FP64 residual
     // replacement (lmtg_set_inner_reduction)
     double inner_reduction = 0.01;
+    lmtg::DiffGraph diff_graph[2];  // the diffusion PCG's chunk graphs, [0] FP64, [1] FP32
     lmtg::DBuf<float> Ke32, K32, Dinv32;
     bool have64 = false, have32 = false, have_vec = false;
     double max_diag = 0;
@@ -248,6 +259,8 @@ void amg_free(lmtg_ctx *c);
 
 // ---- batches (batch.cu) ----
 void batch_free(lmtg_ctx *c);
+// destroys the diffusion PCG's cached chunk graphs (diffusion.cu)
+void diff_graphs_free(lmtg_ctx *c);
 void batch_set_rhs(lmtg_ctx *c, int nrhs, const double *B_host);
 int batch_solve(lmtg_ctx *c, int mode, double tol, int maxit, double timeout_s, lmtg_solve_stats *st,
                 int *pair_iters);
