@@ -164,6 +164,7 @@ int lmtg_destroy(lmtg_ctx *c) {
     batch_free(c);
     recal_free(c);
     amg_free(c);
+    samg_free(c);
     diff_graphs_free(c);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;  // DBuf destructors free device memory

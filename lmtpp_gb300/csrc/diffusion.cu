@@ -19,9 +19,11 @@
 #include <cmath>
 #include <cstring>
 #include <exception>
+#include <memory>
 #include <new>
 #include <vector>
 
+#include "pdl.cuh"
 #include "spmv_bulk.cuh"
 
 namespace lmtg {
@@ -359,7 +361,26 @@ __global__ void __launch_bounds__(kRowThreads)
 // Each product is rounded and then added in column order, as in csr_stream32, so q is
 // bit-identical to k_pcg_spmv_s; p.q is summed in another fixed order.  Every wait is bounded; one that gives up sets
 // LMTG_ERR_TIMEOUT and done in the PCG scalars.
+// The epilogue Epi gives the gathered vector (x), what a row's sum becomes (row) and, with
+// kReduce, the grid total of the rows' contributions (total, by the thread that finishes it):
+// the PCG's q = K p with p.q, and the multigrid's level-0 residual and post-smoothing.
 constexpr int kSBulkCons = 8;
+
+struct EpiSPq {  // q = K p; p.q, alpha = rz / p.q
+    const float *p;
+    float *q;
+    static constexpr bool kReduce = true;
+    __device__ __forceinline__ float x(uint32_t j) const { return __ldg(p + j); }
+    __device__ __forceinline__ void row(uint64_t I, float v, float &acc) const {
+        q[I] = v;
+        acc = fmaf(p[I], v, acc);
+    }
+    __device__ __forceinline__ unsigned *ticket(PcgScalars *S) const { return &S->cnt_a; }
+    __device__ __forceinline__ void total(double v, PcgScalars *S) const {
+        S->pq = v;
+        S->alpha = S->rz / (v + (v == 0.0 ? 1.0 : 0.0));
+    }
+};
 constexpr int kSBulkThreads = 32 * (kSBulkCons + 1);
 
 template <int kCap>
@@ -376,11 +397,13 @@ constexpr size_t sbulk_smem_bytes() {
     return (size_t)kStages * SBulkStage<kCap>::kBytes;
 }
 
-template <int kStages, int kCap>
+// the ring the solvers launch: two stages of up to 3072 entries (a 32-row chunk must fit one)
+constexpr int kSStages = 2, kSCap = 3072;
+
+template <int kStages, int kCap, class Epi>
 __global__ void __launch_bounds__(kSBulkThreads, 4)
     k_pcg_spmv_s_bulk(const uint32_t *__restrict__ rp, const uint32_t *__restrict__ col,
-                      const float *__restrict__ K, const float *__restrict__ p, float *__restrict__ q,
-                      uint64_t n, PcgScalars *S, double *partials) {
+                      const float *__restrict__ K, Epi epi, uint64_t n, PcgScalars *S, double *partials) {
     using St = SBulkStage<kCap>;
     if (*(volatile int *)&S->done) return;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -493,26 +516,22 @@ __global__ void __launch_bounds__(kSBulkThreads, 4)
                 if (I < R1) {
                     const uint32_t rs = sR[I - rbase], re = sR[I + 1 - rbase];
 #pragma unroll 4
-                    for (uint32_t qq = rs; qq < re; ++qq) v += __fmul_rn(sK[qq - kbase], __ldg(p + sC[qq - kbase]));
+                    for (uint32_t qq = rs; qq < re; ++qq) v += __fmul_rn(sK[qq - kbase], epi.x(sC[qq - kbase]));
                 }
                 __syncwarp();
                 if (lane == 0) bulk::mbar_arrive(&empty[slot]);
-                if (I < R1) {
-                    q[I] = v;
-                    acc = fmaf(p[I], v, acc);
-                }
+                if (I < R1) epi.row(I, v, acc);
             } else {
                 __syncwarp();
                 if (lane == 0) bulk::mbar_arrive(&empty[slot]);
             }
         }
     }
-    __syncthreads();
-    const float t[1] = {acc};
-    double out[1];
-    if (grid_reduce_t<1, 0u>(t, partials, &S->cnt_a, out) && threadIdx.x == 0) {
-        S->pq = out[0];
-        S->alpha = S->rz / (out[0] + (out[0] == 0.0 ? 1.0 : 0.0));
+    if constexpr (Epi::kReduce) {
+        __syncthreads();
+        const float t[1] = {acc};
+        double out[1];
+        if (grid_reduce_t<1, 0u>(t, partials, epi.ticket(S), out) && threadIdx.x == 0) epi.total(out[0], S);
     }
 }
 
@@ -646,13 +665,751 @@ __global__ void k_dot_s(const double *__restrict__ a, const double *__restrict__
     if (grid_reduce<1, 0u>(v, partials, ticket, out) && threadIdx.x == 0) *out_p = out[0];
 }
 
-// PCG (Jacobi) on K x = b in precision T, from the current x (x_zero: x is 0, r = b).  b_norm2 >= 0
-// gives |b|^2 for the relative test; beta_den > 0 continues the search direction held in p
-// (reliable update).  Returns the status; *iters the iterations.
+// ---- scalar aggregation multigrid for the FP32 diffusion PCG --------------------------------
+//
+// Jacobi needs O(mesh side) iterations on A = M/dt + theta K (about 620 per implicit-Euler step
+// of the 1024^2 workload).  With lmtg_set_preconditioner(LMTG_PREC_AMG) (the default) and at least
+// kSMinUnknowns unknowns, z = M r is one W-cycle of an unsmoothed-aggregation multigrid built for
+// the scalar matrix, the elasticity multigrid's scheme with one mode per aggregate:
+//   aggregation   the node graph's greedy aggregates (a root with its free neighbours, leftovers
+//                 joined to the aggregate they touch most, the rest grouped around a free node);
+//                 Dirichlet (penalty) nodes stay out
+//   prolongator   q_i = B_i / |B|_aggregate: the constant at level 0 (B = 1), then the previous
+//                 level's normalisation (B = |B|_aggregate) -- the piecewise-constant modes
+//   coarse A      Q^T A Q, thread per aggregate in a fixed order (deterministic)
+//   smoother      damped Jacobi omega = 1 / theta of a degree-1 Chebyshev on [h/30, h], h = 1.2
+//                 lambda_max(D^-1 A) (twelve power steps), the same before and after
+//   cycle         x = omega D^-1 r; res = r - A x; restrict; the coarse correction (a dense solve
+//                 on the coarsest, else the next level's cycle: twice below level 0, the second
+//                 on the residual the first leaves, once deeper); x += Q e;
+//                 x' = x + omega D^-1 (r - A x)
+// The matrices are constant over the time steps, so the hierarchy is built once per diff_setup
+// (structure on the host, numeric part on the device) at the first FP32 solve.
+constexpr uint64_t kSMinUnknowns = 3000, kSCoarsest = 500;
+constexpr int kSMaxLevels = 10, kSGalCap = 64, kSPowerSteps = 12;
+constexpr size_t kSWLevels = 1;  // levels whose coarse correction visits the next level twice
+constexpr uint8_t kSNoSlot = 0xff;
+constexpr uint32_t kSNone = 0xffffffffu;
+
+// level-0 passes of the cycle on the bulk-copy pipeline
+struct EpiSRes {  // res = r - A x
+    const float *xv, *r;
+    float *res;
+    static constexpr bool kReduce = false;
+    __device__ __forceinline__ float x(uint32_t j) const { return __ldg(xv + j); }
+    __device__ __forceinline__ void row(uint64_t I, float v, float &) const { res[I] = r[I] - v; }
+};
+struct EpiSPost {  // z = x + omega D^-1 (r - A x); r.z into rz and beta (as k_s_post)
+    const float *xv, *r, *D;
+    float *z;
+    float omega;
+    int start;
+    double beta_den;
+    static constexpr bool kReduce = true;
+    __device__ __forceinline__ float x(uint32_t j) const { return __ldg(xv + j); }
+    __device__ __forceinline__ void row(uint64_t I, float v, float &acc) const {
+        const float ri = r[I];
+        const float zi = xv[I] + omega * D[I] * (ri - v);
+        z[I] = zi;
+        acc = fmaf(ri, zi, acc);
+    }
+    __device__ __forceinline__ unsigned *ticket(PcgScalars *S) const { return &S->cnt_d; }
+    __device__ __forceinline__ void total(double v, PcgScalars *S) const {
+        if (start) S->beta = beta_den > 0.0 ? v / beta_den : 0.0;
+        else S->beta = v / S->rz;
+        S->rz = v;
+        if (!isfinite(v)) {
+            S->status = LMTG_ERR_NAN;
+            S->done = 1;
+        }
+    }
+};
+
+struct SLevel {
+    uint64_t n = 0, nnz = 0;
+    DBuf<uint32_t> rp, col;            // levels >= 1 (level 0: the context's pattern)
+    DBuf<float> A, Dinv;               // levels >= 1 (level 0: K32, Dinv32)
+    float omega = 1.f;
+    double lambda = 0;
+    DBuf<float> r, xa, xb, res, r2, xb2;  // right-hand side, iterates, residual, second visit
+    // transfer to the next coarser level
+    uint64_t nagg = 0;
+    DBuf<uint32_t> agg, aptr, anode;
+    DBuf<float> q;        // prolongator value per node
+    DBuf<uint8_t> gslot;  // per entry: slot of agg(col) in agg(row)'s coarse row
+};
+
+struct SAmg {
+    std::vector<std::unique_ptr<SLevel>> lv;
+    int nc = 0;  // unknowns of the dense coarsest level
+    DBuf<float> Cinv;
+    DBuf<double> power;
+    int gres = 0, gpost = 0;  // grids of the level-0 bulk-copy passes
+};
+
+void samg_free(lmtg_ctx *c) {
+    if (!c->samg) return;
+    diff_graphs_free(c);  // graphs captured on its buffers
+    delete c->samg;
+    c->samg = nullptr;
+}
+
+// slot of every fine entry's coarse column in its coarse row (rows of aggregated nodes)
+__global__ void k_s_slots(const uint32_t *__restrict__ rp, const uint32_t *__restrict__ col,
+                          const uint32_t *__restrict__ agg, uint64_t n, const uint32_t *__restrict__ crp,
+                          const uint32_t *__restrict__ ccol, uint8_t *__restrict__ gslot) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t a = agg[i];
+        for (uint32_t e = rp[i]; e < rp[i + 1]; ++e) {
+            uint8_t s = kSNoSlot;
+            const uint32_t J = agg[col[e]];
+            if (a != kSNone && J != kSNone) {
+                uint32_t lo = crp[a], hi = crp[a + 1];  // J is in the row: lower_bound finds it
+                while (lo < hi) {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    if (ccol[mid] < J) lo = mid + 1;
+                    else hi = mid;
+                }
+                s = (uint8_t)(lo - crp[a]);
+            }
+            gslot[e] = s;
+        }
+    }
+}
+
+// coarse row a of Q^T A Q, thread per aggregate: its nodes' entries summed in order in a
+// slot-major shared accumulator (conflict-free: acc[slot][thread])
+constexpr int kSGalThreads = 128;
+__global__ void __launch_bounds__(kSGalThreads)
+    k_s_galerkin(const uint32_t *__restrict__ rp, const uint32_t *__restrict__ col, const float *__restrict__ A,
+                 const uint8_t *__restrict__ gslot, const float *__restrict__ q, const uint32_t *__restrict__ aptr,
+                 const uint32_t *__restrict__ anode, uint64_t na, const uint32_t *__restrict__ crp,
+                 const uint32_t *__restrict__ ccol, float *__restrict__ cA) {
+    __shared__ float acc[kSGalCap][kSGalThreads];
+    const int t = threadIdx.x;
+    for (uint64_t a = blockIdx.x * (uint64_t)blockDim.x + t; a < na; a += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t cb = crp[a], cdeg = crp[a + 1] - cb;
+        for (uint32_t s = 0; s < cdeg; ++s) acc[s][t] = 0.f;
+        for (uint32_t u = aptr[a]; u < aptr[a + 1]; ++u) {
+            const uint32_t i = anode[u];
+            const float qi = q[i];
+            for (uint32_t e = rp[i]; e < rp[i + 1]; ++e) {
+                const uint8_t s = gslot[e];
+                if (s != kSNoSlot) acc[s][t] += qi * A[e] * q[col[e]];
+            }
+        }
+        for (uint32_t s = 0; s < cdeg; ++s) {
+            float v = acc[s][t];
+            if (ccol[cb + s] == a && v == 0.f) v = 1.f;  // a decoupled unknown keeps a unit diagonal
+            cA[cb + s] = v;
+        }
+    }
+}
+
+__global__ void k_s_dinv(const uint32_t *__restrict__ rp, const uint32_t *__restrict__ col,
+                         const float *__restrict__ A, uint64_t n, float *__restrict__ Dinv) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        float d = 1.f;
+        for (uint32_t e = rp[i]; e < rp[i + 1]; ++e)
+            if (col[e] == i) d = A[e];
+        Dinv[i] = d != 0.f ? 1.f / d : 1.f;
+    }
+}
+
+__device__ __forceinline__ bool s_done(const PcgScalars *S) { return S && *(volatile const int *)&S->done; }
+
+// one power step w = D^-1 A v / |v| (|v|^2 = the previous step's |w|^2 in prev; 1 on the first),
+// |w|^2 reduced into out
+__global__ void __launch_bounds__(kRowThreads)
+    k_s_power(const uint32_t *__restrict__ rp, const uint32_t *__restrict__ col, const float *__restrict__ A,
+              const float *__restrict__ Dinv, const float *__restrict__ v, float *__restrict__ w, uint64_t n,
+              const double *prev, double *partials, unsigned *ticket, double *out) {
+    __shared__ float tiles[kRowWarps][kTile];
+    const int wp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float sc = 1.f;
+    if (prev) {
+        const float p = (float)*prev;
+        sc = p > 0.f ? rsqrtf(p) : 1.f;
+    }
+    float acc = 0.f;
+    const ChunkRange cr = cta_chunks(n);
+    for (uint64_t ch = cr.first + wp; ch < cr.end; ch += kRowWarps) {
+        const float y = csr_stream32(rp, col, A, ch * 32, n, tiles[wp], [&](uint32_t j) { return __ldg(v + j); });
+        const uint64_t I = ch * 32 + lane;
+        if (I < n) {
+            const float wi = sc * Dinv[I] * y;
+            w[I] = wi;
+            acc = fmaf(wi, wi, acc);
+        }
+    }
+    const float t[1] = {acc};
+    double o[1];
+    if (grid_reduce_t<1, 0u>(t, partials, ticket, o) && threadIdx.x == 0) *out = o[0];
+}
+
+// v = pseudo-random start in [-1, 1)
+__global__ void k_s_rand(float *__restrict__ v, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t h = (uint32_t)(i * 2654435761ull) ^ 0x9e3779b9u;
+        h ^= h >> 16;
+        h *= 0x7feb352du;
+        h ^= h >> 15;
+        v[i] = (float)(h & 0xffffff) * (2.0f / 16777216.0f) - 1.0f;
+    }
+}
+
+// res = r - A x; with D also the next visit's first smoothing step xpre = omega D^-1 res
+__global__ void __launch_bounds__(kRowThreads)
+    k_s_res(const uint32_t *__restrict__ rp, const uint32_t *__restrict__ col, const float *__restrict__ A,
+            const float *__restrict__ x, const float *__restrict__ r, float *__restrict__ res, uint64_t n,
+            const PcgScalars *S, const float *__restrict__ D, float omega, float *__restrict__ xpre) {
+    pdl_wait_trigger();
+    if (s_done(S)) return;
+    __shared__ float tiles[kRowWarps][kTile];
+    const int wp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const ChunkRange cr = cta_chunks(n);
+    for (uint64_t ch = cr.first + wp; ch < cr.end; ch += kRowWarps) {
+        const float y = csr_stream32(rp, col, A, ch * 32, n, tiles[wp], [&](uint32_t j) { return __ldg(x + j); });
+        const uint64_t I = ch * 32 + lane;
+        if (I < n) {
+            const float ri = r[I] - y;
+            res[I] = ri;
+            if (D) xpre[I] = omega * D[I] * ri;
+        }
+    }
+}
+
+// xo = x + omega D^-1 (r - A x); with S_rz (level 0 inside the PCG) r.xo is reduced into rz and
+// beta (beta = rz / rz_old, or on a start rz / beta_den when beta_den > 0, else 0)
+__global__ void __launch_bounds__(kRowThreads)
+    k_s_post(const uint32_t *__restrict__ rp, const uint32_t *__restrict__ col, const float *__restrict__ A,
+             const float *__restrict__ Dinv, const float *__restrict__ x, const float *__restrict__ r,
+             float *__restrict__ xo, float omega, uint64_t n, PcgScalars *S, bool with_rz, int start,
+             double beta_den, double *partials) {
+    pdl_wait_trigger();
+    if (s_done(S)) return;
+    __shared__ float tiles[kRowWarps][kTile];
+    const int wp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float acc = 0.f;
+    const ChunkRange cr = cta_chunks(n);
+    for (uint64_t ch = cr.first + wp; ch < cr.end; ch += kRowWarps) {
+        const float y = csr_stream32(rp, col, A, ch * 32, n, tiles[wp], [&](uint32_t j) { return __ldg(x + j); });
+        const uint64_t I = ch * 32 + lane;
+        if (I < n) {
+            const float ri = r[I];
+            const float z = x[I] + omega * Dinv[I] * (ri - y);
+            xo[I] = z;
+            acc = fmaf(ri, z, acc);
+        }
+    }
+    if (!with_rz) return;
+    const float t[1] = {acc};
+    double out[1];
+    if (grid_reduce_t<1, 0u>(t, partials, &S->cnt_d, out) && threadIdx.x == 0) {
+        if (start) S->beta = beta_den > 0.0 ? out[0] / beta_den : 0.0;
+        else S->beta = out[0] / S->rz;
+        S->rz = out[0];
+        if (!isfinite(out[0])) {
+            S->status = LMTG_ERR_NAN;
+            S->done = 1;
+        }
+    }
+}
+
+// rc = Q^T res per aggregate (thread per aggregate: its node list in order); with Dc also
+// xc = omega_c Dc^-1 rc.  Streaming the lists warp-wide as matrix rows (csr_stream32) took 1.5x
+// longer: the gathers of res are what costs, and fewer of them were in flight.
+__global__ void k_s_restrict(const uint32_t *__restrict__ aptr, const uint32_t *__restrict__ anode,
+                             const float *__restrict__ q, const float *__restrict__ res, float *__restrict__ rc,
+                             uint64_t na, const float *__restrict__ Dc, float omega_c, float *__restrict__ xc,
+                             const PcgScalars *S) {
+    pdl_wait_trigger();
+    if (s_done(S)) return;
+    for (uint64_t a = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; a < na; a += (uint64_t)gridDim.x * blockDim.x) {
+        float v = 0.f;
+        for (uint32_t u = aptr[a]; u < aptr[a + 1]; ++u) {
+            const uint32_t i = anode[u];
+            v = fmaf(q[i], res[i], v);
+        }
+        rc[a] = v;
+        if (Dc) xc[a] = omega_c * Dc[a] * v;
+    }
+}
+
+// x += q (e + e2)[agg] per node (e2 may be null), four nodes per 16-byte access
+__device__ __forceinline__ float s_corr(uint32_t a, float q, const float *e, const float *e2) {
+    if (a == kSNone) return 0.f;
+    return q * (e2 ? e[a] + e2[a] : e[a]);
+}
+__global__ void k_s_prolong(const uint32_t *__restrict__ agg, const float *__restrict__ q, const float *__restrict__ e,
+                            const float *__restrict__ e2, float *__restrict__ x, uint64_t n, const PcgScalars *S) {
+    pdl_wait_trigger();
+    if (s_done(S)) return;
+    const uint64_t step = (uint64_t)gridDim.x * blockDim.x, i0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    const uint64_t n4 = n / 4;
+    for (uint64_t g = i0; g < n4; g += step) {
+        const uint4 a = reinterpret_cast<const uint4 *>(agg)[g];
+        const float4 qq = reinterpret_cast<const float4 *>(q)[g];
+        float4 xx = reinterpret_cast<const float4 *>(x)[g];
+        xx.x += s_corr(a.x, qq.x, e, e2);
+        xx.y += s_corr(a.y, qq.y, e, e2);
+        xx.z += s_corr(a.z, qq.z, e, e2);
+        xx.w += s_corr(a.w, qq.w, e, e2);
+        reinterpret_cast<float4 *>(x)[g] = xx;
+    }
+    for (uint64_t i = 4 * n4 + i0; i < n; i += step) x[i] += s_corr(agg[i], q[i], e, e2);
+}
+
+// e = Cinv r on the coarsest level (warp per row)
+__global__ void k_s_dense(const float *__restrict__ Cinv, const float *__restrict__ r, float *__restrict__ e, int n,
+                          const PcgScalars *S) {
+    pdl_wait_trigger();
+    if (s_done(S)) return;
+    const int lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < n; row += nw) {
+        float s = 0.f;
+        for (int k = lane; k < n; k += 32) s = fmaf(Cinv[(uint64_t)row * n + k], r[k], s);
+        s = warp_sum(s);
+        if (lane == 0) e[row] = s;
+    }
+}
+
+// AMG start / update of the FP32 PCG: the update kernel's x, r and stopping test, and the
+// cycle's first smoothing step xa = omega D^-1 r; z, rz and beta come from the cycle
+__global__ void k_pcg_start_s_amg(const float *__restrict__ r, const float *__restrict__ b,
+                                  const float *__restrict__ Dinv, float *__restrict__ xa, float omega, uint64_t n,
+                                  PcgScalars *S, double *partials) {
+    float t[2] = {0.f, 0.f};  // rr, bb
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const float ri = r[i];
+        xa[i] = omega * Dinv[i] * ri;
+        t[0] = fmaf(ri, ri, t[0]);
+        if (b) t[1] = fmaf(b[i], b[i], t[1]);
+    }
+    double out[2];
+    if (grid_reduce_t<2, 0u>(t, partials, &S->cnt_c, out) && threadIdx.x == 0) {
+        S->rr = out[0];
+        if (b) S->bb = out[1];
+        S->iter = 0;
+        S->status = LMTG_OK;
+        S->done = (out[0] <= S->crit * S->crit * S->bb) ? 1 : 0;
+        if (!isfinite(out[0])) {
+            S->done = 1;
+            S->status = LMTG_ERR_NAN;
+        }
+    }
+}
+
+__global__ void k_pcg_update_s_amg(float *__restrict__ x, float *__restrict__ r, const float *__restrict__ p,
+                                   const float *__restrict__ q, const float *__restrict__ Dinv, float *__restrict__ xa,
+                                   float omega, uint64_t n, PcgScalars *S, double *partials) {
+    if (*(volatile int *)&S->done) return;
+    const double pq = S->pq;
+    const float alpha = (float)S->alpha;
+    float t[1] = {0.f};
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        x[i] = fmaf(alpha, p[i], x[i]);
+        const float ri = fmaf(-alpha, q[i], r[i]);
+        r[i] = ri;
+        xa[i] = omega * Dinv[i] * ri;
+        t[0] = fmaf(ri, ri, t[0]);
+    }
+    double out[1];
+    if (grid_reduce_t<1, 0u>(t, partials, &S->cnt_b, out) && threadIdx.x == 0) {
+        S->iter += 1;
+        S->rr = out[0];
+        if (!isfinite(out[0]) || !isfinite(pq)) {
+            S->status = LMTG_ERR_NAN;
+            S->done = 1;
+        } else if (out[0] <= S->crit * S->crit * S->bb) {
+            S->done = 1;
+        } else if (S->iter >= S->maxit) {
+            S->status = LMTG_ERR_NOT_CONVERGED;
+            S->done = 1;
+        }
+    }
+}
+
+// greedy aggregation of a node graph (rows rp/col), skip[i] = nodes left out; returns aggregates
+static uint64_t s_aggregate(uint64_t n, const std::vector<uint32_t> &rp, const std::vector<uint32_t> &col,
+                            const std::vector<uint8_t> &skip, std::vector<uint32_t> &agg) {
+    agg.assign(n, kSNone);
+    std::vector<uint8_t> state(n, 0);  // 0 free, 1 aggregated, 2 skipped
+    for (uint64_t i = 0; i < n; ++i)
+        if (!skip.empty() && skip[i]) state[i] = 2;
+    uint64_t na = 0;
+    // pass 1: roots whose free neighbours are all unaggregated take them all
+    for (uint64_t i = 0; i < n; ++i) {
+        if (state[i] != 0) continue;
+        bool ok = true;
+        for (uint32_t e = rp[i]; e < rp[i + 1] && ok; ++e) ok = state[col[e]] != 1;
+        if (!ok) continue;
+        for (uint32_t e = rp[i]; e < rp[i + 1]; ++e) {
+            const uint32_t j = col[e];
+            if (state[j] == 0) {
+                agg[j] = (uint32_t)na;
+                state[j] = 1;
+            }
+        }
+        agg[i] = (uint32_t)na;
+        state[i] = 1;
+        ++na;
+    }
+    // pass 2: leftovers join the neighbouring aggregate they touch most (the lowest on ties)
+    std::vector<uint32_t> cand;
+    for (uint64_t i = 0; i < n; ++i) {
+        if (state[i] != 0) continue;
+        cand.clear();
+        for (uint32_t e = rp[i]; e < rp[i + 1]; ++e)
+            if (agg[col[e]] != kSNone) cand.push_back(agg[col[e]]);
+        if (cand.empty()) continue;
+        std::sort(cand.begin(), cand.end());
+        uint32_t best = cand[0];
+        size_t bc = 0;
+        for (size_t k = 0; k < cand.size();) {
+            size_t m = k;
+            while (m < cand.size() && cand[m] == cand[k]) ++m;
+            if (m - k > bc) {
+                bc = m - k;
+                best = cand[k];
+            }
+            k = m;
+        }
+        agg[i] = best;
+        state[i] = 1;
+    }
+    // pass 3: the rest grouped around a free node
+    for (uint64_t i = 0; i < n; ++i) {
+        if (state[i] != 0) continue;
+        for (uint32_t e = rp[i]; e < rp[i + 1]; ++e) {
+            const uint32_t j = col[e];
+            if (state[j] == 0) {
+                agg[j] = (uint32_t)na;
+                state[j] = 1;
+            }
+        }
+        agg[i] = (uint32_t)na;
+        state[i] = 1;
+        ++na;
+    }
+    return na;
+}
+
+template <class T>
+static void s_upload(DBuf<T> &d, const std::vector<T> &h, cudaStream_t s) {
+    d.alloc(h.size() ? h.size() : 1);
+    if (!h.empty()) LMTG_CUDA(cudaMemcpyAsync(d.p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+}
+
+// Hierarchy of the context's scalar matrix: structure (host), then the numeric part (device)
+static void samg_build(lmtg_ctx *c) {
+    Phase ph("lmtg.diff.amg");
+    cudaStream_t s = c->stream;
+    std::unique_ptr<SAmg> M(new SAmg());
+    // level 0 pattern from the device
+    std::vector<uint32_t> rp(c->nn + 1), col;
+    LMTG_CUDA(cudaMemcpyAsync(rp.data(), c->bptr.p, 4 * rp.size(), cudaMemcpyDeviceToHost, s));
+    LMTG_CUDA(cudaStreamSynchronize(s));
+    col.resize(rp.back());
+    LMTG_CUDA(cudaMemcpyAsync(col.data(), c->bcol.p, 4 * col.size(), cudaMemcpyDeviceToHost, s));
+    LMTG_CUDA(cudaStreamSynchronize(s));
+    std::vector<uint8_t> skip(c->nn, 0);
+    for (uint32_t d : c->h_cdof)
+        if (d < c->nn) skip[d] = 1;
+    std::vector<double> B(c->nn, 1.0);
+    uint64_t n = c->nn;
+    for (int l = 0;; ++l) {
+        std::unique_ptr<SLevel> L(new SLevel());
+        L->n = n;
+        L->nnz = rp.back();
+        L->r.alloc(n + 4);
+        L->res.alloc(n + 4);
+        L->xa.alloc(n + 4);
+        L->xb.alloc(n + 4);
+        if (l >= 1) {
+            L->r2.alloc(n + 4);
+            L->xb2.alloc(n + 4);
+            s_upload(L->rp, rp, s);
+            s_upload(L->col, col, s);
+            L->A.alloc(L->nnz);
+            L->Dinv.alloc(n);
+        }
+        const bool coarsest = n <= kSCoarsest || l + 1 >= kSMaxLevels;
+        if (coarsest) {
+            M->lv.push_back(std::move(L));
+            break;
+        }
+        std::vector<uint32_t> agg;
+        const uint64_t na = s_aggregate(n, rp, col, l == 0 ? skip : std::vector<uint8_t>(), agg);
+        // aggregate lists, prolongator values, coarse modes
+        std::vector<uint32_t> aptr(na + 1, 0), anode;
+        for (uint64_t i = 0; i < n; ++i)
+            if (agg[i] != kSNone) ++aptr[agg[i] + 1];
+        for (uint64_t a = 0; a < na; ++a) aptr[a + 1] += aptr[a];
+        anode.resize(aptr[na]);
+        {
+            std::vector<uint32_t> fill(aptr.begin(), aptr.end() - 1);
+            for (uint64_t i = 0; i < n; ++i)
+                if (agg[i] != kSNone) anode[fill[agg[i]]++] = (uint32_t)i;
+        }
+        std::vector<double> Bc(na, 0.0);
+        for (uint64_t i = 0; i < n; ++i)
+            if (agg[i] != kSNone) Bc[agg[i]] += B[i] * B[i];
+        for (auto &v : Bc) v = std::sqrt(v);
+        std::vector<float> q(n, 0.f);
+        for (uint64_t i = 0; i < n; ++i)
+            if (agg[i] != kSNone && Bc[agg[i]] > 0) q[i] = (float)(B[i] / Bc[agg[i]]);
+        // coarse pattern: sorted distinct aggregates of each aggregate's nodes' columns
+        std::vector<uint32_t> crp(na + 1, 0), ccol;
+        {
+            std::vector<uint32_t> mark(na, kSNone), row;
+            for (uint64_t a = 0; a < na; ++a) {
+                row.clear();
+                for (uint32_t u = aptr[a]; u < aptr[a + 1]; ++u) {
+                    const uint32_t i = anode[u];
+                    for (uint32_t e = rp[i]; e < rp[i + 1]; ++e) {
+                        const uint32_t J = agg[col[e]];
+                        if (J != kSNone && mark[J] != a) {
+                            mark[J] = (uint32_t)a;
+                            row.push_back(J);
+                        }
+                    }
+                }
+                std::sort(row.begin(), row.end());
+                LMTG_CHECK(row.size() <= (size_t)kSGalCap, LMTG_ERR_UNSUPPORTED, "diffusion multigrid: coarse row too wide");
+                ccol.insert(ccol.end(), row.begin(), row.end());
+                crp[a + 1] = (uint32_t)ccol.size();
+            }
+        }
+        L->nagg = na;
+        s_upload(L->agg, agg, s);
+        s_upload(L->aptr, aptr, s);
+        s_upload(L->anode, anode, s);
+        s_upload(L->q, q, s);
+        L->gslot.alloc(L->nnz);
+        M->lv.push_back(std::move(L));
+        rp.swap(crp);
+        col.swap(ccol);
+        B.swap(Bc);
+        n = na;
+    }
+    const size_t nl = M->lv.size();
+    M->nc = (nl > 1 && M->lv.back()->n <= 2000) ? (int)M->lv.back()->n : 0;
+    if (!M->nc) {  // no hierarchy (or a coarsest level too large for the dense solve): Jacobi
+        c->samg = M.release();
+        return;
+    }
+    // slots of the fine entries (every level's coarse pattern is uploaded by now)
+    for (size_t l = 0; l + 1 < nl; ++l) {
+        SLevel &F = *M->lv[l], &C = *M->lv[l + 1];
+        k_s_slots<<<grid_for(c, F.n, 128, 8), 128, 0, s>>>(l ? F.rp.p : c->bptr.p, l ? F.col.p : c->bcol.p, F.agg.p,
+                                                            F.n, C.rp.p, C.col.p, F.gslot.p);
+        LMTG_CUDA(cudaGetLastError());
+        c->launches += 1;
+    }
+    // grids of the level-0 bulk-copy passes
+    {
+        constexpr size_t smem = sbulk_smem_bytes<kSStages, kSCap>();
+        int nb = 0;
+        LMTG_CUDA(cudaFuncSetAttribute(k_pcg_spmv_s_bulk<kSStages, kSCap, EpiSRes>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        LMTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_pcg_spmv_s_bulk<kSStages, kSCap, EpiSRes>,
+                                                                kSBulkThreads, smem));
+        M->gres = c->sm_count * (nb > 0 ? nb : 1);
+        LMTG_CUDA(cudaFuncSetAttribute(k_pcg_spmv_s_bulk<kSStages, kSCap, EpiSPost>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        LMTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_pcg_spmv_s_bulk<kSStages, kSCap, EpiSPost>,
+                                                                kSBulkThreads, smem));
+        M->gpost = c->sm_count * (nb > 0 ? nb : 1);
+    }
+    // numeric part: Galerkin products, Jacobi inverses
+    for (size_t l = 0; l + 1 < nl; ++l) {
+        SLevel &F = *M->lv[l], &C = *M->lv[l + 1];
+        k_s_galerkin<<<grid_for(c, F.nagg, kSGalThreads, 8), kSGalThreads, 0, s>>>(
+            l ? F.rp.p : c->bptr.p, l ? F.col.p : c->bcol.p, l ? F.A.p : c->K32.p, F.gslot.p, F.q.p, F.aptr.p,
+            F.anode.p, F.nagg, C.rp.p, C.col.p, C.A.p);
+        k_s_dinv<<<grid_for(c, C.n, 128, 8), 128, 0, s>>>(C.rp.p, C.col.p, C.A.p, C.n, C.Dinv.p);
+        LMTG_CUDA(cudaGetLastError());
+        c->launches += 2;
+    }
+    // smoother weights: twelve power steps per level, queued back to back, read once
+    M->power.alloc(2 * kSPowerSteps * kSMaxLevels);
+    PcgScalars *o = c->scal.p + 1;
+    for (size_t l = 0; l + 1 < nl; ++l) {
+        SLevel &L = *M->lv[l];
+        const uint32_t *lrp = l ? L.rp.p : c->bptr.p, *lcol = l ? L.col.p : c->bcol.p;
+        const float *lA = l ? L.A.p : c->K32.p, *lD = l ? L.Dinv.p : c->Dinv32.p;
+        k_s_rand<<<grid_for(c, L.n, 256), 256, 0, s>>>(L.xa.p, L.n);
+        const int g = grid_for(c, (L.n + 31) / 32 * 32, kRowThreads, 8);
+        for (int it = 0; it < kSPowerSteps; ++it) {
+            float *v = (it & 1) ? L.xb.p : L.xa.p, *w = (it & 1) ? L.xa.p : L.xb.p;
+            double *out = M->power.p + (kSPowerSteps * l + it);
+            k_s_power<<<g, kRowThreads, 0, s>>>(lrp, lcol, lA, lD, v, w, L.n, it ? out - 1 : nullptr, c->partials.p,
+                                                &o->cnt_c, out);
+        }
+        LMTG_CUDA(cudaGetLastError());
+        c->launches += 1 + kSPowerSteps;
+    }
+    std::vector<double> h(kSPowerSteps * kSMaxLevels);
+    LMTG_CUDA(cudaMemcpyAsync(h.data(), M->power.p, 8 * h.size(), cudaMemcpyDeviceToHost, s));
+    // coarsest: dense inverse (FP64 Gauss-Jordan on the host)
+    SLevel &Cz = *M->lv.back();
+    std::vector<uint32_t> zrp(Cz.n + 1), zcol(Cz.nnz);
+    std::vector<float> zA(Cz.nnz);
+    LMTG_CUDA(cudaMemcpyAsync(zrp.data(), Cz.rp.p, 4 * zrp.size(), cudaMemcpyDeviceToHost, s));
+    LMTG_CUDA(cudaMemcpyAsync(zcol.data(), Cz.col.p, 4 * zcol.size(), cudaMemcpyDeviceToHost, s));
+    LMTG_CUDA(cudaMemcpyAsync(zA.data(), Cz.A.p, 4 * zA.size(), cudaMemcpyDeviceToHost, s));
+    LMTG_CUDA(cudaStreamSynchronize(s));
+    for (size_t l = 0; l + 1 < nl; ++l) {
+        SLevel &L = *M->lv[l];
+        const double lam = std::sqrt(std::max(0.0, h[kSPowerSteps * l + kSPowerSteps - 1]));
+        const double hi = 1.2 * lam, lo = hi / 30.0;
+        L.lambda = lam;
+        L.omega = lam > 0 ? (float)(2.0 / (hi + lo)) : 1.f;
+    }
+    const int nc = M->nc;
+    std::vector<double> W((size_t)nc * 2 * nc, 0.0);
+    const size_t w2 = 2 * (size_t)nc;
+    for (int i = 0; i < nc; ++i) {
+        for (uint32_t e = zrp[i]; e < zrp[i + 1]; ++e) W[i * w2 + zcol[e]] = zA[e];
+        W[i * w2 + nc + i] = 1.0;
+    }
+    double dmax = 0;
+    for (int i = 0; i < nc; ++i) dmax = std::max(dmax, std::fabs(W[i * w2 + i]));
+    std::vector<char> dead(nc, 0);
+    for (int cc = 0; cc < nc; ++cc) {
+        int p = cc;
+        for (int r = cc + 1; r < nc; ++r)
+            if (std::fabs(W[r * w2 + cc]) > std::fabs(W[p * w2 + cc])) p = r;
+        if (std::fabs(W[p * w2 + cc]) <= 1e-13 * dmax) {
+            dead[cc] = 1;
+            continue;
+        }
+        if (p != cc)
+            for (size_t k = 0; k < w2; ++k) std::swap(W[cc * w2 + k], W[p * w2 + k]);
+        const double iv = 1.0 / W[cc * w2 + cc];
+        for (size_t k = 0; k < w2; ++k) W[cc * w2 + k] *= iv;
+        for (int r = 0; r < nc; ++r) {
+            if (r == cc) continue;
+            const double f = W[r * w2 + cc];
+            if (f == 0.0) continue;
+            for (size_t k = cc; k < w2; ++k) W[r * w2 + k] -= f * W[cc * w2 + k];
+        }
+    }
+    std::vector<float> Ci((size_t)nc * nc);
+    for (int r = 0; r < nc; ++r)
+        for (int k = 0; k < nc; ++k) Ci[(size_t)r * nc + k] = (dead[r] || dead[k]) ? 0.f : (float)W[r * w2 + nc + k];
+    M->Cinv.alloc(Ci.size());
+    LMTG_CUDA(cudaMemcpyAsync(M->Cinv.p, Ci.data(), 4 * Ci.size(), cudaMemcpyHostToDevice, s));
+    LMTG_CUDA(cudaStreamSynchronize(s));
+    c->samg = M.release();
+}
+
+// the multigrid for this context's FP32 diffusion solves, built on first use; false: Jacobi
+static bool samg_prepare(lmtg_ctx *c) {
+    if (c->precond != LMTG_PREC_AMG || c->nn < kSMinUnknowns) return false;
+    if (!c->samg) samg_build(c);
+    return c->samg && c->samg->nc > 0;
+}
+
+static void s_cycle(lmtg_ctx *c, SAmg &M, size_t l, const float *rhs, float *out, cudaStream_t s, PcgScalars *S);
+
+// level l's coarse correction: level l+1's cycle on N.r (its first smoothing step in N.xa) --
+// once on the dense coarsest (e = N.res) and below the top kSWLevels levels (e = N.xb), else
+// twice, the second visit on the residual the first leaves (e = N.xb, e2 = N.xb2)
+static void s_correction(lmtg_ctx *c, SAmg &M, size_t l, cudaStream_t s, PcgScalars *S, float *&e, float *&e2) {
+    const size_t nl = M.lv.size();
+    SLevel &N = *M.lv[l + 1];
+    e2 = nullptr;
+    if (l + 2 == nl) {
+        e = N.res.p;
+        s_cycle(c, M, l + 1, N.r.p, e, s, S);
+        return;
+    }
+    e = N.xb.p;
+    s_cycle(c, M, l + 1, N.r.p, e, s, S);
+    if (l >= kSWLevels) return;
+    e2 = N.xb2.p;
+    launch_pdl(k_s_res, grid_for(c, (N.n + 31) / 32 * 32, kRowThreads, 8), kRowThreads, 0, s, N.rp.p, N.col.p,
+               N.A.p, e, N.r.p, N.r2.p, N.n, S, N.Dinv.p, N.omega, N.xa.p);
+    c->launches += 1;
+    s_cycle(c, M, l + 1, N.r2.p, e2, s, S);
+}
+
+// the restriction to level l+1 (with its first smoothing step unless it is the dense coarsest)
+// and the prolongation back, shared by the level-0 and deeper cycles
+static void s_restrict(lmtg_ctx *c, SAmg &M, size_t l, cudaStream_t s, PcgScalars *S) {
+    SLevel &L = *M.lv[l], &N = *M.lv[l + 1];
+    const bool ncoarsest = l + 2 == M.lv.size();
+    launch_pdl(k_s_restrict, grid_for(c, L.nagg, 256, 8), 256, 0, s, L.aptr.p, L.anode.p, L.q.p, L.res.p, N.r.p,
+               L.nagg, ncoarsest ? nullptr : N.Dinv.p, N.omega, N.xa.p, S);
+}
+static void s_prolong(lmtg_ctx *c, SLevel &L, const float *e, const float *e2, cudaStream_t s, PcgScalars *S) {
+    launch_pdl(k_s_prolong, grid_for(c, L.n / 4 + 1, 256, 8), 256, 0, s, L.agg.p, L.q.p, e, e2, L.xa.p, L.n, S);
+}
+
+// cycle of level l >= 1 on rhs (first smoothing step already in L.xa) into out
+static void s_cycle(lmtg_ctx *c, SAmg &M, size_t l, const float *rhs, float *out, cudaStream_t s, PcgScalars *S) {
+    SLevel &L = *M.lv[l];
+    if (l + 1 == M.lv.size()) {
+        launch_pdl(k_s_dense, grid_for(c, (uint64_t)M.nc * 32, 256, 4), 256, 0, s, M.Cinv.p, rhs, out, M.nc, S);
+        c->launches += 1;
+        return;
+    }
+    const int g = grid_for(c, (L.n + 31) / 32 * 32, kRowThreads, 8);
+    launch_pdl(k_s_res, g, kRowThreads, 0, s, L.rp.p, L.col.p, L.A.p, L.xa.p, rhs, L.res.p, L.n, S, nullptr, 0.f,
+               nullptr);
+    s_restrict(c, M, l, s, S);
+    float *e, *e2;
+    s_correction(c, M, l, s, S, e, e2);
+    s_prolong(c, L, e, e2, s, S);
+    launch_pdl(k_s_post, g, kRowThreads, 0, s, L.rp.p, L.col.p, L.A.p, L.Dinv.p, L.xa.p, rhs, out, L.omega, L.n, S,
+               false, 0, 0.0, c->partials.p);
+    c->launches += 4;
+}
+
+// the cycle after the update kernel (level 0): r -> z, rz and beta; the residual and the
+// post-smoothing stream K32 by bulk copies when the PCG's SpMV does (sbulk)
+static void s_cycle0(lmtg_ctx *c, const float *r, float *z, cudaStream_t s, int start, double beta_den, bool sbulk) {
+    SAmg &M = *c->samg;
+    PcgScalars *S = c->scal.p;
+    SLevel &L = *M.lv[0];
+    const int g = grid_for(c, (L.n + 31) / 32 * 32, kRowThreads, 8);
+    constexpr size_t smem = sbulk_smem_bytes<kSStages, kSCap>();
+    if (sbulk)
+        k_pcg_spmv_s_bulk<kSStages, kSCap, EpiSRes><<<M.gres, kSBulkThreads, smem, s>>>(
+            c->bptr.p, c->bcol.p, c->K32.p, EpiSRes{L.xa.p, r, L.res.p}, L.n, S, c->partials.p);
+    else
+        launch_pdl(k_s_res, g, kRowThreads, 0, s, c->bptr.p, c->bcol.p, c->K32.p, L.xa.p, r, L.res.p, L.n, S,
+                   nullptr, 0.f, nullptr);
+    s_restrict(c, M, 0, s, S);
+    float *e, *e2;
+    s_correction(c, M, 0, s, S, e, e2);
+    s_prolong(c, L, e, e2, s, S);
+    if (sbulk)
+        k_pcg_spmv_s_bulk<kSStages, kSCap, EpiSPost><<<M.gpost, kSBulkThreads, smem, s>>>(
+            c->bptr.p, c->bcol.p, c->K32.p, EpiSPost{L.xa.p, r, c->Dinv32.p, z, L.omega, start, beta_den}, L.n, S,
+            c->partials.p);
+    else
+        launch_pdl(k_s_post, g, kRowThreads, 0, s, c->bptr.p, c->bcol.p, c->K32.p, c->Dinv32.p, L.xa.p, r, z,
+                   L.omega, L.n, S, true, start, beta_den, c->partials.p);
+    c->launches += 4;
+    LMTG_CUDA(cudaGetLastError());
+}
+
+// PCG on K x = b in precision T, from the current x (x_zero: x is 0, r = b), preconditioned by
+// Jacobi, or for FP32 with amg by the context's multigrid (K = K32).  b_norm2 >= 0 gives |b|^2 for
+// the relative test; beta_den > 0 continues the search direction held in p (reliable update).
+// Returns the status; *iters the iterations.
 template <class T>
 static int diff_pcg_t(lmtg_ctx *c, const T *K, const T *Dinv, const T *b, T *x, T *r, T *z, T *p, T *q,
-                      bool x_zero, double tol, int maxit, double b_norm2, double beta_den, int *iters) {
+                      bool x_zero, double tol, int maxit, double b_norm2, double beta_den, int *iters,
+                      bool amg = false) {
     cudaStream_t s = c->stream;
+    // FP32: the bulk-copy SpMV unless spmv_kind 0 or a 32-row chunk could exceed a stage
+    const bool sbulk = std::is_same<T, float>::value && c->spmv_kind != 0 &&
+                       32ull * c->max_row_blocks <= (uint64_t)kSCap;
     PcgScalars init{};
     init.crit = tol;
     init.crit_kind = LMTG_CRIT_REL_RESIDUAL;
@@ -668,11 +1425,23 @@ static int diff_pcg_t(lmtg_ctx *c, const T *K, const T *Dinv, const T *b, T *x, 
                                                                           &o->rr);
         c->launches += 1;
     }
-    k_pcg_start_s<T><<<ngrid(c), kRowThreads, 0, s>>>(r, b_norm2 >= 0 ? nullptr : b, Dinv, z, c->nn,
-                                                      c->scal.p, c->partials.p);
-    c->launches += 1;
+    if constexpr (std::is_same<T, float>::value) {
+        if (amg) {
+            SLevel &L0 = *c->samg->lv[0];
+            k_pcg_start_s_amg<<<ngrid(c), kRowThreads, 0, s>>>(r, b_norm2 >= 0 ? nullptr : b, c->Dinv32.p,
+                                                               L0.xa.p, L0.omega, c->nn, c->scal.p,
+                                                               c->partials.p);
+            c->launches += 1;
+            s_cycle0(c, r, z, s, 1, beta_den, sbulk);  // z, rz and beta = rz / beta_den (0 on a fresh start)
+        }
+    }
+    if (!amg) {
+        k_pcg_start_s<T><<<ngrid(c), kRowThreads, 0, s>>>(r, b_norm2 >= 0 ? nullptr : b, Dinv, z, c->nn,
+                                                          c->scal.p, c->partials.p);
+        c->launches += 1;
+    }
     LMTG_CUDA(cudaGetLastError());
-    if (beta_den > 0.0) {
+    if (beta_den > 0.0 && !amg) {
         // continue the previous direction: beta = rz_new / beta_den (set after the start kernel)
         PcgScalars h{};
         LMTG_CUDA(cudaMemcpyAsync(&h, c->scal.p, sizeof(h), cudaMemcpyDeviceToHost, s));
@@ -681,27 +1450,26 @@ static int diff_pcg_t(lmtg_ctx *c, const T *K, const T *Dinv, const T *b, T *x, 
         LMTG_CUDA(cudaMemcpyAsync(&c->scal.p->beta, &beta, sizeof(double), cudaMemcpyHostToDevice, s));
         LMTG_CUDA(cudaStreamSynchronize(s));
     }
-    constexpr int kIters = 16;  // iterations per graph launch
+    // iterations per graph launch (a multigrid iteration is ~40 launches: fewer run on after the
+    // convergence test stops the chunk)
+    const int kIters = amg ? 4 : 16;
     const int gr = rgrid(c, k_pcg_spmv_s<T>);
-    // FP32: the bulk-copy SpMV unless spmv_kind 0 or a 32-row chunk could exceed a stage
-    constexpr int kSStages = 2, kSCap = 3072;
-    const bool sbulk = std::is_same<T, float>::value && c->spmv_kind != 0 &&
-                       32ull * c->max_row_blocks <= (uint64_t)kSCap;
     int gr_bulk = 0;
     if (sbulk) {
         constexpr size_t smem = sbulk_smem_bytes<kSStages, kSCap>();
-        LMTG_CUDA(cudaFuncSetAttribute(k_pcg_spmv_s_bulk<kSStages, kSCap>,
+        LMTG_CUDA(cudaFuncSetAttribute(k_pcg_spmv_s_bulk<kSStages, kSCap, EpiSPq>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         int nb = 0;
-        LMTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_pcg_spmv_s_bulk<kSStages, kSCap>,
+        LMTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_pcg_spmv_s_bulk<kSStages, kSCap, EpiSPq>,
                                                                 kSBulkThreads, smem));
         gr_bulk = c->sm_count * (nb > 0 ? nb : 1);
     }
     // the chunk graph of this precision, reused while it was captured on the same buffers
     DiffGraph &dg = c->diff_graph[std::is_same<T, float>::value ? 1 : 0];
-    const void *key[9] = {K, Dinv, b, x, r, z, p, q, reinterpret_cast<const void *>((uintptr_t)sbulk)};
+    const void *key[10] = {K, Dinv, b, x, r, z, p, q, reinterpret_cast<const void *>((uintptr_t)sbulk),
+                           reinterpret_cast<const void *>((uintptr_t)amg)};
     bool cached = dg.exec != nullptr;
-    for (int i = 0; i < 9 && cached; ++i) cached = dg.key[i] == key[i];
+    for (int i = 0; i < 10 && cached; ++i) cached = dg.key[i] == key[i];
     if (!cached) {
         if (dg.exec) cudaGraphExecDestroy(dg.exec);
         if (dg.graph) cudaGraphDestroy(dg.graph);
@@ -711,14 +1479,15 @@ static int diff_pcg_t(lmtg_ctx *c, const T *K, const T *Dinv, const T *b, T *x, 
     cudaGraph_t graph = dg.graph;
     cudaGraphExec_t exec = dg.exec;
     if (!cached) {
+        const uint64_t launches0 = c->launches;
         LMTG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
         for (int k = 0; k < kIters; ++k) {
             k_pcg_dir_s<T><<<ngrid(c), kRowThreads, 0, s>>>(z, p, c->nn, c->scal.p);
             if constexpr (std::is_same<T, float>::value) {
                 if (sbulk)
-                    k_pcg_spmv_s_bulk<kSStages, kSCap>
+                    k_pcg_spmv_s_bulk<kSStages, kSCap, EpiSPq>
                         <<<gr_bulk, kSBulkThreads, sbulk_smem_bytes<kSStages, kSCap>(), s>>>(
-                            c->bptr.p, c->bcol.p, K, p, q, c->nn, c->scal.p, c->partials.p);
+                            c->bptr.p, c->bcol.p, K, EpiSPq{p, q}, c->nn, c->scal.p, c->partials.p);
                 else
                     k_pcg_spmv_s<T><<<gr, kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, K, p, q, c->nn, c->scal.p,
                                                                c->partials.p);
@@ -726,8 +1495,19 @@ static int diff_pcg_t(lmtg_ctx *c, const T *K, const T *Dinv, const T *b, T *x, 
                 k_pcg_spmv_s<T><<<gr, kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, K, p, q, c->nn, c->scal.p,
                                                            c->partials.p);
             }
-            k_pcg_update_s<T><<<ngrid(c), kRowThreads, 0, s>>>(x, r, z, p, q, Dinv, c->nn, c->scal.p,
-                                                               c->partials.p);
+            if constexpr (std::is_same<T, float>::value) {
+                if (amg) {
+                    SLevel &L0 = *c->samg->lv[0];
+                    k_pcg_update_s_amg<<<ngrid(c), kRowThreads, 0, s>>>(x, r, p, q, c->Dinv32.p, L0.xa.p,
+                                                                        L0.omega, c->nn, c->scal.p,
+                                                                        c->partials.p);
+                    s_cycle0(c, r, z, s, 0, 0.0, sbulk);
+                }
+            }
+            if (!amg)
+                k_pcg_update_s<T><<<ngrid(c), kRowThreads, 0, s>>>(x, r, z, p, q, Dinv, c->nn, c->scal.p,
+                                                                   c->partials.p);
+            c->launches += 3;
         }
         cudaError_t ce = cudaStreamEndCapture(s, &graph);
         if (ce != cudaSuccess) throw Error{LMTG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce)};
@@ -738,7 +1518,9 @@ static int diff_pcg_t(lmtg_ctx *c, const T *K, const T *Dinv, const T *b, T *x, 
         }
         dg.graph = graph;
         dg.exec = exec;
-        for (int i = 0; i < 9; ++i) dg.key[i] = key[i];
+        for (int i = 0; i < 10; ++i) dg.key[i] = key[i];
+        dg.launches = c->launches - launches0;  // counted while capturing, run on each replay
+        c->launches = launches0;
     }
     cudaError_t ce = cudaSuccess;
     LMTG_CUDA(cudaMemcpyAsync(c->h_scal, c->scal.p, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
@@ -747,7 +1529,7 @@ static int diff_pcg_t(lmtg_ctx *c, const T *K, const T *Dinv, const T *b, T *x, 
     const int max_chunks = maxit / kIters + 2;
     for (int ch = 0; ch < max_chunks && !finished; ++ch) {
         ce = cudaGraphLaunch(exec, s);
-        c->launches += 3 * kIters;
+        c->launches += dg.launches;
         if (ce == cudaSuccess)
             ce = cudaMemcpyAsync(c->h_scal, c->scal.p, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s);
         if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
@@ -775,7 +1557,7 @@ static int diff_pcg64(lmtg_ctx *c, const double *b, double *x, double tol, int m
 }
 
 // FP32-inner / FP64-refined solve of A x = b with reliable updates (the elasticity solver's
-// scheme on the scalar matrices): FP32 Jacobi-PCG segments on A32 d = r / s, each ending after a
+// scheme on the scalar matrices): FP32 PCG segments (multigrid or Jacobi) on A32 d = r / s, each ending after a
 // reduction of its recursive residual by inner_reduction; x += s d and r = b - A x in FP64; the search
 // direction is kept across the residual replacement.
 static int diff_mixed(lmtg_ctx *c, const double *b, double *x, double tol, int maxit, int *iters) {
@@ -793,6 +1575,7 @@ static int diff_mixed(lmtg_ctx *c, const double *b, double *x, double tol, int m
     k_dot_s<<<ngrid(c), kRowThreads, 0, st>>>(b, b, c->nn, c->partials.p, &o->cnt_c, &o->rr);
     c->launches += 1;
     const double bb = read_rr();
+    const bool amg = samg_prepare(c);
     const double kDelta = c->inner_reduction;
     int total = 0, status = LMTG_OK, outer = 0;
     double s_prev = 0, rz_prev = 0, rel_prev = 0;
@@ -816,11 +1599,14 @@ static int diff_mixed(lmtg_ctx *c, const double *b, double *x, double tol, int m
         if (eta < kDelta) eta = kDelta;
         int it = 0;
         const int s2 = diff_pcg_t<float>(c, c->K32.p, c->Dinv32.p, b32, d32, r32, z32, p32, q32, true,
-                                         eta, maxit - total, 1.0, beta_den, &it);
+                                         eta, maxit - total, 1.0, beta_den, &it, amg);
         total += it;
         ++outer;
         if (s2 == LMTG_ERR_NAN) { status = s2; break; }
-        rz_prev = c->h_scal[0].beta != 0.0 ? c->h_scal[0].rz / c->h_scal[0].beta : 0.0;
+        // r.z of the last direction: the multigrid's cycle is skipped once the update kernel
+        // stops the run, so rz is still that one; the Jacobi update forms the next rz and beta
+        if (amg) rz_prev = c->h_scal[0].rz;
+        else rz_prev = c->h_scal[0].beta != 0.0 ? c->h_scal[0].rz / c->h_scal[0].beta : 0.0;
         s_prev = sc;
         rel_prev = rel;
         have_dir = it > 0 && rz_prev > 0.0;
@@ -870,6 +1656,7 @@ void diff_setup(lmtg_ctx *c, const double *k, uint64_t nk, double rho_c, double 
     LMTG_CHECK(nk == 1 || nk == c->ne, LMTG_ERR_ARG, "conductivity needs 1 or ne values");
     LMTG_CHECK(rho_c > 0 && dt > 0 && theta >= 0 && theta <= 1, LMTG_ERR_ARG, "rho_c, dt > 0, theta in [0,1]");
     c->h_diff_conv.clear();  // the matrices are rebuilt: convection has to be set again
+    samg_free(c);            // and the multigrid with them, at the next FP32 solve
     cudaStream_t s = c->stream;
     if (!c->allocated) {
         build_pattern(c);
@@ -902,6 +1689,7 @@ void diff_setup(lmtg_ctx *c, const double *k, uint64_t nk, double rho_c, double 
                                                               c->K32.p);
     LMTG_CUDA(cudaGetLastError());
     c->launches += 2;
+    c->h_cdof.assign(bnd, bnd + nbnd);  // penalty nodes stay out of the multigrid's aggregates
     if (nbnd) {
         upload_u32(c, c->cdof, bnd, nbnd);
         DBuf<unsigned long long> md;
@@ -1074,6 +1862,7 @@ void diff_set_convection(lmtg_ctx *c, uint64_t nedges, const uint32_t *edges, co
         LMTG_CUDA(cudaGetLastError());
         c->launches += 3;
         LMTG_CUDA(cudaStreamSynchronize(s));
+        samg_free(c);  // A changed: the multigrid is rebuilt at the next FP32 solve
     }
     c->h_diff_conv = load;
     diff_update_load(c);
@@ -1258,6 +2047,7 @@ int lmtg_diff_mesh_set(lmtg_ctx *c, uint64_t nn, const double *pos, uint64_t ne,
         for (uint64_t q = 0; q < 6 * ne; ++q) LMTG_CHECK(conn[q] < nn, LMTG_ERR_ARG, "node id >= nn");
         recal_free(c);
         amg_free(c);
+        samg_free(c);
         diff_graphs_free(c);
         c->elem_type = LMTG_ELEM_TRIANGLE6;
         c->npe = 6;

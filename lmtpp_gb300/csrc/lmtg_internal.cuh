@@ -106,6 +106,7 @@ namespace lmtg {
 struct BatchState;  // batch.cu
 struct RecalState;  // recalage.cu
 struct AmgState;    // amg.cu
+struct SAmg;        // diffusion.cu
 }
 
 namespace lmtg {
@@ -114,7 +115,8 @@ namespace lmtg {
 struct DiffGraph {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    const void *key[9] = {};
+    const void *key[10] = {};
+    uint64_t launches = 0;  // kernels per replay
 };
 }  // namespace lmtg
 
@@ -175,6 +177,7 @@ struct lmtg_ctx {
     // replacement (lmtg_set_inner_reduction)
     double inner_reduction = 0.01;
     lmtg::DiffGraph diff_graph[2];  // the diffusion PCG's chunk graphs, [0] FP64, [1] FP32
+    lmtg::SAmg *samg = nullptr;     // the diffusion FP32 PCG's multigrid (built on first use)
     lmtg::DBuf<float> Ke32, K32, Dinv32;
     bool have64 = false, have32 = false, have_vec = false;
     double max_diag = 0;
@@ -261,6 +264,8 @@ void amg_free(lmtg_ctx *c);
 void batch_free(lmtg_ctx *c);
 // destroys the diffusion PCG's cached chunk graphs (diffusion.cu)
 void diff_graphs_free(lmtg_ctx *c);
+// destroys the diffusion multigrid and the chunk graphs captured on it (diffusion.cu)
+void samg_free(lmtg_ctx *c);
 void batch_set_rhs(lmtg_ctx *c, int nrhs, const double *B_host);
 int batch_solve(lmtg_ctx *c, int mode, double tol, int maxit, double timeout_s, lmtg_solve_stats *st,
                 int *pair_iters);

@@ -89,6 +89,12 @@ class Diffusion:
         m = {"fp64": abi.SOLVE_PCG_F64, "mixed": abi.SOLVE_MIXED_IR}[mode]
         abi.check(self._lib.lmtg_diff_set_solver(self._ctx, m), self._ctx, "set_solver")
 
+    def set_preconditioner(self, kind):
+        """Preconditioner of the mixed step solver's FP32 PCG: 'amg' (default: a W-cycle of the
+        scalar aggregation multigrid, from 3000 unknowns) or 'jacobi'."""
+        k = {"jacobi": abi.PREC_BLOCK_JACOBI, "amg": abi.PREC_AMG}[kind]
+        abi.check(self._lib.lmtg_set_preconditioner(self._ctx, k), self._ctx, "set_preconditioner")
+
     def set_inner_reduction(self, inner_reduction):
         """Recursive-residual reduction of each FP32 segment of the mixed step solver (default 0.01)."""
         abi.check(self._lib.lmtg_set_inner_reduction(self._ctx, float(inner_reduction)), self._ctx,
