@@ -384,7 +384,13 @@ int lmtg_recalage_assemble(lmtg_ctx *ctx);
  * is built at the first mixed solve after lmtg_allocate_matrices or lmtg_set_constraints (nodes
  * with a constraint stay out of the coarse spaces), its numeric part at the first mixed solve
  * after each matrix assembly.  LMTG_PREC_BLOCK_JACOBI: the inverse 3x3 diagonal blocks.  The
- * FP64 PCG always uses block Jacobi. */
+ * FP64 PCG always uses block Jacobi.
+ * The diffusion step solver (lmtg_diff_set_solver LMTG_SOLVE_MIXED_IR) follows the same setting:
+ * with LMTG_PREC_AMG and at least 3,000 nodes its FP32 PCG runs one cycle of a scalar
+ * aggregation multigrid (piecewise-constant coarse spaces without the Dirichlet nodes, damped
+ * Jacobi smoothing, the top level's coarse correction visiting level 1 twice, a dense coarsest
+ * level), built at the first FP32 solve after lmtg_diff_setup or lmtg_diff_set_convection;
+ * Jacobi otherwise. */
 int lmtg_set_preconditioner(lmtg_ctx *ctx, int kind);
 /* The multigrid hierarchy built for the last mixed solve (levels = 0 when none): per level
  * (up to 8) unknowns, stored blocks, damped-Jacobi weight and lambda_max(D^-1 K); the host time
