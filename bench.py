@@ -63,6 +63,10 @@ def parse():
     p.add_argument("--fd", type=int, default=32, help="elements checked by central differences (adjoint mode)")
     p.add_argument("--steps-t", type=int, default=100, help="time steps (transient mode)")
     p.add_argument("--ckpt", type=int, default=10, help="checkpoint interval (transient mode)")
+    p.add_argument("--t-solvers", default="fp64,mixed",
+                   help="step solvers timed in transient mode (comma list of fp64, mixed)")
+    p.add_argument("--t-precond", default="amg", choices=["amg", "jacobi"],
+                   help="preconditioner of the mixed step solver's FP32 PCG (transient mode)")
     p.add_argument("--nsys", type=int, default=256, help="meshes in the batch (batch mode)")
     p.add_argument("--mode", default="bench", choices=["bench", "profile", "solve", "adjoint", "transient", "batch"],
                    help="profile: time the PCG and multigrid kernels once on --side, outside graphs (small ncu case); "
@@ -526,7 +530,7 @@ def adjoint_extra(args):
 
 
 def run_transient(args):
-    print(json.dumps(transient_extra(args)), flush=True)
+    print(json.dumps(transient_extra(args, solvers=tuple(args.t_solvers.split(",")))), flush=True)
 
 
 def transient_extra(args, solvers=("fp64", "mixed"), ckpts=None):
@@ -557,6 +561,9 @@ def transient_extra(args, solvers=("fp64", "mixed"), ckpts=None):
                                                                           SEED, args.steps_t),
            "setup_s": setup_s}
     finals = {}
+    precond = getattr(args, "t_precond", "amg")
+    d.set_preconditioner(precond)
+    out["mixed_preconditioner"] = precond
     for solver in solvers:
         d.set_solver(solver)
         d.set_state(T0)
@@ -573,6 +580,7 @@ def transient_extra(args, solvers=("fp64", "mixed"), ckpts=None):
                                                            np.linalg.norm(finals["fp64"]))
     # the adjoint call runs its own forward sweep; backward = call - that forward
     grads = {}
+    d.set_solver("mixed")
     for ck in (ckpts or sorted({1, args.ckpt})):
         J, g = d.adjoint_misfit(T0, target, args.steps_t, checkpoint_every=ck, tol=1e-10)
         st_a = d.last_stats
@@ -580,8 +588,9 @@ def transient_extra(args, solvers=("fp64", "mixed"), ckpts=None):
         key = "adjoint_ck%d_" % ck
         out[key + "ms"] = st_a["device_ms"]
         out[key + "pcg_iters"] = st_a["iterations"]
-        out[key + "backward_ratio_vs_forward"] = (st_a["device_ms"] - out["forward_ms_mixed"]) / \
-            out["forward_ms_mixed"]
+        if "forward_ms_mixed" in out:
+            out[key + "backward_ratio_vs_forward"] = (st_a["device_ms"] - out["forward_ms_mixed"]) / \
+                out["forward_ms_mixed"]
         out["J"] = J
         out["grad_norm"] = float(np.linalg.norm(g))
     if len(grads) == 2:
