@@ -23,6 +23,7 @@
 #include <new>
 #include <vector>
 
+#include "ffloat.cuh"
 #include "pdl.cuh"
 #include "spmv_bulk.cuh"
 
@@ -1556,6 +1557,120 @@ static int diff_pcg64(lmtg_ctx *c, const double *b, double *x, double tol, int m
                               c->w64[3].p, false, tol, maxit, -1.0, 0.0, iters);
 }
 
+// Refinement residual in float-float: r = b - A x with A, x, b in FP64, each operand split into
+// two floats on the integer pipe, the products formed exactly (FMA two-product of the splits)
+// and summed per row in a compensated sum (Ogita, Rump and Oishi's Dot2), 48 significant bits;
+// written as rs r in float, |rs r|^2 reduced.  The layout is csr_stream32's: lane l takes the
+// tile's entries t0 + 32k + l, the product pairs go to per-warp shared tiles, and each lane sums
+// its own row in column order.  The FP64 kernel k_residual_s<double> spends 0.53 ms at 2 x
+// 1024^2 on FP64 multiplies and adds (2 lanes per clock per SM); this one runs on the FP32 and
+// integer pipes.
+__global__ void __launch_bounds__(kRowThreads)
+    k_residual_s_ff(const uint32_t *__restrict__ rp, const uint32_t *__restrict__ col, const double *__restrict__ K,
+                    const double *__restrict__ x, const double *__restrict__ b, float rs, float *__restrict__ r32,
+                    uint64_t n, double *partials, unsigned *ticket, double *rr_out) {
+    __shared__ float th[kRowWarps][kTile], tl[kRowWarps][kTile];
+    const int wp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float acc = 0.f;
+    const ChunkRange cr = cta_chunks(n);
+    for (uint64_t ch = cr.first + wp; ch < cr.end; ch += kRowWarps) {
+        const uint64_t r0 = ch * 32, I = r0 + lane;
+        const uint32_t rs0 = __ldg(rp + (I < n ? I : n));
+        uint32_t re0 = __shfl_down_sync(0xffffffffu, rs0, 1);
+        if (lane == 31) re0 = __ldg(rp + (r0 + 32 < n ? r0 + 32 : n));
+        const uint32_t e0 = __shfl_sync(0xffffffffu, rs0, 0);
+        const uint32_t e1 = __shfl_sync(0xffffffffu, re0, 31);
+        float sh = 0.f, sc = 0.f;  // the row's Dot2 sum and its compensation
+        for (uint32_t t0 = e0; t0 < e1; t0 += kTile) {
+            const uint32_t nck = (e1 - t0 + 31) / 32;
+            uint32_t cj[kTileChunks];
+            double kv[kTileChunks];
+#pragma unroll
+            for (int k = 0; k < kTileChunks; ++k) {
+                if (k < nck) {
+                    const uint32_t q = t0 + 32 * k + lane;
+                    const bool on = q < e1;
+                    cj[k] = on ? __ldcs(col + q) : 0u;
+                    kv[k] = on ? __ldcs(K + q) : 0.0;
+                }
+            }
+            double xv[kTileChunks];
+#pragma unroll
+            for (int k = 0; k < kTileChunks; ++k)
+                if (k < nck) xv[k] = t0 + 32 * k + lane < e1 ? __ldg(x + cj[k]) : 0.0;
+#pragma unroll
+            for (int k = 0; k < kTileChunks; ++k) {
+                if (k < nck) {
+                    const ff::f2 a = ff::split(kv[k]), v = ff::split(xv[k]);
+                    const float p = a.h * v.h;
+                    float pl = fmaf(a.h, v.h, -p);
+                    pl = fmaf(a.h, v.l, pl);
+                    pl = fmaf(a.l, v.h, pl);
+                    th[wp][32 * k + lane] = p;
+                    tl[wp][32 * k + lane] = pl;
+                }
+            }
+            __syncwarp();
+            const uint32_t lo = rs0 > t0 ? rs0 : t0;
+            const uint32_t hi = re0 < t0 + kTile ? re0 : t0 + kTile;
+            for (uint32_t q = lo; q < hi; ++q) {
+                float e;
+                ff::two_sum(sh, th[wp][q - t0], sh, e);
+                sc += e + tl[wp][q - t0];
+            }
+            __syncwarp();
+        }
+        if (I < n) {
+            const ff::f2 r = ff::add(ff::split(b[I]), ff::neg(ff::renorm(sh, sc)));
+            const float rf = (r.h + r.l) * rs;
+            r32[I] = rf;
+            acc = fmaf(rf, rf, acc);
+        }
+    }
+    const float t[1] = {acc};
+    double out[1];
+    if (grid_reduce_t<1, 0u>(t, partials, ticket, out) && threadIdx.x == 0) *rr_out = out[0];
+}
+
+__global__ void k_scale_s32(float *__restrict__ v, float f, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        v[i] *= f;
+}
+
+// b32 = r / |r| for r = b - A x (A = K64), returns |r|^2: in float-float (ff) or in FP64 (r64)
+static double diff_refinement_residual(lmtg_ctx *c, const double *x, const double *b, double bb, float *b32,
+                                       double *r64, bool ff) {
+    cudaStream_t st = c->stream;
+    PcgScalars *o = c->scal.p + 1;
+    double rr = 0;
+    if (!ff) {
+        k_residual_s<double><<<rgrid(c, k_residual_s<double>), kRowThreads, 0, st>>>(
+            c->bptr.p, c->bcol.p, c->K64.p, x, b, r64, c->nn, c->partials.p, &o->cnt_c, &o->rr);
+        LMTG_CUDA(cudaMemcpyAsync(&rr, &o->rr, 8, cudaMemcpyDeviceToHost, st));
+        LMTG_CUDA(cudaStreamSynchronize(st));
+        if (rr > 0 && std::isfinite(rr)) {
+            k_scale_to32<<<ngrid(c), kRowThreads, 0, st>>>(r64, 1.0 / std::sqrt(rr), b32, c->nn);
+            c->launches += 1;
+        }
+        c->launches += 1;
+        return rr;
+    }
+    // a power of two near 1 / rms(b) keeps the squares of small residuals in the float range
+    const double rms = std::sqrt(bb / (double)(c->nn ? c->nn : 1));
+    const int e = (rms > 0 && std::isfinite(rms)) ? std::max(-100, std::min(100, std::ilogb(rms))) : 0;
+    k_residual_s_ff<<<rgrid(c, k_residual_s_ff), kRowThreads, 0, st>>>(c->bptr.p, c->bcol.p, c->K64.p, x, b,
+                                                                        std::ldexp(1.0f, -e), b32, c->nn,
+                                                                        c->partials.p, &o->cnt_c, &o->rr);
+    LMTG_CUDA(cudaMemcpyAsync(&rr, &o->rr, 8, cudaMemcpyDeviceToHost, st));
+    LMTG_CUDA(cudaStreamSynchronize(st));
+    c->launches += 1;
+    if (rr > 0 && std::isfinite(rr)) {
+        k_scale_s32<<<ngrid(c), kRowThreads, 0, st>>>(b32, (float)(1.0 / std::sqrt(rr)), c->nn);
+        c->launches += 1;
+    }
+    return rr * std::ldexp(1.0, 2 * e);
+}
+
 // FP32-inner / FP64-refined solve of A x = b with reliable updates (the elasticity solver's
 // scheme on the scalar matrices): FP32 PCG segments (multigrid or Jacobi) on A32 d = r / s, each ending after a
 // reduction of its recursive residual by inner_reduction; x += s d and r = b - A x in FP64; the search
@@ -1580,20 +1695,27 @@ static int diff_mixed(lmtg_ctx *c, const double *b, double *x, double tol, int m
     int total = 0, status = LMTG_OK, outer = 0;
     double s_prev = 0, rz_prev = 0, rel_prev = 0;
     bool have_dir = false;
+    // Float-float residuals while the residual is above kFFMinRel of |b| (their rounding stays
+    // orders below it); below, to decide convergence, or when a float-float residual shows no
+    // progress, the FP64 residual takes over for the rest of the solve (the elasticity solver's
+    // rule)
+    constexpr double kFFMinRel = 1e-9;
+    bool ff = true;
     for (;;) {
-        k_residual_s<double><<<rgrid(c, k_residual_s<double>), kRowThreads, 0, st>>>(c->bptr.p, c->bcol.p, c->K64.p, x, b, r64,
-                                                               c->nn, c->partials.p, &o->cnt_c, &o->rr);
-        c->launches += 1;
-        const double rr = read_rr();
-        const double rel = bb > 0 ? std::sqrt(rr / bb) : std::sqrt(rr);
+        double rr = diff_refinement_residual(c, x, b, bb, b32, r64, ff);  // b32 = r / |r|
+        double rel = bb > 0 ? std::sqrt(rr / bb) : std::sqrt(rr);
+        if (ff && (!std::isfinite(rel) || rel <= tol || rel < kFFMinRel || rr == 0.0 ||
+                   (outer > 0 && rel > 0.5 * rel_prev))) {
+            ff = false;
+            rr = diff_refinement_residual(c, x, b, bb, b32, r64, false);
+            rel = bb > 0 ? std::sqrt(rr / bb) : std::sqrt(rr);
+        }
         if (!std::isfinite(rel)) { status = LMTG_ERR_NAN; break; }
         if (rel <= tol || rr == 0.0) break;
         if (total >= maxit || outer >= 400) { status = LMTG_ERR_NOT_CONVERGED; break; }
         if (have_dir && rel > 0.5 * rel_prev) have_dir = false;
         const double sc = std::sqrt(rr);
-        k_scale_to32<<<ngrid(c), kRowThreads, 0, st>>>(r64, 1.0 / sc, b32, c->nn);
         LMTG_CUDA(cudaMemsetAsync(d32, 0, sizeof(float) * c->nn, st));
-        c->launches += 1;
         const double beta_den = have_dir ? rz_prev * (s_prev / sc) : 0.0;
         double eta = 0.5 * tol / rel;
         if (eta < kDelta) eta = kDelta;
