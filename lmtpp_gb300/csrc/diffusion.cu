@@ -384,32 +384,39 @@ struct EpiSPq {  // q = K p; p.q, alpha = rz / p.q
 };
 constexpr int kSBulkThreads = 32 * (kSBulkCons + 1);
 
-template <int kCap>
+// Columns are either the 32-bit indices or, when every |col - row| < 2^15 (a banded numbering,
+// as the structured meshes have), 16-bit deltas col - row: a quarter fewer bytes per entry
+// (values 4 + columns 2), the same products in the same order.
+__device__ __forceinline__ uint32_t col_at(uint32_t c, uint64_t) { return c; }
+__device__ __forceinline__ uint32_t col_at(int16_t d, uint64_t I) { return (uint32_t)((int64_t)I + d); }
+
+template <int kCap, int kColBytes>
 struct SBulkStage {
-    static_assert(kCap % 4 == 0, "16-byte stage parts");
+    static_assert(kCap % 8 == 0, "16-byte stage parts");
     static constexpr uint32_t kKBytes = 4u * kCap + 32u;
-    static constexpr uint32_t kCBytes = 4u * kCap + 32u;
+    static constexpr uint32_t kCBytes = (uint32_t)kColBytes * kCap + 32u;
     static constexpr uint32_t kRBytes = 4u * (32 * kSBulkCons + 1) + 32u + 12u;  // rounded to 16
     static constexpr uint32_t kBytes = kKBytes + kCBytes + kRBytes;
     static_assert(kRBytes % 16 == 0 && kBytes % 16 == 0, "16-byte stage parts");
 };
-template <int kStages, int kCap>
+template <int kStages, int kCap, int kColBytes = 4>
 constexpr size_t sbulk_smem_bytes() {
-    return (size_t)kStages * SBulkStage<kCap>::kBytes;
+    return (size_t)kStages * SBulkStage<kCap, kColBytes>::kBytes;
 }
 
 // the ring the solvers launch: two stages of up to 3072 entries (a 32-row chunk must fit one)
 constexpr int kSStages = 2, kSCap = 3072;
 
-template <int kStages, int kCap, class Epi>
+template <int kStages, int kCap, class Epi, class CT = uint32_t>
 __global__ void __launch_bounds__(kSBulkThreads, 4)
-    k_pcg_spmv_s_bulk(const uint32_t *__restrict__ rp, const uint32_t *__restrict__ col,
+    k_pcg_spmv_s_bulk(const uint32_t *__restrict__ rp, const CT *__restrict__ col,
                       const float *__restrict__ K, Epi epi, uint64_t n, PcgScalars *S, double *partials) {
-    using St = SBulkStage<kCap>;
+    using St = SBulkStage<kCap, (int)sizeof(CT)>;
+    constexpr uint64_t kCB = sizeof(CT);
     if (*(volatile int *)&S->done) return;
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t full[kStages], empty[kStages];
-    __shared__ uint64_t meta[kStages][4];  // first row, end row, first value index, first rp index
+    __shared__ uint64_t meta[kStages][5];  // first row, end row, first value, rp and column index
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const ChunkRange cr = cta_chunks(n);
     const uint64_t row0 = 32 * cr.first, row_end = min(n, 32 * cr.end);
@@ -460,19 +467,21 @@ __global__ void __launch_bounds__(kSBulkThreads, 4)
             const uint64_t g1 = min(row_end, g0 + (uint64_t)(32 * nch));
             if (lane == 0) {
                 const uint64_t kb0 = (4ull * e0) & ~15ull, kb1 = (4ull * e1 + 15ull) & ~15ull;
+                const uint64_t cb0 = (kCB * e0) & ~15ull, cb1 = (kCB * e1 + 15ull) & ~15ull;
                 const uint64_t rb0 = (4ull * g0) & ~15ull, rb1 = (4ull * (g1 + 1) + 15ull) & ~15ull;
                 meta[slot][0] = g0;
                 meta[slot][1] = g1;
                 meta[slot][2] = kb0 / 4;
                 meta[slot][3] = rb0 / 4;
+                meta[slot][4] = cb0 / kCB;
                 unsigned char *dst = smem + (size_t)slot * St::kBytes;
                 const uint64_t pol = bulk::policy_evict_first();
                 __threadfence_block();
-                bulk::mbar_arrive_expect_tx(&full[slot], (uint32_t)(2 * (kb1 - kb0) + (rb1 - rb0)));
+                bulk::mbar_arrive_expect_tx(&full[slot], (uint32_t)((kb1 - kb0) + (cb1 - cb0) + (rb1 - rb0)));
                 bulk::copy_g2s_hint(dst, reinterpret_cast<const unsigned char *>(K) + kb0, (uint32_t)(kb1 - kb0),
                                     &full[slot], pol);
-                bulk::copy_g2s_hint(dst + St::kKBytes, reinterpret_cast<const unsigned char *>(col) + kb0,
-                                    (uint32_t)(kb1 - kb0), &full[slot], pol);
+                bulk::copy_g2s_hint(dst + St::kKBytes, reinterpret_cast<const unsigned char *>(col) + cb0,
+                                    (uint32_t)(cb1 - cb0), &full[slot], pol);
                 bulk::copy_g2s_hint(dst + St::kKBytes + St::kCBytes, reinterpret_cast<const unsigned char *>(rp) + rb0,
                                     (uint32_t)(rb1 - rb0), &full[slot], pol);
             }
@@ -505,10 +514,10 @@ __global__ void __launch_bounds__(kSBulkThreads, 4)
             const uint64_t g0 = meta[slot][0], g1 = meta[slot][1];
             if (g0 == g1) break;
             float *sK = reinterpret_cast<float *>(smem + (size_t)slot * St::kBytes);
-            const uint32_t *sC = reinterpret_cast<const uint32_t *>(smem + (size_t)slot * St::kBytes + St::kKBytes);
+            const CT *sC = reinterpret_cast<const CT *>(smem + (size_t)slot * St::kBytes + St::kKBytes);
             const uint32_t *sR =
                 reinterpret_cast<const uint32_t *>(smem + (size_t)slot * St::kBytes + St::kKBytes + St::kCBytes);
-            const uint64_t kbase = meta[slot][2], rbase = meta[slot][3];
+            const uint64_t kbase = meta[slot][2], rbase = meta[slot][3], cbase = meta[slot][4];
             const uint64_t R0 = g0 + (uint64_t)(32 * warp);
             if (R0 < g1) {
                 const uint64_t R1 = min(g1, R0 + (uint64_t)32);
@@ -517,7 +526,8 @@ __global__ void __launch_bounds__(kSBulkThreads, 4)
                 if (I < R1) {
                     const uint32_t rs = sR[I - rbase], re = sR[I + 1 - rbase];
 #pragma unroll 4
-                    for (uint32_t qq = rs; qq < re; ++qq) v += __fmul_rn(sK[qq - kbase], epi.x(sC[qq - kbase]));
+                    for (uint32_t qq = rs; qq < re; ++qq)
+                        v += __fmul_rn(sK[qq - kbase], epi.x(col_at(sC[qq - cbase], I)));
                 }
                 __syncwarp();
                 if (lane == 0) bulk::mbar_arrive(&empty[slot]);
@@ -533,6 +543,48 @@ __global__ void __launch_bounds__(kSBulkThreads, 4)
         const float t[1] = {acc};
         double out[1];
         if (grid_reduce_t<1, 0u>(t, partials, epi.ticket(S), out) && threadIdx.x == 0) epi.total(out[0], S);
+    }
+}
+
+// grid of one resident wave of the bulk-copy kernel with epilogue Epi and column type CT (the
+// function's shared-memory ceiling set on first use)
+template <class Epi, class CT>
+static int sbulk_grid(lmtg_ctx *c) {
+    static int grid = 0;
+    if (!grid) {
+        constexpr size_t smem = sbulk_smem_bytes<kSStages, kSCap, (int)sizeof(CT)>();
+        auto fn = k_pcg_spmv_s_bulk<kSStages, kSCap, Epi, CT>;
+        LMTG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int nb = 0;
+        LMTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, kSBulkThreads, smem));
+        grid = c->sm_count * (nb > 0 ? nb : 1);
+    }
+    return grid;
+}
+
+// K x through the bulk-copy kernel on the context's pattern: 16-bit column deltas when they fit
+template <class Epi>
+static void sbulk_launch(lmtg_ctx *c, const float *K, Epi epi, cudaStream_t s) {
+    if (c->col16)
+        k_pcg_spmv_s_bulk<kSStages, kSCap, Epi, int16_t>
+            <<<sbulk_grid<Epi, int16_t>(c), kSBulkThreads, sbulk_smem_bytes<kSStages, kSCap, 2>(), s>>>(
+                c->bptr.p, c->bcol16.p, K, epi, c->nn, c->scal.p, c->partials.p);
+    else
+        k_pcg_spmv_s_bulk<kSStages, kSCap, Epi, uint32_t>
+            <<<sbulk_grid<Epi, uint32_t>(c), kSBulkThreads, sbulk_smem_bytes<kSStages, kSCap, 4>(), s>>>(
+                c->bptr.p, c->bcol.p, K, epi, c->nn, c->scal.p, c->partials.p);
+}
+
+// column deltas col - row of the pattern as 16-bit integers; *over = 1 when one does not fit
+__global__ void k_col16(const uint32_t *__restrict__ rp, const uint32_t *__restrict__ col, uint64_t n,
+                        int16_t *__restrict__ c16, int *over) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        for (uint32_t e = rp[i]; e < rp[i + 1]; ++e) {
+            const int64_t d = (int64_t)col[e] - (int64_t)i;
+            const bool fits = d >= -32768 && d <= 32767;
+            c16[e] = fits ? (int16_t)d : (int16_t)0;
+            if (!fits) *over = 1;
+        }
     }
 }
 
@@ -745,7 +797,6 @@ struct SAmg {
     int nc = 0;  // unknowns of the dense coarsest level
     DBuf<float> Cinv;
     DBuf<double> power;
-    int gres = 0, gpost = 0;  // grids of the level-0 bulk-copy passes
 };
 
 void samg_free(lmtg_ctx *c) {
@@ -1209,21 +1260,6 @@ static void samg_build(lmtg_ctx *c) {
         LMTG_CUDA(cudaGetLastError());
         c->launches += 1;
     }
-    // grids of the level-0 bulk-copy passes
-    {
-        constexpr size_t smem = sbulk_smem_bytes<kSStages, kSCap>();
-        int nb = 0;
-        LMTG_CUDA(cudaFuncSetAttribute(k_pcg_spmv_s_bulk<kSStages, kSCap, EpiSRes>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        LMTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_pcg_spmv_s_bulk<kSStages, kSCap, EpiSRes>,
-                                                                kSBulkThreads, smem));
-        M->gres = c->sm_count * (nb > 0 ? nb : 1);
-        LMTG_CUDA(cudaFuncSetAttribute(k_pcg_spmv_s_bulk<kSStages, kSCap, EpiSPost>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        LMTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_pcg_spmv_s_bulk<kSStages, kSCap, EpiSPost>,
-                                                                kSBulkThreads, smem));
-        M->gpost = c->sm_count * (nb > 0 ? nb : 1);
-    }
     // numeric part: Galerkin products, Jacobi inverses
     for (size_t l = 0; l + 1 < nl; ++l) {
         SLevel &F = *M->lv[l], &C = *M->lv[l + 1];
@@ -1377,10 +1413,8 @@ static void s_cycle0(lmtg_ctx *c, const float *r, float *z, cudaStream_t s, int 
     PcgScalars *S = c->scal.p;
     SLevel &L = *M.lv[0];
     const int g = grid_for(c, (L.n + 31) / 32 * 32, kRowThreads, 8);
-    constexpr size_t smem = sbulk_smem_bytes<kSStages, kSCap>();
     if (sbulk)
-        k_pcg_spmv_s_bulk<kSStages, kSCap, EpiSRes><<<M.gres, kSBulkThreads, smem, s>>>(
-            c->bptr.p, c->bcol.p, c->K32.p, EpiSRes{L.xa.p, r, L.res.p}, L.n, S, c->partials.p);
+        sbulk_launch(c, c->K32.p, EpiSRes{L.xa.p, r, L.res.p}, s);
     else
         launch_pdl(k_s_res, g, kRowThreads, 0, s, c->bptr.p, c->bcol.p, c->K32.p, L.xa.p, r, L.res.p, L.n, S,
                    nullptr, 0.f, nullptr);
@@ -1389,9 +1423,7 @@ static void s_cycle0(lmtg_ctx *c, const float *r, float *z, cudaStream_t s, int 
     s_correction(c, M, 0, s, S, e, e2);
     s_prolong(c, L, e, e2, s, S);
     if (sbulk)
-        k_pcg_spmv_s_bulk<kSStages, kSCap, EpiSPost><<<M.gpost, kSBulkThreads, smem, s>>>(
-            c->bptr.p, c->bcol.p, c->K32.p, EpiSPost{L.xa.p, r, c->Dinv32.p, z, L.omega, start, beta_den}, L.n, S,
-            c->partials.p);
+        sbulk_launch(c, c->K32.p, EpiSPost{L.xa.p, r, c->Dinv32.p, z, L.omega, start, beta_den}, s);
     else
         launch_pdl(k_s_post, g, kRowThreads, 0, s, c->bptr.p, c->bcol.p, c->K32.p, c->Dinv32.p, L.xa.p, r, z,
                    L.omega, L.n, S, true, start, beta_den, c->partials.p);
@@ -1455,19 +1487,20 @@ static int diff_pcg_t(lmtg_ctx *c, const T *K, const T *Dinv, const T *b, T *x, 
     // convergence test stops the chunk)
     const int kIters = amg ? 4 : 16;
     const int gr = rgrid(c, k_pcg_spmv_s<T>);
-    int gr_bulk = 0;
-    if (sbulk) {
-        constexpr size_t smem = sbulk_smem_bytes<kSStages, kSCap>();
-        LMTG_CUDA(cudaFuncSetAttribute(k_pcg_spmv_s_bulk<kSStages, kSCap, EpiSPq>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        int nb = 0;
-        LMTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_pcg_spmv_s_bulk<kSStages, kSCap, EpiSPq>,
-                                                                kSBulkThreads, smem));
-        gr_bulk = c->sm_count * (nb > 0 ? nb : 1);
+    if (sbulk) {  // the functions' attributes and grids, set before any capture
+        if (c->col16) {
+            sbulk_grid<EpiSPq, int16_t>(c);
+            sbulk_grid<EpiSRes, int16_t>(c);
+            sbulk_grid<EpiSPost, int16_t>(c);
+        } else {
+            sbulk_grid<EpiSPq, uint32_t>(c);
+            sbulk_grid<EpiSRes, uint32_t>(c);
+            sbulk_grid<EpiSPost, uint32_t>(c);
+        }
     }
     // the chunk graph of this precision, reused while it was captured on the same buffers
     DiffGraph &dg = c->diff_graph[std::is_same<T, float>::value ? 1 : 0];
-    const void *key[10] = {K, Dinv, b, x, r, z, p, q, reinterpret_cast<const void *>((uintptr_t)sbulk),
+    const void *key[10] = {K, Dinv, b, x, r, z, p, q, reinterpret_cast<const void *>((uintptr_t)sbulk + 2 * c->col16),
                            reinterpret_cast<const void *>((uintptr_t)amg)};
     bool cached = dg.exec != nullptr;
     for (int i = 0; i < 10 && cached; ++i) cached = dg.key[i] == key[i];
@@ -1486,9 +1519,7 @@ static int diff_pcg_t(lmtg_ctx *c, const T *K, const T *Dinv, const T *b, T *x, 
             k_pcg_dir_s<T><<<ngrid(c), kRowThreads, 0, s>>>(z, p, c->nn, c->scal.p);
             if constexpr (std::is_same<T, float>::value) {
                 if (sbulk)
-                    k_pcg_spmv_s_bulk<kSStages, kSCap, EpiSPq>
-                        <<<gr_bulk, kSBulkThreads, sbulk_smem_bytes<kSStages, kSCap>(), s>>>(
-                            c->bptr.p, c->bcol.p, K, EpiSPq{p, q}, c->nn, c->scal.p, c->partials.p);
+                    sbulk_launch(c, K, EpiSPq{p, q}, s);
                 else
                     k_pcg_spmv_s<T><<<gr, kRowThreads, 0, s>>>(c->bptr.p, c->bcol.p, K, p, q, c->nn, c->scal.p,
                                                                c->partials.p);
@@ -1795,6 +1826,19 @@ void diff_setup(lmtg_ctx *c, const double *k, uint64_t nk, double rho_c, double 
         for (auto &w : c->w64) w.alloc(c->nn);
         for (auto &w : c->w32) w.alloc(c->nn);
         LMTG_CUDA(cudaMemsetAsync(c->u.p, 0, c->u.bytes(), s));
+        // 16-bit column deltas for the bulk-copy products when the numbering is banded enough
+        c->bcol16.alloc(c->nnzb + 8);  // 16 bytes of slack: bulk copies round their end up
+        DBuf<int> over;
+        over.alloc(1);
+        LMTG_CUDA(cudaMemsetAsync(over.p, 0, sizeof(int), s));
+        k_col16<<<grid_for(c, c->nn, 256, 8), 256, 0, s>>>(c->bptr.p, c->bcol.p, c->nn, c->bcol16.p, over.p);
+        LMTG_CUDA(cudaGetLastError());
+        c->launches += 1;
+        int h_over = 1;
+        LMTG_CUDA(cudaMemcpyAsync(&h_over, over.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+        LMTG_CUDA(cudaStreamSynchronize(s));
+        c->col16 = h_over == 0;
+        if (!c->col16) c->bcol16.release();
         c->allocated = true;
     }
     c->E.alloc(nk);

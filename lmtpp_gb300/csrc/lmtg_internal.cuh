@@ -178,6 +178,8 @@ struct lmtg_ctx {
     double inner_reduction = 0.01;
     lmtg::DiffGraph diff_graph[2];  // the diffusion PCG's chunk graphs, [0] FP64, [1] FP32
     lmtg::SAmg *samg = nullptr;     // the diffusion FP32 PCG's multigrid (built on first use)
+    lmtg::DBuf<int16_t> bcol16;     // diffusion pattern's column deltas col - row, when col16
+    bool col16 = false;
     lmtg::DBuf<float> Ke32, K32, Dinv32;
     bool have64 = false, have32 = false, have_vec = false;
     double max_diag = 0;

@@ -213,3 +213,31 @@ def test_diffusion_multigrid_matches_oracle_and_cuts_iterations():
         its[prec] = st["iterations"]
         d.close()
     assert its["amg"] * 2 < its["jacobi"], its
+
+
+def test_diffusion_wide_numbering_uses_32bit_columns_and_matches():
+    """A node numbering whose column offsets exceed 16 bits (a random relabelling of 257^2
+    nodes) keeps the bulk-copy products on 32-bit column indices; the banded numbering uses 16-bit
+    deltas. Both reach the oracle's states (1e-8 relative) through the multigrid step solver."""
+    rng = np.random.default_rng(33)
+    P0 = O.diffusion_problem(129)
+    k = np.exp(0.3 * rng.standard_normal(P0["conn"].shape[0]))
+    P = O.diffusion_problem(129, k=k, theta=1.0)
+    n = P["pos"].shape[0]
+    states = O.diffusion_run(P, 3)
+    perm = rng.permutation(n)               # new id of old node i: perm[i]
+    inv = np.argsort(perm)
+    pos_p = P["pos"][inv]                   # node j of the relabelled mesh is old node inv[j]
+    conn_p = perm[P["conn"]].astype(np.uint32)
+    assert np.abs(conn_p.astype(np.int64)[:, :, None] - conn_p.astype(np.int64)[:, None, :]).max() > 32767
+    for pos, conn, back in ((P["pos"], P["conn"], None), (pos_p, conn_p, perm)):
+        d = Diffusion(pos, conn)
+        d.setup(k, rho_c=1.0, dt=1e-4, theta=1.0, dirichlet=boundary_nodes(pos), penalty=1e5)
+        d.set_solver("mixed")
+        d.set_state(P["T0"] if back is None else P["T0"][inv])
+        st = d.run(3, tol=1e-12)
+        T = d.get_state()
+        if back is not None:
+            T = T[back]
+        assert np.linalg.norm(T - states[-1]) <= 1e-8 * np.linalg.norm(states[-1]), st
+        d.close()
