@@ -525,7 +525,7 @@ __global__ void __launch_bounds__(kSBulkThreads, 4)
                 float v = 0.f;
                 if (I < R1) {
                     const uint32_t rs = sR[I - rbase], re = sR[I + 1 - rbase];
-#pragma unroll 4
+#pragma unroll 8
                     for (uint32_t qq = rs; qq < re; ++qq)
                         v += __fmul_rn(sK[qq - kbase], epi.x(col_at(sC[qq - cbase], I)));
                 }
