@@ -241,3 +241,35 @@ def test_diffusion_wide_numbering_uses_32bit_columns_and_matches():
             T = T[back]
         assert np.linalg.norm(T - states[-1]) <= 1e-8 * np.linalg.norm(states[-1]), st
         d.close()
+
+
+def test_multigrid_is_rebuilt_after_convection_changes_the_matrix():
+    """The mixed step solver with the multigrid (65^2 nodes, T = 0 on x = 0 only): three steps,
+    then skin convection on the x = 1 edges (A and B change, the multigrid is rebuilt at the next
+    solve), three more steps with the convection load; both stretches against the oracle."""
+    from lmtpp_gb300.diffusion import edges_on
+    P = O.diffusion_problem(33, theta=1.0)
+    pos = P["pos"]
+    left = np.nonzero(pos[:, 0] < 1e-9)[0].astype(np.uint32)
+    rowptr, col = P["rowptr"], P["col"]
+    A, B = O.assemble_diff(pos, P["conn"], 1.0, 1.0, 1e-4, 1.0, rowptr, col)
+    O.penalty(rowptr, col, A, None, left, np.ones(left.size), np.zeros(left.size), 1e5)
+    P.update(A=A, B=B)
+    first = O.diffusion_run(P, 3)
+    edges = edges_on(pos, P["conn"], 0, 1.0)
+    load = O.diffusion_convection(P, edges, 40.0, 0.7)  # adds to P["A"], P["B"]
+    second = O.diffusion_run(P, 3, T0=first[-1], load=load)
+    d = Diffusion(pos, P["conn"])
+    d.setup(1.0, rho_c=1.0, dt=1e-4, theta=1.0, dirichlet=left, penalty=1e5)
+    d.set_penalty_scale(d.get_penalty_scale())
+    d.set_solver("mixed")
+    d.set_state(P["T0"])
+    d.run(3, tol=1e-12)
+    T = d.get_state()
+    assert np.linalg.norm(T - first[-1]) <= 1e-8 * np.linalg.norm(first[-1])
+    d.set_convection(edges, 40.0, 0.7)
+    st = d.run(3, tol=1e-12)
+    T = d.get_state()
+    assert np.linalg.norm(T - second[-1]) <= 1e-8 * np.linalg.norm(second[-1]), st
+    assert np.linalg.norm(second[-1] - first[-1]) > 1e-3 * np.linalg.norm(first[-1])
+    d.close()
