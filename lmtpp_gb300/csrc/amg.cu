@@ -661,29 +661,33 @@ struct EpiPost {
     int start;
     double beta_den;
     static constexpr bool kReduce = true;
+    // four registers per row: lane c < 3 holds x_c and row c of D^-1; lane 8c + 3 holds r_c
+    // (its group's lanes hold the row sum's component c after the reduce-scatter).  Seven
+    // registers per row (r, x and D on lanes 0-2) ran 2.5% slower; nine lanes each holding one
+    // entry of D^-1 (two registers, more shuffles) 10% slower.
     struct Pre {
-        float r0, r1, r2, x, d0, d1, d2;
+        float a, b, c, d;
     };
     __device__ __forceinline__ Pre pre(uint64_t I, int lane, const float *__restrict__ x) const {
-        Pre p{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        Pre p{0.f, 0.f, 0.f, 0.f};
         if (lane < 3) {
             const float *Dr = D + 9 * I + 3 * lane;
-            p = {r[3 * I], r[3 * I + 1], r[3 * I + 2], x[4 * I + lane], Dr[0], Dr[1], Dr[2]};
+            p = {x[4 * I + lane], Dr[0], Dr[1], Dr[2]};
+        } else if ((lane & 7) == 3 && lane < 24) {
+            p.a = r[3 * I + (lane >> 3)];
         }
         return p;
     }
     __device__ __forceinline__ void row(uint64_t I, float qi, int lane, const float *, float &acc,
                                         const Pre &p) const {
-        const float v0 = __shfl_sync(0xffffffffu, qi, 0), v1 = __shfl_sync(0xffffffffu, qi, 8),
-                    v2 = __shfl_sync(0xffffffffu, qi, 16);
-        if (lane < 3) {
-            const float zc = p.x + omega * (p.d0 * (p.r0 - v0) + p.d1 * (p.r1 - v1) + p.d2 * (p.r2 - v2));
-            z[4 * I + lane] = zc;
-            const float rc = lane == 0 ? p.r0 : (lane == 1 ? p.r1 : p.r2);
-            acc = fmaf(rc, zc, acc);
-        } else if (lane == 3) {
-            z[4 * I + 3] = 0.f;  // the padding too: whole 16-byte nodes, no partially written sectors
-        }
+        const float w = p.a - qi;  // r_c - (K x)_c on lane 8c + 3
+        const float w0 = __shfl_sync(0xffffffffu, w, 3), w1 = __shfl_sync(0xffffffffu, w, 11),
+                    w2 = __shfl_sync(0xffffffffu, w, 19);
+        const float zc = p.a + omega * (p.b * w0 + p.c * w1 + p.d * w2);  // lanes 0-2
+        const float zr = __shfl_sync(0xffffffffu, zc, (lane >> 3) & 3);   // z_c on lane 8c + 3
+        if (lane < 3) z[4 * I + lane] = zc;
+        else if (lane == 3) z[4 * I + 3] = 0.f;  // the padding too: whole 16-byte nodes, no partially written sectors
+        if ((lane & 7) == 3 && lane < 24) acc = fmaf(p.a, zr, acc);
     }
     __device__ static unsigned *ticket(PcgScalars *S) { return &S->cnt_d; }
     __device__ void final(PcgScalars *S, double v) const {
