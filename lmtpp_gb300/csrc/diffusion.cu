@@ -12,7 +12,9 @@
 // reference's penalty (formulation.h:1028-1071) on A.
 //
 // One unknown per node: the node-block pattern of pattern.cu is the scalar CSR pattern; a row
-// holds ~9-19 entries, so the SpMV uses 8 lanes per row (4 rows per warp).
+// holds 9 or 19 entries (11.5 on average).  The FP64 products stream a warp's 32 rows at a time
+// (csr_stream32); the FP32 solver's products go through a bulk-copy (TMA) ring with a lane per
+// row, and its preconditioner is Jacobi or the scalar aggregation multigrid below.
 #include <algorithm>
 #include <type_traits>
 #include <chrono>
@@ -722,7 +724,7 @@ __global__ void k_dot_s(const double *__restrict__ a, const double *__restrict__
 //
 // Jacobi needs O(mesh side) iterations on A = M/dt + theta K (about 620 per implicit-Euler step
 // of the 1024^2 workload).  With lmtg_set_preconditioner(LMTG_PREC_AMG) (the default) and at least
-// kSMinUnknowns unknowns, z = M r is one W-cycle of an unsmoothed-aggregation multigrid built for
+// kSMinUnknowns unknowns, z = M r is one cycle of an unsmoothed-aggregation multigrid built for
 // the scalar matrix, the elasticity multigrid's scheme with one mode per aggregate:
 //   aggregation   the node graph's greedy aggregates (a root with its free neighbours, leftovers
 //                 joined to the aggregate they touch most, the rest grouped around a free node);
@@ -736,8 +738,9 @@ __global__ void k_dot_s(const double *__restrict__ a, const double *__restrict__
 //                 on the coarsest, else the next level's cycle: twice below level 0, the second
 //                 on the residual the first leaves, once deeper); x += Q e;
 //                 x' = x + omega D^-1 (r - A x)
-// The matrices are constant over the time steps, so the hierarchy is built once per diff_setup
-// (structure on the host, numeric part on the device) at the first FP32 solve.
+// The matrices are constant over the time steps, so the hierarchy is built once (structure on
+// the host, numeric part on the device) at the first FP32 solve after diff_setup or a change of
+// the convection terms.
 constexpr uint64_t kSMinUnknowns = 3000, kSCoarsest = 500;
 constexpr int kSMaxLevels = 10, kSGalCap = 64, kSPowerSteps = 12;
 constexpr size_t kSWLevels = 1;  // levels whose coarse correction visits the next level twice
