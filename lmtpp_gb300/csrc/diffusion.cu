@@ -1217,9 +1217,10 @@ static void samg_build(lmtg_ctx *c) {
             if (agg[i] != kSNone && Bc[agg[i]] > 0) q[i] = (float)(B[i] / Bc[agg[i]]);
         // coarse pattern: sorted distinct aggregates of each aggregate's nodes' columns
         std::vector<uint32_t> crp(na + 1, 0), ccol;
+        bool wide = false;  // a coarse row beyond the Galerkin kernel's kSGalCap slots
         {
             std::vector<uint32_t> mark(na, kSNone), row;
-            for (uint64_t a = 0; a < na; ++a) {
+            for (uint64_t a = 0; a < na && !wide; ++a) {
                 row.clear();
                 for (uint32_t u = aptr[a]; u < aptr[a + 1]; ++u) {
                     const uint32_t i = anode[u];
@@ -1232,10 +1233,14 @@ static void samg_build(lmtg_ctx *c) {
                     }
                 }
                 std::sort(row.begin(), row.end());
-                LMTG_CHECK(row.size() <= (size_t)kSGalCap, LMTG_ERR_UNSUPPORTED, "diffusion multigrid: coarse row too wide");
+                wide = row.size() > (size_t)kSGalCap;
                 ccol.insert(ccol.end(), row.begin(), row.end());
                 crp[a + 1] = (uint32_t)ccol.size();
             }
+        }
+        if (wide) {  // no coarser level: this one is the coarsest (dense if small enough, else Jacobi)
+            M->lv.push_back(std::move(L));
+            break;
         }
         L->nagg = na;
         s_upload(L->agg, agg, s);
