@@ -166,6 +166,10 @@ int lmtg_destroy(lmtg_ctx *c) {
     amg_free(c);
     samg_free(c);
     diff_graphs_free(c);
+    if (c->aux_stream) {
+        cudaStreamSynchronize(c->aux_stream);
+        cudaStreamDestroy(c->aux_stream);
+    }
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;  // DBuf destructors free device memory
     return LMTG_OK;

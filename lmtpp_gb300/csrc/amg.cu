@@ -1243,6 +1243,46 @@ static void amg_numeric(lmtg_ctx *c) {
     AmgState &A = *c->amg;
     cudaStream_t s = c->stream;
     const size_t nl = A.levels.size();
+    // smoother weights: omega = 1 / theta of a degree-1 Chebyshev on [h/30, h], h = 1.2 lmax.
+    // kPowerSteps power steps per level from a pseudo-random start, each normalising its input by
+    // the previous step's norm on the device: every level's steps are queued back to back and
+    // read once.  Level 0's steps need only its own matrix: they run on the auxiliary stream while
+    // the Galerkin products build the coarse levels (the products' bandwidth-bound passes overlap
+    // the Galerkin kernels' latency-bound ones); the coarser levels' steps follow the join.
+    PcgScalars *o = c->scal.p + 1;
+    auto power_steps = [&](size_t l, cudaStream_t st) {
+        AmgLevel &L = *A.levels[l];
+        const int VS = L.b == 3 ? 4 : 8;
+        const uint64_t nv = (uint64_t)VS * L.nn;
+        const uint32_t *bp = l == 0 ? c->bptr.p : L.bptr.p, *bc = l == 0 ? c->bcol.p : L.bcol.p;
+        const float *K = l == 0 ? c->K32.p : L.K.p, *D = l == 0 ? c->Dinv32.p : L.Dinv.p;
+        k_amg_scale<<<grid_for(c, nv, 256), 256, 0, st>>>(L.xa.p, nullptr, 1.f, nv);  // random start
+        c->launches += 1;
+        const bool bulk = l == 0 && spmv_kind_in_use(c) != 0;
+        if (bulk) bulk0_setup(c);
+        for (int it = 0; it < kPowerSteps; ++it) {
+            float *v = (it & 1) ? L.xb.p : L.xa.p, *w = (it & 1) ? L.xa.p : L.xb.p;
+            double *out2 = A.power.p + 2 * (kPowerSteps * l + it);
+            const double *prev = it ? out2 - 2 : nullptr;
+            const int g = grid_for(c, L.nn * 32, kRowThreads, 8);
+            if (bulk)
+                bulk0_launch(c, v, EpiPower{D, w, prev, out2}, st, o);
+            else if (L.b == 3)
+                k_amg_power<3><<<g, kRowThreads, 0, st>>>(bp, bc, K, D, v, w, L.nn, c->partials.p, &o->cnt_c, prev, out2);
+            else
+                k_amg_power<6><<<g, kRowThreads, 0, st>>>(bp, bc, K, D, v, w, L.nn, c->partials.p, &o->cnt_c, prev, out2);
+            LMTG_CUDA(cudaGetLastError());
+            c->launches += 1;
+        }
+    };
+    if (!c->aux_stream) LMTG_CUDA(cudaStreamCreateWithFlags(&c->aux_stream, cudaStreamNonBlocking));
+    cudaEvent_t fork, join;
+    LMTG_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+    LMTG_CUDA(cudaEventCreateWithFlags(&join, cudaEventDisableTiming));
+    LMTG_CUDA(cudaEventRecord(fork, s));
+    LMTG_CUDA(cudaStreamWaitEvent(c->aux_stream, fork, 0));
+    power_steps(0, c->aux_stream);
+    LMTG_CUDA(cudaEventRecord(join, c->aux_stream));
     for (size_t l = 0; l + 1 < nl; ++l) {
         AmgLevel &F = *A.levels[l], &C = *A.levels[l + 1];
         const uint32_t *fbptr = l == 0 ? c->bptr.p : F.bptr.p;
@@ -1261,36 +1301,11 @@ static void amg_numeric(lmtg_ctx *c) {
         LMTG_CUDA(cudaGetLastError());
         c->launches += 2;
     }
-    // smoother weights: omega = 1 / theta of a degree-1 Chebyshev on [h/30, h], h = 1.2 lmax.
-    // kPowerSteps power steps per level from a pseudo-random start, each normalising its input by
-    // the previous step's norm on the device: every level's steps are queued back to back and
-    // read once.
-    PcgScalars *o = c->scal.p + 1;
-    for (size_t l = 0; l + 1 < nl; ++l) {
-        AmgLevel &L = *A.levels[l];
-        const int VS = L.b == 3 ? 4 : 8;
-        const uint64_t nv = (uint64_t)VS * L.nn;
-        const uint32_t *bp = l == 0 ? c->bptr.p : L.bptr.p, *bc = l == 0 ? c->bcol.p : L.bcol.p;
-        const float *K = l == 0 ? c->K32.p : L.K.p, *D = l == 0 ? c->Dinv32.p : L.Dinv.p;
-        k_amg_scale<<<grid_for(c, nv, 256), 256, 0, s>>>(L.xa.p, nullptr, 1.f, nv);  // random start
-        c->launches += 1;
-        const bool bulk = l == 0 && spmv_kind_in_use(c) != 0;
-        if (bulk) bulk0_setup(c);
-        for (int it = 0; it < kPowerSteps; ++it) {
-            float *v = (it & 1) ? L.xb.p : L.xa.p, *w = (it & 1) ? L.xa.p : L.xb.p;
-            double *out2 = A.power.p + 2 * (kPowerSteps * l + it);
-            const double *prev = it ? out2 - 2 : nullptr;
-            const int g = grid_for(c, L.nn * 32, kRowThreads, 8);
-            if (bulk)
-                bulk0_launch(c, v, EpiPower{D, w, prev, out2}, s, o);
-            else if (L.b == 3)
-                k_amg_power<3><<<g, kRowThreads, 0, s>>>(bp, bc, K, D, v, w, L.nn, c->partials.p, &o->cnt_c, prev, out2);
-            else
-                k_amg_power<6><<<g, kRowThreads, 0, s>>>(bp, bc, K, D, v, w, L.nn, c->partials.p, &o->cnt_c, prev, out2);
-            LMTG_CUDA(cudaGetLastError());
-            c->launches += 1;
-        }
-    }
+    // the coarser levels' steps use the same partials and scalars as level 0's: after the join
+    LMTG_CUDA(cudaStreamWaitEvent(s, join, 0));
+    cudaEventDestroy(fork);
+    cudaEventDestroy(join);
+    for (size_t l = 1; l + 1 < nl; ++l) power_steps(l, s);
     {
         std::vector<double> h(2 * kPowerSteps * (nl - 1));
         LMTG_CUDA(cudaMemcpyAsync(h.data(), A.power.p, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, s));

@@ -123,6 +123,7 @@ struct DiffGraph {
 struct lmtg_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t aux_stream = nullptr;  // work that overlaps the main stream (created on first use)
     std::string err;
     int sm_count = 0;
 
