@@ -1276,6 +1276,12 @@ static void amg_numeric(lmtg_ctx *c) {
         }
     };
     if (!c->aux_stream) LMTG_CUDA(cudaStreamCreateWithFlags(&c->aux_stream, cudaStreamNonBlocking));
+    // on an error between the fork and the join, nothing may leave with level 0's steps still
+    // writing into the hierarchy's buffers
+    struct AuxDrain {
+        cudaStream_t st;
+        ~AuxDrain() { cudaStreamSynchronize(st); }
+    } drain{c->aux_stream};
     cudaEvent_t fork, join;
     LMTG_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
     LMTG_CUDA(cudaEventCreateWithFlags(&join, cudaEventDisableTiming));
