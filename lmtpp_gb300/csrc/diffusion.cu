@@ -1015,6 +1015,28 @@ __global__ void k_s_prolong(const uint32_t *__restrict__ agg, const float *__res
     for (uint64_t i = 4 * n4 + i0; i < n; i += step) x[i] += s_corr(agg[i], q[i], e, e2);
 }
 
+// The post-smoothing of a level >= 1 with its prolongation fused in: out = x~ + omega D^-1
+// (r - A x~), where x~ = x + q (e + e2)[agg] is formed on the fly wherever it is read (the same
+// float operations as k_s_prolong, which this replaces there; x itself is not written).  One
+// launch fewer per visit of a latency-bound level.
+__global__ void __launch_bounds__(kRowThreads)
+    k_s_post_pro(const uint32_t *__restrict__ rp, const uint32_t *__restrict__ col, const float *__restrict__ A,
+                 const float *__restrict__ Dinv, const float *__restrict__ x, const uint32_t *__restrict__ agg,
+                 const float *__restrict__ q, const float *__restrict__ e, const float *__restrict__ e2,
+                 const float *__restrict__ r, float *__restrict__ xo, float omega, uint64_t n, const PcgScalars *S) {
+    pdl_wait_trigger();
+    if (s_done(S)) return;
+    __shared__ float tiles[kRowWarps][kTile];
+    const int wp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    auto xt = [&](uint32_t j) { return __ldg(x + j) + s_corr(__ldg(agg + j), __ldg(q + j), e, e2); };
+    const ChunkRange cr = cta_chunks(n);
+    for (uint64_t ch = cr.first + wp; ch < cr.end; ch += kRowWarps) {
+        const float y = csr_stream32(rp, col, A, ch * 32, n, tiles[wp], xt);
+        const uint64_t I = ch * 32 + lane;
+        if (I < n) xo[I] = xt((uint32_t)I) + omega * Dinv[I] * (r[I] - y);
+    }
+}
+
 // e = Cinv r on the coarsest level (warp per row)
 __global__ void k_s_dense(const float *__restrict__ Cinv, const float *__restrict__ r, float *__restrict__ e, int n,
                           const PcgScalars *S) {
@@ -1427,10 +1449,9 @@ static void s_cycle(lmtg_ctx *c, SAmg &M, size_t l, const float *rhs, float *out
     s_restrict(c, M, l, s, S);
     float *e, *e2;
     s_correction(c, M, l, s, S, e, e2);
-    s_prolong(c, L, e, e2, s, S);
-    launch_pdl(k_s_post, g, kRowThreads, 0, s, L.rp.p, L.col.p, L.A.p, L.Dinv.p, L.xa.p, rhs, out, L.omega, L.n, S,
-               false, 0, 0.0, c->partials.p);
-    c->launches += 4;
+    launch_pdl(k_s_post_pro, g, kRowThreads, 0, s, L.rp.p, L.col.p, L.A.p, L.Dinv.p, L.xa.p, L.agg.p, L.q.p, e, e2,
+               rhs, out, L.omega, L.n, S);
+    c->launches += 3;
 }
 
 // the cycle after the update kernel (level 0): r -> z, rz and beta; the residual and the
